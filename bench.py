@@ -1,0 +1,344 @@
+"""Benchmark of the materialised neighbour-list path on one GB300.
+
+Workload: 1,000,000 atoms uniform at density 0.05 A^-3 in a cubic periodic
+box, cutoff 5 A, Float64 positions, Int32 indices (seeded synthetic input with
+the shape of the reference's benchmark, scripts/benchmark.jl).  One step is
+build_cell_list + materialize_pairlist with R: binning, sort, count, scan and
+fill, all on the device, inputs resident in HBM.  L2 is flushed (256 MiB
+write, untimed) before every timed step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line (rank 0).  --impl reference times the reference's
+sort-based CPU path (the C restatement in oracle/, since Julia is not
+available) on the host cores for the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+N_ATOMS = 1_000_000
+DENSITY = 0.05
+CUTOFF = 5.0
+SEED = 0
+METRIC = "pairs/s (1M atoms, rc 5 A, density 0.05, full pbc, Float64, build_cell_list + materialize_pairlist)"
+WORKLOAD = "uniform 1,000,000 atoms, density 0.05 A^-3, cubic pbc box (L=271.44 A), cutoff 5 A, Float64, Int32 indices"
+ALGO_BYTES_PER_ATOM = 24  # positions read
+ALGO_BYTES_PER_PAIR = 44  # i 4 + j 4 + S 12 + R 24 written
+
+
+def workload():
+    import configs as cf
+
+    X, C, L = cf.uniform_system(N_ATOMS, DENSITY, SEED)
+    return X, C, (True, True, True)
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes of the fill kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "fill_kernel_1M_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = float(parts[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(X, C, pbc, seconds_target=12.0, max_runs=3):
+    """Oracle (C restatement of the reference's sort-based CPU path) on all
+    host cores, on the full workload, a bounded number of runs."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+
+    threads = os.cpu_count() or 1
+    runs, t0 = 0, time.perf_counter()
+    pairs = 0
+    while runs < max_runs:
+        pairs = orc.timed_neighbour_list(X, CUTOFF, C, pbc, threads, with_R=True)
+        runs += 1
+        if time.perf_counter() - t0 > seconds_target:
+            break
+    dt = (time.perf_counter() - t0) / runs
+    return {"value": pairs / dt, "unit": "pairs/s", "cores": threads, "kind": "port",
+            "sample": f"{runs} full run(s) of the 1M-atom workload (build + count + fill + R), {dt:.3f} s each"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    X, C, pbc = workload()
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+
+    orc.build()
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        orc.timed_neighbour_list(X, CUTOFF, C, pbc, threads, with_R=True)
+    t0 = time.perf_counter()
+    pairs = 0
+    for _ in range(args.steps):
+        pairs = orc.timed_neighbour_list(X, CUTOFF, C, pbc, threads, with_R=True)
+    dt = (time.perf_counter() - t0) / args.steps
+    val = pairs / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": "pairs/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "atoms": N_ATOMS, "pairs": int(pairs)},
+        "cpu_baseline": {"value": val, "unit": "pairs/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} timed full runs of the workload after {args.warmup} warm-up runs"},
+        "e2e": {"value": val, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "Julia is not installed on either machine; the reference arm is the C restatement of the "
+                "reference's sort-based CPU path (oracle/nl_oracle.c) on all host threads",
+    }
+    print(json.dumps(line))
+
+
+def run_gpu(args):
+    import torch
+
+    import __graft_entry__ as graft
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(local)
+    dev = torch.device("cuda", local if world > 1 else 0)
+    torch.cuda.set_device(dev)
+    nl = graft.load_package()
+    X, C, pbc = workload()
+    Xd = torch.from_numpy(X).to(dev)
+    eng = nl.NeighbourListEngine(N_ATOMS, C, CUTOFF, pbc, device=dev)
+    total = eng.run(Xd)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        eng.launch(Xd)
+    torch.cuda.synchronize(dev)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    with ClockSampler(dev.index or 0) as clk:
+        barrier()
+        torch.cuda.synchronize(dev)
+        for k in range(args.steps):
+            flush.fill_(k & 0xFF)  # untimed L2 flush (256 MiB > 129 MB L2)
+            starts[k].record(stream)
+            eng.launch(Xd)
+            ends[k].record(stream)
+        torch.cuda.synchronize(dev)
+        barrier()
+    eng.sync_status()
+    step_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends)) / args.steps
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([step_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        step_ms = float(t.item())
+    assert eng.total_pairs() == total
+    rechecks = eng.rechecks()
+
+    # ---- fill kernel alone (same stream, records from the last step)
+    import ctypes as Cc
+
+    from neighbourlists_gb300 import _lib
+    from neighbourlists_gb300.api import _ptr, _stream_handle
+
+    L = _lib.lib()
+    p = eng.plan
+    D, I64, U8 = Cc.POINTER(Cc.c_double), Cc.POINTER(Cc.c_int64), Cc.POINTER(Cc.c_uint8)
+
+    def fill():
+        _lib.check(L.nl_fill_pairs(_ptr(eng.Xs), _ptr(eng.perm), Cc.c_void_p(eng.offs.data_ptr()), N_ATOMS,
+                                   p.cell_cm.ctypes.data_as(D), p.inv_cm.ctypes.data_as(D),
+                                   p.ncells.ctypes.data_as(I64), p.nxyz.ctypes.data_as(I64),
+                                   eng.pbc.ctypes.data_as(U8), CUTOFF, eng.ib, Cc.c_void_p(eng.first.data_ptr()),
+                                   eng.capacity, _ptr(eng.i), _ptr(eng.j), _ptr(eng.S), _ptr(eng.R), _ptr(eng.ws),
+                                   eng.ws.numel(), _stream_handle(stream)))
+
+    fill()
+    fs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    fe = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    for k in range(args.steps):
+        flush.fill_(k & 0xFF)
+        fs[k].record(stream)
+        fill()
+        fe[k].record(stream)
+    torch.cuda.synchronize(dev)
+    eng.sync_status()
+    fill_ms = sum(s.elapsed_time(e) for s, e in zip(fs, fe)) / args.steps
+
+    # ---- end to end through the public API with host buffers
+    ti = eng.ti
+    hX = torch.from_numpy(X).pin_memory()
+    h_i = torch.empty(total, dtype=ti).pin_memory()
+    h_j = torch.empty(total, dtype=ti).pin_memory()
+    h_S = torch.empty((total, 3), dtype=ti).pin_memory()
+    h_R = torch.empty((total, 3), dtype=torch.float64).pin_memory()
+    h_f = torch.empty(N_ATOMS + 1, dtype=ti).pin_memory()
+    Xdev = torch.empty_like(Xd)
+
+    def e2e_step():
+        Xdev.copy_(hX, non_blocking=True)
+        eng.launch(Xdev)
+        h_f.copy_(eng.first, non_blocking=True)
+        h_i.copy_(eng.i[:total], non_blocking=True)
+        h_j.copy_(eng.j[:total], non_blocking=True)
+        h_S.copy_(eng.S[:total], non_blocking=True)
+        h_R.copy_(eng.R[:total], non_blocking=True)
+
+    e2e_step()
+    torch.cuda.synchronize(dev)
+    e2e_steps = max(2, min(args.steps, 5))
+    es, ee = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    es.record(stream)
+    for _ in range(e2e_steps):
+        e2e_step()
+    ee.record(stream)
+    torch.cuda.synchronize(dev)
+    e2e_ms = es.elapsed_time(ee) / e2e_steps
+    eng.sync_status()
+    assert int(h_f[-1]) - 1 == total
+    h2d = X.nbytes
+    d2h = (h_i.numel() * h_i.element_size() + h_j.numel() * h_j.element_size() + h_S.numel() * h_S.element_size()
+           + h_R.numel() * 8 + h_f.numel() * h_f.element_size())
+
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peaks()
+    algo_bytes = ALGO_BYTES_PER_ATOM * N_ATOMS + ALGO_BYTES_PER_PAIR * total
+    achieved = algo_bytes / (fill_ms * 1e-3) / 1e9
+    traffic = ncu_traffic()
+    cpu = cpu_baseline(X, C, pbc) if not args.no_cpu_baseline else None
+    value = world * total / (step_ms * 1e-3)
+    line = {
+        "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "atoms": N_ATOMS, "pairs": int(total), "cutoff": CUTOFF,
+                   "density": DENSITY, "pbc": "TTT", "index_type": "Int32", "with_R": True,
+                   "l2": "flushed before every timed step (256 MiB write, untimed)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "kernel": "k_pairs<fill>",
+                     "algorithmic_bytes": algo_bytes, "kernel_ms": fill_ms,
+                     "traffic": (traffic or {}).get("dram_bytes_per_launch")},
+        "step_roofline_frac": algo_bytes / (step_ms * 1e-3) / 1e9 / peak,
+        "cpu_baseline": cpu,
+        "e2e": {"value": world * total / (e2e_ms * 1e-3), "unit": "pairs/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+        "clocks": clk.summary(),
+        "gpu_launches": 8 * args.steps,
+        "rechecks": rechecks,
+        "recheck_band_rel": float(p.band / (CUTOFF * CUTOFF)),
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,141 @@
+/*
+ * nlgpu.h -- C ABI of the GB300 (sm_103a) neighbour-list engine.
+ *
+ * Drop-in boundary for the sort-based path of NeighbourLists.jl v0.6.2:
+ *   neighbour_list(X, cutoff, cell, pbc; lazy)  (src/cell_list.jl:897-916)
+ *   -> build_cell_list                          (src/cell_list.jl:632-679)
+ *   -> materialize_pairlist / for_each_neighbour (src/gpu_kernels.jl:299-364,
+ *                                                 src/cell_list.jl:779-833)
+ *
+ * Conventions (identical to the reference's data layout):
+ *   - positions: nat x 3 doubles, atom-major (Vector{SVector{3,Float64}});
+ *   - cell / inv_cell: 9 doubles, column-major (SMatrix{3,3} memory order),
+ *     ROWS of the cell are the lattice vectors;
+ *   - every index array is 1-based in the caller's index type TI, selected by
+ *     index_bytes = 4 (Int32) or 8 (Int64); S is nat_pairs x 3 TI (SVector{3,TI});
+ *   - device pointers ("d_" prefix) are CUDA device memory; "stream" is a
+ *     cudaStream_t passed as void* (NULL = legacy default stream);
+ *   - every function returns an NL_* status; nl_last_error() gives details
+ *     for the calling thread.
+ *
+ * Ownership: the caller owns every input/output buffer and the workspace
+ * (sized by nl_workspace_bytes).  The library allocates no device memory.
+ */
+#ifndef NLGPU_H
+#define NLGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+#define NL_OK 0
+#define NL_ERR_ARG 1              /* invalid argument */
+#define NL_ERR_TOO_MANY_CELLS 2   /* cell_list.jl:655-659 "Ratio of simulation cell size to cutoff is very large" */
+#define NL_ERR_NOMEM 3            /* workspace or host allocation too small */
+#define NL_ERR_CUDA 4             /* CUDA runtime error */
+#define NL_ERR_TIMEOUT 5          /* a bounded device-side wait gave up */
+#define NL_ERR_BAD_POSITION 6     /* non-finite position or |frac*ncells| >= 2^30 */
+#define NL_ERR_CAPACITY 7         /* pair buffers smaller than the pair count */
+#define NL_ERR_INDEX_OVERFLOW 8   /* pair count does not fit the index type */
+#define NL_ERR_INCONSISTENT 9     /* a cell list whose cell ids do not match its positions */
+
+/* lazy reductions (nl_lazy_reduce) */
+#define NL_REDUCE_COUNT 0         /* int32 per atom: count_neighbours (cell_list.jl:808-814) */
+#define NL_REDUCE_INV_R6 1        /* double per atom: sum over neighbours of 1/r^6 */
+
+/* Cell analysis: the reference's analyze_cell (cell_list.jl:152-170) plus the
+ * stencil half-width nxyz of materialize_pairlist (gpu_kernels.jl:315-316),
+ * and the FP32 screen band of this engine. */
+typedef struct nl_cell_plan {
+  double inv_cell[9];   /* inv(cell), column-major (StaticArrays operation order) */
+  double lens[3];       /* abs.(lengths(cell)) */
+  int64_t ncells[3];    /* max(floor(lens/cutoff), 1) */
+  int64_t nxyz[3];      /* ceil(cutoff * ncells / lens) */
+  int64_t ncells_total; /* prod(ncells) */
+  double band;          /* half-width of the FP64 recheck band on r^2 (A^2) */
+} nl_cell_plan;
+
+/* Replaces analyze_cell (cell_list.jl:152-170) + nxyz (gpu_kernels.jl:315-316). */
+int nl_analyze_cell(const double cell[9], double cutoff, int index_bytes, nl_cell_plan* plan);
+
+/* Device workspace needed by every call below for a system of nat atoms and
+ * ncells_total cells. */
+size_t nl_workspace_bytes(int64_t nat, int64_t ncells_total);
+
+/* Replaces build_cell_list / _build_sorted_celllist (cell_list.jl:632-679),
+ * i.e. _compute_cell_ids (gpu_kernels.jl:244-255,378-382), _get_sortperm
+ * (cell_list.jl:711-718) and _compute_cell_offsets (gpu_kernels.jl:262-285,
+ * 386-390).  Fills the SortedCellList arrays:
+ *   d_perm[nat], d_X_sorted[nat*3], d_cell_id[nat], d_cell_offsets[ncells_total+1].
+ * inv_cell / ncells are the caller's analyze_cell results.  Asynchronous. */
+int nl_build_cell_list(const double* d_X, int64_t nat, const double cell[9], const double inv_cell[9],
+                       const int64_t ncells[3], const uint8_t pbc[3], double cutoff, int index_bytes,
+                       void* d_perm, double* d_X_sorted, void* d_cell_id, void* d_cell_offsets,
+                       void* d_workspace, size_t workspace_bytes, void* stream);
+
+/* Replaces count_neighbours_kernel! + compute_pair_offsets + _scalar_getindex
+ * (gpu_kernels.jl:132-152, 222-237, 320-333).  From a SortedCellList (any
+ * producer) writes d_first[nat+1] (1-based CSR offsets per atom).  If
+ * total_pairs is non-NULL the call synchronises the stream and stores the pair
+ * count there (and reports any device-side error).  reuse_records = 1 skips the
+ * per-atom record rebuild when the same workspace was just used by
+ * nl_build_cell_list for this very cell list. */
+int nl_count_pairs(const double* d_X_sorted, const void* d_perm, const void* d_cell_id, const void* d_cell_offsets,
+                   int64_t nat, const double cell[9], const double inv_cell[9], const int64_t ncells[3],
+                   const int64_t nxyz[3], const uint8_t pbc[3], double cutoff, int index_bytes, int reuse_records,
+                   void* d_first, int64_t* total_pairs, void* d_workspace, size_t workspace_bytes, void* stream);
+
+/* Replaces fill_pairs_kernel! (gpu_kernels.jl:159-180) and adds the pair
+ * vectors R = X[j] - X[i] + cell' * S (_getR, cell_list.jl:525-531).
+ * Requires the records of a preceding nl_count_pairs / nl_neighbour_list in
+ * the same workspace.  Writes d_i, d_j [capacity], d_S [capacity*3] and, if
+ * d_R is not NULL, d_R [capacity*3].  Asynchronous. */
+int nl_fill_pairs(const double* d_X_sorted, const void* d_perm, const void* d_cell_offsets, int64_t nat,
+                  const double cell[9], const double inv_cell[9], const int64_t ncells[3], const int64_t nxyz[3],
+                  const uint8_t pbc[3], double cutoff, int index_bytes, const void* d_first, int64_t capacity,
+                  void* d_i, void* d_j, void* d_S, double* d_R, void* d_workspace, size_t workspace_bytes,
+                  void* stream);
+
+/* Whole materialised path, neighbour_list(X, cutoff, cell, pbc) with
+ * lazy = false (cell_list.jl:897-916): build + count + scan + fill in one
+ * stream-ordered sequence with no host synchronisation in between.  Pairs
+ * are written only if they fit in capacity.  If total_pairs is non-NULL the
+ * call synchronises, stores the pair count and returns NL_ERR_CAPACITY when
+ * it exceeds capacity (the cell list, first and the records stay valid:
+ * re-run nl_fill_pairs with larger buffers). */
+int nl_neighbour_list(const double* d_X, int64_t nat, const double cell[9], const double inv_cell[9],
+                      const int64_t ncells[3], const int64_t nxyz[3], const uint8_t pbc[3], double cutoff,
+                      int index_bytes, void* d_perm, double* d_X_sorted, void* d_cell_id, void* d_cell_offsets,
+                      void* d_first, int64_t capacity, void* d_i, void* d_j, void* d_S, double* d_R,
+                      int64_t* total_pairs, void* d_workspace, size_t workspace_bytes, void* stream);
+
+/* Lazy mode (for_each_neighbour over every atom, cell_list.jl:779-814) with a
+ * built-in per-atom reduction: NL_REDUCE_COUNT -> int32 d_out[nat];
+ * NL_REDUCE_INV_R6 -> double d_out[nat] = sum_j 1/((r2*r2)*r2), r2 = dot(R,R),
+ * accumulated in the reference's traversal order.  Asynchronous. */
+int nl_lazy_reduce(const double* d_X_sorted, const void* d_perm, const void* d_cell_id, const void* d_cell_offsets,
+                   int64_t nat, const double cell[9], const double inv_cell[9], const int64_t ncells[3],
+                   const int64_t nxyz[3], const uint8_t pbc[3], double cutoff, int index_bytes, int reuse_records,
+                   int op, void* d_out, void* d_workspace, size_t workspace_bytes, void* stream);
+
+/* Synchronises the stream, then reports (and clears) any device-side error
+ * recorded in the workspace by earlier asynchronous calls. */
+int nl_sync_status(void* d_workspace, void* stream);
+
+/* Statistics of the last count pass in this workspace: number of candidate
+ * pairs decided in FP64 (the FP32 screen's recheck band plus exact atoms).
+ * Synchronises the stream. */
+int nl_last_recheck_count(void* d_workspace, void* stream, int64_t* rechecks);
+
+const char* nl_status_string(int status);
+const char* nl_last_error(void);
+int nl_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NLGPU_H */

@@ -1,0 +1,122 @@
+"""ctypes binding of libnlgpu.so (the C ABI declared in include/nlgpu.h).
+
+The library is built in-tree by build.py.  Loading fails loudly if it is
+missing: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libnlgpu.so")
+
+NL_OK = 0
+NL_ERR_ARG = 1
+NL_ERR_TOO_MANY_CELLS = 2
+NL_ERR_NOMEM = 3
+NL_ERR_CUDA = 4
+NL_ERR_TIMEOUT = 5
+NL_ERR_BAD_POSITION = 6
+NL_ERR_CAPACITY = 7
+NL_ERR_INDEX_OVERFLOW = 8
+NL_ERR_INCONSISTENT = 9
+
+NL_REDUCE_COUNT = 0
+NL_REDUCE_INV_R6 = 1
+
+# every symbol include/nlgpu.h declares
+EXPORTED = [
+    "nl_analyze_cell",
+    "nl_workspace_bytes",
+    "nl_build_cell_list",
+    "nl_count_pairs",
+    "nl_fill_pairs",
+    "nl_neighbour_list",
+    "nl_lazy_reduce",
+    "nl_sync_status",
+    "nl_last_recheck_count",
+    "nl_status_string",
+    "nl_last_error",
+    "nl_version",
+]
+
+
+class CellPlan(C.Structure):
+    _fields_ = [
+        ("inv_cell", C.c_double * 9),
+        ("lens", C.c_double * 3),
+        ("ncells", C.c_int64 * 3),
+        ("nxyz", C.c_int64 * 3),
+        ("ncells_total", C.c_int64),
+        ("band", C.c_double),
+    ]
+
+
+class NLError(RuntimeError):
+    """Raised for any non-zero status of the C ABI."""
+
+    def __init__(self, status: int, msg: str):
+        super().__init__(msg)
+        self.status = status
+
+
+_lib = None
+
+_vp = C.c_void_p
+_D = C.POINTER(C.c_double)
+_I64 = C.POINTER(C.c_int64)
+_U8 = C.POINTER(C.c_uint8)
+
+
+def _declare(L):
+    L.nl_analyze_cell.argtypes = [_D, C.c_double, C.c_int, C.POINTER(CellPlan)]
+    L.nl_analyze_cell.restype = C.c_int
+    L.nl_workspace_bytes.argtypes = [C.c_int64, C.c_int64]
+    L.nl_workspace_bytes.restype = C.c_size_t
+    L.nl_build_cell_list.argtypes = [_vp, C.c_int64, _D, _D, _I64, _U8, C.c_double, C.c_int, _vp, _vp, _vp, _vp, _vp,
+                                     C.c_size_t, _vp]
+    L.nl_build_cell_list.restype = C.c_int
+    L.nl_count_pairs.argtypes = [_vp, _vp, _vp, _vp, C.c_int64, _D, _D, _I64, _I64, _U8, C.c_double, C.c_int, C.c_int,
+                                 _vp, _I64, _vp, C.c_size_t, _vp]
+    L.nl_count_pairs.restype = C.c_int
+    L.nl_fill_pairs.argtypes = [_vp, _vp, _vp, C.c_int64, _D, _D, _I64, _I64, _U8, C.c_double, C.c_int, _vp, C.c_int64,
+                                _vp, _vp, _vp, _vp, _vp, C.c_size_t, _vp]
+    L.nl_fill_pairs.restype = C.c_int
+    L.nl_neighbour_list.argtypes = [_vp, C.c_int64, _D, _D, _I64, _I64, _U8, C.c_double, C.c_int, _vp, _vp, _vp, _vp, _vp,
+                                    C.c_int64, _vp, _vp, _vp, _vp, _I64, _vp, C.c_size_t, _vp]
+    L.nl_neighbour_list.restype = C.c_int
+    L.nl_lazy_reduce.argtypes = [_vp, _vp, _vp, _vp, C.c_int64, _D, _D, _I64, _I64, _U8, C.c_double, C.c_int, C.c_int,
+                                 C.c_int, _vp, _vp, C.c_size_t, _vp]
+    L.nl_lazy_reduce.restype = C.c_int
+    L.nl_sync_status.argtypes = [_vp, _vp]
+    L.nl_sync_status.restype = C.c_int
+    L.nl_last_recheck_count.argtypes = [_vp, _vp, _I64]
+    L.nl_last_recheck_count.restype = C.c_int
+    L.nl_status_string.argtypes = [C.c_int]
+    L.nl_status_string.restype = C.c_char_p
+    L.nl_last_error.argtypes = []
+    L.nl_last_error.restype = C.c_char_p
+    L.nl_version.argtypes = []
+    L.nl_version.restype = C.c_int
+
+
+def lib():
+    """Loads libnlgpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(
+                f"{LIB_PATH} is missing: build it with `python neighbourlists.jl_gb300/build.py` "
+                "(the GPU neighbour list has no CPU fallback)")
+        L = C.CDLL(LIB_PATH)
+        _declare(L)
+        _lib = L
+    return _lib
+
+
+def check(status: int) -> None:
+    if status != NL_OK:
+        L = lib()
+        detail = L.nl_last_error().decode(errors="replace")
+        raise NLError(status, f"{L.nl_status_string(status).decode()}: {detail}")

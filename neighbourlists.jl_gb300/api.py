@@ -1,0 +1,365 @@
+"""Host-side mirror of the NeighbourLists.jl API for the GPU path.
+
+Same names, argument meaning and error behaviour as the reference's unified
+API (src/cell_list.jl:839-927) and data types (src/types.jl:34-82):
+
+    neighbour_list(X, cutoff, cell, pbc; lazy, int_type) -> PairList | SortedCellList
+    build_cell_list(X, cutoff, cell, pbc; int_type)       -> SortedCellList
+    materialize_pairlist(clist)                           -> PairList
+    npairs, nsites, nneigs, maxneigs/max_neighbours, neigs, neigss, neighbours,
+    num_neighbours, count_neighbours, for_each_neighbour
+
+Differences a caller sees:
+  * arrays live on the GPU as torch tensors (the reference's CuArrays);
+  * indices (i, j, perm, cell_id, cell_offsets, first) are 1-based, as in the
+    reference, in int32 (Int32, default) or int64 (Int64);
+  * PairList additionally carries R (npairs x 3 float64), bit-equal to the
+    reference's _getR (cell_list.jl:525-531).
+
+``cell`` is 3x3 with ROWS = lattice vectors (``cell[k, :]`` is vector k),
+exactly like the reference.  Every call goes through libnlgpu.so; there is no
+CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import Callable, Optional, Tuple
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import NLError, check, lib
+
+__all__ = [
+    "SortedCellList", "PairList", "NLError", "analyze_cell", "build_cell_list", "materialize_pairlist",
+    "neighbour_list", "npairs", "nsites", "nneigs", "maxneigs", "max_neighbours", "neigs", "neigss", "neighbours",
+    "num_neighbours", "count_neighbours", "for_each_neighbour", "lazy_reduce", "cutoff",
+]
+
+_D = C.POINTER(C.c_double)
+_I64 = C.POINTER(C.c_int64)
+_U8 = C.POINTER(C.c_uint8)
+
+
+# ----------------------------------------------------------------- helpers --
+def _index_bytes(int_type) -> int:
+    if int_type in (torch.int32, np.int32, "Int32", "int32"):
+        return 4
+    if int_type in (torch.int64, np.int64, "Int64", "int64"):
+        return 8
+    raise ValueError(f"int_type must be Int32 or Int64, got {int_type!r}")
+
+
+def _tdtype(index_bytes: int):
+    return torch.int32 if index_bytes == 4 else torch.int64
+
+
+def _colmajor(cell) -> np.ndarray:
+    c = np.asarray(cell, dtype=np.float64)
+    if c.shape != (3, 3):
+        raise ValueError("cell must be a 3x3 matrix (rows are lattice vectors)")
+    return np.ascontiguousarray(c.T).reshape(9)
+
+
+def _pbc(pbc) -> np.ndarray:
+    p = [bool(b) for b in pbc]
+    if len(p) != 3:
+        raise ValueError("pbc must have 3 entries")
+    return np.array([1 if b else 0 for b in p], dtype=np.uint8)
+
+
+def _ptr(t: Optional[torch.Tensor]):
+    return C.c_void_p(t.data_ptr()) if t is not None and t.numel() > 0 else C.c_void_p(0)
+
+
+def _stream_handle(stream=None):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+def _device_positions(X) -> torch.Tensor:
+    """(N,3) float64 contiguous CUDA tensor; host arrays are copied to the GPU."""
+    if isinstance(X, torch.Tensor):
+        t = X
+    else:
+        t = torch.from_numpy(np.ascontiguousarray(np.asarray(X, dtype=np.float64).reshape(-1, 3)))
+    if t.dtype != torch.float64:
+        raise TypeError("positions must be Float64 (float64)")
+    t = t.reshape(-1, 3)
+    if not t.is_cuda:
+        t = t.to("cuda", non_blocking=False)
+    return t.contiguous()
+
+
+@dataclass
+class CellPlan:
+    """analyze_cell (cell_list.jl:152-170) + nxyz (gpu_kernels.jl:315-316)."""
+    cell_cm: np.ndarray        # 9 doubles, column-major
+    inv_cm: np.ndarray         # 9 doubles, column-major
+    lens: np.ndarray
+    ncells: np.ndarray         # int64[3]
+    nxyz: np.ndarray           # int64[3]
+    ncells_total: int
+    band: float
+
+    @property
+    def inv_cell(self) -> np.ndarray:
+        return self.inv_cm.reshape(3, 3).T.copy()
+
+
+def analyze_cell(cell, cutoff: float, int_type=torch.int32) -> CellPlan:
+    plan = _lib.CellPlan()
+    cm = _colmajor(cell)
+    check(lib().nl_analyze_cell(cm.ctypes.data_as(_D), float(cutoff), _index_bytes(int_type), C.byref(plan)))
+    return CellPlan(cm, np.array(plan.inv_cell[:]), np.array(plan.lens[:]), np.array(plan.ncells[:], dtype=np.int64),
+                    np.array(plan.nxyz[:], dtype=np.int64), int(plan.ncells_total), float(plan.band))
+
+
+# ------------------------------------------------------------------- types --
+@dataclass
+class SortedCellList:
+    """Mirror of SortedCellList (src/types.jl:70-82)."""
+    X: torch.Tensor              # positions sorted by cell id (N,3)
+    X_orig: torch.Tensor         # original positions (N,3)
+    perm: torch.Tensor           # sorted index -> original index (1-based)
+    cell_id: torch.Tensor        # cell id per sorted atom (1-based)
+    cell_offsets: torch.Tensor   # CSR over cells (1-based, ncells_total+1)
+    cell: np.ndarray             # 3x3, rows = lattice vectors
+    inv_cell: np.ndarray         # 3x3
+    pbc: Tuple[bool, bool, bool]
+    cutoff: float
+    ncells: np.ndarray           # int64[3]
+    ncells_total: int
+    _plan: CellPlan = field(repr=False, default=None)
+    _ws: torch.Tensor = field(repr=False, default=None)
+    _records: bool = field(repr=False, default=False)
+
+    @property
+    def index_bytes(self) -> int:
+        return 4 if self.perm.dtype == torch.int32 else 8
+
+
+@dataclass
+class PairList:
+    """Mirror of PairList (src/types.jl:34-43) plus the pair vectors R."""
+    X: torch.Tensor              # positions the list refers to (original order)
+    C: np.ndarray                # 3x3 cell
+    cutoff: float
+    i: torch.Tensor              # 1-based
+    j: torch.Tensor              # 1-based
+    S: torch.Tensor              # (npairs, 3) integer cell shifts
+    first: torch.Tensor          # 1-based CSR per atom (nsites+1)
+    R: Optional[torch.Tensor] = None   # (npairs, 3) float64, R = X[j]-X[i]+C'S
+    rechecks: int = 0            # candidates decided in FP64 (statistics)
+
+    def __post_init__(self):
+        self._first_host = None
+
+    def _first_np(self) -> np.ndarray:
+        if self._first_host is None:
+            self._first_host = self.first.cpu().numpy().astype(np.int64)
+        return self._first_host
+
+
+# --------------------------------------------------------------- building --
+def _plan_args(clist: SortedCellList):
+    p = clist._plan
+    return (p.cell_cm.ctypes.data_as(_D), p.inv_cm.ctypes.data_as(_D), p.ncells.ctypes.data_as(_I64),
+            p.nxyz.ctypes.data_as(_I64))
+
+
+def _new_workspace(nat: int, ncells_total: int, device) -> torch.Tensor:
+    nbytes = int(lib().nl_workspace_bytes(nat, ncells_total))
+    if nbytes == 0:
+        raise NLError(_lib.NL_ERR_ARG, "invalid workspace size")
+    return torch.empty(nbytes, dtype=torch.uint8, device=device)
+
+
+def build_cell_list(X, cutoff: float, cell, pbc, int_type=torch.int32, stream=None) -> SortedCellList:
+    """build_cell_list(X, cutoff, cell, pbc; int_type) (cell_list.jl:632-679)."""
+    ib = _index_bytes(int_type)
+    Xd = _device_positions(X)
+    nat = int(Xd.shape[0])
+    plan = analyze_cell(cell, cutoff, int_type)
+    dev = Xd.device
+    ti = _tdtype(ib)
+    perm = torch.empty(nat, dtype=ti, device=dev)
+    Xs = torch.empty((nat, 3), dtype=torch.float64, device=dev)
+    cid = torch.empty(nat, dtype=ti, device=dev)
+    offs = torch.empty(plan.ncells_total + 1, dtype=ti, device=dev)
+    ws = _new_workspace(nat, plan.ncells_total, dev)
+    pb = _pbc(pbc)
+    with torch.cuda.device(dev):
+        check(lib().nl_build_cell_list(_ptr(Xd), nat, plan.cell_cm.ctypes.data_as(_D), plan.inv_cm.ctypes.data_as(_D),
+                                       plan.ncells.ctypes.data_as(_I64), pb.ctypes.data_as(_U8), float(cutoff), ib,
+                                       _ptr(perm), _ptr(Xs), _ptr(cid), C.c_void_p(offs.data_ptr()), _ptr(ws),
+                                       ws.numel(), _stream_handle(stream)))
+        check(lib().nl_sync_status(_ptr(ws), _stream_handle(stream)))
+    cellm = np.asarray(cell, dtype=np.float64).reshape(3, 3).copy()
+    return SortedCellList(Xs, Xd, perm, cid, offs, cellm, plan.inv_cell, tuple(bool(b) for b in pb), float(cutoff),
+                          plan.ncells.copy(), plan.ncells_total, plan, ws, True)
+
+
+def materialize_pairlist(clist: SortedCellList, with_R: bool = True, stream=None) -> PairList:
+    """materialize_pairlist(clist) (gpu_kernels.jl:299-364) + R."""
+    nat = int(clist.X_orig.shape[0])
+    ib = clist.index_bytes
+    dev = clist.X_orig.device
+    ti = _tdtype(ib)
+    if clist._ws is None:
+        clist._ws = _new_workspace(nat, clist.ncells_total, dev)
+        clist._records = False
+    ws = clist._ws
+    pb = _pbc(clist.pbc)
+    cm, im, nc, nx = _plan_args(clist)
+    first = torch.empty(nat + 1, dtype=ti, device=dev)
+    total = C.c_int64(0)
+    sh = _stream_handle(stream)
+    with torch.cuda.device(dev):
+        check(lib().nl_count_pairs(_ptr(clist.X), _ptr(clist.perm), _ptr(clist.cell_id),
+                                   C.c_void_p(clist.cell_offsets.data_ptr()), nat, cm, im, nc, nx,
+                                   pb.ctypes.data_as(_U8), clist.cutoff, ib, 1 if clist._records else 0,
+                                   C.c_void_p(first.data_ptr()), C.byref(total), _ptr(ws), ws.numel(), sh))
+        clist._records = True
+        rechecks = C.c_int64(0)
+        check(lib().nl_last_recheck_count(_ptr(ws), sh, C.byref(rechecks)))
+        P = int(total.value)
+        i = torch.empty(P, dtype=ti, device=dev)
+        j = torch.empty(P, dtype=ti, device=dev)
+        S = torch.empty((P, 3), dtype=ti, device=dev)
+        R = torch.empty((P, 3), dtype=torch.float64, device=dev) if with_R else None
+        if P > 0:
+            check(lib().nl_fill_pairs(_ptr(clist.X), _ptr(clist.perm), C.c_void_p(clist.cell_offsets.data_ptr()), nat,
+                                      cm, im, nc, nx, pb.ctypes.data_as(_U8), clist.cutoff, ib,
+                                      C.c_void_p(first.data_ptr()), P, _ptr(i), _ptr(j), _ptr(S), _ptr(R), _ptr(ws),
+                                      ws.numel(), sh))
+            check(lib().nl_sync_status(_ptr(ws), sh))
+    return PairList(clist.X_orig, clist.cell.copy(), clist.cutoff, i, j, S, first, R, int(rechecks.value))
+
+
+def neighbour_list(X, cutoff: float, cell, pbc, lazy: bool = False, int_type=torch.int32, with_R: bool = True,
+                   stream=None):
+    """neighbour_list(X, cutoff, cell, pbc; lazy, int_type) (cell_list.jl:897-916)."""
+    clist = build_cell_list(X, cutoff, cell, pbc, int_type=int_type, stream=stream)
+    if lazy:
+        return clist
+    return materialize_pairlist(clist, with_R=with_R, stream=stream)
+
+
+def lazy_reduce(clist: SortedCellList, op: str = "count", stream=None) -> torch.Tensor:
+    """Built-in reductions of the lazy traversal over every atom:
+    "count" -> int32 neighbour count per atom (count_neighbours for all i);
+    "inv_r6" -> float64 per-atom sum of 1/r^6 in the reference's order."""
+    nat = int(clist.X_orig.shape[0])
+    dev = clist.X_orig.device
+    if op == "count":
+        code, out = _lib.NL_REDUCE_COUNT, torch.zeros(nat, dtype=torch.int32, device=dev)
+    elif op == "inv_r6":
+        code, out = _lib.NL_REDUCE_INV_R6, torch.zeros(nat, dtype=torch.float64, device=dev)
+    else:
+        raise ValueError("op must be 'count' or 'inv_r6'")
+    if clist._ws is None:
+        clist._ws = _new_workspace(nat, clist.ncells_total, dev)
+        clist._records = False
+    ws = clist._ws
+    pb = _pbc(clist.pbc)
+    cm, im, nc, nx = _plan_args(clist)
+    sh = _stream_handle(stream)
+    with torch.cuda.device(dev):
+        check(lib().nl_lazy_reduce(_ptr(clist.X), _ptr(clist.perm), _ptr(clist.cell_id),
+                                   C.c_void_p(clist.cell_offsets.data_ptr()), nat, cm, im, nc, nx,
+                                   pb.ctypes.data_as(_U8), clist.cutoff, clist.index_bytes,
+                                   1 if clist._records else 0, code, _ptr(out), _ptr(ws), ws.numel(), sh))
+        clist._records = True
+        check(lib().nl_sync_status(_ptr(ws), sh))
+    return out
+
+
+# --------------------------------------------------------------- accessors --
+def npairs(nlist: PairList) -> int:
+    return int(nlist.i.shape[0])
+
+
+def nsites(x) -> int:
+    if isinstance(x, PairList):
+        return int(x.first.shape[0]) - 1
+    return int(x.X_orig.shape[0])
+
+
+def cutoff(x) -> float:
+    return float(x.cutoff)
+
+
+def nneigs(nlist: PairList, i0: int) -> int:
+    f = nlist._first_np()
+    return int(f[i0] - f[i0 - 1])
+
+
+def maxneigs(nlist: PairList) -> int:
+    if nsites(nlist) == 0:
+        raise ValueError("maxneigs of an empty PairList")
+    f = nlist._first_np()
+    return int(np.max(np.diff(f)))
+
+
+max_neighbours = maxneigs
+
+
+def neigss(nlist: PairList, i0: int):
+    """neigss(nlist, i0) -> (j, R, S) (cell_list.jl:583-598): views of atom i0's
+    neighbours (i0 is 1-based).  R comes from the device R buffer, bit-equal to
+    the reference's _getR."""
+    f = nlist._first_np()
+    a, b = int(f[i0 - 1]) - 1, int(f[i0]) - 1
+    R = nlist.R[a:b] if nlist.R is not None else _getR(nlist, a, b)
+    return nlist.j[a:b], R, nlist.S[a:b]
+
+
+def neigs(nlist: PairList, i0: int):
+    j, R, _ = neigss(nlist, i0)
+    return j, R
+
+
+def _getR(nlist: PairList, a: int, b: int) -> torch.Tensor:
+    raise NLError(_lib.NL_ERR_ARG, "this PairList was materialised without R (with_R=False)")
+
+
+def count_neighbours(clist: SortedCellList, i: int) -> int:
+    """count_neighbours(clist, i) (cell_list.jl:808-814), i 1-based."""
+    return int(lazy_reduce(clist, "count")[i - 1].item())
+
+
+def neighbours(x, i: int):
+    """neighbours(nlist, i) = neigss; neighbours(clist, i) -> (js, Rs, Ss)
+    (cell_list.jl:606, 821-833)."""
+    if isinstance(x, PairList):
+        return neigss(x, i)
+    nl = _lazy_pairlist(x)
+    return neigss(nl, i)
+
+
+def _lazy_pairlist(clist: SortedCellList) -> PairList:
+    cached = getattr(clist, "_lazy_nl", None)
+    if cached is None:
+        cached = materialize_pairlist(clist)
+        object.__setattr__(clist, "_lazy_nl", cached)
+    return cached
+
+
+def num_neighbours(x, i: int) -> int:
+    """num_neighbours (cell_list.jl:926-927)."""
+    if isinstance(x, PairList):
+        return nneigs(x, i)
+    return count_neighbours(x, i)
+
+
+def for_each_neighbour(f: Callable, clist: SortedCellList, i: int) -> None:
+    """for_each_neighbour(f, clist, i) (cell_list.jl:779-801): calls
+    f(j, R, S) for each neighbour of atom i (1-based) in the reference's order.
+    The traversal runs on the GPU; f runs on the host."""
+    js, Rs, Ss = neighbours(clist, i)
+    js, Rs, Ss = js.cpu().numpy(), Rs.cpu().numpy(), Ss.cpu().numpy()
+    for k in range(js.shape[0]):
+        f(int(js[k]), Rs[k], Ss[k])

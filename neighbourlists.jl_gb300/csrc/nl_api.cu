@@ -1,0 +1,594 @@
+// C ABI of the neighbour-list engine (declared in include/nlgpu.h).
+//
+// Host orchestration of the kernels in nl_build.cu / nl_pairs.cu, the
+// restated cell analysis of the reference (analyze_cell, cell_list.jl:152-170,
+// with StaticArrays' 3x3 inv/det/cross/norm operation order), and the
+// rigorous half-width of the FP32 screen's FP64 recheck band.
+//
+// Host floating point must not be contracted into FMAs (Julia rounds every
+// operation): the build passes -ffp-contract=off to the host compiler.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "nl_build.cuh"
+#include "nl_common.cuh"
+#include "nl_pairs.cuh"
+#include "nlgpu.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int status, const std::string& msg) {
+  g_last_error = msg;
+  return status;
+}
+
+int cuda_fail(cudaError_t e, const char* where) {
+  return fail(NL_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+// ------------------------------------------------ StaticArrays 3x3 algebra --
+void sa_cross(const double* a, const double* b, double* o) {
+  o[0] = a[1] * b[2] - a[2] * b[1];
+  o[1] = a[2] * b[0] - a[0] * b[2];
+  o[2] = a[0] * b[1] - a[1] * b[0];
+}
+double sa_dot(const double* a, const double* b) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
+double sa_norm(const double* a) { return std::sqrt((a[0] * a[0] + a[1] * a[1]) + a[2] * a[2]); }
+double sa_det(const double* M) {
+  double c[3];
+  sa_cross(M + 3, M + 6, c);
+  return sa_dot(M, c);
+}
+// inv of a column-major 3x3: rows of the result are y0, y1, y2 with
+// y0 = x1 x x2 / d, y1 = x2 x (x0/d), y2 = (x0/d) x x1, d = x0 . (x1 x x2).
+void sa_inv(const double* M, double* out) {
+  double x0[3] = {M[0], M[1], M[2]}, x1[3] = {M[3], M[4], M[5]}, x2[3] = {M[6], M[7], M[8]};
+  double y0[3], y1[3], y2[3];
+  sa_cross(x1, x2, y0);
+  const double d = sa_dot(x0, y0);
+  for (int k = 0; k < 3; ++k) {
+    x0[k] = x0[k] / d;
+    y0[k] = y0[k] / d;
+  }
+  sa_cross(x2, x0, y1);
+  sa_cross(x0, x1, y2);
+  for (int c = 0; c < 3; ++c) {
+    out[0 + 3 * c] = y0[c];
+    out[1 + 3 * c] = y1[c];
+    out[2 + 3 * c] = y2[c];
+  }
+}
+// lengths(C) = det(C) ./ (|r2 x r3|, |r3 x r1|, |r1 x r2|), cell_list.jl:94-95
+void lengths(const double* C, double* lens) {
+  const double r1[3] = {C[0], C[3], C[6]}, r2[3] = {C[1], C[4], C[7]}, r3[3] = {C[2], C[5], C[8]};
+  const double det = sa_det(C);
+  double c[3];
+  sa_cross(r2, r3, c);
+  lens[0] = det / sa_norm(c);
+  sa_cross(r3, r1, c);
+  lens[1] = det / sa_norm(c);
+  sa_cross(r1, r2, c);
+  lens[2] = det / sa_norm(c);
+}
+
+// ------------------------------------------------------- FP32 screen band --
+// The kernel screens candidates with r2_32 = |v_j - u_i|^2 where u (per atom)
+// and v = u_j + d.b (per candidate) are FP32 sums of FP64-exact cell-local
+// coordinates t (|t_k| <= kMaxT for non-exact atoms) times the bin vectors b_k.
+// Per Cartesian component r the FP32 error of R is at most
+//   e_r = 2^-24 * 1.01 * ((11 T + 2) B_r + 4 O_r + |R_r|) + e64,
+//   B_r = sum_k |b_kr|,  O_r = sum_k nxyz_k |b_kr|,
+// where e64 = 2^-29 (1 + cond(C)) sum_k |b_k| bounds the difference between
+// the reference's FP64 R and the exact R of the FP64 t values for atoms with
+// |frac*n| <= kMaxY.  With |R_r| <= cutoff near the cutoff, the error of r2 is
+// at most Delta = sum_r (2 rc e_r + e_r^2) + 3.03 * 2^-24 rc^2 + 2^-51 rc^2.
+// The band is max(1e-5 rc^2, 2 Delta): outside it the FP32 decision equals
+// the FP64 one, inside it the kernel decides in FP64.
+double screen_band(const double* C, const double* inv, const int64_t* ns, const int64_t* nxyz, double rc) {
+  const double eps = std::ldexp(1.0, -24);
+  double b[3][3], B[3] = {0, 0, 0}, O[3] = {0, 0, 0}, bsum = 0;
+  for (int k = 0; k < 3; ++k) {
+    double nk = 0;
+    for (int r = 0; r < 3; ++r) {
+      b[k][r] = C[k + 3 * r] / double(ns[k]);
+      B[r] += std::fabs(b[k][r]);
+      O[r] += double(nxyz[k]) * std::fabs(b[k][r]);
+      nk += b[k][r] * b[k][r];
+    }
+    bsum += std::sqrt(nk);
+  }
+  double cn = 0, in = 0;  // infinity norms
+  for (int r = 0; r < 3; ++r) {
+    double rc_ = 0, ri = 0;
+    for (int c = 0; c < 3; ++c) {
+      rc_ += std::fabs(C[r + 3 * c]);
+      ri += std::fabs(inv[r + 3 * c]);
+    }
+    cn = std::fmax(cn, rc_);
+    in = std::fmax(in, ri);
+  }
+  const double cond = cn * in;
+  const double e64 = std::ldexp(1.0, -29) * (1.0 + cond) * bsum;
+  const double T = nl::kMaxT;
+  double delta = 0;
+  for (int r = 0; r < 3; ++r) {
+    const double e = eps * 1.01 * ((11 * T + 2) * B[r] + 4 * O[r] + rc) + e64;
+    delta += 2 * rc * e + e * e;
+  }
+  delta += 3.03 * eps * rc * rc + std::ldexp(1.0, -51) * rc * rc;
+  return std::fmax(1e-5 * rc * rc, 2 * delta);
+}
+
+int analyze(const double* cell, double cutoff, int index_bytes, nl_cell_plan* p) {
+  if (!(cutoff > 0) || !std::isfinite(cutoff)) return fail(NL_ERR_ARG, "cutoff must be positive and finite");
+  if (index_bytes != 4 && index_bytes != 8) return fail(NL_ERR_ARG, "index_bytes must be 4 or 8");
+  sa_inv(cell, p->inv_cell);
+  lengths(cell, p->lens);
+  const double tmax = index_bytes == 4 ? 2147483647.0 : 9223372036854775807.0;
+  long double prod = 1;
+  for (int k = 0; k < 3; ++k) {
+    p->lens[k] = std::fabs(p->lens[k]);
+    const double t = std::floor(p->lens[k] / cutoff);
+    if (!(t < tmax)) return fail(NL_ERR_TOO_MANY_CELLS, "Ratio of simulation cell size to cutoff is very large.");
+    p->ncells[k] = t < 1 ? 1 : int64_t(t);
+    prod *= (long double)p->ncells[k];
+  }
+  if (prod > (long double)tmax)
+    return fail(NL_ERR_TOO_MANY_CELLS,
+                "Ratio of simulation cell size to cutoff is very large. Use a larger integer type (e.g. Int64), "
+                "larger cutoff, or smaller simulation cell.");
+  if (prod > 2147483646.0L)
+    return fail(NL_ERR_TOO_MANY_CELLS, "more than 2^31-2 cells: use a larger cutoff or a smaller simulation cell");
+  p->ncells_total = p->ncells[0] * p->ncells[1] * p->ncells[2];
+  for (int k = 0; k < 3; ++k) {
+    const double v = std::ceil(cutoff * (double(p->ncells[k]) / p->lens[k]));
+    if (!(v < 1e9)) return fail(NL_ERR_ARG, "degenerate cell: stencil half-width is not finite");
+    p->nxyz[k] = int64_t(v);
+  }
+  p->band = screen_band(cell, p->inv_cell, p->ncells, p->nxyz, cutoff);
+  return NL_OK;
+}
+
+// ------------------------------------------------------------- workspace --
+constexpr size_t kAlign = 256;
+size_t up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
+
+struct Layout {
+  // [err 64 | stats 64] [pairs zero region: counters 64 | st_pairs]
+  // [build zero region: counters 64 | st_cells | cell_count] [arrays...]
+  size_t err, stats, pcount, st_pairs, pend, bcount, st_cells, cell_count, bend;
+  size_t totals, cell_start, cid, ticket, rec, tmp, rec_sorted, counts, big_list, end;
+};
+
+Layout layout(int64_t nat, int64_t ncells) {
+  Layout L;
+  size_t o = 0;
+  L.err = o;
+  L.stats = o + 64;
+  o += 128;
+  L.pcount = o;
+  o += 64;
+  L.st_pairs = o;
+  o += up(sizeof(unsigned long long) * size_t(nl::scan_tiles(nat > 0 ? nat : 1)));
+  L.pend = o;
+  L.bcount = o;
+  o += 64;
+  L.st_cells = o;
+  o += up(sizeof(unsigned long long) * size_t(nl::scan_tiles(ncells > 0 ? ncells : 1)));
+  L.cell_count = o;
+  o += up(sizeof(int) * size_t(ncells));
+  L.bend = o;
+  L.totals = o;
+  o += 64;
+  L.cell_start = o;
+  o += up(sizeof(int) * size_t(ncells + 1));
+  const size_t n = size_t(nat > 0 ? nat : 1);
+  L.cid = o;
+  o += up(sizeof(int) * n);
+  L.ticket = o;
+  o += up(sizeof(int) * n);
+  L.rec = o;
+  o += up(sizeof(float4) * n);
+  L.tmp = o;
+  o += up(sizeof(int) * n);
+  L.rec_sorted = o;
+  o += up(sizeof(float4) * n);
+  L.counts = o;
+  o += up(sizeof(int) * n);
+  L.big_list = o;
+  o += up(sizeof(int) * size_t(ncells < (int64_t)n ? ncells : (int64_t)n));
+  L.end = o;
+  return L;
+}
+
+template <typename T>
+T* at(void* ws, size_t off) {
+  return reinterpret_cast<T*>(static_cast<char*>(ws) + off);
+}
+
+int num_sms() {
+  static int cache[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 148;
+  if (!cache[dev]) {
+    int n = 0;
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    cache[dev] = n > 0 ? n : 148;
+  }
+  return cache[dev];
+}
+
+struct Pinned {
+  long long* p = nullptr;
+  Pinned() { cudaHostAlloc(reinterpret_cast<void**>(&p), 64, cudaHostAllocDefault); }
+  ~Pinned() {
+    if (p) cudaFreeHost(p);
+  }
+};
+long long* pinned_scratch() {
+  thread_local Pinned pin;
+  return pin.p;
+}
+
+int check_common(int64_t nat, const int64_t* ncells, const int64_t* nxyz, int index_bytes, void* ws,
+                 size_t ws_bytes, Layout& L, int64_t& ncells_total) {
+  if (index_bytes != 4 && index_bytes != 8) return fail(NL_ERR_ARG, "index_bytes must be 4 or 8");
+  if (nat < 0 || nat > 2147483646LL) return fail(NL_ERR_ARG, "nat must be in [0, 2^31-2]");
+  long double prod = 1;
+  for (int k = 0; k < 3; ++k) {
+    if (ncells[k] < 1) return fail(NL_ERR_ARG, "ncells must be >= 1");
+    prod *= (long double)ncells[k];
+    if (nxyz && (nxyz[k] < 0 || nxyz[k] > 64))
+      return fail(NL_ERR_ARG, "stencil half-width nxyz must be in [0, 64] (cutoff at most 64 cell widths)");
+  }
+  if (prod > 2147483646.0L) return fail(NL_ERR_TOO_MANY_CELLS, "more than 2^31-2 cells");
+  if (index_bytes == 4 && prod > 2147483647.0L)
+    return fail(NL_ERR_TOO_MANY_CELLS, "Ratio of simulation cell size to cutoff is very large.");
+  ncells_total = int64_t(prod);
+  L = layout(nat, ncells_total);
+  if (!ws || ws_bytes < L.end) return fail(NL_ERR_NOMEM, "workspace too small (see nl_workspace_bytes)");
+  return NL_OK;
+}
+
+nl::Geometry make_geometry(const double* cell, const double* inv, const int64_t* ns, const int64_t* nxyz,
+                           const uint8_t* pbc, double cutoff, int64_t nat) {
+  nl::Geometry g;
+  std::memcpy(g.C, cell, sizeof(g.C));
+  std::memcpy(g.inv, inv, sizeof(g.inv));
+  g.cutoff_sq = cutoff * cutoff;
+  for (int k = 0; k < 3; ++k) {
+    g.ns[k] = int(ns[k]);
+    g.nxyz[k] = nxyz ? int(nxyz[k]) : 0;
+    g.pbc[k] = pbc[k] ? 1 : 0;
+    for (int r = 0; r < 3; ++r) g.b[3 * k + r] = float(cell[k + 3 * r] / double(ns[k]));
+  }
+  g.ncells = int(ns[0] * ns[1] * ns[2]);
+  g.nat = int(nat);
+  double band = 0;
+  if (nxyz) {
+    band = screen_band(cell, inv, ns, nxyz, cutoff);
+  }
+  const double lo = g.cutoff_sq - band, hi = g.cutoff_sq + band;
+  float flo = float(lo), fhi = float(hi);
+  if (double(flo) > lo) flo = std::nextafter(flo, -INFINITY);
+  if (double(fhi) < hi) fhi = std::nextafter(fhi, INFINITY);
+  g.lo = lo > 0 ? flo : -1.0f;  // lo <= 0: every candidate is rechecked
+  g.hi = fhi;
+  return g;
+}
+
+int status_from_flags(unsigned f) {
+  if (f & nl::kFlagBadPosition)
+    return fail(NL_ERR_BAD_POSITION, "non-finite position or |frac * ncells| >= 2^30 (cannot be binned)");
+  if (f & nl::kFlagInconsistent) return fail(NL_ERR_INCONSISTENT, "cell list ids do not match its positions");
+  if (f & nl::kFlagTimeout) return fail(NL_ERR_TIMEOUT, "a bounded device-side wait timed out");
+  if (f & nl::kFlagIndexOverflow) return fail(NL_ERR_INDEX_OVERFLOW, "pair count does not fit the index type");
+  if (f & nl::kFlagCapacity) return fail(NL_ERR_CAPACITY, "pair buffers are smaller than the pair count");
+  return NL_OK;
+}
+
+// read err word (and optionally a total) after synchronising; clears err
+int sync_read(void* ws, cudaStream_t st, const long long* d_total, int64_t* total) {
+  long long* h = pinned_scratch();
+  if (!h) return fail(NL_ERR_NOMEM, "cannot allocate pinned host scratch");
+  cudaError_t e = cudaMemcpyAsync(h, ws, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && d_total) e = cudaMemcpyAsync(h + 1, d_total, sizeof(long long), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ws, 0, sizeof(unsigned), st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "synchronise");
+  unsigned flags = *reinterpret_cast<unsigned*>(h);
+  if (d_total && total) *total = h[1];
+  return status_from_flags(flags);
+}
+
+template <typename TI>
+int build_impl(const double* X, int64_t nat, const nl::Geometry& g, TI* perm, double* Xs, TI* cell_id,
+               TI* cell_offsets, void* ws, const Layout& L, cudaStream_t st) {
+  const int sms = num_sms();
+  cudaError_t e = cudaMemsetAsync(ws, 0, L.bend, st);  // err, stats, both zero regions
+  if (e != cudaSuccess) return cuda_fail(e, "memset workspace");
+  if (nat == 0) {
+    // empty system: cell_offsets all ones (cell_list.jl:731-734) -- the scan
+    // of the (zeroed) histogram produces exactly that
+    nl::launch_scan<TI>(at<int>(ws, L.cell_count), g.ncells, cell_offsets, at<int>(ws, L.cell_start),
+                        at<unsigned long long>(ws, L.st_cells), at<int>(ws, L.bcount), at<long long>(ws, L.totals),
+                        at<unsigned>(ws, L.err), st);
+    e = cudaGetLastError();
+    return e == cudaSuccess ? NL_OK : cuda_fail(e, "launch");
+  }
+  int* cid = at<int>(ws, L.cid);
+  int* ticket = at<int>(ws, L.ticket);
+  float4* rec = at<float4>(ws, L.rec);
+  int* cell_count = at<int>(ws, L.cell_count);
+  int* cell_start = at<int>(ws, L.cell_start);
+  unsigned* err = at<unsigned>(ws, L.err);
+  int* bcount = at<int>(ws, L.bcount);
+  nl::launch_bin(g, X, int(nat), cid, ticket, rec, cell_count, err, sms, st);
+  nl::launch_scan<TI>(cell_count, g.ncells, cell_offsets, cell_start, at<unsigned long long>(ws, L.st_cells), bcount,
+                      at<long long>(ws, L.totals), err, st);
+  nl::launch_scatter(int(nat), cid, ticket, cell_start, at<int>(ws, L.tmp), sms, st);
+  nl::launch_fix<TI>(int(nat), at<int>(ws, L.tmp), cid, cell_start, X, rec, perm, cell_id, Xs,
+                     at<float4>(ws, L.rec_sorted), at<int>(ws, L.big_list), bcount + 1, sms, st);
+  e = cudaGetLastError();
+  return e == cudaSuccess ? NL_OK : cuda_fail(e, "launch build kernels");
+}
+
+template <typename TI>
+nl::PairArgs<TI> pair_args(const nl::Geometry& g, const TI* cell_offsets, const TI* perm, const double* Xs, void* ws,
+                           const Layout& L) {
+  nl::PairArgs<TI> a;
+  std::memset(&a, 0, sizeof(a));
+  a.g = g;
+  a.cell_offsets = cell_offsets;
+  a.perm = perm;
+  a.Xs = Xs;
+  a.rec = at<float4>(ws, L.rec_sorted);
+  a.stats = at<unsigned long long>(ws, L.stats);
+  a.err = at<unsigned>(ws, L.err);
+  return a;
+}
+
+template <typename TI>
+int count_impl(const nl::Geometry& g, const double* Xs, const TI* perm, const TI* cell_id, const TI* cell_offsets,
+               int reuse, TI* first, void* ws, const Layout& L, cudaStream_t st) {
+  const int sms = num_sms();
+  // reuse: keep err (set by the build), reset stats and the pair scan state
+  const size_t z0 = reuse ? L.stats : L.err;
+  cudaError_t e = cudaMemsetAsync(static_cast<char*>(ws) + z0, 0, L.pend - z0, st);
+  if (e != cudaSuccess) return cuda_fail(e, "memset workspace");
+  if (g.nat == 0) {
+    // first = [1]
+    static const TI one = 1;
+    e = cudaMemcpyAsync(first, &one, sizeof(TI), cudaMemcpyHostToDevice, st);
+    return e == cudaSuccess ? NL_OK : cuda_fail(e, "empty system");
+  }
+  if (!reuse)
+    nl::launch_prepare<TI>(g, Xs, cell_id, perm, g.nat, at<float4>(ws, L.rec_sorted), at<unsigned>(ws, L.err), sms, st);
+  nl::PairArgs<TI> a = pair_args<TI>(g, cell_offsets, perm, Xs, ws, L);
+  a.counts = at<int>(ws, L.counts);
+  nl::launch_pairs<TI>(nl::kModeCount, a, sms, st);
+  nl::launch_scan<TI>(at<int>(ws, L.counts), g.nat, first, nullptr, at<unsigned long long>(ws, L.st_pairs),
+                      at<int>(ws, L.pcount), at<long long>(ws, L.totals) + 1, at<unsigned>(ws, L.err), st);
+  e = cudaGetLastError();
+  return e == cudaSuccess ? NL_OK : cuda_fail(e, "launch count kernels");
+}
+
+template <typename TI>
+int fill_impl(const nl::Geometry& g, const double* Xs, const TI* perm, const TI* cell_offsets, const TI* first,
+              int64_t capacity, TI* oi, TI* oj, TI* oS, double* oR, void* ws, const Layout& L, cudaStream_t st) {
+  if (g.nat == 0 || capacity <= 0) return NL_OK;
+  nl::PairArgs<TI> a = pair_args<TI>(g, cell_offsets, perm, Xs, ws, L);
+  a.first = first;
+  a.oi = oi;
+  a.oj = oj;
+  a.oS = oS;
+  a.oR = oR;
+  a.capacity = capacity;
+  nl::launch_pairs<TI>(nl::kModeFill, a, num_sms(), st);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? NL_OK : cuda_fail(e, "launch fill kernel");
+}
+
+}  // namespace
+
+// ======================================================================
+extern "C" {
+
+int nl_version(void) { return 1; }
+
+const char* nl_last_error(void) { return g_last_error.c_str(); }
+
+const char* nl_status_string(int s) {
+  switch (s) {
+    case NL_OK: return "ok";
+    case NL_ERR_ARG: return "invalid argument";
+    case NL_ERR_TOO_MANY_CELLS: return "too many cells";
+    case NL_ERR_NOMEM: return "out of memory";
+    case NL_ERR_CUDA: return "CUDA error";
+    case NL_ERR_TIMEOUT: return "device wait timed out";
+    case NL_ERR_BAD_POSITION: return "position cannot be binned";
+    case NL_ERR_CAPACITY: return "pair buffer capacity exceeded";
+    case NL_ERR_INDEX_OVERFLOW: return "index type overflow";
+    case NL_ERR_INCONSISTENT: return "inconsistent cell list";
+    default: return "unknown status";
+  }
+}
+
+int nl_analyze_cell(const double cell[9], double cutoff, int index_bytes, nl_cell_plan* plan) {
+  if (!cell || !plan) return fail(NL_ERR_ARG, "null argument");
+  return analyze(cell, cutoff, index_bytes, plan);
+}
+
+size_t nl_workspace_bytes(int64_t nat, int64_t ncells_total) {
+  if (nat < 0 || ncells_total < 1) return 0;
+  return layout(nat, ncells_total).end;
+}
+
+int nl_build_cell_list(const double* d_X, int64_t nat, const double cell[9], const double inv_cell[9],
+                       const int64_t ncells[3], const uint8_t pbc[3], double cutoff, int index_bytes, void* d_perm,
+                       double* d_X_sorted, void* d_cell_id, void* d_cell_offsets, void* d_workspace,
+                       size_t workspace_bytes, void* stream) {
+  if (!cell || !inv_cell || !ncells || !pbc || !d_cell_offsets || (nat > 0 && (!d_X || !d_perm || !d_X_sorted || !d_cell_id)))
+    return fail(NL_ERR_ARG, "null argument");
+  Layout L;
+  int64_t nct;
+  int s = check_common(nat, ncells, nullptr, index_bytes, d_workspace, workspace_bytes, L, nct);
+  if (s) return s;
+  const nl::Geometry g = make_geometry(cell, inv_cell, ncells, nullptr, pbc, cutoff, nat);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (index_bytes == 4)
+    return build_impl<int32_t>(d_X, nat, g, static_cast<int32_t*>(d_perm), d_X_sorted, static_cast<int32_t*>(d_cell_id),
+                               static_cast<int32_t*>(d_cell_offsets), d_workspace, L, st);
+  return build_impl<int64_t>(d_X, nat, g, static_cast<int64_t*>(d_perm), d_X_sorted, static_cast<int64_t*>(d_cell_id),
+                             static_cast<int64_t*>(d_cell_offsets), d_workspace, L, st);
+}
+
+int nl_count_pairs(const double* d_X_sorted, const void* d_perm, const void* d_cell_id, const void* d_cell_offsets,
+                   int64_t nat, const double cell[9], const double inv_cell[9], const int64_t ncells[3],
+                   const int64_t nxyz[3], const uint8_t pbc[3], double cutoff, int index_bytes, int reuse_records,
+                   void* d_first, int64_t* total_pairs, void* d_workspace, size_t workspace_bytes, void* stream) {
+  if (!cell || !inv_cell || !ncells || !nxyz || !pbc || !d_first || !d_cell_offsets ||
+      (nat > 0 && (!d_X_sorted || !d_perm || !d_cell_id)))
+    return fail(NL_ERR_ARG, "null argument");
+  Layout L;
+  int64_t nct;
+  int s = check_common(nat, ncells, nxyz, index_bytes, d_workspace, workspace_bytes, L, nct);
+  if (s) return s;
+  const nl::Geometry g = make_geometry(cell, inv_cell, ncells, nxyz, pbc, cutoff, nat);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (index_bytes == 4)
+    s = count_impl<int32_t>(g, d_X_sorted, static_cast<const int32_t*>(d_perm), static_cast<const int32_t*>(d_cell_id),
+                            static_cast<const int32_t*>(d_cell_offsets), reuse_records, static_cast<int32_t*>(d_first),
+                            d_workspace, L, st);
+  else
+    s = count_impl<int64_t>(g, d_X_sorted, static_cast<const int64_t*>(d_perm), static_cast<const int64_t*>(d_cell_id),
+                            static_cast<const int64_t*>(d_cell_offsets), reuse_records, static_cast<int64_t*>(d_first),
+                            d_workspace, L, st);
+  if (s) return s;
+  if (total_pairs) {
+    if (nat == 0) {
+      *total_pairs = 0;
+      return sync_read(d_workspace, st, nullptr, nullptr);
+    }
+    return sync_read(d_workspace, st, at<long long>(d_workspace, L.totals) + 1, total_pairs);
+  }
+  return NL_OK;
+}
+
+int nl_fill_pairs(const double* d_X_sorted, const void* d_perm, const void* d_cell_offsets, int64_t nat,
+                  const double cell[9], const double inv_cell[9], const int64_t ncells[3], const int64_t nxyz[3],
+                  const uint8_t pbc[3], double cutoff, int index_bytes, const void* d_first, int64_t capacity,
+                  void* d_i, void* d_j, void* d_S, double* d_R, void* d_workspace, size_t workspace_bytes,
+                  void* stream) {
+  if (!cell || !inv_cell || !ncells || !nxyz || !pbc || !d_first || !d_cell_offsets)
+    return fail(NL_ERR_ARG, "null argument");
+  if (capacity > 0 && (!d_i || !d_j || !d_S || !d_X_sorted || !d_perm)) return fail(NL_ERR_ARG, "null argument");
+  Layout L;
+  int64_t nct;
+  int s = check_common(nat, ncells, nxyz, index_bytes, d_workspace, workspace_bytes, L, nct);
+  if (s) return s;
+  const nl::Geometry g = make_geometry(cell, inv_cell, ncells, nxyz, pbc, cutoff, nat);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (index_bytes == 4)
+    return fill_impl<int32_t>(g, d_X_sorted, static_cast<const int32_t*>(d_perm), static_cast<const int32_t*>(d_cell_offsets),
+                              static_cast<const int32_t*>(d_first), capacity, static_cast<int32_t*>(d_i),
+                              static_cast<int32_t*>(d_j), static_cast<int32_t*>(d_S), d_R, d_workspace, L, st);
+  return fill_impl<int64_t>(g, d_X_sorted, static_cast<const int64_t*>(d_perm), static_cast<const int64_t*>(d_cell_offsets),
+                            static_cast<const int64_t*>(d_first), capacity, static_cast<int64_t*>(d_i),
+                            static_cast<int64_t*>(d_j), static_cast<int64_t*>(d_S), d_R, d_workspace, L, st);
+}
+
+int nl_neighbour_list(const double* d_X, int64_t nat, const double cell[9], const double inv_cell[9],
+                      const int64_t ncells[3], const int64_t nxyz[3], const uint8_t pbc[3], double cutoff,
+                      int index_bytes, void* d_perm, double* d_X_sorted, void* d_cell_id, void* d_cell_offsets,
+                      void* d_first, int64_t capacity, void* d_i, void* d_j, void* d_S, double* d_R,
+                      int64_t* total_pairs, void* d_workspace, size_t workspace_bytes, void* stream) {
+  int s = nl_build_cell_list(d_X, nat, cell, inv_cell, ncells, pbc, cutoff, index_bytes, d_perm, d_X_sorted, d_cell_id,
+                             d_cell_offsets, d_workspace, workspace_bytes, stream);
+  if (s) return s;
+  s = nl_count_pairs(d_X_sorted, d_perm, d_cell_id, d_cell_offsets, nat, cell, inv_cell, ncells, nxyz, pbc, cutoff,
+                     index_bytes, 1, d_first, nullptr, d_workspace, workspace_bytes, stream);
+  if (s) return s;
+  s = nl_fill_pairs(d_X_sorted, d_perm, d_cell_offsets, nat, cell, inv_cell, ncells, nxyz, pbc, cutoff, index_bytes,
+                    d_first, capacity, d_i, d_j, d_S, d_R, d_workspace, workspace_bytes, stream);
+  if (s) return s;
+  if (total_pairs) {
+    Layout L = layout(nat, ncells[0] * ncells[1] * ncells[2]);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (nat == 0) {
+      *total_pairs = 0;
+      return sync_read(d_workspace, st, nullptr, nullptr);
+    }
+    s = sync_read(d_workspace, st, at<long long>(d_workspace, L.totals) + 1, total_pairs);
+    if (s == NL_OK && *total_pairs > capacity) return fail(NL_ERR_CAPACITY, "pair buffers are smaller than the pair count");
+    return s;
+  }
+  return NL_OK;
+}
+
+int nl_lazy_reduce(const double* d_X_sorted, const void* d_perm, const void* d_cell_id, const void* d_cell_offsets,
+                   int64_t nat, const double cell[9], const double inv_cell[9], const int64_t ncells[3],
+                   const int64_t nxyz[3], const uint8_t pbc[3], double cutoff, int index_bytes, int reuse_records,
+                   int op, void* d_out, void* d_workspace, size_t workspace_bytes, void* stream) {
+  if (!cell || !inv_cell || !ncells || !nxyz || !pbc || !d_cell_offsets ||
+      (nat > 0 && (!d_X_sorted || !d_perm || !d_cell_id || !d_out)))
+    return fail(NL_ERR_ARG, "null argument");
+  if (op != NL_REDUCE_COUNT && op != NL_REDUCE_INV_R6) return fail(NL_ERR_ARG, "unknown reduction");
+  Layout L;
+  int64_t nct;
+  int s = check_common(nat, ncells, nxyz, index_bytes, d_workspace, workspace_bytes, L, nct);
+  if (s) return s;
+  if (nat == 0) return NL_OK;
+  const nl::Geometry g = make_geometry(cell, inv_cell, ncells, nxyz, pbc, cutoff, nat);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaSuccess;
+  if (!reuse_records) e = cudaMemsetAsync(d_workspace, 0, 128, st);
+  if (e != cudaSuccess) return cuda_fail(e, "memset workspace");
+  const int sms = num_sms();
+  auto run = [&](auto tag) {
+    using TI = decltype(tag);
+    if (!reuse_records)
+      nl::launch_prepare<TI>(g, d_X_sorted, static_cast<const TI*>(d_cell_id), static_cast<const TI*>(d_perm), g.nat,
+                             at<float4>(d_workspace, L.rec_sorted), at<unsigned>(d_workspace, L.err), sms, st);
+    nl::PairArgs<TI> a =
+        pair_args<TI>(g, static_cast<const TI*>(d_cell_offsets), static_cast<const TI*>(d_perm), d_X_sorted, d_workspace, L);
+    if (op == NL_REDUCE_COUNT) {
+      a.counts = static_cast<int*>(d_out);
+      nl::launch_pairs<TI>(nl::kModeCount, a, sms, st);
+    } else {
+      a.per_atom = static_cast<double*>(d_out);
+      nl::launch_pairs<TI>(nl::kModeLazyR6, a, sms, st);
+    }
+  };
+  if (index_bytes == 4)
+    run(int32_t(0));
+  else
+    run(int64_t(0));
+  e = cudaGetLastError();
+  return e == cudaSuccess ? NL_OK : cuda_fail(e, "launch lazy kernel");
+}
+
+int nl_sync_status(void* d_workspace, void* stream) {
+  if (!d_workspace) return fail(NL_ERR_ARG, "null workspace");
+  return sync_read(d_workspace, static_cast<cudaStream_t>(stream), nullptr, nullptr);
+}
+
+int nl_last_recheck_count(void* d_workspace, void* stream, int64_t* rechecks) {
+  if (!d_workspace || !rechecks) return fail(NL_ERR_ARG, "null argument");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  long long* h = pinned_scratch();
+  if (!h) return fail(NL_ERR_NOMEM, "cannot allocate pinned host scratch");
+  cudaError_t e = cudaMemcpyAsync(h, static_cast<char*>(d_workspace) + 64, sizeof(long long), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "read statistics");
+  *rechecks = h[0];
+  return NL_OK;
+}
+
+}  // extern "C"

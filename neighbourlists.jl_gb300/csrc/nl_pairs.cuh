@@ -1,0 +1,31 @@
+// Launchers of the pair-traversal kernels (nl_pairs.cu).
+#pragma once
+#include "nl_common.cuh"
+
+namespace nl {
+
+enum PairMode : int { kModeCount = 0, kModeFill = 1, kModeLazyR6 = 2 };
+
+template <typename TI>
+struct PairArgs {
+  Geometry g;
+  const TI* cell_offsets;   // 1-based CSR over cells (ncells+1)
+  const TI* perm;           // sorted slot -> 1-based original index
+  const double* Xs;         // sorted positions (nat x 3)
+  const float4* rec;        // sorted FP32 records
+  const TI* first;          // fill: 1-based pair offsets per original atom (nat+1)
+  int* counts;              // count: pairs per original atom
+  TI* oi;                   // fill outputs (1-based i, j; S as 3 x TI; R as 3 x double)
+  TI* oj;
+  TI* oS;
+  double* oR;               // may be null (R not wanted)
+  long long capacity;       // pairs the output buffers hold
+  double* per_atom;         // lazy: per-atom reduction
+  unsigned long long* stats;  // [0] += FP64 rechecks
+  unsigned* err;
+};
+
+template <typename TI>
+void launch_pairs(int mode, const PairArgs<TI>& a, int num_sms, cudaStream_t st);
+
+}  // namespace nl

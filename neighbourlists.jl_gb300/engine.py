@@ -1,0 +1,103 @@
+"""Reusable materialised neighbour-list pipeline (one system, fixed size).
+
+Keeps the workspace, the SortedCellList arrays and the pair buffers resident
+on the device between calls, as an MD loop that rebuilds its list every step
+would.  One call of ``launch`` enqueues the whole path (nl_neighbour_list:
+binning, sort, count, scan, fill) on a stream with no host synchronisation;
+``run`` additionally checks the pair count and grows the buffers when needed.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import check, lib
+from .api import PairList, _index_bytes, _pbc, _ptr, _stream_handle, _tdtype, analyze_cell
+
+_D = C.POINTER(C.c_double)
+_I64 = C.POINTER(C.c_int64)
+_U8 = C.POINTER(C.c_uint8)
+
+
+class NeighbourListEngine:
+    def __init__(self, nat: int, cell, cutoff: float, pbc, int_type=torch.int32, with_R: bool = True,
+                 capacity: Optional[int] = None, device="cuda"):
+        self.nat = int(nat)
+        self.cell = np.asarray(cell, dtype=np.float64).reshape(3, 3).copy()
+        self.cutoff = float(cutoff)
+        self.pbc = _pbc(pbc)
+        self.ib = _index_bytes(int_type)
+        self.ti = _tdtype(self.ib)
+        self.with_R = with_R
+        self.device = torch.device(device)
+        self.plan = analyze_cell(self.cell, self.cutoff, int_type)
+        p = self.plan
+        nbytes = int(lib().nl_workspace_bytes(self.nat, p.ncells_total))
+        self.ws = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
+        self.perm = torch.empty(self.nat, dtype=self.ti, device=self.device)
+        self.Xs = torch.empty((self.nat, 3), dtype=torch.float64, device=self.device)
+        self.cid = torch.empty(self.nat, dtype=self.ti, device=self.device)
+        self.offs = torch.empty(p.ncells_total + 1, dtype=self.ti, device=self.device)
+        self.first = torch.empty(self.nat + 1, dtype=self.ti, device=self.device)
+        self.capacity = 0
+        self.i = self.j = self.S = self.R = None
+        if capacity is None:
+            # expected pairs for a homogeneous system plus headroom
+            vol = abs(float(np.linalg.det(self.cell)))
+            rho = self.nat / vol if vol > 0 else 0.0
+            capacity = int(1.15 * self.nat * rho * 4.0 / 3.0 * np.pi * self.cutoff ** 3) + 1024
+        self._alloc(capacity)
+        self.last_total = None
+
+    def _alloc(self, capacity: int):
+        capacity = max(int(capacity), 1)
+        self.capacity = capacity
+        self.i = torch.empty(capacity, dtype=self.ti, device=self.device)
+        self.j = torch.empty(capacity, dtype=self.ti, device=self.device)
+        self.S = torch.empty((capacity, 3), dtype=self.ti, device=self.device)
+        self.R = torch.empty((capacity, 3), dtype=torch.float64, device=self.device) if self.with_R else None
+
+    def _call(self, X: torch.Tensor, total_ptr, stream):
+        p = self.plan
+        return lib().nl_neighbour_list(
+            _ptr(X), self.nat, p.cell_cm.ctypes.data_as(_D), p.inv_cm.ctypes.data_as(_D), p.ncells.ctypes.data_as(_I64),
+            p.nxyz.ctypes.data_as(_I64), self.pbc.ctypes.data_as(_U8), self.cutoff, self.ib, _ptr(self.perm),
+            _ptr(self.Xs), _ptr(self.cid), C.c_void_p(self.offs.data_ptr()), C.c_void_p(self.first.data_ptr()),
+            self.capacity, _ptr(self.i), _ptr(self.j), _ptr(self.S), _ptr(self.R), total_ptr, _ptr(self.ws),
+            self.ws.numel(), _stream_handle(stream))
+
+    def launch(self, X: torch.Tensor, stream=None) -> None:
+        """Enqueue the whole pipeline; no host synchronisation."""
+        check(self._call(X, None, stream))
+
+    def run(self, X: torch.Tensor, stream=None) -> int:
+        """Run the pipeline, check errors, grow the pair buffers if needed."""
+        total = C.c_int64(0)
+        s = self._call(X, C.byref(total), stream)
+        if s == _lib.NL_ERR_CAPACITY:
+            self._alloc(int(total.value * 1.1) + 1024)
+            s = self._call(X, C.byref(total), stream)
+        check(s)
+        self.last_total = int(total.value)
+        return self.last_total
+
+    def sync_status(self, stream=None) -> None:
+        check(lib().nl_sync_status(_ptr(self.ws), _stream_handle(stream)))
+
+    def total_pairs(self) -> int:
+        """Pair count of the last launch (reads the device; synchronises)."""
+        return int(self.first[-1].item()) - 1
+
+    def rechecks(self, stream=None) -> int:
+        r = C.c_int64(0)
+        check(lib().nl_last_recheck_count(_ptr(self.ws), _stream_handle(stream), C.byref(r)))
+        return int(r.value)
+
+    def pairlist(self, X: torch.Tensor) -> PairList:
+        P = self.total_pairs()
+        return PairList(X, self.cell.copy(), self.cutoff, self.i[:P], self.j[:P], self.S[:P], self.first,
+                        self.R[:P] if self.R is not None else None)

@@ -1,0 +1,233 @@
+"""GPU parity: the sm_103a kernels, called through the C ABI, against the CPU
+oracle on the same seeded inputs.  i, j, S, first and the bits of R must be
+identical -- not only after canonical (i, j, S) ordering but in the
+reference's own output order -- and the SortedCellList arrays must equal the
+reference's stable sort.  Cases follow the reference's tests
+(test/test_sortbased.jl, test/test_gpu.jl, test/test_unified_api.jl,
+test/test_atoms_base.jl) and the benchmark configurations."""
+import numpy as np
+import pytest
+import torch
+
+import configs as cf
+import golden_io
+
+pytestmark = pytest.mark.gpu
+
+
+def to_np(t):
+    return t.detach().cpu().numpy()
+
+
+def assert_identical(g, o, with_R=True):
+    assert int(g.i.shape[0]) == o.npairs
+    np.testing.assert_array_equal(to_np(g.first).astype(np.int64), o.first)
+    np.testing.assert_array_equal(to_np(g.i).astype(np.int64), o.i)
+    np.testing.assert_array_equal(to_np(g.j).astype(np.int64), o.j)
+    np.testing.assert_array_equal(to_np(g.S).astype(np.int64), o.S)
+    if with_R:
+        gr = to_np(g.R)
+        assert np.array_equal(gr.view(np.int64), o.R.view(np.int64)), "R bits differ"
+
+
+def run_both(nlpkg, orc, X, rc, cell, pbc, int_type=torch.int32):
+    g = nlpkg.neighbour_list(torch.from_numpy(np.ascontiguousarray(X, dtype=np.float64)).cuda(), rc, cell, pbc,
+                             int_type=int_type)
+    o = orc.neighbour_list(X, rc, cell, pbc, nthreads=8)
+    return g, o
+
+
+def test_golden_fixtures_bit_identical(nlpkg):
+    for case in golden_io.load_all():
+        g = nlpkg.neighbour_list(torch.from_numpy(case["X"]).cuda(), case["cutoff"], case["cell"], case["pbc"])
+        assert int(g.i.shape[0]) == case["i"].shape[0], case["name"]
+        for key in ("i", "j", "S", "first"):
+            assert np.array_equal(to_np(getattr(g, key)).astype(np.int64), case[key]), (case["name"], key)
+        assert np.array_equal(to_np(g.R).view(np.int64), case["R"].view(np.int64)), case["name"]
+
+
+@pytest.mark.parametrize("seed", range(5))
+def test_random_configs(nlpkg, orc, seed):
+    N = 50 + 37 * seed
+    X, C, L = cf.rand_config(N, seed=100 + seed)
+    assert_identical(*run_both(nlpkg, orc, X, 0.33 * L, C, (True, True, True)))
+
+
+@pytest.mark.parametrize("pbc", cf.ALL_PBC)
+def test_all_pbc(nlpkg, orc, pbc):
+    X, C, L = cf.rand_config(50, seed=7)
+    assert_identical(*run_both(nlpkg, orc, X, 0.33 * L, C, pbc))
+    X, C, L = cf.rand_config(3000, seed=8)
+    assert_identical(*run_both(nlpkg, orc, X, 5.0, C, pbc))
+
+
+def test_triclinic_elongated_large_cutoff(nlpkg, orc):
+    X, C = cf.rand_config_triclinic(80, seed=3)
+    assert_identical(*run_both(nlpkg, orc, X, 3.0, C, (True, True, True)))
+    C2 = np.diag([5.0, 5.0, 20.0])
+    X2 = np.random.default_rng(4).random((80, 3)) @ C2
+    assert_identical(*run_both(nlpkg, orc, X2, 3.0, C2, (True, True, True)))
+    X3, C3, L3 = cf.rand_config(30, seed=5)
+    assert_identical(*run_both(nlpkg, orc, X3, 0.6 * L3, C3, (True, True, True)))
+
+
+@pytest.mark.parametrize("N", [500, 1000, 2000])
+def test_sizes(nlpkg, orc, N):
+    X, C, L = cf.rand_config(N, seed=N)
+    assert_identical(*run_both(nlpkg, orc, X, 0.25 * L, C, (True, True, True)))
+
+
+def test_high_density(nlpkg, orc):
+    """test/test_gpu.jl:78-86: 200 atoms in a 5 A box, cutoff 2."""
+    X = np.random.default_rng(6).random((200, 3)) * 5.0
+    assert_identical(*run_both(nlpkg, orc, X, 2.0, np.diag([5.0] * 3), (True, True, True)))
+
+
+def test_dense_big_cells(nlpkg, orc):
+    """Cells with hundreds / thousands of atoms (the shared-memory and
+    ordered-scan fix-up paths of the sort)."""
+    X = np.random.default_rng(7).random((3000, 3)) * 4.0
+    assert_identical(*run_both(nlpkg, orc, X, 1.1, np.diag([4.0] * 3), (True, True, True)))
+    X = np.random.default_rng(8).random((9000, 3)) * 2.0
+    assert_identical(*run_both(nlpkg, orc, X, 0.3, np.diag([2.0] * 3), (True, False, True)))
+
+
+def test_edge_cases(nlpkg, orc):
+    C = np.diag([10.0] * 3)
+    for X, pbc in (([[5.0, 5.0, 5.0]], (1, 1, 1)), ([[5.0, 5.0, 5.0], [5.0, 5.0, 6.0]], (1, 1, 1)),
+                   ([[1.0, 1.0, 1.0], [8.0, 8.0, 8.0]], (0, 0, 0))):
+        g, o = run_both(nlpkg, orc, np.array(X), 3.0, C, pbc)
+        assert_identical(g, o)
+    g = nlpkg.neighbour_list(torch.zeros((0, 3), dtype=torch.float64, device="cuda"), 3.0, C, (1, 1, 1))
+    assert nlpkg.npairs(g) == 0 and to_np(g.first).tolist() == [1]
+    clist = nlpkg.build_cell_list(torch.zeros((0, 3), dtype=torch.float64, device="cuda"), 3.0, C, (1, 1, 1))
+    assert set(to_np(clist.cell_offsets).tolist()) == {1}
+    two = nlpkg.neighbour_list(torch.tensor([[5.0, 5.0, 5.0], [5.0, 5.0, 6.0]], dtype=torch.float64).cuda(), 3.0, C,
+                               (1, 1, 1))
+    assert nlpkg.max_neighbours(two) == 1
+
+
+def test_kats(nlpkg):
+    X, C = cf.fcc_cubic(3.61, (4, 2, 3))
+    g = nlpkg.neighbour_list(torch.from_numpy(X).cuda(), 3.5, C, (True, True, True))
+    assert all(nlpkg.num_neighbours(g, i) == 12 for i in range(1, nlpkg.nsites(g) + 1))
+    X = np.array([[0.0, 0.0, 0.0], [0.0, 0.0, 2.0], [0.0, 10.0, 0.0]])
+    g = nlpkg.neighbour_list(torch.from_numpy(X).cuda(), 5.0, np.diag(X.max(0) - X.min(0) + 1), (False,) * 3)
+    j, R, S = nlpkg.neighbours(g, 1)
+    assert to_np(j).tolist() == [2] and to_np(R).tolist() == [[0.0, 0.0, 2.0]]
+    j, R, S = nlpkg.neighbours(g, 3)
+    assert len(j) == 0
+
+
+def test_diamond_multi_image(nlpkg, orc):
+    X, C = cf.diamond_primitive()
+    g, o = run_both(nlpkg, orc, X, 6.0, C, (True, True, True))
+    assert o.npairs == 92
+    assert_identical(g, o)
+
+
+def test_issue6_outside_box(nlpkg, orc):
+    for pbc in cf.ALL_PBC:
+        X, C, L = cf.rand_config(600, seed=31)
+        idx = np.arange(1, 601)
+        sh = np.stack([(idx % 3) - 1, ((idx + 1) % 3) - 1, ((idx + 2) % 3) - 1], 1).astype(float)
+        Xp = X + sh * L * np.array([1.0 if p else 0.0 for p in pbc])
+        assert_identical(*run_both(nlpkg, orc, Xp, 5.0, C, pbc))
+    # far outside on open axes (clamped cells, FP64-only "exact" atoms)
+    X, C, L = cf.rand_config(500, seed=32)
+    X[::7, 2] -= 3 * L
+    X[::11, 0] += 2.5 * L
+    assert_identical(*run_both(nlpkg, orc, X, 5.0, C, (False, True, False)))
+
+
+def test_config_10k(nlpkg, orc):
+    X, C, _ = cf.rand_config(10000, seed=0)
+    g, o = run_both(nlpkg, orc, X, 5.0, C, (True, True, True))
+    assert abs(o.npairs - 261800) < 3000
+    assert_identical(g, o)
+
+
+def test_config_fcc_sheared_32k(nlpkg, orc):
+    X, C, pbc = cf.fcc_sheared(n=20, seed=0)
+    assert_identical(*run_both(nlpkg, orc, X, 5.0, C, pbc))
+
+
+def test_int64_and_no_R(nlpkg, orc):
+    X, C = cf.rand_config_triclinic(700, seed=13)
+    g, o = run_both(nlpkg, orc, X, 3.3, C, (True, False, True), int_type=torch.int64)
+    assert g.i.dtype == torch.int64 and g.S.dtype == torch.int64
+    assert_identical(g, o)
+    g2 = nlpkg.neighbour_list(torch.from_numpy(X).cuda(), 3.3, C, (True, False, True), with_R=False)
+    assert g2.R is None
+    assert_identical(g2, o, with_R=False)
+
+
+def test_sorted_cell_list_fields(nlpkg, orc):
+    X, C, pbc = cf.fcc_sheared(n=6, seed=4)
+    for it in (torch.int32, torch.int64):
+        g = nlpkg.build_cell_list(torch.from_numpy(X).cuda(), 5.0, C, pbc, int_type=it)
+        o = orc.build_cell_list(X, 5.0, C, pbc)
+        np.testing.assert_array_equal(to_np(g.perm).astype(np.int64), o.perm)
+        np.testing.assert_array_equal(to_np(g.cell_id).astype(np.int64), o.cell_id)
+        np.testing.assert_array_equal(to_np(g.cell_offsets).astype(np.int64), o.cell_offsets)
+        assert np.array_equal(to_np(g.X).view(np.int64), o.X.view(np.int64))
+
+
+def test_materialize_foreign_cell_list(nlpkg, orc):
+    """A SortedCellList produced elsewhere (here by the oracle, i.e. the
+    reference's CPU build) is materialised by the GPU kernels."""
+    X, C, L = cf.rand_config(4000, seed=14)
+    o = orc.build_cell_list(X, 5.0, C, (True, True, False))
+    plan = nlpkg.analyze_cell(C, 5.0)
+    dev = "cuda"
+    clist = nlpkg.SortedCellList(
+        torch.from_numpy(o.X).to(dev), torch.from_numpy(o.X_orig).to(dev),
+        torch.from_numpy(o.perm.astype(np.int32)).to(dev), torch.from_numpy(o.cell_id.astype(np.int32)).to(dev),
+        torch.from_numpy(o.cell_offsets.astype(np.int32)).to(dev), C, plan.inv_cell, (True, True, False), 5.0,
+        plan.ncells, plan.ncells_total, plan, None, False)
+    g = nlpkg.materialize_pairlist(clist)
+    assert_identical(g, orc.neighbour_list(X, 5.0, C, (True, True, False)))
+
+
+def test_lazy_reductions(nlpkg, orc):
+    X, C, L = cf.rand_config(5000, seed=15)
+    Xd = torch.from_numpy(X).cuda()
+    clist = nlpkg.neighbour_list(Xd, 5.0, C, (True, True, True), lazy=True)
+    assert isinstance(clist, nlpkg.SortedCellList)
+    o = orc.neighbour_list(X, 5.0, C, (True, True, True))
+    cnt = to_np(nlpkg.lazy_reduce(clist, "count"))
+    np.testing.assert_array_equal(cnt, np.diff(o.first))
+    s = to_np(nlpkg.lazy_reduce(clist, "inv_r6"))
+    ref = orc.lazy_sum_r6(orc.build_cell_list(X, 5.0, C, (True, True, True)))
+    # per-atom sums follow the reference's traversal order: bit-identical
+    assert np.array_equal(s.view(np.int64), ref.view(np.int64))
+    assert nlpkg.count_neighbours(clist, 17) == int(np.diff(o.first)[16])
+    js, Rs, Ss = nlpkg.neighbours(clist, 17)
+    a, b = o.first[16] - 1, o.first[17] - 1
+    np.testing.assert_array_equal(to_np(js).astype(np.int64), o.j[a:b])
+    seen = []
+    nlpkg.for_each_neighbour(lambda j, R, S: seen.append(j), clist, 17)
+    assert seen == o.j[a:b].tolist()
+
+
+def test_engine_reuse_and_capacity(nlpkg, orc):
+    X, C, L = cf.rand_config(20000, seed=16)
+    Xd = torch.from_numpy(X).cuda()
+    eng = nlpkg.NeighbourListEngine(20000, C, 5.0, (True, True, True), capacity=1000)
+    total = eng.run(Xd)  # grows the buffers after NL_ERR_CAPACITY
+    o = orc.neighbour_list(X, 5.0, C, (True, True, True), nthreads=8)
+    assert total == o.npairs and eng.capacity >= total
+    assert_identical(eng.pairlist(Xd), o)
+    for _ in range(3):
+        eng.launch(Xd)
+    eng.sync_status()
+    assert_identical(eng.pairlist(Xd), o)
+    assert eng.rechecks() >= 0
+
+
+def test_bad_position_reported(nlpkg):
+    X = torch.rand((100, 3), dtype=torch.float64, device="cuda") * 10
+    X[5, 1] = float("nan")
+    with pytest.raises(nlpkg.NLError) as e:
+        nlpkg.neighbour_list(X, 3.0, np.diag([10.0] * 3), (True, True, True))
+    assert e.value.status == 6

@@ -1,0 +1,183 @@
+"""Host-side checks of the C ABI that need no GPU: the library loads and
+exports every declared symbol, the restated cell analysis is bit-equal to the
+oracle's, argument errors map to the reference's error behaviour, and the
+FP32 screen band is wide enough (numpy emulation of the kernel arithmetic)."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+import configs as cf
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "nlgpu.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:int|size_t|const char\*)\s+(nl_\w+)\s*\(", src, re.M)))
+
+
+def test_library_exports_every_declared_symbol(nlpkg):
+    L = nlpkg.lib()
+    decl = declared_symbols()
+    assert len(decl) >= 12
+    for name in decl:
+        assert hasattr(L, name), name
+    assert sorted(decl) == sorted(nlpkg._lib.EXPORTED)
+    assert L.nl_version() >= 1
+
+
+CELLS = [
+    np.diag([58.48, 58.48, 58.48]),
+    cf.triclinic_cell(),
+    cf.fcc_sheared(n=20)[1],
+    cf.diamond_primitive()[1],
+    np.array([[7.0, 0.3, -0.2], [1.1, 6.5, 0.4], [-0.7, 2.2, 9.1]]),
+    np.array([[3.0, 0.0, 0.0], [2.9, 0.5, 0.0], [0.1, 0.2, 40.0]]),
+]
+
+
+@pytest.mark.parametrize("k", range(len(CELLS)))
+@pytest.mark.parametrize("rc", [1.7, 3.0, 5.0, 6.0])
+def test_analyze_cell_bit_equal_to_oracle(nlpkg, orc, k, rc):
+    cell = CELLS[k]
+    p = nlpkg.analyze_cell(cell, rc)
+    o = orc.analyze_cell(cell, rc)
+    assert np.array_equal(p.inv_cell.view(np.int64), o.inv_cell.view(np.int64))
+    assert np.array_equal(p.lens.view(np.int64), o.lens.view(np.int64))
+    assert np.array_equal(p.ncells, o.ncells)
+    assert np.array_equal(p.nxyz, o.nxyz)
+    assert p.ncells_total == int(np.prod(o.ncells))
+
+
+def test_too_many_cells_error(nlpkg):
+    cell = np.diag([1e6, 1e6, 1e6])
+    with pytest.raises(nlpkg.NLError) as e:
+        nlpkg.analyze_cell(cell, 1e-3)
+    assert e.value.status == 2 and "very large" in str(e.value)
+    # Int64 lifts the index-type limit but not the engine's 2^31-2 cell limit
+    with pytest.raises(nlpkg.NLError):
+        nlpkg.analyze_cell(cell, 1e-3, int_type="Int64")
+
+
+def test_argument_errors_before_any_device_work(nlpkg):
+    L = nlpkg.lib()
+    D = C.POINTER(C.c_double)
+    I64 = C.POINTER(C.c_int64)
+    U8 = C.POINTER(C.c_uint8)
+    cell = np.ascontiguousarray(np.diag([10.0, 10.0, 10.0]).T).reshape(9)
+    inv = np.ascontiguousarray(np.diag([0.1, 0.1, 0.1]).T).reshape(9)
+    ns = np.array([3, 3, 3], dtype=np.int64)
+    pbc = np.ones(3, dtype=np.uint8)
+    # workspace too small
+    st = L.nl_build_cell_list(C.c_void_p(8), 10, cell.ctypes.data_as(D), inv.ctypes.data_as(D),
+                              ns.ctypes.data_as(I64), pbc.ctypes.data_as(U8), 3.0, 4, C.c_void_p(8), C.c_void_p(8),
+                              C.c_void_p(8), C.c_void_p(8), C.c_void_p(8), 16, None)
+    assert st == 3
+    # bad index type
+    plan = nlpkg._lib.CellPlan()
+    assert L.nl_analyze_cell(cell.ctypes.data_as(D), 3.0, 2, C.byref(plan)) == 1
+    assert L.nl_analyze_cell(cell.ctypes.data_as(D), -1.0, 4, C.byref(plan)) == 1
+    assert L.nl_workspace_bytes(-1, 1) == 0
+    assert L.nl_workspace_bytes(1000, 27) > 1000 * 48
+
+
+# ---------------------------------------------------------------- screen --
+def _f32(x):
+    return np.asarray(x, dtype=np.float64).astype(np.float32)
+
+
+def _fma32(a, b, c):
+    return _f32(np.asarray(a, np.float64) * np.asarray(b, np.float64) + np.asarray(c, np.float64))
+
+
+def _bin(inv_cm, ns, pbc, X):
+    """Restates the kernel binning: returns cell (1-based), winding, t (FP64)."""
+    f = np.stack([(inv_cm[3 * k] * X[:, 0] + inv_cm[3 * k + 1] * X[:, 1]) + inv_cm[3 * k + 2] * X[:, 2]
+                  for k in range(3)], 1)
+    y = f * ns
+    c0 = np.floor(y + 1.0).astype(np.int64)
+    c = np.empty_like(c0)
+    w = np.zeros_like(c0)
+    for k in range(3):
+        if pbc[k]:
+            w[:, k] = np.floor_divide(c0[:, k] - 1, ns[k])
+            c[:, k] = c0[:, k] - w[:, k] * ns[k]
+        else:
+            c[:, k] = np.clip(c0[:, k], 1, ns[k])
+    m = (c - 1) + w * ns
+    return c, w, y - m
+
+
+def _screen_errors(cell, rc, pbc, X, pairs_per=400, seed=0):
+    """Max |r2_fp32 - r2_fp64| over random candidate pairs, and the band."""
+    from neighbourlists_gb300 import analyze_cell  # noqa: F401  (package loaded by fixture)
+
+    rng = np.random.default_rng(seed)
+    cm = np.ascontiguousarray(cell.T).reshape(9)
+    import oracle as orc_mod
+
+    info = orc_mod.analyze_cell(cell, rc)
+    inv_cm = np.ascontiguousarray(info.inv_cell.T).reshape(9)
+    ns = info.ncells
+    nx = info.nxyz
+    c, w, t = _bin(inv_cm, ns, pbc, X)
+    b = np.array([[cell[k, r] / ns[k] for r in range(3)] for k in range(3)])  # b[k, r]
+    b32 = _f32(b)
+    t32 = _f32(t)
+    u = np.stack([_fma32(t32[:, 2], b32[2, r], _fma32(t32[:, 1], b32[1, r], _f32(t32[:, 0] * b32[0, r])))
+                  for r in range(3)], 1)
+    ok = (np.abs(t) <= 2.0).all(1)
+    n = X.shape[0]
+    worst = 0.0
+    for _ in range(pairs_per):
+        i, j = rng.integers(0, n, 2)
+        if not (ok[i] and ok[j]):
+            continue
+        d = c[j] - c[i]
+        # bring d into the stencil like the traversal does (wrapped cell offsets)
+        for k in range(3):
+            if pbc[k]:
+                d[k] = ((d[k] + ns[k] // 2) % ns[k]) - ns[k] // 2
+        if np.any(np.abs(d) > nx):
+            continue
+        sl = np.zeros(3, dtype=np.int64)
+        for k in range(3):
+            if pbc[k]:
+                sl[k] = np.floor_divide(c[i, k] + d[k] - 1, ns[k])
+        S = sl + w[i] - w[j]
+        R64 = (X[j] - X[i]) + np.array([(cell[0, r] * S[0] + cell[1, r] * S[1]) + cell[2, r] * S[2] for r in range(3)])
+        r2_64 = (R64[0] * R64[0] + R64[1] * R64[1]) + R64[2] * R64[2]
+        if r2_64 > 4 * rc * rc:
+            continue
+        fd = d.astype(np.float32)
+        off = np.array([_fma32(fd[2], b32[2, r], _fma32(fd[1], b32[1, r], _f32(fd[0] * b32[0, r]))) for r in range(3)])
+        v = _f32(u[j] + off)
+        R32 = _f32(v - u[i])
+        r2_32 = _fma32(R32[2], R32[2], _fma32(R32[1], R32[1], _f32(R32[0] * R32[0])))
+        err = abs(float(r2_32) - r2_64) if r2_64 < rc * rc * 1.1 else 0.0
+        worst = max(worst, err)
+    return worst
+
+
+@pytest.mark.parametrize("case", ["cubic", "triclinic", "sheared", "outside"])
+def test_screen_band_bounds_fp32_error(nlpkg, orc, case):
+    rng = np.random.default_rng(5)
+    if case == "cubic":
+        X, cell, _ = cf.rand_config(3000, seed=1)
+        pbc, rc = (True, True, True), 5.0
+    elif case == "triclinic":
+        X, cell = cf.rand_config_triclinic(2000, seed=2)
+        pbc, rc = (True, False, True), 3.0
+    elif case == "sheared":
+        X, cell, pbc = cf.fcc_sheared(n=6, seed=3)
+        rc = 5.0
+    else:  # atoms on cell corners and shifted by whole periods
+        X, cell, L = cf.rand_config(2000, seed=4)
+        X = np.round(X / (L / 11)) * (L / 11) + rng.integers(-2, 3, X.shape) * L
+        pbc, rc = (True, True, True), 5.0
+    band = nlpkg.analyze_cell(cell, rc).band
+    worst = _screen_errors(cell, rc, pbc, X, pairs_per=6000)
+    assert worst <= band / 2, (worst, band)
