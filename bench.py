@@ -40,10 +40,10 @@ ALGO_BYTES_PER_ATOM = 24  # positions read
 ALGO_BYTES_PER_PAIR = 44  # i 4 + j 4 + S 12 + R 24 written
 
 
-def workload():
+def workload(n_atoms=N_ATOMS):
     import configs as cf
 
-    X, C, L = cf.uniform_system(N_ATOMS, DENSITY, SEED)
+    X, C, L = cf.uniform_system(n_atoms, DENSITY, SEED)
     return X, C, (True, True, True)
 
 
@@ -190,9 +190,10 @@ def run_gpu(args):
     dev = torch.device("cuda", local if world > 1 else 0)
     torch.cuda.set_device(dev)
     nl = graft.load_package()
-    X, C, pbc = workload()
+    n_atoms = args.atoms
+    X, C, pbc = workload(n_atoms)
     Xd = torch.from_numpy(X).to(dev)
-    eng = nl.NeighbourListEngine(N_ATOMS, C, CUTOFF, pbc, device=dev)
+    eng = nl.NeighbourListEngine(n_atoms, C, CUTOFF, pbc, device=dev)
     total = eng.run(Xd)
     stream = torch.cuda.current_stream(dev)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
@@ -240,7 +241,7 @@ def run_gpu(args):
     D, I64, U8 = Cc.POINTER(Cc.c_double), Cc.POINTER(Cc.c_int64), Cc.POINTER(Cc.c_uint8)
 
     def fill():
-        _lib.check(L.nl_fill_pairs(_ptr(eng.Xs), _ptr(eng.perm), Cc.c_void_p(eng.offs.data_ptr()), N_ATOMS,
+        _lib.check(L.nl_fill_pairs(_ptr(eng.Xs), _ptr(eng.perm), Cc.c_void_p(eng.offs.data_ptr()), n_atoms,
                                    p.cell_cm.ctypes.data_as(D), p.inv_cm.ctypes.data_as(D),
                                    p.ncells.ctypes.data_as(I64), p.nxyz.ctypes.data_as(I64),
                                    eng.pbc.ctypes.data_as(U8), CUTOFF, eng.ib, Cc.c_void_p(eng.first.data_ptr()),
@@ -260,13 +261,56 @@ def run_gpu(args):
     fill_ms = sum(s.elapsed_time(e) for s, e in zip(fs, fe)) / args.steps
 
     # ---- end to end through the public API with host buffers
+    e2e = None
+    if not args.no_e2e:
+        e2e = measure_e2e(eng, X, Xd, total, stream, dev, args)
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peaks()
+    algo_bytes = ALGO_BYTES_PER_ATOM * n_atoms + ALGO_BYTES_PER_PAIR * total
+    achieved = algo_bytes / (fill_ms * 1e-3) / 1e9
+    traffic = ncu_traffic() if n_atoms == N_ATOMS else None
+    cpu = cpu_baseline(X, C, pbc) if not args.no_cpu_baseline else None
+    value = world * total / (step_ms * 1e-3)
+    if e2e is not None:
+        e2e["value"] = world * total / (e2e["ms_per_step"] * 1e-3)
+    line = {
+        "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD if n_atoms == N_ATOMS else f"uniform {n_atoms} atoms (profiling size)",
+                   "atoms": n_atoms, "pairs": int(total), "cutoff": CUTOFF,
+                   "density": DENSITY, "pbc": "TTT", "index_type": "Int32", "with_R": True,
+                   "l2": "flushed before every timed step (256 MiB write, untimed)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "kernel": "k_pairs<fill>",
+                     "algorithmic_bytes": algo_bytes, "kernel_ms": fill_ms,
+                     "traffic": (traffic or {}).get("dram_bytes_per_launch")},
+        "step_roofline_frac": algo_bytes / (step_ms * 1e-3) / 1e9 / peak,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "clocks": clk.summary(),
+        "gpu_launches": 8 * args.steps,
+        "rechecks": rechecks,
+        "recheck_band_rel": float(p.band / (CUTOFF * CUTOFF)),
+    }
+    print(json.dumps(line))
+
+
+def measure_e2e(eng, X, Xd, total, stream, dev, args):
+    """Same metric through the engine with HOST buffers: pinned positions
+    copied in, every output array (first, i, j, S, R) copied back, per step."""
+    import torch
+
+    n_atoms = X.shape[0]
     ti = eng.ti
     hX = torch.from_numpy(X).pin_memory()
     h_i = torch.empty(total, dtype=ti).pin_memory()
     h_j = torch.empty(total, dtype=ti).pin_memory()
     h_S = torch.empty((total, 3), dtype=ti).pin_memory()
     h_R = torch.empty((total, 3), dtype=torch.float64).pin_memory()
-    h_f = torch.empty(N_ATOMS + 1, dtype=ti).pin_memory()
+    h_f = torch.empty(n_atoms + 1, dtype=ti).pin_memory()
     Xdev = torch.empty_like(Xd)
 
     def e2e_step():
@@ -293,37 +337,8 @@ def run_gpu(args):
     h2d = X.nbytes
     d2h = (h_i.numel() * h_i.element_size() + h_j.numel() * h_j.element_size() + h_S.numel() * h_S.element_size()
            + h_R.numel() * 8 + h_f.numel() * h_f.element_size())
-
-    if rank != 0:
-        return
-    peak, peak_kind = measured_peaks()
-    algo_bytes = ALGO_BYTES_PER_ATOM * N_ATOMS + ALGO_BYTES_PER_PAIR * total
-    achieved = algo_bytes / (fill_ms * 1e-3) / 1e9
-    traffic = ncu_traffic()
-    cpu = cpu_baseline(X, C, pbc) if not args.no_cpu_baseline else None
-    value = world * total / (step_ms * 1e-3)
-    line = {
-        "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "atoms": N_ATOMS, "pairs": int(total), "cutoff": CUTOFF,
-                   "density": DENSITY, "pbc": "TTT", "index_type": "Int32", "with_R": True,
-                   "l2": "flushed before every timed step (256 MiB write, untimed)",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_kind": peak_kind, "kernel": "k_pairs<fill>",
-                     "algorithmic_bytes": algo_bytes, "kernel_ms": fill_ms,
-                     "traffic": (traffic or {}).get("dram_bytes_per_launch")},
-        "step_roofline_frac": algo_bytes / (step_ms * 1e-3) / 1e9 / peak,
-        "cpu_baseline": cpu,
-        "e2e": {"value": world * total / (e2e_ms * 1e-3), "unit": "pairs/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
-        "clocks": clk.summary(),
-        "gpu_launches": 8 * args.steps,
-        "rechecks": rechecks,
-        "recheck_band_rel": float(p.band / (CUTOFF * CUTOFF)),
-    }
-    print(json.dumps(line))
+    return {"value": None, "unit": "pairs/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+            "ms_per_step": e2e_ms}
 
 
 def main():
@@ -333,6 +348,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--atoms", type=int, default=N_ATOMS, help="system size (profiling runs use a smaller one)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

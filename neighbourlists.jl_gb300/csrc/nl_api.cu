@@ -14,6 +14,7 @@
 #include <cstring>
 #include <string>
 
+#include "nl_api_internal.h"
 #include "nl_build.cuh"
 #include "nl_common.cuh"
 #include "nl_pairs.cuh"
@@ -80,9 +81,11 @@ void lengths(const double* C, double* lens) {
 // ------------------------------------------------------- FP32 screen band --
 // The kernel screens candidates with r2_32 = |v_j - u_i|^2 where u (per atom)
 // and v = u_j + d.b (per candidate) are FP32 sums of FP64-exact cell-local
-// coordinates t (|t_k| <= kMaxT for non-exact atoms) times the bin vectors b_k.
+// coordinates t (|t_k| <= kMaxT for non-exact atoms) times the bin vectors b_k;
+// t carries at most 2^-24 (|t| + 2) of rounding (FP32 rounding of the FP64
+// value, or the double-float binning's final FP32 operations).
 // Per Cartesian component r the FP32 error of R is at most
-//   e_r = 2^-24 * 1.01 * ((11 T + 2) B_r + 4 O_r + |R_r|) + e64,
+//   e_r = 2^-24 * 1.01 * ((11 T + 6) B_r + 4 O_r + |R_r|) + e64,
 //   B_r = sum_k |b_kr|,  O_r = sum_k nxyz_k |b_kr|,
 // where e64 = 2^-29 (1 + cond(C)) sum_k |b_k| bounds the difference between
 // the reference's FP64 R and the exact R of the FP64 t values for atoms with
@@ -118,7 +121,7 @@ double screen_band(const double* C, const double* inv, const int64_t* ns, const 
   const double T = nl::kMaxT;
   double delta = 0;
   for (int r = 0; r < 3; ++r) {
-    const double e = eps * 1.01 * ((11 * T + 2) * B[r] + 4 * O[r] + rc) + e64;
+    const double e = eps * 1.01 * ((11 * T + 6) * B[r] + 4 * O[r] + rc) + e64;
     delta += 2 * rc * e + e * e;
   }
   delta += 3.03 * eps * rc * rc + std::ldexp(1.0, -51) * rc * rc;
@@ -163,7 +166,7 @@ struct Layout {
   // [err 64 | stats 64] [pairs zero region: counters 64 | st_pairs]
   // [build zero region: counters 64 | st_cells | cell_count] [arrays...]
   size_t err, stats, pcount, st_pairs, pend, bcount, st_cells, cell_count, bend;
-  size_t totals, cell_start, cid, ticket, rec, tmp, rec_sorted, counts, big_list, end;
+  size_t totals, cell_start, cid, ticket, rec, tmp, rec_sorted, scell, counts, masks, big_list, end;
 };
 
 Layout layout(int64_t nat, int64_t ncells) {
@@ -199,8 +202,12 @@ Layout layout(int64_t nat, int64_t ncells) {
   o += up(sizeof(int) * n);
   L.rec_sorted = o;
   o += up(sizeof(float4) * n);
+  L.scell = o;
+  o += up(sizeof(int) * n);
   L.counts = o;
   o += up(sizeof(int) * n);
+  L.masks = o;
+  o += up(sizeof(unsigned) * size_t(nl::kMaskWords) * n);
   L.big_list = o;
   o += up(sizeof(int) * size_t(ncells < (int64_t)n ? ncells : (int64_t)n));
   L.end = o;
@@ -244,8 +251,8 @@ int check_common(int64_t nat, const int64_t* ncells, const int64_t* nxyz, int in
   for (int k = 0; k < 3; ++k) {
     if (ncells[k] < 1) return fail(NL_ERR_ARG, "ncells must be >= 1");
     prod *= (long double)ncells[k];
-    if (nxyz && (nxyz[k] < 0 || nxyz[k] > 64))
-      return fail(NL_ERR_ARG, "stencil half-width nxyz must be in [0, 64] (cutoff at most 64 cell widths)");
+    if (nxyz && (nxyz[k] < 0 || nxyz[k] > 62))
+      return fail(NL_ERR_ARG, "stencil half-width nxyz must be in [0, 62] (cutoff at most 62 cell widths)");
   }
   if (prod > 2147483646.0L) return fail(NL_ERR_TOO_MANY_CELLS, "more than 2^31-2 cells");
   if (index_bytes == 4 && prod > 2147483647.0L)
@@ -280,6 +287,14 @@ nl::Geometry make_geometry(const double* cell, const double* inv, const int64_t*
   if (double(fhi) < hi) fhi = std::nextafter(fhi, INFINITY);
   g.lo = lo > 0 ? flo : -1.0f;  // lo <= 0: every candidate is rechecked
   g.hi = fhi;
+  // inv[m,k] * ns[k] as a float pair for the double-float binning
+  for (int k = 0; k < 3; ++k)
+    for (int m = 0; m < 3; ++m) {
+      const double q = inv[3 * k + m] * double(ns[k]);
+      const float qh = float(q);
+      g.qh[3 * k + m] = qh;
+      g.ql[3 * k + m] = float(q - double(qh));
+    }
   return g;
 }
 
@@ -334,7 +349,7 @@ int build_impl(const double* X, int64_t nat, const nl::Geometry& g, TI* perm, do
                       at<long long>(ws, L.totals), err, st);
   nl::launch_scatter(int(nat), cid, ticket, cell_start, at<int>(ws, L.tmp), sms, st);
   nl::launch_fix<TI>(int(nat), at<int>(ws, L.tmp), cid, cell_start, X, rec, perm, cell_id, Xs,
-                     at<float4>(ws, L.rec_sorted), at<int>(ws, L.big_list), bcount + 1, sms, st);
+                     at<float4>(ws, L.rec_sorted), at<int>(ws, L.scell), at<int>(ws, L.big_list), bcount + 1, sms, st);
   e = cudaGetLastError();
   return e == cudaSuccess ? NL_OK : cuda_fail(e, "launch build kernels");
 }
@@ -349,6 +364,8 @@ nl::PairArgs<TI> pair_args(const nl::Geometry& g, const TI* cell_offsets, const 
   a.perm = perm;
   a.Xs = Xs;
   a.rec = at<float4>(ws, L.rec_sorted);
+  a.scell = at<int>(ws, L.scell);
+  a.masks = at<unsigned>(ws, L.masks);
   a.stats = at<unsigned long long>(ws, L.stats);
   a.err = at<unsigned>(ws, L.err);
   return a;
@@ -369,7 +386,8 @@ int count_impl(const nl::Geometry& g, const double* Xs, const TI* perm, const TI
     return e == cudaSuccess ? NL_OK : cuda_fail(e, "empty system");
   }
   if (!reuse)
-    nl::launch_prepare<TI>(g, Xs, cell_id, perm, g.nat, at<float4>(ws, L.rec_sorted), at<unsigned>(ws, L.err), sms, st);
+    nl::launch_prepare<TI>(g, Xs, cell_id, perm, g.nat, at<float4>(ws, L.rec_sorted), at<int>(ws, L.scell),
+                           at<unsigned>(ws, L.err), sms, st);
   nl::PairArgs<TI> a = pair_args<TI>(g, cell_offsets, perm, Xs, ws, L);
   a.counts = at<int>(ws, L.counts);
   nl::launch_pairs<TI>(nl::kModeCount, a, sms, st);
@@ -396,6 +414,11 @@ int fill_impl(const nl::Geometry& g, const double* Xs, const TI* perm, const TI*
 }
 
 }  // namespace
+
+namespace nl {
+int report(int status, const std::string& msg) { return fail(status, msg); }
+int status_from_device_flags(unsigned flags) { return status_from_flags(flags); }
+}  // namespace nl
 
 // ======================================================================
 extern "C" {
@@ -555,7 +578,8 @@ int nl_lazy_reduce(const double* d_X_sorted, const void* d_perm, const void* d_c
     using TI = decltype(tag);
     if (!reuse_records)
       nl::launch_prepare<TI>(g, d_X_sorted, static_cast<const TI*>(d_cell_id), static_cast<const TI*>(d_perm), g.nat,
-                             at<float4>(d_workspace, L.rec_sorted), at<unsigned>(d_workspace, L.err), sms, st);
+                             at<float4>(d_workspace, L.rec_sorted), at<int>(d_workspace, L.scell),
+                             at<unsigned>(d_workspace, L.err), sms, st);
     nl::PairArgs<TI> a =
         pair_args<TI>(g, static_cast<const TI*>(d_cell_offsets), static_cast<const TI*>(d_perm), d_X_sorted, d_workspace, L);
     if (op == NL_REDUCE_COUNT) {

@@ -40,7 +40,7 @@ __global__ void __launch_bounds__(256) k_bin(Geometry g, const double* __restric
     if (valid) {
       const double x0 = X[3LL * i + 0], x1 = X[3LL * i + 1], x2 = X[3LL * i + 2];
       Binned bn;
-      if (!bin_position(g, x0, x1, x2, bn)) atomicOr(err, kFlagBadPosition);
+      if (!bin_fast(g, x0, x1, x2, bn) && !bin_position(g, x0, x1, x2, bn)) atomicOr(err, kFlagBadPosition);
       c = linear_cell(g, bn.c[0], bn.c[1], bn.c[2]);
       rec[i] = make_record(g, bn);
       cid[i] = c;
@@ -67,9 +67,10 @@ template <typename TI>
 __device__ __forceinline__ void write_sorted(long long dst, int i, int c, const double* __restrict__ X,
                                              const float4* __restrict__ rec, TI* __restrict__ perm,
                                              TI* __restrict__ cell_id, double* __restrict__ Xs,
-                                             float4* __restrict__ rec_sorted) {
+                                             float4* __restrict__ rec_sorted, int* __restrict__ scell) {
   perm[dst] = TI(i) + 1;
   cell_id[dst] = TI(c) + 1;
+  scell[dst] = c;
   Xs[3 * dst + 0] = X[3LL * i + 0];
   Xs[3 * dst + 1] = X[3LL * i + 1];
   Xs[3 * dst + 2] = X[3LL * i + 2];
@@ -85,8 +86,8 @@ __global__ void __launch_bounds__(256) k_fix(int nat, const int* __restrict__ tm
                                              const int* __restrict__ cell_start, const double* __restrict__ X,
                                              const float4* __restrict__ rec, TI* __restrict__ perm,
                                              TI* __restrict__ cell_id, double* __restrict__ Xs,
-                                             float4* __restrict__ rec_sorted, int* __restrict__ big_list,
-                                             int* __restrict__ big_count) {
+                                             float4* __restrict__ rec_sorted, int* __restrict__ scell,
+                                             int* __restrict__ big_list, int* __restrict__ big_count) {
   for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < nat; s += (long long)gridDim.x * blockDim.x) {
     const int i = tmp[s];
     const int c = cid[i];
@@ -98,7 +99,7 @@ __global__ void __launch_bounds__(256) k_fix(int nat, const int* __restrict__ tm
     }
     int rank = 0;
     for (int t = start; t < start + k; ++t) rank += tmp[t] < i;
-    write_sorted<TI>(start + rank, i, c, X, rec, perm, cell_id, Xs, rec_sorted);
+    write_sorted<TI>(start + rank, i, c, X, rec, perm, cell_id, Xs, rec_sorted, scell);
   }
 }
 
@@ -114,6 +115,7 @@ __global__ void __launch_bounds__(kFixBigThreads) k_fix_big(int nat, const int* 
                                                             const float4* __restrict__ rec, TI* __restrict__ perm,
                                                             TI* __restrict__ cell_id, double* __restrict__ Xs,
                                                             float4* __restrict__ rec_sorted,
+                                                            int* __restrict__ scell,
                                                             const int* __restrict__ big_list,
                                                             const int* __restrict__ big_count) {
   __shared__ int s[kBigSort];
@@ -144,7 +146,7 @@ __global__ void __launch_bounds__(kFixBigThreads) k_fix_big(int nat, const int* 
           __syncthreads();
         }
       for (int t = threadIdx.x; t < k; t += blockDim.x)
-        write_sorted<TI>(start + t, s[t], c, X, rec, perm, cell_id, Xs, rec_sorted);
+        write_sorted<TI>(start + t, s[t], c, X, rec, perm, cell_id, Xs, rec_sorted, scell);
       __syncthreads();
     } else {
       int run = 0;
@@ -161,7 +163,7 @@ __global__ void __launch_bounds__(kFixBigThreads) k_fix_big(int nat, const int* 
           tot += s_warp[w];
         }
         if (f) write_sorted<TI>(start + run + before + __popc(m & lanemask_lt()), i, c, X, rec, perm, cell_id, Xs,
-                                rec_sorted);
+                                rec_sorted, scell);
         run += tot;
         __syncthreads();
       }
@@ -176,13 +178,16 @@ __global__ void __launch_bounds__(kFixBigThreads) k_fix_big(int nat, const int* 
 template <typename TI>
 __global__ void __launch_bounds__(256) k_prepare(Geometry g, const double* __restrict__ Xs,
                                                  const TI* __restrict__ cell_id, const TI* __restrict__ perm, int nat,
-                                                 float4* __restrict__ rec_sorted, unsigned* __restrict__ err) {
+                                                 float4* __restrict__ rec_sorted, int* __restrict__ scell,
+                                                 unsigned* __restrict__ err) {
   for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < nat; s += (long long)gridDim.x * blockDim.x) {
     Binned bn;
-    if (!bin_position(g, Xs[3 * s + 0], Xs[3 * s + 1], Xs[3 * s + 2], bn)) atomicOr(err, kFlagBadPosition);
+    const double x0 = Xs[3 * s + 0], x1 = Xs[3 * s + 1], x2 = Xs[3 * s + 2];
+    if (!bin_fast(g, x0, x1, x2, bn) && !bin_position(g, x0, x1, x2, bn)) atomicOr(err, kFlagBadPosition);
     rec_sorted[s] = make_record(g, bn);
-    if ((long long)cell_id[s] != (long long)linear_cell(g, bn.c[0], bn.c[1], bn.c[2]) + 1)
-      atomicOr(err, kFlagInconsistent);
+    const int c = linear_cell(g, bn.c[0], bn.c[1], bn.c[2]);
+    scell[s] = c;
+    if ((long long)cell_id[s] != (long long)c + 1) atomicOr(err, kFlagInconsistent);
     if ((long long)perm[s] < 1 || (long long)perm[s] > nat) atomicOr(err, kFlagInconsistent);
   }
 }
@@ -208,20 +213,20 @@ void launch_scatter(int nat, const int* cid, const int* ticket, const int* cell_
 
 template <typename TI>
 void launch_fix(int nat, const int* tmp, const int* cid, const int* cell_start, const double* X, const float4* rec,
-                TI* perm, TI* cell_id, double* Xs, float4* rec_sorted, int* big_list, int* big_count, int num_sms,
-                cudaStream_t st) {
+                TI* perm, TI* cell_id, double* Xs, float4* rec_sorted, int* scell, int* big_list, int* big_count,
+                int num_sms, cudaStream_t st) {
   if (nat <= 0) return;
   k_fix<TI><<<grid_for(nat, 256, num_sms * 8), 256, 0, st>>>(nat, tmp, cid, cell_start, X, rec, perm, cell_id, Xs,
-                                                             rec_sorted, big_list, big_count);
+                                                             rec_sorted, scell, big_list, big_count);
   k_fix_big<TI><<<num_sms, kFixBigThreads, 0, st>>>(nat, tmp, cid, cell_start, X, rec, perm, cell_id, Xs, rec_sorted,
-                                                     big_list, big_count);
+                                                     scell, big_list, big_count);
 }
 
 template <typename TI>
 void launch_prepare(const Geometry& g, const double* Xs, const TI* cell_id, const TI* perm, int nat,
-                    float4* rec_sorted, unsigned* err, int num_sms, cudaStream_t st) {
+                    float4* rec_sorted, int* scell, unsigned* err, int num_sms, cudaStream_t st) {
   if (nat <= 0) return;
-  k_prepare<TI><<<grid_for(nat, 256, num_sms * 8), 256, 0, st>>>(g, Xs, cell_id, perm, nat, rec_sorted, err);
+  k_prepare<TI><<<grid_for(nat, 256, num_sms * 8), 256, 0, st>>>(g, Xs, cell_id, perm, nat, rec_sorted, scell, err);
 }
 
 template <typename TI>
@@ -233,9 +238,9 @@ void launch_scan(const int* in, long long n, TI* out1, int* out0, unsigned long 
 
 #define NL_INST(TI)                                                                                                  \
   template void launch_fix<TI>(int, const int*, const int*, const int*, const double*, const float4*, TI*, TI*,     \
-                               double*, float4*, int*, int*, int, cudaStream_t);                                    \
-  template void launch_prepare<TI>(const Geometry&, const double*, const TI*, const TI*, int, float4*, unsigned*, \
-                                   int, cudaStream_t);                                                              \
+                               double*, float4*, int*, int*, int*, int, cudaStream_t);                              \
+  template void launch_prepare<TI>(const Geometry&, const double*, const TI*, const TI*, int, float4*, int*,     \
+                                   unsigned*, int, cudaStream_t);                                                   \
   template void launch_scan<TI>(const int*, long long, TI*, int*, unsigned long long*, int*, long long*, unsigned*, \
                                 cudaStream_t);
 NL_INST(int32_t)

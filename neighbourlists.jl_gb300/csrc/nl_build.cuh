@@ -15,11 +15,11 @@ void launch_scatter(int nat, const int* cid, const int* ticket, const int* cell_
                     cudaStream_t st);
 template <typename TI>
 void launch_fix(int nat, const int* tmp, const int* cid, const int* cell_start, const double* X, const float4* rec,
-                TI* perm, TI* cell_id, double* Xs, float4* rec_sorted, int* big_list, int* big_count, int num_sms,
-                cudaStream_t st);
+                TI* perm, TI* cell_id, double* Xs, float4* rec_sorted, int* scell, int* big_list, int* big_count,
+                int num_sms, cudaStream_t st);
 template <typename TI>
 void launch_prepare(const Geometry& g, const double* Xs, const TI* cell_id, const TI* perm, int nat,
-                    float4* rec_sorted, unsigned* err, int num_sms, cudaStream_t st);
+                    float4* rec_sorted, int* scell, unsigned* err, int num_sms, cudaStream_t st);
 template <typename TI>
 void launch_scan(const int* in, long long n, TI* out1, int* out0, unsigned long long* status, int* counter,
                  long long* total, unsigned* err, cudaStream_t st);

@@ -47,6 +47,7 @@ struct Geometry {
   int nat;
   float b[9];      // bin vectors: b[3k + r] = float(C[k,r] / ns[k])
   float lo, hi;    // FP32 screen: accept r2 < lo, reject r2 > hi, else FP64 recheck
+  float qh[9], ql[9];  // inv[m,k]*ns[k] as a float pair, index 3k + m (fast binning)
 };
 
 // Per-atom record in cell-sorted order: float4 (u.x, u.y, u.z, meta) where
@@ -113,7 +114,7 @@ __device__ __forceinline__ int wrap_shift(int i, int n, int pbc, int& s) {
 struct Binned {
   int c[3];      // 1-based wrapped/clamped cell index
   int w[3];      // winding
-  double t[3];   // cell-local coordinate (cell units)
+  float t[3];    // cell-local coordinate (cell units), rounded to FP32
   bool exact;    // route through the FP64 path
 };
 
@@ -136,15 +137,94 @@ __device__ __forceinline__ bool bin_position(const Geometry& g, double x0, doubl
     o.w[k] = s;
     long long m = (long long)(c - 1) + (long long)s * (long long)g.ns[k];
     double t = dsub(y, double(m));
-    o.t[k] = t;
+    o.t[k] = __double2float_rn(t);
     if (!(fabs(t) <= kMaxT) || !(fabs(y) <= kMaxY) || s > 127 || s < -127) exact = true;
   }
   o.exact = exact;
   return ok;
 }
 
+// ---------------------------------------------------------- fast binning --
+// Splits a double exactly into three floats (x = a + b + c) with integer
+// operations.  Returns false for zero-free values outside [2^-60, 2^60] and
+// for non-finite values (the caller then bins in FP64).
+__device__ __forceinline__ bool split3(double x, float& a, float& b, float& c) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+  if ((bits << 1) == 0ull) {
+    a = b = c = 0.f;
+    return true;
+  }
+  const int e = int((bits >> 52) & 0x7FF);
+  if (e < 1023 - 60 || e > 1023 + 60) return false;
+  const unsigned sign = unsigned(bits >> 32) & 0x80000000u;
+  const unsigned long long m = (bits & ((1ull << 52) - 1)) | (1ull << 52);
+  const unsigned hi24 = unsigned(m >> 29);            // top 24 bits, leading bit at 23
+  const unsigned r = unsigned(m & ((1u << 29) - 1));  // remaining 29 bits
+  a = __uint_as_float(sign | (unsigned(e - 896) << 23) | (hi24 & 0x7FFFFFu));
+  const float rf = __uint2float_rn(r);                // r rounded to 24 bits
+  const int low = int(r - __float2uint_rn(rf));       // |low| <= 16, exact
+  const float scale = __uint_as_float(unsigned(e - 1075 + 127) << 23);  // 2^(e-1075)
+  b = __uint_as_float(__float_as_uint(rf * scale) | sign);
+  c = __uint_as_float(__float_as_uint(float(low) * scale) ^ sign);
+  return true;
+}
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// Cell index, winding and cell-local coordinate from a double-float
+// evaluation of y_k = sum_m inv[m,k] x_m n_k on the FP32 pipe (relative error
+// about 2^-44).  The cell index equals the reference's floor(frac*n + 1)
+// whenever the fractional part of y + 1 is farther than `margin` from an
+// integer; otherwise (and for out-of-range values) this returns false and the
+// caller bins with the reference's FP64 arithmetic (bin_position).
+__device__ __forceinline__ bool bin_fast(const Geometry& g, double x0, double x1, double x2, Binned& o) {
+  float a[3], b[3], c[3];
+  if (!split3(x0, a[0], b[0], c[0]) || !split3(x1, a[1], b[1], c[1]) || !split3(x2, a[2], b[2], c[2])) return false;
+  bool exact = false;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    float p[3], low = 0.f, mag = 0.f;
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      const float qh = g.qh[3 * k + m], ql = g.ql[3 * k + m];
+      p[m] = qh * a[m];
+      const float e = fmaf(qh, a[m], -p[m]);
+      const float sm = fmaf(qh, b[m], fmaf(ql, a[m], fmaf(qh, c[m], ql * b[m])));
+      low += e + sm;
+      mag += fabsf(p[m]);
+    }
+    float s01, e01, s012, e012;
+    two_sum(p[0], p[1], s01, e01);
+    two_sum(s01, p[2], s012, e012);
+    low += e01 + e012;
+    const float yh = s012 + low;             // y = yh + yl (fast two-sum)
+    const float yl = low - (yh - s012);
+    if (!(fabsf(yh) < 4194304.f)) return false;  // 2^22
+    const float z = yh + 1.0f;                   // exact for |yh| < 2^22
+    const float fl = floorf(z);
+    const float fr = (z - fl) + yl;              // fractional part of y + 1
+    const float margin = fmaxf(9.5367431640625e-07f, mag * 3.637978807091713e-12f);  // 2^-20, 2^-38 * sum|terms|
+    if (!(fr > margin && fr < 1.0f - margin)) return false;
+    const int c0 = int(fl);
+    int s;
+    const int cc = wrap_shift(c0, g.ns[k], g.pbc[k], s);
+    o.c[k] = cc;
+    o.w[k] = s;
+    const int mm = (cc - 1) + s * g.ns[k];
+    const float t = (yh - float(mm)) + yl;
+    o.t[k] = t;
+    if (!(fabsf(t) <= float(kMaxT)) || !(fabsf(yh) <= float(kMaxY)) || s > 127 || s < -127) exact = true;
+  }
+  o.exact = exact;
+  return true;
+}
+
 __device__ __forceinline__ float4 make_record(const Geometry& g, const Binned& bn) {
-  float t0 = __double2float_rn(bn.t[0]), t1 = __double2float_rn(bn.t[1]), t2 = __double2float_rn(bn.t[2]);
+  float t0 = bn.t[0], t1 = bn.t[1], t2 = bn.t[2];
   float4 r;
   r.x = fmaf(t2, g.b[6], fmaf(t1, g.b[3], t0 * g.b[0]));
   r.y = fmaf(t2, g.b[7], fmaf(t1, g.b[4], t0 * g.b[1]));
@@ -152,6 +232,9 @@ __device__ __forceinline__ float4 make_record(const Geometry& g, const Binned& b
   bool ex = bn.exact;
   unsigned meta = pack_meta(ex ? 0 : bn.w[0], ex ? 0 : bn.w[1], ex ? 0 : bn.w[2], ex);
   r.w = __uint_as_float(meta);
+  if (ex) {  // an exact atom screens as NaN: every FP32 comparison fails
+    r.x = r.y = r.z = __int_as_float(0x7fc00000);
+  }
   return r;
 }
 

@@ -12,11 +12,12 @@
 // the same (2n+1)^3 stencil (the reference computes it per atom from the same
 // cell), so the warp stages the stencil's candidate atoms once in shared
 // memory as FP32 positions relative to the home cell's corner, then screens
-// every home atom against them with one candidate per lane.
+// home atoms against them: each lane loads one candidate and tests it against
+// kGroup home atoms at once.
 //
 // Precision: the screen runs in FP32 on cell-local offsets.  Geometry.lo/hi
-// bracket cutoff^2 by a band that provably exceeds the FP32 error (see the
-// host-side screen_band); only candidates inside the band, or involving an
+// bracket cutoff^2 by a band that provably exceeds the FP32 error (host-side
+// screen_band in nl_api.cu); only candidates inside the band, or involving an
 // "exact" atom, are decided in FP64 with the reference arithmetic
 // R = (xj - xi) + C'S, r2 = dot(R,R), r2 < cutoff^2.  The accepted pair set is
 // therefore identical to the reference's.
@@ -30,23 +31,35 @@
 
 namespace nl {
 
-constexpr int kPairWarps = 4;   // warps per block
-constexpr int kChunk = 192;     // staged candidates per warp and pass
-constexpr int kQ = 64;          // pair queue per warp
+#ifndef NL_PAIR_MIN_BLOCKS
+#define NL_PAIR_MIN_BLOCKS 7
+#endif
+#ifndef NL_PAIR_GROUP
+#define NL_PAIR_GROUP 2
+#endif
+#ifndef NL_PAIR_CHUNK
+#define NL_PAIR_CHUNK 192
+#endif
+constexpr int kPairWarps = 4;                    // warps per block
+constexpr int kMinBlocks = NL_PAIR_MIN_BLOCKS;   // resident blocks per SM the register budget targets
+constexpr int kChunk = NL_PAIR_CHUNK;            // staged candidates per warp and pass
+constexpr int kGroup = NL_PAIR_GROUP;            // home atoms screened per candidate load
+constexpr int kRing = 64;       // pair queue (ring) per warp
 constexpr int kCsR = 2;         // C'S table covers |S_k| <= kCsR
 constexpr int kCsN = 2 * kCsR + 1;
+constexpr unsigned kExactBit = 1u << 24;
 
 struct __align__(16) WarpSmem {
-  float4 cv[kChunk];        // candidate: (x, y, z) relative to home corner, w = meta bits
-  int2 ci[kChunk];          // candidate: (sorted slot, packed s_loop)
+  float4 cv[kChunk];        // candidate: (x, y, z) relative to home corner; w = packed S base | exact bit
+  int cslot[kChunk];        // candidate: sorted slot
   double hx[32][3];         // home batch: FP64 positions
+  long long hnext[32];      // home batch: next output slot (fill) / running count (count)
   double hacc[32];          // home batch: lazy accumulators
-  long long hbase[32];      // home batch: first[orig] - 1
-  long long qslot[kQ];      // queue: output slot
-  double qval[32];          // queue: lazy values
+  long long rslot[kRing];   // queue: output slot
+  int rent[kRing];          // queue: (home atom << 16) | candidate
+  double rval[32];          // queue: lazy values
   int horig[32];            // home batch: original index (0-based)
-  unsigned hmeta[32];       // home batch: meta bits
-  int q[kQ];                // queue: (home atom << 16) | candidate
+  unsigned hmeta[32];       // home batch: packed windings | exact bit
 };
 
 __device__ __forceinline__ unsigned lt_mask() {
@@ -60,124 +73,217 @@ __device__ __forceinline__ int clampi(T v, int hi) {
   return v < T(0) ? 0 : (v > T(hi) ? hi : int(v));
 }
 
-__device__ __forceinline__ int pack3(int a, int b, int c) {
-  return int((unsigned(a) & 0xFFu) | ((unsigned(b) & 0xFFu) << 8) | ((unsigned(c) & 0xFFu) << 16));
+__device__ __forceinline__ unsigned pack3(int a, int b, int c) {
+  return (unsigned(a) & 0xFFu) | ((unsigned(b) & 0xFFu) << 8) | ((unsigned(c) & 0xFFu) << 16);
 }
-__device__ __forceinline__ int unpack3(int p, int k) { return int(int8_t((unsigned(p) >> (8 * k)) & 0xFFu)); }
+__device__ __forceinline__ int unpack3(unsigned p, int k) { return int(int8_t((p >> (8 * k)) & 0xFFu)); }
 
-// R = (xj - xi) + C'S with the reference's operation order.  For S == 0 the
-// sum reduces to (xj - xi) + (+-0): that is xj - xi unless the difference is
-// itself a zero, where the IEEE sign rule for adding two zeros applies.
+// RN(d + z) where z is +-0: d itself unless d is a zero, in which case the
+// IEEE sum of two zeros is -0 only if both are -0.  Integer operations only.
+__device__ __forceinline__ double add_signed_zero(double d, double z) {
+  const long long bd = __double_as_longlong(d);
+  return (bd << 1) != 0 ? d : __longlong_as_double(bd & __double_as_longlong(z));
+}
+
+// R = (xj - xi) + C'S with the reference's operation order.  The three sums
+// with C'S are only issued when the warp holds a pair with S != 0 (for S == 0
+// C'S is a vector of signed zeros and the sum is exact, see add_signed_zero).
 __device__ __forceinline__ void pair_R(const Geometry& g, const double* cs_tab, const double* xi, const double* xj,
-                                       int S0, int S1, int S2, double* R) {
-  const double d0 = dsub(xj[0], xi[0]), d1 = dsub(xj[1], xi[1]), d2 = dsub(xj[2], xi[2]);
-  if ((S0 | S1 | S2) == 0) {
-    const double* z = cs_tab + 3 * ((kCsN * kCsN + kCsN + 1) * kCsR);  // entry S = (0,0,0)
-    R[0] = d0 != 0.0 ? d0 : __longlong_as_double(__double_as_longlong(d0) & __double_as_longlong(z[0]));
-    R[1] = d1 != 0.0 ? d1 : __longlong_as_double(__double_as_longlong(d1) & __double_as_longlong(z[1]));
-    R[2] = d2 != 0.0 ? d2 : __longlong_as_double(__double_as_longlong(d2) & __double_as_longlong(z[2]));
-    return;
+                                       int S0, int S1, int S2, bool active, double* R) {
+  R[0] = dsub(xj[0], xi[0]);
+  R[1] = dsub(xj[1], xi[1]);
+  R[2] = dsub(xj[2], xi[2]);
+  const bool nz = active && (S0 | S1 | S2) != 0;
+  if (__any_sync(0xffffffffu, nz)) {
+    if (nz) {
+      double c0, c1, c2;
+      if (abs(S0) <= kCsR && abs(S1) <= kCsR && abs(S2) <= kCsR) {
+        const double* t = cs_tab + 3 * ((S0 + kCsR) + kCsN * ((S1 + kCsR) + kCsN * (S2 + kCsR)));
+        c0 = t[0];
+        c1 = t[1];
+        c2 = t[2];
+      } else {
+        c0 = cts_k(g.C, S0, S1, S2, 0);
+        c1 = cts_k(g.C, S0, S1, S2, 1);
+        c2 = cts_k(g.C, S0, S1, S2, 2);
+      }
+      R[0] = dadd(R[0], c0);
+      R[1] = dadd(R[1], c1);
+      R[2] = dadd(R[2], c2);
+    }
   }
-  double c0, c1, c2;
-  if (abs(S0) <= kCsR && abs(S1) <= kCsR && abs(S2) <= kCsR) {
-    const double* t = cs_tab + 3 * ((S0 + kCsR) + kCsN * ((S1 + kCsR) + kCsN * (S2 + kCsR)));
-    c0 = t[0];
-    c1 = t[1];
-    c2 = t[2];
-  } else {
-    c0 = cts_k(g.C, S0, S1, S2, 0);
-    c1 = cts_k(g.C, S0, S1, S2, 1);
-    c2 = cts_k(g.C, S0, S1, S2, 2);
+  if (!nz) {
+    const double* z = cs_tab + 3 * ((kCsN * kCsN + kCsN + 1) * kCsR);  // C'(0,0,0): signed zeros
+    R[0] = add_signed_zero(R[0], z[0]);
+    R[1] = add_signed_zero(R[1], z[1]);
+    R[2] = add_signed_zero(R[2], z[2]);
   }
-  R[0] = dadd(d0, c0);
-  R[1] = dadd(d1, c1);
-  R[2] = dadd(d2, c2);
 }
 
 __device__ __forceinline__ double dot_ref(const double* R) {
   return dadd(dadd(dmul(R[0], R[0]), dmul(R[1], R[1])), dmul(R[2], R[2]));
 }
 
-// S = s_loop + wi - wj (gpu_kernels.jl:88).  Windings come from the packed
-// records unless either atom is "exact", in which case they are recomputed
-// from the FP64 positions.
-__device__ __forceinline__ void pair_S(const Geometry& g, const double* xi, const double* xj, unsigned mi,
-                                       unsigned mj, int slp, int* S) {
-  if (!meta_exact(mi) && !meta_exact(mj)) {
+// S = s_loop + wi - wj (gpu_kernels.jl:88).  A candidate word cw holds
+// pack3(s_loop - wj) for a regular candidate, or pack3(s_loop) | exact bit
+// for an exact one.  Exact pairs recompute both windings in FP64.
+__device__ __forceinline__ void pair_S(const Geometry& g, const double* xi, const double* xj, unsigned mi, unsigned cw,
+                                       int* S) {
+  if (!((mi | cw) & kExactBit)) {
 #pragma unroll
-    for (int k = 0; k < 3; ++k) S[k] = unpack3(slp, k) + meta_w(mi, k) - meta_w(mj, k);
+    for (int k = 0; k < 3; ++k) S[k] = unpack3(cw, k) + meta_w(mi, k);
   } else {
     Binned bi, bj;
     bin_position(g, xi[0], xi[1], xi[2], bi);
     bin_position(g, xj[0], xj[1], xj[2], bj);
 #pragma unroll
-    for (int k = 0; k < 3; ++k) S[k] = unpack3(slp, k) + bi.w[k] - bj.w[k];
+    for (int k = 0; k < 3; ++k) {
+      const int sl = (cw & kExactBit) ? unpack3(cw, k) : unpack3(cw, k) + bj.w[k];
+      S[k] = sl + bi.w[k] - bj.w[k];
+    }
   }
 }
 
+// Full FP64 decision of one candidate pair with the reference arithmetic.
+__device__ __forceinline__ bool exact_pair(const Geometry& g, const double* Xs, int slot_i, int slot_j, unsigned mi,
+                                           unsigned cw) {
+  double xi[3], xj[3];
+  xi[0] = Xs[3LL * slot_i + 0];
+  xi[1] = Xs[3LL * slot_i + 1];
+  xi[2] = Xs[3LL * slot_i + 2];
+  xj[0] = Xs[3LL * slot_j + 0];
+  xj[1] = Xs[3LL * slot_j + 1];
+  xj[2] = Xs[3LL * slot_j + 2];
+  int S[3];
+  pair_S(g, xi, xj, mi, cw, S);
+  double R[3];
+  R[0] = dadd(dsub(xj[0], xi[0]), cts_k(g.C, S[0], S[1], S[2], 0));
+  R[1] = dadd(dsub(xj[1], xi[1]), cts_k(g.C, S[0], S[1], S[2], 1));
+  R[2] = dadd(dsub(xj[2], xi[2]), cts_k(g.C, S[0], S[1], S[2], 2));
+  return dot_ref(R) < g.cutoff_sq;
+}
+
+// Processes n <= 32 queued pairs starting at ring position head.
 template <typename TI, int MODE>
-__device__ __forceinline__ void flush_queue(const PairArgs<TI>& A, const double* cs_tab, WarpSmem& W, int n,
-                                            int lane) {
-  if (lane < n) {
-    const int e = W.q[lane];
-    const int a = e >> 16, f = e & 0xFFFF;
-    const int slot_j = W.ci[f].x;
-    const unsigned mj = __float_as_uint(W.cv[f].w), mi = W.hmeta[a];
-    double xj[3];
+__device__ __forceinline__ void flush_ring(const PairArgs<TI>& A, const double* cs_tab, WarpSmem& W, int head, int n,
+                                           int lane) {
+  const bool act = lane < n;
+  const int rp = (head + lane) & (kRing - 1);
+  const int e = act ? W.rent[rp] : 0;
+  const int a = e >> 16, f = e & 0xFFFF;
+  const int slot_j = W.cslot[f];
+  const unsigned cw = __float_as_uint(W.cv[f].w), mi = W.hmeta[a];
+  double xj[3];
+  const double* xi = W.hx[a];
+  int S[3] = {0, 0, 0};
+  if (act) {
     xj[0] = A.Xs[3LL * slot_j + 0];
     xj[1] = A.Xs[3LL * slot_j + 1];
     xj[2] = A.Xs[3LL * slot_j + 2];
-    const double* xi = W.hx[a];
-    int S[3];
-    pair_S(A.g, xi, xj, mi, mj, W.ci[f].y, S);
-    if (MODE == kModeFill) {
-      const long long out = W.qslot[lane];
-      if (out < A.capacity) {
-        A.oi[out] = TI(W.horig[a]) + 1;
-        A.oj[out] = TI(clampi(A.perm[slot_j] - 1, A.g.nat - 1)) + 1;
-        A.oS[3 * out + 0] = TI(S[0]);
-        A.oS[3 * out + 1] = TI(S[1]);
-        A.oS[3 * out + 2] = TI(S[2]);
-        if (A.oR) {
-          double R[3];
-          pair_R(A.g, cs_tab, xi, xj, S[0], S[1], S[2], R);
-          A.oR[3 * out + 0] = R[0];
-          A.oR[3 * out + 1] = R[1];
-          A.oR[3 * out + 2] = R[2];
-        }
-      } else {
-        atomicOr(A.err, kFlagCapacity);
-      }
-    } else {  // lazy: f(R) = 1 / ((r2*r2)*r2)
-      double R[3];
-      pair_R(A.g, cs_tab, xi, xj, S[0], S[1], S[2], R);
-      const double r2 = dot_ref(R);
-      W.qval[lane] = __ddiv_rn(1.0, dmul(dmul(r2, r2), r2));
+    pair_S(A.g, xi, xj, mi, cw, S);
+  } else {
+    xj[0] = xj[1] = xj[2] = 0.0;
+  }
+  if (MODE == kModeFill) {
+    const long long out = act ? W.rslot[rp] : 0;
+    const bool wr = act && out < A.capacity;
+    if (act && !wr) atomicOr(A.err, kFlagCapacity);
+    if (wr) {
+      A.oi[out] = TI(W.horig[a]) + 1;
+      A.oj[out] = TI(clampi(A.perm[slot_j] - 1, A.g.nat - 1)) + 1;
+      A.oS[3 * out + 0] = TI(S[0]);
+      A.oS[3 * out + 1] = TI(S[1]);
+      A.oS[3 * out + 2] = TI(S[2]);
     }
+    if (A.oR) {
+      double R[3];
+      pair_R(A.g, cs_tab, xi, xj, S[0], S[1], S[2], act, R);
+      if (wr) {
+        A.oR[3 * out + 0] = R[0];
+        A.oR[3 * out + 1] = R[1];
+        A.oR[3 * out + 2] = R[2];
+      }
+    }
+  } else {  // lazy: f(R) = 1 / ((r2*r2)*r2)
+    double R[3];
+    pair_R(A.g, cs_tab, xi, xj, S[0], S[1], S[2], act, R);
+    if (act) {
+      const double r2 = dot_ref(R);
+      W.rval[lane] = __ddiv_rn(1.0, dmul(dmul(r2, r2), r2));
+    }
+    __syncwarp();
+    // accumulate in queue order: every atom's sum follows the reference's
+    // traversal order exactly
+    if (lane == 0)
+      for (int q = 0; q < n; ++q) {
+        const int aa = W.rent[(head + q) & (kRing - 1)] >> 16;
+        W.hacc[aa] = dadd(W.hacc[aa], W.rval[q]);
+      }
   }
   __syncwarp();
-  if (MODE == kModeLazyR6) {
-    // accumulate in queue order so that every atom's sum follows the
-    // reference's traversal order exactly
-    if (lane == 0)
-      for (int e = 0; e < n; ++e) {
-        const int a = W.q[e] >> 16;
-        W.hacc[a] = dadd(W.hacc[a], W.qval[e]);
-      }
-    __syncwarp();
+}
+
+// wrap_shift without a division for the common case of an index already
+// inside [1, n]
+__device__ __forceinline__ int wrap_shift_fast(int i, int n, int pbc, int& s) {
+  if (i >= 1 && i <= n) {
+    s = 0;
+    return i;
   }
+  return wrap_shift(i, n, pbc, s);
+}
+
+constexpr int kStencilTab = 512;  // stencil offsets tabulated per block up to this size
+
+// Stencil cell q of home cell (hc0, hc1, hc2): its 0-based linear index (or
+// -1 when it falls outside an open axis), packed loop shift and FP32 offset
+// d.b of its lower corner from the home corner.
+__device__ __forceinline__ int stencil_cell(const Geometry& g, const unsigned* dtab, int sx, int sy, int hc0, int hc1,
+                                            int hc2, int q, unsigned& slp, float& ox, float& oy, float& oz) {
+  int d0, d1, d2;
+  if (q < kStencilTab) {
+    const unsigned dq = dtab[q];
+    d0 = unpack3(dq, 0);
+    d1 = unpack3(dq, 1);
+    d2 = unpack3(dq, 2);
+  } else {
+    d0 = q % sx - g.nxyz[0];
+    d1 = (q / sx) % sy - g.nxyz[1];
+    d2 = q / (sx * sy) - g.nxyz[2];
+  }
+  const bool inb = (g.pbc[0] || (hc0 + d0 >= 1 && hc0 + d0 <= g.ns[0])) &&
+                   (g.pbc[1] || (hc1 + d1 >= 1 && hc1 + d1 <= g.ns[1])) &&
+                   (g.pbc[2] || (hc2 + d2 >= 1 && hc2 + d2 <= g.ns[2]));
+  if (!inb) return -1;
+  int s0, s1, s2;
+  const int c0 = wrap_shift_fast(hc0 + d0, g.ns[0], g.pbc[0], s0);
+  const int c1 = wrap_shift_fast(hc1 + d1, g.ns[1], g.pbc[1], s1);
+  const int c2 = wrap_shift_fast(hc2 + d2, g.ns[2], g.pbc[2], s2);
+  slp = pack3(s0, s1, s2);  // |s| <= 63: the host limits nxyz to 62
+  const float fd0 = float(d0), fd1 = float(d1), fd2 = float(d2);
+  ox = fmaf(fd2, g.b[6], fmaf(fd1, g.b[3], fd0 * g.b[0]));
+  oy = fmaf(fd2, g.b[7], fmaf(fd1, g.b[4], fd0 * g.b[1]));
+  oz = fmaf(fd2, g.b[8], fmaf(fd1, g.b[5], fd0 * g.b[2]));
+  return linear_cell(g, c0, c1, c2);
 }
 
 template <typename TI, int MODE>
-__global__ void __launch_bounds__(kPairWarps * 32) k_pairs(PairArgs<TI> A) {
+__global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<TI> A) {
   __shared__ WarpSmem sm[kPairWarps];
   __shared__ double cs_tab[3 * kCsN * kCsN * kCsN];
+  __shared__ unsigned dtab[kStencilTab];  // packed (d0, d1, d2) of stencil cell q
   const Geometry& g = A.g;
   for (int t = threadIdx.x; t < kCsN * kCsN * kCsN; t += blockDim.x) {
     const int s0 = t % kCsN - kCsR, s1 = (t / kCsN) % kCsN - kCsR, s2 = t / (kCsN * kCsN) - kCsR;
     cs_tab[3 * t + 0] = cts_k(g.C, s0, s1, s2, 0);
     cs_tab[3 * t + 1] = cts_k(g.C, s0, s1, s2, 1);
     cs_tab[3 * t + 2] = cts_k(g.C, s0, s1, s2, 2);
+  }
+  {
+    const int tx = 2 * g.nxyz[0] + 1, ty = 2 * g.nxyz[1] + 1;
+    const int tn = min(kStencilTab, tx * ty * (2 * g.nxyz[2] + 1));
+    for (int t = threadIdx.x; t < tn; t += blockDim.x)
+      dtab[t] = pack3(t % tx - g.nxyz[0], (t / tx) % ty - g.nxyz[1], t / (tx * ty) - g.nxyz[2]);
   }
   __syncthreads();
 
@@ -187,60 +293,53 @@ __global__ void __launch_bounds__(kPairWarps * 32) k_pairs(PairArgs<TI> A) {
   const int sx = 2 * g.nxyz[0] + 1, sy = 2 * g.nxyz[1] + 1, sz = 2 * g.nxyz[2] + 1;
   const int nst = sx * sy * sz;
   const int center = g.nxyz[0] + sx * (g.nxyz[1] + sy * g.nxyz[2]);
-  unsigned long long rechecks = 0;
+  const float lo = g.lo, hi = g.hi;
+  unsigned rechecks = 0;
 
-  for (int h = blockIdx.x * kPairWarps + warp; h < g.ncells; h += nwarps) {
-    // offsets are clamped to [0, nat] so that a malformed cell list (which the
-    // prepare pass reports as inconsistent) can never index out of bounds
-    const int hs = clampi(A.cell_offsets[h] - 1, g.nat), he = clampi(A.cell_offsets[h + 1] - 1, g.nat);
+  // Ranges of the next cell are prefetched one cell ahead: its home range and,
+  // per lane, the range of its stencil cell in the first group of 32.
+  int h = blockIdx.x * kPairWarps + warp;
+  // (0-based slot offsets, clamped to [0, nat])
+  int pf_hs = 0, pf_he = 0, pf_lo = 0, pf_hi = 0;
+  auto prefetch = [&](int hh) {
+    if (hh >= g.ncells) return;
+    pf_hs = clampi(A.cell_offsets[hh] - 1, g.nat);
+    pf_he = clampi(A.cell_offsets[hh + 1] - 1, g.nat);
+    const int c0 = hh % g.ns[0] + 1, c1 = (hh / g.ns[0]) % g.ns[1] + 1, c2 = hh / (g.ns[0] * g.ns[1]) + 1;
+    unsigned sl;
+    float a, b, c;
+    const int lin = lane < nst ? stencil_cell(g, dtab, sx, sy, c0, c1, c2, lane, sl, a, b, c) : -1;
+    pf_lo = lin >= 0 ? clampi(A.cell_offsets[lin] - 1, g.nat) : 0;
+    pf_hi = lin >= 0 ? clampi(A.cell_offsets[lin + 1] - 1, g.nat) : 0;
+  };
+  prefetch(h);
+  for (; h < g.ncells; h += nwarps) {
+    // offsets are clamped to [0, nat] so that a malformed cell list (which
+    // the prepare pass reports as inconsistent) never indexes out of bounds
+    const int hs = pf_hs, he = pf_he;
+    const int g0_lo = pf_lo, g0_hi = pf_hi;
+    prefetch(h + nwarps);  // loads in flight while this cell is processed
     if (hs >= he) continue;
     const int hc0 = h % g.ns[0] + 1, hc1 = (h / g.ns[0]) % g.ns[1] + 1, hc2 = h / (g.ns[0] * g.ns[1]) + 1;
 
-    for (int hb = hs; hb < he; hb += 32) {
+    bool skip_cell = false;
+    for (int hb = hs; hb < he && !skip_cell; hb += 32) {
       const int nb = min(32, he - hb);
       float ux = 0.f, uy = 0.f, uz = 0.f;
-      long long my_run = 0;  // pairs emitted so far by home atom hb+lane
-      if (lane < nb) {
-        const int s = hb + lane;
-        const float4 r = A.rec[s];
-        ux = r.x;
-        uy = r.y;
-        uz = r.z;
-        W.hmeta[lane] = __float_as_uint(r.w);
-        const int orig = clampi(A.perm[s] - 1, g.nat - 1);
-        W.horig[lane] = orig;
-        W.hx[lane][0] = A.Xs[3LL * s + 0];
-        W.hx[lane][1] = A.Xs[3LL * s + 1];
-        W.hx[lane][2] = A.Xs[3LL * s + 2];
-        if (MODE == kModeFill) W.hbase[lane] = (long long)A.first[orig] - 1;
-        if (MODE == kModeLazyR6) W.hacc[lane] = 0.0;
-      }
-      int qn = 0;
-      __syncwarp();
+      int head = 0, tail = 0;  // ring queue (fill / lazy)
 
       for (int gb = 0; gb < nst; gb += 32) {
-        // ---- stencil cell held by this lane
+        // ---- stencil cell held by this lane (reference order: dx fastest)
         const int q = gb + lane;
-        int cstart = 0, ccount = 0, slp = 0;
+        int cstart = 0, ccount = 0;
+        unsigned slp = 0;
         float ox = 0.f, oy = 0.f, oz = 0.f;
         if (q < nst) {
-          const int d0 = q % sx - g.nxyz[0], d1 = (q / sx) % sy - g.nxyz[1], d2 = q / (sx * sy) - g.nxyz[2];
-          const bool inb = (g.pbc[0] || (hc0 + d0 >= 1 && hc0 + d0 <= g.ns[0])) &&
-                           (g.pbc[1] || (hc1 + d1 >= 1 && hc1 + d1 <= g.ns[1])) &&
-                           (g.pbc[2] || (hc2 + d2 >= 1 && hc2 + d2 <= g.ns[2]));
-          if (inb) {
-            int s0, s1, s2;
-            const int c0 = wrap_shift(hc0 + d0, g.ns[0], g.pbc[0], s0);
-            const int c1 = wrap_shift(hc1 + d1, g.ns[1], g.pbc[1], s1);
-            const int c2 = wrap_shift(hc2 + d2, g.ns[2], g.pbc[2], s2);
-            const int lin = linear_cell(g, c0, c1, c2);
-            cstart = clampi(A.cell_offsets[lin] - 1, g.nat);
-            ccount = max(clampi(A.cell_offsets[lin + 1] - 1, g.nat) - cstart, 0);
-            slp = pack3(s0, s1, s2);
-            const float fd0 = float(d0), fd1 = float(d1), fd2 = float(d2);
-            ox = fmaf(fd2, g.b[6], fmaf(fd1, g.b[3], fd0 * g.b[0]));
-            oy = fmaf(fd2, g.b[7], fmaf(fd1, g.b[4], fd0 * g.b[1]));
-            oz = fmaf(fd2, g.b[8], fmaf(fd1, g.b[5], fd0 * g.b[2]));
+          const int lin = stencil_cell(g, dtab, sx, sy, hc0, hc1, hc2, q, slp, ox, oy, oz);
+          if (lin >= 0) {
+            cstart = gb == 0 ? g0_lo : clampi(A.cell_offsets[lin] - 1, g.nat);
+            const int cend = gb == 0 ? g0_hi : clampi(A.cell_offsets[lin + 1] - 1, g.nat);
+            ccount = max(cend - cstart, 0);
           }
         }
         int incl = ccount;
@@ -250,18 +349,49 @@ __global__ void __launch_bounds__(kPairWarps * 32) k_pairs(PairArgs<TI> A) {
           if (lane >= o) incl += v;
         }
         const int tg = __shfl_sync(0xffffffffu, incl, 31);
-        // flattened index of the home atoms inside this group (center cell)
-        const int cl = center - gb;
+        // cells whose candidates fit the acceptance masks: the count pass
+        // records them and the fill pass leaves them to k_emit
+        const bool masked = A.masks != nullptr && nst <= 32 && tg <= 32 * kMaskWords;
+        if (MODE == kModeFill && masked) {
+          skip_cell = true;
+          break;
+        }
+        const int cl = center - gb;  // home cell (center of the stencil) in this group?
         const int center_excl = (cl >= 0 && cl < 32) ? __shfl_sync(0xffffffffu, incl - ccount, cl & 31) : -1;
 
-        for (int cb = 0; cb < tg; cb += kChunk) {
+        for (int cb = 0; cb < tg || (gb == 0 && cb == 0); cb += kChunk) {
           const int nch = min(kChunk, tg - cb);
-          if (MODE != kModeCount && qn > 0) {
-            flush_queue<TI, MODE>(A, cs_tab, W, qn, lane);
-            qn = 0;
+          if (MODE != kModeCount && tail > head) {  // queued pairs refer to the previous chunk
+            flush_ring<TI, MODE>(A, cs_tab, W, head, tail - head, lane);
+            head = tail;
           }
           __syncwarp();
-          // ---- stage the chunk
+          if (gb == 0 && cb == 0) {
+            // home batch
+            if (lane < nb) {
+              const int s = hb + lane;
+              const float4 r = A.rec[s];  // exact atoms carry NaN coordinates
+              ux = r.x;
+              uy = r.y;
+              uz = r.z;
+              W.hmeta[lane] = __float_as_uint(r.w);
+              const int orig = clampi(A.perm[s] - 1, g.nat - 1);
+              W.horig[lane] = orig;
+              if (MODE != kModeCount) {
+                W.hx[lane][0] = A.Xs[3LL * s + 0];
+                W.hx[lane][1] = A.Xs[3LL * s + 1];
+                W.hx[lane][2] = A.Xs[3LL * s + 2];
+              }
+              W.hnext[lane] = MODE == kModeFill ? (long long)A.first[orig] - 1 : 0;
+              if (MODE == kModeLazyR6) W.hacc[lane] = 0.0;
+            }
+          }
+          if (nch <= 0) {
+            __syncwarp();
+            continue;
+          }
+          // ---- stage the chunk: home-relative FP32 positions, packed S base;
+          // exact candidates stay NaN, padding up to whole rounds is +inf
           for (int f0 = 0; f0 < nch; f0 += 32) {
             const int f = f0 + lane;
             const int gf = cb + min(f, nch - 1);
@@ -274,86 +404,133 @@ __global__ void __launch_bounds__(kPairWarps * 32) k_pairs(PairArgs<TI> A) {
             const int q_incl = __shfl_sync(0xffffffffu, incl, qq);
             const int q_cnt = __shfl_sync(0xffffffffu, ccount, qq);
             const int q_start = __shfl_sync(0xffffffffu, cstart, qq);
-            const int q_slp = __shfl_sync(0xffffffffu, slp, qq);
+            const unsigned q_slp = __shfl_sync(0xffffffffu, slp, qq);
             const float qx = __shfl_sync(0xffffffffu, ox, qq);
             const float qy = __shfl_sync(0xffffffffu, oy, qq);
             const float qz = __shfl_sync(0xffffffffu, oz, qq);
             if (f < nch) {
               const int slot = q_start + (gf - (q_incl - q_cnt));
               const float4 r = A.rec[slot];
-              W.cv[f] = make_float4(r.x + qx, r.y + qy, r.z + qz, r.w);
-              W.ci[f] = make_int2(slot, q_slp);
+              const unsigned mj = __float_as_uint(r.w);
+              unsigned cw;
+              if (mj & kExactBit) {
+                cw = q_slp | kExactBit;
+              } else {
+                const int b0 = unpack3(q_slp, 0) - meta_w(mj, 0), b1 = unpack3(q_slp, 1) - meta_w(mj, 1),
+                          b2 = unpack3(q_slp, 2) - meta_w(mj, 2);
+                cw = (abs(b0) > 127 || abs(b1) > 127 || abs(b2) > 127) ? (q_slp | kExactBit) : pack3(b0, b1, b2);
+              }
+              const float nan = __int_as_float(0x7fc00000);
+              const bool ex = (cw & kExactBit) != 0;
+              W.cv[f] = make_float4(ex ? nan : r.x + qx, ex ? nan : r.y + qy, ex ? nan : r.z + qz,
+                                    __uint_as_float(cw));
+              W.cslot[f] = slot;
+            } else {
+              const float inf = __int_as_float(0x7f800000);
+              W.cv[f] = make_float4(inf, inf, inf, 0.f);
             }
           }
           __syncwarp();
 
-          // ---- screen every home atom of the batch
-          for (int a = 0; a < nb; ++a) {
-            const float ax = __shfl_sync(0xffffffffu, ux, a);
-            const float ay = __shfl_sync(0xffffffffu, uy, a);
-            const float az = __shfl_sync(0xffffffffu, uz, a);
-            long long run = __shfl_sync(0xffffffffu, my_run, a);
-            const unsigned mi = W.hmeta[a];
-            const bool exact_i = meta_exact(mi);
-            // the self candidate (j == i with zero loop shift) sits in the center cell
-            const int self_f = center_excl >= 0 ? center_excl + (hb + a - hs) - cb : -1;
-            for (int r0 = 0; r0 < nch; r0 += 32) {
-              const int f = r0 + lane;
-              bool acc = false;
-              if (f < nch && f != self_f) {
-                const float4 c = W.cv[f];
-                const float rx = c.x - ax, ry = c.y - ay, rz = c.z - az;
-                const float r2 = fmaf(rz, rz, fmaf(ry, ry, rx * rx));
-                const unsigned mj = __float_as_uint(c.w);
-                const bool ex = exact_i || meta_exact(mj);
-                if (!ex && r2 < g.lo) {
-                  acc = true;
-                } else if (ex || r2 <= g.hi) {
-                  // FP64 decision with the reference arithmetic
-                  ++rechecks;
-                  const int slot_j = W.ci[f].x;
-                  double xj[3];
-                  xj[0] = A.Xs[3LL * slot_j + 0];
-                  xj[1] = A.Xs[3LL * slot_j + 1];
-                  xj[2] = A.Xs[3LL * slot_j + 2];
-                  int S[3];
-                  pair_S(g, W.hx[a], xj, mi, mj, W.ci[f].y, S);
-                  double R[3];
-                  pair_R(g, cs_tab, W.hx[a], xj, S[0], S[1], S[2], R);
-                  acc = dot_ref(R) < g.cutoff_sq;
-                }
-              }
-              const unsigned mask = __ballot_sync(0xffffffffu, acc);
-              const int np = __popc(mask);
-              if (MODE != kModeCount && np) {
-                const int rank = __popc(mask & lt_mask());
-                if (acc) {
-                  W.q[qn + rank] = (a << 16) | f;
-                  if (MODE == kModeFill) W.qslot[qn + rank] = W.hbase[a] + run + rank;
-                }
-                qn += np;
-                __syncwarp();
-                if (qn >= 32) {
-                  flush_queue<TI, MODE>(A, cs_tab, W, 32, lane);
-                  qn -= 32;
-                  // move the overflow [32, 32+qn) down to [0, qn); the ranges are disjoint
-                  if (lane < qn) {
-                    W.q[lane] = W.q[32 + lane];
-                    W.qslot[lane] = W.qslot[32 + lane];
-                  }
-                  __syncwarp();
-                }
-              }
-              run += np;
+          // ---- screen the home batch, kGroup atoms per candidate load.
+          // A test is pure FP32: accept 0 < r2 < lo, reject r2 > hi; the rest
+          // (the band, r2 == 0 which includes the self candidate, and NaN from
+          // exact atoms) is resolved in the warp-uniform rare branch.
+          const int nround = (nch + 31) & ~31;
+          for (int a0 = 0; a0 < nb; a0 += kGroup) {
+            float ax[kGroup], ay[kGroup], az[kGroup];
+            long long next[kGroup];
+            unsigned word[kGroup];  // count mode: lane w keeps acceptance word w
+#pragma unroll
+            for (int k = 0; k < kGroup; ++k) {
+              const int a = min(a0 + k, nb - 1);
+              const bool use = a0 + k < nb;
+              const float inf = __int_as_float(0x7f800000);
+              ax[k] = use ? __shfl_sync(0xffffffffu, ux, a) : inf;
+              ay[k] = use ? __shfl_sync(0xffffffffu, uy, a) : inf;
+              az[k] = use ? __shfl_sync(0xffffffffu, uz, a) : inf;
+              next[k] = W.hnext[a];
+              word[k] = 0u;
             }
-            if (lane == a) my_run = run;
+            for (int r0 = 0; r0 < nround; r0 += 32) {
+              const int f = r0 + lane;
+              const float4 c = W.cv[f];
+              bool acc[kGroup], unc[kGroup];
+              bool any_unc = false;
+#pragma unroll
+              for (int k = 0; k < kGroup; ++k) {
+                const float rx = c.x - ax[k], ry = c.y - ay[k], rz = c.z - az[k];
+                const float r2 = fmaf(rz, rz, fmaf(ry, ry, rx * rx));
+                acc[k] = r2 < lo && r2 > 0.f;
+                unc[k] = !(r2 > hi) && !acc[k];
+                any_unc |= unc[k];
+              }
+              if (__any_sync(0xffffffffu, any_unc)) {
+#pragma unroll
+                for (int k = 0; k < kGroup; ++k)
+                  if (unc[k]) {
+                    const int a = a0 + k;
+                    // the self candidate (j == i, zero loop shift) sits in the home cell
+                    const int self_f = center_excl >= 0 ? center_excl + (hb + a - hs) - cb : -1;
+                    if (f >= nch || a >= nb || f == self_f) {
+                      acc[k] = false;
+                    } else {
+                      ++rechecks;
+                      acc[k] = exact_pair(g, A.Xs, hb + a, W.cslot[f], W.hmeta[a], __float_as_uint(c.w));
+                    }
+                  }
+              }
+              if (MODE == kModeCount) {
+#pragma unroll
+                for (int k = 0; k < kGroup; ++k) {
+                  const unsigned mask = __ballot_sync(0xffffffffu, acc[k]);
+                  next[k] += __popc(mask);
+                  if (lane == ((cb + r0) >> 5)) word[k] = mask;
+                }
+              } else {
+#pragma unroll
+                for (int k = 0; k < kGroup; ++k) {
+                  const unsigned mask = __ballot_sync(0xffffffffu, acc[k]);
+                  if (mask == 0u) continue;
+                  const int np = __popc(mask);
+                  const int rank = __popc(mask & lt_mask());
+                  if (acc[k]) {
+                    const int rp = (tail + rank) & (kRing - 1);
+                    W.rent[rp] = ((a0 + k) << 16) | f;
+                    W.rslot[rp] = next[k] + rank;
+                  }
+                  tail += np;
+                  next[k] += np;
+                  if (tail - head >= 32) {
+                    __syncwarp();
+                    flush_ring<TI, MODE>(A, cs_tab, W, head, 32, lane);
+                    head += 32;
+                  }
+                }
+              }
+            }
+            if (MODE == kModeCount && masked) {
+              // lanes [cb/32, cb/32 + nround/32) hold this chunk's words
+              const int w = lane - (cb >> 5);
+              if (w >= 0 && w < (nround >> 5)) {
+#pragma unroll
+                for (int k = 0; k < kGroup; ++k)
+                  if (a0 + k < nb) A.masks[(long long)(hb + a0 + k) * kMaskWords + lane] = word[k];
+              }
+            }
+            __syncwarp();
+#pragma unroll
+            for (int k = 0; k < kGroup; ++k)
+              if (lane == k && a0 + k < nb) W.hnext[a0 + k] = next[k];
+            __syncwarp();
           }
         }
       }
-      if (MODE != kModeCount && qn > 0) flush_queue<TI, MODE>(A, cs_tab, W, qn, lane);
+      if (skip_cell) break;
+      if (MODE != kModeCount && tail > head) flush_ring<TI, MODE>(A, cs_tab, W, head, tail - head, lane);
       __syncwarp();
       if (lane < nb) {
-        if (MODE == kModeCount) A.counts[W.horig[lane]] = int(my_run);
+        if (MODE == kModeCount) A.counts[W.horig[lane]] = int(W.hnext[lane]);
         if (MODE == kModeLazyR6) A.per_atom[W.horig[lane]] = W.hacc[lane];
       }
       __syncwarp();
@@ -362,19 +539,171 @@ __global__ void __launch_bounds__(kPairWarps * 32) k_pairs(PairArgs<TI> A) {
   // statistics: number of FP64 decisions
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) rechecks += __shfl_xor_sync(0xffffffffu, rechecks, o);
-  if (lane == 0 && rechecks) atomicAdd(A.stats, rechecks);
+  if (lane == 0 && rechecks) atomicAdd(A.stats, (unsigned long long)rechecks);
+}
+
+// ------------------------------------------------------------------------
+// Emit: writes the pairs of every masked home cell from the acceptance masks
+// recorded by the count pass -- no staging and no screening.  One warp per
+// home cell; for each home atom, lane l takes the l-th accepted candidate
+// (bit order = the reference's traversal order), so a pass writes up to 32
+// consecutive output slots of one atom with coalesced stores.
+constexpr int kEmitWarps = 4;
+
+struct __align__(16) EmitSmem {
+  int qincl[32];      // inclusive candidate prefix of the stencil cells
+  int qstart[32];     // first sorted slot of each stencil cell
+  unsigned qslp[32];  // packed loop shift of each stencil cell
+};
+
+template <typename TI>
+__global__ void __launch_bounds__(kEmitWarps * 32) k_emit(PairArgs<TI> A) {
+  __shared__ EmitSmem es[kEmitWarps];
+  __shared__ double cs_tab[3 * kCsN * kCsN * kCsN];
+  __shared__ unsigned dtab[kStencilTab];
+  const Geometry& g = A.g;
+  for (int t = threadIdx.x; t < kCsN * kCsN * kCsN; t += blockDim.x) {
+    const int s0 = t % kCsN - kCsR, s1 = (t / kCsN) % kCsN - kCsR, s2 = t / (kCsN * kCsN) - kCsR;
+    cs_tab[3 * t + 0] = cts_k(g.C, s0, s1, s2, 0);
+    cs_tab[3 * t + 1] = cts_k(g.C, s0, s1, s2, 1);
+    cs_tab[3 * t + 2] = cts_k(g.C, s0, s1, s2, 2);
+  }
+  const int sx = 2 * g.nxyz[0] + 1, sy = 2 * g.nxyz[1] + 1, sz = 2 * g.nxyz[2] + 1;
+  const int nst = sx * sy * sz;
+  for (int t = threadIdx.x; t < min(kStencilTab, nst); t += blockDim.x)
+    dtab[t] = pack3(t % sx - g.nxyz[0], (t / sx) % sy - g.nxyz[1], t / (sx * sy) - g.nxyz[2]);
+  __syncthreads();
+  if (nst > 32) return;  // no cell of this system is masked
+
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  EmitSmem& E = es[warp];
+  const int nwarps = gridDim.x * kEmitWarps;
+  for (int h = blockIdx.x * kEmitWarps + warp; h < g.ncells; h += nwarps) {
+    const int hs = clampi(A.cell_offsets[h] - 1, g.nat), he = clampi(A.cell_offsets[h + 1] - 1, g.nat);
+    if (hs >= he) continue;
+    const int hc0 = h % g.ns[0] + 1, hc1 = (h / g.ns[0]) % g.ns[1] + 1, hc2 = h / (g.ns[0] * g.ns[1]) + 1;
+    int cstart = 0, ccount = 0;
+    unsigned slp = 0;
+    if (lane < nst) {
+      float ox, oy, oz;
+      const int lin = stencil_cell(g, dtab, sx, sy, hc0, hc1, hc2, lane, slp, ox, oy, oz);
+      if (lin >= 0) {
+        cstart = clampi(A.cell_offsets[lin] - 1, g.nat);
+        ccount = max(clampi(A.cell_offsets[lin + 1] - 1, g.nat) - cstart, 0);
+      }
+    }
+    int incl = ccount;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    const int tg = __shfl_sync(0xffffffffu, incl, 31);
+    if (tg > 32 * kMaskWords) continue;  // left to the screening fill
+    E.qincl[lane] = incl;
+    E.qstart[lane] = cstart;
+    E.qslp[lane] = slp;
+    __syncwarp();
+    const int nw = (tg + 31) >> 5;
+
+    for (int si = hs; si < he; ++si) {
+      const unsigned word = lane < nw ? A.masks[(long long)si * kMaskWords + lane] : 0u;
+      const int c = __popc(word);
+      int wincl = c;
+#pragma unroll
+      for (int o = 1; o < 16; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, wincl, o);
+        if (lane >= o) wincl += v;
+      }
+      const int n = __shfl_sync(0xffffffffu, wincl, 15);
+      if (n == 0) continue;
+      const float4 ri = A.rec[si];
+      const unsigned mi = __float_as_uint(ri.w);
+      const int orig_i = clampi(A.perm[si] - 1, g.nat - 1);
+      const long long base = (long long)A.first[orig_i] - 1;
+      double xi[3];
+      xi[0] = A.Xs[3LL * si + 0];
+      xi[1] = A.Xs[3LL * si + 1];
+      xi[2] = A.Xs[3LL * si + 2];
+      for (int p = 0; p < n; p += 32) {
+        const int e = p + lane;
+        const bool act = e < n;
+        // the word holding the e-th accepted candidate: smallest w with wincl_w > e
+        int w = 0;
+#pragma unroll
+        for (int step = 8; step > 0; step >>= 1) {
+          const int v = __shfl_sync(0xffffffffu, wincl, w + step - 1);
+          if (v <= e) w += step;
+        }
+        const int wexcl = __shfl_sync(0xffffffffu, wincl - c, w);
+        const unsigned m = __shfl_sync(0xffffffffu, word, w);
+        const int f = act ? 32 * w + int(__fns(m, 0, e - wexcl + 1)) : 0;
+        // the stencil cell of candidate f: smallest q with qincl_q > f
+        int q = 0;
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1)
+          if (E.qincl[q + step - 1] <= f) q += step;
+        const int slot_j = E.qstart[q] + f - (q > 0 ? E.qincl[q - 1] : 0);
+        int S[3] = {0, 0, 0};
+        double xj[3] = {0.0, 0.0, 0.0};
+        if (act) {
+          const unsigned sl = E.qslp[q];
+          const unsigned mj = __float_as_uint(A.rec[slot_j].w);
+          xj[0] = A.Xs[3LL * slot_j + 0];
+          xj[1] = A.Xs[3LL * slot_j + 1];
+          xj[2] = A.Xs[3LL * slot_j + 2];
+          if (!((mi | mj) & kExactBit)) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) S[k] = unpack3(sl, k) + meta_w(mi, k) - meta_w(mj, k);
+          } else {
+            Binned bi, bj;
+            bin_position(g, xi[0], xi[1], xi[2], bi);
+            bin_position(g, xj[0], xj[1], xj[2], bj);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) S[k] = unpack3(sl, k) + bi.w[k] - bj.w[k];
+          }
+        }
+        const long long out = base + e;
+        const bool wr = act && out < A.capacity;
+        if (act && !wr) atomicOr(A.err, kFlagCapacity);
+        if (wr) {
+          A.oi[out] = TI(orig_i) + 1;
+          A.oj[out] = TI(clampi(A.perm[slot_j] - 1, g.nat - 1)) + 1;
+          A.oS[3 * out + 0] = TI(S[0]);
+          A.oS[3 * out + 1] = TI(S[1]);
+          A.oS[3 * out + 2] = TI(S[2]);
+        }
+        if (A.oR) {
+          double R[3];
+          pair_R(g, cs_tab, xi, xj, S[0], S[1], S[2], act, R);
+          if (wr) {
+            A.oR[3 * out + 0] = R[0];
+            A.oR[3 * out + 1] = R[1];
+            A.oR[3 * out + 2] = R[2];
+          }
+        }
+      }
+    }
+    __syncwarp();
+  }
 }
 
 template <typename TI>
 void launch_pairs(int mode, const PairArgs<TI>& a, int num_sms, cudaStream_t st) {
   if (a.g.nat <= 0 || a.g.ncells <= 0) return;
-  const int per_sm = 6;  // resident blocks per SM targeted by the grid
   long long blocks = ((long long)a.g.ncells + kPairWarps - 1) / kPairWarps;
-  if (blocks > (long long)num_sms * per_sm) blocks = (long long)num_sms * per_sm;
+  if (blocks > (long long)num_sms * kMinBlocks) blocks = (long long)num_sms * kMinBlocks;
   if (blocks < 1) blocks = 1;
   switch (mode) {
     case kModeCount: k_pairs<TI, kModeCount><<<int(blocks), kPairWarps * 32, 0, st>>>(a); break;
-    case kModeFill: k_pairs<TI, kModeFill><<<int(blocks), kPairWarps * 32, 0, st>>>(a); break;
+    case kModeFill:
+      if (a.masks) {
+        long long eb = ((long long)a.g.ncells + kEmitWarps - 1) / kEmitWarps;
+        if (eb > (long long)num_sms * 16) eb = (long long)num_sms * 16;
+        k_emit<TI><<<int(eb), kEmitWarps * 32, 0, st>>>(a);
+      }
+      k_pairs<TI, kModeFill><<<int(blocks), kPairWarps * 32, 0, st>>>(a);
+      break;
     default: k_pairs<TI, kModeLazyR6><<<int(blocks), kPairWarps * 32, 0, st>>>(a); break;
   }
 }

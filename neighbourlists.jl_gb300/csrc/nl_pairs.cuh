@@ -6,6 +6,12 @@ namespace nl {
 
 enum PairMode : int { kModeCount = 0, kModeFill = 1, kModeLazyR6 = 2 };
 
+// The count pass records, per home atom, the acceptance bitmask of its
+// candidates (bit f = the f-th candidate in the reference's traversal order)
+// when the home cell's stencil has at most 32 cells and 32*kMaskWords
+// candidates.  The fill pass then writes those pairs without screening again.
+constexpr int kMaskWords = 12;
+
 template <typename TI>
 struct PairArgs {
   Geometry g;
@@ -13,6 +19,7 @@ struct PairArgs {
   const TI* perm;           // sorted slot -> 1-based original index
   const double* Xs;         // sorted positions (nat x 3)
   const float4* rec;        // sorted FP32 records
+  const int* scell;         // sorted slot -> 0-based cell index
   const TI* first;          // fill: 1-based pair offsets per original atom (nat+1)
   int* counts;              // count: pairs per original atom
   TI* oi;                   // fill outputs (1-based i, j; S as 3 x TI; R as 3 x double)
@@ -21,6 +28,7 @@ struct PairArgs {
   double* oR;               // may be null (R not wanted)
   long long capacity;       // pairs the output buffers hold
   double* per_atom;         // lazy: per-atom reduction
+  unsigned* masks;          // per sorted slot: kMaskWords acceptance words
   unsigned long long* stats;  // [0] += FP64 rechecks
   unsigned* err;
 };

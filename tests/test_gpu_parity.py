@@ -231,3 +231,32 @@ def test_bad_position_reported(nlpkg):
     with pytest.raises(nlpkg.NLError) as e:
         nlpkg.neighbour_list(X, 3.0, np.diag([10.0] * 3), (True, True, True))
     assert e.value.status == 6
+
+
+def test_binning_on_cell_boundaries(nlpkg, orc):
+    """Positions exactly on, and one ulp either side of, cell faces; tiny
+    negatives; zeros; large windings.  The fast double-float binning must
+    fall back to the reference's FP64 binning wherever it cannot decide."""
+    L = 30.0
+    C = np.diag([L, L, L])
+    n = 6  # cells per axis at rc = 5
+    faces = np.arange(-2 * n, 3 * n + 1) * (L / n)
+    vals = np.concatenate([faces, np.nextafter(faces, -np.inf), np.nextafter(faces, np.inf),
+                           [0.0, -0.0, -5e-17 * L, 5e-17 * L, 1e-300, -1e-300]])
+    rng = np.random.default_rng(17)
+    X = rng.choice(vals, size=(3000, 3))
+    for pbc in [(True, True, True), (False, True, False)]:
+        g = nlpkg.build_cell_list(torch.from_numpy(X).cuda(), 5.0, C, pbc)
+        o = orc.build_cell_list(X, 5.0, C, pbc)
+        np.testing.assert_array_equal(to_np(g.perm).astype(np.int64), o.perm)
+        np.testing.assert_array_equal(to_np(g.cell_id).astype(np.int64), o.cell_id)
+        Xs = X[rng.choice(3000, 400, replace=False)] + rng.normal(0, 0.5, (400, 3))
+        assert_identical(*run_both(nlpkg, orc, Xs, 5.0, C, pbc))
+    # triclinic cell, points on sheared faces
+    C2 = cf.fcc_sheared(n=4)[1]
+    F = rng.choice(np.arange(-4, 9) / 4.0, size=(2000, 3))
+    X2 = F @ C2
+    g = nlpkg.build_cell_list(torch.from_numpy(X2).cuda(), 3.0, C2, (True, True, False))
+    o = orc.build_cell_list(X2, 3.0, C2, (True, True, False))
+    np.testing.assert_array_equal(to_np(g.cell_id).astype(np.int64), o.cell_id)
+    np.testing.assert_array_equal(to_np(g.perm).astype(np.int64), o.perm)
