@@ -19,7 +19,9 @@
  *     for the calling thread.
  *
  * Ownership: the caller owns every input/output buffer and the workspace
- * (sized by nl_workspace_bytes).  The library allocates no device memory.
+ * (sized by nl_workspace_bytes).  The library allocates no device memory at
+ * run time; its device image holds the 32 MiB scratch array of
+ * nl_neighbour_list_static.
  */
 #ifndef NLGPU_H
 #define NLGPU_H
@@ -121,6 +123,24 @@ int nl_lazy_reduce(const double* d_X_sorted, const void* d_perm, const void* d_c
                    int64_t nat, const double cell[9], const double inv_cell[9], const int64_t ncells[3],
                    const int64_t nxyz[3], const uint8_t pbc[3], double cutoff, int index_bytes, int reuse_records,
                    int op, void* d_out, void* d_workspace, size_t workspace_bytes, void* stream);
+
+/* nl_neighbour_list without a workspace, for callers that cannot allocate
+ * device memory (a framework pool owns the device, a real-time loop forbids
+ * allocation after start-up, or the host code may not call cudaMalloc).  No
+ * counterpart in the reference: it exists only because this engine needs
+ * scratch memory.  The scratch is a fixed 32 MiB array inside the library,
+ * present on every GPU that loads it until the process exits; systems that
+ * need more (about 600k atoms at liquid density) are rejected with
+ * NL_ERR_NOMEM.  The first call on each device resolves the array's address
+ * and should come before any stream capture.  Every call reuses the same
+ * array: calls that overlap on the GPU race and must be serialised.  The call
+ * allocates nothing; pass total_pairs to synchronise and get the pair count
+ * and the status of the device-side checks. */
+int nl_neighbour_list_static(const double* d_X, int64_t nat, const double cell[9], const double inv_cell[9],
+                             const int64_t ncells[3], const int64_t nxyz[3], const uint8_t pbc[3], double cutoff,
+                             int index_bytes, void* d_perm, double* d_X_sorted, void* d_cell_id, void* d_cell_offsets,
+                             void* d_first, int64_t capacity, void* d_i, void* d_j, void* d_S, double* d_R,
+                             int64_t* total_pairs, void* stream);
 
 /* Synchronises the stream, then reports (and clears) any device-side error
  * recorded in the workspace by earlier asynchronous calls. */
