@@ -166,7 +166,8 @@ struct Layout {
   // [err 64 | stats 64] [pairs zero region: counters 64 | st_pairs]
   // [build zero region: counters 64 | st_cells | cell_count] [arrays...]
   size_t err, stats, pcount, st_pairs, pend, bcount, st_cells, cell_count, bend;
-  size_t totals, cell_start, cid, ticket, rec, tmp, rec_sorted, scell, counts, masks, big_list, end;
+  size_t totals, cell_start, cid, ticket, rec, tmp, rec_sorted, scell, counts, masks, cs_table, unmasked, big_list,
+      end;
 };
 
 Layout layout(int64_t nat, int64_t ncells) {
@@ -208,6 +209,10 @@ Layout layout(int64_t nat, int64_t ncells) {
   o += up(sizeof(int) * n);
   L.masks = o;
   o += up(sizeof(unsigned) * size_t(nl::kMaskWords) * n);
+  L.cs_table = o;
+  o += up(sizeof(double) * 3 * 125);
+  L.unmasked = o;
+  o += up(sizeof(int) * size_t(ncells > 0 ? ncells : 1));
   L.big_list = o;
   o += up(sizeof(int) * size_t(ncells < (int64_t)n ? ncells : (int64_t)n));
   L.end = o;
@@ -366,6 +371,9 @@ nl::PairArgs<TI> pair_args(const nl::Geometry& g, const TI* cell_offsets, const 
   a.rec = at<float4>(ws, L.rec_sorted);
   a.scell = at<int>(ws, L.scell);
   a.masks = at<unsigned>(ws, L.masks);
+  a.cs_table = at<double>(ws, L.cs_table);
+  a.unmasked = at<int>(ws, L.unmasked);
+  a.n_unmasked = at<int>(ws, L.pcount) + 4;  // zeroed with the pair scan state
   a.stats = at<unsigned long long>(ws, L.stats);
   a.err = at<unsigned>(ws, L.err);
   return a;
@@ -572,6 +580,8 @@ int nl_lazy_reduce(const double* d_X_sorted, const void* d_perm, const void* d_c
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   cudaError_t e = cudaSuccess;
   if (!reuse_records) e = cudaMemsetAsync(d_workspace, 0, 128, st);
+  // the count kernel appends its unmasked cells to a list counted in pcount
+  if (e == cudaSuccess) e = cudaMemsetAsync(static_cast<char*>(d_workspace) + L.pcount, 0, 64, st);
   if (e != cudaSuccess) return cuda_fail(e, "memset workspace");
   const int sms = num_sms();
   auto run = [&](auto tag) {

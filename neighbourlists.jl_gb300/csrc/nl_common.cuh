@@ -52,13 +52,21 @@ struct Geometry {
 
 // Per-atom record in cell-sorted order: float4 (u.x, u.y, u.z, meta) where
 // u = sum_k t_k b_k is the FP32 position relative to the lower corner of the
-// atom's (wrapped) cell and meta packs the winding numbers and a flag.
-__host__ __device__ inline unsigned pack_meta(int w0, int w1, int w2, bool exact) {
-  return (unsigned(w0) & 0xFFu) | ((unsigned(w1) & 0xFFu) << 8) | ((unsigned(w2) & 0xFFu) << 16) |
-         (exact ? (1u << 24) : 0u);
+// atom's (wrapped) cell and meta packs the winding numbers, each biased by
+// +128 into a 10-bit field (bits 0-9, 10-19, 20-29), and the exact flag (bit
+// 30).  The same 10-bit field layout carries the per-candidate S base in the
+// pair kernels, so that one packed subtraction yields three small integers.
+constexpr unsigned kMetaExact = 1u << 30;
+constexpr unsigned kMetaFields = (1u << 30) - 1u;
+__host__ __device__ inline unsigned pack10(int a, int b, int c) {
+  return (unsigned(a) & 1023u) | ((unsigned(b) & 1023u) << 10) | ((unsigned(c) & 1023u) << 20);
 }
-__host__ __device__ inline int meta_w(unsigned m, int k) { return int(int8_t((m >> (8 * k)) & 0xFFu)); }
-__host__ __device__ inline bool meta_exact(unsigned m) { return (m >> 24) & 1u; }
+__host__ __device__ inline int field10(unsigned m, int k) { return int((m >> (10 * k)) & 1023u); }
+__host__ __device__ inline unsigned pack_meta(int w0, int w1, int w2, bool exact) {
+  return pack10(w0 + 128, w1 + 128, w2 + 128) | (exact ? kMetaExact : 0u);
+}
+__host__ __device__ inline int meta_w(unsigned m, int k) { return field10(m, k) - 128; }
+__host__ __device__ inline bool meta_exact(unsigned m) { return (m & kMetaExact) != 0u; }
 
 // Atoms whose cell-local coordinate |t_k| exceeds this (open-axis atoms far
 // outside the box), whose |frac*n| exceeds kMaxY, or whose winding does not

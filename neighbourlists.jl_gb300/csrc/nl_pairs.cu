@@ -47,7 +47,7 @@ constexpr int kGroup = NL_PAIR_GROUP;            // home atoms screened per cand
 constexpr int kRing = 64;       // pair queue (ring) per warp
 constexpr int kCsR = 2;         // C'S table covers |S_k| <= kCsR
 constexpr int kCsN = 2 * kCsR + 1;
-constexpr unsigned kExactBit = 1u << 24;
+constexpr unsigned kExactBit = kMetaExact;
 
 struct __align__(16) WarpSmem {
   float4 cv[kChunk];        // candidate: (x, y, z) relative to home corner; w = packed S base | exact bit
@@ -124,21 +124,30 @@ __device__ __forceinline__ double dot_ref(const double* R) {
   return dadd(dadd(dmul(R[0], R[0]), dmul(R[1], R[1])), dmul(R[2], R[2]));
 }
 
-// S = s_loop + wi - wj (gpu_kernels.jl:88).  A candidate word cw holds
-// pack3(s_loop - wj) for a regular candidate, or pack3(s_loop) | exact bit
-// for an exact one.  Exact pairs recompute both windings in FP64.
+// The candidate word of stencil cell q: 10-bit fields s_loop + 640.  With
+// the record's meta (fields wj + 128) the packed difference
+//   cw = cand_base(q) - (meta_j & kMetaFields)   (no borrow between fields)
+// holds s_loop - wj + 512 per field; for an exact candidate (whose meta
+// windings are zero) it holds s_loop + 512, and the exact bit is or-ed in.
+__device__ __forceinline__ unsigned cand_base(int s0, int s1, int s2) { return pack10(s0 + 640, s1 + 640, s2 + 640); }
+__device__ __forceinline__ unsigned cand_word(unsigned base, unsigned mj) {
+  return (base - (mj & kMetaFields)) | (mj & kMetaExact);
+}
+
+// S = s_loop + wi - wj (gpu_kernels.jl:88) from a candidate word.  Exact pairs
+// recompute both windings in FP64.
 __device__ __forceinline__ void pair_S(const Geometry& g, const double* xi, const double* xj, unsigned mi, unsigned cw,
                                        int* S) {
   if (!((mi | cw) & kExactBit)) {
 #pragma unroll
-    for (int k = 0; k < 3; ++k) S[k] = unpack3(cw, k) + meta_w(mi, k);
+    for (int k = 0; k < 3; ++k) S[k] = field10(cw, k) + field10(mi, k) - 640;
   } else {
     Binned bi, bj;
     bin_position(g, xi[0], xi[1], xi[2], bi);
     bin_position(g, xj[0], xj[1], xj[2], bj);
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      const int sl = (cw & kExactBit) ? unpack3(cw, k) : unpack3(cw, k) + bj.w[k];
+      const int sl = (cw & kExactBit) ? field10(cw, k) - 512 : field10(cw, k) - 512 + bj.w[k];
       S[k] = sl + bi.w[k] - bj.w[k];
     }
   }
@@ -223,6 +232,17 @@ __device__ __forceinline__ void flush_ring(const PairArgs<TI>& A, const double* 
   __syncwarp();
 }
 
+// C'S for |S_k| <= kCsR with the reference's operation order, built once per
+// call (one block) and read by the fill / emit / lazy kernels.
+__global__ void k_cs_table(Geometry g, double* __restrict__ out) {
+  for (int t = threadIdx.x; t < kCsN * kCsN * kCsN; t += blockDim.x) {
+    const int s0 = t % kCsN - kCsR, s1 = (t / kCsN) % kCsN - kCsR, s2 = t / (kCsN * kCsN) - kCsR;
+    out[3 * t + 0] = cts_k(g.C, s0, s1, s2, 0);
+    out[3 * t + 1] = cts_k(g.C, s0, s1, s2, 1);
+    out[3 * t + 2] = cts_k(g.C, s0, s1, s2, 2);
+  }
+}
+
 // wrap_shift without a division for the common case of an index already
 // inside [1, n]
 __device__ __forceinline__ int wrap_shift_fast(int i, int n, int pbc, int& s) {
@@ -259,7 +279,7 @@ __device__ __forceinline__ int stencil_cell(const Geometry& g, const unsigned* d
   const int c0 = wrap_shift_fast(hc0 + d0, g.ns[0], g.pbc[0], s0);
   const int c1 = wrap_shift_fast(hc1 + d1, g.ns[1], g.pbc[1], s1);
   const int c2 = wrap_shift_fast(hc2 + d2, g.ns[2], g.pbc[2], s2);
-  slp = pack3(s0, s1, s2);  // |s| <= 63: the host limits nxyz to 62
+  slp = cand_base(s0, s1, s2);  // |s| <= 63: the host limits nxyz to 62
   const float fd0 = float(d0), fd1 = float(d1), fd2 = float(d2);
   ox = fmaf(fd2, g.b[6], fmaf(fd1, g.b[3], fd0 * g.b[0]));
   oy = fmaf(fd2, g.b[7], fmaf(fd1, g.b[4], fd0 * g.b[1]));
@@ -273,12 +293,8 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
   __shared__ double cs_tab[3 * kCsN * kCsN * kCsN];
   __shared__ unsigned dtab[kStencilTab];  // packed (d0, d1, d2) of stencil cell q
   const Geometry& g = A.g;
-  for (int t = threadIdx.x; t < kCsN * kCsN * kCsN; t += blockDim.x) {
-    const int s0 = t % kCsN - kCsR, s1 = (t / kCsN) % kCsN - kCsR, s2 = t / (kCsN * kCsN) - kCsR;
-    cs_tab[3 * t + 0] = cts_k(g.C, s0, s1, s2, 0);
-    cs_tab[3 * t + 1] = cts_k(g.C, s0, s1, s2, 1);
-    cs_tab[3 * t + 2] = cts_k(g.C, s0, s1, s2, 2);
-  }
+  if (MODE != kModeCount)
+    for (int t = threadIdx.x; t < 3 * kCsN * kCsN * kCsN; t += blockDim.x) cs_tab[t] = A.cs_table[t];
   {
     const int tx = 2 * g.nxyz[0] + 1, ty = 2 * g.nxyz[1] + 1;
     const int tn = min(kStencilTab, tx * ty * (2 * g.nxyz[2] + 1));
@@ -298,11 +314,16 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
 
   // Ranges of the next cell are prefetched one cell ahead: its home range and,
   // per lane, the range of its stencil cell in the first group of 32.
-  int h = blockIdx.x * kPairWarps + warp;
+  // The fill pass visits only the cells that the count pass could not mask
+  // (k_emit writes the others); count and lazy visit every cell.
+  const int ncell_iter = MODE == kModeFill ? min(*A.n_unmasked, g.ncells) : g.ncells;
+  auto cell_at = [&](int idx) { return MODE == kModeFill ? clampi(A.unmasked[idx], g.ncells - 1) : idx; };
+  int idx = blockIdx.x * kPairWarps + warp;
   // (0-based slot offsets, clamped to [0, nat])
   int pf_hs = 0, pf_he = 0, pf_lo = 0, pf_hi = 0;
-  auto prefetch = [&](int hh) {
-    if (hh >= g.ncells) return;
+  auto prefetch = [&](int pidx) {
+    if (pidx >= ncell_iter) return;
+    const int hh = cell_at(pidx);
     pf_hs = clampi(A.cell_offsets[hh] - 1, g.nat);
     pf_he = clampi(A.cell_offsets[hh + 1] - 1, g.nat);
     const int c0 = hh % g.ns[0] + 1, c1 = (hh / g.ns[0]) % g.ns[1] + 1, c2 = hh / (g.ns[0] * g.ns[1]) + 1;
@@ -312,18 +333,18 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
     pf_lo = lin >= 0 ? clampi(A.cell_offsets[lin] - 1, g.nat) : 0;
     pf_hi = lin >= 0 ? clampi(A.cell_offsets[lin + 1] - 1, g.nat) : 0;
   };
-  prefetch(h);
-  for (; h < g.ncells; h += nwarps) {
+  prefetch(idx);
+  for (; idx < ncell_iter; idx += nwarps) {
+    const int h = cell_at(idx);
     // offsets are clamped to [0, nat] so that a malformed cell list (which
     // the prepare pass reports as inconsistent) never indexes out of bounds
     const int hs = pf_hs, he = pf_he;
     const int g0_lo = pf_lo, g0_hi = pf_hi;
-    prefetch(h + nwarps);  // loads in flight while this cell is processed
+    prefetch(idx + nwarps);  // loads in flight while this cell is processed
     if (hs >= he) continue;
     const int hc0 = h % g.ns[0] + 1, hc1 = (h / g.ns[0]) % g.ns[1] + 1, hc2 = h / (g.ns[0] * g.ns[1]) + 1;
 
-    bool skip_cell = false;
-    for (int hb = hs; hb < he && !skip_cell; hb += 32) {
+    for (int hb = hs; hb < he; hb += 32) {
       const int nb = min(32, he - hb);
       float ux = 0.f, uy = 0.f, uz = 0.f;
       int head = 0, tail = 0;  // ring queue (fill / lazy)
@@ -351,10 +372,10 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
         const int tg = __shfl_sync(0xffffffffu, incl, 31);
         // cells whose candidates fit the acceptance masks: the count pass
         // records them and the fill pass leaves them to k_emit
-        const bool masked = A.masks != nullptr && nst <= 32 && tg <= 32 * kMaskWords;
-        if (MODE == kModeFill && masked) {
-          skip_cell = true;
-          break;
+        const bool masked = nst <= 32 && tg <= 32 * kMaskWords;
+        if (MODE == kModeCount && !masked && gb == 0 && hb == hs && lane == 0) {
+          const int u = atomicAdd(A.n_unmasked, 1);
+          if (u < g.ncells) A.unmasked[u] = h;
         }
         const int cl = center - gb;  // home cell (center of the stencil) in this group?
         const int center_excl = (cl >= 0 && cl < 32) ? __shfl_sync(0xffffffffu, incl - ccount, cl & 31) : -1;
@@ -413,13 +434,7 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
               const float4 r = A.rec[slot];
               const unsigned mj = __float_as_uint(r.w);
               unsigned cw;
-              if (mj & kExactBit) {
-                cw = q_slp | kExactBit;
-              } else {
-                const int b0 = unpack3(q_slp, 0) - meta_w(mj, 0), b1 = unpack3(q_slp, 1) - meta_w(mj, 1),
-                          b2 = unpack3(q_slp, 2) - meta_w(mj, 2);
-                cw = (abs(b0) > 127 || abs(b1) > 127 || abs(b2) > 127) ? (q_slp | kExactBit) : pack3(b0, b1, b2);
-              }
+              cw = cand_word(q_slp, mj);
               const float nan = __int_as_float(0x7fc00000);
               const bool ex = (cw & kExactBit) != 0;
               W.cv[f] = make_float4(ex ? nan : r.x + qx, ex ? nan : r.y + qy, ex ? nan : r.z + qz,
@@ -526,7 +541,6 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
           }
         }
       }
-      if (skip_cell) break;
       if (MODE != kModeCount && tail > head) flush_ring<TI, MODE>(A, cs_tab, W, head, tail - head, lane);
       __syncwarp();
       if (lane < nb) {
@@ -544,17 +558,43 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
 
 // ------------------------------------------------------------------------
 // Emit: writes the pairs of every masked home cell from the acceptance masks
-// recorded by the count pass -- no staging and no screening.  One warp per
-// home cell; for each home atom, lane l takes the l-th accepted candidate
-// (bit order = the reference's traversal order), so a pass writes up to 32
-// consecutive output slots of one atom with coalesced stores.
+// recorded by the count pass -- no staging of candidates and no screening.
+// One warp per home cell, one home atom at a time: lanes 0..nw-1 hold the
+// atom's acceptance words, a shuffle scan numbers its accepted candidates,
+// and lane r resolves and writes the atom's r-th pair.  The output slots
+// first[i] + r are consecutive, so the stores coalesce.  Candidate f maps to
+// its stencil cell through a per-cell byte table.
 constexpr int kEmitWarps = 4;
+constexpr int kEmitCand = 32 * kMaskWords;  // candidates a masked cell may have
 
 struct __align__(16) EmitSmem {
-  int qincl[32];      // inclusive candidate prefix of the stencil cells
-  int qstart[32];     // first sorted slot of each stencil cell
-  unsigned qslp[32];  // packed loop shift of each stencil cell
+  double hx[32][3];             // home batch: FP64 positions
+  long long hbase[32];          // home batch: first output slot (0-based)
+  int horig[32];                // home batch: original index (0-based)
+  unsigned hmeta[32];           // home batch: packed windings | exact bit
+  int qstart[32];               // stencil cell q: first sorted slot
+  int qexcl[32];                // stencil cell q: candidates before it
+  unsigned qslp[32];            // stencil cell q: candidate word base
+  unsigned char cq[kEmitCand];  // candidate f -> its stencil cell q
 };
+
+// position of the (k+1)-th set bit of m (0 <= k < popc(m)), by bisection
+__device__ __forceinline__ int nth_set_bit(unsigned m, int k) {
+  int pos = 0;
+#pragma unroll
+  for (int half = 16; half > 0; half >>= 1) {
+    const unsigned low = m & ((1u << half) - 1u);
+    const int c = __popc(low);
+    if (k >= c) {
+      k -= c;
+      m >>= half;
+      pos += half;
+    } else {
+      m = low;
+    }
+  }
+  return pos;
+}
 
 template <typename TI>
 __global__ void __launch_bounds__(kEmitWarps * 32) k_emit(PairArgs<TI> A) {
@@ -562,18 +602,13 @@ __global__ void __launch_bounds__(kEmitWarps * 32) k_emit(PairArgs<TI> A) {
   __shared__ double cs_tab[3 * kCsN * kCsN * kCsN];
   __shared__ unsigned dtab[kStencilTab];
   const Geometry& g = A.g;
-  for (int t = threadIdx.x; t < kCsN * kCsN * kCsN; t += blockDim.x) {
-    const int s0 = t % kCsN - kCsR, s1 = (t / kCsN) % kCsN - kCsR, s2 = t / (kCsN * kCsN) - kCsR;
-    cs_tab[3 * t + 0] = cts_k(g.C, s0, s1, s2, 0);
-    cs_tab[3 * t + 1] = cts_k(g.C, s0, s1, s2, 1);
-    cs_tab[3 * t + 2] = cts_k(g.C, s0, s1, s2, 2);
-  }
   const int sx = 2 * g.nxyz[0] + 1, sy = 2 * g.nxyz[1] + 1, sz = 2 * g.nxyz[2] + 1;
   const int nst = sx * sy * sz;
-  for (int t = threadIdx.x; t < min(kStencilTab, nst); t += blockDim.x)
+  if (nst > 32) return;  // no cell of this system is masked (uniform over the grid)
+  for (int t = threadIdx.x; t < 3 * kCsN * kCsN * kCsN; t += blockDim.x) cs_tab[t] = A.cs_table[t];
+  for (int t = threadIdx.x; t < nst; t += blockDim.x)
     dtab[t] = pack3(t % sx - g.nxyz[0], (t / sx) % sy - g.nxyz[1], t / (sx * sy) - g.nxyz[2]);
   __syncthreads();
-  if (nst > 32) return;  // no cell of this system is masked
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   EmitSmem& E = es[warp];
@@ -599,92 +634,90 @@ __global__ void __launch_bounds__(kEmitWarps * 32) k_emit(PairArgs<TI> A) {
       if (lane >= o) incl += v;
     }
     const int tg = __shfl_sync(0xffffffffu, incl, 31);
-    if (tg > 32 * kMaskWords) continue;  // left to the screening fill
-    E.qincl[lane] = incl;
-    E.qstart[lane] = cstart;
-    E.qslp[lane] = slp;
-    __syncwarp();
+    if (tg > kEmitCand) continue;  // left to the screening fill
     const int nw = (tg + 31) >> 5;
+    __syncwarp();  // the previous cell's tables are no longer read
+    E.qstart[lane] = cstart;
+    E.qexcl[lane] = incl - ccount;
+    E.qslp[lane] = slp;
+    for (int f = incl - ccount; f < incl; ++f) E.cq[f] = (unsigned char)lane;
 
-    for (int si = hs; si < he; ++si) {
-      const unsigned word = lane < nw ? A.masks[(long long)si * kMaskWords + lane] : 0u;
-      const int c = __popc(word);
-      int wincl = c;
-#pragma unroll
-      for (int o = 1; o < 16; o <<= 1) {
-        const int v = __shfl_up_sync(0xffffffffu, wincl, o);
-        if (lane >= o) wincl += v;
+    for (int hb = hs; hb < he; hb += 32) {
+      const int nb = min(32, he - hb);
+      __syncwarp();
+      if (lane < nb) {
+        const int si = hb + lane;
+        const int orig = clampi(A.perm[si] - 1, g.nat - 1);
+        E.horig[lane] = orig;
+        E.hbase[lane] = (long long)A.first[orig] - 1;
+        E.hmeta[lane] = __float_as_uint(A.rec[si].w);
+        E.hx[lane][0] = A.Xs[3LL * si + 0];
+        E.hx[lane][1] = A.Xs[3LL * si + 1];
+        E.hx[lane][2] = A.Xs[3LL * si + 2];
       }
-      const int n = __shfl_sync(0xffffffffu, wincl, 15);
-      if (n == 0) continue;
-      const float4 ri = A.rec[si];
-      const unsigned mi = __float_as_uint(ri.w);
-      const int orig_i = clampi(A.perm[si] - 1, g.nat - 1);
-      const long long base = (long long)A.first[orig_i] - 1;
-      double xi[3];
-      xi[0] = A.Xs[3LL * si + 0];
-      xi[1] = A.Xs[3LL * si + 1];
-      xi[2] = A.Xs[3LL * si + 2];
-      for (int p = 0; p < n; p += 32) {
-        const int e = p + lane;
-        const bool act = e < n;
-        // the word holding the e-th accepted candidate: smallest w with wincl_w > e
-        int w = 0;
+      __syncwarp();
+      for (int a = 0; a < nb; ++a) {
+        // the atom's acceptance words (bit f = candidate f) and their
+        // inclusive prefix of set bits over lanes 0..15 (nw <= 12)
+        const unsigned m = lane < nw ? A.masks[(long long)(hb + a) * kMaskWords + lane] : 0u;
+        int wincl = __popc(m);
 #pragma unroll
-        for (int step = 8; step > 0; step >>= 1) {
-          const int v = __shfl_sync(0xffffffffu, wincl, w + step - 1);
-          if (v <= e) w += step;
+        for (int o = 1; o < 16; o <<= 1) {
+          const int v = __shfl_up_sync(0xffffffffu, wincl, o);
+          if (lane >= o) wincl += v;
         }
-        const int wexcl = __shfl_sync(0xffffffffu, wincl - c, w);
-        const unsigned m = __shfl_sync(0xffffffffu, word, w);
-        const int f = act ? 32 * w + int(__fns(m, 0, e - wexcl + 1)) : 0;
-        // the stencil cell of candidate f: smallest q with qincl_q > f
-        int q = 0;
+        const int n = __shfl_sync(0xffffffffu, wincl, 15);
+        if (n == 0) continue;
+        const double* xi = E.hx[a];
+        const unsigned mi = E.hmeta[a];
+        const long long base = E.hbase[a];
+        const TI ti = TI(E.horig[a]) + 1;
+        for (int p = 0; p < n; p += 32) {
+          const int r = p + lane;
+          const bool act = r < n;
+          const int rr = min(r, n - 1);
+          // word of the rr-th accepted candidate: smallest w with wincl_w > rr
+          int w = 0;
 #pragma unroll
-        for (int step = 16; step > 0; step >>= 1)
-          if (E.qincl[q + step - 1] <= f) q += step;
-        const int slot_j = E.qstart[q] + f - (q > 0 ? E.qincl[q - 1] : 0);
-        int S[3] = {0, 0, 0};
-        double xj[3] = {0.0, 0.0, 0.0};
-        if (act) {
-          const unsigned sl = E.qslp[q];
+          for (int step = 8; step > 0; step >>= 1) {
+            const int v = __shfl_sync(0xffffffffu, wincl, w + step - 1);
+            if (v <= rr) w += step;
+          }
+          const unsigned mw = __shfl_sync(0xffffffffu, m, w);
+          const int wex = __shfl_sync(0xffffffffu, wincl, w) - __popc(mw);
+          const int f = 32 * w + nth_set_bit(mw, rr - wex);  // w < nw, so f < kEmitCand
+          const int q = E.cq[f];
+          const int slot_j = clampi(E.qstart[q] + f - E.qexcl[q], g.nat - 1);
           const unsigned mj = __float_as_uint(A.rec[slot_j].w);
+          double xj[3];
           xj[0] = A.Xs[3LL * slot_j + 0];
           xj[1] = A.Xs[3LL * slot_j + 1];
           xj[2] = A.Xs[3LL * slot_j + 2];
-          if (!((mi | mj) & kExactBit)) {
-#pragma unroll
-            for (int k = 0; k < 3; ++k) S[k] = unpack3(sl, k) + meta_w(mi, k) - meta_w(mj, k);
-          } else {
-            Binned bi, bj;
-            bin_position(g, xi[0], xi[1], xi[2], bi);
-            bin_position(g, xj[0], xj[1], xj[2], bj);
-#pragma unroll
-            for (int k = 0; k < 3; ++k) S[k] = unpack3(sl, k) + bi.w[k] - bj.w[k];
-          }
-        }
-        const long long out = base + e;
-        const bool wr = act && out < A.capacity;
-        if (act && !wr) atomicOr(A.err, kFlagCapacity);
-        if (wr) {
-          A.oi[out] = TI(orig_i) + 1;
-          A.oj[out] = TI(clampi(A.perm[slot_j] - 1, g.nat - 1)) + 1;
-          A.oS[3 * out + 0] = TI(S[0]);
-          A.oS[3 * out + 1] = TI(S[1]);
-          A.oS[3 * out + 2] = TI(S[2]);
-        }
-        if (A.oR) {
-          double R[3];
-          pair_R(g, cs_tab, xi, xj, S[0], S[1], S[2], act, R);
+          const int oj = clampi(A.perm[slot_j] - 1, g.nat - 1);
+          int S[3];
+          pair_S(g, xi, xj, mi, cand_word(E.qslp[q], mj), S);
+          const long long out = base + r;
+          const bool wr = act && out < A.capacity;
+          if (act && !wr) atomicOr(A.err, kFlagCapacity);
           if (wr) {
-            A.oR[3 * out + 0] = R[0];
-            A.oR[3 * out + 1] = R[1];
-            A.oR[3 * out + 2] = R[2];
+            A.oi[out] = ti;
+            A.oj[out] = TI(oj) + 1;
+            A.oS[3 * out + 0] = TI(S[0]);
+            A.oS[3 * out + 1] = TI(S[1]);
+            A.oS[3 * out + 2] = TI(S[2]);
+          }
+          if (A.oR) {
+            double R[3];
+            pair_R(g, cs_tab, xi, xj, S[0], S[1], S[2], act, R);
+            if (wr) {
+              A.oR[3 * out + 0] = R[0];
+              A.oR[3 * out + 1] = R[1];
+              A.oR[3 * out + 2] = R[2];
+            }
           }
         }
       }
     }
-    __syncwarp();
   }
 }
 
@@ -696,15 +729,18 @@ void launch_pairs(int mode, const PairArgs<TI>& a, int num_sms, cudaStream_t st)
   if (blocks < 1) blocks = 1;
   switch (mode) {
     case kModeCount: k_pairs<TI, kModeCount><<<int(blocks), kPairWarps * 32, 0, st>>>(a); break;
-    case kModeFill:
-      if (a.masks) {
-        long long eb = ((long long)a.g.ncells + kEmitWarps - 1) / kEmitWarps;
-        if (eb > (long long)num_sms * 16) eb = (long long)num_sms * 16;
-        k_emit<TI><<<int(eb), kEmitWarps * 32, 0, st>>>(a);
-      }
+    case kModeFill: {
+      k_cs_table<<<1, 128, 0, st>>>(a.g, a.cs_table);
+      long long eb = ((long long)a.g.ncells + kEmitWarps - 1) / kEmitWarps;
+      if (eb > (long long)num_sms * 16) eb = (long long)num_sms * 16;
+      k_emit<TI><<<int(eb), kEmitWarps * 32, 0, st>>>(a);
       k_pairs<TI, kModeFill><<<int(blocks), kPairWarps * 32, 0, st>>>(a);
       break;
-    default: k_pairs<TI, kModeLazyR6><<<int(blocks), kPairWarps * 32, 0, st>>>(a); break;
+    }
+    default:
+      k_cs_table<<<1, 128, 0, st>>>(a.g, a.cs_table);
+      k_pairs<TI, kModeLazyR6><<<int(blocks), kPairWarps * 32, 0, st>>>(a);
+      break;
   }
 }
 

@@ -29,6 +29,9 @@ struct PairArgs {
   long long capacity;       // pairs the output buffers hold
   double* per_atom;         // lazy: per-atom reduction
   unsigned* masks;          // per sorted slot: kMaskWords acceptance words
+  double* cs_table;         // C'S for |S_k| <= 2 (built once per call by k_cs_table)
+  int* unmasked;            // count pass: home cells left to the screening fill
+  int* n_unmasked;          // length of that list
   unsigned long long* stats;  // [0] += FP64 rechecks
   unsigned* err;
 };
