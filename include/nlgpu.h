@@ -142,6 +142,54 @@ int nl_neighbour_list_static(const double* d_X, int64_t nat, const double cell[9
                              void* d_first, int64_t capacity, void* d_i, void* d_j, void* d_S, double* d_R,
                              int64_t* total_pairs, void* stream);
 
+/* ---- batches of independent systems -------------------------------------
+ * No counterpart in the reference, which handles one system per call: a
+ * batch replaces a loop of neighbour_list(X_s, cutoff_s, cell_s, pbc_s)
+ * calls (cell_list.jl:897-916) by one launch per stage over all systems.
+ *
+ * Layout: the atoms of system s are rows atom0[s] .. atom0[s]+nat_s-1 of the
+ * batch's X (atom0 = running sum of nat).  Every per-system output is the
+ * reference's array for that system, placed one after another in system
+ * order, with system-local 1-based values:
+ *   perm, cell_id, X_sorted : at atom0[s]            (nat_s entries)
+ *   cell_offsets            : at cell0[s] + s        (ncells_s + 1 entries)
+ *   first                   : at atom0[s] + s        (nat_s + 1 entries)
+ *   i, j, S, R              : at pair_offsets[s]     (npairs_s entries)
+ * where cell0 is the running sum of ncells_total and pair_offsets (nsys + 1
+ * int64, written by the call) the running sum of the pair counts. */
+typedef struct nl_system {
+  int64_t nat;          /* atoms of this system */
+  double cell[9];       /* column-major, rows = lattice vectors */
+  double inv_cell[9];   /* the caller's analyze_cell results, as for nl_build_cell_list */
+  int64_t ncells[3];
+  int64_t nxyz[3];
+  uint8_t pbc[3];
+  double cutoff;
+} nl_system;
+
+typedef struct nl_batch nl_batch;   /* host-side plan of a batch (opaque) */
+
+/* Validates the systems and builds the host plan.  index_bytes applies to
+ * every system. */
+int nl_batch_create(const nl_system* systems, int nsys, int index_bytes, nl_batch** batch);
+void nl_batch_destroy(nl_batch* batch);
+/* Workspace bytes for the batch, and its total atoms / cells. */
+size_t nl_batch_workspace_bytes(const nl_batch* batch);
+int nl_batch_sizes(const nl_batch* batch, int64_t* total_atoms, int64_t* total_cells);
+/* Copies the batch's geometry tables into the workspace (returns after the
+ * copy has completed).  Needed once per workspace before any run; runs do
+ * not modify the tables, so many runs (and stream captures of runs) can
+ * follow one upload. */
+int nl_batch_upload(const nl_batch* batch, void* d_workspace, size_t workspace_bytes, void* stream);
+/* Build + count + fill of every system of the batch, stream-ordered, with
+ * no host synchronisation unless total_pairs is non-NULL (then as
+ * nl_neighbour_list: the batch's total pair count, NL_ERR_CAPACITY when it
+ * exceeds capacity). */
+int nl_batch_neighbour_list(const nl_batch* batch, const double* d_X, void* d_perm, double* d_X_sorted,
+                            void* d_cell_id, void* d_cell_offsets, void* d_first, int64_t* d_pair_offsets,
+                            int64_t capacity, void* d_i, void* d_j, void* d_S, double* d_R, int64_t* total_pairs,
+                            void* d_workspace, size_t workspace_bytes, void* stream);
+
 /* Synchronises the stream, then reports (and clears) any device-side error
  * recorded in the workspace by earlier asynchronous calls. */
 int nl_sync_status(void* d_workspace, void* stream);

@@ -24,4 +24,5 @@ from .api import (  # noqa: F401
     nsites,
     num_neighbours,
 )
+from .batch import BatchNeighbourList  # noqa: F401
 from .engine import NeighbourListEngine  # noqa: F401

@@ -35,6 +35,12 @@ EXPORTED = [
     "nl_neighbour_list",
     "nl_neighbour_list_static",
     "nl_lazy_reduce",
+    "nl_batch_create",
+    "nl_batch_destroy",
+    "nl_batch_workspace_bytes",
+    "nl_batch_sizes",
+    "nl_batch_upload",
+    "nl_batch_neighbour_list",
     "nl_sync_status",
     "nl_last_recheck_count",
     "nl_status_string",
@@ -51,6 +57,19 @@ class CellPlan(C.Structure):
         ("nxyz", C.c_int64 * 3),
         ("ncells_total", C.c_int64),
         ("band", C.c_double),
+    ]
+
+
+class System(C.Structure):
+    """nl_system: one system of a batch."""
+    _fields_ = [
+        ("nat", C.c_int64),
+        ("cell", C.c_double * 9),
+        ("inv_cell", C.c_double * 9),
+        ("ncells", C.c_int64 * 3),
+        ("nxyz", C.c_int64 * 3),
+        ("pbc", C.c_uint8 * 3),
+        ("cutoff", C.c_double),
     ]
 
 
@@ -93,6 +112,19 @@ def _declare(L):
     L.nl_lazy_reduce.argtypes = [_vp, _vp, _vp, _vp, C.c_int64, _D, _D, _I64, _I64, _U8, C.c_double, C.c_int, C.c_int,
                                  C.c_int, _vp, _vp, C.c_size_t, _vp]
     L.nl_lazy_reduce.restype = C.c_int
+    L.nl_batch_create.argtypes = [C.POINTER(System), C.c_int, C.c_int, C.POINTER(_vp)]
+    L.nl_batch_create.restype = C.c_int
+    L.nl_batch_destroy.argtypes = [_vp]
+    L.nl_batch_destroy.restype = None
+    L.nl_batch_workspace_bytes.argtypes = [_vp]
+    L.nl_batch_workspace_bytes.restype = C.c_size_t
+    L.nl_batch_sizes.argtypes = [_vp, _I64, _I64]
+    L.nl_batch_sizes.restype = C.c_int
+    L.nl_batch_upload.argtypes = [_vp, _vp, C.c_size_t, _vp]
+    L.nl_batch_upload.restype = C.c_int
+    L.nl_batch_neighbour_list.argtypes = [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int64, _vp, _vp, _vp, _vp, _I64,
+                                          _vp, C.c_size_t, _vp]
+    L.nl_batch_neighbour_list.restype = C.c_int
     L.nl_sync_status.argtypes = [_vp, _vp]
     L.nl_sync_status.restype = C.c_int
     L.nl_last_recheck_count.argtypes = [_vp, _vp, _I64]

@@ -12,7 +12,9 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <new>
 #include <string>
+#include <vector>
 
 #include "nl_api_internal.h"
 #include "nl_build.cuh"
@@ -349,11 +351,12 @@ int build_impl(const double* X, int64_t nat, const nl::Geometry& g, TI* perm, do
   int* cell_start = at<int>(ws, L.cell_start);
   unsigned* err = at<unsigned>(ws, L.err);
   int* bcount = at<int>(ws, L.bcount);
-  nl::launch_bin(g, X, int(nat), cid, ticket, rec, cell_count, err, sms, st);
+  const nl::SysIndex single{nullptr, nullptr, nullptr, 0};
+  nl::launch_bin(g, single, X, int(nat), cid, ticket, rec, cell_count, err, sms, st);
   nl::launch_scan<TI>(cell_count, g.ncells, cell_offsets, cell_start, at<unsigned long long>(ws, L.st_cells), bcount,
                       at<long long>(ws, L.totals), err, st);
   nl::launch_scatter(int(nat), cid, ticket, cell_start, at<int>(ws, L.tmp), sms, st);
-  nl::launch_fix<TI>(int(nat), at<int>(ws, L.tmp), cid, cell_start, X, rec, perm, cell_id, Xs,
+  nl::launch_fix<TI>(single, int(nat), at<int>(ws, L.tmp), cid, cell_start, X, rec, perm, cell_id, Xs,
                      at<float4>(ws, L.rec_sorted), at<int>(ws, L.scell), at<int>(ws, L.big_list), bcount + 1, sms, st);
   e = cudaGetLastError();
   return e == cudaSuccess ? NL_OK : cuda_fail(e, "launch build kernels");
@@ -365,6 +368,8 @@ nl::PairArgs<TI> pair_args(const nl::Geometry& g, const TI* cell_offsets, const 
   nl::PairArgs<TI> a;
   std::memset(&a, 0, sizeof(a));
   a.g = g;
+  a.nat_total = g.nat;
+  a.ncells_total = g.ncells;
   a.cell_offsets = cell_offsets;
   a.perm = perm;
   a.Xs = Xs;
@@ -419,6 +424,105 @@ int fill_impl(const nl::Geometry& g, const double* Xs, const TI* perm, const TI*
   nl::launch_pairs<TI>(nl::kModeFill, a, num_sms(), st);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? NL_OK : cuda_fail(e, "launch fill kernel");
+}
+
+// --------------------------------------------------------------- batches --
+struct BatchLayout {
+  Layout L;  // the single-system layout for all atoms and cells of the batch
+  size_t geo, atom0, cell0, cs, first_all, end;
+};
+
+BatchLayout batch_layout(int64_t nat, int64_t ncells, int nsys) {
+  BatchLayout B;
+  B.L = layout(nat, ncells);
+  size_t o = B.L.end;
+  B.geo = o;
+  o += up(sizeof(nl::Geometry) * size_t(nsys));
+  B.atom0 = o;
+  o += up(sizeof(int) * size_t(nsys + 1));
+  B.cell0 = o;
+  o += up(sizeof(int) * size_t(nsys + 1));
+  B.cs = o;
+  o += up(sizeof(double) * size_t(nl::kCsTableDoubles) * size_t(nsys));
+  B.first_all = o;
+  o += up(sizeof(int64_t) * size_t(nat + 1));
+  B.end = o;
+  return B;
+}
+
+}  // namespace
+
+struct nl_batch {
+  int nsys = 0;
+  int index_bytes = 4;
+  int64_t nat = 0, ncells = 0;
+  std::vector<nl::Geometry> geo;
+  std::vector<int> atom0, cell0;
+  BatchLayout B;
+};
+
+namespace {
+
+template <typename TI>
+int batch_impl(const nl_batch& b, const double* X, TI* perm, double* Xs, TI* cell_id, TI* cell_offsets, TI* first,
+               long long* pair_offsets, int64_t capacity, TI* oi, TI* oj, TI* oS, double* oR, void* ws,
+               cudaStream_t st) {
+  const Layout& L = b.B.L;
+  const int sms = num_sms();
+  const int na = int(b.nat), nc = int(b.ncells);
+  cudaError_t e = cudaMemsetAsync(ws, 0, L.bend, st);  // err, stats, both zero regions
+  if (e != cudaSuccess) return cuda_fail(e, "memset workspace");
+  const nl::SysIndex si{at<nl::Geometry>(ws, b.B.geo), at<int>(ws, b.B.atom0), at<int>(ws, b.B.cell0), b.nsys};
+  int* cid = at<int>(ws, L.cid);
+  int* ticket = at<int>(ws, L.ticket);
+  float4* rec = at<float4>(ws, L.rec);
+  int* cell_count = at<int>(ws, L.cell_count);
+  int* cell_start = at<int>(ws, L.cell_start);
+  unsigned* err = at<unsigned>(ws, L.err);
+  int* bcount = at<int>(ws, L.bcount);
+  TI* first_all = at<TI>(ws, b.B.first_all);
+  nl::Geometry g0;
+  std::memset(&g0, 0, sizeof(g0));
+  // stage (a)/(b): bin, sort, cell offsets
+  nl::launch_bin(g0, si, X, na, cid, ticket, rec, cell_count, err, sms, st);
+  nl::launch_scan<TI>(cell_count, nc, nullptr, cell_start, at<unsigned long long>(ws, L.st_cells), bcount,
+                      at<long long>(ws, L.totals), err, st);
+  nl::launch_scatter(na, cid, ticket, cell_start, at<int>(ws, L.tmp), sms, st);
+  nl::launch_fix<TI>(si, na, at<int>(ws, L.tmp), cid, cell_start, X, rec, perm, cell_id, Xs,
+                     at<float4>(ws, L.rec_sorted), at<int>(ws, L.scell), at<int>(ws, L.big_list), bcount + 1, sms, st);
+  nl::launch_batch_cell_offsets<TI>(si, nc, cell_start, cell_offsets, sms, st);
+  // stage (c): count and per-atom offsets
+  nl::PairArgs<TI> a = pair_args<TI>(g0, cell_offsets, perm, Xs, ws, L);
+  a.geo = si.geo;
+  a.sys_atom = si.atom0;
+  a.sys_cell = si.cell0;
+  a.cs_sys = at<double>(ws, b.B.cs);
+  a.nsys = b.nsys;
+  a.nat_total = na;
+  a.ncells_total = nc;
+  a.counts = at<int>(ws, L.counts);
+  if (na > 0) {
+    nl::launch_pairs<TI>(nl::kModeCount, a, sms, st);
+    nl::launch_scan<TI>(at<int>(ws, L.counts), na, first_all, nullptr, at<unsigned long long>(ws, L.st_pairs),
+                        at<int>(ws, L.pcount), at<long long>(ws, L.totals) + 1, err, st);
+  } else {
+    static const TI one = 1;
+    e = cudaMemcpyAsync(first_all, &one, sizeof(TI), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(e, "empty batch");
+  }
+  nl::launch_batch_first<TI>(si, na, first_all, first, pair_offsets, sms, st);
+  // stage (d): pairs
+  if (na > 0 && capacity > 0) {
+    a.first = first_all;
+    a.oi = oi;
+    a.oj = oj;
+    a.oS = oS;
+    a.oR = oR;
+    a.capacity = capacity;
+    nl::launch_pairs<TI>(nl::kModeFill, a, sms, st);
+  }
+  e = cudaGetLastError();
+  return e == cudaSuccess ? NL_OK : cuda_fail(e, "launch batch kernels");
 }
 
 }  // namespace
@@ -606,6 +710,115 @@ int nl_lazy_reduce(const double* d_X_sorted, const void* d_perm, const void* d_c
     run(int64_t(0));
   e = cudaGetLastError();
   return e == cudaSuccess ? NL_OK : cuda_fail(e, "launch lazy kernel");
+}
+
+int nl_batch_create(const nl_system* systems, int nsys, int index_bytes, nl_batch** batch) {
+  if (!batch || (nsys > 0 && !systems)) return fail(NL_ERR_ARG, "null argument");
+  *batch = nullptr;
+  if (nsys < 1) return fail(NL_ERR_ARG, "a batch needs at least one system");
+  if (index_bytes != 4 && index_bytes != 8) return fail(NL_ERR_ARG, "index_bytes must be 4 or 8");
+  nl_batch* b = new (std::nothrow) nl_batch;
+  if (!b) return fail(NL_ERR_NOMEM, "cannot allocate the batch plan");
+  b->nsys = nsys;
+  b->index_bytes = index_bytes;
+  b->geo.resize(size_t(nsys));
+  b->atom0.resize(size_t(nsys) + 1);
+  b->cell0.resize(size_t(nsys) + 1);
+  int64_t na = 0, nc = 0;
+  for (int s = 0; s < nsys; ++s) {
+    const nl_system& y = systems[s];
+    Layout Ls;
+    int64_t nct;
+    // per-system checks of the single-system calls (a dummy workspace size)
+    int st = check_common(y.nat, y.ncells, y.nxyz, index_bytes, reinterpret_cast<void*>(1), ~size_t(0), Ls, nct);
+    if (st == NL_OK && (!(y.cutoff > 0) || !std::isfinite(y.cutoff))) st = fail(NL_ERR_ARG, "cutoff must be positive");
+    if (st) {
+      g_last_error = "system " + std::to_string(s) + ": " + g_last_error;
+      delete b;
+      return st;
+    }
+    b->atom0[size_t(s)] = int(na);
+    b->cell0[size_t(s)] = int(nc);
+    b->geo[size_t(s)] = make_geometry(y.cell, y.inv_cell, y.ncells, y.nxyz, y.pbc, y.cutoff, y.nat);
+    na += y.nat;
+    nc += nct;
+    if (na > 2147483646LL || nc + nsys > 2147483646LL) {
+      delete b;
+      return fail(NL_ERR_ARG, "a batch holds at most 2^31-2 atoms and 2^31-2 cells");
+    }
+  }
+  b->atom0[size_t(nsys)] = int(na);
+  b->cell0[size_t(nsys)] = int(nc);
+  b->nat = na;
+  b->ncells = nc;
+  b->B = batch_layout(na, nc, nsys);
+  *batch = b;
+  return NL_OK;
+}
+
+void nl_batch_destroy(nl_batch* batch) { delete batch; }
+
+size_t nl_batch_workspace_bytes(const nl_batch* batch) { return batch ? batch->B.end : 0; }
+
+int nl_batch_sizes(const nl_batch* batch, int64_t* total_atoms, int64_t* total_cells) {
+  if (!batch) return fail(NL_ERR_ARG, "null batch");
+  if (total_atoms) *total_atoms = batch->nat;
+  if (total_cells) *total_cells = batch->ncells;
+  return NL_OK;
+}
+
+int nl_batch_upload(const nl_batch* batch, void* d_workspace, size_t workspace_bytes, void* stream) {
+  if (!batch || !d_workspace) return fail(NL_ERR_ARG, "null argument");
+  if (workspace_bytes < batch->B.end) return fail(NL_ERR_NOMEM, "workspace too small (see nl_batch_workspace_bytes)");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const BatchLayout& B = batch->B;
+  // pageable sources: each copy returns once its source has been consumed
+  cudaError_t e = cudaMemcpyAsync(at<char>(d_workspace, B.geo), batch->geo.data(),
+                                  sizeof(nl::Geometry) * batch->geo.size(), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(at<char>(d_workspace, B.atom0), batch->atom0.data(), sizeof(int) * batch->atom0.size(),
+                        cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(at<char>(d_workspace, B.cell0), batch->cell0.data(), sizeof(int) * batch->cell0.size(),
+                        cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return cuda_fail(e, "upload batch tables");
+  nl::launch_cs_tables(at<nl::Geometry>(d_workspace, B.geo), batch->nsys, at<double>(d_workspace, B.cs), st);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  return e == cudaSuccess ? NL_OK : cuda_fail(e, "upload batch tables");
+}
+
+int nl_batch_neighbour_list(const nl_batch* batch, const double* d_X, void* d_perm, double* d_X_sorted,
+                            void* d_cell_id, void* d_cell_offsets, void* d_first, int64_t* d_pair_offsets,
+                            int64_t capacity, void* d_i, void* d_j, void* d_S, double* d_R, int64_t* total_pairs,
+                            void* d_workspace, size_t workspace_bytes, void* stream) {
+  if (!batch || !d_cell_offsets || !d_first || !d_pair_offsets || !d_workspace) return fail(NL_ERR_ARG, "null argument");
+  if (batch->nat > 0 && (!d_X || !d_perm || !d_X_sorted || !d_cell_id)) return fail(NL_ERR_ARG, "null argument");
+  if (capacity > 0 && (!d_i || !d_j || !d_S)) return fail(NL_ERR_ARG, "null argument");
+  if (workspace_bytes < batch->B.end) return fail(NL_ERR_NOMEM, "workspace too small (see nl_batch_workspace_bytes)");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int s;
+  if (batch->index_bytes == 4)
+    s = batch_impl<int32_t>(*batch, d_X, static_cast<int32_t*>(d_perm), d_X_sorted, static_cast<int32_t*>(d_cell_id),
+                            static_cast<int32_t*>(d_cell_offsets), static_cast<int32_t*>(d_first),
+                            reinterpret_cast<long long*>(d_pair_offsets), capacity, static_cast<int32_t*>(d_i),
+                            static_cast<int32_t*>(d_j), static_cast<int32_t*>(d_S), d_R, d_workspace, st);
+  else
+    s = batch_impl<int64_t>(*batch, d_X, static_cast<int64_t*>(d_perm), d_X_sorted, static_cast<int64_t*>(d_cell_id),
+                            static_cast<int64_t*>(d_cell_offsets), static_cast<int64_t*>(d_first),
+                            reinterpret_cast<long long*>(d_pair_offsets), capacity, static_cast<int64_t*>(d_i),
+                            static_cast<int64_t*>(d_j), static_cast<int64_t*>(d_S), d_R, d_workspace, st);
+  if (s) return s;
+  if (total_pairs) {
+    if (batch->nat == 0) {
+      *total_pairs = 0;
+      return sync_read(d_workspace, st, nullptr, nullptr);
+    }
+    s = sync_read(d_workspace, st, at<long long>(d_workspace, batch->B.L.totals) + 1, total_pairs);
+    if (s == NL_OK && *total_pairs > capacity) return fail(NL_ERR_CAPACITY, "pair buffers are smaller than the pair count");
+    return s;
+  }
+  return NL_OK;
 }
 
 int nl_sync_status(void* d_workspace, void* stream) {

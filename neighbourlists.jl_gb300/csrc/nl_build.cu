@@ -14,6 +14,7 @@
 // stable sortperm, so perm, the sorted positions and the sorted cell ids are
 // bit-identical to the reference's SortedCellList.
 #include "nl_build.cuh"
+#include "nl_pairs.cuh"
 
 namespace nl {
 
@@ -27,7 +28,8 @@ __device__ __forceinline__ unsigned lanemask_lt() {
 // One thread per atom (original order).  Writes the 0-based cell id, the
 // ticket (rank among the atoms of that cell that reached the histogram
 // first) and the FP32 cell-local record.
-__global__ void __launch_bounds__(256) k_bin(Geometry g, const double* __restrict__ X, int nat,
+template <bool BATCH>
+__global__ void __launch_bounds__(256) k_bin(Geometry g1, SysIndex si, const double* __restrict__ X, int nat,
                                              int* __restrict__ cid, int* __restrict__ ticket,
                                              float4* __restrict__ rec, int* __restrict__ cell_count,
                                              unsigned* __restrict__ err) {
@@ -39,9 +41,11 @@ __global__ void __launch_bounds__(256) k_bin(Geometry g, const double* __restric
     int c = 0;
     if (valid) {
       const double x0 = X[3LL * i + 0], x1 = X[3LL * i + 1], x2 = X[3LL * i + 2];
+      const int sys = BATCH ? batch_system(si.atom0, si.nsys, i) : 0;
+      const Geometry& g = BATCH ? si.geo[sys] : g1;
       Binned bn;
       if (!bin_fast(g, x0, x1, x2, bn) && !bin_position(g, x0, x1, x2, bn)) atomicOr(err, kFlagBadPosition);
-      c = linear_cell(g, bn.c[0], bn.c[1], bn.c[2]);
+      c = linear_cell(g, bn.c[0], bn.c[1], bn.c[2]) + (BATCH ? si.cell0[sys] : 0);
       rec[i] = make_record(g, bn);
       cid[i] = c;
     }
@@ -64,12 +68,19 @@ __global__ void __launch_bounds__(256) k_scatter(int nat, const int* __restrict_
 }
 
 template <typename TI>
-__device__ __forceinline__ void write_sorted(long long dst, int i, int c, const double* __restrict__ X,
-                                             const float4* __restrict__ rec, TI* __restrict__ perm,
-                                             TI* __restrict__ cell_id, double* __restrict__ Xs,
-                                             float4* __restrict__ rec_sorted, int* __restrict__ scell) {
-  perm[dst] = TI(i) + 1;
-  cell_id[dst] = TI(c) + 1;
+__device__ __forceinline__ void write_sorted(const SysIndex& si, long long dst, int i, int c,
+                                             const double* __restrict__ X, const float4* __restrict__ rec,
+                                             TI* __restrict__ perm, TI* __restrict__ cell_id,
+                                             double* __restrict__ Xs, float4* __restrict__ rec_sorted,
+                                             int* __restrict__ scell) {
+  int li = i, lc = c;
+  if (si.nsys > 0) {  // system-local indices
+    const int sys = batch_system(si.atom0, si.nsys, i);
+    li -= si.atom0[sys];
+    lc -= si.cell0[sys];
+  }
+  perm[dst] = TI(li) + 1;
+  cell_id[dst] = TI(lc) + 1;
   scell[dst] = c;
   Xs[3 * dst + 0] = X[3LL * i + 0];
   Xs[3 * dst + 1] = X[3LL * i + 1];
@@ -82,7 +93,7 @@ __device__ __forceinline__ void write_sorted(long long dst, int i, int c, const 
 // position of atom i is (cell start) + #{atoms of the cell with index < i}.
 // Larger cells are listed for k_fix_big.
 template <typename TI>
-__global__ void __launch_bounds__(256) k_fix(int nat, const int* __restrict__ tmp, const int* __restrict__ cid,
+__global__ void __launch_bounds__(256) k_fix(SysIndex si, int nat, const int* __restrict__ tmp, const int* __restrict__ cid,
                                              const int* __restrict__ cell_start, const double* __restrict__ X,
                                              const float4* __restrict__ rec, TI* __restrict__ perm,
                                              TI* __restrict__ cell_id, double* __restrict__ Xs,
@@ -99,7 +110,7 @@ __global__ void __launch_bounds__(256) k_fix(int nat, const int* __restrict__ tm
     }
     int rank = 0;
     for (int t = start; t < start + k; ++t) rank += tmp[t] < i;
-    write_sorted<TI>(start + rank, i, c, X, rec, perm, cell_id, Xs, rec_sorted, scell);
+    write_sorted<TI>(si, start + rank, i, c, X, rec, perm, cell_id, Xs, rec_sorted, scell);
   }
 }
 
@@ -108,7 +119,7 @@ __global__ void __launch_bounds__(256) k_fix(int nat, const int* __restrict__ tm
 // memory (bitonic); larger ones are rebuilt by a block-wide ordered scan over
 // all atoms (stable by construction).
 template <typename TI>
-__global__ void __launch_bounds__(kFixBigThreads) k_fix_big(int nat, const int* __restrict__ tmp,
+__global__ void __launch_bounds__(kFixBigThreads) k_fix_big(SysIndex si, int nat, const int* __restrict__ tmp,
                                                             const int* __restrict__ cid,
                                                             const int* __restrict__ cell_start,
                                                             const double* __restrict__ X,
@@ -146,7 +157,7 @@ __global__ void __launch_bounds__(kFixBigThreads) k_fix_big(int nat, const int* 
           __syncthreads();
         }
       for (int t = threadIdx.x; t < k; t += blockDim.x)
-        write_sorted<TI>(start + t, s[t], c, X, rec, perm, cell_id, Xs, rec_sorted, scell);
+        write_sorted<TI>(si, start + t, s[t], c, X, rec, perm, cell_id, Xs, rec_sorted, scell);
       __syncthreads();
     } else {
       int run = 0;
@@ -162,8 +173,9 @@ __global__ void __launch_bounds__(kFixBigThreads) k_fix_big(int nat, const int* 
           if (w < warp) before += s_warp[w];
           tot += s_warp[w];
         }
-        if (f) write_sorted<TI>(start + run + before + __popc(m & lanemask_lt()), i, c, X, rec, perm, cell_id, Xs,
-                                rec_sorted, scell);
+        if (f)
+          write_sorted<TI>(si, start + run + before + __popc(m & lanemask_lt()), i, c, X, rec, perm, cell_id, Xs,
+                           rec_sorted, scell);
         run += tot;
         __syncthreads();
       }
@@ -192,6 +204,44 @@ __global__ void __launch_bounds__(256) k_prepare(Geometry g, const double* __res
   }
 }
 
+// ----------------------------------------------------------------- batches --
+// largest s in [0, nsys) with first[s] + s <= e (first nondecreasing)
+__device__ __forceinline__ int batch_entry_system(const int* __restrict__ first, int nsys, long long e) {
+  int lo = 0, hi = nsys - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if ((long long)first[mid] + mid <= e)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+template <typename TI>
+__global__ void __launch_bounds__(256) k_batch_cell_offsets(SysIndex si, long long n_out,
+                                                            const int* __restrict__ cell_start,
+                                                            TI* __restrict__ cell_offsets) {
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n_out; e += (long long)gridDim.x * blockDim.x) {
+    const int s = batch_entry_system(si.cell0, si.nsys, e);
+    const long long k = e - si.cell0[s] - s;  // 0 .. ncells_s
+    cell_offsets[e] = TI(cell_start[si.cell0[s] + k] - si.atom0[s] + 1);
+  }
+}
+
+template <typename TI>
+__global__ void __launch_bounds__(256) k_batch_first(SysIndex si, long long n_out, const TI* __restrict__ first_all,
+                                                     TI* __restrict__ first, long long* __restrict__ pair_offsets) {
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n_out; e += (long long)gridDim.x * blockDim.x) {
+    const int s = batch_entry_system(si.atom0, si.nsys, e);
+    const long long k = e - si.atom0[s] - s;  // 0 .. nat_s
+    const long long base = (long long)first_all[si.atom0[s]] - 1;
+    first[e] = TI((long long)first_all[si.atom0[s] + k] - base);
+    if (k == 0) pair_offsets[s] = base;
+    if (e == n_out - 1) pair_offsets[si.nsys] = (long long)first_all[si.atom0[si.nsys]] - 1;
+  }
+}
+
 // ------------------------------------------------------------- launchers --
 static inline int grid_for(long long n, int block, int max_blocks) {
   long long g = (n + block - 1) / block;
@@ -199,10 +249,29 @@ static inline int grid_for(long long n, int block, int max_blocks) {
   return g < 1 ? 1 : int(g);
 }
 
-void launch_bin(const Geometry& g, const double* X, int nat, int* cid, int* ticket, float4* rec, int* cell_count,
-                unsigned* err, int num_sms, cudaStream_t st) {
+void launch_bin(const Geometry& g, const SysIndex& si, const double* X, int nat, int* cid, int* ticket, float4* rec,
+                int* cell_count, unsigned* err, int num_sms, cudaStream_t st) {
   if (nat <= 0) return;
-  k_bin<<<grid_for(nat, 256, num_sms * 8), 256, 0, st>>>(g, X, nat, cid, ticket, rec, cell_count, err);
+  if (si.nsys > 0)
+    k_bin<true><<<grid_for(nat, 256, num_sms * 8), 256, 0, st>>>(g, si, X, nat, cid, ticket, rec, cell_count, err);
+  else
+    k_bin<false><<<grid_for(nat, 256, num_sms * 8), 256, 0, st>>>(g, si, X, nat, cid, ticket, rec, cell_count, err);
+}
+
+template <typename TI>
+void launch_batch_cell_offsets(const SysIndex& si, int ncells_total, const int* cell_start, TI* cell_offsets,
+                               int num_sms, cudaStream_t st) {
+  const long long n = (long long)ncells_total + si.nsys;
+  if (si.nsys <= 0 || n <= 0) return;
+  k_batch_cell_offsets<TI><<<grid_for(n, 256, num_sms * 8), 256, 0, st>>>(si, n, cell_start, cell_offsets);
+}
+
+template <typename TI>
+void launch_batch_first(const SysIndex& si, int nat_total, const TI* first_all, TI* first, long long* pair_offsets,
+                        int num_sms, cudaStream_t st) {
+  const long long n = (long long)nat_total + si.nsys;
+  if (si.nsys <= 0) return;
+  k_batch_first<TI><<<grid_for(n, 256, num_sms * 8), 256, 0, st>>>(si, n, first_all, first, pair_offsets);
 }
 
 void launch_scatter(int nat, const int* cid, const int* ticket, const int* cell_start, int* tmp, int num_sms,
@@ -212,14 +281,14 @@ void launch_scatter(int nat, const int* cid, const int* ticket, const int* cell_
 }
 
 template <typename TI>
-void launch_fix(int nat, const int* tmp, const int* cid, const int* cell_start, const double* X, const float4* rec,
-                TI* perm, TI* cell_id, double* Xs, float4* rec_sorted, int* scell, int* big_list, int* big_count,
-                int num_sms, cudaStream_t st) {
+void launch_fix(const SysIndex& si, int nat, const int* tmp, const int* cid, const int* cell_start, const double* X,
+                const float4* rec, TI* perm, TI* cell_id, double* Xs, float4* rec_sorted, int* scell, int* big_list,
+                int* big_count, int num_sms, cudaStream_t st) {
   if (nat <= 0) return;
-  k_fix<TI><<<grid_for(nat, 256, num_sms * 8), 256, 0, st>>>(nat, tmp, cid, cell_start, X, rec, perm, cell_id, Xs,
+  k_fix<TI><<<grid_for(nat, 256, num_sms * 8), 256, 0, st>>>(si, nat, tmp, cid, cell_start, X, rec, perm, cell_id, Xs,
                                                              rec_sorted, scell, big_list, big_count);
-  k_fix_big<TI><<<num_sms, kFixBigThreads, 0, st>>>(nat, tmp, cid, cell_start, X, rec, perm, cell_id, Xs, rec_sorted,
-                                                     scell, big_list, big_count);
+  k_fix_big<TI><<<num_sms, kFixBigThreads, 0, st>>>(si, nat, tmp, cid, cell_start, X, rec, perm, cell_id, Xs,
+                                                     rec_sorted, scell, big_list, big_count);
 }
 
 template <typename TI>
@@ -237,8 +306,10 @@ void launch_scan(const int* in, long long n, TI* out1, int* out0, unsigned long 
 }
 
 #define NL_INST(TI)                                                                                                  \
-  template void launch_fix<TI>(int, const int*, const int*, const int*, const double*, const float4*, TI*, TI*,     \
-                               double*, float4*, int*, int*, int*, int, cudaStream_t);                              \
+  template void launch_fix<TI>(const SysIndex&, int, const int*, const int*, const int*, const double*,            \
+                               const float4*, TI*, TI*, double*, float4*, int*, int*, int*, int, cudaStream_t);     \
+  template void launch_batch_cell_offsets<TI>(const SysIndex&, int, const int*, TI*, int, cudaStream_t);            \
+  template void launch_batch_first<TI>(const SysIndex&, int, const TI*, TI*, long long*, int, cudaStream_t);        \
   template void launch_prepare<TI>(const Geometry&, const double*, const TI*, const TI*, int, float4*, int*,     \
                                    unsigned*, int, cudaStream_t);                                                   \
   template void launch_scan<TI>(const int*, long long, TI*, int*, unsigned long long*, int*, long long*, unsigned*, \

@@ -174,8 +174,8 @@ __device__ __forceinline__ bool exact_pair(const Geometry& g, const double* Xs, 
 
 // Processes n <= 32 queued pairs starting at ring position head.
 template <typename TI, int MODE>
-__device__ __forceinline__ void flush_ring(const PairArgs<TI>& A, const double* cs_tab, WarpSmem& W, int head, int n,
-                                           int lane) {
+__device__ __forceinline__ void flush_ring(const PairArgs<TI>& A, const Geometry& g, const double* cs_tab, WarpSmem& W,
+                                           int head, int n, int lane) {
   const bool act = lane < n;
   const int rp = (head + lane) & (kRing - 1);
   const int e = act ? W.rent[rp] : 0;
@@ -189,7 +189,7 @@ __device__ __forceinline__ void flush_ring(const PairArgs<TI>& A, const double* 
     xj[0] = A.Xs[3LL * slot_j + 0];
     xj[1] = A.Xs[3LL * slot_j + 1];
     xj[2] = A.Xs[3LL * slot_j + 2];
-    pair_S(A.g, xi, xj, mi, cw, S);
+    pair_S(g, xi, xj, mi, cw, S);
   } else {
     xj[0] = xj[1] = xj[2] = 0.0;
   }
@@ -199,14 +199,14 @@ __device__ __forceinline__ void flush_ring(const PairArgs<TI>& A, const double* 
     if (act && !wr) atomicOr(A.err, kFlagCapacity);
     if (wr) {
       A.oi[out] = TI(W.horig[a]) + 1;
-      A.oj[out] = TI(clampi(A.perm[slot_j] - 1, A.g.nat - 1)) + 1;
+      A.oj[out] = TI(clampi(A.perm[slot_j] - 1, g.nat - 1)) + 1;
       A.oS[3 * out + 0] = TI(S[0]);
       A.oS[3 * out + 1] = TI(S[1]);
       A.oS[3 * out + 2] = TI(S[2]);
     }
     if (A.oR) {
       double R[3];
-      pair_R(A.g, cs_tab, xi, xj, S[0], S[1], S[2], act, R);
+      pair_R(g, cs_tab, xi, xj, S[0], S[1], S[2], act, R);
       if (wr) {
         A.oR[3 * out + 0] = R[0];
         A.oR[3 * out + 1] = R[1];
@@ -215,7 +215,7 @@ __device__ __forceinline__ void flush_ring(const PairArgs<TI>& A, const double* 
     }
   } else {  // lazy: f(R) = 1 / ((r2*r2)*r2)
     double R[3];
-    pair_R(A.g, cs_tab, xi, xj, S[0], S[1], S[2], act, R);
+    pair_R(g, cs_tab, xi, xj, S[0], S[1], S[2], act, R);
     if (act) {
       const double r2 = dot_ref(R);
       W.rval[lane] = __ddiv_rn(1.0, dmul(dmul(r2, r2), r2));
@@ -243,6 +243,18 @@ __global__ void k_cs_table(Geometry g, double* __restrict__ out) {
   }
 }
 
+// Batches: one block per system.
+__global__ void k_cs_tables(const Geometry* __restrict__ geo, double* __restrict__ out) {
+  const Geometry& g = geo[blockIdx.x];
+  double* o = out + 3 * kCsN * kCsN * kCsN * (long long)blockIdx.x;
+  for (int t = threadIdx.x; t < kCsN * kCsN * kCsN; t += blockDim.x) {
+    const int s0 = t % kCsN - kCsR, s1 = (t / kCsN) % kCsN - kCsR, s2 = t / (kCsN * kCsN) - kCsR;
+    o[3 * t + 0] = cts_k(g.C, s0, s1, s2, 0);
+    o[3 * t + 1] = cts_k(g.C, s0, s1, s2, 1);
+    o[3 * t + 2] = cts_k(g.C, s0, s1, s2, 2);
+  }
+}
+
 // wrap_shift without a division for the common case of an index already
 // inside [1, n]
 __device__ __forceinline__ int wrap_shift_fast(int i, int n, int pbc, int& s) {
@@ -258,10 +270,10 @@ constexpr int kStencilTab = 512;  // stencil offsets tabulated per block up to t
 // Stencil cell q of home cell (hc0, hc1, hc2): its 0-based linear index (or
 // -1 when it falls outside an open axis), packed loop shift and FP32 offset
 // d.b of its lower corner from the home corner.
-__device__ __forceinline__ int stencil_cell(const Geometry& g, const unsigned* dtab, int sx, int sy, int hc0, int hc1,
-                                            int hc2, int q, unsigned& slp, float& ox, float& oy, float& oz) {
+__device__ __forceinline__ int stencil_cell(const Geometry& g, const unsigned* dtab, int tabn, int sx, int sy, int hc0,
+                                            int hc1, int hc2, int q, unsigned& slp, float& ox, float& oy, float& oz) {
   int d0, d1, d2;
-  if (q < kStencilTab) {
+  if (q < tabn) {
     const unsigned dq = dtab[q];
     d0 = unpack3(dq, 0);
     d1 = unpack3(dq, 1);
@@ -287,49 +299,85 @@ __device__ __forceinline__ int stencil_cell(const Geometry& g, const unsigned* d
   return linear_cell(g, c0, c1, c2);
 }
 
-template <typename TI, int MODE>
+// Per-warp view of the system that owns a home cell (batches: every warp
+// copies its current system's geometry and stencil table to shared memory).
+template <bool BATCH>
+struct SysView {
+  int s = 0;      // system index
+  int abase = 0;  // first global slot / original atom of the system
+  int coff = 0;   // index of the system's cell 0 in cell_offsets
+  int hl = 0;     // home cell within the system
+};
+
+template <typename TI, bool BATCH>
+__device__ __forceinline__ void load_system(const PairArgs<TI>& A, int s, Geometry& gw, unsigned* wtab, int lane) {
+  __syncwarp();
+  const int* src = reinterpret_cast<const int*>(A.geo + s);
+  int* dst = reinterpret_cast<int*>(&gw);
+  for (int k = lane; k < int(sizeof(Geometry) / 4); k += 32) dst[k] = src[k];
+  __syncwarp();
+  const int sx = 2 * gw.nxyz[0] + 1, sy = 2 * gw.nxyz[1] + 1, sz = 2 * gw.nxyz[2] + 1;
+  if (lane < sx * sy * sz)
+    wtab[lane] = pack3(lane % sx - gw.nxyz[0], (lane / sx) % sy - gw.nxyz[1], lane / (sx * sy) - gw.nxyz[2]);
+  __syncwarp();
+}
+
+template <typename TI, int MODE, bool BATCH>
 __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<TI> A) {
   __shared__ WarpSmem sm[kPairWarps];
-  __shared__ double cs_tab[3 * kCsN * kCsN * kCsN];
-  __shared__ unsigned dtab[kStencilTab];  // packed (d0, d1, d2) of stencil cell q
-  const Geometry& g = A.g;
-  if (MODE != kModeCount)
-    for (int t = threadIdx.x; t < 3 * kCsN * kCsN * kCsN; t += blockDim.x) cs_tab[t] = A.cs_table[t];
-  {
+  __shared__ double cs_blk[BATCH ? 1 : 3 * kCsN * kCsN * kCsN];
+  __shared__ unsigned dtab_blk[BATCH ? 32 * kPairWarps : kStencilTab];  // packed (d0, d1, d2) of stencil cell q
+  __shared__ Geometry geo_w[BATCH ? kPairWarps : 1];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const Geometry& g = BATCH ? geo_w[warp] : A.g;
+  const unsigned* dtab = BATCH ? dtab_blk + 32 * warp : dtab_blk;
+  constexpr int tabn = BATCH ? 32 : kStencilTab;
+  if (!BATCH) {
+    if (MODE != kModeCount)
+      for (int t = threadIdx.x; t < 3 * kCsN * kCsN * kCsN; t += blockDim.x) cs_blk[t] = A.cs_table[t];
     const int tx = 2 * g.nxyz[0] + 1, ty = 2 * g.nxyz[1] + 1;
     const int tn = min(kStencilTab, tx * ty * (2 * g.nxyz[2] + 1));
     for (int t = threadIdx.x; t < tn; t += blockDim.x)
-      dtab[t] = pack3(t % tx - g.nxyz[0], (t / tx) % ty - g.nxyz[1], t / (tx * ty) - g.nxyz[2]);
+      dtab_blk[t] = pack3(t % tx - g.nxyz[0], (t / tx) % ty - g.nxyz[1], t / (tx * ty) - g.nxyz[2]);
+    __syncthreads();
   }
-  __syncthreads();
+  const double* cs_tab = cs_blk;
 
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   WarpSmem& W = sm[warp];
   const int nwarps = gridDim.x * kPairWarps;
-  const int sx = 2 * g.nxyz[0] + 1, sy = 2 * g.nxyz[1] + 1, sz = 2 * g.nxyz[2] + 1;
-  const int nst = sx * sy * sz;
-  const int center = g.nxyz[0] + sx * (g.nxyz[1] + sy * g.nxyz[2]);
-  const float lo = g.lo, hi = g.hi;
+  int sx = 0, sy = 0, nst = 0, center = 0;
+  float lo = 0.f, hi = 0.f;
+  auto set_stencil = [&]() {
+    sx = 2 * g.nxyz[0] + 1;
+    sy = 2 * g.nxyz[1] + 1;
+    nst = sx * sy * (2 * g.nxyz[2] + 1);
+    center = g.nxyz[0] + sx * (g.nxyz[1] + sy * g.nxyz[2]);
+    lo = g.lo;
+    hi = g.hi;
+  };
+  if (!BATCH) set_stencil();
+  int cur_sys = -1;
   unsigned rechecks = 0;
 
-  // Ranges of the next cell are prefetched one cell ahead: its home range and,
-  // per lane, the range of its stencil cell in the first group of 32.
+  // Single systems prefetch the ranges of the next cell one cell ahead: its
+  // home range and, per lane, the range of its stencil cell in the first
+  // group of 32.
   // The fill pass visits only the cells that the count pass could not mask
   // (k_emit writes the others); count and lazy visit every cell.
-  const int ncell_iter = MODE == kModeFill ? min(*A.n_unmasked, g.ncells) : g.ncells;
-  auto cell_at = [&](int idx) { return MODE == kModeFill ? clampi(A.unmasked[idx], g.ncells - 1) : idx; };
+  const int ncell_iter = MODE == kModeFill ? min(*A.n_unmasked, A.ncells_total) : A.ncells_total;
+  auto cell_at = [&](int idx) { return MODE == kModeFill ? clampi(A.unmasked[idx], A.ncells_total - 1) : idx; };
   int idx = blockIdx.x * kPairWarps + warp;
   // (0-based slot offsets, clamped to [0, nat])
   int pf_hs = 0, pf_he = 0, pf_lo = 0, pf_hi = 0;
   auto prefetch = [&](int pidx) {
-    if (pidx >= ncell_iter) return;
+    if (BATCH || pidx >= ncell_iter) return;
     const int hh = cell_at(pidx);
     pf_hs = clampi(A.cell_offsets[hh] - 1, g.nat);
     pf_he = clampi(A.cell_offsets[hh + 1] - 1, g.nat);
     const int c0 = hh % g.ns[0] + 1, c1 = (hh / g.ns[0]) % g.ns[1] + 1, c2 = hh / (g.ns[0] * g.ns[1]) + 1;
     unsigned sl;
     float a, b, c;
-    const int lin = lane < nst ? stencil_cell(g, dtab, sx, sy, c0, c1, c2, lane, sl, a, b, c) : -1;
+    const int lin = lane < nst ? stencil_cell(g, dtab, tabn, sx, sy, c0, c1, c2, lane, sl, a, b, c) : -1;
     pf_lo = lin >= 0 ? clampi(A.cell_offsets[lin] - 1, g.nat) : 0;
     pf_hi = lin >= 0 ? clampi(A.cell_offsets[lin + 1] - 1, g.nat) : 0;
   };
@@ -338,11 +386,28 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
     const int h = cell_at(idx);
     // offsets are clamped to [0, nat] so that a malformed cell list (which
     // the prepare pass reports as inconsistent) never indexes out of bounds
-    const int hs = pf_hs, he = pf_he;
+    int hs = pf_hs, he = pf_he;
     const int g0_lo = pf_lo, g0_hi = pf_hi;
+    SysView<BATCH> sv;
+    sv.hl = h;
+    if constexpr (BATCH) {
+      sv.s = batch_system(A.sys_cell, A.nsys, h);
+      if (sv.s != cur_sys) {
+        load_system<TI, BATCH>(A, sv.s, geo_w[warp], dtab_blk + 32 * warp, lane);
+        set_stencil();
+        cur_sys = sv.s;
+      }
+      cs_tab = A.cs_sys + 3 * kCsN * kCsN * kCsN * (long long)sv.s;
+      sv.abase = A.sys_atom[sv.s];
+      sv.coff = A.sys_cell[sv.s] + sv.s;
+      sv.hl = h - A.sys_cell[sv.s];
+      hs = clampi(A.cell_offsets[sv.coff + sv.hl] - 1 + sv.abase, A.nat_total);
+      he = clampi(A.cell_offsets[sv.coff + sv.hl + 1] - 1 + sv.abase, A.nat_total);
+    }
     prefetch(idx + nwarps);  // loads in flight while this cell is processed
     if (hs >= he) continue;
-    const int hc0 = h % g.ns[0] + 1, hc1 = (h / g.ns[0]) % g.ns[1] + 1, hc2 = h / (g.ns[0] * g.ns[1]) + 1;
+    const int hl = sv.hl;
+    const int hc0 = hl % g.ns[0] + 1, hc1 = (hl / g.ns[0]) % g.ns[1] + 1, hc2 = hl / (g.ns[0] * g.ns[1]) + 1;
 
     for (int hb = hs; hb < he; hb += 32) {
       const int nb = min(32, he - hb);
@@ -356,10 +421,11 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
         unsigned slp = 0;
         float ox = 0.f, oy = 0.f, oz = 0.f;
         if (q < nst) {
-          const int lin = stencil_cell(g, dtab, sx, sy, hc0, hc1, hc2, q, slp, ox, oy, oz);
+          const int lin = stencil_cell(g, dtab, tabn, sx, sy, hc0, hc1, hc2, q, slp, ox, oy, oz);
           if (lin >= 0) {
-            cstart = gb == 0 ? g0_lo : clampi(A.cell_offsets[lin] - 1, g.nat);
-            const int cend = gb == 0 ? g0_hi : clampi(A.cell_offsets[lin + 1] - 1, g.nat);
+            const bool pre = !BATCH && gb == 0;
+            cstart = pre ? g0_lo : clampi(A.cell_offsets[sv.coff + lin] - 1 + sv.abase, A.nat_total);
+            const int cend = pre ? g0_hi : clampi(A.cell_offsets[sv.coff + lin + 1] - 1 + sv.abase, A.nat_total);
             ccount = max(cend - cstart, 0);
           }
         }
@@ -375,7 +441,7 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
         const bool masked = nst <= 32 && tg <= 32 * kMaskWords;
         if (MODE == kModeCount && !masked && gb == 0 && hb == hs && lane == 0) {
           const int u = atomicAdd(A.n_unmasked, 1);
-          if (u < g.ncells) A.unmasked[u] = h;
+          if (u < A.ncells_total) A.unmasked[u] = h;
         }
         const int cl = center - gb;  // home cell (center of the stencil) in this group?
         const int center_excl = (cl >= 0 && cl < 32) ? __shfl_sync(0xffffffffu, incl - ccount, cl & 31) : -1;
@@ -383,7 +449,7 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
         for (int cb = 0; cb < tg || (gb == 0 && cb == 0); cb += kChunk) {
           const int nch = min(kChunk, tg - cb);
           if (MODE != kModeCount && tail > head) {  // queued pairs refer to the previous chunk
-            flush_ring<TI, MODE>(A, cs_tab, W, head, tail - head, lane);
+            flush_ring<TI, MODE>(A, g, cs_tab, W, head, tail - head, lane);
             head = tail;
           }
           __syncwarp();
@@ -403,7 +469,7 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
                 W.hx[lane][1] = A.Xs[3LL * s + 1];
                 W.hx[lane][2] = A.Xs[3LL * s + 2];
               }
-              W.hnext[lane] = MODE == kModeFill ? (long long)A.first[orig] - 1 : 0;
+              W.hnext[lane] = MODE == kModeFill ? (long long)A.first[sv.abase + orig] - 1 : 0;
               if (MODE == kModeLazyR6) W.hacc[lane] = 0.0;
             }
           }
@@ -518,7 +584,7 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
                   next[k] += np;
                   if (tail - head >= 32) {
                     __syncwarp();
-                    flush_ring<TI, MODE>(A, cs_tab, W, head, 32, lane);
+                    flush_ring<TI, MODE>(A, g, cs_tab, W, head, 32, lane);
                     head += 32;
                   }
                 }
@@ -541,11 +607,11 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
           }
         }
       }
-      if (MODE != kModeCount && tail > head) flush_ring<TI, MODE>(A, cs_tab, W, head, tail - head, lane);
+      if (MODE != kModeCount && tail > head) flush_ring<TI, MODE>(A, g, cs_tab, W, head, tail - head, lane);
       __syncwarp();
       if (lane < nb) {
-        if (MODE == kModeCount) A.counts[W.horig[lane]] = int(W.hnext[lane]);
-        if (MODE == kModeLazyR6) A.per_atom[W.horig[lane]] = W.hacc[lane];
+        if (MODE == kModeCount) A.counts[sv.abase + W.horig[lane]] = int(W.hnext[lane]);
+        if (MODE == kModeLazyR6) A.per_atom[sv.abase + W.horig[lane]] = W.hacc[lane];
       }
       __syncwarp();
     }
@@ -564,7 +630,11 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
 // and lane r resolves and writes the atom's r-th pair.  The output slots
 // first[i] + r are consecutive, so the stores coalesce.  Candidate f maps to
 // its stencil cell through a per-cell byte table.
+#ifndef NL_EMIT_MIN_BLOCKS
+#define NL_EMIT_MIN_BLOCKS 8
+#endif
 constexpr int kEmitWarps = 4;
+constexpr int kEmitMinBlocks = NL_EMIT_MIN_BLOCKS;  // resident blocks per SM the register budget targets
 constexpr int kEmitCand = 32 * kMaskWords;  // candidates a masked cell may have
 
 struct __align__(16) EmitSmem {
@@ -596,35 +666,58 @@ __device__ __forceinline__ int nth_set_bit(unsigned m, int k) {
   return pos;
 }
 
-template <typename TI>
-__global__ void __launch_bounds__(kEmitWarps * 32) k_emit(PairArgs<TI> A) {
+template <typename TI, bool BATCH>
+__global__ void __launch_bounds__(kEmitWarps * 32, kEmitMinBlocks) k_emit(PairArgs<TI> A) {
   __shared__ EmitSmem es[kEmitWarps];
-  __shared__ double cs_tab[3 * kCsN * kCsN * kCsN];
-  __shared__ unsigned dtab[kStencilTab];
-  const Geometry& g = A.g;
-  const int sx = 2 * g.nxyz[0] + 1, sy = 2 * g.nxyz[1] + 1, sz = 2 * g.nxyz[2] + 1;
-  const int nst = sx * sy * sz;
-  if (nst > 32) return;  // no cell of this system is masked (uniform over the grid)
-  for (int t = threadIdx.x; t < 3 * kCsN * kCsN * kCsN; t += blockDim.x) cs_tab[t] = A.cs_table[t];
-  for (int t = threadIdx.x; t < nst; t += blockDim.x)
-    dtab[t] = pack3(t % sx - g.nxyz[0], (t / sx) % sy - g.nxyz[1], t / (sx * sy) - g.nxyz[2]);
-  __syncthreads();
-
+  __shared__ double cs_blk[BATCH ? 1 : 3 * kCsN * kCsN * kCsN];
+  __shared__ unsigned dtab_blk[32 * (BATCH ? kEmitWarps : 1)];
+  __shared__ Geometry geo_w[BATCH ? kEmitWarps : 1];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const Geometry& g = BATCH ? geo_w[warp] : A.g;
+  const unsigned* dtab = BATCH ? dtab_blk + 32 * warp : dtab_blk;
+  int sx = 2 * g.nxyz[0] + 1, sy = 2 * g.nxyz[1] + 1;
+  int nst = sx * sy * (2 * g.nxyz[2] + 1);
+  if (!BATCH) {
+    if (nst > 32) return;  // no cell of this system is masked (uniform over the grid)
+    for (int t = threadIdx.x; t < 3 * kCsN * kCsN * kCsN; t += blockDim.x) cs_blk[t] = A.cs_table[t];
+    for (int t = threadIdx.x; t < nst; t += blockDim.x)
+      dtab_blk[t] = pack3(t % sx - g.nxyz[0], (t / sx) % sy - g.nxyz[1], t / (sx * sy) - g.nxyz[2]);
+    __syncthreads();
+  }
+  const double* cs_tab = cs_blk;
+  int cur_sys = -1;
+
   EmitSmem& E = es[warp];
   const int nwarps = gridDim.x * kEmitWarps;
-  for (int h = blockIdx.x * kEmitWarps + warp; h < g.ncells; h += nwarps) {
-    const int hs = clampi(A.cell_offsets[h] - 1, g.nat), he = clampi(A.cell_offsets[h + 1] - 1, g.nat);
+  for (int h = blockIdx.x * kEmitWarps + warp; h < A.ncells_total; h += nwarps) {
+    int abase = 0, coff = 0, hl = h;
+    if constexpr (BATCH) {
+      const int s = batch_system(A.sys_cell, A.nsys, h);
+      if (s != cur_sys) {
+        load_system<TI, BATCH>(A, s, geo_w[warp], dtab_blk + 32 * warp, lane);
+        sx = 2 * g.nxyz[0] + 1;
+        sy = 2 * g.nxyz[1] + 1;
+        nst = sx * sy * (2 * g.nxyz[2] + 1);
+        cur_sys = s;
+      }
+      if (nst > 32) continue;  // left to the screening fill
+      cs_tab = A.cs_sys + 3 * kCsN * kCsN * kCsN * (long long)s;
+      abase = A.sys_atom[s];
+      coff = A.sys_cell[s] + s;
+      hl = h - A.sys_cell[s];
+    }
+    const int hs = clampi(A.cell_offsets[coff + hl] - 1 + abase, A.nat_total);
+    const int he = clampi(A.cell_offsets[coff + hl + 1] - 1 + abase, A.nat_total);
     if (hs >= he) continue;
-    const int hc0 = h % g.ns[0] + 1, hc1 = (h / g.ns[0]) % g.ns[1] + 1, hc2 = h / (g.ns[0] * g.ns[1]) + 1;
+    const int hc0 = hl % g.ns[0] + 1, hc1 = (hl / g.ns[0]) % g.ns[1] + 1, hc2 = hl / (g.ns[0] * g.ns[1]) + 1;
     int cstart = 0, ccount = 0;
     unsigned slp = 0;
     if (lane < nst) {
       float ox, oy, oz;
-      const int lin = stencil_cell(g, dtab, sx, sy, hc0, hc1, hc2, lane, slp, ox, oy, oz);
+      const int lin = stencil_cell(g, dtab, 32, sx, sy, hc0, hc1, hc2, lane, slp, ox, oy, oz);
       if (lin >= 0) {
-        cstart = clampi(A.cell_offsets[lin] - 1, g.nat);
-        ccount = max(clampi(A.cell_offsets[lin + 1] - 1, g.nat) - cstart, 0);
+        cstart = clampi(A.cell_offsets[coff + lin] - 1 + abase, A.nat_total);
+        ccount = max(clampi(A.cell_offsets[coff + lin + 1] - 1 + abase, A.nat_total) - cstart, 0);
       }
     }
     int incl = ccount;
@@ -649,17 +742,19 @@ __global__ void __launch_bounds__(kEmitWarps * 32) k_emit(PairArgs<TI> A) {
         const int si = hb + lane;
         const int orig = clampi(A.perm[si] - 1, g.nat - 1);
         E.horig[lane] = orig;
-        E.hbase[lane] = (long long)A.first[orig] - 1;
+        E.hbase[lane] = (long long)A.first[abase + orig] - 1;
         E.hmeta[lane] = __float_as_uint(A.rec[si].w);
         E.hx[lane][0] = A.Xs[3LL * si + 0];
         E.hx[lane][1] = A.Xs[3LL * si + 1];
         E.hx[lane][2] = A.Xs[3LL * si + 2];
       }
       __syncwarp();
+      // the atom's acceptance words (bit f = candidate f), one atom ahead
+      unsigned m_next = lane < nw ? A.masks[(long long)hb * kMaskWords + lane] : 0u;
       for (int a = 0; a < nb; ++a) {
-        // the atom's acceptance words (bit f = candidate f) and their
-        // inclusive prefix of set bits over lanes 0..15 (nw <= 12)
-        const unsigned m = lane < nw ? A.masks[(long long)(hb + a) * kMaskWords + lane] : 0u;
+        const unsigned m = m_next;
+        if (a + 1 < nb && lane < nw) m_next = A.masks[(long long)(hb + a + 1) * kMaskWords + lane];
+        // inclusive prefix of the words' set bits over lanes 0..15 (nw <= 12)
         int wincl = __popc(m);
 #pragma unroll
         for (int o = 1; o < 16; o <<= 1) {
@@ -687,7 +782,7 @@ __global__ void __launch_bounds__(kEmitWarps * 32) k_emit(PairArgs<TI> A) {
           const int wex = __shfl_sync(0xffffffffu, wincl, w) - __popc(mw);
           const int f = 32 * w + nth_set_bit(mw, rr - wex);  // w < nw, so f < kEmitCand
           const int q = E.cq[f];
-          const int slot_j = clampi(E.qstart[q] + f - E.qexcl[q], g.nat - 1);
+          const int slot_j = clampi(E.qstart[q] + f - E.qexcl[q], A.nat_total - 1);
           const unsigned mj = __float_as_uint(A.rec[slot_j].w);
           double xj[3];
           xj[0] = A.Xs[3LL * slot_j + 0];
@@ -721,27 +816,39 @@ __global__ void __launch_bounds__(kEmitWarps * 32) k_emit(PairArgs<TI> A) {
   }
 }
 
-template <typename TI>
-void launch_pairs(int mode, const PairArgs<TI>& a, int num_sms, cudaStream_t st) {
-  if (a.g.nat <= 0 || a.g.ncells <= 0) return;
-  long long blocks = ((long long)a.g.ncells + kPairWarps - 1) / kPairWarps;
+template <typename TI, bool BATCH>
+static void launch_modes(int mode, const PairArgs<TI>& a, int num_sms, cudaStream_t st) {
+  if (a.nat_total <= 0 || a.ncells_total <= 0) return;
+  long long blocks = ((long long)a.ncells_total + kPairWarps - 1) / kPairWarps;
   if (blocks > (long long)num_sms * kMinBlocks) blocks = (long long)num_sms * kMinBlocks;
   if (blocks < 1) blocks = 1;
   switch (mode) {
-    case kModeCount: k_pairs<TI, kModeCount><<<int(blocks), kPairWarps * 32, 0, st>>>(a); break;
+    case kModeCount: k_pairs<TI, kModeCount, BATCH><<<int(blocks), kPairWarps * 32, 0, st>>>(a); break;
     case kModeFill: {
-      k_cs_table<<<1, 128, 0, st>>>(a.g, a.cs_table);
-      long long eb = ((long long)a.g.ncells + kEmitWarps - 1) / kEmitWarps;
+      if (!BATCH) k_cs_table<<<1, 128, 0, st>>>(a.g, a.cs_table);
+      long long eb = ((long long)a.ncells_total + kEmitWarps - 1) / kEmitWarps;
       if (eb > (long long)num_sms * 16) eb = (long long)num_sms * 16;
-      k_emit<TI><<<int(eb), kEmitWarps * 32, 0, st>>>(a);
-      k_pairs<TI, kModeFill><<<int(blocks), kPairWarps * 32, 0, st>>>(a);
+      k_emit<TI, BATCH><<<int(eb), kEmitWarps * 32, 0, st>>>(a);
+      k_pairs<TI, kModeFill, BATCH><<<int(blocks), kPairWarps * 32, 0, st>>>(a);
       break;
     }
     default:
-      k_cs_table<<<1, 128, 0, st>>>(a.g, a.cs_table);
-      k_pairs<TI, kModeLazyR6><<<int(blocks), kPairWarps * 32, 0, st>>>(a);
+      if (!BATCH) k_cs_table<<<1, 128, 0, st>>>(a.g, a.cs_table);
+      k_pairs<TI, kModeLazyR6, BATCH><<<int(blocks), kPairWarps * 32, 0, st>>>(a);
       break;
   }
+}
+
+template <typename TI>
+void launch_pairs(int mode, const PairArgs<TI>& a, int num_sms, cudaStream_t st) {
+  if (a.nsys > 0)
+    launch_modes<TI, true>(mode, a, num_sms, st);
+  else
+    launch_modes<TI, false>(mode, a, num_sms, st);
+}
+
+void launch_cs_tables(const Geometry* geo, int nsys, double* out, cudaStream_t st) {
+  if (nsys > 0) k_cs_tables<<<nsys, 128, 0, st>>>(geo, out);
 }
 
 template void launch_pairs<int32_t>(int, const PairArgs<int32_t>&, int, cudaStream_t);

@@ -12,16 +12,32 @@ enum PairMode : int { kModeCount = 0, kModeFill = 1, kModeLazyR6 = 2 };
 // candidates.  The fill pass then writes those pairs without screening again.
 constexpr int kMaskWords = 12;
 
+// doubles in one C'S table (|S_k| <= 2)
+constexpr int kCsTableDoubles = 3 * 125;
+
+// A batch of independent systems is laid out as concatenated slots: system
+// s owns sorted slots / original atoms [sys_atom[s], sys_atom[s+1]) and cells
+// [sys_cell[s], sys_cell[s+1]) of the batch.  Its caller-facing arrays are
+// the reference's per-system arrays placed one after another: perm and
+// cell_id hold system-local 1-based values, and its cell_offsets (ncells+1
+// entries) start at sys_cell[s] + s.
 template <typename TI>
 struct PairArgs {
-  Geometry g;
-  const TI* cell_offsets;   // 1-based CSR over cells (ncells+1)
-  const TI* perm;           // sorted slot -> 1-based original index
+  Geometry g;               // single system (nsys == 0)
+  const Geometry* geo;      // batch: geometry of each system
+  const int* sys_atom;      // batch: nsys+1 slot offsets
+  const int* sys_cell;      // batch: nsys+1 cell offsets
+  const double* cs_sys;     // batch: C'S table of each system
+  int nsys;                 // 0 for a single system
+  int nat_total;            // slots of the whole launch
+  int ncells_total;         // cells of the whole launch
+  const TI* cell_offsets;   // 1-based CSR over cells (ncells+1 per system)
+  const TI* perm;           // sorted slot -> 1-based original index within the system
   const double* Xs;         // sorted positions (nat x 3)
   const float4* rec;        // sorted FP32 records
   const int* scell;         // sorted slot -> 0-based cell index
-  const TI* first;          // fill: 1-based pair offsets per original atom (nat+1)
-  int* counts;              // count: pairs per original atom
+  const TI* first;          // fill: 1-based pair offsets per original atom of the launch (nat_total+1)
+  int* counts;              // count: pairs per original atom of the launch
   TI* oi;                   // fill outputs (1-based i, j; S as 3 x TI; R as 3 x double)
   TI* oj;
   TI* oS;
@@ -36,7 +52,23 @@ struct PairArgs {
   unsigned* err;
 };
 
+// largest s in [0, nsys) with first[s] <= x (first nondecreasing)
+__device__ __forceinline__ int batch_system(const int* __restrict__ first, int nsys, int x) {
+  int lo = 0, hi = nsys - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (first[mid] <= x)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
 template <typename TI>
 void launch_pairs(int mode, const PairArgs<TI>& a, int num_sms, cudaStream_t st);
+
+// batches: the C'S table of every system
+void launch_cs_tables(const Geometry* geo, int nsys, double* out, cudaStream_t st);
 
 }  // namespace nl

@@ -5,7 +5,8 @@
 // AcceleratedKernels.accumulate! followed by `.+= 1`
 // (gpu_kernels.jl:222-237 for `first`, :262-285 for `cell_offsets`):
 //   out1[0] = 1, out1[k+1] = out1[k] + in[k]      (TI, length n+1)
-// and optionally the same 0-based in int32 (out0, length n+1) for internal use.
+// and optionally the same 0-based in int32 (out0, length n+1) for internal use
+// (either output may be null).
 //
 // Every wait on another tile's status is bounded: after kSpinLimit polls the
 // tile sets kFlagTimeout in the error word and proceeds, so the kernel
@@ -114,14 +115,14 @@ __global__ void __launch_bounds__(kScanBlock) k_scan_offsets(const int* __restri
   for (int k = 0; k < kScanItems; ++k) {
     long long idx = base + k;
     if (idx < n) {
-      out1[idx] = TI(run + 1);
+      if (out1) out1[idx] = TI(run + 1);
       if (out0) out0[idx] = int(run);
     }
     run += v[k];
   }
   // the thread owning element n-1 also writes the sentinel and the total
   if (n > 0 && base <= n - 1 && n - 1 < base + kScanItems) {
-    out1[n] = TI(run + 1);
+    if (out1) out1[n] = TI(run + 1);
     if (out0) out0[n] = int(run);
     if (total) *total = run;
     if (run + 1 > IndexTraits<TI>::kMax) atomicOr(err, kFlagIndexOverflow);

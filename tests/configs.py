@@ -73,3 +73,26 @@ def diamond_primitive(a=5.43):
 def uniform_system(N, density=0.05, seed=0):
     """Large-system workload: N atoms uniform in a cubic pbc box."""
     return rand_config(N, density, seed)
+
+
+def batch_systems(nsys, seed=0, nmin=8, nmax=4096):
+    """Many small systems: N log-uniform in [nmin, nmax], triclinic cells with
+    density U[0.03, 0.10] and off-diagonals U(+-0.15 diag), pbc per axis with
+    probability 0.8, cutoff U[3, 6].  Returns [(X, cell, cutoff, pbc), ...]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(nsys):
+        n = int(np.exp(rng.uniform(np.log(nmin), np.log(nmax + 1))))
+        n = min(max(n, nmin), nmax)
+        rho = rng.uniform(0.03, 0.10)
+        L = (n / rho) ** (1.0 / 3.0)
+        cell = np.diag([L, L, L]) * rng.uniform(0.85, 1.15, size=3)
+        for r in range(3):
+            for c in range(3):
+                if r != c:
+                    cell[r, c] = rng.uniform(-0.15, 0.15) * cell[r, r]
+        X = rng.random((n, 3)) @ cell
+        pbc = tuple(bool(b) for b in rng.random(3) < 0.8)
+        rc = rng.uniform(3.0, 6.0)
+        out.append((X, cell, rc, pbc))
+    return out

@@ -1,0 +1,94 @@
+"""Batches of independent systems (nl_batch_neighbour_list) against the
+oracle, system by system: every per-system SortedCellList array, first, i, j,
+S and the bits of R must equal the single-system reference results."""
+import numpy as np
+import pytest
+import torch
+
+import configs as cf
+
+pytestmark = pytest.mark.gpu
+
+
+def to_np(t):
+    return t.detach().cpu().numpy()
+
+
+def check_batch(nlpkg, orc, systems, int_type=torch.int32, capacity=None):
+    b = nlpkg.BatchNeighbourList([(x.shape[0], c, rc, p) for (x, c, rc, p) in systems], int_type=int_type,
+                                 capacity=capacity)
+    X = np.concatenate([x for (x, _, _, _) in systems]) if systems else np.zeros((0, 3))
+    Xd = torch.from_numpy(np.ascontiguousarray(X, dtype=np.float64)).cuda()
+    total = b.run(Xd)
+    ti = 4 if int_type == torch.int32 else 8
+    po = b.pair_offsets_host()
+    assert po[0] == 0 and po[-1] == total
+    for s, (x, c, rc, p) in enumerate(systems):
+        clist, pl = b.system(s, Xd)
+        oc = orc.build_cell_list(x, rc, c, p, ti_bytes=ti)
+        assert np.array_equal(to_np(clist.perm).astype(np.int64), oc.perm), s
+        assert np.array_equal(to_np(clist.cell_id).astype(np.int64), oc.cell_id), s
+        assert np.array_equal(to_np(clist.cell_offsets).astype(np.int64), oc.cell_offsets), s
+        assert np.array_equal(to_np(clist.X).view(np.int64), oc.X.view(np.int64)), s
+        o = orc.neighbour_list(x, rc, c, p, ti_bytes=ti, nthreads=8)
+        assert int(pl.i.shape[0]) == o.npairs, s
+        assert np.array_equal(to_np(pl.first).astype(np.int64), o.first), s
+        assert np.array_equal(to_np(pl.i).astype(np.int64), o.i), s
+        assert np.array_equal(to_np(pl.j).astype(np.int64), o.j), s
+        assert np.array_equal(to_np(pl.S).astype(np.int64), o.S), s
+        assert np.array_equal(to_np(pl.R).view(np.int64), o.R.view(np.int64)), s
+    return b, total
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_batch_random_systems(nlpkg, orc, seed):
+    check_batch(nlpkg, orc, cf.batch_systems(40, seed=seed, nmax=700))
+
+
+def test_batch_int64(nlpkg, orc):
+    check_batch(nlpkg, orc, cf.batch_systems(12, seed=5, nmax=500), int_type=torch.int64)
+
+
+def test_batch_edge_systems(nlpkg, orc):
+    """Empty and one-atom systems, a one-cell system with a 5x5x5 stencil
+    (diamond primitive, rc 6), open boundaries, a dense cell (> 256 atoms in
+    one cell) and a triclinic cell, mixed in one batch."""
+    rng = np.random.default_rng(3)
+    Xd, Cd = cf.diamond_primitive()
+    Cbox = np.diag([7.0, 7.0, 7.0])
+    dense = rng.random((600, 3)) * 7.0
+    Xt, Ct = cf.rand_config_triclinic(80, seed=3)
+    Xf, Cf, pf = cf.fcc_sheared(n=4, seed=1)
+    systems = [
+        (np.zeros((0, 3)), np.diag([10.0, 10.0, 10.0]), 3.0, (True, True, True)),
+        (np.array([[1.0, 2.0, 3.0]]), np.diag([10.0, 10.0, 10.0]), 3.0, (True, True, True)),
+        (Xd, Cd, 6.0, (True, True, True)),
+        (rng.random((50, 3)) * 20.0, np.diag([20.0, 20.0, 20.0]), 4.0, (False, False, False)),
+        (dense, Cbox, 2.5, (True, True, True)),
+        (Xt, Ct, 3.0, (True, True, True)),
+        (Xf, Cf, 5.0, pf),
+        (np.zeros((0, 3)), np.diag([5.0, 5.0, 5.0]), 2.0, (False, True, False)),
+    ]
+    b, total = check_batch(nlpkg, orc, systems)
+    assert total == sum(orc.neighbour_list(x, rc, c, p).npairs for (x, c, rc, p) in systems)
+
+
+def test_batch_matches_single_calls_and_repeats(nlpkg, orc):
+    systems = cf.batch_systems(16, seed=9, nmax=400)
+    b = nlpkg.BatchNeighbourList([(x.shape[0], c, rc, p) for (x, c, rc, p) in systems])
+    X = torch.from_numpy(np.concatenate([s[0] for s in systems])).cuda()
+    t1 = b.run(X)
+    i1, R1 = b.i[:t1].clone(), b.R[:t1].clone()
+    b.launch(X)  # second run into the same buffers, no host synchronisation
+    b.sync_status()
+    assert torch.equal(b.i[:t1], i1) and torch.equal(b.R[:t1].view(torch.int64), R1.view(torch.int64))
+    for s, (x, c, rc, p) in enumerate(systems):
+        _, pl = b.system(s, X)
+        g = nlpkg.neighbour_list(torch.from_numpy(x).cuda(), rc, c, p)
+        assert torch.equal(pl.i, g.i) and torch.equal(pl.j, g.j) and torch.equal(pl.S, g.S)
+        assert torch.equal(pl.R.view(torch.int64), g.R.view(torch.int64))
+
+
+def test_batch_capacity_growth(nlpkg, orc):
+    systems = cf.batch_systems(10, seed=11, nmax=300)
+    check_batch(nlpkg, orc, systems, capacity=5)

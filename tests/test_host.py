@@ -16,7 +16,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def declared_symbols():
     src = open(os.path.join(ROOT, "include", "nlgpu.h")).read()
-    return sorted(set(re.findall(r"^\s*(?:int|size_t|const char\*)\s+(nl_\w+)\s*\(", src, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|size_t|void|const char\*)\s+(nl_\w+)\s*\(", src, re.M)))
 
 
 def test_library_exports_every_declared_symbol(nlpkg):
@@ -181,3 +181,30 @@ def test_screen_band_bounds_fp32_error(nlpkg, orc, case):
     band = nlpkg.analyze_cell(cell, rc).band
     worst = _screen_errors(cell, rc, pbc, X, pairs_per=6000)
     assert worst <= band / 2, (worst, band)
+
+
+def test_batch_plan_on_host(nlpkg):
+    """nl_batch_create validates systems and sizes the workspace without a GPU."""
+    import ctypes as C
+    L = nlpkg._lib.lib()
+    arr = (nlpkg._lib.System * 2)()
+    for s, n in enumerate((10, 0)):
+        p = nlpkg.analyze_cell(np.diag([10.0, 12.0, 14.0]), 3.0)
+        arr[s].nat = n
+        arr[s].cell[:] = p.cell_cm.tolist()
+        arr[s].inv_cell[:] = p.inv_cm.tolist()
+        arr[s].ncells[:] = p.ncells.tolist()
+        arr[s].nxyz[:] = p.nxyz.tolist()
+        arr[s].pbc[:] = [1, 1, 0]
+        arr[s].cutoff = 3.0
+    h = C.c_void_p()
+    assert L.nl_batch_create(arr, 2, 4, C.byref(h)) == 0
+    na, nc = C.c_int64(), C.c_int64()
+    assert L.nl_batch_sizes(h, C.byref(na), C.byref(nc)) == 0
+    assert na.value == 10 and nc.value == 2 * 3 * 4 * 4
+    assert L.nl_batch_workspace_bytes(h) >= L.nl_workspace_bytes(10, nc.value)
+    L.nl_batch_destroy(h)
+    arr[1].nxyz[0] = 63
+    assert L.nl_batch_create(arr, 2, 4, C.byref(h)) == nlpkg._lib.NL_ERR_ARG
+    assert b"system 1" in L.nl_last_error()
+    assert L.nl_batch_create(arr, 0, 4, C.byref(h)) == nlpkg._lib.NL_ERR_ARG
