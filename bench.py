@@ -38,6 +38,9 @@ METRIC = "pairs/s (1M atoms, rc 5 A, density 0.05, full pbc, Float64, build_cell
 WORKLOAD = "uniform 1,000,000 atoms, density 0.05 A^-3, cubic pbc box (L=271.44 A), cutoff 5 A, Float64, Int32 indices"
 ALGO_BYTES_PER_ATOM = 24  # positions read
 ALGO_BYTES_PER_PAIR = 44  # i 4 + j 4 + S 12 + R 24 written
+# kernels of one step: k_bin, k_scan_offsets (cells), k_scatter, k_fix, k_fix_big,
+# k_pairs<count>, k_scan_offsets (pairs), k_cs_table, k_emit, k_pairs<fill>
+LAUNCHES_PER_STEP = 10
 
 
 def workload(n_atoms=N_ATOMS):
@@ -264,6 +267,15 @@ def run_gpu(args):
     e2e = None
     if not args.no_e2e:
         e2e = measure_e2e(eng, X, Xd, total, stream, dev, args)
+    extra = {}
+    if not args.no_extra and n_atoms == N_ATOMS:
+        extra_steps = max(3, min(args.steps, 10))
+        extra["lazy"] = bench_lazy(nl, eng, Xd, X, C, pbc, stream, flush, extra_steps)
+        del eng
+        torch.cuda.empty_cache()
+        extra["batched"] = bench_batched(nl, dev, stream, flush, extra_steps)
+        torch.cuda.empty_cache()
+        extra["atoms_4m"] = bench_4m(nl, dev, stream, flush, extra_steps)
     if rank != 0:
         return
     peak, peak_kind = measured_peaks()
@@ -284,18 +296,122 @@ def run_gpu(args):
                    "l2": "flushed before every timed step (256 MiB write, untimed)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_kind": peak_kind, "kernel": "k_pairs<fill>",
+                     "peak_kind": peak_kind, "kernel": "write pass (k_emit + k_cs_table + k_pairs<fill>)",
                      "algorithmic_bytes": algo_bytes, "kernel_ms": fill_ms,
                      "traffic": (traffic or {}).get("dram_bytes_per_launch")},
         "step_roofline_frac": algo_bytes / (step_ms * 1e-3) / 1e9 / peak,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "clocks": clk.summary(),
-        "gpu_launches": 8 * args.steps,
+        "gpu_launches": LAUNCHES_PER_STEP * args.steps,
         "rechecks": rechecks,
         "recheck_band_rel": float(p.band / (CUTOFF * CUTOFF)),
+        **extra,
     }
     print(json.dumps(line))
+
+
+def timed_steps(fn, steps, flush, stream):
+    """Mean CUDA-event time (ms) of fn over `steps` calls, L2 flushed before each."""
+    import torch
+
+    ts = []
+    for k in range(steps):
+        flush.fill_(k & 0xFF)
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        fn()
+        e.record(stream)
+        ts.append((s, e))
+    torch.cuda.synchronize()
+    return sum(s.elapsed_time(e) for s, e in ts) / steps
+
+
+def bench_batched(nl, dev, stream, flush, steps):
+    """4,096 uneven systems: one batched pass (captured in a CUDA graph, launch
+    shapes autotuned) against the plain per-system launches of the same
+    systems on the same GPU; outputs compared bit for bit."""
+    import torch
+    import configs as cf
+
+    systems = cf.batch_systems(4096, seed=0)
+    X = np.ascontiguousarray(np.concatenate([x for (x, _, _, _) in systems]))
+    Xd = torch.from_numpy(X).to(dev)
+    b = nl.BatchNeighbourList([(x.shape[0], c, rc, p) for (x, c, rc, p) in systems], device=dev)
+    total = b.run(Xd)
+    tune = nl.autotune(b, Xd, reps=2)
+    b.capture(Xd)
+    batch_ms = timed_steps(b.replay, steps, flush, stream)
+    b.sync_status()
+    # plain: one engine and one nl_neighbour_list call per system
+    engines, views = [], []
+    for s, (x, c, rc, p) in enumerate(systems):
+        a0, a1 = int(b.atom0[s]), int(b.atom0[s + 1])
+        engines.append(nl.NeighbourListEngine(x.shape[0], c, rc, p, device=dev, capacity=x.shape[0] * 64 + 64))
+        views.append(Xd[a0:a1])
+    for e, v in zip(engines, views):
+        e.run(v)
+
+    def plain():
+        for e, v in zip(engines, views):
+            e.launch(v)
+
+    plain_steps = max(1, min(steps, 2))
+    plain_ms = timed_steps(plain, plain_steps, flush, stream)
+    # bit-identical outputs (every system)
+    po = b.pair_offsets_host()
+    same = True
+    for s, e in enumerate(engines):
+        p0, p1 = int(po[s]), int(po[s + 1])
+        t = e.total_pairs()
+        same &= (t == p1 - p0 and torch.equal(e.i[:t], b.i[p0:p1]) and torch.equal(e.j[:t], b.j[p0:p1])
+                 and torch.equal(e.S[:t], b.S[p0:p1])
+                 and torch.equal(e.R[:t].view(torch.int64), b.R[p0:p1].view(torch.int64)))
+    nsys = len(systems)
+    return {"workload": "4,096 systems, atoms log-uniform [8, 4096] (2,740,812 atoms), triclinic, density "
+                        "U[0.03,0.10], off-diagonals U(+-0.15 diag), pbc per axis p=0.8, cutoff U[3,6] A, seed 0",
+            "systems": nsys, "atoms": int(X.shape[0]), "pairs": int(total),
+            "systems_per_s": nsys / (batch_ms * 1e-3), "ms_per_batch": batch_ms,
+            "pairs_per_s": total / (batch_ms * 1e-3),
+            "plain_systems_per_s": nsys / (plain_ms * 1e-3), "plain_ms": plain_ms,
+            "speedup_vs_plain": plain_ms / batch_ms, "identical_to_plain": bool(same),
+            "cuda_graph": True, "autotune": {k: tune[k] for k in ("pair_blocks_per_sm", "emit_blocks_per_sm", "ms")},
+            "l2": "flushed before every timed step"}
+
+
+def bench_lazy(nl, eng, Xd, X, C, pbc, stream, flush, steps):
+    """Lazy traversal with the built-in per-atom reduction sum_j 1/r^6 on the
+    1M-atom cell list, against the FP64 oracle."""
+    import torch
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+
+    eng.launch(Xd)
+    clist = eng.cell_list(Xd)
+    out = nl.lazy_reduce(clist, "inv_r6")
+    ms = timed_steps(lambda: nl.lazy_reduce(clist, "inv_r6", out=out, sync=False), steps, flush, stream)
+    eng.sync_status()
+    got = out.cpu().numpy()
+    ref = orc.lazy_sum_r6(orc.build_cell_list(X, CUTOFF, C, pbc), nthreads=os.cpu_count() or 1)
+    rel = np.abs(got - ref) / np.maximum(np.abs(ref), 1e-300)
+    return {"workload": "lazy sum_j 1/r^6 per atom, same 1M-atom cell list", "ms": ms,
+            "pairs_per_s": eng.last_total / (ms * 1e-3), "max_rel_err_vs_oracle": float(rel.max()),
+            "bit_identical": bool(np.array_equal(got.view(np.int64), ref.view(np.int64))),
+            "tolerance": 1e-12}
+
+
+def bench_4m(nl, dev, stream, flush, steps):
+    import torch
+
+    X, C, pbc = workload(4_000_000)
+    Xd = torch.from_numpy(X).to(dev)
+    eng = nl.NeighbourListEngine(X.shape[0], C, CUTOFF, pbc, device=dev)
+    total = eng.run(Xd)
+    ms = timed_steps(lambda: eng.launch(Xd), steps, flush, stream)
+    eng.sync_status()
+    return {"workload": "uniform 4,000,000 atoms, density 0.05, cubic pbc box, cutoff 5 A", "pairs": int(total),
+            "ms_per_step": ms, "pairs_per_s": total / (ms * 1e-3), "rechecks": eng.rechecks()}
 
 
 def measure_e2e(eng, X, Xd, total, stream, dev, args):
@@ -349,6 +465,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the lazy / batched / 4M sections")
     ap.add_argument("--atoms", type=int, default=N_ATOMS, help="system size (profiling runs use a smaller one)")
     args = ap.parse_args()
     if args.impl == "reference":

@@ -68,6 +68,13 @@ int nl_analyze_cell(const double cell[9], double cutoff, int index_bytes, nl_cel
  * ncells_total cells. */
 size_t nl_workspace_bytes(int64_t nat, int64_t ncells_total);
 
+/* Smallest workspace every call accepts: without room for the per-atom pair
+ * lists of the count pass, every cell is written by the (slower) screening
+ * write pass, with identical results.  Count and fill of one list must be
+ * given the same workspace size (a mismatch is reported as
+ * NL_ERR_INCONSISTENT). */
+size_t nl_workspace_min_bytes(int64_t nat, int64_t ncells_total);
+
 /* Replaces build_cell_list / _build_sorted_celllist (cell_list.jl:632-679),
  * i.e. _compute_cell_ids (gpu_kernels.jl:244-255,378-382), _get_sortperm
  * (cell_list.jl:711-718) and _compute_cell_offsets (gpu_kernels.jl:262-285,
@@ -130,7 +137,7 @@ int nl_lazy_reduce(const double* d_X_sorted, const void* d_perm, const void* d_c
  * counterpart in the reference: it exists only because this engine needs
  * scratch memory.  The scratch is a fixed 32 MiB array inside the library,
  * present on every GPU that loads it until the process exits; systems that
- * need more (about 600k atoms at liquid density) are rejected with
+ * need more (about 500k atoms at liquid density) are rejected with
  * NL_ERR_NOMEM.  The first call on each device resolves the array's address
  * and should come before any stream capture.  Every call reuses the same
  * array: calls that overlap on the GPU race and must be serialised.  The call
@@ -172,6 +179,11 @@ typedef struct nl_batch nl_batch;   /* host-side plan of a batch (opaque) */
 /* Validates the systems and builds the host plan.  index_bytes applies to
  * every system. */
 int nl_batch_create(const nl_system* systems, int nsys, int index_bytes, nl_batch** batch);
+/* Same, from raw systems: cells[9*s..] column-major, cutoffs[s], pbc[3*s..],
+ * nat[s]; the cell analysis (analyze_cell + nxyz, as nl_analyze_cell) runs
+ * inside.  For callers that assemble many small systems per batch (serving). */
+int nl_batch_create_auto(const double* cells, const double* cutoffs, const uint8_t* pbc, const int64_t* nat, int nsys,
+                         int index_bytes, nl_batch** batch);
 void nl_batch_destroy(nl_batch* batch);
 /* Workspace bytes for the batch, and its total atoms / cells. */
 size_t nl_batch_workspace_bytes(const nl_batch* batch);
@@ -189,6 +201,20 @@ int nl_batch_neighbour_list(const nl_batch* batch, const double* d_X, void* d_pe
                             void* d_cell_id, void* d_cell_offsets, void* d_first, int64_t* d_pair_offsets,
                             int64_t capacity, void* d_i, void* d_j, void* d_S, double* d_R, int64_t* total_pairs,
                             void* d_workspace, size_t workspace_bytes, void* stream);
+
+/* ---- launch tuning ------------------------------------------------------
+ * Grid sizes of the pair kernels, as picked by an autotuner (the Python
+ * package's autotune()).  0 keeps the default (every resident block slot of
+ * every SM).  Results never depend on the tuning. */
+typedef struct nl_tuning {
+  int pair_blocks_per_sm;   /* count / screening write / lazy kernels, 1..7 */
+  int emit_blocks_per_sm;   /* list write kernel, 1..16 */
+} nl_tuning;
+
+/* Tuning of the single-system calls made by the calling thread (NULL: defaults). */
+int nl_set_tuning(const nl_tuning* tuning);
+/* Tuning of one batch (NULL: defaults). */
+int nl_batch_set_tuning(nl_batch* batch, const nl_tuning* tuning);
 
 /* Synchronises the stream, then reports (and clears) any device-side error
  * recorded in the workspace by earlier asynchronous calls. */

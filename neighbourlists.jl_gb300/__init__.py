@@ -26,3 +26,5 @@ from .api import (  # noqa: F401
 )
 from .batch import BatchNeighbourList  # noqa: F401
 from .engine import NeighbourListEngine  # noqa: F401
+from .serving import NeighbourListServer, Request, poisson_trace  # noqa: F401
+from .tuning import autotune  # noqa: F401

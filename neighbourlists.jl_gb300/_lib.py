@@ -29,6 +29,7 @@ NL_REDUCE_INV_R6 = 1
 EXPORTED = [
     "nl_analyze_cell",
     "nl_workspace_bytes",
+    "nl_workspace_min_bytes",
     "nl_build_cell_list",
     "nl_count_pairs",
     "nl_fill_pairs",
@@ -36,11 +37,14 @@ EXPORTED = [
     "nl_neighbour_list_static",
     "nl_lazy_reduce",
     "nl_batch_create",
+    "nl_batch_create_auto",
     "nl_batch_destroy",
     "nl_batch_workspace_bytes",
     "nl_batch_sizes",
     "nl_batch_upload",
     "nl_batch_neighbour_list",
+    "nl_set_tuning",
+    "nl_batch_set_tuning",
     "nl_sync_status",
     "nl_last_recheck_count",
     "nl_status_string",
@@ -73,6 +77,11 @@ class System(C.Structure):
     ]
 
 
+class Tuning(C.Structure):
+    """nl_tuning: grid sizes of the pair kernels (0 = default)."""
+    _fields_ = [("pair_blocks_per_sm", C.c_int), ("emit_blocks_per_sm", C.c_int)]
+
+
 class NLError(RuntimeError):
     """Raised for any non-zero status of the C ABI."""
 
@@ -94,6 +103,8 @@ def _declare(L):
     L.nl_analyze_cell.restype = C.c_int
     L.nl_workspace_bytes.argtypes = [C.c_int64, C.c_int64]
     L.nl_workspace_bytes.restype = C.c_size_t
+    L.nl_workspace_min_bytes.argtypes = [C.c_int64, C.c_int64]
+    L.nl_workspace_min_bytes.restype = C.c_size_t
     L.nl_build_cell_list.argtypes = [_vp, C.c_int64, _D, _D, _I64, _U8, C.c_double, C.c_int, _vp, _vp, _vp, _vp, _vp,
                                      C.c_size_t, _vp]
     L.nl_build_cell_list.restype = C.c_int
@@ -114,6 +125,8 @@ def _declare(L):
     L.nl_lazy_reduce.restype = C.c_int
     L.nl_batch_create.argtypes = [C.POINTER(System), C.c_int, C.c_int, C.POINTER(_vp)]
     L.nl_batch_create.restype = C.c_int
+    L.nl_batch_create_auto.argtypes = [_vp, _vp, _vp, _vp, C.c_int, C.c_int, C.POINTER(_vp)]
+    L.nl_batch_create_auto.restype = C.c_int
     L.nl_batch_destroy.argtypes = [_vp]
     L.nl_batch_destroy.restype = None
     L.nl_batch_workspace_bytes.argtypes = [_vp]
@@ -125,6 +138,10 @@ def _declare(L):
     L.nl_batch_neighbour_list.argtypes = [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int64, _vp, _vp, _vp, _vp, _I64,
                                           _vp, C.c_size_t, _vp]
     L.nl_batch_neighbour_list.restype = C.c_int
+    L.nl_set_tuning.argtypes = [C.POINTER(Tuning)]
+    L.nl_set_tuning.restype = C.c_int
+    L.nl_batch_set_tuning.argtypes = [_vp, C.POINTER(Tuning)]
+    L.nl_batch_set_tuning.restype = C.c_int
     L.nl_sync_status.argtypes = [_vp, _vp]
     L.nl_sync_status.restype = C.c_int
     L.nl_last_recheck_count.argtypes = [_vp, _vp, _I64]

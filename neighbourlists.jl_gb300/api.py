@@ -248,18 +248,25 @@ def neighbour_list(X, cutoff: float, cell, pbc, lazy: bool = False, int_type=tor
     return materialize_pairlist(clist, with_R=with_R, stream=stream)
 
 
-def lazy_reduce(clist: SortedCellList, op: str = "count", stream=None) -> torch.Tensor:
+def lazy_reduce(clist: SortedCellList, op: str = "count", stream=None, out: Optional[torch.Tensor] = None,
+                sync: bool = True) -> torch.Tensor:
     """Built-in reductions of the lazy traversal over every atom:
     "count" -> int32 neighbour count per atom (count_neighbours for all i);
-    "inv_r6" -> float64 per-atom sum of 1/r^6 in the reference's order."""
-    nat = int(clist.X_orig.shape[0])
-    dev = clist.X_orig.device
+    "inv_r6" -> float64 per-atom sum of 1/r^6 in the reference's order.
+    ``out`` reuses an output tensor; ``sync=False`` leaves the error check to
+    a later nl_sync_status on the cell list's workspace."""
+    nat = int(clist.X.shape[0])
+    dev = clist.X.device
     if op == "count":
-        code, out = _lib.NL_REDUCE_COUNT, torch.zeros(nat, dtype=torch.int32, device=dev)
+        code, dt = _lib.NL_REDUCE_COUNT, torch.int32
     elif op == "inv_r6":
-        code, out = _lib.NL_REDUCE_INV_R6, torch.zeros(nat, dtype=torch.float64, device=dev)
+        code, dt = _lib.NL_REDUCE_INV_R6, torch.float64
     else:
         raise ValueError("op must be 'count' or 'inv_r6'")
+    if out is None:
+        out = torch.zeros(nat, dtype=dt, device=dev)
+    elif out.dtype != dt or out.numel() != nat or not out.is_cuda:
+        raise ValueError(f"out must be a CUDA {dt} tensor of {nat} entries")
     if clist._ws is None:
         clist._ws = _new_workspace(nat, clist.ncells_total, dev)
         clist._records = False
@@ -273,7 +280,8 @@ def lazy_reduce(clist: SortedCellList, op: str = "count", stream=None) -> torch.
                                    pb.ctypes.data_as(_U8), clist.cutoff, clist.index_bytes,
                                    1 if clist._records else 0, code, _ptr(out), _ptr(ws), ws.numel(), sh))
         clist._records = True
-        check(lib().nl_sync_status(_ptr(ws), sh))
+        if sync:
+            check(lib().nl_sync_status(_ptr(ws), sh))
     return out
 
 

@@ -132,6 +132,29 @@ class BatchNeighbourList:
         self.last_total = int(total.value)
         return self.last_total
 
+    def set_tuning(self, pair_blocks_per_sm: int = 0, emit_blocks_per_sm: int = 0) -> None:
+        t = _lib.Tuning(int(pair_blocks_per_sm), int(emit_blocks_per_sm))
+        check(lib().nl_batch_set_tuning(self._h, C.byref(t)))
+
+    def capture(self, X: torch.Tensor) -> torch.cuda.CUDAGraph:
+        """Captures one launch on X in a CUDA graph (the buffers stay fixed);
+        ``replay()`` re-runs every stage of every system with one graph launch."""
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            self.launch(X)  # first launch outside the capture
+        torch.cuda.current_stream().wait_stream(side)
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.launch(X)
+        self._graph = g
+        return g
+
+    def replay(self) -> None:
+        self._po_host = None
+        self._graph.replay()
+
     def sync_status(self, stream=None) -> None:
         check(lib().nl_sync_status(_ptr(self.ws), _stream_handle(stream)))
 

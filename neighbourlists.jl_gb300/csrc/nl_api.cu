@@ -25,6 +25,7 @@
 namespace {
 
 thread_local std::string g_last_error;
+thread_local nl_tuning g_tuning = {0, 0};  // single-system calls of this thread
 
 int fail(int status, const std::string& msg) {
   g_last_error = msg;
@@ -168,8 +169,9 @@ struct Layout {
   // [err 64 | stats 64] [pairs zero region: counters 64 | st_pairs]
   // [build zero region: counters 64 | st_cells | cell_count] [arrays...]
   size_t err, stats, pcount, st_pairs, pend, bcount, st_cells, cell_count, bend;
-  size_t totals, cell_start, cid, ticket, rec, tmp, rec_sorted, scell, counts, masks, cs_table, unmasked, big_list,
-      end;
+  size_t totals, cell_start, cid, ticket, rec, tmp, rec_sorted, scell, counts, lcount, sorig, cs_table, unmasked,
+      big_list, base_end, lists, end;
+  bool use_lists = true;  // the workspace holds the pair lists (it reaches `end`)
 };
 
 Layout layout(int64_t nat, int64_t ncells) {
@@ -209,14 +211,21 @@ Layout layout(int64_t nat, int64_t ncells) {
   o += up(sizeof(int) * n);
   L.counts = o;
   o += up(sizeof(int) * n);
-  L.masks = o;
-  o += up(sizeof(unsigned) * size_t(nl::kMaskWords) * n);
+  L.lcount = o;
+  o += up(sizeof(int) * n);
+  L.sorig = o;
+  o += up(sizeof(int) * n);
   L.cs_table = o;
   o += up(sizeof(double) * 3 * 125);
   L.unmasked = o;
   o += up(sizeof(int) * size_t(ncells > 0 ? ncells : 1));
   L.big_list = o;
   o += up(sizeof(int) * size_t(ncells < (int64_t)n ? ncells : (int64_t)n));
+  // the pair lists come last: a workspace that ends before them still runs
+  // every call, with the screening write pass for every cell
+  L.base_end = o;
+  L.lists = o;
+  o += up(sizeof(uint2) * size_t(nl::kListCap) * n);
   L.end = o;
   return L;
 }
@@ -266,7 +275,9 @@ int check_common(int64_t nat, const int64_t* ncells, const int64_t* nxyz, int in
     return fail(NL_ERR_TOO_MANY_CELLS, "Ratio of simulation cell size to cutoff is very large.");
   ncells_total = int64_t(prod);
   L = layout(nat, ncells_total);
-  if (!ws || ws_bytes < L.end) return fail(NL_ERR_NOMEM, "workspace too small (see nl_workspace_bytes)");
+  if (!ws || ws_bytes < L.base_end) return fail(NL_ERR_NOMEM, "workspace too small (see nl_workspace_bytes)");
+  // list entries are addressed with 32-bit offsets
+  L.use_lists = ws_bytes >= L.end && (unsigned long long)nat * nl::kListCap < (1ull << 32);
   return NL_OK;
 }
 
@@ -375,10 +386,16 @@ nl::PairArgs<TI> pair_args(const nl::Geometry& g, const TI* cell_offsets, const 
   a.Xs = Xs;
   a.rec = at<float4>(ws, L.rec_sorted);
   a.scell = at<int>(ws, L.scell);
-  a.masks = at<unsigned>(ws, L.masks);
+  a.list_cap = L.use_lists ? nl::kListCap : 0;
+  a.lists = L.use_lists ? at<uint2>(ws, L.lists) : nullptr;
+  a.lcount = at<int>(ws, L.lcount);
+  a.sorig = at<int>(ws, L.sorig);
+  a.cap_rec = at<int>(ws, L.pcount) + 2;  // the count pass's list_cap, checked by the write pass
   a.cs_table = at<double>(ws, L.cs_table);
   a.unmasked = at<int>(ws, L.unmasked);
   a.n_unmasked = at<int>(ws, L.pcount) + 4;  // zeroed with the pair scan state
+  a.pair_blocks_per_sm = g_tuning.pair_blocks_per_sm;
+  a.emit_blocks_per_sm = g_tuning.emit_blocks_per_sm;
   a.stats = at<unsigned long long>(ws, L.stats);
   a.err = at<unsigned>(ws, L.err);
   return a;
@@ -435,6 +452,7 @@ struct BatchLayout {
 BatchLayout batch_layout(int64_t nat, int64_t ncells, int nsys) {
   BatchLayout B;
   B.L = layout(nat, ncells);
+  B.L.use_lists = (unsigned long long)nat * nl::kListCap < (1ull << 32);
   size_t o = B.L.end;
   B.geo = o;
   o += up(sizeof(nl::Geometry) * size_t(nsys));
@@ -459,6 +477,7 @@ struct nl_batch {
   std::vector<nl::Geometry> geo;
   std::vector<int> atom0, cell0;
   BatchLayout B;
+  nl_tuning tuning = {0, 0};
 };
 
 namespace {
@@ -501,6 +520,8 @@ int batch_impl(const nl_batch& b, const double* X, TI* perm, double* Xs, TI* cel
   a.nat_total = na;
   a.ncells_total = nc;
   a.counts = at<int>(ws, L.counts);
+  a.pair_blocks_per_sm = b.tuning.pair_blocks_per_sm;
+  a.emit_blocks_per_sm = b.tuning.emit_blocks_per_sm;
   if (na > 0) {
     nl::launch_pairs<TI>(nl::kModeCount, a, sms, st);
     nl::launch_scan<TI>(at<int>(ws, L.counts), na, first_all, nullptr, at<unsigned long long>(ws, L.st_pairs),
@@ -530,6 +551,10 @@ int batch_impl(const nl_batch& b, const double* X, TI* perm, double* Xs, TI* cel
 namespace nl {
 int report(int status, const std::string& msg) { return fail(status, msg); }
 int status_from_device_flags(unsigned flags) { return status_from_flags(flags); }
+size_t workspace_min_bytes(int64_t nat, int64_t ncells_total) {
+  if (nat < 0 || ncells_total < 1) return 0;
+  return layout(nat, ncells_total).base_end;
+}
 }  // namespace nl
 
 // ======================================================================
@@ -564,6 +589,8 @@ size_t nl_workspace_bytes(int64_t nat, int64_t ncells_total) {
   if (nat < 0 || ncells_total < 1) return 0;
   return layout(nat, ncells_total).end;
 }
+
+size_t nl_workspace_min_bytes(int64_t nat, int64_t ncells_total) { return nl::workspace_min_bytes(nat, ncells_total); }
 
 int nl_build_cell_list(const double* d_X, int64_t nat, const double cell[9], const double inv_cell[9],
                        const int64_t ncells[3], const uint8_t pbc[3], double cutoff, int index_bytes, void* d_perm,
@@ -696,6 +723,10 @@ int nl_lazy_reduce(const double* d_X_sorted, const void* d_perm, const void* d_c
                              at<unsigned>(d_workspace, L.err), sms, st);
     nl::PairArgs<TI> a =
         pair_args<TI>(g, static_cast<const TI*>(d_cell_offsets), static_cast<const TI*>(d_perm), d_X_sorted, d_workspace, L);
+    a.list_cap = 0;  // lazy: nothing is written later
+    a.lists = nullptr;
+    a.lcount = nullptr;
+    a.cap_rec = nullptr;
     if (op == NL_REDUCE_COUNT) {
       a.counts = static_cast<int*>(d_out);
       nl::launch_pairs<TI>(nl::kModeCount, a, sms, st);
@@ -754,6 +785,31 @@ int nl_batch_create(const nl_system* systems, int nsys, int index_bytes, nl_batc
   b->B = batch_layout(na, nc, nsys);
   *batch = b;
   return NL_OK;
+}
+
+int nl_batch_create_auto(const double* cells, const double* cutoffs, const uint8_t* pbc, const int64_t* nat, int nsys,
+                         int index_bytes, nl_batch** batch) {
+  if (!batch || (nsys > 0 && (!cells || !cutoffs || !pbc || !nat))) return fail(NL_ERR_ARG, "null argument");
+  if (nsys < 1) return fail(NL_ERR_ARG, "a batch needs at least one system");
+  std::vector<nl_system> sys(static_cast<size_t>(nsys));
+  for (int s = 0; s < nsys; ++s) {
+    nl_system& y = sys[size_t(s)];
+    nl_cell_plan p;
+    if (int st = analyze(cells + 9 * size_t(s), cutoffs[s], index_bytes, &p)) {
+      g_last_error = "system " + std::to_string(s) + ": " + g_last_error;
+      return st;
+    }
+    y.nat = nat[s];
+    std::memcpy(y.cell, cells + 9 * size_t(s), sizeof(y.cell));
+    std::memcpy(y.inv_cell, p.inv_cell, sizeof(y.inv_cell));
+    for (int k = 0; k < 3; ++k) {
+      y.ncells[k] = p.ncells[k];
+      y.nxyz[k] = p.nxyz[k];
+      y.pbc[k] = pbc[3 * size_t(s) + k] ? 1 : 0;
+    }
+    y.cutoff = cutoffs[s];
+  }
+  return nl_batch_create(sys.data(), nsys, index_bytes, batch);
 }
 
 void nl_batch_destroy(nl_batch* batch) { delete batch; }
@@ -818,6 +874,26 @@ int nl_batch_neighbour_list(const nl_batch* batch, const double* d_X, void* d_pe
     if (s == NL_OK && *total_pairs > capacity) return fail(NL_ERR_CAPACITY, "pair buffers are smaller than the pair count");
     return s;
   }
+  return NL_OK;
+}
+
+static int check_tuning(const nl_tuning* t) {
+  if (t && (t->pair_blocks_per_sm < 0 || t->pair_blocks_per_sm > 7 || t->emit_blocks_per_sm < 0 ||
+            t->emit_blocks_per_sm > 16))
+    return fail(NL_ERR_ARG, "tuning out of range (pair 0..7, emit 0..16 blocks per SM)");
+  return NL_OK;
+}
+
+int nl_set_tuning(const nl_tuning* tuning) {
+  if (int s = check_tuning(tuning)) return s;
+  g_tuning = tuning ? *tuning : nl_tuning{0, 0};
+  return NL_OK;
+}
+
+int nl_batch_set_tuning(nl_batch* batch, const nl_tuning* tuning) {
+  if (!batch) return fail(NL_ERR_ARG, "null batch");
+  if (int s = check_tuning(tuning)) return s;
+  batch->tuning = tuning ? *tuning : nl_tuning{0, 0};
   return NL_OK;
 }
 

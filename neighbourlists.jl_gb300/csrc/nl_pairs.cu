@@ -234,7 +234,10 @@ __device__ __forceinline__ void flush_ring(const PairArgs<TI>& A, const Geometry
 
 // C'S for |S_k| <= kCsR with the reference's operation order, built once per
 // call (one block) and read by the fill / emit / lazy kernels.
-__global__ void k_cs_table(Geometry g, double* __restrict__ out) {
+__global__ void k_cs_table(Geometry g, double* __restrict__ out, const int* __restrict__ cap_rec, int list_cap,
+                           unsigned* __restrict__ err) {
+  // the write pass must use the lists the count pass made (same workspace size)
+  if (threadIdx.x == 0 && cap_rec && *cap_rec != list_cap) atomicOr(err, kFlagInconsistent);
   for (int t = threadIdx.x; t < kCsN * kCsN * kCsN; t += blockDim.x) {
     const int s0 = t % kCsN - kCsR, s1 = (t / kCsN) % kCsN - kCsR, s2 = t / (kCsN * kCsN) - kCsR;
     out[3 * t + 0] = cts_k(g.C, s0, s1, s2, 0);
@@ -358,6 +361,8 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
   if (!BATCH) set_stencil();
   int cur_sys = -1;
   unsigned rechecks = 0;
+  const int list_cap = MODE == kModeCount ? A.list_cap : 0;
+  if (MODE == kModeCount && A.cap_rec && blockIdx.x == 0 && threadIdx.x == 0) *A.cap_rec = list_cap;
 
   // Single systems prefetch the ranges of the next cell one cell ahead: its
   // home range and, per lane, the range of its stencil cell in the first
@@ -407,6 +412,7 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
     prefetch(idx + nwarps);  // loads in flight while this cell is processed
     if (hs >= he) continue;
     const int hl = sv.hl;
+    bool overflow = false;  // count: an atom of this cell has more than list_cap pairs
     const int hc0 = hl % g.ns[0] + 1, hc1 = (hl / g.ns[0]) % g.ns[1] + 1, hc2 = hl / (g.ns[0] * g.ns[1]) + 1;
 
     for (int hb = hs; hb < he; hb += 32) {
@@ -436,13 +442,6 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
           if (lane >= o) incl += v;
         }
         const int tg = __shfl_sync(0xffffffffu, incl, 31);
-        // cells whose candidates fit the acceptance masks: the count pass
-        // records them and the fill pass leaves them to k_emit
-        const bool masked = nst <= 32 && tg <= 32 * kMaskWords;
-        if (MODE == kModeCount && !masked && gb == 0 && hb == hs && lane == 0) {
-          const int u = atomicAdd(A.n_unmasked, 1);
-          if (u < A.ncells_total) A.unmasked[u] = h;
-        }
         const int cl = center - gb;  // home cell (center of the stencil) in this group?
         const int center_excl = (cl >= 0 && cl < 32) ? __shfl_sync(0xffffffffu, incl - ccount, cl & 31) : -1;
 
@@ -521,7 +520,6 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
           for (int a0 = 0; a0 < nb; a0 += kGroup) {
             float ax[kGroup], ay[kGroup], az[kGroup];
             long long next[kGroup];
-            unsigned word[kGroup];  // count mode: lane w keeps acceptance word w
 #pragma unroll
             for (int k = 0; k < kGroup; ++k) {
               const int a = min(a0 + k, nb - 1);
@@ -531,7 +529,6 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
               ay[k] = use ? __shfl_sync(0xffffffffu, uy, a) : inf;
               az[k] = use ? __shfl_sync(0xffffffffu, uz, a) : inf;
               next[k] = W.hnext[a];
-              word[k] = 0u;
             }
             for (int r0 = 0; r0 < nround; r0 += 32) {
               const int f = r0 + lane;
@@ -561,12 +558,19 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
                     }
                   }
               }
-              if (MODE == kModeCount) {
+              if constexpr (MODE == kModeCount) {
 #pragma unroll
                 for (int k = 0; k < kGroup; ++k) {
                   const unsigned mask = __ballot_sync(0xffffffffu, acc[k]);
+                  if (mask != 0u && list_cap > 0) {
+                    // list entry: (slot of j, candidate word), in traversal order
+                    // (32-bit offsets: the host keeps nat * list_cap below 2^32)
+                    const unsigned pos = unsigned(next[k]) + unsigned(__popc(mask & lt_mask()));
+                    if (acc[k] && pos < unsigned(list_cap))
+                      A.lists[unsigned(hb + a0 + k) * unsigned(list_cap) + pos] =
+                          make_uint2(unsigned(W.cslot[f]), __float_as_uint(c.w));
+                  }
                   next[k] += __popc(mask);
-                  if (lane == ((cb + r0) >> 5)) word[k] = mask;
                 }
               } else {
 #pragma unroll
@@ -590,15 +594,6 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
                 }
               }
             }
-            if (MODE == kModeCount && masked) {
-              // lanes [cb/32, cb/32 + nround/32) hold this chunk's words
-              const int w = lane - (cb >> 5);
-              if (w >= 0 && w < (nround >> 5)) {
-#pragma unroll
-                for (int k = 0; k < kGroup; ++k)
-                  if (a0 + k < nb) A.masks[(long long)(hb + a0 + k) * kMaskWords + lane] = word[k];
-              }
-            }
             __syncwarp();
 #pragma unroll
             for (int k = 0; k < kGroup; ++k)
@@ -610,10 +605,24 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
       if (MODE != kModeCount && tail > head) flush_ring<TI, MODE>(A, g, cs_tab, W, head, tail - head, lane);
       __syncwarp();
       if (lane < nb) {
-        if (MODE == kModeCount) A.counts[sv.abase + W.horig[lane]] = int(W.hnext[lane]);
+        if (MODE == kModeCount) {
+          const int cnt = int(W.hnext[lane]);
+          A.counts[sv.abase + W.horig[lane]] = cnt;
+          if (A.lcount) {
+            A.lcount[hb + lane] = cnt;
+            A.sorig[hb + lane] = sv.abase + W.horig[lane];
+          }
+          overflow |= cnt > list_cap;
+        }
         if (MODE == kModeLazyR6) A.per_atom[sv.abase + W.horig[lane]] = W.hacc[lane];
       }
       __syncwarp();
+    }
+    // a cell with an atom whose list overflowed (or with no lists at all) is
+    // written by the screening write pass
+    if (MODE == kModeCount && __any_sync(0xffffffffu, overflow) && lane == 0) {
+      const int u = atomicAdd(A.n_unmasked, 1);
+      if (u < A.ncells_total) A.unmasked[u] = h;
     }
   }
   // statistics: number of FP64 decisions
@@ -623,217 +632,157 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
 }
 
 // ------------------------------------------------------------------------
-// Emit: writes the pairs of every masked home cell from the acceptance masks
-// recorded by the count pass -- no staging of candidates and no screening.
-// One warp per home cell, one home atom at a time: lanes 0..nw-1 hold the
-// atom's acceptance words, a shuffle scan numbers its accepted candidates,
-// and lane r resolves and writes the atom's r-th pair.  The output slots
-// first[i] + r are consecutive, so the stores coalesce.  Candidate f maps to
-// its stencil cell through a per-cell byte table.
+// Emit: writes i, j, S, R of every atom whose pairs the count pass listed --
+// no stencil, no staging and no screening.  One warp takes 32 consecutive
+// sorted slots; their per-atom data go to shared memory, then the warp walks
+// the atoms one at a time, lane r writing the atom's r-th pair.  The output
+// slots first[i] + r are consecutive, so the stores coalesce.  Passes run as
+// a two-stage pipeline: a pass's list entries and gathers are issued before
+// the previous pass computes S and R and stores.
 #ifndef NL_EMIT_MIN_BLOCKS
 #define NL_EMIT_MIN_BLOCKS 8
 #endif
 constexpr int kEmitWarps = 4;
 constexpr int kEmitMinBlocks = NL_EMIT_MIN_BLOCKS;  // resident blocks per SM the register budget targets
-constexpr int kEmitCand = 32 * kMaskWords;  // candidates a masked cell may have
 
-struct __align__(16) EmitSmem {
-  double hx[32][3];             // home batch: FP64 positions
-  long long hbase[32];          // home batch: first output slot (0-based)
-  int horig[32];                // home batch: original index (0-based)
-  unsigned hmeta[32];           // home batch: packed windings | exact bit
-  int qstart[32];               // stencil cell q: first sorted slot
-  int qexcl[32];                // stencil cell q: candidates before it
-  unsigned qslp[32];            // stencil cell q: candidate word base
-  unsigned char cq[kEmitCand];  // candidate f -> its stencil cell q
+struct __align__(16) EmitAtoms {
+  long long sbuf[96];   // a pass's S, three words per pair, staged for contiguous stores
+  double rbuf[96];      // a pass's R, likewise
+  double xi[32][3];     // FP64 position
+  long long base[32];   // first output slot (0-based)
+  long long ti[32];     // output value of i (system-local, 1-based)
+  unsigned mi[32];      // packed windings | exact bit
+  int n[32];            // listed pairs (0 when written by the screening pass)
+  int sys[32];          // batch: system of the slot
 };
-
-// position of the (k+1)-th set bit of m (0 <= k < popc(m)), by bisection
-__device__ __forceinline__ int nth_set_bit(unsigned m, int k) {
-  int pos = 0;
-#pragma unroll
-  for (int half = 16; half > 0; half >>= 1) {
-    const unsigned low = m & ((1u << half) - 1u);
-    const int c = __popc(low);
-    if (k >= c) {
-      k -= c;
-      m >>= half;
-      pos += half;
-    } else {
-      m = low;
-    }
-  }
-  return pos;
-}
 
 template <typename TI, bool BATCH>
 __global__ void __launch_bounds__(kEmitWarps * 32, kEmitMinBlocks) k_emit(PairArgs<TI> A) {
-  __shared__ EmitSmem es[kEmitWarps];
+  __shared__ EmitAtoms ea[kEmitWarps];
   __shared__ double cs_blk[BATCH ? 1 : 3 * kCsN * kCsN * kCsN];
-  __shared__ unsigned dtab_blk[32 * (BATCH ? kEmitWarps : 1)];
-  __shared__ Geometry geo_w[BATCH ? kEmitWarps : 1];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const Geometry& g = BATCH ? geo_w[warp] : A.g;
-  const unsigned* dtab = BATCH ? dtab_blk + 32 * warp : dtab_blk;
-  int sx = 2 * g.nxyz[0] + 1, sy = 2 * g.nxyz[1] + 1;
-  int nst = sx * sy * (2 * g.nxyz[2] + 1);
   if (!BATCH) {
-    if (nst > 32) return;  // no cell of this system is masked (uniform over the grid)
     for (int t = threadIdx.x; t < 3 * kCsN * kCsN * kCsN; t += blockDim.x) cs_blk[t] = A.cs_table[t];
-    for (int t = threadIdx.x; t < nst; t += blockDim.x)
-      dtab_blk[t] = pack3(t % sx - g.nxyz[0], (t / sx) % sy - g.nxyz[1], t / (sx * sy) - g.nxyz[2]);
     __syncthreads();
   }
-  const double* cs_tab = cs_blk;
-  int cur_sys = -1;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  EmitAtoms& E = ea[warp];
+  const int K = A.list_cap;
+  const long long nwarps = (long long)gridDim.x * kEmitWarps;
+  for (long long c0 = ((long long)blockIdx.x * kEmitWarps + warp) * 32; c0 < A.nat_total; c0 += nwarps * 32) {
+    const int na = int(min(32LL, A.nat_total - c0));
+    __syncwarp();
+    if (lane < na) {
+      const int slot = int(c0) + lane;
+      int n = A.lcount[slot];
+      E.n[lane] = n > K ? 0 : n;  // overflowed atoms belong to the screening pass
+      E.base[lane] = (long long)A.first[clampi(A.sorig[slot], A.nat_total - 1)] - 1;
+      E.ti[lane] = (long long)A.perm[slot];
+      E.mi[lane] = __float_as_uint(A.rec[slot].w);
+      E.xi[lane][0] = A.Xs[3LL * slot + 0];
+      E.xi[lane][1] = A.Xs[3LL * slot + 1];
+      E.xi[lane][2] = A.Xs[3LL * slot + 2];
+      E.sys[lane] = BATCH ? batch_system(A.sys_atom, A.nsys, slot) : 0;
+    }
+    __syncwarp();
 
-  EmitSmem& E = es[warp];
-  const int nwarps = gridDim.x * kEmitWarps;
-  for (int h = blockIdx.x * kEmitWarps + warp; h < A.ncells_total; h += nwarps) {
-    int abase = 0, coff = 0, hl = h;
-    if constexpr (BATCH) {
-      const int s = batch_system(A.sys_cell, A.nsys, h);
-      if (s != cur_sys) {
-        load_system<TI, BATCH>(A, s, geo_w[warp], dtab_blk + 32 * warp, lane);
-        sx = 2 * g.nxyz[0] + 1;
-        sy = 2 * g.nxyz[1] + 1;
-        nst = sx * sy * (2 * g.nxyz[2] + 1);
-        cur_sys = s;
+    bool pv = false;  // a pass waits for stage 2
+    int pa = 0, pr = 0, pn = 0;
+    unsigned pcw = 0;
+    long long poj = 0;
+    double pxj0 = 0.0, pxj1 = 0.0, pxj2 = 0.0;
+    // The pass's pairs occupy output slots [out0, out0 + nact): i and j are
+    // stored per lane, S and R are staged in shared memory and stored as
+    // consecutive words, so every store instruction covers whole sectors.
+    auto finish = [&]() {
+      const bool act = pr < pn;
+      const double* xi = E.xi[pa];
+      const double xj[3] = {pxj0, pxj1, pxj2};
+      const Geometry& g = BATCH ? A.geo[E.sys[pa]] : A.g;
+      const double* cs_tab = BATCH ? A.cs_sys + 3 * kCsN * kCsN * kCsN * (long long)E.sys[pa] : cs_blk;
+      int S[3];
+      pair_S(g, xi, xj, E.mi[pa], pcw, S);
+      const long long out0 = E.base[pa] + (pr - lane);
+      const int nact = min(32, pn - (pr - lane));
+      const long long out = out0 + lane;
+      const bool wr = act && out < A.capacity;
+      if (act && !wr) atomicOr(A.err, kFlagCapacity);
+      if (wr) {
+        A.oi[out] = TI(E.ti[pa]);
+        A.oj[out] = TI(poj);
       }
-      if (nst > 32) continue;  // left to the screening fill
-      cs_tab = A.cs_sys + 3 * kCsN * kCsN * kCsN * (long long)s;
-      abase = A.sys_atom[s];
-      coff = A.sys_cell[s] + s;
-      hl = h - A.sys_cell[s];
-    }
-    const int hs = clampi(A.cell_offsets[coff + hl] - 1 + abase, A.nat_total);
-    const int he = clampi(A.cell_offsets[coff + hl + 1] - 1 + abase, A.nat_total);
-    if (hs >= he) continue;
-    const int hc0 = hl % g.ns[0] + 1, hc1 = (hl / g.ns[0]) % g.ns[1] + 1, hc2 = hl / (g.ns[0] * g.ns[1]) + 1;
-    int cstart = 0, ccount = 0;
-    unsigned slp = 0;
-    if (lane < nst) {
-      float ox, oy, oz;
-      const int lin = stencil_cell(g, dtab, 32, sx, sy, hc0, hc1, hc2, lane, slp, ox, oy, oz);
-      if (lin >= 0) {
-        cstart = clampi(A.cell_offsets[coff + lin] - 1 + abase, A.nat_total);
-        ccount = max(clampi(A.cell_offsets[coff + lin + 1] - 1 + abase, A.nat_total) - cstart, 0);
-      }
-    }
-    int incl = ccount;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int v = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += v;
-    }
-    const int tg = __shfl_sync(0xffffffffu, incl, 31);
-    if (tg > kEmitCand) continue;  // left to the screening fill
-    const int nw = (tg + 31) >> 5;
-    __syncwarp();  // the previous cell's tables are no longer read
-    E.qstart[lane] = cstart;
-    E.qexcl[lane] = incl - ccount;
-    E.qslp[lane] = slp;
-    for (int f = incl - ccount; f < incl; ++f) E.cq[f] = (unsigned char)lane;
-
-    for (int hb = hs; hb < he; hb += 32) {
-      const int nb = min(32, he - hb);
-      __syncwarp();
-      if (lane < nb) {
-        const int si = hb + lane;
-        const int orig = clampi(A.perm[si] - 1, g.nat - 1);
-        E.horig[lane] = orig;
-        E.hbase[lane] = (long long)A.first[abase + orig] - 1;
-        E.hmeta[lane] = __float_as_uint(A.rec[si].w);
-        E.hx[lane][0] = A.Xs[3LL * si + 0];
-        E.hx[lane][1] = A.Xs[3LL * si + 1];
-        E.hx[lane][2] = A.Xs[3LL * si + 2];
+      E.sbuf[3 * lane + 0] = S[0];
+      E.sbuf[3 * lane + 1] = S[1];
+      E.sbuf[3 * lane + 2] = S[2];
+      if (A.oR) {
+        double R[3];
+        pair_R(g, cs_tab, xi, xj, S[0], S[1], S[2], act, R);
+        E.rbuf[3 * lane + 0] = R[0];
+        E.rbuf[3 * lane + 1] = R[1];
+        E.rbuf[3 * lane + 2] = R[2];
       }
       __syncwarp();
-      // the atom's acceptance words (bit f = candidate f), one atom ahead
-      unsigned m_next = lane < nw ? A.masks[(long long)hb * kMaskWords + lane] : 0u;
-      for (int a = 0; a < nb; ++a) {
-        const unsigned m = m_next;
-        if (a + 1 < nb && lane < nw) m_next = A.masks[(long long)(hb + a + 1) * kMaskWords + lane];
-        // inclusive prefix of the words' set bits over lanes 0..15 (nw <= 12)
-        int wincl = __popc(m);
+      const long long wend = 3 * min(out0 + nact, A.capacity);  // words that fit the buffers
 #pragma unroll
-        for (int o = 1; o < 16; o <<= 1) {
-          const int v = __shfl_up_sync(0xffffffffu, wincl, o);
-          if (lane >= o) wincl += v;
-        }
-        const int n = __shfl_sync(0xffffffffu, wincl, 15);
-        if (n == 0) continue;
-        const double* xi = E.hx[a];
-        const unsigned mi = E.hmeta[a];
-        const long long base = E.hbase[a];
-        const TI ti = TI(E.horig[a]) + 1;
-        for (int p = 0; p < n; p += 32) {
-          const int r = p + lane;
-          const bool act = r < n;
-          const int rr = min(r, n - 1);
-          // word of the rr-th accepted candidate: smallest w with wincl_w > rr
-          int w = 0;
-#pragma unroll
-          for (int step = 8; step > 0; step >>= 1) {
-            const int v = __shfl_sync(0xffffffffu, wincl, w + step - 1);
-            if (v <= rr) w += step;
-          }
-          const unsigned mw = __shfl_sync(0xffffffffu, m, w);
-          const int wex = __shfl_sync(0xffffffffu, wincl, w) - __popc(mw);
-          const int f = 32 * w + nth_set_bit(mw, rr - wex);  // w < nw, so f < kEmitCand
-          const int q = E.cq[f];
-          const int slot_j = clampi(E.qstart[q] + f - E.qexcl[q], A.nat_total - 1);
-          const unsigned mj = __float_as_uint(A.rec[slot_j].w);
-          double xj[3];
-          xj[0] = A.Xs[3LL * slot_j + 0];
-          xj[1] = A.Xs[3LL * slot_j + 1];
-          xj[2] = A.Xs[3LL * slot_j + 2];
-          const int oj = clampi(A.perm[slot_j] - 1, g.nat - 1);
-          int S[3];
-          pair_S(g, xi, xj, mi, cand_word(E.qslp[q], mj), S);
-          const long long out = base + r;
-          const bool wr = act && out < A.capacity;
-          if (act && !wr) atomicOr(A.err, kFlagCapacity);
-          if (wr) {
-            A.oi[out] = ti;
-            A.oj[out] = TI(oj) + 1;
-            A.oS[3 * out + 0] = TI(S[0]);
-            A.oS[3 * out + 1] = TI(S[1]);
-            A.oS[3 * out + 2] = TI(S[2]);
-          }
-          if (A.oR) {
-            double R[3];
-            pair_R(g, cs_tab, xi, xj, S[0], S[1], S[2], act, R);
-            if (wr) {
-              A.oR[3 * out + 0] = R[0];
-              A.oR[3 * out + 1] = R[1];
-              A.oR[3 * out + 2] = R[2];
-            }
-          }
+      for (int k = 0; k < 3; ++k) {
+        const int t = lane + 32 * k;
+        const long long wpos = 3 * out0 + t;
+        if (t < 3 * nact && wpos < wend) {
+          A.oS[wpos] = TI(E.sbuf[t]);
+          if (A.oR) A.oR[wpos] = E.rbuf[t];
         }
       }
+      __syncwarp();
+    };
+    for (int a = 0; a < na; ++a) {
+      const int n = E.n[a];
+      const uint2* lst = A.lists + (c0 + a) * K;
+      for (int p = 0; p < n; p += 32) {
+        const int r = p + lane;
+        const uint2 e = lst[min(r, n - 1)];
+        const int slot_j = clampi(int(e.x), A.nat_total - 1);
+        const double xj0 = A.Xs[3LL * slot_j + 0];
+        const double xj1 = A.Xs[3LL * slot_j + 1];
+        const double xj2 = A.Xs[3LL * slot_j + 2];
+        const long long oj = (long long)A.perm[slot_j];
+        if (pv) finish();
+        pv = true;
+        pa = a;
+        pr = r;
+        pn = n;
+        pcw = e.y;
+        poj = oj;
+        pxj0 = xj0;
+        pxj1 = xj1;
+        pxj2 = xj2;
+      }
     }
+    if (pv) finish();
   }
 }
 
 template <typename TI, bool BATCH>
 static void launch_modes(int mode, const PairArgs<TI>& a, int num_sms, cudaStream_t st) {
   if (a.nat_total <= 0 || a.ncells_total <= 0) return;
+  // grids: at most the resident blocks per SM (or the tuned number) on every SM
+  const int pbps = a.pair_blocks_per_sm > 0 ? min(a.pair_blocks_per_sm, kMinBlocks) : kMinBlocks;
+  const int ebps = a.emit_blocks_per_sm > 0 ? min(a.emit_blocks_per_sm, 16) : kEmitMinBlocks;
   long long blocks = ((long long)a.ncells_total + kPairWarps - 1) / kPairWarps;
-  if (blocks > (long long)num_sms * kMinBlocks) blocks = (long long)num_sms * kMinBlocks;
+  if (blocks > (long long)num_sms * pbps) blocks = (long long)num_sms * pbps;
   if (blocks < 1) blocks = 1;
   switch (mode) {
     case kModeCount: k_pairs<TI, kModeCount, BATCH><<<int(blocks), kPairWarps * 32, 0, st>>>(a); break;
     case kModeFill: {
-      if (!BATCH) k_cs_table<<<1, 128, 0, st>>>(a.g, a.cs_table);
-      long long eb = ((long long)a.ncells_total + kEmitWarps - 1) / kEmitWarps;
-      if (eb > (long long)num_sms * 16) eb = (long long)num_sms * 16;
-      k_emit<TI, BATCH><<<int(eb), kEmitWarps * 32, 0, st>>>(a);
+      if (!BATCH) k_cs_table<<<1, 128, 0, st>>>(a.g, a.cs_table, a.cap_rec, a.list_cap, a.err);
+      if (a.list_cap > 0) {
+        long long eb = ((long long)a.nat_total + 32 * kEmitWarps - 1) / (32 * kEmitWarps);
+        if (eb > (long long)num_sms * ebps) eb = (long long)num_sms * ebps;
+        k_emit<TI, BATCH><<<int(eb), kEmitWarps * 32, 0, st>>>(a);
+      }
       k_pairs<TI, kModeFill, BATCH><<<int(blocks), kPairWarps * 32, 0, st>>>(a);
       break;
     }
     default:
-      if (!BATCH) k_cs_table<<<1, 128, 0, st>>>(a.g, a.cs_table);
+      if (!BATCH) k_cs_table<<<1, 128, 0, st>>>(a.g, a.cs_table, nullptr, 0, a.err);
       k_pairs<TI, kModeLazyR6, BATCH><<<int(blocks), kPairWarps * 32, 0, st>>>(a);
       break;
   }

@@ -6,11 +6,12 @@ namespace nl {
 
 enum PairMode : int { kModeCount = 0, kModeFill = 1, kModeLazyR6 = 2 };
 
-// The count pass records, per home atom, the acceptance bitmask of its
-// candidates (bit f = the f-th candidate in the reference's traversal order)
-// when the home cell's stencil has at most 32 cells and 32*kMaskWords
-// candidates.  The fill pass then writes those pairs without screening again.
-constexpr int kMaskWords = 12;
+// The count pass records, per home atom, its accepted candidates in the
+// reference's traversal order -- (sorted slot of j, candidate word) -- in a
+// list of kListCap entries.  The write pass (k_emit) turns the lists into
+// i, j, S, R without screening again; cells with an atom of more than
+// kListCap pairs are listed for the screening write pass instead.
+constexpr int kListCap = 64;
 
 // doubles in one C'S table (|S_k| <= 2)
 constexpr int kCsTableDoubles = 3 * 125;
@@ -44,10 +45,16 @@ struct PairArgs {
   double* oR;               // may be null (R not wanted)
   long long capacity;       // pairs the output buffers hold
   double* per_atom;         // lazy: per-atom reduction
-  unsigned* masks;          // per sorted slot: kMaskWords acceptance words
+  uint2* lists;             // per sorted slot: list_cap accepted (slot_j, candidate word)
+  int* lcount;              // per sorted slot: pairs of the atom (count pass)
+  int* sorig;               // per sorted slot: original atom index within the launch (0-based)
+  int list_cap;             // kListCap, or 0: no lists (every cell takes the screening write pass)
+  int* cap_rec;             // list_cap of the count pass (the write pass checks it)
   double* cs_table;         // C'S for |S_k| <= 2 (built once per call by k_cs_table)
-  int* unmasked;            // count pass: home cells left to the screening fill
+  int* unmasked;            // count pass: home cells left to the screening write pass
   int* n_unmasked;          // length of that list
+  int pair_blocks_per_sm;   // launch tuning (0 = default): count / screening grids
+  int emit_blocks_per_sm;   // launch tuning (0 = default): list write grid
   unsigned long long* stats;  // [0] += FP64 rechecks
   unsigned* err;
 };

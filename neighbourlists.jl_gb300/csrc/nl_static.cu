@@ -68,11 +68,13 @@ extern "C" int nl_neighbour_list_static(const double* d_X, int64_t nat, const do
   if (!ncells) return nl::report(NL_ERR_ARG, "null argument");
   if (ncells[0] < 1 || ncells[1] < 1 || ncells[2] < 1) return nl::report(NL_ERR_ARG, "ncells must be >= 1");
   const long double cells = (long double)ncells[0] * ncells[1] * ncells[2];
-  const size_t need = cells > 2147483646.0L ? 0 : nl_workspace_bytes(nat, int64_t(cells));
+  // the static scratch holds the pair lists only for small systems; larger
+  // ones run with the screening write pass (same results)
+  const size_t need = cells > 2147483646.0L ? 0 : nl::workspace_min_bytes(nat, int64_t(cells));
   if (need == 0 || need > kStaticScratchBytes)
     return nl::report(NL_ERR_NOMEM, "system needs " + std::to_string(need) +
                                         " bytes of scratch, more than the 32 MiB static scratch of "
-                                        "nl_neighbour_list_static (about 600k atoms at liquid density); "
+                                        "nl_neighbour_list_static (about 500k atoms at liquid density); "
                                         "use nl_neighbour_list with a caller-allocated workspace");
   void* scratch = nullptr;
   int s = scratch_for_current_device(&scratch);

@@ -16,7 +16,7 @@ import torch
 
 from . import _lib
 from ._lib import check, lib
-from .api import PairList, _index_bytes, _pbc, _ptr, _stream_handle, _tdtype, analyze_cell
+from .api import PairList, SortedCellList, _index_bytes, _pbc, _ptr, _stream_handle, _tdtype, analyze_cell
 
 _D = C.POINTER(C.c_double)
 _I64 = C.POINTER(C.c_int64)
@@ -52,6 +52,8 @@ class NeighbourListEngine:
             capacity = int(1.15 * self.nat * rho * 4.0 / 3.0 * np.pi * self.cutoff ** 3) + 1024
         self._alloc(capacity)
         self.last_total = None
+        self.tuning = _lib.Tuning(0, 0)
+        self._graph = None
 
     def _alloc(self, capacity: int):
         capacity = max(int(capacity), 1)
@@ -63,6 +65,7 @@ class NeighbourListEngine:
 
     def _call(self, X: torch.Tensor, total_ptr, stream):
         p = self.plan
+        check(lib().nl_set_tuning(C.byref(self.tuning)))
         return lib().nl_neighbour_list(
             _ptr(X), self.nat, p.cell_cm.ctypes.data_as(_D), p.inv_cm.ctypes.data_as(_D), p.ncells.ctypes.data_as(_I64),
             p.nxyz.ctypes.data_as(_I64), self.pbc.ctypes.data_as(_U8), self.cutoff, self.ib, _ptr(self.perm),
@@ -85,6 +88,26 @@ class NeighbourListEngine:
         self.last_total = int(total.value)
         return self.last_total
 
+    def set_tuning(self, pair_blocks_per_sm: int = 0, emit_blocks_per_sm: int = 0) -> None:
+        self.tuning = _lib.Tuning(int(pair_blocks_per_sm), int(emit_blocks_per_sm))
+
+    def capture(self, X: torch.Tensor) -> torch.cuda.CUDAGraph:
+        """Captures one launch on X in a CUDA graph; ``replay()`` re-runs it."""
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            self.launch(X)
+        torch.cuda.current_stream().wait_stream(side)
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.launch(X)
+        self._graph = g
+        return g
+
+    def replay(self) -> None:
+        self._graph.replay()
+
     def sync_status(self, stream=None) -> None:
         check(lib().nl_sync_status(_ptr(self.ws), _stream_handle(stream)))
 
@@ -96,6 +119,14 @@ class NeighbourListEngine:
         r = C.c_int64(0)
         check(lib().nl_last_recheck_count(_ptr(self.ws), _stream_handle(stream), C.byref(r)))
         return int(r.value)
+
+    def cell_list(self, X: torch.Tensor) -> SortedCellList:
+        """The SortedCellList of the last launch (shares the workspace, whose
+        records lazy_reduce reuses)."""
+        p = self.plan
+        return SortedCellList(self.Xs, X, self.perm, self.cid, self.offs, self.cell.copy(), p.inv_cell,
+                              tuple(bool(b) for b in self.pbc), self.cutoff, p.ncells, p.ncells_total, p, self.ws,
+                              True)
 
     def pairlist(self, X: torch.Tensor) -> PairList:
         P = self.total_pairs()

@@ -1,0 +1,325 @@
+"""Continuous-batching request loop over the batched engine.
+
+Requests (one system each: positions, cell, cutoff, pbc) arrive over time.
+The server keeps per-slot device arenas resident -- positions, workspace,
+cell-list arrays and pair buffers, grown on demand and then reused -- and
+runs up to ``slots`` batches at once, each on its own CUDA stream.  Whenever a
+slot is free, every queued request that fits is admitted into one new batch:
+admission is bounded by the predicted pair-buffer bytes of all in-flight
+batches (``pair_budget_bytes``) and by the batch's atom and system limits, in
+arrival order.  Requests that arrive while batches are on the GPU wait only
+until a slot and budget free up; their batch then overlaps with the batches
+still running.  A finished batch hands each request its own views of the
+outputs (or copies, with ``copy_results``); a batch whose pairs exceed the
+prediction is re-run with larger buffers.
+
+``mode="plain"`` serves every request alone through the single-system entry
+point on the same slots (the per-request baseline).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import time
+from collections import deque
+from dataclasses import dataclass, field
+from typing import Deque, List, Optional
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import check, lib
+from .api import _colmajor, _index_bytes, _pbc, _ptr, _tdtype, analyze_cell
+
+_D = C.POINTER(C.c_double)
+_I64 = C.POINTER(C.c_int64)
+_U8 = C.POINTER(C.c_uint8)
+
+
+@dataclass
+class Request:
+    rid: int
+    X: np.ndarray              # (n, 3) float64 positions (host)
+    cell: np.ndarray           # 3x3, rows are lattice vectors
+    cutoff: float
+    pbc: tuple
+    t_arrive: float = 0.0      # server clock (s)
+    t_done: Optional[float] = None
+    npairs: Optional[int] = None
+    result: Optional[dict] = field(default=None, repr=False)  # first, i, j, S, R (device tensors)
+
+    @property
+    def nat(self) -> int:
+        return int(self.X.shape[0])
+
+    def predicted_pairs(self) -> int:
+        """Expected pairs of a homogeneous system plus headroom."""
+        vol = abs(float(np.linalg.det(np.asarray(self.cell, dtype=np.float64))))
+        n = self.nat
+        exp = n * (n / vol) * 4.0 / 3.0 * math.pi * self.cutoff ** 3 if vol > 0 else 0.0
+        return int(1.3 * exp + 8 * math.sqrt(exp + 1.0)) + 64
+
+
+class _Slot:
+    """One in-flight batch: stream, completion event and resident arenas."""
+
+    def __init__(self, device):
+        self.device = device
+        self.stream = torch.cuda.Stream(device=device)
+        self.event = torch.cuda.Event()
+        self.bufs = {}
+        self.h_X = None
+        self.reqs: List[Request] = []
+        self.handle = None
+        self.pred_bytes = 0
+        self.busy = False
+
+    def buf(self, name, numel, dtype):
+        t = self.bufs.get(name)
+        if t is None or t.numel() < numel or t.dtype != dtype:
+            t = torch.empty(max(int(numel * 1.25), 1), dtype=dtype, device=self.device)
+            self.bufs[name] = t
+        return t
+
+    def host_X(self, n):
+        if self.h_X is None or self.h_X.shape[0] < n:
+            self.h_X = torch.empty((max(int(n * 1.25), 1), 3), dtype=torch.float64).pin_memory()
+        return self.h_X
+
+
+class NeighbourListServer:
+    def __init__(self, pair_budget_bytes: float = 40e9, slots: int = 3, max_batch_atoms: int = 4_000_000,
+                 max_batch_systems: int = 8192, int_type=torch.int32, with_R: bool = True, device="cuda",
+                 mode: str = "batched", copy_results: bool = False):
+        if mode not in ("batched", "plain"):
+            raise ValueError("mode must be 'batched' or 'plain'")
+        self.ib = _index_bytes(int_type)
+        self.ti = _tdtype(self.ib)
+        self.with_R = with_R
+        self.device = torch.device(device)
+        self.mode = mode
+        self.copy_results = copy_results
+        self.budget = float(pair_budget_bytes)
+        self.max_atoms = int(max_batch_atoms)
+        self.max_systems = int(max_batch_systems) if mode == "batched" else 1
+        self.bytes_per_pair = 2 * self.ib + 3 * self.ib + (24 if with_R else 0)
+        self.slots = [_Slot(self.device) for _ in range(slots)]
+        self.queue: Deque[Request] = deque()
+        self.inflight_bytes = 0
+        self.batches = 0
+        self.reruns = 0
+
+    # ----------------------------------------------------------- requests --
+    def submit(self, req: Request) -> None:
+        self.queue.append(req)
+
+    def busy(self) -> bool:
+        return bool(self.queue) or any(s.busy for s in self.slots)
+
+    def poll(self, now_fn=time.perf_counter) -> List[Request]:
+        """Finishes every slot whose batch completed; returns its requests."""
+        done = []
+        for s in self.slots:
+            if s.busy and s.event.query():
+                done.extend(self._finish(s, now_fn()))
+        return done
+
+    def admit(self) -> int:
+        """Launches queued requests on free slots; returns requests admitted."""
+        n = 0
+        for s in self.slots:
+            if s.busy or not self.queue:
+                continue
+            reqs, atoms, pred = [], 0, 0
+            while self.queue and len(reqs) < self.max_systems:
+                r = self.queue[0]
+                rb = r.predicted_pairs() * self.bytes_per_pair
+                if reqs and (atoms + r.nat > self.max_atoms or self.inflight_bytes + pred + rb > self.budget):
+                    break
+                if not reqs and self.inflight_bytes + rb > self.budget and any(x.busy for x in self.slots):
+                    break  # wait for memory to free up
+                reqs.append(self.queue.popleft())
+                atoms += r.nat
+                pred += rb
+            if not reqs:
+                break
+            self._launch(s, reqs, pred)
+            n += len(reqs)
+        return n
+
+    # ------------------------------------------------------------ batches --
+    def _launch(self, s: _Slot, reqs: List[Request], pred_bytes: int) -> None:
+        s.reqs, s.pred_bytes, s.busy = reqs, pred_bytes, True
+        self.inflight_bytes += pred_bytes
+        self.batches += 1
+        nat = sum(r.nat for r in reqs)
+        hX = s.host_X(nat)
+        hXn = hX.numpy()
+        o = 0
+        for r in reqs:
+            hXn[o:o + r.nat] = r.X
+            o += r.nat
+        Xd = s.buf("X", 3 * max(nat, 1), torch.float64)
+        with torch.cuda.stream(s.stream):
+            if nat:
+                Xd[:3 * nat].view(nat, 3).copy_(hX[:nat], non_blocking=True)
+            cap = max(sum(r.predicted_pairs() for r in reqs), 1)
+            if self.mode == "batched":
+                self._launch_batched(s, reqs, nat, cap)
+            else:
+                self._launch_plain(s, reqs[0], cap)
+            s.event.record(s.stream)
+
+    def _outputs(self, s: _Slot, cap: int):
+        i = s.buf("i", cap, self.ti)
+        j = s.buf("j", cap, self.ti)
+        S = s.buf("S", 3 * cap, self.ti)
+        R = s.buf("R", 3 * cap, torch.float64) if self.with_R else None
+        return i, j, S, R, min(i.numel(), j.numel(), S.numel() // 3, R.numel() // 3 if R is not None else 1 << 62)
+
+    def _launch_batched(self, s: _Slot, reqs: List[Request], nat: int, cap: int) -> None:
+        L = lib()
+        n = len(reqs)
+        cells = np.concatenate([_colmajor(r.cell) for r in reqs])
+        cut = np.array([r.cutoff for r in reqs], dtype=np.float64)
+        pb = np.concatenate([_pbc(r.pbc) for r in reqs])
+        nats = np.array([r.nat for r in reqs], dtype=np.int64)
+        if s.handle is not None:
+            L.nl_batch_destroy(s.handle)
+            s.handle = None
+        h = C.c_void_p()
+        check(L.nl_batch_create_auto(cells.ctypes.data_as(_D), cut.ctypes.data_as(_D), pb.ctypes.data_as(_U8),
+                                     nats.ctypes.data_as(_I64), n, self.ib, C.byref(h)))
+        s.handle = h
+        na, nc = C.c_int64(), C.c_int64()
+        check(L.nl_batch_sizes(h, C.byref(na), C.byref(nc)))
+        ws = s.buf("ws", int(L.nl_batch_workspace_bytes(h)), torch.uint8)
+        st = C.c_void_p(s.stream.cuda_stream)
+        check(L.nl_batch_upload(h, _ptr(ws), ws.numel(), st))
+        s.nc = int(nc.value)
+        perm = s.buf("perm", max(nat, 1), self.ti)
+        Xs = s.buf("Xs", 3 * max(nat, 1), torch.float64)
+        cid = s.buf("cid", max(nat, 1), self.ti)
+        offs = s.buf("offs", s.nc + n, self.ti)
+        first = s.buf("first", nat + n, self.ti)
+        po = s.buf("po", n + 1, torch.int64)
+        i, j, S, R, capacity = self._outputs(s, cap)
+        s.launch_args = (perm, Xs, cid, offs, first, po, ws)
+        s.capacity = capacity
+        check(L.nl_batch_neighbour_list(h, _ptr(s.bufs["X"]), _ptr(perm), _ptr(Xs), _ptr(cid),
+                                        C.c_void_p(offs.data_ptr()), C.c_void_p(first.data_ptr()),
+                                        C.c_void_p(po.data_ptr()), capacity, _ptr(i), _ptr(j), _ptr(S), _ptr(R),
+                                        None, _ptr(ws), ws.numel(), st))
+
+    def _launch_plain(self, s: _Slot, r: Request, cap: int) -> None:
+        L = lib()
+        plan = analyze_cell(r.cell, r.cutoff, self.ti)
+        nat = r.nat
+        ws = s.buf("ws", int(L.nl_workspace_bytes(nat, plan.ncells_total)), torch.uint8)
+        perm = s.buf("perm", max(nat, 1), self.ti)
+        Xs = s.buf("Xs", 3 * max(nat, 1), torch.float64)
+        cid = s.buf("cid", max(nat, 1), self.ti)
+        offs = s.buf("offs", plan.ncells_total + 1, self.ti)
+        first = s.buf("first", nat + 1, self.ti)
+        i, j, S, R, capacity = self._outputs(s, cap)
+        pb = _pbc(r.pbc)
+        s.launch_args = (plan, ws, first)
+        s.capacity = capacity
+        check(L.nl_neighbour_list(_ptr(s.bufs["X"]), nat, plan.cell_cm.ctypes.data_as(_D),
+                                  plan.inv_cm.ctypes.data_as(_D), plan.ncells.ctypes.data_as(_I64),
+                                  plan.nxyz.ctypes.data_as(_I64), pb.ctypes.data_as(_U8), float(r.cutoff), self.ib,
+                                  _ptr(perm), _ptr(Xs), _ptr(cid), C.c_void_p(offs.data_ptr()),
+                                  C.c_void_p(first.data_ptr()), capacity, _ptr(i), _ptr(j), _ptr(S), _ptr(R), None,
+                                  _ptr(ws), ws.numel(), C.c_void_p(s.stream.cuda_stream)))
+
+    def _finish(self, s: _Slot, t_done: float) -> List[Request]:
+        L = lib()
+        st = C.c_void_p(s.stream.cuda_stream)
+        if self.mode == "batched":
+            perm, Xs, cid, offs, first, po, ws = s.launch_args
+            n = len(s.reqs)
+            po_h = po[:n + 1].cpu().numpy()
+            total = int(po_h[-1])
+        else:
+            plan, ws, first = s.launch_args
+            total = int(first[s.reqs[0].nat].item()) - 1
+            po_h = np.array([0, total], dtype=np.int64)
+        status = L.nl_sync_status(_ptr(ws), st)
+        if status == _lib.NL_ERR_CAPACITY or total > s.capacity:
+            # more pairs than predicted: run the batch again with room for all
+            self.reruns += 1
+            with torch.cuda.stream(s.stream):
+                if self.mode == "batched":
+                    nat = sum(r.nat for r in s.reqs)
+                    self._launch_batched(s, s.reqs, nat, total)
+                else:
+                    self._launch_plain(s, s.reqs[0], total)
+            s.stream.synchronize()
+            return self._finish(s, t_done)
+        check(status)
+        i, j, S, R = s.bufs["i"], s.bufs["j"], s.bufs["S"], s.bufs.get("R")
+        a0 = 0
+        for k, r in enumerate(s.reqs):
+            p0, p1 = int(po_h[k]), int(po_h[k + 1])
+            f0 = a0 + k if self.mode == "batched" else 0
+            res = {"first": first[f0:f0 + r.nat + 1], "i": i[p0:p1], "j": j[p0:p1],
+                   "S": S[3 * p0:3 * p1].view(-1, 3), "R": R[3 * p0:3 * p1].view(-1, 3) if R is not None else None}
+            if self.copy_results:
+                res = {key: (v.clone() if v is not None else None) for key, v in res.items()}
+            r.result, r.npairs, r.t_done = res, p1 - p0, t_done
+            a0 += r.nat
+        done = s.reqs
+        s.reqs, s.busy = [], False
+        self.inflight_bytes -= s.pred_bytes
+        s.pred_bytes = 0
+        return done
+
+    def close(self) -> None:
+        for s in self.slots:
+            if s.handle is not None:
+                lib().nl_batch_destroy(s.handle)
+                s.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -------------------------------------------------------------- traces --
+    def run_trace(self, requests: List[Request], idle_sleep: float = 20e-6) -> dict:
+        """Serves requests whose t_arrive are offsets (s) from the start, with
+        the wall clock as the arrival clock.  Returns latency / throughput."""
+        reqs = sorted(requests, key=lambda r: r.t_arrive)
+        t0 = time.perf_counter()
+        k = 0
+        while k < len(reqs) or self.busy():
+            now = time.perf_counter() - t0
+            while k < len(reqs) and reqs[k].t_arrive <= now:
+                self.submit(reqs[k])
+                k += 1
+            finished = self.poll(lambda: time.perf_counter() - t0)
+            launched = self.admit()
+            if launched or finished:
+                continue
+            if not self.busy() and k < len(reqs):
+                # idle until the next arrival
+                time.sleep(max(0.0, min(reqs[k].t_arrive - (time.perf_counter() - t0), 1e-3)))
+            else:
+                time.sleep(idle_sleep)
+        wall = time.perf_counter() - t0
+        lat = np.array([r.t_done - r.t_arrive for r in reqs]) * 1e3
+        pairs = sum(r.npairs for r in reqs)
+        span = max(r.t_done for r in reqs) - min(r.t_arrive for r in reqs)
+        return {"requests": len(reqs), "batches": self.batches, "reruns": self.reruns,
+                "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                "mean_ms": float(lat.mean()), "systems_per_s": len(reqs) / span, "pairs_per_s": pairs / span,
+                "wall_s": wall}
+
+
+def poisson_trace(systems, rate: float, seed: int = 0) -> List[Request]:
+    """Requests for (X, cell, cutoff, pbc) tuples with Poisson arrivals."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, size=len(systems)))
+    return [Request(k, x, c, rc, p, float(t[k])) for k, (x, c, rc, p) in enumerate(systems)]

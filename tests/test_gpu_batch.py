@@ -92,3 +92,38 @@ def test_batch_matches_single_calls_and_repeats(nlpkg, orc):
 def test_batch_capacity_growth(nlpkg, orc):
     systems = cf.batch_systems(10, seed=11, nmax=300)
     check_batch(nlpkg, orc, systems, capacity=5)
+
+
+def test_batch_graph_replay_and_autotune(nlpkg, orc):
+    """A captured CUDA graph and every tuned launch shape give the same bits."""
+    systems = cf.batch_systems(24, seed=13, nmax=500)
+    b = nlpkg.BatchNeighbourList([(x.shape[0], c, rc, p) for (x, c, rc, p) in systems])
+    X = torch.from_numpy(np.concatenate([s[0] for s in systems])).cuda()
+    t = b.run(X)
+    ref = [x[:t].clone() for x in (b.i, b.j, b.S)] + [b.R[:t].clone().view(torch.int64), b.first.clone()]
+    res = nlpkg.autotune(b, X, candidates=[(3, 4), (7, 16), (5, 8)], reps=1)
+    assert len(res["trials"]) == 3
+    b.capture(X)
+    for _ in range(2):
+        b.replay()
+    torch.cuda.synchronize()
+    b.sync_status()
+    got = [x[:t] for x in (b.i, b.j, b.S)] + [b.R[:t].view(torch.int64), b.first]
+    for u, v in zip(ref, got):
+        assert torch.equal(u, v)
+
+
+def test_engine_graph_replay(nlpkg, orc):
+    X, C, L = cf.rand_config(20000, seed=21)
+    eng = nlpkg.NeighbourListEngine(X.shape[0], C, 5.0, (True, True, True))
+    Xd = torch.from_numpy(X).cuda()
+    t = eng.run(Xd)
+    eng.set_tuning(3, 4)
+    eng.capture(Xd)
+    eng.i[:t].zero_()
+    eng.replay()
+    torch.cuda.synchronize()
+    eng.sync_status()
+    o = orc.neighbour_list(X, 5.0, C, (True, True, True), nthreads=8)
+    assert np.array_equal(eng.i[:t].cpu().numpy().astype(np.int64), o.i)
+    assert np.array_equal(eng.R[:t].cpu().numpy().view(np.int64), o.R.view(np.int64))

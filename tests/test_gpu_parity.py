@@ -260,3 +260,24 @@ def test_binning_on_cell_boundaries(nlpkg, orc):
     o = orc.build_cell_list(X2, 3.0, C2, (True, True, False))
     np.testing.assert_array_equal(to_np(g.cell_id).astype(np.int64), o.cell_id)
     np.testing.assert_array_equal(to_np(g.perm).astype(np.int64), o.perm)
+
+
+@pytest.mark.parametrize("case", ["10k", "fcc"])
+def test_minimal_workspace_screening_write(nlpkg, orc, case):
+    """A workspace without room for the pair lists: every cell goes through
+    the screening write pass; results are identical."""
+    if case == "10k":
+        X, C, L = cf.rand_config(10000, seed=0)
+        pbc, rc = (True, True, True), 5.0
+    else:
+        X, C, pbc = cf.fcc_sheared(n=6, seed=2)
+        rc = 5.0
+    eng = nlpkg.NeighbourListEngine(X.shape[0], C, rc, pbc)
+    lib = nlpkg._lib.lib()
+    full = int(lib.nl_workspace_bytes(X.shape[0], eng.plan.ncells_total))
+    small = int(lib.nl_workspace_min_bytes(X.shape[0], eng.plan.ncells_total))
+    assert 0 < small < full
+    eng.ws = torch.empty(small, dtype=torch.uint8, device="cuda")
+    eng.run(torch.from_numpy(X).cuda())
+    o = orc.neighbour_list(X, rc, C, pbc, nthreads=8)
+    assert_identical(eng.pairlist(None), o)

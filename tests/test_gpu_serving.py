@@ -1,0 +1,66 @@
+"""The continuous-batching server: every result is the same alone and in the
+mix (bit for bit: integer outputs and the bits of R), equal to the oracle,
+with budget-bounded admission and re-runs when the pair prediction is low."""
+import numpy as np
+import pytest
+import torch
+
+import configs as cf
+
+pytestmark = pytest.mark.gpu
+
+
+def mixed_systems():
+    systems = cf.batch_systems(40, seed=31, nmax=900)
+    X, C, L = cf.rand_config(20000, seed=32)
+    systems.insert(17, (X, C, 5.0, (True, True, True)))
+    return systems
+
+
+def serve(nlpkg, systems, rate=1e6, **kw):
+    srv = nlpkg.NeighbourListServer(copy_results=True, **kw)
+    reqs = nlpkg.poisson_trace(systems, rate=rate, seed=1)
+    stats = srv.run_trace(reqs)
+    srv.close()
+    return reqs, stats, srv
+
+
+def same(a, b):
+    return (torch.equal(a["first"], b["first"]) and torch.equal(a["i"], b["i"]) and torch.equal(a["j"], b["j"])
+            and torch.equal(a["S"], b["S"]) and torch.equal(a["R"].view(torch.int64), b["R"].view(torch.int64)))
+
+
+def test_same_alone_and_in_mix(nlpkg, orc):
+    systems = mixed_systems()
+    mix, stats, srv = serve(nlpkg, systems, slots=2)
+    assert stats["requests"] == len(systems) and srv.batches < len(systems)  # requests were batched
+    for r in mix:
+        alone, _, _ = serve(nlpkg, [(r.X, r.cell, r.cutoff, r.pbc)], slots=1)
+        assert same(alone[0].result, r.result), r.rid
+    for r in mix[::7]:
+        o = orc.neighbour_list(r.X, r.cutoff, r.cell, r.pbc, nthreads=8)
+        assert np.array_equal(r.result["i"].cpu().numpy().astype(np.int64), o.i)
+        assert np.array_equal(r.result["R"].cpu().numpy().view(np.int64), o.R.view(np.int64))
+
+
+def test_plain_mode_matches_batched(nlpkg):
+    systems = mixed_systems()[:12]
+    a, _, _ = serve(nlpkg, systems, slots=2)
+    b, _, srv = serve(nlpkg, systems, slots=2, mode="plain")
+    assert srv.batches == len(systems)
+    for x, y in zip(a, b):
+        assert same(x.result, y.result)
+
+
+def test_budget_bounds_admission_and_reruns(nlpkg, monkeypatch):
+    systems = mixed_systems()[:16]
+    ref, _, _ = serve(nlpkg, systems, slots=2)
+    # a budget below one batch's worth serialises admission
+    _, stats, srv = serve(nlpkg, systems, slots=3, pair_budget_bytes=2e5)
+    assert srv.batches > 3
+    # a prediction far too low forces re-runs; results do not change
+    monkeypatch.setattr(nlpkg.Request, "predicted_pairs", lambda self: 1)
+    got, stats, srv = serve(nlpkg, systems, slots=2)
+    assert stats["reruns"] > 0
+    for x, y in zip(ref, got):
+        assert same(x.result, y.result)
