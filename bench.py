@@ -65,7 +65,7 @@ def measured_peaks():
 
 def ncu_traffic():
     """Per-launch DRAM bytes of the fill kernel from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "fill_kernel_1M_traffic.json")
+    p = os.path.join(ROOT, "profiles", "k_emit_1M_traffic.json")
     if os.path.exists(p):
         with open(p) as f:
             return json.load(f)
@@ -276,6 +276,8 @@ def run_gpu(args):
         extra["batched"] = bench_batched(nl, dev, stream, flush, extra_steps)
         torch.cuda.empty_cache()
         extra["atoms_4m"] = bench_4m(nl, dev, stream, flush, extra_steps)
+        torch.cuda.empty_cache()
+        extra["serving"] = bench_serving(nl, dev)
     if rank != 0:
         return
     peak, peak_kind = measured_peaks()
@@ -399,6 +401,46 @@ def bench_lazy(nl, eng, Xd, X, C, pbc, stream, flush, steps):
             "pairs_per_s": eng.last_total / (ms * 1e-3), "max_rel_err_vs_oracle": float(rel.max()),
             "bit_identical": bool(np.array_equal(got.view(np.int64), ref.view(np.int64))),
             "tolerance": 1e-12}
+
+
+def serving_requests(n_req, seed=7):
+    """Requests drawn from the batched distribution, 5% replaced by large
+    systems of 50k-200k atoms (density 0.05, cutoff 5 A, full pbc)."""
+    import configs as cf
+
+    systems = cf.batch_systems(n_req, seed=seed)
+    rng = np.random.default_rng(seed + 1)
+    for k in rng.choice(n_req, size=max(1, n_req // 20), replace=False):
+        n = int(rng.uniform(50_000, 200_000))
+        X, C, _ = cf.rand_config(n, DENSITY, seed=10_000 + int(k))
+        systems[int(k)] = (X, C, CUTOFF, (True, True, True))
+    return systems
+
+
+def bench_serving(nl, dev, rates=(1_000, 5_000, 20_000, 50_000), n_req=1_500):
+    """Poisson arrivals at each rate through the continuous-batching server
+    (40 GB pair budget) and through plain per-request launches."""
+    import torch
+
+    # clients hand over pinned position buffers (copied to the device per request)
+    systems = [(torch.from_numpy(x).pin_memory(), c, rc, p) for (x, c, rc, p) in serving_requests(n_req)]
+    out = {"workload": f"{n_req} requests per rate: the batched distribution (4,096-system config) with 5% "
+                       "large systems of 50k-200k atoms (density 0.05, rc 5 A); Poisson arrivals; 40 GB pair "
+                       "budget; pinned request buffers; latency = arrival to results on the device",
+           "rates": {}}
+    for mode in ("batched", "plain"):
+        warm = nl.NeighbourListServer(device=dev, mode=mode)  # grows the arenas once
+        warm.run_trace(nl.poisson_trace(systems[:200], 1e6, seed=0))
+        warm.close()
+        for rate in rates:
+            srv = nl.NeighbourListServer(device=dev, mode=mode)
+            st = srv.run_trace(nl.poisson_trace(systems, rate, seed=int(rate)))
+            srv.close()
+            out["rates"].setdefault(str(rate), {})[mode] = {k: st[k] for k in (
+                "p50_ms", "p99_ms", "systems_per_s", "pairs_per_s", "batches", "reruns")}
+    top = out["rates"][str(rates[-1])]
+    out["speedup_vs_plain_at_max_rate"] = top["batched"]["systems_per_s"] / top["plain"]["systems_per_s"]
+    return out
 
 
 def bench_4m(nl, dev, stream, flush, steps):

@@ -207,8 +207,8 @@ int nl_batch_neighbour_list(const nl_batch* batch, const double* d_X, void* d_pe
  * package's autotune()).  0 keeps the default (every resident block slot of
  * every SM).  Results never depend on the tuning. */
 typedef struct nl_tuning {
-  int pair_blocks_per_sm;   /* count / screening write / lazy kernels, 1..7 */
-  int emit_blocks_per_sm;   /* list write kernel, 1..16 */
+  int pair_blocks_per_sm;   /* count / screening write / lazy kernels, 1..256 */
+  int emit_blocks_per_sm;   /* list write kernel, 1..256 */
 } nl_tuning;
 
 /* Tuning of the single-system calls made by the calling thread (NULL: defaults). */

@@ -723,14 +723,21 @@ int nl_lazy_reduce(const double* d_X_sorted, const void* d_perm, const void* d_c
                              at<unsigned>(d_workspace, L.err), sms, st);
     nl::PairArgs<TI> a =
         pair_args<TI>(g, static_cast<const TI*>(d_cell_offsets), static_cast<const TI*>(d_perm), d_X_sorted, d_workspace, L);
-    a.list_cap = 0;  // lazy: nothing is written later
-    a.lists = nullptr;
-    a.lcount = nullptr;
-    a.cap_rec = nullptr;
+    a.cap_rec = nullptr;  // a later nl_fill_pairs must not take these lists for its own
     if (op == NL_REDUCE_COUNT) {
+      a.list_cap = 0;  // the counts are the result: no lists
+      a.lists = nullptr;
+      a.lcount = nullptr;
       a.counts = static_cast<int*>(d_out);
       nl::launch_pairs<TI>(nl::kModeCount, a, sms, st);
     } else {
+      // with room for the lists: count pass with lists, each atom's sum from
+      // its list, screening pass only for overflowed cells; else one
+      // screening traversal
+      if (a.list_cap > 0) {
+        a.counts = at<int>(d_workspace, L.counts);
+        nl::launch_pairs<TI>(nl::kModeCount, a, sms, st);
+      }
       a.per_atom = static_cast<double*>(d_out);
       nl::launch_pairs<TI>(nl::kModeLazyR6, a, sms, st);
     }
@@ -878,9 +885,9 @@ int nl_batch_neighbour_list(const nl_batch* batch, const double* d_X, void* d_pe
 }
 
 static int check_tuning(const nl_tuning* t) {
-  if (t && (t->pair_blocks_per_sm < 0 || t->pair_blocks_per_sm > 7 || t->emit_blocks_per_sm < 0 ||
-            t->emit_blocks_per_sm > 16))
-    return fail(NL_ERR_ARG, "tuning out of range (pair 0..7, emit 0..16 blocks per SM)");
+  if (t && (t->pair_blocks_per_sm < 0 || t->pair_blocks_per_sm > 256 || t->emit_blocks_per_sm < 0 ||
+            t->emit_blocks_per_sm > 256))
+    return fail(NL_ERR_ARG, "tuning out of range (0..256 blocks per SM)");
   return NL_OK;
 }
 

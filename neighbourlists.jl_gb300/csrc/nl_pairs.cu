@@ -369,8 +369,10 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
   // group of 32.
   // The fill pass visits only the cells that the count pass could not mask
   // (k_emit writes the others); count and lazy visit every cell.
-  const int ncell_iter = MODE == kModeFill ? min(*A.n_unmasked, A.ncells_total) : A.ncells_total;
-  auto cell_at = [&](int idx) { return MODE == kModeFill ? clampi(A.unmasked[idx], A.ncells_total - 1) : idx; };
+  // (so does the lazy pass when the per-atom lists cover the other cells)
+  const bool listed = MODE == kModeFill || (MODE == kModeLazyR6 && A.list_cap > 0);
+  const int ncell_iter = listed ? min(*A.n_unmasked, A.ncells_total) : A.ncells_total;
+  auto cell_at = [&](int idx) { return listed ? clampi(A.unmasked[idx], A.ncells_total - 1) : idx; };
   int idx = blockIdx.x * kPairWarps + warp;
   // (0-based slot offsets, clamped to [0, nat])
   int pf_hs = 0, pf_he = 0, pf_lo = 0, pf_hi = 0;
@@ -706,9 +708,11 @@ __global__ void __launch_bounds__(kEmitWarps * 32, kEmitMinBlocks) k_emit(PairAr
       const long long out = out0 + lane;
       const bool wr = act && out < A.capacity;
       if (act && !wr) atomicOr(A.err, kFlagCapacity);
+      // outputs are written once and never re-read here: streaming stores keep
+      // the gathered positions and the lists in L2
       if (wr) {
-        A.oi[out] = TI(E.ti[pa]);
-        A.oj[out] = TI(poj);
+        __stcs(A.oi + out, TI(E.ti[pa]));
+        __stcs(A.oj + out, TI(poj));
       }
       E.sbuf[3 * lane + 0] = S[0];
       E.sbuf[3 * lane + 1] = S[1];
@@ -727,8 +731,8 @@ __global__ void __launch_bounds__(kEmitWarps * 32, kEmitMinBlocks) k_emit(PairAr
         const int t = lane + 32 * k;
         const long long wpos = 3 * out0 + t;
         if (t < 3 * nact && wpos < wend) {
-          A.oS[wpos] = TI(E.sbuf[t]);
-          if (A.oR) A.oR[wpos] = E.rbuf[t];
+          __stcs(A.oS + wpos, TI(E.sbuf[t]));
+          if (A.oR) __stcs(A.oR + wpos, E.rbuf[t]);
         }
       }
       __syncwarp();
@@ -738,12 +742,12 @@ __global__ void __launch_bounds__(kEmitWarps * 32, kEmitMinBlocks) k_emit(PairAr
       const uint2* lst = A.lists + (c0 + a) * K;
       for (int p = 0; p < n; p += 32) {
         const int r = p + lane;
-        const uint2 e = lst[min(r, n - 1)];
+        const uint2 e = __ldcs(lst + min(r, n - 1));  // read once
         const int slot_j = clampi(int(e.x), A.nat_total - 1);
-        const double xj0 = A.Xs[3LL * slot_j + 0];
-        const double xj1 = A.Xs[3LL * slot_j + 1];
-        const double xj2 = A.Xs[3LL * slot_j + 2];
-        const long long oj = (long long)A.perm[slot_j];
+        const double xj0 = __ldg(A.Xs + 3LL * slot_j + 0);
+        const double xj1 = __ldg(A.Xs + 3LL * slot_j + 1);
+        const double xj2 = __ldg(A.Xs + 3LL * slot_j + 2);
+        const long long oj = (long long)__ldg(A.perm + slot_j);
         if (pv) finish();
         pv = true;
         pa = a;
@@ -760,12 +764,81 @@ __global__ void __launch_bounds__(kEmitWarps * 32, kEmitMinBlocks) k_emit(PairAr
   }
 }
 
+// ------------------------------------------------------------------------
+// Lazy reduction from the count pass's lists: one thread per sorted atom
+// walks its list in the reference's traversal order and accumulates
+// 1 / ((r2*r2)*r2) exactly as the traversal does (for_each_neighbour with a
+// sequential per-atom sum), 32 atoms per warp in parallel.  Atoms of cells
+// whose lists overflowed are summed by the screening lazy pass.
+__device__ __forceinline__ void pair_R_lane(const Geometry& g, const double* cs_tab, const double* xi,
+                                            const double* xj, int S0, int S1, int S2, double* R) {
+  R[0] = dsub(xj[0], xi[0]);
+  R[1] = dsub(xj[1], xi[1]);
+  R[2] = dsub(xj[2], xi[2]);
+  if ((S0 | S1 | S2) != 0) {
+    double c0, c1, c2;
+    if (abs(S0) <= kCsR && abs(S1) <= kCsR && abs(S2) <= kCsR) {
+      const double* t = cs_tab + 3 * ((S0 + kCsR) + kCsN * ((S1 + kCsR) + kCsN * (S2 + kCsR)));
+      c0 = t[0];
+      c1 = t[1];
+      c2 = t[2];
+    } else {
+      c0 = cts_k(g.C, S0, S1, S2, 0);
+      c1 = cts_k(g.C, S0, S1, S2, 1);
+      c2 = cts_k(g.C, S0, S1, S2, 2);
+    }
+    R[0] = dadd(R[0], c0);
+    R[1] = dadd(R[1], c1);
+    R[2] = dadd(R[2], c2);
+  } else {
+    const double* z = cs_tab + 3 * ((kCsN * kCsN + kCsN + 1) * kCsR);  // C'(0,0,0): signed zeros
+    R[0] = add_signed_zero(R[0], z[0]);
+    R[1] = add_signed_zero(R[1], z[1]);
+    R[2] = add_signed_zero(R[2], z[2]);
+  }
+}
+
+template <typename TI, bool BATCH>
+__global__ void __launch_bounds__(128) k_lazy_lists(PairArgs<TI> A) {
+  __shared__ double cs_blk[BATCH ? 1 : 3 * kCsN * kCsN * kCsN];
+  if (!BATCH) {
+    for (int t = threadIdx.x; t < 3 * kCsN * kCsN * kCsN; t += blockDim.x) cs_blk[t] = A.cs_table[t];
+    __syncthreads();
+  }
+  const int K = A.list_cap;
+  for (long long slot = (long long)blockIdx.x * blockDim.x + threadIdx.x; slot < A.nat_total;
+       slot += (long long)gridDim.x * blockDim.x) {
+    const int n = A.lcount[slot];
+    if (n > K) continue;  // the screening lazy pass sums this atom
+    const int sys = BATCH ? batch_system(A.sys_atom, A.nsys, int(slot)) : 0;
+    const Geometry& g = BATCH ? A.geo[sys] : A.g;
+    const double* cs_tab = BATCH ? A.cs_sys + 3 * kCsN * kCsN * kCsN * (long long)sys : cs_blk;
+    const double xi[3] = {A.Xs[3 * slot + 0], A.Xs[3 * slot + 1], A.Xs[3 * slot + 2]};
+    const unsigned mi = __float_as_uint(A.rec[slot].w);
+    const uint2* lst = A.lists + slot * K;
+    double acc = 0.0;
+    for (int r = 0; r < n; ++r) {
+      const uint2 e = lst[r];
+      const int sj = clampi(int(e.x), A.nat_total - 1);
+      const double xj[3] = {A.Xs[3LL * sj + 0], A.Xs[3LL * sj + 1], A.Xs[3LL * sj + 2]};
+      int S[3];
+      pair_S(g, xi, xj, mi, e.y, S);
+      double R[3];
+      pair_R_lane(g, cs_tab, xi, xj, S[0], S[1], S[2], R);
+      const double r2 = dot_ref(R);
+      acc = dadd(acc, __ddiv_rn(1.0, dmul(dmul(r2, r2), r2)));
+    }
+    A.per_atom[clampi(A.sorig[slot], A.nat_total - 1)] = acc;
+  }
+}
+
 template <typename TI, bool BATCH>
 static void launch_modes(int mode, const PairArgs<TI>& a, int num_sms, cudaStream_t st) {
   if (a.nat_total <= 0 || a.ncells_total <= 0) return;
-  // grids: at most the resident blocks per SM (or the tuned number) on every SM
-  const int pbps = a.pair_blocks_per_sm > 0 ? min(a.pair_blocks_per_sm, kMinBlocks) : kMinBlocks;
-  const int ebps = a.emit_blocks_per_sm > 0 ? min(a.emit_blocks_per_sm, 16) : kEmitMinBlocks;
+  // grids: the tuned number of blocks per SM (default: the resident ones);
+  // every kernel walks its cells / atoms in a grid-stride loop
+  const int pbps = a.pair_blocks_per_sm > 0 ? a.pair_blocks_per_sm : kMinBlocks;
+  const int ebps = a.emit_blocks_per_sm > 0 ? a.emit_blocks_per_sm : kEmitMinBlocks;
   long long blocks = ((long long)a.ncells_total + kPairWarps - 1) / kPairWarps;
   if (blocks > (long long)num_sms * pbps) blocks = (long long)num_sms * pbps;
   if (blocks < 1) blocks = 1;
@@ -783,6 +856,11 @@ static void launch_modes(int mode, const PairArgs<TI>& a, int num_sms, cudaStrea
     }
     default:
       if (!BATCH) k_cs_table<<<1, 128, 0, st>>>(a.g, a.cs_table, nullptr, 0, a.err);
+      if (a.list_cap > 0) {
+        long long lb = ((long long)a.nat_total + 127) / 128;
+        if (lb > (long long)num_sms * 16) lb = (long long)num_sms * 16;
+        k_lazy_lists<TI, BATCH><<<int(lb), 128, 0, st>>>(a);
+      }
       k_pairs<TI, kModeLazyR6, BATCH><<<int(blocks), kPairWarps * 32, 0, st>>>(a);
       break;
   }

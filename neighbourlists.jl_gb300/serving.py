@@ -40,7 +40,7 @@ _U8 = C.POINTER(C.c_uint8)
 @dataclass
 class Request:
     rid: int
-    X: np.ndarray              # (n, 3) float64 positions (host)
+    X: object                  # (n, 3) float64 positions: numpy array, or a pinned torch tensor (copied directly)
     cell: np.ndarray           # 3x3, rows are lattice vectors
     cutoff: float
     pbc: tuple
@@ -55,10 +55,14 @@ class Request:
 
     def predicted_pairs(self) -> int:
         """Expected pairs of a homogeneous system plus headroom."""
-        vol = abs(float(np.linalg.det(np.asarray(self.cell, dtype=np.float64))))
-        n = self.nat
-        exp = n * (n / vol) * 4.0 / 3.0 * math.pi * self.cutoff ** 3 if vol > 0 else 0.0
-        return int(1.3 * exp + 8 * math.sqrt(exp + 1.0)) + 64
+        p = self.__dict__.get("_pred")
+        if p is None:
+            vol = abs(float(np.linalg.det(np.asarray(self.cell, dtype=np.float64))))
+            n = self.nat
+            exp = n * (n / vol) * 4.0 / 3.0 * math.pi * self.cutoff ** 3 if vol > 0 else 0.0
+            p = int(1.3 * exp + 8 * math.sqrt(exp + 1.0)) + 64
+            self.__dict__["_pred"] = p
+        return p
 
 
 class _Slot:
@@ -154,15 +158,22 @@ class NeighbourListServer:
         self.inflight_bytes += pred_bytes
         self.batches += 1
         nat = sum(r.nat for r in reqs)
-        hX = s.host_X(nat)
-        hXn = hX.numpy()
-        o = 0
-        for r in reqs:
-            hXn[o:o + r.nat] = r.X
-            o += r.nat
         Xd = s.buf("X", 3 * max(nat, 1), torch.float64)
         with torch.cuda.stream(s.stream):
-            if nat:
+            if all(isinstance(r.X, torch.Tensor) and r.X.is_pinned() for r in reqs):
+                # pinned request buffers: one asynchronous copy each, no host staging
+                o = 0
+                for r in reqs:
+                    if r.nat:
+                        Xd[3 * o:3 * (o + r.nat)].view(r.nat, 3).copy_(r.X, non_blocking=True)
+                    o += r.nat
+            elif nat:
+                hX = s.host_X(nat)
+                hXn = hX.numpy()
+                o = 0
+                for r in reqs:
+                    hXn[o:o + r.nat] = r.X.numpy() if isinstance(r.X, torch.Tensor) else r.X
+                    o += r.nat
                 Xd[:3 * nat].view(nat, 3).copy_(hX[:nat], non_blocking=True)
             cap = max(sum(r.predicted_pairs() for r in reqs), 1)
             if self.mode == "batched":

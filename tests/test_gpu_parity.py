@@ -281,3 +281,25 @@ def test_minimal_workspace_screening_write(nlpkg, orc, case):
     eng.run(torch.from_numpy(X).cuda())
     o = orc.neighbour_list(X, rc, C, pbc, nthreads=8)
     assert_identical(eng.pairlist(None), o)
+
+
+@pytest.mark.parametrize("case", ["dense", "fcc", "min_workspace"])
+def test_lazy_inv_r6_paths(nlpkg, orc, case):
+    """Lazy sum 1/r^6: from the per-atom lists, through the screening pass for
+    overflowed cells (dense: > 64 pairs per atom), and with no lists at all
+    (minimal workspace) -- bit-identical to the oracle in every case."""
+    if case == "dense":
+        X = np.random.default_rng(6).random((400, 3)) * 6.0
+        C, pbc, rc = np.diag([6.0] * 3), (True, True, True), 2.2
+    else:
+        X, C, pbc = cf.fcc_sheared(n=5, seed=4)
+        rc = 5.0
+    clist = nlpkg.build_cell_list(torch.from_numpy(X).cuda(), rc, C, pbc)
+    if case == "min_workspace":
+        lib = nlpkg._lib.lib()
+        clist._ws = torch.empty(int(lib.nl_workspace_min_bytes(X.shape[0], clist.ncells_total)),
+                                dtype=torch.uint8, device="cuda")
+        clist._records = False
+    s = to_np(nlpkg.lazy_reduce(clist, "inv_r6"))
+    ref = orc.lazy_sum_r6(orc.build_cell_list(X, rc, C, pbc))
+    assert np.array_equal(s.view(np.int64), ref.view(np.int64))

@@ -45,7 +45,8 @@ def test_same_alone_and_in_mix(nlpkg, orc):
 
 def test_plain_mode_matches_batched(nlpkg):
     systems = mixed_systems()[:12]
-    a, _, _ = serve(nlpkg, systems, slots=2)
+    pinned = [(torch.from_numpy(x).pin_memory(), c, rc, p) for (x, c, rc, p) in systems]
+    a, _, _ = serve(nlpkg, pinned, slots=2)  # pinned request buffers, copied per request
     b, _, srv = serve(nlpkg, systems, slots=2, mode="plain")
     assert srv.batches == len(systems)
     for x, y in zip(a, b):
