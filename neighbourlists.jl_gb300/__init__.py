@@ -23,6 +23,8 @@ from .api import (  # noqa: F401
     npairs,
     nsites,
     num_neighbours,
+    pairs,
+    sites,
 )
 from .batch import BatchNeighbourList  # noqa: F401
 from .engine import NeighbourListEngine  # noqa: F401

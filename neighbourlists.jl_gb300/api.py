@@ -35,7 +35,8 @@ from ._lib import NLError, check, lib
 __all__ = [
     "SortedCellList", "PairList", "NLError", "analyze_cell", "build_cell_list", "materialize_pairlist",
     "neighbour_list", "npairs", "nsites", "nneigs", "maxneigs", "max_neighbours", "neigs", "neigss", "neighbours",
-    "num_neighbours", "count_neighbours", "for_each_neighbour", "lazy_reduce", "cutoff",
+    "num_neighbours", "count_neighbours", "for_each_neighbour", "lazy_reduce", "cutoff", "pairs", "sites",
+    "PairIterator", "SiteIterator",
 ]
 
 _D = C.POINTER(C.c_double)
@@ -371,3 +372,50 @@ def for_each_neighbour(f: Callable, clist: SortedCellList, i: int) -> None:
     js, Rs, Ss = js.cpu().numpy(), Rs.cpu().numpy(), Ss.cpu().numpy()
     for k in range(js.shape[0]):
         f(int(js[k]), Rs[k], Ss[k])
+
+
+# --------------------------------------------------------------- iterators --
+class PairIterator:
+    """pairs(nlist) (iterators.jl:12-26): yields (i, j, R) for every pair in
+    list order (1-based i, j; R a float64[3]).  The device buffers are read in
+    host blocks of ``block`` pairs."""
+
+    def __init__(self, nlist: PairList, block: int = 1 << 16):
+        self.nlist, self.block = nlist, int(block)
+
+    def __len__(self) -> int:
+        return npairs(self.nlist)
+
+    def __iter__(self):
+        nl = self.nlist
+        for a in range(0, npairs(nl), self.block):
+            b = min(a + self.block, npairs(nl))
+            i = nl.i[a:b].cpu().numpy()
+            j = nl.j[a:b].cpu().numpy()
+            R = (nl.R[a:b] if nl.R is not None else _getR(nl, a, b)).cpu().numpy()
+            for k in range(b - a):
+                yield int(i[k]), int(j[k]), R[k]
+
+
+class SiteIterator:
+    """sites(nlist) (iterators.jl:28-40): yields (i, j, R) per site, with j and
+    R the device views of site i's neighbours (neigs)."""
+
+    def __init__(self, nlist: PairList):
+        self.nlist = nlist
+
+    def __len__(self) -> int:
+        return nsites(self.nlist)
+
+    def __iter__(self):
+        for i in range(1, nsites(self.nlist) + 1):
+            j, R = neigs(self.nlist, i)
+            yield i, j, R
+
+
+def pairs(nlist: PairList) -> PairIterator:
+    return PairIterator(nlist)
+
+
+def sites(nlist: PairList) -> SiteIterator:
+    return SiteIterator(nlist)

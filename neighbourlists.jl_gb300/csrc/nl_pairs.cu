@@ -60,6 +60,8 @@ struct __align__(16) WarpSmem {
   double rval[32];          // queue: lazy values
   int horig[32];            // home batch: original index (0-based)
   unsigned hmeta[32];       // home batch: packed windings | exact bit
+  float box[6];             // home batch: bounding box (x lo/hi, y lo/hi, z lo/hi) of the FP32 records
+  int prune;                // home batch: the box may prune candidates (no exact home atom)
 };
 
 __device__ __forceinline__ unsigned lt_mask() {
@@ -151,6 +153,20 @@ __device__ __forceinline__ void pair_S(const Geometry& g, const double* xi, cons
       S[k] = sl + bi.w[k] - bj.w[k];
     }
   }
+}
+
+// The candidate is the home atom itself with zero loop shift (the reference
+// skips i == j && s_loop == 0, gpu_kernels.jl:82); the same atom seen through
+// a periodic image is a neighbour.  s_loop comes back from the candidate word:
+// its fields hold s_loop - w_j + 512 (w_j = w_i here) or, for an exact atom,
+// s_loop + 512.
+__device__ __forceinline__ bool is_self(int cand_slot, int home_slot, unsigned cw, unsigned mi) {
+  if (cand_slot != home_slot) return false;
+  const bool ex = (cw & kMetaExact) != 0;
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+    if (field10(cw, k) - 512 + (ex ? 0 : field10(mi, k) - 128) != 0) return false;
+  return true;
 }
 
 // Full FP64 decision of one candidate pair with the reference arithmetic.
@@ -420,6 +436,7 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
     for (int hb = hs; hb < he; hb += 32) {
       const int nb = min(32, he - hb);
       float ux = 0.f, uy = 0.f, uz = 0.f;
+
       int head = 0, tail = 0;  // ring queue (fill / lazy)
 
       for (int gb = 0; gb < nst; gb += 32) {
@@ -444,9 +461,6 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
           if (lane >= o) incl += v;
         }
         const int tg = __shfl_sync(0xffffffffu, incl, 31);
-        const int cl = center - gb;  // home cell (center of the stencil) in this group?
-        const int center_excl = (cl >= 0 && cl < 32) ? __shfl_sync(0xffffffffu, incl - ccount, cl & 31) : -1;
-
         for (int cb = 0; cb < tg || (gb == 0 && cb == 0); cb += kChunk) {
           const int nch = min(kChunk, tg - cb);
           if (MODE != kModeCount && tail > head) {  // queued pairs refer to the previous chunk
@@ -473,13 +487,47 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
               W.hnext[lane] = MODE == kModeFill ? (long long)A.first[sv.abase + orig] - 1 : 0;
               if (MODE == kModeLazyR6) W.hacc[lane] = 0.0;
             }
+            // bounding box of the home batch: candidates farther than the
+            // screen's reject bound from it are not staged
+            {
+              const float inf = __int_as_float(0x7f800000);
+              const bool in = lane < nb;
+              float bl[3] = {in ? ux : inf, in ? uy : inf, in ? uz : inf};
+              float bh[3] = {in ? ux : -inf, in ? uy : -inf, in ? uz : -inf};
+#pragma unroll
+              for (int d = 0; d < 3; ++d)
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                  bl[d] = fminf(bl[d], __shfl_xor_sync(0xffffffffu, bl[d], o));
+                  bh[d] = fmaxf(bh[d], __shfl_xor_sync(0xffffffffu, bh[d], o));
+                }
+              // an exact home atom (NaN record) is tested against every candidate
+              const bool pr = !__any_sync(0xffffffffu, in && (W.hmeta[lane] & kExactBit) != 0);
+              if (lane == 0) {
+                W.box[0] = bl[0];
+                W.box[1] = bh[0];
+                W.box[2] = bl[1];
+                W.box[3] = bh[1];
+                W.box[4] = bl[2];
+                W.box[5] = bh[2];
+                W.prune = pr;
+              }
+            }
           }
           if (nch <= 0) {
             __syncwarp();
             continue;
           }
           // ---- stage the chunk: home-relative FP32 positions, packed S base;
-          // exact candidates stay NaN, padding up to whole rounds is +inf
+          // exact candidates stay NaN, padding up to whole rounds is +inf.
+          // Candidates whose distance from the home batch's bounding box is
+          // above the reject bound are dropped; the kept ones stay in
+          // traversal order.  (The box distance is computed with the screen's
+          // own operations on smaller magnitudes, so by monotonicity of
+          // rounding it never exceeds any home atom's screened r2.)
+          int nkeep = 0;
+          __syncwarp();
+          const bool prune = W.prune != 0;
           for (int f0 = 0; f0 < nch; f0 += 32) {
             const int f = f0 + lane;
             const int gf = cb + min(f, nch - 1);
@@ -496,20 +544,36 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
             const float qx = __shfl_sync(0xffffffffu, ox, qq);
             const float qy = __shfl_sync(0xffffffffu, oy, qq);
             const float qz = __shfl_sync(0xffffffffu, oz, qq);
+            bool keep = false;
+            float4 cv;
+            int slot = 0;
             if (f < nch) {
-              const int slot = q_start + (gf - (q_incl - q_cnt));
+              slot = q_start + (gf - (q_incl - q_cnt));
               const float4 r = A.rec[slot];
               const unsigned mj = __float_as_uint(r.w);
-              unsigned cw;
-              cw = cand_word(q_slp, mj);
+              const unsigned cw = cand_word(q_slp, mj);
               const float nan = __int_as_float(0x7fc00000);
               const bool ex = (cw & kExactBit) != 0;
-              W.cv[f] = make_float4(ex ? nan : r.x + qx, ex ? nan : r.y + qy, ex ? nan : r.z + qz,
-                                    __uint_as_float(cw));
-              W.cslot[f] = slot;
-            } else {
+              cv = make_float4(ex ? nan : r.x + qx, ex ? nan : r.y + qy, ex ? nan : r.z + qz, __uint_as_float(cw));
+              const float dx = fmaxf(fmaxf(W.box[0] - cv.x, cv.x - W.box[1]), 0.f);
+              const float dy = fmaxf(fmaxf(W.box[2] - cv.y, cv.y - W.box[3]), 0.f);
+              const float dz = fmaxf(fmaxf(W.box[4] - cv.z, cv.z - W.box[5]), 0.f);
+              const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+              keep = ex || !(prune && d2 > hi);
+            }
+            const unsigned km = __ballot_sync(0xffffffffu, keep);
+            if (keep) {
+              const int pos = nkeep + __popc(km & lt_mask());
+              W.cv[pos] = cv;
+              W.cslot[pos] = slot;
+            }
+            nkeep += __popc(km);
+          }
+          {
+            const int pos = nkeep + lane;  // padding up to a whole round
+            if (pos < ((nkeep + 31) & ~31)) {
               const float inf = __int_as_float(0x7f800000);
-              W.cv[f] = make_float4(inf, inf, inf, 0.f);
+              W.cv[pos] = make_float4(inf, inf, inf, 0.f);
             }
           }
           __syncwarp();
@@ -518,7 +582,7 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
           // A test is pure FP32: accept 0 < r2 < lo, reject r2 > hi; the rest
           // (the band, r2 == 0 which includes the self candidate, and NaN from
           // exact atoms) is resolved in the warp-uniform rare branch.
-          const int nround = (nch + 31) & ~31;
+          const int nround = (nkeep + 31) & ~31;
           for (int a0 = 0; a0 < nb; a0 += kGroup) {
             float ax[kGroup], ay[kGroup], az[kGroup];
             long long next[kGroup];
@@ -550,9 +614,7 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
                 for (int k = 0; k < kGroup; ++k)
                   if (unc[k]) {
                     const int a = a0 + k;
-                    // the self candidate (j == i, zero loop shift) sits in the home cell
-                    const int self_f = center_excl >= 0 ? center_excl + (hb + a - hs) - cb : -1;
-                    if (f >= nch || a >= nb || f == self_f) {
+                    if (f >= nkeep || a >= nb || is_self(W.cslot[f], hb + a, __float_as_uint(c.w), W.hmeta[a])) {
                       acc[k] = false;
                     } else {
                       ++rechecks;

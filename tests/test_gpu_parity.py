@@ -303,3 +303,20 @@ def test_lazy_inv_r6_paths(nlpkg, orc, case):
     s = to_np(nlpkg.lazy_reduce(clist, "inv_r6"))
     ref = orc.lazy_sum_r6(orc.build_cell_list(X, rc, C, pbc))
     assert np.array_equal(s.view(np.int64), ref.view(np.int64))
+
+
+def test_pair_and_site_iterators(nlpkg, orc):
+    """pairs / sites (iterators.jl:12-40) over the device buffers."""
+    X, C, L = cf.rand_config(300, seed=41)
+    nl = nlpkg.neighbour_list(torch.from_numpy(X).cuda(), 0.3 * L, C, (True, True, True))
+    o = orc.neighbour_list(X, 0.3 * L, C, (True, True, True))
+    items = list(nlpkg.pairs(nl))
+    assert len(items) == o.npairs == len(nlpkg.pairs(nl))
+    assert [t[0] for t in items] == o.i.tolist() and [t[1] for t in items] == o.j.tolist()
+    assert np.array_equal(np.stack([t[2] for t in items]).view(np.int64), o.R.view(np.int64))
+    sites = list(nlpkg.sites(nl))
+    assert len(sites) == 300
+    for i, j, R in sites[::37]:
+        a, b = o.first[i - 1] - 1, o.first[i] - 1
+        assert np.array_equal(to_np(j).astype(np.int64), o.j[a:b])
+        assert np.array_equal(to_np(R).view(np.int64), o.R[a:b].view(np.int64))
