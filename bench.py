@@ -377,7 +377,7 @@ def bench_batched(nl, dev, stream, flush, steps):
             "pairs_per_s": total / (batch_ms * 1e-3),
             "plain_systems_per_s": nsys / (plain_ms * 1e-3), "plain_ms": plain_ms,
             "speedup_vs_plain": plain_ms / batch_ms, "identical_to_plain": bool(same),
-            "cuda_graph": True, "autotune": {k: tune[k] for k in ("pair_blocks_per_sm", "emit_blocks_per_sm", "ms")},
+            "cuda_graph": True, "autotune": {k: tune[k] for k in ("pair_blocks_per_sm", "emit_blocks_per_sm", "count_kernel", "ms")},
             "l2": "flushed before every timed step"}
 
 

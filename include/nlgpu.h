@@ -209,6 +209,7 @@ int nl_batch_neighbour_list(const nl_batch* batch, const double* d_X, void* d_pe
 typedef struct nl_tuning {
   int pair_blocks_per_sm;   /* count / screening write / lazy kernels, 1..256 */
   int emit_blocks_per_sm;   /* list write kernel, 1..256 */
+  int count_kernel;         /* 0 default (= 1), 1 one warp per home cell, 2 one thread per home atom */
 } nl_tuning;
 
 /* Tuning of the single-system calls made by the calling thread (NULL: defaults). */

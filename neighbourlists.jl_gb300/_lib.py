@@ -79,7 +79,7 @@ class System(C.Structure):
 
 class Tuning(C.Structure):
     """nl_tuning: grid sizes of the pair kernels (0 = default)."""
-    _fields_ = [("pair_blocks_per_sm", C.c_int), ("emit_blocks_per_sm", C.c_int)]
+    _fields_ = [("pair_blocks_per_sm", C.c_int), ("emit_blocks_per_sm", C.c_int), ("count_kernel", C.c_int)]
 
 
 class NLError(RuntimeError):

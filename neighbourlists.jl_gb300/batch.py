@@ -132,8 +132,8 @@ class BatchNeighbourList:
         self.last_total = int(total.value)
         return self.last_total
 
-    def set_tuning(self, pair_blocks_per_sm: int = 0, emit_blocks_per_sm: int = 0) -> None:
-        t = _lib.Tuning(int(pair_blocks_per_sm), int(emit_blocks_per_sm))
+    def set_tuning(self, pair_blocks_per_sm: int = 0, emit_blocks_per_sm: int = 0, count_kernel: int = 0) -> None:
+        t = _lib.Tuning(int(pair_blocks_per_sm), int(emit_blocks_per_sm), int(count_kernel))
         check(lib().nl_batch_set_tuning(self._h, C.byref(t)))
 
     def capture(self, X: torch.Tensor) -> torch.cuda.CUDAGraph:

@@ -25,7 +25,8 @@
 namespace {
 
 thread_local std::string g_last_error;
-thread_local nl_tuning g_tuning = {0, 0};  // single-system calls of this thread
+thread_local nl_tuning g_tuning = {0, 0, 0};  // single-system calls of this thread
+
 
 int fail(int status, const std::string& msg) {
   g_last_error = msg;
@@ -166,9 +167,9 @@ constexpr size_t kAlign = 256;
 size_t up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
 
 struct Layout {
-  // [err 64 | stats 64] [pairs zero region: counters 64 | st_pairs]
+  // [err 64 | stats 64] [pairs zero region: counters 64 | st_pairs | cell_flag]
   // [build zero region: counters 64 | st_cells | cell_count] [arrays...]
-  size_t err, stats, pcount, st_pairs, pend, bcount, st_cells, cell_count, bend;
+  size_t err, stats, pcount, st_pairs, cell_flag, pend, bcount, st_cells, cell_count, bend;
   size_t totals, cell_start, cid, ticket, rec, tmp, rec_sorted, scell, counts, lcount, sorig, cs_table, unmasked,
       big_list, base_end, lists, end;
   bool use_lists = true;  // the workspace holds the pair lists (it reaches `end`)
@@ -184,6 +185,8 @@ Layout layout(int64_t nat, int64_t ncells) {
   o += 64;
   L.st_pairs = o;
   o += up(sizeof(unsigned long long) * size_t(nl::scan_tiles(nat > 0 ? nat : 1)));
+  L.cell_flag = o;
+  o += up(sizeof(int) * size_t(ncells > 0 ? ncells : 1));
   L.pend = o;
   L.bcount = o;
   o += 64;
@@ -394,6 +397,8 @@ nl::PairArgs<TI> pair_args(const nl::Geometry& g, const TI* cell_offsets, const 
   a.cs_table = at<double>(ws, L.cs_table);
   a.unmasked = at<int>(ws, L.unmasked);
   a.n_unmasked = at<int>(ws, L.pcount) + 4;  // zeroed with the pair scan state
+  a.cell_flag = at<int>(ws, L.cell_flag);     // likewise
+  a.count_kernel = g_tuning.count_kernel;
   a.pair_blocks_per_sm = g_tuning.pair_blocks_per_sm;
   a.emit_blocks_per_sm = g_tuning.emit_blocks_per_sm;
   a.stats = at<unsigned long long>(ws, L.stats);
@@ -477,7 +482,7 @@ struct nl_batch {
   std::vector<nl::Geometry> geo;
   std::vector<int> atom0, cell0;
   BatchLayout B;
-  nl_tuning tuning = {0, 0};
+  nl_tuning tuning = {0, 0, 0};
 };
 
 namespace {
@@ -522,6 +527,7 @@ int batch_impl(const nl_batch& b, const double* X, TI* perm, double* Xs, TI* cel
   a.counts = at<int>(ws, L.counts);
   a.pair_blocks_per_sm = b.tuning.pair_blocks_per_sm;
   a.emit_blocks_per_sm = b.tuning.emit_blocks_per_sm;
+  a.count_kernel = b.tuning.count_kernel;
   if (na > 0) {
     nl::launch_pairs<TI>(nl::kModeCount, a, sms, st);
     nl::launch_scan<TI>(at<int>(ws, L.counts), na, first_all, nullptr, at<unsigned long long>(ws, L.st_pairs),
@@ -712,7 +718,7 @@ int nl_lazy_reduce(const double* d_X_sorted, const void* d_perm, const void* d_c
   cudaError_t e = cudaSuccess;
   if (!reuse_records) e = cudaMemsetAsync(d_workspace, 0, 128, st);
   // the count kernel appends its unmasked cells to a list counted in pcount
-  if (e == cudaSuccess) e = cudaMemsetAsync(static_cast<char*>(d_workspace) + L.pcount, 0, 64, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(static_cast<char*>(d_workspace) + L.pcount, 0, L.pend - L.pcount, st);
   if (e != cudaSuccess) return cuda_fail(e, "memset workspace");
   const int sms = num_sms();
   auto run = [&](auto tag) {
@@ -886,21 +892,21 @@ int nl_batch_neighbour_list(const nl_batch* batch, const double* d_X, void* d_pe
 
 static int check_tuning(const nl_tuning* t) {
   if (t && (t->pair_blocks_per_sm < 0 || t->pair_blocks_per_sm > 256 || t->emit_blocks_per_sm < 0 ||
-            t->emit_blocks_per_sm > 256))
-    return fail(NL_ERR_ARG, "tuning out of range (0..256 blocks per SM)");
+            t->emit_blocks_per_sm > 256 || t->count_kernel < 0 || t->count_kernel > 2))
+    return fail(NL_ERR_ARG, "tuning out of range (0..256 blocks per SM, count kernel 0..2)");
   return NL_OK;
 }
 
 int nl_set_tuning(const nl_tuning* tuning) {
   if (int s = check_tuning(tuning)) return s;
-  g_tuning = tuning ? *tuning : nl_tuning{0, 0};
+  g_tuning = tuning ? *tuning : nl_tuning{0, 0, 0};
   return NL_OK;
 }
 
 int nl_batch_set_tuning(nl_batch* batch, const nl_tuning* tuning) {
   if (!batch) return fail(NL_ERR_ARG, "null batch");
   if (int s = check_tuning(tuning)) return s;
-  batch->tuning = tuning ? *tuning : nl_tuning{0, 0};
+  batch->tuning = tuning ? *tuning : nl_tuning{0, 0, 0};
   return NL_OK;
 }
 

@@ -706,11 +706,15 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
 #ifndef NL_EMIT_MIN_BLOCKS
 #define NL_EMIT_MIN_BLOCKS 8
 #endif
+#ifndef NL_EMIT_STAGES
+#define NL_EMIT_STAGES 3
+#endif
 constexpr int kEmitWarps = 4;
 constexpr int kEmitMinBlocks = NL_EMIT_MIN_BLOCKS;  // resident blocks per SM the register budget targets
 
 struct __align__(16) EmitAtoms {
   long long sbuf[96];   // a pass's S, three words per pair, staged for contiguous stores
+  unsigned short pass[64];  // the chunk's passes: atom << 8 | pass within the atom
   double rbuf[96];      // a pass's R, likewise
   double xi[32][3];     // FP64 position
   long long base[32];   // first output slot (0-based)
@@ -799,6 +803,57 @@ __global__ void __launch_bounds__(kEmitWarps * 32, kEmitMinBlocks) k_emit(PairAr
       }
       __syncwarp();
     };
+#if NL_EMIT_STAGES == 3
+    // three stages over the chunk's passes: list entries two passes ahead,
+    // gathers one pass ahead, S / R / stores for the current pass
+    {
+      const int c = lane < na ? (E.n[lane] + 31) >> 5 : 0;  // passes of atom `lane`
+      int ci = c;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, ci, o);
+        if (lane >= o) ci += v;
+      }
+      const int npass = __shfl_sync(0xffffffffu, ci, 31);
+      for (int k = 0; k < c; ++k) E.pass[ci - c + k] = (unsigned short)((lane << 8) | k);
+      __syncwarp();
+      uint2 eB = make_uint2(0u, 0u);
+      int aB = 0, rB = 0;
+      for (int t = 0; t < npass + 2; ++t) {
+        uint2 eA = make_uint2(0u, 0u);
+        int aA = 0, rA = 0;
+        if (t < npass) {  // stage 1: list entries
+          const unsigned pd = E.pass[t];
+          aA = int(pd >> 8);
+          rA = 32 * int(pd & 255u) + lane;
+          const int n = E.n[aA];
+          eA = __ldcs(A.lists + (c0 + aA) * K + min(rA, n - 1));  // read once
+        }
+        double xj0 = 0.0, xj1 = 0.0, xj2 = 0.0;
+        long long oj = 0;
+        if (t >= 1 && t - 1 < npass) {  // stage 2: gathers
+          const int slot_j = clampi(int(eB.x), A.nat_total - 1);
+          xj0 = __ldg(A.Xs + 3LL * slot_j + 0);
+          xj1 = __ldg(A.Xs + 3LL * slot_j + 1);
+          xj2 = __ldg(A.Xs + 3LL * slot_j + 2);
+          oj = (long long)__ldg(A.perm + slot_j);
+        }
+        if (pv) finish();  // stage 3
+        pv = t >= 1 && t - 1 < npass;
+        pa = aB;
+        pr = rB;
+        pn = E.n[aB];
+        pcw = eB.y;
+        poj = oj;
+        pxj0 = xj0;
+        pxj1 = xj1;
+        pxj2 = xj2;
+        eB = eA;
+        aB = aA;
+        rB = rA;
+      }
+    }
+#else
     for (int a = 0; a < na; ++a) {
       const int n = E.n[a];
       const uint2* lst = A.lists + (c0 + a) * K;
@@ -823,7 +878,121 @@ __global__ void __launch_bounds__(kEmitWarps * 32, kEmitMinBlocks) k_emit(PairAr
       }
     }
     if (pv) finish();
+#endif
   }
+}
+
+// ------------------------------------------------------------------------
+// Count pass with one thread per home atom.  Each thread walks its own
+// stencil in the reference's order (dz, dy, dx; then the cell's atoms in
+// sorted order), screens every candidate with the same FP32 arithmetic as
+// the cell kernel (candidate v = u_j + d.b relative to the home cell's
+// corner, r2 of v - u_i; FP64 decision inside the band, for exact atoms and
+// for r2 == 0), counts, and appends accepted candidates to its list.  Threads
+// of one home cell walk the same candidates in lockstep (one address per
+// cell per load); the warp's trip count per stencil cell is the largest of
+// its home cells'.
+#ifndef NL_COUNT_MIN_BLOCKS
+#define NL_COUNT_MIN_BLOCKS 8
+#endif
+constexpr int kCountThreads = 128;
+
+template <typename TI, bool BATCH>
+__global__ void __launch_bounds__(kCountThreads, NL_COUNT_MIN_BLOCKS) k_count_atoms(PairArgs<TI> A) {
+  __shared__ unsigned dtab_blk[BATCH ? 1 : kStencilTab];
+  if (!BATCH) {
+    const int tx = 2 * A.g.nxyz[0] + 1, ty = 2 * A.g.nxyz[1] + 1;
+    const int tn = min(kStencilTab, tx * ty * (2 * A.g.nxyz[2] + 1));
+    for (int t = threadIdx.x; t < tn; t += blockDim.x)
+      dtab_blk[t] = pack3(t % tx - A.g.nxyz[0], (t / tx) % ty - A.g.nxyz[1], t / (tx * ty) - A.g.nxyz[2]);
+    __syncthreads();
+  }
+  const int list_cap = A.list_cap;
+  if (A.cap_rec && blockIdx.x == 0 && threadIdx.x == 0) *A.cap_rec = list_cap;
+  unsigned rechecks = 0;
+  for (long long sl = (long long)blockIdx.x * blockDim.x + threadIdx.x; sl < A.nat_total;
+       sl += (long long)gridDim.x * blockDim.x) {
+    const int slot = int(sl);
+    const int sys = BATCH ? batch_system(A.sys_atom, A.nsys, slot) : 0;
+    const Geometry& g = BATCH ? A.geo[sys] : A.g;
+    const int abase = BATCH ? A.sys_atom[sys] : 0;
+    const int coff = BATCH ? A.sys_cell[sys] + sys : 0;
+    const int hl = clampi(A.scell[slot] - (BATCH ? A.sys_cell[sys] : 0), g.ncells - 1);
+    const int hc0 = hl % g.ns[0] + 1, hc1 = (hl / g.ns[0]) % g.ns[1] + 1, hc2 = hl / (g.ns[0] * g.ns[1]) + 1;
+    const float4 u = A.rec[slot];
+    const unsigned mi = __float_as_uint(u.w);
+    const float lo = g.lo, hi = g.hi;
+    const int sx = 2 * g.nxyz[0] + 1, sy = 2 * g.nxyz[1] + 1;
+    const int nst = sx * sy * (2 * g.nxyz[2] + 1);
+    const int tabn = BATCH ? 0 : kStencilTab;
+    uint2* lst = A.lists ? A.lists + (long long)slot * list_cap : nullptr;
+    int cnt = 0;
+    // stencil cell q+1 is resolved (and its range loaded) while q is screened
+    unsigned n_slp = 0;
+    float n_ox = 0.f, n_oy = 0.f, n_oz = 0.f;
+    int n_cs = 0, n_ce = 0;
+    auto resolve = [&](int q) {
+      n_cs = n_ce = 0;
+      if (q >= nst) return;
+      const int lin = stencil_cell(g, dtab_blk, tabn, sx, sy, hc0, hc1, hc2, q, n_slp, n_ox, n_oy, n_oz);
+      if (lin < 0) return;
+      n_cs = clampi(A.cell_offsets[coff + lin] - 1 + abase, A.nat_total);
+      n_ce = clampi(A.cell_offsets[coff + lin + 1] - 1 + abase, A.nat_total);
+    };
+    resolve(0);
+    for (int q = 0; q < nst; ++q) {
+      const unsigned slp = n_slp;
+      const float ox = n_ox, oy = n_oy, oz = n_oz;
+      const int cs = n_cs, ce = n_ce;
+      resolve(q + 1);
+      // four candidates per step: their loads are in flight together
+      for (int j0 = cs; j0 < ce; j0 += 4) {
+        float4 rr[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) rr[k] = A.rec[min(j0 + k, ce - 1)];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const int j = j0 + k;
+          if (j >= ce) break;
+          const float4 r = rr[k];
+          const unsigned cw = cand_word(slp, __float_as_uint(r.w));
+          const bool ex = (cw & kExactBit) != 0;
+          const float nan = __int_as_float(0x7fc00000);
+          const float cx = ex ? nan : r.x + ox, cy = ex ? nan : r.y + oy, cz = ex ? nan : r.z + oz;
+          const float rx = cx - u.x, ry = cy - u.y, rz = cz - u.z;
+          const float r2 = fmaf(rz, rz, fmaf(ry, ry, rx * rx));
+          bool acc = r2 < lo && r2 > 0.f;
+          if (!(r2 > hi) && !acc) {
+            if (is_self(j, slot, cw, mi)) {
+              acc = false;
+            } else {
+              ++rechecks;
+              acc = exact_pair(g, A.Xs, slot, j, mi, cw);
+            }
+          }
+          if (acc) {
+            if (cnt < list_cap) lst[cnt] = make_uint2(unsigned(j), cw);
+            ++cnt;
+          }
+        }
+      }
+    }
+    const int orig = clampi(A.perm[slot] - 1, g.nat - 1);
+    A.counts[abase + orig] = cnt;
+    if (A.lcount) {
+      A.lcount[slot] = cnt;
+      A.sorig[slot] = abase + orig;
+    }
+    if (cnt > list_cap) {
+      // the atom's cell goes to the screening write pass, once
+      const int hg = (BATCH ? A.sys_cell[sys] : 0) + hl;
+      if (atomicExch(A.cell_flag + hg, 1) == 0) {
+        const int uix = atomicAdd(A.n_unmasked, 1);
+        if (uix < A.ncells_total) A.unmasked[uix] = hg;
+      }
+    }
+  }
+  if (rechecks) atomicAdd(A.stats, (unsigned long long)rechecks);
 }
 
 // ------------------------------------------------------------------------
@@ -905,7 +1074,16 @@ static void launch_modes(int mode, const PairArgs<TI>& a, int num_sms, cudaStrea
   if (blocks > (long long)num_sms * pbps) blocks = (long long)num_sms * pbps;
   if (blocks < 1) blocks = 1;
   switch (mode) {
-    case kModeCount: k_pairs<TI, kModeCount, BATCH><<<int(blocks), kPairWarps * 32, 0, st>>>(a); break;
+    case kModeCount:
+      if (a.count_kernel != 2) {  // default: one warp per home cell
+        k_pairs<TI, kModeCount, BATCH><<<int(blocks), kPairWarps * 32, 0, st>>>(a);
+      } else {
+        const int cbps = a.pair_blocks_per_sm > 0 ? a.pair_blocks_per_sm : NL_COUNT_MIN_BLOCKS;
+        long long cb = ((long long)a.nat_total + kCountThreads - 1) / kCountThreads;
+        if (cb > (long long)num_sms * cbps) cb = (long long)num_sms * cbps;
+        k_count_atoms<TI, BATCH><<<int(cb), kCountThreads, 0, st>>>(a);
+      }
+      break;
     case kModeFill: {
       if (!BATCH) k_cs_table<<<1, 128, 0, st>>>(a.g, a.cs_table, a.cap_rec, a.list_cap, a.err);
       if (a.list_cap > 0) {

@@ -53,6 +53,8 @@ struct PairArgs {
   double* cs_table;         // C'S for |S_k| <= 2 (built once per call by k_cs_table)
   int* unmasked;            // count pass: home cells left to the screening write pass
   int* n_unmasked;          // length of that list
+  int* cell_flag;           // per cell (zeroed per count): already in that list
+  int count_kernel;         // 0 / 1: one warp per home cell, 2: one thread per home atom
   int pair_blocks_per_sm;   // launch tuning (0 = default): count / screening grids
   int emit_blocks_per_sm;   // launch tuning (0 = default): list write grid
   unsigned long long* stats;  // [0] += FP64 rechecks

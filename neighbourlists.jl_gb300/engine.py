@@ -52,7 +52,7 @@ class NeighbourListEngine:
             capacity = int(1.15 * self.nat * rho * 4.0 / 3.0 * np.pi * self.cutoff ** 3) + 1024
         self._alloc(capacity)
         self.last_total = None
-        self.tuning = _lib.Tuning(0, 0)
+        self.tuning = _lib.Tuning(0, 0, 0)
         self._graph = None
 
     def _alloc(self, capacity: int):
@@ -88,8 +88,8 @@ class NeighbourListEngine:
         self.last_total = int(total.value)
         return self.last_total
 
-    def set_tuning(self, pair_blocks_per_sm: int = 0, emit_blocks_per_sm: int = 0) -> None:
-        self.tuning = _lib.Tuning(int(pair_blocks_per_sm), int(emit_blocks_per_sm))
+    def set_tuning(self, pair_blocks_per_sm: int = 0, emit_blocks_per_sm: int = 0, count_kernel: int = 0) -> None:
+        self.tuning = _lib.Tuning(int(pair_blocks_per_sm), int(emit_blocks_per_sm), int(count_kernel))
 
     def capture(self, X: torch.Tensor) -> torch.cuda.CUDAGraph:
         """Captures one launch on X in a CUDA graph; ``replay()`` re-runs it."""

@@ -127,3 +127,18 @@ def test_engine_graph_replay(nlpkg, orc):
     o = orc.neighbour_list(X, 5.0, C, (True, True, True), nthreads=8)
     assert np.array_equal(eng.i[:t].cpu().numpy().astype(np.int64), o.i)
     assert np.array_equal(eng.R[:t].cpu().numpy().view(np.int64), o.R.view(np.int64))
+
+
+@pytest.mark.parametrize("count_kernel", [1, 2])
+def test_batch_both_count_kernels(nlpkg, orc, count_kernel):
+    systems = cf.batch_systems(30, seed=17, nmax=600)
+    b = nlpkg.BatchNeighbourList([(x.shape[0], c, rc, p) for (x, c, rc, p) in systems])
+    b.set_tuning(0, 0, count_kernel)
+    X = torch.from_numpy(np.concatenate([s[0] for s in systems])).cuda()
+    b.run(X)
+    for s, (x, c, rc, p) in enumerate(systems):
+        _, pl = b.system(s, X)
+        o = orc.neighbour_list(x, rc, c, p, nthreads=8)
+        assert np.array_equal(to_np(pl.j).astype(np.int64), o.j), s
+        assert np.array_equal(to_np(pl.S).astype(np.int64), o.S), s
+        assert np.array_equal(to_np(pl.R).view(np.int64), o.R.view(np.int64)), s

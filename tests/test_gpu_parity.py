@@ -320,3 +320,25 @@ def test_pair_and_site_iterators(nlpkg, orc):
         a, b = o.first[i - 1] - 1, o.first[i] - 1
         assert np.array_equal(to_np(j).astype(np.int64), o.j[a:b])
         assert np.array_equal(to_np(R).view(np.int64), o.R[a:b].view(np.int64))
+
+
+@pytest.mark.parametrize("count_kernel", [1, 2])
+def test_both_count_kernels(nlpkg, orc, count_kernel):
+    """The warp-per-cell and thread-per-atom count passes give the same bits
+    (open and periodic axes, triclinic, a one-cell multi-image system, dense
+    cells that overflow the lists)."""
+    Xd_, Cd = cf.diamond_primitive()
+    Xf, Cf, pf = cf.fcc_sheared(n=5, seed=9)
+    cases = [
+        (cf.rand_config(3000, seed=51)[0], np.diag([cf.rand_config(3000, seed=51)[2]] * 3), 5.0, (True, False, True)),
+        (Xf, Cf, 5.0, pf),
+        (Xd_, Cd, 6.0, (True, True, True)),
+        (np.random.default_rng(52).random((400, 3)) * 6.0, np.diag([6.0] * 3), 2.2, (True, True, True)),
+        (cf.rand_config_triclinic(200, seed=53)[0], cf.triclinic_cell(), 3.0, (True, True, False)),
+    ]
+    for X, C, rc, pbc in cases:
+        eng = nlpkg.NeighbourListEngine(X.shape[0], C, rc, pbc)
+        eng.set_tuning(0, 0, count_kernel)
+        eng.run(torch.from_numpy(np.ascontiguousarray(X)).cuda())
+        o = orc.neighbour_list(X, rc, C, pbc, nthreads=8)
+        assert_identical(eng.pairlist(None), o)
