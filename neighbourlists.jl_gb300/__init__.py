@@ -26,6 +26,7 @@ from .api import (  # noqa: F401
     pairs,
     sites,
 )
+from .atoms import System, build_cell_list_system, isolated_cell, neighbour_list_system  # noqa: F401
 from .batch import BatchNeighbourList  # noqa: F401
 from .engine import NeighbourListEngine  # noqa: F401
 from .serving import NeighbourListServer, Request, poisson_trace  # noqa: F401

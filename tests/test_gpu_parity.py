@@ -342,3 +342,23 @@ def test_both_count_kernels(nlpkg, orc, count_kernel):
         eng.run(torch.from_numpy(np.ascontiguousarray(X)).cuda())
         o = orc.neighbour_list(X, rc, C, pbc, nthreads=8)
         assert_identical(eng.pairlist(None), o)
+
+
+def test_system_entry_points(nlpkg, orc):
+    """AtomsBase-style systems (ext/NeighbourListsAtomsBaseExt.jl): periodic
+    cell with a unit scale, and an isolated cluster whose cell is its
+    bounding box diag(max - min + 1) with positions left in place."""
+    X, C = cf.fcc_cubic(3.61, (3, 3, 3))
+    sysp = nlpkg.System(X / 8.0, C / 8.0, (True, True, True))  # a unit 8x larger; exact rescaling
+    nl = nlpkg.neighbour_list_system(sysp, 0.625, length_unit=8.0)
+    o = orc.neighbour_list(X, 5.0, C, (True, True, True))
+    assert_identical(nl, o)
+    rng = np.random.default_rng(61)
+    Xc = rng.random((120, 3)) * 12.0 + np.array([40.0, -5.0, 3.0])
+    iso = nlpkg.System(Xc, None, (False, False, False))
+    Ci = nlpkg.isolated_cell(Xc)
+    assert np.array_equal(Ci, np.diag((Xc.max(0) - Xc.min(0)) + 1.0))
+    nl = nlpkg.neighbour_list_system(iso, 4.0)
+    assert_identical(nl, orc.neighbour_list(Xc, 4.0, Ci, (False, False, False)))
+    clist = nlpkg.neighbour_list_system(iso, 4.0, lazy=True)
+    assert isinstance(clist, nlpkg.SortedCellList)
