@@ -707,7 +707,7 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
 #define NL_EMIT_MIN_BLOCKS 8
 #endif
 #ifndef NL_EMIT_STAGES
-#define NL_EMIT_STAGES 3
+#define NL_EMIT_STAGES 4
 #endif
 constexpr int kEmitWarps = 4;
 constexpr int kEmitMinBlocks = NL_EMIT_MIN_BLOCKS;  // resident blocks per SM the register budget targets
@@ -803,7 +803,85 @@ __global__ void __launch_bounds__(kEmitWarps * 32, kEmitMinBlocks) k_emit(PairAr
       }
       __syncwarp();
     };
-#if NL_EMIT_STAGES == 3
+#if NL_EMIT_STAGES == 4
+    // Three stages over the chunk's passes -- list entry (pass h), gathers
+    // (pass h-1), S / R / stores (pass h-2) -- with two register sets used
+    // alternately, so that no value waits to be copied between stages: the
+    // gathers of a pass are consumed only after another pass's stores.
+    {
+      const int c = lane < na ? (E.n[lane] + 31) >> 5 : 0;  // passes of atom `lane`
+      int ci = c;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, ci, o);
+        if (lane >= o) ci += v;
+      }
+      const int npass = __shfl_sync(0xffffffffu, ci, 31);
+      for (int k = 0; k < c; ++k) E.pass[ci - c + k] = (unsigned short)((lane << 8) | k);
+      __syncwarp();
+      struct StE {
+        uint2 e;
+        int a, r;
+        bool v;
+      };
+      struct StG {
+        double x0, x1, x2;
+        long long oj;
+        unsigned cw;
+        int a, r;
+        bool v;
+      };
+      auto stage_e = [&](int h, StE& t) {
+        t.v = h < npass;
+        if (t.v) {
+          const unsigned pd = E.pass[h];
+          t.a = int(pd >> 8);
+          t.r = 32 * int(pd & 255u) + lane;
+          t.e = __ldcs(A.lists + (c0 + t.a) * K + min(t.r, E.n[t.a] - 1));  // read once
+        }
+      };
+      auto stage_g = [&](const StE& t, StG& u) {
+        u.v = t.v;
+        if (u.v) {
+          const int slot_j = clampi(int(t.e.x), A.nat_total - 1);
+          u.x0 = __ldg(A.Xs + 3LL * slot_j + 0);
+          u.x1 = __ldg(A.Xs + 3LL * slot_j + 1);
+          u.x2 = __ldg(A.Xs + 3LL * slot_j + 2);
+          u.oj = (long long)__ldg(A.perm + slot_j);
+          u.cw = t.e.y;
+          u.a = t.a;
+          u.r = t.r;
+        }
+      };
+      auto stage_f = [&](const StG& u) {
+        if (u.v) {
+          pa = u.a;
+          pr = u.r;
+          pn = E.n[u.a];
+          pcw = u.cw;
+          poj = u.oj;
+          pxj0 = u.x0;
+          pxj1 = u.x1;
+          pxj2 = u.x2;
+          finish();
+        }
+      };
+      StE e0, e1;
+      StG g0, g1;
+      e0.v = e1.v = false;
+      g0.v = g1.v = false;
+      e0.a = e0.r = e1.a = e1.r = 0;
+      e0.e = e1.e = make_uint2(0u, 0u);
+      for (int h = 0; h < npass + 2; h += 2) {
+        stage_e(h, e0);
+        stage_g(e1, g1);
+        stage_f(g0);
+        stage_e(h + 1, e1);
+        stage_g(e0, g0);
+        stage_f(g1);
+      }
+    }
+#elif NL_EMIT_STAGES == 3
     // three stages over the chunk's passes: list entries two passes ahead,
     // gathers one pass ahead, S / R / stores for the current pass
     {

@@ -47,7 +47,20 @@ class Request:
     t_arrive: float = 0.0      # server clock (s)
     t_done: Optional[float] = None
     npairs: Optional[int] = None
-    result: Optional[dict] = field(default=None, repr=False)  # first, i, j, S, R (device tensors)
+    _res: Optional[tuple] = field(default=None, repr=False)
+
+    @property
+    def result(self) -> Optional[dict]:
+        """first, i, j, S, R of this request (device tensors).  Views into the
+        slot's arenas are valid until that slot runs its next batch; a server
+        with ``copy_results`` hands out copies."""
+        if self._res is None:
+            return None
+        if isinstance(self._res, dict):
+            return self._res
+        first, i, j, S, R, f0, p0, p1 = self._res
+        return {"first": first[f0:f0 + self.nat + 1], "i": i[p0:p1], "j": j[p0:p1],
+                "S": S[3 * p0:3 * p1].view(-1, 3), "R": R[3 * p0:3 * p1].view(-1, 3) if R is not None else None}
 
     @property
     def nat(self) -> int:
@@ -104,6 +117,7 @@ class NeighbourListServer:
         self.device = torch.device(device)
         self.mode = mode
         self.copy_results = copy_results
+        self.direct_copy_atoms = 8192  # pinned requests at least this large skip the staging copy
         self.budget = float(pair_budget_bytes)
         self.max_atoms = int(max_batch_atoms)
         self.max_systems = int(max_batch_systems) if mode == "batched" else 1
@@ -160,21 +174,25 @@ class NeighbourListServer:
         nat = sum(r.nat for r in reqs)
         Xd = s.buf("X", 3 * max(nat, 1), torch.float64)
         with torch.cuda.stream(s.stream):
-            if all(isinstance(r.X, torch.Tensor) and r.X.is_pinned() for r in reqs):
-                # pinned request buffers: one asynchronous copy each, no host staging
-                o = 0
-                for r in reqs:
-                    if r.nat:
-                        Xd[3 * o:3 * (o + r.nat)].view(r.nat, 3).copy_(r.X, non_blocking=True)
-                    o += r.nat
-            elif nat:
+            if nat:
+                # small requests are gathered into the slot's pinned staging
+                # buffer and copied at once; large pinned ones are copied
+                # directly (DMA, no host copy)
                 hX = s.host_X(nat)
                 hXn = hX.numpy()
-                o = 0
+                o, run0 = 0, 0
                 for r in reqs:
-                    hXn[o:o + r.nat] = r.X.numpy() if isinstance(r.X, torch.Tensor) else r.X
+                    direct = r.nat >= self.direct_copy_atoms and isinstance(r.X, torch.Tensor) and r.X.is_pinned()
+                    if direct:
+                        if o > run0:
+                            Xd[3 * run0:3 * o].view(o - run0, 3).copy_(hX[run0:o], non_blocking=True)
+                        Xd[3 * o:3 * (o + r.nat)].view(r.nat, 3).copy_(r.X, non_blocking=True)
+                        run0 = o + r.nat
+                    else:
+                        hXn[o:o + r.nat] = r.X.numpy() if isinstance(r.X, torch.Tensor) else r.X
                     o += r.nat
-                Xd[:3 * nat].view(nat, 3).copy_(hX[:nat], non_blocking=True)
+                if o > run0:
+                    Xd[3 * run0:3 * o].view(o - run0, 3).copy_(hX[run0:o], non_blocking=True)
             cap = max(sum(r.predicted_pairs() for r in reqs), 1)
             if self.mode == "batched":
                 self._launch_batched(s, reqs, nat, cap)
@@ -274,11 +292,10 @@ class NeighbourListServer:
         for k, r in enumerate(s.reqs):
             p0, p1 = int(po_h[k]), int(po_h[k + 1])
             f0 = a0 + k if self.mode == "batched" else 0
-            res = {"first": first[f0:f0 + r.nat + 1], "i": i[p0:p1], "j": j[p0:p1],
-                   "S": S[3 * p0:3 * p1].view(-1, 3), "R": R[3 * p0:3 * p1].view(-1, 3) if R is not None else None}
+            r._res = (first, i, j, S, R, f0, p0, p1)  # views are made on access
             if self.copy_results:
-                res = {key: (v.clone() if v is not None else None) for key, v in res.items()}
-            r.result, r.npairs, r.t_done = res, p1 - p0, t_done
+                r._res = {key: (v.clone() if v is not None else None) for key, v in r.result.items()}
+            r.npairs, r.t_done = p1 - p0, t_done
             a0 += r.nat
         done = s.reqs
         s.reqs, s.busy = [], False
