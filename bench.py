@@ -268,7 +268,7 @@ def run_gpu(args):
     if not args.no_e2e:
         e2e = measure_e2e(eng, X, Xd, total, stream, dev, args)
     extra = {}
-    if not args.no_extra and n_atoms == N_ATOMS:
+    if not args.no_extra and n_atoms == N_ATOMS and rank == 0:
         extra_steps = max(3, min(args.steps, 10))
         extra["lazy"] = bench_lazy(nl, eng, Xd, X, C, pbc, stream, flush, extra_steps)
         del eng

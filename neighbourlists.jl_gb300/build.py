@@ -54,7 +54,8 @@ def _headers_mtime() -> float:
 
 def _compile(src: str, verbose: bool, ptxas_v: bool) -> str:
     obj = os.path.join(BUILD, src.replace(".cu", ".o"))
-    cmd = [nvcc(), "-c", os.path.join(CSRC, src), "-o", obj] + flags(["-Xptxas", "-v"] if ptxas_v else [])
+    extra = os.environ.get("NLGPU_EXTRA_FLAGS", "").split()
+    cmd = [nvcc(), "-c", os.path.join(CSRC, src), "-o", obj] + flags(extra + (["-Xptxas", "-v"] if ptxas_v else []))
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
@@ -64,7 +65,13 @@ def _compile(src: str, verbose: bool, ptxas_v: bool) -> str:
 
 
 def build(force: bool = False, verbose: bool = False, ptxas_v: bool = False) -> str:
+    """Compiles libnlgpu.so when a source is newer.  NLGPU_EXTRA_FLAGS (e.g.
+    "-DNL_EMIT_FLAT=1") rebuilds with extra compile flags, for trying the
+    kernels' compile-time variants."""
     os.makedirs(BUILD, exist_ok=True)
+    extra = os.environ.get("NLGPU_EXTRA_FLAGS", "").split()
+    if extra:
+        force = True
     newest = max(_headers_mtime(), *(os.path.getmtime(os.path.join(CSRC, s)) for s in SOURCES),
                  os.path.getmtime(__file__))
     if not force and not ptxas_v and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:

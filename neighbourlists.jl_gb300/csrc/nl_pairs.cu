@@ -40,10 +40,14 @@ namespace nl {
 #ifndef NL_PAIR_CHUNK
 #define NL_PAIR_CHUNK 192
 #endif
+#ifndef NL_STAGE_UNROLL
+#define NL_STAGE_UNROLL 2
+#endif
 constexpr int kPairWarps = 4;                    // warps per block
 constexpr int kMinBlocks = NL_PAIR_MIN_BLOCKS;   // resident blocks per SM the register budget targets
 constexpr int kChunk = NL_PAIR_CHUNK;            // staged candidates per warp and pass
 constexpr int kGroup = NL_PAIR_GROUP;            // home atoms screened per candidate load
+constexpr int kStageUnroll = NL_STAGE_UNROLL;    // staging iterations interleaved (loads in flight)
 constexpr int kRing = 64;       // pair queue (ring) per warp
 constexpr int kCsR = 2;         // C'S table covers |S_k| <= kCsR
 constexpr int kCsN = 2 * kCsR + 1;
@@ -528,6 +532,7 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
           int nkeep = 0;
           __syncwarp();
           const bool prune = W.prune != 0;
+#pragma unroll kStageUnroll
           for (int f0 = 0; f0 < nch; f0 += 32) {
             const int f = f0 + lane;
             const int gf = cb + min(f, nch - 1);
@@ -701,14 +706,11 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
 // sorted slots; their per-atom data go to shared memory, then the warp walks
 // the atoms one at a time, lane r writing the atom's r-th pair.  The output
 // slots first[i] + r are consecutive, so the stores coalesce.  Passes run as
-// a two-stage pipeline: a pass's list entries and gathers are issued before
-// the previous pass computes S and R and stores.
+// a three-stage pipeline (list entries, gathers, S / R / stores).
 #ifndef NL_EMIT_MIN_BLOCKS
 #define NL_EMIT_MIN_BLOCKS 8
 #endif
-#ifndef NL_EMIT_STAGES
-#define NL_EMIT_STAGES 4
-#endif
+
 constexpr int kEmitWarps = 4;
 constexpr int kEmitMinBlocks = NL_EMIT_MIN_BLOCKS;  // resident blocks per SM the register budget targets
 
@@ -753,8 +755,7 @@ __global__ void __launch_bounds__(kEmitWarps * 32, kEmitMinBlocks) k_emit(PairAr
     }
     __syncwarp();
 
-    bool pv = false;  // a pass waits for stage 2
-    int pa = 0, pr = 0, pn = 0;
+    int pa = 0, pr = 0, pn = 0;  // the pass in stage 3
     unsigned pcw = 0;
     long long poj = 0;
     double pxj0 = 0.0, pxj1 = 0.0, pxj2 = 0.0;
@@ -803,7 +804,6 @@ __global__ void __launch_bounds__(kEmitWarps * 32, kEmitMinBlocks) k_emit(PairAr
       }
       __syncwarp();
     };
-#if NL_EMIT_STAGES == 4
     // Three stages over the chunk's passes -- list entry (pass h), gathers
     // (pass h-1), S / R / stores (pass h-2) -- with two register sets used
     // alternately, so that no value waits to be copied between stages: the
@@ -881,82 +881,6 @@ __global__ void __launch_bounds__(kEmitWarps * 32, kEmitMinBlocks) k_emit(PairAr
         stage_f(g1);
       }
     }
-#elif NL_EMIT_STAGES == 3
-    // three stages over the chunk's passes: list entries two passes ahead,
-    // gathers one pass ahead, S / R / stores for the current pass
-    {
-      const int c = lane < na ? (E.n[lane] + 31) >> 5 : 0;  // passes of atom `lane`
-      int ci = c;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int v = __shfl_up_sync(0xffffffffu, ci, o);
-        if (lane >= o) ci += v;
-      }
-      const int npass = __shfl_sync(0xffffffffu, ci, 31);
-      for (int k = 0; k < c; ++k) E.pass[ci - c + k] = (unsigned short)((lane << 8) | k);
-      __syncwarp();
-      uint2 eB = make_uint2(0u, 0u);
-      int aB = 0, rB = 0;
-      for (int t = 0; t < npass + 2; ++t) {
-        uint2 eA = make_uint2(0u, 0u);
-        int aA = 0, rA = 0;
-        if (t < npass) {  // stage 1: list entries
-          const unsigned pd = E.pass[t];
-          aA = int(pd >> 8);
-          rA = 32 * int(pd & 255u) + lane;
-          const int n = E.n[aA];
-          eA = __ldcs(A.lists + (c0 + aA) * K + min(rA, n - 1));  // read once
-        }
-        double xj0 = 0.0, xj1 = 0.0, xj2 = 0.0;
-        long long oj = 0;
-        if (t >= 1 && t - 1 < npass) {  // stage 2: gathers
-          const int slot_j = clampi(int(eB.x), A.nat_total - 1);
-          xj0 = __ldg(A.Xs + 3LL * slot_j + 0);
-          xj1 = __ldg(A.Xs + 3LL * slot_j + 1);
-          xj2 = __ldg(A.Xs + 3LL * slot_j + 2);
-          oj = (long long)__ldg(A.perm + slot_j);
-        }
-        if (pv) finish();  // stage 3
-        pv = t >= 1 && t - 1 < npass;
-        pa = aB;
-        pr = rB;
-        pn = E.n[aB];
-        pcw = eB.y;
-        poj = oj;
-        pxj0 = xj0;
-        pxj1 = xj1;
-        pxj2 = xj2;
-        eB = eA;
-        aB = aA;
-        rB = rA;
-      }
-    }
-#else
-    for (int a = 0; a < na; ++a) {
-      const int n = E.n[a];
-      const uint2* lst = A.lists + (c0 + a) * K;
-      for (int p = 0; p < n; p += 32) {
-        const int r = p + lane;
-        const uint2 e = __ldcs(lst + min(r, n - 1));  // read once
-        const int slot_j = clampi(int(e.x), A.nat_total - 1);
-        const double xj0 = __ldg(A.Xs + 3LL * slot_j + 0);
-        const double xj1 = __ldg(A.Xs + 3LL * slot_j + 1);
-        const double xj2 = __ldg(A.Xs + 3LL * slot_j + 2);
-        const long long oj = (long long)__ldg(A.perm + slot_j);
-        if (pv) finish();
-        pv = true;
-        pa = a;
-        pr = r;
-        pn = n;
-        pcw = e.y;
-        poj = oj;
-        pxj0 = xj0;
-        pxj1 = xj1;
-        pxj2 = xj2;
-      }
-    }
-    if (pv) finish();
-#endif
   }
 }
 
