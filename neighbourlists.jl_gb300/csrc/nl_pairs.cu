@@ -27,6 +27,8 @@
 // with ballots that preserve lane order, so each atom's pairs come out in the
 // reference's order, and R is computed with the reference's operations, so
 // i, j, S, R and first are bit-identical to the reference's arrays.
+#include <type_traits>
+
 #include "nl_pairs.cuh"
 
 namespace nl {
@@ -590,7 +592,9 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
           const int nround = (nkeep + 31) & ~31;
           for (int a0 = 0; a0 < nb; a0 += kGroup) {
             float ax[kGroup], ay[kGroup], az[kGroup];
-            long long next[kGroup];
+            // running pair count (count) or next output slot (fill) of each atom
+            using NextT = std::conditional_t<MODE == kModeFill, long long, int>;
+            NextT next[kGroup];
 #pragma unroll
             for (int k = 0; k < kGroup; ++k) {
               const int a = min(a0 + k, nb - 1);
@@ -599,7 +603,7 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
               ax[k] = use ? __shfl_sync(0xffffffffu, ux, a) : inf;
               ay[k] = use ? __shfl_sync(0xffffffffu, uy, a) : inf;
               az[k] = use ? __shfl_sync(0xffffffffu, uz, a) : inf;
-              next[k] = W.hnext[a];
+              next[k] = NextT(W.hnext[a]);
             }
             for (int r0 = 0; r0 < nround; r0 += 32) {
               const int f = r0 + lane;
@@ -628,19 +632,23 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
                   }
               }
               if constexpr (MODE == kModeCount) {
+                unsigned m[kGroup];
 #pragma unroll
-                for (int k = 0; k < kGroup; ++k) {
-                  const unsigned mask = __ballot_sync(0xffffffffu, acc[k]);
-                  if (mask != 0u && list_cap > 0) {
-                    // list entry: (slot of j, candidate word), in traversal order
-                    // (32-bit offsets: the host keeps nat * list_cap below 2^32)
-                    const unsigned pos = unsigned(next[k]) + unsigned(__popc(mask & lt_mask()));
+                for (int k = 0; k < kGroup; ++k) m[k] = __ballot_sync(0xffffffffu, acc[k]);
+                if (list_cap > 0) {
+                  // list entry: (slot of j, candidate word), in traversal order
+                  // (32-bit offsets: the host keeps nat * list_cap below 2^32)
+                  const uint2 ent = make_uint2(unsigned(W.cslot[f]), __float_as_uint(c.w));
+                  const unsigned lt = lt_mask();
+#pragma unroll
+                  for (int k = 0; k < kGroup; ++k) {
+                    const unsigned pos = unsigned(next[k]) + unsigned(__popc(m[k] & lt));
                     if (acc[k] && pos < unsigned(list_cap))
-                      A.lists[unsigned(hb + a0 + k) * unsigned(list_cap) + pos] =
-                          make_uint2(unsigned(W.cslot[f]), __float_as_uint(c.w));
+                      A.lists[unsigned(hb + a0 + k) * unsigned(list_cap) + pos] = ent;
                   }
-                  next[k] += __popc(mask);
                 }
+#pragma unroll
+                for (int k = 0; k < kGroup; ++k) next[k] += __popc(m[k]);
               } else {
 #pragma unroll
                 for (int k = 0; k < kGroup; ++k) {
