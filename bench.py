@@ -457,8 +457,9 @@ def bench_4m(nl, dev, stream, flush, steps):
 
 
 def measure_e2e(eng, X, Xd, total, stream, dev, args):
-    """Same metric through the engine with HOST buffers: pinned positions
-    copied in, every output array (first, i, j, S, R) copied back, per step."""
+    """Same metric through the engine with HOST buffers (launch_host): pinned
+    positions copied in, every output array (first, i, j, S, R) copied back
+    on several copy streams, per step."""
     import torch
 
     n_atoms = X.shape[0]
@@ -469,16 +470,10 @@ def measure_e2e(eng, X, Xd, total, stream, dev, args):
     h_S = torch.empty((total, 3), dtype=ti).pin_memory()
     h_R = torch.empty((total, 3), dtype=torch.float64).pin_memory()
     h_f = torch.empty(n_atoms + 1, dtype=ti).pin_memory()
-    Xdev = torch.empty_like(Xd)
+    out = {"first": h_f, "i": h_i, "j": h_j, "S": h_S, "R": h_R}
 
     def e2e_step():
-        Xdev.copy_(hX, non_blocking=True)
-        eng.launch(Xdev)
-        h_f.copy_(eng.first, non_blocking=True)
-        h_i.copy_(eng.i[:total], non_blocking=True)
-        h_j.copy_(eng.j[:total], non_blocking=True)
-        h_S.copy_(eng.S[:total], non_blocking=True)
-        h_R.copy_(eng.R[:total], non_blocking=True)
+        eng.launch_host(hX, out, stream=stream)
 
     e2e_step()
     torch.cuda.synchronize(dev)

@@ -108,6 +108,37 @@ class NeighbourListEngine:
     def replay(self) -> None:
         self._graph.replay()
 
+    def launch_host(self, hX: torch.Tensor, out: dict, copy_streams: int = 4, stream=None) -> None:
+        """End to end with host buffers: copies pinned positions ``hX`` in,
+        runs the pipeline, and copies first / i / j / S / R back into the
+        pinned host tensors of ``out`` (keys "first", "i", "j", "S", "R"; the
+        pair arrays sized for the expected pair count).  The copies out are
+        spread over ``copy_streams`` streams so that several copy engines run
+        at once; ``stream`` (default: current) waits for all of them, so work
+        or events recorded on it afterwards see the finished copies."""
+        main = stream if stream is not None else torch.cuda.current_stream(self.device)
+        if getattr(self, "_Xdev", None) is None or self._Xdev.shape[0] != self.nat:
+            self._Xdev = torch.empty((self.nat, 3), dtype=torch.float64, device=self.device)
+        if len(getattr(self, "_copy_streams", [])) != copy_streams:
+            self._copy_streams = [torch.cuda.Stream(device=self.device) for _ in range(copy_streams)]
+        with torch.cuda.stream(main):
+            self._Xdev.copy_(hX, non_blocking=True)
+            self.launch(self._Xdev, main)
+            done = torch.cuda.Event()
+            done.record(main)
+        P = out["i"].shape[0]
+        jobs = [(out["first"], self.first), (out["i"], self.i[:P]), (out["j"], self.j[:P]), (out["S"], self.S[:P])]
+        if out.get("R") is not None:
+            h = P // 2  # the largest array goes in two halves
+            jobs += [(out["R"][:h], self.R[:h]), (out["R"][h:], self.R[h:P])]
+        for k, (dst, src) in enumerate(jobs):
+            cs = self._copy_streams[k % copy_streams]
+            cs.wait_event(done)
+            with torch.cuda.stream(cs):
+                dst.copy_(src, non_blocking=True)
+        for cs in self._copy_streams:
+            main.wait_stream(cs)
+
     def sync_status(self, stream=None) -> None:
         check(lib().nl_sync_status(_ptr(self.ws), _stream_handle(stream)))
 

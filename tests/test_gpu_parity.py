@@ -362,3 +362,23 @@ def test_system_entry_points(nlpkg, orc):
     assert_identical(nl, orc.neighbour_list(Xc, 4.0, Ci, (False, False, False)))
     clist = nlpkg.neighbour_list_system(iso, 4.0, lazy=True)
     assert isinstance(clist, nlpkg.SortedCellList)
+
+
+def test_engine_launch_host(nlpkg, orc):
+    """End to end with pinned host buffers on several copy streams."""
+    X, C, L = cf.rand_config(30000, seed=71)
+    eng = nlpkg.NeighbourListEngine(X.shape[0], C, 5.0, (True, True, True))
+    t = eng.run(torch.from_numpy(X).cuda())
+    hX = torch.from_numpy(X).pin_memory()
+    out = {"first": torch.empty(X.shape[0] + 1, dtype=torch.int32).pin_memory(),
+           "i": torch.empty(t, dtype=torch.int32).pin_memory(), "j": torch.empty(t, dtype=torch.int32).pin_memory(),
+           "S": torch.empty((t, 3), dtype=torch.int32).pin_memory(),
+           "R": torch.empty((t, 3), dtype=torch.float64).pin_memory()}
+    eng.launch_host(hX, out)
+    torch.cuda.synchronize()
+    eng.sync_status()
+    o = orc.neighbour_list(X, 5.0, C, (True, True, True), nthreads=8)
+    assert np.array_equal(out["first"].numpy().astype(np.int64), o.first)
+    assert np.array_equal(out["j"].numpy().astype(np.int64), o.j)
+    assert np.array_equal(out["S"].numpy().astype(np.int64), o.S)
+    assert np.array_equal(out["R"].numpy().view(np.int64), o.R.view(np.int64))
