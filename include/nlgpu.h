@@ -122,6 +122,17 @@ int nl_neighbour_list(const double* d_X, int64_t nat, const double cell[9], cons
                       void* d_first, int64_t capacity, void* d_i, void* d_j, void* d_S, double* d_R,
                       int64_t* total_pairs, void* d_workspace, size_t workspace_bytes, void* stream);
 
+/* nl_neighbour_list for a half list: of the two directions (i, j, S) and
+ * (j, i, -S) of every pair only the one with j > i is kept, and for a
+ * periodic image of an atom itself (j == i) the one with S > 0
+ * lexicographically; each atom's pairs stay in the reference's order.  No
+ * counterpart in the reference (force loops that visit every pair once). */
+int nl_neighbour_list_half(const double* d_X, int64_t nat, const double cell[9], const double inv_cell[9],
+                           const int64_t ncells[3], const int64_t nxyz[3], const uint8_t pbc[3], double cutoff,
+                           int index_bytes, void* d_perm, double* d_X_sorted, void* d_cell_id, void* d_cell_offsets,
+                           void* d_first, int64_t capacity, void* d_i, void* d_j, void* d_S, double* d_R,
+                           int64_t* total_pairs, void* d_workspace, size_t workspace_bytes, void* stream);
+
 /* Lazy mode (for_each_neighbour over every atom, cell_list.jl:779-814) with a
  * built-in per-atom reduction: NL_REDUCE_COUNT -> int32 d_out[nat];
  * NL_REDUCE_INV_R6 -> double d_out[nat] = sum_j 1/((r2*r2)*r2), r2 = dot(R,R),

@@ -35,6 +35,7 @@ EXPORTED = [
     "nl_fill_pairs",
     "nl_neighbour_list",
     "nl_neighbour_list_static",
+    "nl_neighbour_list_half",
     "nl_lazy_reduce",
     "nl_batch_create",
     "nl_batch_create_auto",
@@ -117,6 +118,8 @@ def _declare(L):
     L.nl_neighbour_list.argtypes = [_vp, C.c_int64, _D, _D, _I64, _I64, _U8, C.c_double, C.c_int, _vp, _vp, _vp, _vp, _vp,
                                     C.c_int64, _vp, _vp, _vp, _vp, _I64, _vp, C.c_size_t, _vp]
     L.nl_neighbour_list.restype = C.c_int
+    L.nl_neighbour_list_half.argtypes = L.nl_neighbour_list.argtypes
+    L.nl_neighbour_list_half.restype = C.c_int
     L.nl_neighbour_list_static.argtypes = [_vp, C.c_int64, _D, _D, _I64, _I64, _U8, C.c_double, C.c_int, _vp, _vp,
                                            _vp, _vp, _vp, C.c_int64, _vp, _vp, _vp, _vp, _I64, _vp]
     L.nl_neighbour_list_static.restype = C.c_int

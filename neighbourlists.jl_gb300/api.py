@@ -241,8 +241,20 @@ def materialize_pairlist(clist: SortedCellList, with_R: bool = True, stream=None
 
 
 def neighbour_list(X, cutoff: float, cell, pbc, lazy: bool = False, int_type=torch.int32, with_R: bool = True,
-                   stream=None):
-    """neighbour_list(X, cutoff, cell, pbc; lazy, int_type) (cell_list.jl:897-916)."""
+                   stream=None, half: bool = False):
+    """neighbour_list(X, cutoff, cell, pbc; lazy, int_type) (cell_list.jl:897-916).
+    ``half=True`` returns a half list (each unordered pair once: j > i, or
+    j == i with S > 0 lexicographically), which the reference does not have."""
+    if half:
+        if lazy:
+            raise ValueError("a half list is a materialised list (lazy=False)")
+        from .engine import NeighbourListEngine
+
+        Xd = _device_positions(X)
+        eng = NeighbourListEngine(int(Xd.shape[0]), cell, cutoff, pbc, int_type=int_type, with_R=with_R,
+                                  device=Xd.device, half=True)
+        eng.run(Xd, stream)
+        return eng.pairlist(Xd)
     clist = build_cell_list(X, cutoff, cell, pbc, int_type=int_type, stream=stream)
     if lazy:
         return clist

@@ -408,7 +408,7 @@ nl::PairArgs<TI> pair_args(const nl::Geometry& g, const TI* cell_offsets, const 
 
 template <typename TI>
 int count_impl(const nl::Geometry& g, const double* Xs, const TI* perm, const TI* cell_id, const TI* cell_offsets,
-               int reuse, TI* first, void* ws, const Layout& L, cudaStream_t st) {
+               int reuse, TI* first, void* ws, const Layout& L, cudaStream_t st, int half = 0) {
   const int sms = num_sms();
   // reuse: keep err (set by the build), reset stats and the pair scan state
   const size_t z0 = reuse ? L.stats : L.err;
@@ -425,6 +425,7 @@ int count_impl(const nl::Geometry& g, const double* Xs, const TI* perm, const TI
                            at<unsigned>(ws, L.err), sms, st);
   nl::PairArgs<TI> a = pair_args<TI>(g, cell_offsets, perm, Xs, ws, L);
   a.counts = at<int>(ws, L.counts);
+  a.half = half;
   nl::launch_pairs<TI>(nl::kModeCount, a, sms, st);
   nl::launch_scan<TI>(at<int>(ws, L.counts), g.nat, first, nullptr, at<unsigned long long>(ws, L.st_pairs),
                       at<int>(ws, L.pcount), at<long long>(ws, L.totals) + 1, at<unsigned>(ws, L.err), st);
@@ -434,9 +435,11 @@ int count_impl(const nl::Geometry& g, const double* Xs, const TI* perm, const TI
 
 template <typename TI>
 int fill_impl(const nl::Geometry& g, const double* Xs, const TI* perm, const TI* cell_offsets, const TI* first,
-              int64_t capacity, TI* oi, TI* oj, TI* oS, double* oR, void* ws, const Layout& L, cudaStream_t st) {
+              int64_t capacity, TI* oi, TI* oj, TI* oS, double* oR, void* ws, const Layout& L, cudaStream_t st,
+              int half = 0) {
   if (g.nat == 0 || capacity <= 0) return NL_OK;
   nl::PairArgs<TI> a = pair_args<TI>(g, cell_offsets, perm, Xs, ws, L);
+  a.half = half;
   a.first = first;
   a.oi = oi;
   a.oj = oj;
@@ -617,10 +620,11 @@ int nl_build_cell_list(const double* d_X, int64_t nat, const double cell[9], con
                              static_cast<int64_t*>(d_cell_offsets), d_workspace, L, st);
 }
 
-int nl_count_pairs(const double* d_X_sorted, const void* d_perm, const void* d_cell_id, const void* d_cell_offsets,
-                   int64_t nat, const double cell[9], const double inv_cell[9], const int64_t ncells[3],
-                   const int64_t nxyz[3], const uint8_t pbc[3], double cutoff, int index_bytes, int reuse_records,
-                   void* d_first, int64_t* total_pairs, void* d_workspace, size_t workspace_bytes, void* stream) {
+static int count_pairs_entry(const double* d_X_sorted, const void* d_perm, const void* d_cell_id,
+                             const void* d_cell_offsets, int64_t nat, const double cell[9], const double inv_cell[9],
+                             const int64_t ncells[3], const int64_t nxyz[3], const uint8_t pbc[3], double cutoff,
+                             int index_bytes, int reuse_records, void* d_first, int64_t* total_pairs, void* d_workspace,
+                             size_t workspace_bytes, void* stream, int half) {
   if (!cell || !inv_cell || !ncells || !nxyz || !pbc || !d_first || !d_cell_offsets ||
       (nat > 0 && (!d_X_sorted || !d_perm || !d_cell_id)))
     return fail(NL_ERR_ARG, "null argument");
@@ -633,11 +637,11 @@ int nl_count_pairs(const double* d_X_sorted, const void* d_perm, const void* d_c
   if (index_bytes == 4)
     s = count_impl<int32_t>(g, d_X_sorted, static_cast<const int32_t*>(d_perm), static_cast<const int32_t*>(d_cell_id),
                             static_cast<const int32_t*>(d_cell_offsets), reuse_records, static_cast<int32_t*>(d_first),
-                            d_workspace, L, st);
+                            d_workspace, L, st, half);
   else
     s = count_impl<int64_t>(g, d_X_sorted, static_cast<const int64_t*>(d_perm), static_cast<const int64_t*>(d_cell_id),
                             static_cast<const int64_t*>(d_cell_offsets), reuse_records, static_cast<int64_t*>(d_first),
-                            d_workspace, L, st);
+                            d_workspace, L, st, half);
   if (s) return s;
   if (total_pairs) {
     if (nat == 0) {
@@ -649,11 +653,19 @@ int nl_count_pairs(const double* d_X_sorted, const void* d_perm, const void* d_c
   return NL_OK;
 }
 
-int nl_fill_pairs(const double* d_X_sorted, const void* d_perm, const void* d_cell_offsets, int64_t nat,
-                  const double cell[9], const double inv_cell[9], const int64_t ncells[3], const int64_t nxyz[3],
-                  const uint8_t pbc[3], double cutoff, int index_bytes, const void* d_first, int64_t capacity,
-                  void* d_i, void* d_j, void* d_S, double* d_R, void* d_workspace, size_t workspace_bytes,
-                  void* stream) {
+int nl_count_pairs(const double* d_X_sorted, const void* d_perm, const void* d_cell_id, const void* d_cell_offsets,
+                   int64_t nat, const double cell[9], const double inv_cell[9], const int64_t ncells[3],
+                   const int64_t nxyz[3], const uint8_t pbc[3], double cutoff, int index_bytes, int reuse_records,
+                   void* d_first, int64_t* total_pairs, void* d_workspace, size_t workspace_bytes, void* stream) {
+  return count_pairs_entry(d_X_sorted, d_perm, d_cell_id, d_cell_offsets, nat, cell, inv_cell, ncells, nxyz, pbc, cutoff,
+                           index_bytes, reuse_records, d_first, total_pairs, d_workspace, workspace_bytes, stream, 0);
+}
+
+static int fill_pairs_entry(const double* d_X_sorted, const void* d_perm, const void* d_cell_offsets, int64_t nat,
+                            const double cell[9], const double inv_cell[9], const int64_t ncells[3],
+                            const int64_t nxyz[3], const uint8_t pbc[3], double cutoff, int index_bytes,
+                            const void* d_first, int64_t capacity, void* d_i, void* d_j, void* d_S, double* d_R,
+                            void* d_workspace, size_t workspace_bytes, void* stream, int half) {
   if (!cell || !inv_cell || !ncells || !nxyz || !pbc || !d_first || !d_cell_offsets)
     return fail(NL_ERR_ARG, "null argument");
   if (capacity > 0 && (!d_i || !d_j || !d_S || !d_X_sorted || !d_perm)) return fail(NL_ERR_ARG, "null argument");
@@ -666,25 +678,62 @@ int nl_fill_pairs(const double* d_X_sorted, const void* d_perm, const void* d_ce
   if (index_bytes == 4)
     return fill_impl<int32_t>(g, d_X_sorted, static_cast<const int32_t*>(d_perm), static_cast<const int32_t*>(d_cell_offsets),
                               static_cast<const int32_t*>(d_first), capacity, static_cast<int32_t*>(d_i),
-                              static_cast<int32_t*>(d_j), static_cast<int32_t*>(d_S), d_R, d_workspace, L, st);
+                              static_cast<int32_t*>(d_j), static_cast<int32_t*>(d_S), d_R, d_workspace, L, st, half);
   return fill_impl<int64_t>(g, d_X_sorted, static_cast<const int64_t*>(d_perm), static_cast<const int64_t*>(d_cell_offsets),
                             static_cast<const int64_t*>(d_first), capacity, static_cast<int64_t*>(d_i),
-                            static_cast<int64_t*>(d_j), static_cast<int64_t*>(d_S), d_R, d_workspace, L, st);
+                            static_cast<int64_t*>(d_j), static_cast<int64_t*>(d_S), d_R, d_workspace, L, st, half);
 }
+
+int nl_fill_pairs(const double* d_X_sorted, const void* d_perm, const void* d_cell_offsets, int64_t nat,
+                  const double cell[9], const double inv_cell[9], const int64_t ncells[3], const int64_t nxyz[3],
+                  const uint8_t pbc[3], double cutoff, int index_bytes, const void* d_first, int64_t capacity,
+                  void* d_i, void* d_j, void* d_S, double* d_R, void* d_workspace, size_t workspace_bytes,
+                  void* stream) {
+  return fill_pairs_entry(d_X_sorted, d_perm, d_cell_offsets, nat, cell, inv_cell, ncells, nxyz, pbc, cutoff,
+                          index_bytes, d_first, capacity, d_i, d_j, d_S, d_R, d_workspace, workspace_bytes, stream, 0);
+}
+
+static int neighbour_list_entry(const double* d_X, int64_t nat, const double cell[9], const double inv_cell[9],
+                                const int64_t ncells[3], const int64_t nxyz[3], const uint8_t pbc[3], double cutoff,
+                                int index_bytes, void* d_perm, double* d_X_sorted, void* d_cell_id,
+                                void* d_cell_offsets, void* d_first, int64_t capacity, void* d_i, void* d_j, void* d_S,
+                                double* d_R, int64_t* total_pairs, void* d_workspace, size_t workspace_bytes,
+                                void* stream, int half);
 
 int nl_neighbour_list(const double* d_X, int64_t nat, const double cell[9], const double inv_cell[9],
                       const int64_t ncells[3], const int64_t nxyz[3], const uint8_t pbc[3], double cutoff,
                       int index_bytes, void* d_perm, double* d_X_sorted, void* d_cell_id, void* d_cell_offsets,
                       void* d_first, int64_t capacity, void* d_i, void* d_j, void* d_S, double* d_R,
                       int64_t* total_pairs, void* d_workspace, size_t workspace_bytes, void* stream) {
+  return neighbour_list_entry(d_X, nat, cell, inv_cell, ncells, nxyz, pbc, cutoff, index_bytes, d_perm, d_X_sorted,
+                              d_cell_id, d_cell_offsets, d_first, capacity, d_i, d_j, d_S, d_R, total_pairs,
+                              d_workspace, workspace_bytes, stream, 0);
+}
+
+int nl_neighbour_list_half(const double* d_X, int64_t nat, const double cell[9], const double inv_cell[9],
+                           const int64_t ncells[3], const int64_t nxyz[3], const uint8_t pbc[3], double cutoff,
+                           int index_bytes, void* d_perm, double* d_X_sorted, void* d_cell_id, void* d_cell_offsets,
+                           void* d_first, int64_t capacity, void* d_i, void* d_j, void* d_S, double* d_R,
+                           int64_t* total_pairs, void* d_workspace, size_t workspace_bytes, void* stream) {
+  return neighbour_list_entry(d_X, nat, cell, inv_cell, ncells, nxyz, pbc, cutoff, index_bytes, d_perm, d_X_sorted,
+                              d_cell_id, d_cell_offsets, d_first, capacity, d_i, d_j, d_S, d_R, total_pairs,
+                              d_workspace, workspace_bytes, stream, 1);
+}
+
+static int neighbour_list_entry(const double* d_X, int64_t nat, const double cell[9], const double inv_cell[9],
+                                const int64_t ncells[3], const int64_t nxyz[3], const uint8_t pbc[3], double cutoff,
+                                int index_bytes, void* d_perm, double* d_X_sorted, void* d_cell_id,
+                                void* d_cell_offsets, void* d_first, int64_t capacity, void* d_i, void* d_j, void* d_S,
+                                double* d_R, int64_t* total_pairs, void* d_workspace, size_t workspace_bytes,
+                                void* stream, int half) {
   int s = nl_build_cell_list(d_X, nat, cell, inv_cell, ncells, pbc, cutoff, index_bytes, d_perm, d_X_sorted, d_cell_id,
                              d_cell_offsets, d_workspace, workspace_bytes, stream);
   if (s) return s;
-  s = nl_count_pairs(d_X_sorted, d_perm, d_cell_id, d_cell_offsets, nat, cell, inv_cell, ncells, nxyz, pbc, cutoff,
-                     index_bytes, 1, d_first, nullptr, d_workspace, workspace_bytes, stream);
+  s = count_pairs_entry(d_X_sorted, d_perm, d_cell_id, d_cell_offsets, nat, cell, inv_cell, ncells, nxyz, pbc, cutoff,
+                        index_bytes, 1, d_first, nullptr, d_workspace, workspace_bytes, stream, half);
   if (s) return s;
-  s = nl_fill_pairs(d_X_sorted, d_perm, d_cell_offsets, nat, cell, inv_cell, ncells, nxyz, pbc, cutoff, index_bytes,
-                    d_first, capacity, d_i, d_j, d_S, d_R, d_workspace, workspace_bytes, stream);
+  s = fill_pairs_entry(d_X_sorted, d_perm, d_cell_offsets, nat, cell, inv_cell, ncells, nxyz, pbc, cutoff, index_bytes,
+                       d_first, capacity, d_i, d_j, d_S, d_R, d_workspace, workspace_bytes, stream, half);
   if (s) return s;
   if (total_pairs) {
     Layout L = layout(nat, ncells[0] * ncells[1] * ncells[2]);

@@ -58,6 +58,7 @@ constexpr unsigned kExactBit = kMetaExact;
 struct __align__(16) WarpSmem {
   float4 cv[kChunk];        // candidate: (x, y, z) relative to home corner; w = packed S base | exact bit
   int cslot[kChunk];        // candidate: sorted slot
+  int corig[kChunk];        // candidate: original index within its system (half lists)
   double hx[32][3];         // home batch: FP64 positions
   long long hnext[32];      // home batch: next output slot (fill) / running count (count)
   double hacc[32];          // home batch: lazy accumulators
@@ -173,6 +174,18 @@ __device__ __forceinline__ bool is_self(int cand_slot, int home_slot, unsigned c
   for (int k = 0; k < 3; ++k)
     if (field10(cw, k) - 512 + (ex ? 0 : field10(mi, k) - 128) != 0) return false;
   return true;
+}
+
+// Half lists keep (i, j, S) when j > i, or j == i (a periodic image of the
+// atom itself) and S > 0 lexicographically; of the two directions of every
+// accepted pair exactly one is kept.  For j == i, S is the loop shift.
+__device__ __forceinline__ bool half_keep(int oi, int oj, unsigned cw, unsigned mi) {
+  if (oj != oi) return oj > oi;
+  const bool ex = (cw & kMetaExact) != 0;
+  int s[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) s[k] = field10(cw, k) - 512 + (ex ? 0 : field10(mi, k) - 128);
+  return s[0] > 0 || (s[0] == 0 && (s[1] > 0 || (s[1] == 0 && s[2] > 0)));
 }
 
 // Full FP64 decision of one candidate pair with the reference arithmetic.
@@ -573,6 +586,7 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
               const int pos = nkeep + __popc(km & lt_mask());
               W.cv[pos] = cv;
               W.cslot[pos] = slot;
+              if (A.half) W.corig[pos] = int(A.perm[slot]) - 1;
             }
             nkeep += __popc(km);
           }
@@ -630,6 +644,11 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
                       acc[k] = exact_pair(g, A.Xs, hb + a, W.cslot[f], W.hmeta[a], __float_as_uint(c.w));
                     }
                   }
+              }
+              if (A.half) {  // half list: keep each unordered pair once
+#pragma unroll
+                for (int k = 0; k < kGroup; ++k)
+                  if (acc[k]) acc[k] = half_keep(W.horig[a0 + k], W.corig[f], __float_as_uint(c.w), W.hmeta[a0 + k]);
               }
               if constexpr (MODE == kModeCount) {
                 unsigned m[kGroup];
@@ -931,6 +950,7 @@ __global__ void __launch_bounds__(kCountThreads, NL_COUNT_MIN_BLOCKS) k_count_at
     const int hc0 = hl % g.ns[0] + 1, hc1 = (hl / g.ns[0]) % g.ns[1] + 1, hc2 = hl / (g.ns[0] * g.ns[1]) + 1;
     const float4 u = A.rec[slot];
     const unsigned mi = __float_as_uint(u.w);
+    const int horig = clampi(A.perm[slot] - 1, g.nat - 1);
     const float lo = g.lo, hi = g.hi;
     const int sx = 2 * g.nxyz[0] + 1, sy = 2 * g.nxyz[1] + 1;
     const int nst = sx * sy * (2 * g.nxyz[2] + 1);
@@ -980,6 +1000,7 @@ __global__ void __launch_bounds__(kCountThreads, NL_COUNT_MIN_BLOCKS) k_count_at
               acc = exact_pair(g, A.Xs, slot, j, mi, cw);
             }
           }
+          if (acc && A.half) acc = half_keep(horig, int(A.perm[j]) - 1, cw, mi);
           if (acc) {
             if (cnt < list_cap) lst[cnt] = make_uint2(unsigned(j), cw);
             ++cnt;
@@ -987,11 +1008,10 @@ __global__ void __launch_bounds__(kCountThreads, NL_COUNT_MIN_BLOCKS) k_count_at
         }
       }
     }
-    const int orig = clampi(A.perm[slot] - 1, g.nat - 1);
-    A.counts[abase + orig] = cnt;
+    A.counts[abase + horig] = cnt;
     if (A.lcount) {
       A.lcount[slot] = cnt;
-      A.sorig[slot] = abase + orig;
+      A.sorig[slot] = abase + horig;
     }
     if (cnt > list_cap) {
       // the atom's cell goes to the screening write pass, once

@@ -55,6 +55,7 @@ struct PairArgs {
   int* n_unmasked;          // length of that list
   int* cell_flag;           // per cell (zeroed per count): already in that list
   int count_kernel;         // 0 / 1: one warp per home cell, 2: one thread per home atom
+  int half;                 // count / write: keep each unordered pair once (j > i, or j == i and S > 0)
   int pair_blocks_per_sm;   // launch tuning (0 = default): count / screening grids
   int emit_blocks_per_sm;   // launch tuning (0 = default): list write grid
   unsigned long long* stats;  // [0] += FP64 rechecks

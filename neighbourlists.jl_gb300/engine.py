@@ -25,7 +25,7 @@ _U8 = C.POINTER(C.c_uint8)
 
 class NeighbourListEngine:
     def __init__(self, nat: int, cell, cutoff: float, pbc, int_type=torch.int32, with_R: bool = True,
-                 capacity: Optional[int] = None, device="cuda"):
+                 capacity: Optional[int] = None, device="cuda", half: bool = False):
         self.nat = int(nat)
         self.cell = np.asarray(cell, dtype=np.float64).reshape(3, 3).copy()
         self.cutoff = float(cutoff)
@@ -33,6 +33,7 @@ class NeighbourListEngine:
         self.ib = _index_bytes(int_type)
         self.ti = _tdtype(self.ib)
         self.with_R = with_R
+        self.half = bool(half)  # keep each unordered pair once (nl_neighbour_list_half)
         self.device = torch.device(device)
         self.plan = analyze_cell(self.cell, self.cutoff, int_type)
         p = self.plan
@@ -49,7 +50,7 @@ class NeighbourListEngine:
             # expected pairs for a homogeneous system plus headroom
             vol = abs(float(np.linalg.det(self.cell)))
             rho = self.nat / vol if vol > 0 else 0.0
-            capacity = int(1.15 * self.nat * rho * 4.0 / 3.0 * np.pi * self.cutoff ** 3) + 1024
+            capacity = int(1.15 * self.nat * rho * 4.0 / 3.0 * np.pi * self.cutoff ** 3 / (2 if half else 1)) + 1024
         self._alloc(capacity)
         self.last_total = None
         self.tuning = _lib.Tuning(0, 0, 0)
@@ -66,7 +67,8 @@ class NeighbourListEngine:
     def _call(self, X: torch.Tensor, total_ptr, stream):
         p = self.plan
         check(lib().nl_set_tuning(C.byref(self.tuning)))
-        return lib().nl_neighbour_list(
+        entry = lib().nl_neighbour_list_half if self.half else lib().nl_neighbour_list
+        return entry(
             _ptr(X), self.nat, p.cell_cm.ctypes.data_as(_D), p.inv_cm.ctypes.data_as(_D), p.ncells.ctypes.data_as(_I64),
             p.nxyz.ctypes.data_as(_I64), self.pbc.ctypes.data_as(_U8), self.cutoff, self.ib, _ptr(self.perm),
             _ptr(self.Xs), _ptr(self.cid), C.c_void_p(self.offs.data_ptr()), C.c_void_p(self.first.data_ptr()),

@@ -382,3 +382,47 @@ def test_engine_launch_host(nlpkg, orc):
     assert np.array_equal(out["j"].numpy().astype(np.int64), o.j)
     assert np.array_equal(out["S"].numpy().astype(np.int64), o.S)
     assert np.array_equal(out["R"].numpy().view(np.int64), o.R.view(np.int64))
+
+
+def half_of(o):
+    """The oracle's full list filtered to a half list: j > i, or j == i and
+    S > 0 lexicographically (order kept)."""
+    S = o.S
+    pos = (S[:, 0] > 0) | ((S[:, 0] == 0) & ((S[:, 1] > 0) | ((S[:, 1] == 0) & (S[:, 2] > 0))))
+    keep = (o.j > o.i) | ((o.j == o.i) & pos)
+    counts = np.bincount(o.i[keep] - 1, minlength=o.first.shape[0] - 1)
+    first = np.concatenate([[1], 1 + np.cumsum(counts)])
+    return keep, first
+
+
+@pytest.mark.parametrize("case", ["10k", "fcc", "diamond", "dense", "triclinic"])
+@pytest.mark.parametrize("count_kernel", [1, 2])
+def test_half_lists(nlpkg, orc, case, count_kernel):
+    """nl_neighbour_list_half == the full list filtered to j > i (or the
+    periodic images of an atom itself with S > 0), in the reference's order;
+    both count tilings; dense cells take the screening write pass."""
+    if case == "10k":
+        X, C, L = cf.rand_config(10000, seed=0)
+        rc, pbc = 5.0, (True, True, True)
+    elif case == "fcc":
+        X, C, pbc = cf.fcc_sheared(n=5, seed=3)
+        rc = 5.0
+    elif case == "diamond":
+        X, C = cf.diamond_primitive()
+        rc, pbc = 6.0, (True, True, True)
+    elif case == "dense":
+        X, C, pbc, rc = np.random.default_rng(81).random((400, 3)) * 6.0, np.diag([6.0] * 3), (True, True, True), 2.2
+    else:
+        X, C = cf.rand_config_triclinic(300, seed=82)
+        rc, pbc = 3.0, (True, False, True)
+    eng = nlpkg.NeighbourListEngine(X.shape[0], C, rc, pbc, half=True)
+    eng.set_tuning(0, 0, count_kernel)
+    t = eng.run(torch.from_numpy(np.ascontiguousarray(X)).cuda())
+    o = orc.neighbour_list(X, rc, C, pbc, nthreads=8)
+    keep, first = half_of(o)
+    assert t == int(keep.sum())
+    assert np.array_equal(eng.first.cpu().numpy().astype(np.int64), first)
+    assert np.array_equal(eng.i[:t].cpu().numpy().astype(np.int64), o.i[keep])
+    assert np.array_equal(eng.j[:t].cpu().numpy().astype(np.int64), o.j[keep])
+    assert np.array_equal(eng.S[:t].cpu().numpy().astype(np.int64), o.S[keep])
+    assert np.array_equal(eng.R[:t].cpu().numpy().view(np.int64), o.R[keep].view(np.int64))
