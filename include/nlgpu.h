@@ -133,6 +133,19 @@ int nl_neighbour_list_half(const double* d_X, int64_t nat, const double cell[9],
                            void* d_first, int64_t capacity, void* d_i, void* d_j, void* d_S, double* d_R,
                            int64_t* total_pairs, void* d_workspace, size_t workspace_bytes, void* stream);
 
+/* R = (X[j] - X[i]) + C'S for every pair of an existing list, the
+ * reference's _getR (cell_list.jl:525-531) over the whole list: d_X are the
+ * original-order positions (nat x 3), d_i / d_j 1-based, d_S npairs x 3, all
+ * in the index type.  Used for lists built without R and for Verlet reuse
+ * (the pairs of an earlier list, the positions of now).  Asynchronous. */
+int nl_pair_vectors(const double* d_X, int64_t nat, const double cell[9], int index_bytes, const void* d_i,
+                    const void* d_j, const void* d_S, int64_t npairs, double* d_R, void* stream);
+
+/* Largest |X[a] - X_ref[a]|^2 over the atoms (FP64; NaN if any position is
+ * NaN) into *d_out; the Verlet skin test of a reused list.  No counterpart in
+ * the reference.  Asynchronous; d_out is device memory. */
+int nl_max_displacement_sq(const double* d_X, const double* d_Xref, int64_t nat, double* d_out, void* stream);
+
 /* Lazy mode (for_each_neighbour over every atom, cell_list.jl:779-814) with a
  * built-in per-atom reduction: NL_REDUCE_COUNT -> int32 d_out[nat];
  * NL_REDUCE_INV_R6 -> double d_out[nat] = sum_j 1/((r2*r2)*r2), r2 = dot(R,R),

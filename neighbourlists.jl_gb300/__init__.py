@@ -23,6 +23,7 @@ from .api import (  # noqa: F401
     npairs,
     nsites,
     num_neighbours,
+    pair_vectors,
     pairs,
     sites,
 )
@@ -31,3 +32,4 @@ from .batch import BatchNeighbourList  # noqa: F401
 from .engine import NeighbourListEngine  # noqa: F401
 from .serving import NeighbourListServer, Request, poisson_trace  # noqa: F401
 from .tuning import autotune  # noqa: F401
+from .verlet import VerletList  # noqa: F401

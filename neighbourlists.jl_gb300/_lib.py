@@ -37,6 +37,8 @@ EXPORTED = [
     "nl_neighbour_list_static",
     "nl_neighbour_list_half",
     "nl_lazy_reduce",
+    "nl_pair_vectors",
+    "nl_max_displacement_sq",
     "nl_batch_create",
     "nl_batch_create_auto",
     "nl_batch_destroy",
@@ -145,6 +147,10 @@ def _declare(L):
     L.nl_set_tuning.restype = C.c_int
     L.nl_batch_set_tuning.argtypes = [_vp, C.POINTER(Tuning)]
     L.nl_batch_set_tuning.restype = C.c_int
+    L.nl_pair_vectors.argtypes = [_vp, C.c_int64, _D, C.c_int, _vp, _vp, _vp, C.c_int64, _vp, _vp]
+    L.nl_pair_vectors.restype = C.c_int
+    L.nl_max_displacement_sq.argtypes = [_vp, _vp, C.c_int64, _vp, _vp]
+    L.nl_max_displacement_sq.restype = C.c_int
     L.nl_sync_status.argtypes = [_vp, _vp]
     L.nl_sync_status.restype = C.c_int
     L.nl_last_recheck_count.argtypes = [_vp, _vp, _I64]

@@ -36,7 +36,7 @@ __all__ = [
     "SortedCellList", "PairList", "NLError", "analyze_cell", "build_cell_list", "materialize_pairlist",
     "neighbour_list", "npairs", "nsites", "nneigs", "maxneigs", "max_neighbours", "neigs", "neigss", "neighbours",
     "num_neighbours", "count_neighbours", "for_each_neighbour", "lazy_reduce", "cutoff", "pairs", "sites",
-    "PairIterator", "SiteIterator",
+    "PairIterator", "SiteIterator", "pair_vectors",
 ]
 
 _D = C.POINTER(C.c_double)
@@ -343,8 +343,26 @@ def neigs(nlist: PairList, i0: int):
     return j, R
 
 
+def pair_vectors(X: torch.Tensor, cell, i: torch.Tensor, j: torch.Tensor, S: torch.Tensor,
+                 out: Optional[torch.Tensor] = None, stream=None) -> torch.Tensor:
+    """R = (X[j] - X[i]) + C'S for every pair (the reference's _getR,
+    cell_list.jl:525-531), bit-equal to the R of a materialised list."""
+    P = int(i.shape[0])
+    if out is None:
+        out = torch.empty((P, 3), dtype=torch.float64, device=X.device)
+    cm = _colmajor(cell)
+    ib = 4 if i.dtype == torch.int32 else 8
+    check(lib().nl_pair_vectors(_ptr(X), int(X.shape[0]), cm.ctypes.data_as(_D), ib, _ptr(i), _ptr(j), _ptr(S), P,
+                                _ptr(out), _stream_handle(stream)))
+    return out
+
+
 def _getR(nlist: PairList, a: int, b: int) -> torch.Tensor:
-    raise NLError(_lib.NL_ERR_ARG, "this PairList was materialised without R (with_R=False)")
+    """R of pairs a..b-1 of a list materialised without R, on the device."""
+    if nlist.X is None:
+        raise NLError(_lib.NL_ERR_ARG, "this PairList has neither R nor the positions to compute it")
+    X = nlist.X.to(torch.float64).contiguous()
+    return pair_vectors(X, nlist.C, nlist.i[a:b], nlist.j[a:b], nlist.S[a:b].contiguous())
 
 
 def count_neighbours(clist: SortedCellList, i: int) -> int:

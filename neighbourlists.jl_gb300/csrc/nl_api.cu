@@ -959,6 +959,38 @@ int nl_batch_set_tuning(nl_batch* batch, const nl_tuning* tuning) {
   return NL_OK;
 }
 
+int nl_pair_vectors(const double* d_X, int64_t nat, const double cell[9], int index_bytes, const void* d_i,
+                    const void* d_j, const void* d_S, int64_t npairs, double* d_R, void* stream) {
+  if (!cell || npairs < 0 || nat < 0) return fail(NL_ERR_ARG, "invalid argument");
+  if (index_bytes != 4 && index_bytes != 8) return fail(NL_ERR_ARG, "index_bytes must be 4 or 8");
+  if (npairs == 0) return NL_OK;
+  if (!d_X || !d_i || !d_j || !d_S || !d_R || nat == 0) return fail(NL_ERR_ARG, "null argument");
+  if (nat > 2147483646LL) return fail(NL_ERR_ARG, "nat must be in [0, 2^31-2]");
+  nl::Geometry g;
+  std::memset(&g, 0, sizeof(g));
+  std::memcpy(g.C, cell, sizeof(g.C));
+  g.nat = int(nat);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (index_bytes == 4)
+    nl::launch_pair_vectors<int32_t>(g, d_X, static_cast<const int32_t*>(d_i), static_cast<const int32_t*>(d_j),
+                                     static_cast<const int32_t*>(d_S), npairs, d_R, num_sms(), st);
+  else
+    nl::launch_pair_vectors<int64_t>(g, d_X, static_cast<const int64_t*>(d_i), static_cast<const int64_t*>(d_j),
+                                     static_cast<const int64_t*>(d_S), npairs, d_R, num_sms(), st);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? NL_OK : cuda_fail(e, "launch pair vectors");
+}
+
+int nl_max_displacement_sq(const double* d_X, const double* d_Xref, int64_t nat, double* d_out, void* stream) {
+  if (!d_out || nat < 0 || (nat > 0 && (!d_X || !d_Xref))) return fail(NL_ERR_ARG, "null argument");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaMemsetAsync(d_out, 0, sizeof(double), st);
+  if (e != cudaSuccess) return cuda_fail(e, "memset");
+  nl::launch_max_disp_sq(d_X, d_Xref, nat, reinterpret_cast<unsigned long long*>(d_out), num_sms(), st);
+  e = cudaGetLastError();
+  return e == cudaSuccess ? NL_OK : cuda_fail(e, "launch max displacement");
+}
+
 int nl_sync_status(void* d_workspace, void* stream) {
   if (!d_workspace) return fail(NL_ERR_ARG, "null workspace");
   return sync_read(d_workspace, static_cast<cudaStream_t>(stream), nullptr, nullptr);

@@ -1093,6 +1093,76 @@ __global__ void __launch_bounds__(128) k_lazy_lists(PairArgs<TI> A) {
   }
 }
 
+// ------------------------------------------------------------------------
+// R = (X[j] - X[i]) + C'S for an existing pair list (the reference's _getR,
+// cell_list.jl:525-531, over every pair; Verlet reuse recomputes R this way
+// for moved atoms), and the largest squared displacement of a set of
+// positions from reference positions.
+template <typename TI>
+__global__ void __launch_bounds__(256) k_pair_vectors(Geometry g, const double* __restrict__ X, const TI* __restrict__ pi,
+                                                      const TI* __restrict__ pj, const TI* __restrict__ pS,
+                                                      long long npairs, double* __restrict__ R) {
+  __shared__ double cs_blk[3 * kCsN * kCsN * kCsN];
+  for (int t = threadIdx.x; t < kCsN * kCsN * kCsN; t += blockDim.x) {
+    const int s0 = t % kCsN - kCsR, s1 = (t / kCsN) % kCsN - kCsR, s2 = t / (kCsN * kCsN) - kCsR;
+    cs_blk[3 * t + 0] = cts_k(g.C, s0, s1, s2, 0);
+    cs_blk[3 * t + 1] = cts_k(g.C, s0, s1, s2, 1);
+    cs_blk[3 * t + 2] = cts_k(g.C, s0, s1, s2, 2);
+  }
+  __syncthreads();
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < npairs;
+       p += (long long)gridDim.x * blockDim.x) {
+    const long long i = clampi((long long)pi[p] - 1, g.nat - 1), j = clampi((long long)pj[p] - 1, g.nat - 1);
+    const double xi[3] = {X[3 * i + 0], X[3 * i + 1], X[3 * i + 2]};
+    const double xj[3] = {X[3 * j + 0], X[3 * j + 1], X[3 * j + 2]};
+    double r[3];
+    pair_R_lane(g, cs_blk, xi, xj, int(pS[3 * p + 0]), int(pS[3 * p + 1]), int(pS[3 * p + 2]), r);
+    R[3 * p + 0] = r[0];
+    R[3 * p + 1] = r[1];
+    R[3 * p + 2] = r[2];
+  }
+}
+
+__global__ void __launch_bounds__(256) k_max_disp_sq(const double* __restrict__ X, const double* __restrict__ Xref,
+                                                     long long nat, unsigned long long* __restrict__ out) {
+  double m = 0.0;
+  for (long long a = (long long)blockIdx.x * blockDim.x + threadIdx.x; a < nat; a += (long long)gridDim.x * blockDim.x) {
+    const double d0 = X[3 * a + 0] - Xref[3 * a + 0], d1 = X[3 * a + 1] - Xref[3 * a + 1],
+                 d2 = X[3 * a + 2] - Xref[3 * a + 2];
+    const double d = d0 * d0 + d1 * d1 + d2 * d2;
+    m = (d > m || d != d) ? d : m;  // a NaN displacement forces a rebuild
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const double v = __shfl_xor_sync(0xffffffffu, m, o);
+    m = (v > m || v != v) ? v : m;
+  }
+  // non-negative doubles (and NaN) order like their bit patterns
+  if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
+}
+
+template <typename TI>
+void launch_pair_vectors(const Geometry& g, const double* X, const TI* pi, const TI* pj, const TI* pS,
+                         long long npairs, double* R, int num_sms, cudaStream_t st) {
+  if (npairs <= 0) return;
+  long long b = (npairs + 255) / 256;
+  if (b > (long long)num_sms * 8) b = (long long)num_sms * 8;
+  k_pair_vectors<TI><<<int(b), 256, 0, st>>>(g, X, pi, pj, pS, npairs, R);
+}
+
+void launch_max_disp_sq(const double* X, const double* Xref, long long nat, unsigned long long* out, int num_sms,
+                        cudaStream_t st) {
+  if (nat <= 0) return;
+  long long b = (nat + 255) / 256;
+  if (b > (long long)num_sms * 8) b = (long long)num_sms * 8;
+  k_max_disp_sq<<<int(b), 256, 0, st>>>(X, Xref, nat, out);
+}
+
+template void launch_pair_vectors<int32_t>(const Geometry&, const double*, const int32_t*, const int32_t*,
+                                           const int32_t*, long long, double*, int, cudaStream_t);
+template void launch_pair_vectors<int64_t>(const Geometry&, const double*, const int64_t*, const int64_t*,
+                                           const int64_t*, long long, double*, int, cudaStream_t);
+
 template <typename TI, bool BATCH>
 static void launch_modes(int mode, const PairArgs<TI>& a, int num_sms, cudaStream_t st) {
   if (a.nat_total <= 0 || a.ncells_total <= 0) return;

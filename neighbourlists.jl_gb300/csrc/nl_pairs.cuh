@@ -78,6 +78,13 @@ __device__ __forceinline__ int batch_system(const int* __restrict__ first, int n
 template <typename TI>
 void launch_pairs(int mode, const PairArgs<TI>& a, int num_sms, cudaStream_t st);
 
+// R = (X[j] - X[i]) + C'S of an existing list; largest squared displacement
+template <typename TI>
+void launch_pair_vectors(const Geometry& g, const double* X, const TI* pi, const TI* pj, const TI* pS,
+                         long long npairs, double* R, int num_sms, cudaStream_t st);
+void launch_max_disp_sq(const double* X, const double* Xref, long long nat, unsigned long long* out, int num_sms,
+                        cudaStream_t st);
+
 // batches: the C'S table of every system
 void launch_cs_tables(const Geometry* geo, int nsys, double* out, cudaStream_t st);
 

@@ -426,3 +426,44 @@ def test_half_lists(nlpkg, orc, case, count_kernel):
     assert np.array_equal(eng.j[:t].cpu().numpy().astype(np.int64), o.j[keep])
     assert np.array_equal(eng.S[:t].cpu().numpy().astype(np.int64), o.S[keep])
     assert np.array_equal(eng.R[:t].cpu().numpy().view(np.int64), o.R[keep].view(np.int64))
+
+
+def test_pair_vectors_and_lists_without_R(nlpkg, orc):
+    """R of a list built without R comes from nl_pair_vectors, bit-equal."""
+    X, C, L = cf.rand_config(4000, seed=91)
+    nl = nlpkg.neighbour_list(torch.from_numpy(X).cuda(), 5.0, C, (True, False, True), with_R=False)
+    o = orc.neighbour_list(X, 5.0, C, (True, False, True))
+    for i in (1, 17, 4000):
+        j, R, S = nlpkg.neigss(nl, i)
+        a, b = o.first[i - 1] - 1, o.first[i] - 1
+        assert np.array_equal(to_np(R).view(np.int64), o.R[a:b].view(np.int64))
+    R = nlpkg.pair_vectors(nl.X, C, nl.i, nl.j, nl.S)
+    assert np.array_equal(to_np(R).view(np.int64), o.R.view(np.int64))
+
+
+def test_verlet_reuse(nlpkg, orc):
+    """Lists built at cutoff + skin are reused while atoms move less than
+    skin / 2: R is recomputed for the new positions (bit-equal to the
+    reference formula) and every pair within the cutoff is in the list."""
+    X0, C, L = cf.rand_config(6000, seed=92)
+    rc, skin, pbc = 5.0, 1.0, (True, True, True)
+    v = nlpkg.VerletList(X0.shape[0], C, rc, skin, pbc)
+    rng = np.random.default_rng(93)
+    X = X0.copy()
+    for step in range(4):
+        Xd = torch.from_numpy(X).cuda()
+        rebuilt = v.update(Xd)
+        assert rebuilt == (step in (0, 3))
+        P = v.engine.total_pairs()
+        i, j, S = (t[:P].cpu().numpy().astype(np.int64) for t in (v.engine.i, v.engine.j, v.engine.S))
+        R = v.engine.R[:P].cpu().numpy()
+        Sf = S.astype(np.float64)
+        cs = (Sf[:, 0:1] * C[0] + Sf[:, 1:2] * C[1]) + Sf[:, 2:3] * C[2]  # C'S, left fold, no FMA
+        ref = (X[j - 1] - X[i - 1]) + cs  # _getR (cell_list.jl:525-531)
+        assert np.array_equal(R.view(np.int64), ref.view(np.int64))
+        o = orc.neighbour_list(X, rc, C, pbc)
+        inside = np.einsum("ij,ij->i", R, R) < rc * rc
+        got = set(zip(i[inside].tolist(), j[inside].tolist(), map(tuple, S[inside].tolist())))
+        want = set(zip(o.i.tolist(), o.j.tolist(), map(tuple, o.S.tolist())))
+        assert got == want
+        X = X + rng.uniform(-0.12, 0.12, size=X.shape) * (1.0 if step < 2 else 4.0)
