@@ -277,6 +277,8 @@ def run_gpu(args):
         torch.cuda.empty_cache()
         extra["atoms_4m"] = bench_4m(nl, dev, stream, flush, extra_steps)
         torch.cuda.empty_cache()
+        extra.update(bench_half_and_verlet(nl, dev, stream, flush, extra_steps))
+        torch.cuda.empty_cache()
         extra["serving"] = bench_serving(nl, dev)
     if rank != 0:
         return
@@ -441,6 +443,35 @@ def bench_serving(nl, dev, rates=(1_000, 5_000, 20_000, 50_000), n_req=1_500):
     top = out["rates"][str(rates[-1])]
     out["speedup_vs_plain_at_max_rate"] = top["batched"]["systems_per_s"] / top["plain"]["systems_per_s"]
     return out
+
+
+def bench_half_and_verlet(nl, dev, stream, flush, steps):
+    """The same 1M-atom system as a half list, and Verlet reuse at cutoff +
+    skin 0.5 A: a reuse step (displacement test + R for the kept pairs)
+    against a rebuild."""
+    import torch
+
+    X, C, pbc = workload()
+    Xd = torch.from_numpy(X).to(dev)
+    eng = nl.NeighbourListEngine(X.shape[0], C, CUTOFF, pbc, device=dev, half=True)
+    total = eng.run(Xd)
+    half_ms = timed_steps(lambda: eng.launch(Xd), steps, flush, stream)
+    eng.sync_status()
+    del eng
+    skin = 0.5
+    v = nl.VerletList(X.shape[0], C, CUTOFF, skin, pbc, device=dev)
+    v.update(Xd)
+    vpairs = v.engine.total_pairs()
+    rng = np.random.default_rng(5)
+    Xm = torch.from_numpy(X + rng.uniform(-0.05, 0.05, size=X.shape)).to(dev)
+    reuse_ms = timed_steps(lambda: v.update(Xm), steps, flush, stream)
+    rebuild_ms = timed_steps(lambda: v.engine.launch(Xm), steps, flush, stream)
+    v.engine.sync_status()
+    return {"half": {"workload": "1M-atom workload as a half list (j > i)", "pairs": int(total), "ms_per_step": half_ms,
+                     "pairs_per_s": total / (half_ms * 1e-3)},
+            "verlet": {"workload": f"1M-atom workload, list at cutoff + {skin} A skin, atoms moved by up to 0.05 A",
+                       "pairs": int(vpairs), "reuse_ms": reuse_ms, "rebuild_ms": rebuild_ms,
+                       "reuses": v.reuses, "rebuilds": v.rebuilds}}
 
 
 def bench_4m(nl, dev, stream, flush, steps):
