@@ -170,7 +170,7 @@ struct Layout {
   // [err 64 | stats 64] [pairs zero region: counters 64 | st_pairs | cell_flag]
   // [build zero region: counters 64 | st_cells | cell_count] [arrays...]
   size_t err, stats, pcount, st_pairs, cell_flag, pend, bcount, st_cells, cell_count, bend;
-  size_t totals, cell_start, cid, ticket, rec, tmp, rec_sorted, scell, counts, lcount, sorig, cs_table, unmasked,
+  size_t totals, cell_start, cid, ticket, rec, tmp, rec_sorted, scell, counts, lcount, sorig, cs_table, screen_cells,
       big_list, base_end, lists, end;
   bool use_lists = true;  // the workspace holds the pair lists (it reaches `end`)
 };
@@ -220,7 +220,7 @@ Layout layout(int64_t nat, int64_t ncells) {
   o += up(sizeof(int) * n);
   L.cs_table = o;
   o += up(sizeof(double) * 3 * 125);
-  L.unmasked = o;
+  L.screen_cells = o;
   o += up(sizeof(int) * size_t(ncells > 0 ? ncells : 1));
   L.big_list = o;
   o += up(sizeof(int) * size_t(ncells < (int64_t)n ? ncells : (int64_t)n));
@@ -395,8 +395,8 @@ nl::PairArgs<TI> pair_args(const nl::Geometry& g, const TI* cell_offsets, const 
   a.sorig = at<int>(ws, L.sorig);
   a.cap_rec = at<int>(ws, L.pcount) + 2;  // the count pass's list_cap, checked by the write pass
   a.cs_table = at<double>(ws, L.cs_table);
-  a.unmasked = at<int>(ws, L.unmasked);
-  a.n_unmasked = at<int>(ws, L.pcount) + 4;  // zeroed with the pair scan state
+  a.screen_cells = at<int>(ws, L.screen_cells);
+  a.n_screen_cells = at<int>(ws, L.pcount) + 4;  // zeroed with the pair scan state
   a.cell_flag = at<int>(ws, L.cell_flag);     // likewise
   a.count_kernel = g_tuning.count_kernel;
   a.pair_blocks_per_sm = g_tuning.pair_blocks_per_sm;
@@ -766,7 +766,7 @@ int nl_lazy_reduce(const double* d_X_sorted, const void* d_perm, const void* d_c
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   cudaError_t e = cudaSuccess;
   if (!reuse_records) e = cudaMemsetAsync(d_workspace, 0, 128, st);
-  // the count kernel appends its unmasked cells to a list counted in pcount
+  // the count kernel appends the cells left to the screening pass to a list counted in pcount
   if (e == cudaSuccess) e = cudaMemsetAsync(static_cast<char*>(d_workspace) + L.pcount, 0, L.pend - L.pcount, st);
   if (e != cudaSuccess) return cuda_fail(e, "memset workspace");
   const int sms = num_sms();

@@ -402,12 +402,12 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
   // Single systems prefetch the ranges of the next cell one cell ahead: its
   // home range and, per lane, the range of its stencil cell in the first
   // group of 32.
-  // The fill pass visits only the cells that the count pass could not mask
+  // The fill pass visits only the cells whose pairs the count pass could not list
   // (k_emit writes the others); count and lazy visit every cell.
   // (so does the lazy pass when the per-atom lists cover the other cells)
   const bool listed = MODE == kModeFill || (MODE == kModeLazyR6 && A.list_cap > 0);
-  const int ncell_iter = listed ? min(*A.n_unmasked, A.ncells_total) : A.ncells_total;
-  auto cell_at = [&](int idx) { return listed ? clampi(A.unmasked[idx], A.ncells_total - 1) : idx; };
+  const int ncell_iter = listed ? min(*A.n_screen_cells, A.ncells_total) : A.ncells_total;
+  auto cell_at = [&](int idx) { return listed ? clampi(A.screen_cells[idx], A.ncells_total - 1) : idx; };
   int idx = blockIdx.x * kPairWarps + warp;
   // (0-based slot offsets, clamped to [0, nat])
   int pf_hs = 0, pf_he = 0, pf_lo = 0, pf_hi = 0;
@@ -717,8 +717,8 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
     // a cell with an atom whose list overflowed (or with no lists at all) is
     // written by the screening write pass
     if (MODE == kModeCount && __any_sync(0xffffffffu, overflow) && lane == 0) {
-      const int u = atomicAdd(A.n_unmasked, 1);
-      if (u < A.ncells_total) A.unmasked[u] = h;
+      const int u = atomicAdd(A.n_screen_cells, 1);
+      if (u < A.ncells_total) A.screen_cells[u] = h;
     }
   }
   // statistics: number of FP64 decisions
@@ -1017,8 +1017,8 @@ __global__ void __launch_bounds__(kCountThreads, NL_COUNT_MIN_BLOCKS) k_count_at
       // the atom's cell goes to the screening write pass, once
       const int hg = (BATCH ? A.sys_cell[sys] : 0) + hl;
       if (atomicExch(A.cell_flag + hg, 1) == 0) {
-        const int uix = atomicAdd(A.n_unmasked, 1);
-        if (uix < A.ncells_total) A.unmasked[uix] = hg;
+        const int uix = atomicAdd(A.n_screen_cells, 1);
+        if (uix < A.ncells_total) A.screen_cells[uix] = hg;
       }
     }
   }

@@ -51,8 +51,8 @@ struct PairArgs {
   int list_cap;             // kListCap, or 0: no lists (every cell takes the screening write pass)
   int* cap_rec;             // list_cap of the count pass (the write pass checks it)
   double* cs_table;         // C'S for |S_k| <= 2 (built once per call by k_cs_table)
-  int* unmasked;            // count pass: home cells left to the screening write pass
-  int* n_unmasked;          // length of that list
+  int* screen_cells;            // count pass: home cells left to the screening write pass
+  int* n_screen_cells;          // length of that list
   int* cell_flag;           // per cell (zeroed per count): already in that list
   int count_kernel;         // 0 / 1: one warp per home cell, 2: one thread per home atom
   int half;                 // count / write: keep each unordered pair once (j > i, or j == i and S > 0)
