@@ -64,15 +64,16 @@ class NeighbourListEngine:
         self.S = torch.empty((capacity, 3), dtype=self.ti, device=self.device)
         self.R = torch.empty((capacity, 3), dtype=torch.float64, device=self.device) if self.with_R else None
 
-    def _call(self, X: torch.Tensor, total_ptr, stream):
+    def _call(self, X: torch.Tensor, total_ptr, stream, outputs=None):
         p = self.plan
         check(lib().nl_set_tuning(C.byref(self.tuning)))
         entry = lib().nl_neighbour_list_half if self.half else lib().nl_neighbour_list
+        i, j, S, R, cap = outputs if outputs is not None else (self.i, self.j, self.S, self.R, self.capacity)
         return entry(
             _ptr(X), self.nat, p.cell_cm.ctypes.data_as(_D), p.inv_cm.ctypes.data_as(_D), p.ncells.ctypes.data_as(_I64),
             p.nxyz.ctypes.data_as(_I64), self.pbc.ctypes.data_as(_U8), self.cutoff, self.ib, _ptr(self.perm),
             _ptr(self.Xs), _ptr(self.cid), C.c_void_p(self.offs.data_ptr()), C.c_void_p(self.first.data_ptr()),
-            self.capacity, _ptr(self.i), _ptr(self.j), _ptr(self.S), _ptr(self.R), total_ptr, _ptr(self.ws),
+            cap, _ptr(i), _ptr(j), _ptr(S), _ptr(R), total_ptr, _ptr(self.ws),
             self.ws.numel(), _stream_handle(stream))
 
     def launch(self, X: torch.Tensor, stream=None) -> None:
@@ -110,17 +111,34 @@ class NeighbourListEngine:
     def replay(self) -> None:
         self._graph.replay()
 
-    def launch_host(self, hX: torch.Tensor, out: dict, copy_streams: int = 4, stream=None) -> None:
+    def launch_host(self, hX: torch.Tensor, out: dict, copy_streams: int = 4, stream=None,
+                    direct: bool = False) -> None:
         """End to end with host buffers: copies pinned positions ``hX`` in,
-        runs the pipeline, and copies first / i / j / S / R back into the
+        runs the pipeline, and brings first / i / j / S / R back into the
         pinned host tensors of ``out`` (keys "first", "i", "j", "S", "R"; the
-        pair arrays sized for the expected pair count).  The copies out are
-        spread over ``copy_streams`` streams so that several copy engines run
-        at once; ``stream`` (default: current) waits for all of them, so work
-        or events recorded on it afterwards see the finished copies."""
+        pair arrays sized for the expected pair count).
+
+        direct=False: the pairs are written to the device buffers and copied
+        out, spread over ``copy_streams`` streams so that several copy engines
+        run at once.  direct=True: the write pass stores i, j, S, R straight
+        into the pinned host tensors (they are addressable from the GPU) and
+        only ``first`` is copied.  ``stream`` (default: current) waits for
+        everything, so work or events recorded on it afterwards see the
+        finished outputs."""
         main = stream if stream is not None else torch.cuda.current_stream(self.device)
         if getattr(self, "_Xdev", None) is None or self._Xdev.shape[0] != self.nat:
             self._Xdev = torch.empty((self.nat, 3), dtype=torch.float64, device=self.device)
+        if direct:
+            P = out["i"].shape[0]
+            for key in ("i", "j", "S", "R"):
+                t = out.get(key)
+                if t is not None and not t.is_pinned():
+                    raise ValueError("direct output needs pinned host tensors")
+            with torch.cuda.stream(main):
+                self._Xdev.copy_(hX, non_blocking=True)
+                check(self._call(self._Xdev, None, main, outputs=(out["i"], out["j"], out["S"], out.get("R"), P)))
+                out["first"].copy_(self.first, non_blocking=True)
+            return
         if len(getattr(self, "_copy_streams", [])) != copy_streams:
             self._copy_streams = [torch.cuda.Stream(device=self.device) for _ in range(copy_streams)]
         with torch.cuda.stream(main):
