@@ -1166,10 +1166,12 @@ template void launch_pair_vectors<int64_t>(const Geometry&, const double*, const
 template <typename TI, bool BATCH>
 static void launch_modes(int mode, const PairArgs<TI>& a, int num_sms, cudaStream_t st) {
   if (a.nat_total <= 0 || a.ncells_total <= 0) return;
-  // grids: the tuned number of blocks per SM (default: the resident ones);
-  // every kernel walks its cells / atoms in a grid-stride loop
-  const int pbps = a.pair_blocks_per_sm > 0 ? a.pair_blocks_per_sm : kMinBlocks;
-  const int ebps = a.emit_blocks_per_sm > 0 ? a.emit_blocks_per_sm : kEmitMinBlocks;
+  // grids: the tuned number of blocks per SM, by default twice (count) and
+  // four times (write) the resident ones, so that the tail of uneven cells
+  // and atoms balances over the SMs; every kernel walks its cells / atoms in
+  // a grid-stride loop
+  const int pbps = a.pair_blocks_per_sm > 0 ? a.pair_blocks_per_sm : 2 * kMinBlocks;
+  const int ebps = a.emit_blocks_per_sm > 0 ? a.emit_blocks_per_sm : 4 * kEmitMinBlocks;
   long long blocks = ((long long)a.ncells_total + kPairWarps - 1) / kPairWarps;
   if (blocks > (long long)num_sms * pbps) blocks = (long long)num_sms * pbps;
   if (blocks < 1) blocks = 1;
