@@ -467,3 +467,29 @@ def test_verlet_reuse(nlpkg, orc):
         want = set(zip(o.i.tolist(), o.j.tolist(), map(tuple, o.S.tolist())))
         assert got == want
         X = X + rng.uniform(-0.12, 0.12, size=X.shape) * (1.0 if step < 2 else 4.0)
+
+
+def test_half_int64_and_verlet_half(nlpkg, orc):
+    """Half lists in Int64, and Verlet reuse of a half list."""
+    X, C, L = cf.rand_config(5000, seed=101)
+    pbc = (True, True, False)
+    eng = nlpkg.NeighbourListEngine(X.shape[0], C, 5.0, pbc, int_type=torch.int64, half=True)
+    t = eng.run(torch.from_numpy(X).cuda())
+    o = orc.neighbour_list(X, 5.0, C, pbc, ti_bytes=8, nthreads=8)
+    keep, first = half_of(o)
+    assert t == int(keep.sum()) and eng.i.dtype == torch.int64
+    assert np.array_equal(eng.j[:t].cpu().numpy(), o.j[keep])
+    assert np.array_equal(eng.R[:t].cpu().numpy().view(np.int64), o.R[keep].view(np.int64))
+    v = nlpkg.VerletList(X.shape[0], C, 4.0, 1.0, pbc, half=True)
+    v.update(torch.from_numpy(X).cuda())
+    X2 = X + np.random.default_rng(102).uniform(-0.1, 0.1, size=X.shape)
+    assert not v.update(torch.from_numpy(X2).cuda())
+    P = v.engine.total_pairs()
+    i, j, S = (t_[:P].cpu().numpy().astype(np.int64) for t_ in (v.engine.i, v.engine.j, v.engine.S))
+    R = v.engine.R[:P].cpu().numpy()
+    inside = np.einsum("ij,ij->i", R, R) < 16.0
+    o2 = orc.neighbour_list(X2, 4.0, C, pbc)
+    keep2, _ = half_of(o2)
+    got = set(zip(i[inside].tolist(), j[inside].tolist(), map(tuple, S[inside].tolist())))
+    want = set(zip(o2.i[keep2].tolist(), o2.j[keep2].tolist(), map(tuple, o2.S[keep2].tolist())))
+    assert got == want
