@@ -226,6 +226,56 @@ int nl_batch_neighbour_list(const nl_batch* batch, const double* d_X, void* d_pe
                             int64_t capacity, void* d_i, void* d_j, void* d_S, double* d_R, int64_t* total_pairs,
                             void* d_workspace, size_t workspace_bytes, void* stream);
 
+/* ---- legacy linked-list PairList -----------------------------------------
+ * The reference's legacy constructor PairList(X::Vector{SVec}, cutoff, cell,
+ * pbc; int_type, fixcell) (cell_list.jl:11-20, _pairlist_ :369-385), kept
+ * there as a second implementation.  Its arithmetic differs from the
+ * sort-based path: the distance is formed from bin-relative positions
+ * (_find_neighbours_!, :301-366), S = (ci0 - cj + xyz) .÷ ns with a
+ * truncating division, and each atom's neighbours are sorted by j
+ * (sort_neigs!, :427-446; ties keep the traversal order).  These calls
+ * reproduce it exactly: i, j, S and first equal the reference's.
+ *
+ * Sequence: nl_legacy_fix_cell (fixcell = true) -> nl_analyze_cell on the
+ * fixed cell -> nl_legacy_count_pairs -> allocate -> nl_legacy_fill_pairs. */
+
+/* Workspace the cell fix needs (any larger workspace works). */
+#define NL_LEGACY_FIX_WORKSPACE_BYTES 256
+
+/* Replaces _fix_cell_ (cell_list.jl:459-505): d_X_fixed (nat x 3, may equal
+ * d_X) receives the positions with periodic fractional coordinates outside
+ * [0, 1) wrapped by mod(., 1) and, when an open axis has atoms outside the
+ * cell, every position shifted by -cell' * min_lambda; cell_fixed (host)
+ * receives the cell, with the rows of such open axes enlarged.
+ * Synchronises the stream (the new cell depends on the positions). */
+int nl_legacy_fix_cell(const double* d_X, int64_t nat, const double cell[9], const uint8_t pbc[3], double* d_X_fixed,
+                       double cell_fixed[9], void* d_workspace, size_t workspace_bytes, void* stream);
+
+/* Device workspace of the legacy count / fill calls (it holds the legacy
+ * cell list: the reference's legacy PairList does not return one). */
+size_t nl_legacy_workspace_bytes(int64_t nat, int64_t ncells_total, int index_bytes);
+
+/* Replaces _celllist_ + _pairlist_(clist) + get_first (cell_list.jl:185-297,
+ * 401-418): bins the atoms (d_X: the positions the list refers to, after
+ * the cell fix if any), counts each atom's pairs with the legacy arithmetic
+ * and writes d_first[nat+1].  cell / inv_cell / ncells / nxyz are
+ * nl_analyze_cell's results for that cell.  If total_pairs is non-NULL the
+ * call synchronises and stores the pair count. */
+int nl_legacy_count_pairs(const double* d_X, int64_t nat, const double cell[9], const double inv_cell[9],
+                          const int64_t ncells[3], const int64_t nxyz[3], const uint8_t pbc[3], double cutoff,
+                          int index_bytes, void* d_first, int64_t* total_pairs, void* d_workspace,
+                          size_t workspace_bytes, void* stream);
+
+/* Writes d_i, d_j [capacity] and d_S [capacity*3]: every atom's pairs sorted
+ * by j as sort_neigs! leaves them (cell_list.jl:427-446).  Requires the
+ * preceding nl_legacy_count_pairs in the same workspace.  Asynchronous;
+ * pairs beyond capacity are not written (NL_ERR_CAPACITY at the next
+ * nl_sync_status). */
+int nl_legacy_fill_pairs(int64_t nat, const double cell[9], const double inv_cell[9], const int64_t ncells[3],
+                         const int64_t nxyz[3], const uint8_t pbc[3], double cutoff, int index_bytes,
+                         const void* d_first, int64_t capacity, void* d_i, void* d_j, void* d_S, void* d_workspace,
+                         size_t workspace_bytes, void* stream);
+
 /* ---- launch tuning ------------------------------------------------------
  * Grid sizes of the pair kernels, as picked by an autotuner (the Python
  * package's autotune()).  0 keeps the default (every resident block slot of

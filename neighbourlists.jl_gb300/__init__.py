@@ -12,6 +12,7 @@ from .api import (  # noqa: F401
     cutoff,
     for_each_neighbour,
     lazy_reduce,
+    legacy_pairlist,
     materialize_pairlist,
     max_neighbours,
     maxneigs,

@@ -22,6 +22,8 @@ NL_ERR_CAPACITY = 7
 NL_ERR_INDEX_OVERFLOW = 8
 NL_ERR_INCONSISTENT = 9
 
+NL_LEGACY_FIX_WORKSPACE_BYTES = 256
+
 NL_REDUCE_COUNT = 0
 NL_REDUCE_INV_R6 = 1
 
@@ -46,6 +48,10 @@ EXPORTED = [
     "nl_batch_sizes",
     "nl_batch_upload",
     "nl_batch_neighbour_list",
+    "nl_legacy_fix_cell",
+    "nl_legacy_workspace_bytes",
+    "nl_legacy_count_pairs",
+    "nl_legacy_fill_pairs",
     "nl_set_tuning",
     "nl_batch_set_tuning",
     "nl_sync_status",
@@ -143,6 +149,16 @@ def _declare(L):
     L.nl_batch_neighbour_list.argtypes = [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int64, _vp, _vp, _vp, _vp, _I64,
                                           _vp, C.c_size_t, _vp]
     L.nl_batch_neighbour_list.restype = C.c_int
+    L.nl_legacy_fix_cell.argtypes = [_vp, C.c_int64, _D, _U8, _vp, _D, _vp, C.c_size_t, _vp]
+    L.nl_legacy_fix_cell.restype = C.c_int
+    L.nl_legacy_workspace_bytes.argtypes = [C.c_int64, C.c_int64, C.c_int]
+    L.nl_legacy_workspace_bytes.restype = C.c_size_t
+    L.nl_legacy_count_pairs.argtypes = [_vp, C.c_int64, _D, _D, _I64, _I64, _U8, C.c_double, C.c_int, _vp, _I64, _vp,
+                                        C.c_size_t, _vp]
+    L.nl_legacy_count_pairs.restype = C.c_int
+    L.nl_legacy_fill_pairs.argtypes = [C.c_int64, _D, _D, _I64, _I64, _U8, C.c_double, C.c_int, _vp, C.c_int64, _vp,
+                                       _vp, _vp, _vp, C.c_size_t, _vp]
+    L.nl_legacy_fill_pairs.restype = C.c_int
     L.nl_set_tuning.argtypes = [C.POINTER(Tuning)]
     L.nl_set_tuning.restype = C.c_int
     L.nl_batch_set_tuning.argtypes = [_vp, C.POINTER(Tuning)]

@@ -36,7 +36,7 @@ __all__ = [
     "SortedCellList", "PairList", "NLError", "analyze_cell", "build_cell_list", "materialize_pairlist",
     "neighbour_list", "npairs", "nsites", "nneigs", "maxneigs", "max_neighbours", "neigs", "neigss", "neighbours",
     "num_neighbours", "count_neighbours", "for_each_neighbour", "lazy_reduce", "cutoff", "pairs", "sites",
-    "PairIterator", "SiteIterator", "pair_vectors",
+    "PairIterator", "SiteIterator", "pair_vectors", "legacy_pairlist",
 ]
 
 _D = C.POINTER(C.c_double)
@@ -259,6 +259,65 @@ def neighbour_list(X, cutoff: float, cell, pbc, lazy: bool = False, int_type=tor
     if lazy:
         return clist
     return materialize_pairlist(clist, with_R=with_R, stream=stream)
+
+
+def legacy_pairlist(X, cutoff: float, cell, pbc, int_type=torch.int32, fixcell: bool = True, with_R: bool = False,
+                    stream=None) -> PairList:
+    """The reference's legacy linked-list constructor
+    PairList(X::Vector{SVec}, cutoff, cell, pbc; int_type, fixcell)
+    (cell_list.jl:11-20, 369-385), on the GPU.
+
+    With ``fixcell`` the positions are first moved into the cell and the cell
+    enlarged along open axes as _fix_cell_ does (:459-505); the returned
+    PairList refers to those positions (``X``) and that cell (``C``), like the
+    reference's.  i, j, S and first equal the reference's legacy list: its own
+    distance arithmetic and shift formula, each atom's neighbours sorted by j.
+    ``with_R`` adds R = X[j] - X[i] + C'S (_getR) for the returned X and C."""
+    ib = _index_bytes(int_type)
+    ti = _tdtype(ib)
+    Xd = _device_positions(X)
+    nat = int(Xd.shape[0])
+    dev = Xd.device
+    pb = _pbc(pbc)
+    sh = _stream_handle(stream)
+    cm = _colmajor(cell)
+    with torch.cuda.device(dev):
+        if fixcell:
+            Xf = torch.empty_like(Xd)
+            cfix = np.zeros(9)
+            scratch = torch.empty(_lib.NL_LEGACY_FIX_WORKSPACE_BYTES, dtype=torch.uint8, device=dev)
+            check(lib().nl_legacy_fix_cell(_ptr(Xd), nat, cm.ctypes.data_as(_D), pb.ctypes.data_as(_U8), _ptr(Xf),
+                                           cfix.ctypes.data_as(_D), _ptr(scratch), scratch.numel(), sh))
+            cellm = cfix.reshape(3, 3).T.copy()
+        else:
+            Xf = Xd
+            cellm = np.asarray(cell, dtype=np.float64).reshape(3, 3).copy()
+        plan = analyze_cell(cellm, cutoff, int_type)
+        nbytes = int(lib().nl_legacy_workspace_bytes(nat, plan.ncells_total, ib))
+        if nbytes == 0:
+            raise NLError(_lib.NL_ERR_ARG, "invalid workspace size")
+        ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        first = torch.empty(nat + 1, dtype=ti, device=dev)
+        total = C.c_int64(0)
+        args = (plan.cell_cm.ctypes.data_as(_D), plan.inv_cm.ctypes.data_as(_D), plan.ncells.ctypes.data_as(_I64),
+                plan.nxyz.ctypes.data_as(_I64), pb.ctypes.data_as(_U8), float(cutoff), ib)
+        check(lib().nl_legacy_count_pairs(_ptr(Xf), nat, *args, C.c_void_p(first.data_ptr()), C.byref(total),
+                                          _ptr(ws), ws.numel(), sh))
+        rechecks = C.c_int64(0)
+        check(lib().nl_last_recheck_count(_ptr(ws), sh, C.byref(rechecks)))
+        P = int(total.value)
+        i = torch.empty(P, dtype=ti, device=dev)
+        j = torch.empty(P, dtype=ti, device=dev)
+        S = torch.empty((P, 3), dtype=ti, device=dev)
+        if P > 0:
+            check(lib().nl_legacy_fill_pairs(nat, *args, C.c_void_p(first.data_ptr()), P, _ptr(i), _ptr(j), _ptr(S),
+                                             _ptr(ws), ws.numel(), sh))
+            check(lib().nl_sync_status(_ptr(ws), sh))
+        R = None
+        if with_R:
+            R = pair_vectors(Xf, cellm, i, j, S, stream=stream) if P > 0 else torch.empty((0, 3), dtype=torch.float64,
+                                                                                          device=dev)
+    return PairList(Xf, cellm, float(cutoff), i, j, S, first, R, int(rechecks.value))
 
 
 def lazy_reduce(clist: SortedCellList, op: str = "count", stream=None, out: Optional[torch.Tensor] = None,

@@ -19,6 +19,7 @@
 #include "nl_api_internal.h"
 #include "nl_build.cuh"
 #include "nl_common.cuh"
+#include "nl_legacy.cuh"
 #include "nl_pairs.cuh"
 #include "nlgpu.h"
 
@@ -449,6 +450,135 @@ int fill_impl(const nl::Geometry& g, const double* Xs, const TI* perm, const TI*
   nl::launch_pairs<TI>(nl::kModeFill, a, num_sms(), st);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? NL_OK : cuda_fail(e, "launch fill kernel");
+}
+
+// ------------------------------------------------- legacy linked-list path --
+// The legacy path keeps its own cell list in the workspace (the reference's
+// legacy PairList does not expose it), after the sort-based layout's
+// list-free part, followed by the per-slot legacy records.
+struct LegacyLayout {
+  Layout L;
+  size_t perm, Xs, cell_id, cell_offsets, D, Df, c0, end;
+};
+
+LegacyLayout legacy_layout(int64_t nat, int64_t ncells, int index_bytes) {
+  LegacyLayout Q;
+  Q.L = layout(nat, ncells);
+  Q.L.use_lists = false;
+  const size_t n = size_t(nat > 0 ? nat : 1), ib = size_t(index_bytes);
+  size_t o = Q.L.base_end;
+  Q.perm = o;
+  o += up(ib * n);
+  Q.Xs = o;
+  o += up(3 * sizeof(double) * n);
+  Q.cell_id = o;
+  o += up(ib * n);
+  Q.cell_offsets = o;
+  o += up(ib * size_t(ncells + 1));
+  Q.D = o;
+  o += up(3 * sizeof(double) * n);
+  Q.Df = o;
+  o += up(sizeof(float4) * n);
+  Q.c0 = o;
+  o += up(sizeof(int4) * n);
+  Q.end = o;
+  return Q;
+}
+
+// bins = hcat(C[1,:]/n1, C[2,:]/n2, C[3,:]/n3) (cell_list.jl:258): column k is
+// row k of the cell divided by ns[k]
+nl::LegacyGeo legacy_geo(const double* cell, const double* inv, const int64_t* ns, const int64_t* nxyz,
+                         const uint8_t* pbc, double cutoff, int64_t nat) {
+  nl::LegacyGeo g;
+  std::memset(&g, 0, sizeof(g));
+  std::memcpy(g.inv, inv, sizeof(g.inv));
+  double offmax = 0;
+  for (int k = 0; k < 3; ++k)
+    for (int r = 0; r < 3; ++r) g.bins[r + 3 * k] = cell[k + 3 * r] / double(ns[k]);
+  for (int r = 0; r < 3; ++r) {
+    double m = 0;
+    for (int k = 0; k < 3; ++k) m += std::fabs(g.bins[r + 3 * k]) * double(nxyz[k]);
+    offmax = m > offmax ? m : offmax;
+  }
+  g.offmax = offmax * (1.0 + 1e-12);
+  g.cutoff = cutoff;
+  g.cutoff_sq = cutoff * cutoff;  // clist.cutoff^2 (:305)
+  for (int k = 0; k < 3; ++k) {
+    g.ns[k] = int(ns[k]);
+    g.nxyz[k] = int(nxyz[k]);
+    g.pbc[k] = pbc[k] ? 1 : 0;
+  }
+  g.ncells = int(ns[0] * ns[1] * ns[2]);
+  g.nat = int(nat);
+  return g;
+}
+
+template <typename TI>
+nl::LegacyArgs<TI> legacy_args(const nl::LegacyGeo& lg, void* ws, const LegacyLayout& Q) {
+  nl::LegacyArgs<TI> a;
+  std::memset(&a, 0, sizeof(a));
+  a.g = lg;
+  a.Xs = at<double>(ws, Q.Xs);
+  a.perm = at<TI>(ws, Q.perm);
+  a.cell_start = at<int>(ws, Q.L.cell_start);
+  a.D = at<double>(ws, Q.D);
+  a.Df = at<float4>(ws, Q.Df);
+  a.c0 = at<int4>(ws, Q.c0);
+  a.dmax = at<unsigned>(ws, Q.L.pcount) + 8;  // zeroed with the build's region
+  a.counts = at<int>(ws, Q.L.counts);
+  a.blocks_per_sm = g_tuning.pair_blocks_per_sm;
+  a.stats = at<unsigned long long>(ws, Q.L.stats);
+  a.err = at<unsigned>(ws, Q.L.err);
+  return a;
+}
+
+// build (the legacy cell list) + per-slot records + count + pair offsets
+template <typename TI>
+int legacy_count_impl(const double* X, int64_t nat, const nl::Geometry& g, const nl::LegacyGeo& lg, TI* first,
+                      void* ws, const LegacyLayout& Q, cudaStream_t st) {
+  int s = build_impl<TI>(X, nat, g, at<TI>(ws, Q.perm), at<double>(ws, Q.Xs), at<TI>(ws, Q.cell_id),
+                         at<TI>(ws, Q.cell_offsets), ws, Q.L, st);
+  if (s) return s;
+  if (nat == 0) {  // first = [1] (get_first of an empty list, :416)
+    static const TI one = 1;
+    cudaError_t e = cudaMemcpyAsync(first, &one, sizeof(TI), cudaMemcpyHostToDevice, st);
+    return e == cudaSuccess ? NL_OK : cuda_fail(e, "empty system");
+  }
+  const int sms = num_sms();
+  nl::LegacyArgs<TI> a = legacy_args<TI>(lg, ws, Q);
+  nl::launch_legacy_prepare<TI>(a, sms, st);
+  nl::launch_legacy_pairs<TI>(false, a, sms, st);
+  nl::launch_scan<TI>(a.counts, nat, first, nullptr, at<unsigned long long>(ws, Q.L.st_pairs), at<int>(ws, Q.L.pcount),
+                      at<long long>(ws, Q.L.totals) + 1, a.err, st);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? NL_OK : cuda_fail(e, "launch legacy count kernels");
+}
+
+template <typename TI>
+int legacy_fill_impl(const nl::LegacyGeo& lg, const TI* first, int64_t capacity, TI* oi, TI* oj, TI* oS, void* ws,
+                     const LegacyLayout& Q, cudaStream_t st) {
+  if (lg.nat == 0 || capacity <= 0) return NL_OK;
+  nl::LegacyArgs<TI> a = legacy_args<TI>(lg, ws, Q);
+  a.first = first;
+  a.oi = oi;
+  a.oj = oj;
+  a.oS = oS;
+  a.capacity = capacity;
+  nl::launch_legacy_pairs<TI>(true, a, num_sms(), st);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? NL_OK : cuda_fail(e, "launch legacy fill kernel");
+}
+
+int legacy_check(int64_t nat, const int64_t* ncells, const int64_t* nxyz, int index_bytes, void* ws, size_t ws_bytes,
+                 LegacyLayout& Q) {
+  Layout L;
+  int64_t nct;
+  int s = check_common(nat, ncells, nxyz, index_bytes, ws, ws_bytes, L, nct);
+  if (s == NL_ERR_NOMEM) return fail(NL_ERR_NOMEM, "workspace too small (see nl_legacy_workspace_bytes)");
+  if (s) return s;
+  Q = legacy_layout(nat, nct, index_bytes);
+  if (!ws || ws_bytes < Q.end) return fail(NL_ERR_NOMEM, "workspace too small (see nl_legacy_workspace_bytes)");
+  return NL_OK;
 }
 
 // --------------------------------------------------------------- batches --
@@ -989,6 +1119,118 @@ int nl_max_displacement_sq(const double* d_X, const double* d_Xref, int64_t nat,
   nl::launch_max_disp_sq(d_X, d_Xref, nat, reinterpret_cast<unsigned long long*>(d_out), num_sms(), st);
   e = cudaGetLastError();
   return e == cudaSuccess ? NL_OK : cuda_fail(e, "launch max displacement");
+}
+
+size_t nl_legacy_workspace_bytes(int64_t nat, int64_t ncells_total, int index_bytes) {
+  if (nat < 0 || ncells_total < 1 || (index_bytes != 4 && index_bytes != 8)) return 0;
+  return legacy_layout(nat, ncells_total, index_bytes).end;
+}
+
+int nl_legacy_fix_cell(const double* d_X, int64_t nat, const double cell[9], const uint8_t pbc[3], double* d_X_fixed,
+                       double cell_fixed[9], void* d_workspace, size_t workspace_bytes, void* stream) {
+  if (!cell || !pbc || !cell_fixed || !d_workspace) return fail(NL_ERR_ARG, "null argument");
+  if (nat < 0 || nat > 2147483646LL) return fail(NL_ERR_ARG, "nat must be in [0, 2^31-2]");
+  if (nat > 0 && (!d_X || !d_X_fixed)) return fail(NL_ERR_ARG, "null argument");
+  if (workspace_bytes < NL_LEGACY_FIX_WORKSPACE_BYTES) return fail(NL_ERR_NOMEM, "workspace too small for the cell fix");
+  double C[9];
+  std::memcpy(C, cell, sizeof(C));
+  std::memcpy(cell_fixed, C, sizeof(C));
+  if (nat == 0) return NL_OK;  // no atom moves, the cell stays
+  double inv[9];
+  sa_inv(C, inv);  // invCt = inv(C)' (:460)
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // error word at 0; open-axis extremes at 64: min from 0.0, max from 1.0 (:462-463)
+  unsigned long long init[6];
+  for (int k = 0; k < 3; ++k) {
+    init[k] = nl::legacy_key(0.0);
+    init[3 + k] = nl::legacy_key(1.0);
+  }
+  cudaError_t e = cudaMemsetAsync(d_workspace, 0, 64, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(at<char>(d_workspace, 64), init, sizeof(init), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return cuda_fail(e, "initialise cell fix");
+  const int pb[3] = {pbc[0] ? 1 : 0, pbc[1] ? 1 : 0, pbc[2] ? 1 : 0};
+  nl::launch_legacy_fix(inv, C, pb, d_X, d_X_fixed, int(nat), at<unsigned long long>(d_workspace, 64),
+                        at<unsigned>(d_workspace, 0), num_sms(), st);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "launch cell fix");
+  long long* h = pinned_scratch();
+  if (!h) return fail(NL_ERR_NOMEM, "cannot allocate pinned host scratch");
+  e = cudaMemcpyAsync(h, d_workspace, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h + 1, at<char>(d_workspace, 64), 6 * sizeof(long long), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "read cell fix");
+  if (int s = status_from_flags(*reinterpret_cast<unsigned*>(h))) return s;
+  double min_lam[3], max_lam[3];
+  for (int k = 0; k < 3; ++k) {
+    min_lam[k] = nl::legacy_unkey((unsigned long long)h[1 + k]);
+    max_lam[k] = nl::legacy_unkey((unsigned long long)h[4 + k]);
+  }
+  const double mn = std::fmin(std::fmin(min_lam[0], min_lam[1]), min_lam[2]);
+  const double mx = std::fmax(std::fmax(max_lam[0], max_lam[1]), max_lam[2]);
+  if (mn < 0.0 || mx > 1.0) {  // :488-503
+    // t = -C' * min_lam, parsed as (-C') * min_lam
+    double t[3];
+    for (int k = 0; k < 3; ++k)
+      t[k] = ((-C[3 * k + 0]) * min_lam[0] + (-C[3 * k + 1]) * min_lam[1]) + (-C[3 * k + 2]) * min_lam[2];
+    nl::launch_legacy_shift(d_X_fixed, int(nat), t, num_sms(), st);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "launch cell fix shift");
+    for (int k = 0; k < 3; ++k) {
+      max_lam[k] = max_lam[k] - min_lam[k];
+      min_lam[k] = 0.0;
+    }
+    for (int k = 0; k < 3; ++k)
+      if (max_lam[k] > 1) max_lam[k] = max_lam[k] * 1.01;
+    for (int r = 0; r < 3; ++r)  // row r of the new cell = max_lam[r] * row r
+      for (int c = 0; c < 3; ++c) cell_fixed[r + 3 * c] = max_lam[r] * C[r + 3 * c];
+  }
+  return NL_OK;
+}
+
+int nl_legacy_count_pairs(const double* d_X, int64_t nat, const double cell[9], const double inv_cell[9],
+                          const int64_t ncells[3], const int64_t nxyz[3], const uint8_t pbc[3], double cutoff,
+                          int index_bytes, void* d_first, int64_t* total_pairs, void* d_workspace,
+                          size_t workspace_bytes, void* stream) {
+  if (!cell || !inv_cell || !ncells || !nxyz || !pbc || !d_first || (nat > 0 && !d_X))
+    return fail(NL_ERR_ARG, "null argument");
+  if (!(cutoff > 0)) return fail(NL_ERR_ARG, "cutoff must be positive");
+  LegacyLayout Q;
+  int s = legacy_check(nat, ncells, nxyz, index_bytes, d_workspace, workspace_bytes, Q);
+  if (s) return s;
+  const nl::Geometry g = make_geometry(cell, inv_cell, ncells, nullptr, pbc, cutoff, nat);
+  const nl::LegacyGeo lg = legacy_geo(cell, inv_cell, ncells, nxyz, pbc, cutoff, nat);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (index_bytes == 4)
+    s = legacy_count_impl<int32_t>(d_X, nat, g, lg, static_cast<int32_t*>(d_first), d_workspace, Q, st);
+  else
+    s = legacy_count_impl<int64_t>(d_X, nat, g, lg, static_cast<int64_t*>(d_first), d_workspace, Q, st);
+  if (s) return s;
+  if (total_pairs) {
+    if (nat == 0) {
+      *total_pairs = 0;
+      return sync_read(d_workspace, st, nullptr, nullptr);
+    }
+    return sync_read(d_workspace, st, at<long long>(d_workspace, Q.L.totals) + 1, total_pairs);
+  }
+  return NL_OK;
+}
+
+int nl_legacy_fill_pairs(int64_t nat, const double cell[9], const double inv_cell[9], const int64_t ncells[3],
+                         const int64_t nxyz[3], const uint8_t pbc[3], double cutoff, int index_bytes,
+                         const void* d_first, int64_t capacity, void* d_i, void* d_j, void* d_S, void* d_workspace,
+                         size_t workspace_bytes, void* stream) {
+  if (!cell || !inv_cell || !ncells || !nxyz || !pbc || !d_first) return fail(NL_ERR_ARG, "null argument");
+  if (capacity > 0 && (!d_i || !d_j || !d_S)) return fail(NL_ERR_ARG, "null argument");
+  LegacyLayout Q;
+  int s = legacy_check(nat, ncells, nxyz, index_bytes, d_workspace, workspace_bytes, Q);
+  if (s) return s;
+  const nl::LegacyGeo lg = legacy_geo(cell, inv_cell, ncells, nxyz, pbc, cutoff, nat);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (index_bytes == 4)
+    return legacy_fill_impl<int32_t>(lg, static_cast<const int32_t*>(d_first), capacity, static_cast<int32_t*>(d_i),
+                                     static_cast<int32_t*>(d_j), static_cast<int32_t*>(d_S), d_workspace, Q, st);
+  return legacy_fill_impl<int64_t>(lg, static_cast<const int64_t*>(d_first), capacity, static_cast<int64_t*>(d_i),
+                                   static_cast<int64_t*>(d_j), static_cast<int64_t*>(d_S), d_workspace, Q, st);
 }
 
 int nl_sync_status(void* d_workspace, void* stream) {

@@ -183,6 +183,93 @@ def test_screen_band_bounds_fp32_error(nlpkg, orc, case):
     assert worst <= band / 2, (worst, band)
 
 
+# ---------------------------------------------------------- legacy screen --
+def _legacy_band(cell_cm, ns, nxyz, rc, Df):
+    """The legacy kernel's band (nl_legacy.cu): e = 4u(2M + O), B = 2(4u rc^2
+    + 2 sqrt(3)(rc + e) e + 3 e^2), M = max |D| in FP32 rounded up."""
+    u = 2.0 ** -24
+    bins = np.array([[cell_cm[k + 3 * r] / ns[k] for k in range(3)] for r in range(3)])  # bins[r, k]
+    O = max(sum(abs(bins[r, k]) * nxyz[k] for k in range(3)) for r in range(3)) * (1 + 1e-12)
+    M = float(np.max(np.abs(Df))) if Df.size else 0.0
+    e = 4 * u * (2 * M + O) * 1.0001
+    return bins, 2 * (4 * u * rc * rc + 2 * np.sqrt(3) * (rc + e) * e + 3 * e * e)
+
+
+@pytest.mark.parametrize("case", ["cubic", "triclinic", "open_outside"])
+def test_legacy_screen_band_bounds_fp32_error(nlpkg, case):
+    """Every candidate whose FP32 legacy distance lies outside rc^2 -+ B is
+    decided the same way by the reference's FP64 legacy arithmetic
+    (cell_list.jl:346-352), so the FP64 recheck of the band is enough."""
+    rng = np.random.default_rng(9)
+    if case == "cubic":
+        X, cell, _ = cf.rand_config(700, seed=31)
+        pbc, rc = (True, True, True), 5.0
+    elif case == "triclinic":
+        X, cell = cf.rand_config_triclinic(500, seed=32)
+        pbc, rc = (True, False, True), 3.0
+    else:  # fixcell = false: atoms far outside along the open axis
+        X, cell = cf.rand_config_triclinic(500, seed=33)
+        X = X + np.outer(rng.normal(0, 8.0, len(X)), [0.0, 0.0, 1.0])
+        pbc, rc = (True, True, False), 3.0
+    plan = nlpkg.analyze_cell(cell, rc)
+    cm, inv, ns, nxyz = plan.cell_cm, plan.inv_cm, plan.ncells, plan.nxyz
+    f = np.stack([(inv[3 * k] * X[:, 0] + inv[3 * k + 1] * X[:, 1]) + inv[3 * k + 2] * X[:, 2] for k in range(3)], 1)
+    c0 = np.floor(f * ns + 1.0).astype(np.int64)
+    ct = np.stack([c0[:, k] if pbc[k] else np.clip(c0[:, k], 1, ns[k]) for k in range(3)], 1)
+    bins0 = np.array([[cm[k + 3 * r] / ns[k] for k in range(3)] for r in range(3)])
+    v = (ct - 1).astype(np.float64)
+    D = np.stack([X[:, r] - ((bins0[r, 0] * v[:, 0] + bins0[r, 1] * v[:, 1]) + bins0[r, 2] * v[:, 2])
+                  for r in range(3)], 1)
+    Df = D.astype(np.float32)
+    bins, B = _legacy_band(cm, ns, nxyz, rc, np.abs(D).astype(np.float32))
+    worst_ratio = 0.0
+    for x in range(-nxyz[0], nxyz[0] + 1):
+        for y in range(-nxyz[1], nxyz[1] + 1):
+            for z in range(-nxyz[2], nxyz[2] + 1):
+                off = np.array([(bins[r, 0] * x + bins[r, 1] * y) + bins[r, 2] * z for r in range(3)])
+                d64 = (D[None, :, :] - D[:, None, :]) + off
+                r64 = (d64[..., 0] * d64[..., 0] + d64[..., 1] * d64[..., 1]) + d64[..., 2] * d64[..., 2]
+                d32 = (Df[None, :, :] - Df[:, None, :]) + off.astype(np.float32)
+                r32 = (d32[..., 0] * d32[..., 0] + d32[..., 1] * d32[..., 1]) + d32[..., 2] * d32[..., 2]
+                near = r64 < 4 * rc * rc
+                err = np.abs(r32[near].astype(np.float64) - r64[near])
+                if err.size:
+                    worst_ratio = max(worst_ratio, float(err.max()) / B)
+                assert not np.any((r64 < rc * rc) & (r32.astype(np.float64) > rc * rc + B))
+                assert not np.any((r64 >= rc * rc) & (r32.astype(np.float64) < rc * rc - B))
+    assert worst_ratio < 0.5, worst_ratio
+
+
+def test_legacy_argument_errors_before_any_device_work(nlpkg):
+    L = nlpkg.lib()
+    D = C.POINTER(C.c_double)
+    I64 = C.POINTER(C.c_int64)
+    U8 = C.POINTER(C.c_uint8)
+    cell = np.ascontiguousarray(np.diag([10.0, 10.0, 10.0]).T).reshape(9)
+    inv = np.ascontiguousarray(np.diag([0.1, 0.1, 0.1]).T).reshape(9)
+    ns = np.array([3, 3, 3], dtype=np.int64)
+    nx = np.array([1, 1, 1], dtype=np.int64)
+    pbc = np.ones(3, dtype=np.uint8)
+    out = np.zeros(9)
+    assert L.nl_legacy_workspace_bytes(-1, 1, 4) == 0
+    assert L.nl_legacy_workspace_bytes(10, 27, 3) == 0
+    assert L.nl_legacy_workspace_bytes(1000, 27, 8) > L.nl_workspace_min_bytes(1000, 27) + 1000 * 80
+    # null cell / too small workspace for the cell fix
+    assert L.nl_legacy_fix_cell(C.c_void_p(8), 10, None, pbc.ctypes.data_as(U8), C.c_void_p(8),
+                                out.ctypes.data_as(D), C.c_void_p(8), 256, None) == 1
+    assert L.nl_legacy_fix_cell(C.c_void_p(8), 10, cell.ctypes.data_as(D), pbc.ctypes.data_as(U8), C.c_void_p(8),
+                                out.ctypes.data_as(D), C.c_void_p(8), 16, None) == 3
+    # workspace smaller than nl_legacy_workspace_bytes
+    need = L.nl_legacy_workspace_bytes(10, 27, 4)
+    total = C.c_int64(0)
+    assert L.nl_legacy_count_pairs(C.c_void_p(8), 10, cell.ctypes.data_as(D), inv.ctypes.data_as(D),
+                                   ns.ctypes.data_as(I64), nx.ctypes.data_as(I64), pbc.ctypes.data_as(U8), 3.0, 4,
+                                   C.c_void_p(8), C.byref(total), C.c_void_p(8), need - 1, None) == 3
+    assert L.nl_legacy_fill_pairs(10, cell.ctypes.data_as(D), inv.ctypes.data_as(D), ns.ctypes.data_as(I64),
+                                  nx.ctypes.data_as(I64), pbc.ctypes.data_as(U8), 3.0, 4, C.c_void_p(8), 10,
+                                  None, None, None, C.c_void_p(8), need, None) == 1
+
+
 def test_batch_plan_on_host(nlpkg):
     """nl_batch_create validates systems and sizes the workspace without a GPU."""
     import ctypes as C
