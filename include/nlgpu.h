@@ -226,6 +226,49 @@ int nl_batch_neighbour_list(const nl_batch* batch, const double* d_X, void* d_pe
                             int64_t capacity, void* d_i, void* d_j, void* d_S, double* d_R, int64_t* total_pairs,
                             void* d_workspace, size_t workspace_bytes, void* stream);
 
+/* ---- Float32 positions ----------------------------------------------------
+ * The reference is generic in the position type T; with T = Float32 (its GPU
+ * tests run Float64 and Float32, test/test_gpu.jl:14, test/test_utils.jl:239)
+ * build_cell_list converts cell and cutoff to Float32 (cell_list.jl:637-639)
+ * and every floating-point operation -- analyze_cell, position_to_cell_index,
+ * R = xj - xi + C'S, dot(R, R) < cutoff^2 -- rounds to Float32.  These calls
+ * are the Float64 calls above with that arithmetic: positions (nat x 3), the
+ * cell and cutoff and R (npairs x 3) are float; the index arrays and the
+ * workspace (nl_workspace_bytes) are unchanged.  Positions whose winding
+ * exceeds 511 box lengths cannot be binned (NL_ERR_BAD_POSITION). */
+typedef struct nl_cell_plan_f32 {
+  float inv_cell[9];    /* inv(cell) in Float32, column-major */
+  float lens[3];        /* abs.(lengths(cell)) in Float32 */
+  int64_t ncells[3];
+  int64_t nxyz[3];
+  int64_t ncells_total;
+} nl_cell_plan_f32;
+
+/* analyze_cell (cell_list.jl:152-170) + nxyz (gpu_kernels.jl:315-316) in Float32. */
+int nl_analyze_cell_f32(const float cell[9], float cutoff, int index_bytes, nl_cell_plan_f32* plan);
+/* nl_build_cell_list for Float32 positions. */
+int nl_build_cell_list_f32(const float* d_X, int64_t nat, const float cell[9], const float inv_cell[9],
+                           const int64_t ncells[3], const uint8_t pbc[3], float cutoff, int index_bytes, void* d_perm,
+                           float* d_X_sorted, void* d_cell_id, void* d_cell_offsets, void* d_workspace,
+                           size_t workspace_bytes, void* stream);
+/* nl_count_pairs for Float32 positions. */
+int nl_count_pairs_f32(const float* d_X_sorted, const void* d_perm, const void* d_cell_id, const void* d_cell_offsets,
+                       int64_t nat, const float cell[9], const float inv_cell[9], const int64_t ncells[3],
+                       const int64_t nxyz[3], const uint8_t pbc[3], float cutoff, int index_bytes, int reuse_records,
+                       void* d_first, int64_t* total_pairs, void* d_workspace, size_t workspace_bytes, void* stream);
+/* nl_fill_pairs for Float32 positions (d_R: capacity x 3 floats, may be NULL). */
+int nl_fill_pairs_f32(const float* d_X_sorted, const void* d_perm, const void* d_cell_offsets, int64_t nat,
+                      const float cell[9], const float inv_cell[9], const int64_t ncells[3], const int64_t nxyz[3],
+                      const uint8_t pbc[3], float cutoff, int index_bytes, const void* d_first, int64_t capacity,
+                      void* d_i, void* d_j, void* d_S, float* d_R, void* d_workspace, size_t workspace_bytes,
+                      void* stream);
+/* nl_neighbour_list for Float32 positions. */
+int nl_neighbour_list_f32(const float* d_X, int64_t nat, const float cell[9], const float inv_cell[9],
+                          const int64_t ncells[3], const int64_t nxyz[3], const uint8_t pbc[3], float cutoff,
+                          int index_bytes, void* d_perm, float* d_X_sorted, void* d_cell_id, void* d_cell_offsets,
+                          void* d_first, int64_t capacity, void* d_i, void* d_j, void* d_S, float* d_R,
+                          int64_t* total_pairs, void* d_workspace, size_t workspace_bytes, void* stream);
+
 /* ---- legacy linked-list PairList -----------------------------------------
  * The reference's legacy constructor PairList(X::Vector{SVec}, cutoff, cell,
  * pbc; int_type, fixcell) (cell_list.jl:11-20, _pairlist_ :369-385), kept

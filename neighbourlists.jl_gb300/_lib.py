@@ -48,6 +48,11 @@ EXPORTED = [
     "nl_batch_sizes",
     "nl_batch_upload",
     "nl_batch_neighbour_list",
+    "nl_analyze_cell_f32",
+    "nl_build_cell_list_f32",
+    "nl_count_pairs_f32",
+    "nl_fill_pairs_f32",
+    "nl_neighbour_list_f32",
     "nl_legacy_fix_cell",
     "nl_legacy_workspace_bytes",
     "nl_legacy_count_pairs",
@@ -70,6 +75,16 @@ class CellPlan(C.Structure):
         ("nxyz", C.c_int64 * 3),
         ("ncells_total", C.c_int64),
         ("band", C.c_double),
+    ]
+
+
+class CellPlanF32(C.Structure):
+    _fields_ = [
+        ("inv_cell", C.c_float * 9),
+        ("lens", C.c_float * 3),
+        ("ncells", C.c_int64 * 3),
+        ("nxyz", C.c_int64 * 3),
+        ("ncells_total", C.c_int64),
     ]
 
 
@@ -149,6 +164,21 @@ def _declare(L):
     L.nl_batch_neighbour_list.argtypes = [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int64, _vp, _vp, _vp, _vp, _I64,
                                           _vp, C.c_size_t, _vp]
     L.nl_batch_neighbour_list.restype = C.c_int
+    _F = C.POINTER(C.c_float)
+    L.nl_analyze_cell_f32.argtypes = [_F, C.c_float, C.c_int, C.POINTER(CellPlanF32)]
+    L.nl_analyze_cell_f32.restype = C.c_int
+    L.nl_build_cell_list_f32.argtypes = [_vp, C.c_int64, _F, _F, _I64, _U8, C.c_float, C.c_int, _vp, _vp, _vp, _vp,
+                                         _vp, C.c_size_t, _vp]
+    L.nl_build_cell_list_f32.restype = C.c_int
+    L.nl_count_pairs_f32.argtypes = [_vp, _vp, _vp, _vp, C.c_int64, _F, _F, _I64, _I64, _U8, C.c_float, C.c_int,
+                                     C.c_int, _vp, _I64, _vp, C.c_size_t, _vp]
+    L.nl_count_pairs_f32.restype = C.c_int
+    L.nl_fill_pairs_f32.argtypes = [_vp, _vp, _vp, C.c_int64, _F, _F, _I64, _I64, _U8, C.c_float, C.c_int, _vp,
+                                    C.c_int64, _vp, _vp, _vp, _vp, _vp, C.c_size_t, _vp]
+    L.nl_fill_pairs_f32.restype = C.c_int
+    L.nl_neighbour_list_f32.argtypes = [_vp, C.c_int64, _F, _F, _I64, _I64, _U8, C.c_float, C.c_int, _vp, _vp, _vp,
+                                        _vp, _vp, C.c_int64, _vp, _vp, _vp, _vp, _I64, _vp, C.c_size_t, _vp]
+    L.nl_neighbour_list_f32.restype = C.c_int
     L.nl_legacy_fix_cell.argtypes = [_vp, C.c_int64, _D, _U8, _vp, _D, _vp, C.c_size_t, _vp]
     L.nl_legacy_fix_cell.restype = C.c_int
     L.nl_legacy_workspace_bytes.argtypes = [C.c_int64, C.c_int64, C.c_int]

@@ -40,6 +40,7 @@ __all__ = [
 ]
 
 _D = C.POINTER(C.c_double)
+_F = C.POINTER(C.c_float)
 _I64 = C.POINTER(C.c_int64)
 _U8 = C.POINTER(C.c_uint8)
 
@@ -80,14 +81,17 @@ def _stream_handle(stream=None):
     return C.c_void_p(s.cuda_stream)
 
 
-def _device_positions(X) -> torch.Tensor:
-    """(N,3) float64 contiguous CUDA tensor; host arrays are copied to the GPU."""
+def _device_positions(X, f32_ok: bool = False) -> torch.Tensor:
+    """(N,3) float64 contiguous CUDA tensor -- or float32 where the call has a
+    single-precision path (f32_ok); host arrays are copied to the GPU."""
     if isinstance(X, torch.Tensor):
         t = X
     else:
-        t = torch.from_numpy(np.ascontiguousarray(np.asarray(X, dtype=np.float64).reshape(-1, 3)))
-    if t.dtype != torch.float64:
-        raise TypeError("positions must be Float64 (float64)")
+        a = np.asarray(X)
+        dt = np.float32 if (f32_ok and a.dtype == np.float32) else np.float64
+        t = torch.from_numpy(np.ascontiguousarray(a.astype(dt, copy=False).reshape(-1, 3)))
+    if t.dtype != torch.float64 and not (f32_ok and t.dtype == torch.float32):
+        raise TypeError("positions must be Float64 (float64)" + (" or Float32 (float32)" if f32_ok else ""))
     t = t.reshape(-1, 3)
     if not t.is_cuda:
         t = t.to("cuda", non_blocking=False)
@@ -110,9 +114,20 @@ class CellPlan:
         return self.inv_cm.reshape(3, 3).T.copy()
 
 
-def analyze_cell(cell, cutoff: float, int_type=torch.int32) -> CellPlan:
-    plan = _lib.CellPlan()
+def analyze_cell(cell, cutoff: float, int_type=torch.int32, float32: bool = False) -> CellPlan:
+    """``float32=True``: the analysis with T = Float32 -- cell and cutoff
+    converted to Float32 as build_cell_list does (cell_list.jl:637-639), every
+    operation in single precision; the plan's arrays are then float32."""
     cm = _colmajor(cell)
+    if float32:
+        plan32 = _lib.CellPlanF32()
+        cm32 = cm.astype(np.float32)
+        check(lib().nl_analyze_cell_f32(cm32.ctypes.data_as(_F), np.float32(cutoff).item(), _index_bytes(int_type),
+                                        C.byref(plan32)))
+        return CellPlan(cm32, np.array(plan32.inv_cell[:], dtype=np.float32), np.array(plan32.lens[:], dtype=np.float32),
+                        np.array(plan32.ncells[:], dtype=np.int64), np.array(plan32.nxyz[:], dtype=np.int64),
+                        int(plan32.ncells_total), 0.0)
+    plan = _lib.CellPlan()
     check(lib().nl_analyze_cell(cm.ctypes.data_as(_D), float(cutoff), _index_bytes(int_type), C.byref(plan)))
     return CellPlan(cm, np.array(plan.inv_cell[:]), np.array(plan.lens[:]), np.array(plan.ncells[:], dtype=np.int64),
                     np.array(plan.nxyz[:], dtype=np.int64), int(plan.ncells_total), float(plan.band))
@@ -167,8 +182,13 @@ class PairList:
 # --------------------------------------------------------------- building --
 def _plan_args(clist: SortedCellList):
     p = clist._plan
-    return (p.cell_cm.ctypes.data_as(_D), p.inv_cm.ctypes.data_as(_D), p.ncells.ctypes.data_as(_I64),
+    fp = _F if p.cell_cm.dtype == np.float32 else _D
+    return (p.cell_cm.ctypes.data_as(fp), p.inv_cm.ctypes.data_as(fp), p.ncells.ctypes.data_as(_I64),
             p.nxyz.ctypes.data_as(_I64))
+
+
+def _is_f32(clist: SortedCellList) -> bool:
+    return clist.X.dtype == torch.float32
 
 
 def _new_workspace(nat: int, ncells_total: int, device) -> torch.Tensor:
@@ -179,27 +199,38 @@ def _new_workspace(nat: int, ncells_total: int, device) -> torch.Tensor:
 
 
 def build_cell_list(X, cutoff: float, cell, pbc, int_type=torch.int32, stream=None) -> SortedCellList:
-    """build_cell_list(X, cutoff, cell, pbc; int_type) (cell_list.jl:632-679)."""
+    """build_cell_list(X, cutoff, cell, pbc; int_type) (cell_list.jl:632-679).
+    Float32 positions take the single-precision path (the reference with
+    T = Float32: cell and cutoff converted to Float32, every operation in
+    single precision)."""
     ib = _index_bytes(int_type)
-    Xd = _device_positions(X)
+    Xd = _device_positions(X, f32_ok=True)
+    f32 = Xd.dtype == torch.float32
     nat = int(Xd.shape[0])
-    plan = analyze_cell(cell, cutoff, int_type)
+    plan = analyze_cell(cell, cutoff, int_type, float32=f32)
     dev = Xd.device
     ti = _tdtype(ib)
     perm = torch.empty(nat, dtype=ti, device=dev)
-    Xs = torch.empty((nat, 3), dtype=torch.float64, device=dev)
+    Xs = torch.empty((nat, 3), dtype=Xd.dtype, device=dev)
     cid = torch.empty(nat, dtype=ti, device=dev)
     offs = torch.empty(plan.ncells_total + 1, dtype=ti, device=dev)
     ws = _new_workspace(nat, plan.ncells_total, dev)
     pb = _pbc(pbc)
+    rc = np.float32(cutoff).item() if f32 else float(cutoff)
     with torch.cuda.device(dev):
-        check(lib().nl_build_cell_list(_ptr(Xd), nat, plan.cell_cm.ctypes.data_as(_D), plan.inv_cm.ctypes.data_as(_D),
-                                       plan.ncells.ctypes.data_as(_I64), pb.ctypes.data_as(_U8), float(cutoff), ib,
-                                       _ptr(perm), _ptr(Xs), _ptr(cid), C.c_void_p(offs.data_ptr()), _ptr(ws),
-                                       ws.numel(), _stream_handle(stream)))
+        if f32:
+            check(lib().nl_build_cell_list_f32(_ptr(Xd), nat, plan.cell_cm.ctypes.data_as(_F),
+                                               plan.inv_cm.ctypes.data_as(_F), plan.ncells.ctypes.data_as(_I64),
+                                               pb.ctypes.data_as(_U8), rc, ib, _ptr(perm), _ptr(Xs), _ptr(cid),
+                                               C.c_void_p(offs.data_ptr()), _ptr(ws), ws.numel(), _stream_handle(stream)))
+        else:
+            check(lib().nl_build_cell_list(_ptr(Xd), nat, plan.cell_cm.ctypes.data_as(_D),
+                                           plan.inv_cm.ctypes.data_as(_D), plan.ncells.ctypes.data_as(_I64),
+                                           pb.ctypes.data_as(_U8), rc, ib, _ptr(perm), _ptr(Xs), _ptr(cid),
+                                           C.c_void_p(offs.data_ptr()), _ptr(ws), ws.numel(), _stream_handle(stream)))
         check(lib().nl_sync_status(_ptr(ws), _stream_handle(stream)))
-    cellm = np.asarray(cell, dtype=np.float64).reshape(3, 3).copy()
-    return SortedCellList(Xs, Xd, perm, cid, offs, cellm, plan.inv_cell, tuple(bool(b) for b in pb), float(cutoff),
+    cellm = np.asarray(cell, dtype=np.float64).reshape(3, 3).astype(np.float32 if f32 else np.float64)
+    return SortedCellList(Xs, Xd, perm, cid, offs, cellm, plan.inv_cell, tuple(bool(b) for b in pb), rc,
                           plan.ncells.copy(), plan.ncells_total, plan, ws, True)
 
 
@@ -218,6 +249,8 @@ def materialize_pairlist(clist: SortedCellList, with_R: bool = True, stream=None
     first = torch.empty(nat + 1, dtype=ti, device=dev)
     total = C.c_int64(0)
     sh = _stream_handle(stream)
+    if _is_f32(clist):
+        return _materialize_f32(clist, with_R, ws, pb, (cm, im, nc, nx), first, sh)
     with torch.cuda.device(dev):
         check(lib().nl_count_pairs(_ptr(clist.X), _ptr(clist.perm), _ptr(clist.cell_id),
                                    C.c_void_p(clist.cell_offsets.data_ptr()), nat, cm, im, nc, nx,
@@ -238,6 +271,33 @@ def materialize_pairlist(clist: SortedCellList, with_R: bool = True, stream=None
                                       ws.numel(), sh))
             check(lib().nl_sync_status(_ptr(ws), sh))
     return PairList(clist.X_orig, clist.cell.copy(), clist.cutoff, i, j, S, first, R, int(rechecks.value))
+
+
+def _materialize_f32(clist: SortedCellList, with_R: bool, ws, pb, plan_args, first, sh) -> PairList:
+    """materialize_pairlist with T = Float32: i, j, S, first and R (float32)."""
+    nat = int(clist.X_orig.shape[0])
+    ib = clist.index_bytes
+    dev = clist.X_orig.device
+    ti = _tdtype(ib)
+    total = C.c_int64(0)
+    with torch.cuda.device(dev):
+        check(lib().nl_count_pairs_f32(_ptr(clist.X), _ptr(clist.perm), _ptr(clist.cell_id),
+                                       C.c_void_p(clist.cell_offsets.data_ptr()), nat, *plan_args,
+                                       pb.ctypes.data_as(_U8), clist.cutoff, ib, 1 if clist._records else 0,
+                                       C.c_void_p(first.data_ptr()), C.byref(total), _ptr(ws), ws.numel(), sh))
+        clist._records = True
+        P = int(total.value)
+        i = torch.empty(P, dtype=ti, device=dev)
+        j = torch.empty(P, dtype=ti, device=dev)
+        S = torch.empty((P, 3), dtype=ti, device=dev)
+        R = torch.empty((P, 3), dtype=torch.float32, device=dev) if with_R else None
+        if P > 0:
+            check(lib().nl_fill_pairs_f32(_ptr(clist.X), _ptr(clist.perm), C.c_void_p(clist.cell_offsets.data_ptr()),
+                                          nat, *plan_args, pb.ctypes.data_as(_U8), clist.cutoff, ib,
+                                          C.c_void_p(first.data_ptr()), P, _ptr(i), _ptr(j), _ptr(S), _ptr(R),
+                                          _ptr(ws), ws.numel(), sh))
+            check(lib().nl_sync_status(_ptr(ws), sh))
+    return PairList(clist.X_orig, clist.cell.copy(), clist.cutoff, i, j, S, first, R, 0)
 
 
 def neighbour_list(X, cutoff: float, cell, pbc, lazy: bool = False, int_type=torch.int32, with_R: bool = True,
@@ -320,6 +380,27 @@ def legacy_pairlist(X, cutoff: float, cell, pbc, int_type=torch.int32, fixcell: 
     return PairList(Xf, cellm, float(cutoff), i, j, S, first, R, int(rechecks.value))
 
 
+def _count_f32(clist: SortedCellList, stream=None) -> torch.Tensor:
+    """first (pair offsets) of a Float32 cell list from the count pass."""
+    nat = int(clist.X.shape[0])
+    dev = clist.X.device
+    if clist._ws is None:
+        clist._ws = _new_workspace(nat, clist.ncells_total, dev)
+        clist._records = False
+    ws = clist._ws
+    first = torch.empty(nat + 1, dtype=_tdtype(clist.index_bytes), device=dev)
+    sh = _stream_handle(stream)
+    with torch.cuda.device(dev):
+        check(lib().nl_count_pairs_f32(_ptr(clist.X), _ptr(clist.perm), _ptr(clist.cell_id),
+                                       C.c_void_p(clist.cell_offsets.data_ptr()), nat, *_plan_args(clist),
+                                       _pbc(clist.pbc).ctypes.data_as(_U8), clist.cutoff, clist.index_bytes,
+                                       1 if clist._records else 0, C.c_void_p(first.data_ptr()), None, _ptr(ws),
+                                       ws.numel(), sh))
+        clist._records = True
+        check(lib().nl_sync_status(_ptr(ws), sh))
+    return first
+
+
 def lazy_reduce(clist: SortedCellList, op: str = "count", stream=None, out: Optional[torch.Tensor] = None,
                 sync: bool = True) -> torch.Tensor:
     """Built-in reductions of the lazy traversal over every atom:
@@ -329,6 +410,16 @@ def lazy_reduce(clist: SortedCellList, op: str = "count", stream=None, out: Opti
     a later nl_sync_status on the cell list's workspace."""
     nat = int(clist.X.shape[0])
     dev = clist.X.device
+    if _is_f32(clist):
+        # Float32 positions: the count pass of the single-precision path
+        if op != "count":
+            raise ValueError("the built-in Σ r^-6 reduction takes Float64 positions; Float32 lists support 'count'")
+        first = _count_f32(clist, stream)
+        counts = (first[1:] - first[:-1]).to(torch.int32)
+        if out is None:
+            return counts
+        out.copy_(counts)
+        return out
     if op == "count":
         code, dt = _lib.NL_REDUCE_COUNT, torch.int32
     elif op == "inv_r6":
@@ -420,6 +511,8 @@ def _getR(nlist: PairList, a: int, b: int) -> torch.Tensor:
     """R of pairs a..b-1 of a list materialised without R, on the device."""
     if nlist.X is None:
         raise NLError(_lib.NL_ERR_ARG, "this PairList has neither R nor the positions to compute it")
+    if nlist.X.dtype == torch.float32:
+        raise NLError(_lib.NL_ERR_ARG, "a Float32 list carries R only when materialised with_R=True")
     X = nlist.X.to(torch.float64).contiguous()
     return pair_vectors(X, nlist.C, nlist.i[a:b], nlist.j[a:b], nlist.S[a:b].contiguous())
 

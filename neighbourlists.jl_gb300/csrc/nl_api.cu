@@ -19,6 +19,7 @@
 #include "nl_api_internal.h"
 #include "nl_build.cuh"
 #include "nl_common.cuh"
+#include "nl_f32.cuh"
 #include "nl_legacy.cuh"
 #include "nl_pairs.cuh"
 #include "nlgpu.h"
@@ -39,25 +40,36 @@ int cuda_fail(cudaError_t e, const char* where) {
 }
 
 // ------------------------------------------------ StaticArrays 3x3 algebra --
-void sa_cross(const double* a, const double* b, double* o) {
+// T = double, or float for the single-precision path (every operation then
+// rounds to Float32, as Julia's Float32 arithmetic does).
+template <typename T>
+void sa_cross(const T* a, const T* b, T* o) {
   o[0] = a[1] * b[2] - a[2] * b[1];
   o[1] = a[2] * b[0] - a[0] * b[2];
   o[2] = a[0] * b[1] - a[1] * b[0];
 }
-double sa_dot(const double* a, const double* b) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
-double sa_norm(const double* a) { return std::sqrt((a[0] * a[0] + a[1] * a[1]) + a[2] * a[2]); }
-double sa_det(const double* M) {
-  double c[3];
+template <typename T>
+T sa_dot(const T* a, const T* b) {
+  return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2];
+}
+template <typename T>
+T sa_norm(const T* a) {
+  return std::sqrt((a[0] * a[0] + a[1] * a[1]) + a[2] * a[2]);
+}
+template <typename T>
+T sa_det(const T* M) {
+  T c[3];
   sa_cross(M + 3, M + 6, c);
   return sa_dot(M, c);
 }
 // inv of a column-major 3x3: rows of the result are y0, y1, y2 with
 // y0 = x1 x x2 / d, y1 = x2 x (x0/d), y2 = (x0/d) x x1, d = x0 . (x1 x x2).
-void sa_inv(const double* M, double* out) {
-  double x0[3] = {M[0], M[1], M[2]}, x1[3] = {M[3], M[4], M[5]}, x2[3] = {M[6], M[7], M[8]};
-  double y0[3], y1[3], y2[3];
+template <typename T>
+void sa_inv(const T* M, T* out) {
+  T x0[3] = {M[0], M[1], M[2]}, x1[3] = {M[3], M[4], M[5]}, x2[3] = {M[6], M[7], M[8]};
+  T y0[3], y1[3], y2[3];
   sa_cross(x1, x2, y0);
-  const double d = sa_dot(x0, y0);
+  const T d = sa_dot(x0, y0);
   for (int k = 0; k < 3; ++k) {
     x0[k] = x0[k] / d;
     y0[k] = y0[k] / d;
@@ -71,10 +83,11 @@ void sa_inv(const double* M, double* out) {
   }
 }
 // lengths(C) = det(C) ./ (|r2 x r3|, |r3 x r1|, |r1 x r2|), cell_list.jl:94-95
-void lengths(const double* C, double* lens) {
-  const double r1[3] = {C[0], C[3], C[6]}, r2[3] = {C[1], C[4], C[7]}, r3[3] = {C[2], C[5], C[8]};
-  const double det = sa_det(C);
-  double c[3];
+template <typename T>
+void lengths(const T* C, T* lens) {
+  const T r1[3] = {C[0], C[3], C[6]}, r2[3] = {C[1], C[4], C[7]}, r3[3] = {C[2], C[5], C[8]};
+  const T det = sa_det(C);
+  T c[3];
   sa_cross(r2, r3, c);
   lens[0] = det / sa_norm(c);
   sa_cross(r3, r1, c);
@@ -448,6 +461,137 @@ int fill_impl(const nl::Geometry& g, const double* Xs, const TI* perm, const TI*
   a.oR = oR;
   a.capacity = capacity;
   nl::launch_pairs<TI>(nl::kModeFill, a, num_sms(), st);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? NL_OK : cuda_fail(e, "launch fill kernel");
+}
+
+// ------------------------------------------------- single-precision path --
+// analyze_cell (cell_list.jl:152-170) and nxyz (gpu_kernels.jl:315-316) with
+// T = Float32: every operation rounds to Float32.
+int analyze_f32(const float* cell, float cutoff, int index_bytes, nl_cell_plan_f32* p) {
+  if (!(cutoff > 0) || !std::isfinite(cutoff)) return fail(NL_ERR_ARG, "cutoff must be positive and finite");
+  if (index_bytes != 4 && index_bytes != 8) return fail(NL_ERR_ARG, "index_bytes must be 4 or 8");
+  sa_inv(cell, p->inv_cell);
+  lengths(cell, p->lens);
+  // floor(TI, x) accepts x < typemax(TI) + 1 (a power of two in Float32)
+  const float tmax = index_bytes == 4 ? 2147483648.0f : 9223372036854775808.0f;
+  long double prod = 1;
+  for (int k = 0; k < 3; ++k) {
+    p->lens[k] = std::fabs(p->lens[k]);
+    const float t = std::floor(p->lens[k] / cutoff);
+    if (!(t < tmax)) return fail(NL_ERR_TOO_MANY_CELLS, "Ratio of simulation cell size to cutoff is very large.");
+    p->ncells[k] = t < 1 ? 1 : int64_t(t);
+    prod *= (long double)p->ncells[k];
+  }
+  if (prod > (long double)(index_bytes == 4 ? 2147483647.0 : 9223372036854775807.0))
+    return fail(NL_ERR_TOO_MANY_CELLS,
+                "Ratio of simulation cell size to cutoff is very large. Use a larger integer type (e.g. Int64), "
+                "larger cutoff, or smaller simulation cell.");
+  if (prod > 2147483646.0L)
+    return fail(NL_ERR_TOO_MANY_CELLS, "more than 2^31-2 cells: use a larger cutoff or a smaller simulation cell");
+  p->ncells_total = p->ncells[0] * p->ncells[1] * p->ncells[2];
+  for (int k = 0; k < 3; ++k) {
+    const float v = std::ceil(cutoff * (float(p->ncells[k]) / p->lens[k]));
+    if (!(v < 1e9f)) return fail(NL_ERR_ARG, "degenerate cell: stencil half-width is not finite");
+    p->nxyz[k] = int64_t(v);
+  }
+  return NL_OK;
+}
+
+nl::Geo32 make_geo32(const float* cell, const float* inv, const int64_t* ns, const int64_t* nxyz, const uint8_t* pbc,
+                     float cutoff, int64_t nat) {
+  nl::Geo32 g;
+  std::memset(&g, 0, sizeof(g));
+  std::memcpy(g.C, cell, sizeof(g.C));
+  std::memcpy(g.inv, inv, sizeof(g.inv));
+  g.cutoff_sq = cutoff * cutoff;  // clist.cutoff^2 in Float32
+  for (int k = 0; k < 3; ++k) {
+    g.ns[k] = int(ns[k]);
+    g.nxyz[k] = nxyz ? int(nxyz[k]) : 0;
+    g.pbc[k] = pbc[k] ? 1 : 0;
+  }
+  g.ncells = int(ns[0] * ns[1] * ns[2]);
+  g.nat = int(nat);
+  return g;
+}
+
+template <typename TI>
+int build_impl32(const float* X, int64_t nat, const nl::Geo32& g, TI* perm, float* Xs, TI* cell_id, TI* cell_offsets,
+                 void* ws, const Layout& L, cudaStream_t st) {
+  const int sms = num_sms();
+  cudaError_t e = cudaMemsetAsync(ws, 0, L.bend, st);
+  if (e != cudaSuccess) return cuda_fail(e, "memset workspace");
+  int* cell_count = at<int>(ws, L.cell_count);
+  int* cell_start = at<int>(ws, L.cell_start);
+  unsigned* err = at<unsigned>(ws, L.err);
+  int* bcount = at<int>(ws, L.bcount);
+  if (nat > 0)
+    nl::launch_bin32(g, X, int(nat), at<int>(ws, L.cid), at<int>(ws, L.ticket), at<float4>(ws, L.rec), cell_count, err,
+                     sms, st);
+  // an empty system scans the zeroed histogram: cell_offsets all ones
+  nl::launch_scan<TI>(cell_count, g.ncells, cell_offsets, cell_start, at<unsigned long long>(ws, L.st_cells), bcount,
+                      at<long long>(ws, L.totals), err, st);
+  if (nat > 0) {
+    const nl::SysIndex single{nullptr, nullptr, nullptr, 0};
+    nl::launch_scatter(int(nat), at<int>(ws, L.cid), at<int>(ws, L.ticket), cell_start, at<int>(ws, L.tmp), sms, st);
+    nl::launch_fix<TI, float>(single, int(nat), at<int>(ws, L.tmp), at<int>(ws, L.cid), cell_start, X,
+                              at<float4>(ws, L.rec), perm, cell_id, Xs, at<float4>(ws, L.rec_sorted),
+                              at<int>(ws, L.scell), at<int>(ws, L.big_list), bcount + 1, sms, st);
+  }
+  e = cudaGetLastError();
+  return e == cudaSuccess ? NL_OK : cuda_fail(e, "launch build kernels");
+}
+
+template <typename TI>
+nl::Pairs32Args<TI> pairs32_args(const nl::Geo32& g, const TI* cell_offsets, const TI* perm, void* ws,
+                                 const Layout& L) {
+  nl::Pairs32Args<TI> a;
+  std::memset(&a, 0, sizeof(a));
+  a.g = g;
+  a.rec = at<float4>(ws, L.rec_sorted);
+  a.scell = at<int>(ws, L.scell);
+  a.cell_offsets = cell_offsets;
+  a.perm = perm;
+  a.counts = at<int>(ws, L.counts);
+  a.err = at<unsigned>(ws, L.err);
+  return a;
+}
+
+template <typename TI>
+int count_impl32(const nl::Geo32& g, const float* Xs, const TI* perm, const TI* cell_id, const TI* cell_offsets,
+                 int reuse, TI* first, void* ws, const Layout& L, cudaStream_t st) {
+  const int sms = num_sms();
+  const size_t z0 = reuse ? L.stats : L.err;
+  cudaError_t e = cudaMemsetAsync(static_cast<char*>(ws) + z0, 0, L.pend - z0, st);
+  if (e != cudaSuccess) return cuda_fail(e, "memset workspace");
+  if (g.nat == 0) {
+    static const TI one = 1;
+    e = cudaMemcpyAsync(first, &one, sizeof(TI), cudaMemcpyHostToDevice, st);
+    return e == cudaSuccess ? NL_OK : cuda_fail(e, "empty system");
+  }
+  if (!reuse)
+    nl::launch_prepare32<TI>(g, Xs, cell_id, perm, g.nat, at<float4>(ws, L.rec_sorted), at<int>(ws, L.scell),
+                             at<unsigned>(ws, L.err), sms, st);
+  const nl::Pairs32Args<TI> a = pairs32_args<TI>(g, cell_offsets, perm, ws, L);
+  nl::launch_pairs32<TI>(false, a, sms, st);
+  nl::launch_scan<TI>(a.counts, g.nat, first, nullptr, at<unsigned long long>(ws, L.st_pairs), at<int>(ws, L.pcount),
+                      at<long long>(ws, L.totals) + 1, a.err, st);
+  e = cudaGetLastError();
+  return e == cudaSuccess ? NL_OK : cuda_fail(e, "launch count kernels");
+}
+
+template <typename TI>
+int fill_impl32(const nl::Geo32& g, const TI* perm, const TI* cell_offsets, const TI* first, int64_t capacity, TI* oi,
+                TI* oj, TI* oS, float* oR, void* ws, const Layout& L, cudaStream_t st) {
+  if (g.nat == 0 || capacity <= 0) return NL_OK;
+  nl::Pairs32Args<TI> a = pairs32_args<TI>(g, cell_offsets, perm, ws, L);
+  a.first = first;
+  a.oi = oi;
+  a.oj = oj;
+  a.oS = oS;
+  a.oR = oR;
+  a.capacity = capacity;
+  nl::launch_pairs32<TI>(true, a, num_sms(), st);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? NL_OK : cuda_fail(e, "launch fill kernel");
 }
@@ -1119,6 +1263,114 @@ int nl_max_displacement_sq(const double* d_X, const double* d_Xref, int64_t nat,
   nl::launch_max_disp_sq(d_X, d_Xref, nat, reinterpret_cast<unsigned long long*>(d_out), num_sms(), st);
   e = cudaGetLastError();
   return e == cudaSuccess ? NL_OK : cuda_fail(e, "launch max displacement");
+}
+
+int nl_analyze_cell_f32(const float cell[9], float cutoff, int index_bytes, nl_cell_plan_f32* plan) {
+  if (!cell || !plan) return fail(NL_ERR_ARG, "null argument");
+  return analyze_f32(cell, cutoff, index_bytes, plan);
+}
+
+int nl_build_cell_list_f32(const float* d_X, int64_t nat, const float cell[9], const float inv_cell[9],
+                           const int64_t ncells[3], const uint8_t pbc[3], float cutoff, int index_bytes, void* d_perm,
+                           float* d_X_sorted, void* d_cell_id, void* d_cell_offsets, void* d_workspace,
+                           size_t workspace_bytes, void* stream) {
+  if (!cell || !inv_cell || !ncells || !pbc || !d_cell_offsets || (nat > 0 && (!d_X || !d_perm || !d_X_sorted || !d_cell_id)))
+    return fail(NL_ERR_ARG, "null argument");
+  Layout L;
+  int64_t nct;
+  int s = check_common(nat, ncells, nullptr, index_bytes, d_workspace, workspace_bytes, L, nct);
+  if (s) return s;
+  const nl::Geo32 g = make_geo32(cell, inv_cell, ncells, nullptr, pbc, cutoff, nat);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (index_bytes == 4)
+    return build_impl32<int32_t>(d_X, nat, g, static_cast<int32_t*>(d_perm), d_X_sorted,
+                                 static_cast<int32_t*>(d_cell_id), static_cast<int32_t*>(d_cell_offsets), d_workspace, L,
+                                 st);
+  return build_impl32<int64_t>(d_X, nat, g, static_cast<int64_t*>(d_perm), d_X_sorted, static_cast<int64_t*>(d_cell_id),
+                               static_cast<int64_t*>(d_cell_offsets), d_workspace, L, st);
+}
+
+int nl_count_pairs_f32(const float* d_X_sorted, const void* d_perm, const void* d_cell_id, const void* d_cell_offsets,
+                       int64_t nat, const float cell[9], const float inv_cell[9], const int64_t ncells[3],
+                       const int64_t nxyz[3], const uint8_t pbc[3], float cutoff, int index_bytes, int reuse_records,
+                       void* d_first, int64_t* total_pairs, void* d_workspace, size_t workspace_bytes, void* stream) {
+  if (!cell || !inv_cell || !ncells || !nxyz || !pbc || !d_first || !d_cell_offsets ||
+      (nat > 0 && (!d_X_sorted || !d_perm || !d_cell_id)))
+    return fail(NL_ERR_ARG, "null argument");
+  Layout L;
+  int64_t nct;
+  int s = check_common(nat, ncells, nxyz, index_bytes, d_workspace, workspace_bytes, L, nct);
+  if (s) return s;
+  const nl::Geo32 g = make_geo32(cell, inv_cell, ncells, nxyz, pbc, cutoff, nat);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (index_bytes == 4)
+    s = count_impl32<int32_t>(g, d_X_sorted, static_cast<const int32_t*>(d_perm),
+                              static_cast<const int32_t*>(d_cell_id), static_cast<const int32_t*>(d_cell_offsets),
+                              reuse_records, static_cast<int32_t*>(d_first), d_workspace, L, st);
+  else
+    s = count_impl32<int64_t>(g, d_X_sorted, static_cast<const int64_t*>(d_perm),
+                              static_cast<const int64_t*>(d_cell_id), static_cast<const int64_t*>(d_cell_offsets),
+                              reuse_records, static_cast<int64_t*>(d_first), d_workspace, L, st);
+  if (s) return s;
+  if (total_pairs) {
+    if (nat == 0) {
+      *total_pairs = 0;
+      return sync_read(d_workspace, st, nullptr, nullptr);
+    }
+    return sync_read(d_workspace, st, at<long long>(d_workspace, L.totals) + 1, total_pairs);
+  }
+  return NL_OK;
+}
+
+int nl_fill_pairs_f32(const float* d_X_sorted, const void* d_perm, const void* d_cell_offsets, int64_t nat,
+                      const float cell[9], const float inv_cell[9], const int64_t ncells[3], const int64_t nxyz[3],
+                      const uint8_t pbc[3], float cutoff, int index_bytes, const void* d_first, int64_t capacity,
+                      void* d_i, void* d_j, void* d_S, float* d_R, void* d_workspace, size_t workspace_bytes,
+                      void* stream) {
+  if (!cell || !inv_cell || !ncells || !nxyz || !pbc || !d_first || !d_cell_offsets)
+    return fail(NL_ERR_ARG, "null argument");
+  if (capacity > 0 && (!d_i || !d_j || !d_S || !d_X_sorted || !d_perm)) return fail(NL_ERR_ARG, "null argument");
+  Layout L;
+  int64_t nct;
+  int s = check_common(nat, ncells, nxyz, index_bytes, d_workspace, workspace_bytes, L, nct);
+  if (s) return s;
+  const nl::Geo32 g = make_geo32(cell, inv_cell, ncells, nxyz, pbc, cutoff, nat);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (index_bytes == 4)
+    return fill_impl32<int32_t>(g, static_cast<const int32_t*>(d_perm), static_cast<const int32_t*>(d_cell_offsets),
+                                static_cast<const int32_t*>(d_first), capacity, static_cast<int32_t*>(d_i),
+                                static_cast<int32_t*>(d_j), static_cast<int32_t*>(d_S), d_R, d_workspace, L, st);
+  return fill_impl32<int64_t>(g, static_cast<const int64_t*>(d_perm), static_cast<const int64_t*>(d_cell_offsets),
+                              static_cast<const int64_t*>(d_first), capacity, static_cast<int64_t*>(d_i),
+                              static_cast<int64_t*>(d_j), static_cast<int64_t*>(d_S), d_R, d_workspace, L, st);
+}
+
+int nl_neighbour_list_f32(const float* d_X, int64_t nat, const float cell[9], const float inv_cell[9],
+                          const int64_t ncells[3], const int64_t nxyz[3], const uint8_t pbc[3], float cutoff,
+                          int index_bytes, void* d_perm, float* d_X_sorted, void* d_cell_id, void* d_cell_offsets,
+                          void* d_first, int64_t capacity, void* d_i, void* d_j, void* d_S, float* d_R,
+                          int64_t* total_pairs, void* d_workspace, size_t workspace_bytes, void* stream) {
+  int s = nl_build_cell_list_f32(d_X, nat, cell, inv_cell, ncells, pbc, cutoff, index_bytes, d_perm, d_X_sorted,
+                                 d_cell_id, d_cell_offsets, d_workspace, workspace_bytes, stream);
+  if (s) return s;
+  s = nl_count_pairs_f32(d_X_sorted, d_perm, d_cell_id, d_cell_offsets, nat, cell, inv_cell, ncells, nxyz, pbc, cutoff,
+                         index_bytes, 1, d_first, nullptr, d_workspace, workspace_bytes, stream);
+  if (s) return s;
+  s = nl_fill_pairs_f32(d_X_sorted, d_perm, d_cell_offsets, nat, cell, inv_cell, ncells, nxyz, pbc, cutoff, index_bytes,
+                        d_first, capacity, d_i, d_j, d_S, d_R, d_workspace, workspace_bytes, stream);
+  if (s) return s;
+  if (total_pairs) {
+    Layout L = layout(nat, ncells[0] * ncells[1] * ncells[2]);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (nat == 0) {
+      *total_pairs = 0;
+      return sync_read(d_workspace, st, nullptr, nullptr);
+    }
+    s = sync_read(d_workspace, st, at<long long>(d_workspace, L.totals) + 1, total_pairs);
+    if (s == NL_OK && *total_pairs > capacity) return fail(NL_ERR_CAPACITY, "pair buffers are smaller than the pair count");
+    return s;
+  }
+  return NL_OK;
 }
 
 size_t nl_legacy_workspace_bytes(int64_t nat, int64_t ncells_total, int index_bytes) {

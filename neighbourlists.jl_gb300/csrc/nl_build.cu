@@ -67,11 +67,11 @@ __global__ void __launch_bounds__(256) k_scatter(int nat, const int* __restrict_
     tmp[cell_start[cid[i]] + ticket[i]] = int(i);
 }
 
-template <typename TI>
+template <typename TI, typename TX>
 __device__ __forceinline__ void write_sorted(const SysIndex& si, long long dst, int i, int c,
-                                             const double* __restrict__ X, const float4* __restrict__ rec,
+                                             const TX* __restrict__ X, const float4* __restrict__ rec,
                                              TI* __restrict__ perm, TI* __restrict__ cell_id,
-                                             double* __restrict__ Xs, float4* __restrict__ rec_sorted,
+                                             TX* __restrict__ Xs, float4* __restrict__ rec_sorted,
                                              int* __restrict__ scell) {
   int li = i, lc = c;
   if (si.nsys > 0) {  // system-local indices
@@ -92,11 +92,11 @@ __device__ __forceinline__ void write_sorted(const SysIndex& si, long long dst, 
 // One thread per sorted slot.  For cells of at most kFixMax atoms the stable
 // position of atom i is (cell start) + #{atoms of the cell with index < i}.
 // Larger cells are listed for k_fix_big.
-template <typename TI>
+template <typename TI, typename TX>
 __global__ void __launch_bounds__(256) k_fix(SysIndex si, int nat, const int* __restrict__ tmp, const int* __restrict__ cid,
-                                             const int* __restrict__ cell_start, const double* __restrict__ X,
+                                             const int* __restrict__ cell_start, const TX* __restrict__ X,
                                              const float4* __restrict__ rec, TI* __restrict__ perm,
-                                             TI* __restrict__ cell_id, double* __restrict__ Xs,
+                                             TI* __restrict__ cell_id, TX* __restrict__ Xs,
                                              float4* __restrict__ rec_sorted, int* __restrict__ scell,
                                              int* __restrict__ big_list, int* __restrict__ big_count) {
   for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < nat; s += (long long)gridDim.x * blockDim.x) {
@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(256) k_fix(SysIndex si, int nat, const int* __
     }
     int rank = 0;
     for (int t = start; t < start + k; ++t) rank += tmp[t] < i;
-    write_sorted<TI>(si, start + rank, i, c, X, rec, perm, cell_id, Xs, rec_sorted, scell);
+    write_sorted<TI, TX>(si, start + rank, i, c, X, rec, perm, cell_id, Xs, rec_sorted, scell);
   }
 }
 
@@ -118,13 +118,13 @@ __global__ void __launch_bounds__(256) k_fix(SysIndex si, int nat, const int* __
 // One block per listed cell.  Cells up to kBigSort atoms are sorted in shared
 // memory (bitonic); larger ones are rebuilt by a block-wide ordered scan over
 // all atoms (stable by construction).
-template <typename TI>
+template <typename TI, typename TX>
 __global__ void __launch_bounds__(kFixBigThreads) k_fix_big(SysIndex si, int nat, const int* __restrict__ tmp,
                                                             const int* __restrict__ cid,
                                                             const int* __restrict__ cell_start,
-                                                            const double* __restrict__ X,
+                                                            const TX* __restrict__ X,
                                                             const float4* __restrict__ rec, TI* __restrict__ perm,
-                                                            TI* __restrict__ cell_id, double* __restrict__ Xs,
+                                                            TI* __restrict__ cell_id, TX* __restrict__ Xs,
                                                             float4* __restrict__ rec_sorted,
                                                             int* __restrict__ scell,
                                                             const int* __restrict__ big_list,
@@ -157,7 +157,7 @@ __global__ void __launch_bounds__(kFixBigThreads) k_fix_big(SysIndex si, int nat
           __syncthreads();
         }
       for (int t = threadIdx.x; t < k; t += blockDim.x)
-        write_sorted<TI>(si, start + t, s[t], c, X, rec, perm, cell_id, Xs, rec_sorted, scell);
+        write_sorted<TI, TX>(si, start + t, s[t], c, X, rec, perm, cell_id, Xs, rec_sorted, scell);
       __syncthreads();
     } else {
       int run = 0;
@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(kFixBigThreads) k_fix_big(SysIndex si, int nat
           tot += s_warp[w];
         }
         if (f)
-          write_sorted<TI>(si, start + run + before + __popc(m & lanemask_lt()), i, c, X, rec, perm, cell_id, Xs,
+          write_sorted<TI, TX>(si, start + run + before + __popc(m & lanemask_lt()), i, c, X, rec, perm, cell_id, Xs,
                            rec_sorted, scell);
         run += tot;
         __syncthreads();
@@ -280,15 +280,15 @@ void launch_scatter(int nat, const int* cid, const int* ticket, const int* cell_
   k_scatter<<<grid_for(nat, 256, num_sms * 8), 256, 0, st>>>(nat, cid, ticket, cell_start, tmp);
 }
 
-template <typename TI>
-void launch_fix(const SysIndex& si, int nat, const int* tmp, const int* cid, const int* cell_start, const double* X,
-                const float4* rec, TI* perm, TI* cell_id, double* Xs, float4* rec_sorted, int* scell, int* big_list,
+template <typename TI, typename TX>
+void launch_fix(const SysIndex& si, int nat, const int* tmp, const int* cid, const int* cell_start, const TX* X,
+                const float4* rec, TI* perm, TI* cell_id, TX* Xs, float4* rec_sorted, int* scell, int* big_list,
                 int* big_count, int num_sms, cudaStream_t st) {
   if (nat <= 0) return;
-  k_fix<TI><<<grid_for(nat, 256, num_sms * 8), 256, 0, st>>>(si, nat, tmp, cid, cell_start, X, rec, perm, cell_id, Xs,
-                                                             rec_sorted, scell, big_list, big_count);
-  k_fix_big<TI><<<num_sms, kFixBigThreads, 0, st>>>(si, nat, tmp, cid, cell_start, X, rec, perm, cell_id, Xs,
-                                                     rec_sorted, scell, big_list, big_count);
+  k_fix<TI, TX><<<grid_for(nat, 256, num_sms * 8), 256, 0, st>>>(si, nat, tmp, cid, cell_start, X, rec, perm, cell_id,
+                                                                 Xs, rec_sorted, scell, big_list, big_count);
+  k_fix_big<TI, TX><<<num_sms, kFixBigThreads, 0, st>>>(si, nat, tmp, cid, cell_start, X, rec, perm, cell_id, Xs,
+                                                         rec_sorted, scell, big_list, big_count);
 }
 
 template <typename TI>
@@ -306,8 +306,12 @@ void launch_scan(const int* in, long long n, TI* out1, int* out0, unsigned long 
 }
 
 #define NL_INST(TI)                                                                                                  \
-  template void launch_fix<TI>(const SysIndex&, int, const int*, const int*, const int*, const double*,            \
-                               const float4*, TI*, TI*, double*, float4*, int*, int*, int*, int, cudaStream_t);     \
+  template void launch_fix<TI, double>(const SysIndex&, int, const int*, const int*, const int*, const double*,    \
+                                       const float4*, TI*, TI*, double*, float4*, int*, int*, int*, int,            \
+                                       cudaStream_t);                                                               \
+  template void launch_fix<TI, float>(const SysIndex&, int, const int*, const int*, const int*, const float*,      \
+                                      const float4*, TI*, TI*, float*, float4*, int*, int*, int*, int,              \
+                                      cudaStream_t);                                                                \
   template void launch_batch_cell_offsets<TI>(const SysIndex&, int, const int*, TI*, int, cudaStream_t);            \
   template void launch_batch_first<TI>(const SysIndex&, int, const TI*, TI*, long long*, int, cudaStream_t);        \
   template void launch_prepare<TI>(const Geometry&, const double*, const TI*, const TI*, int, float4*, int*,     \

@@ -23,9 +23,10 @@ void launch_bin(const Geometry& g, const SysIndex& si, const double* X, int nat,
                 int* cell_count, unsigned* err, int num_sms, cudaStream_t st);
 void launch_scatter(int nat, const int* cid, const int* ticket, const int* cell_start, int* tmp, int num_sms,
                     cudaStream_t st);
-template <typename TI>
-void launch_fix(const SysIndex& si, int nat, const int* tmp, const int* cid, const int* cell_start, const double* X,
-                const float4* rec, TI* perm, TI* cell_id, double* Xs, float4* rec_sorted, int* scell, int* big_list,
+// TX: position type (double; float for the single-precision path)
+template <typename TI, typename TX = double>
+void launch_fix(const SysIndex& si, int nat, const int* tmp, const int* cid, const int* cell_start, const TX* X,
+                const float4* rec, TI* perm, TI* cell_id, TX* Xs, float4* rec_sorted, int* scell, int* big_list,
                 int* big_count, int num_sms, cudaStream_t st);
 // batches: the per-system cell_offsets (ncells_s + 1 entries each, system s
 // first at cell0[s] + s) from the launch's 0-based cell starts

@@ -37,9 +37,8 @@ def build() -> str:
 def lib():
     global _lib
     if _lib is None:
-        if not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(
-            os.path.join(_HERE, "nl_oracle.c")
-        ):
+        newest = max(os.path.getmtime(os.path.join(_HERE, f)) for f in ("nl_oracle.c", "nl_oracle_f32.c", "Makefile"))
+        if not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < newest:
             build()
         _lib = C.CDLL(_LIB_PATH)
         _declare(_lib)
@@ -63,7 +62,25 @@ class _Result(C.Structure):
     ]
 
 
+class _ResultF32(C.Structure):
+    _fields_ = [
+        ("nat", C.c_int64),
+        ("npairs", C.c_int64),
+        ("ncells", C.c_int64),
+        ("perm", C.POINTER(C.c_int64)),
+        ("cell_id", C.POINTER(C.c_int64)),
+        ("cell_offsets", C.POINTER(C.c_int64)),
+        ("first", C.POINTER(C.c_int64)),
+        ("i", C.POINTER(C.c_int64)),
+        ("j", C.POINTER(C.c_int64)),
+        ("S", C.POINTER(C.c_int64)),
+        ("X_sorted", C.POINTER(C.c_float)),
+        ("R", C.POINTER(C.c_float)),
+    ]
+
+
 _D = C.POINTER(C.c_double)
+_F = C.POINTER(C.c_float)
 _I = C.POINTER(C.c_int64)
 _U8 = C.POINTER(C.c_uint8)
 
@@ -90,6 +107,11 @@ def _declare(L):
     L.orc_legacy_pairlist.argtypes = [_D, C.c_int64, _D, _U8, C.c_double, C.c_int, C.c_int, C.POINTER(_Result), _D]
     L.orc_legacy_pairlist.restype = C.c_int64
     L.orc_fix_cell.argtypes = [_D, C.c_int64, _D, _U8]
+    L.orc_analyze_cell_f32.argtypes = [_F, C.c_float, C.c_int, _F, _I, _F, _I]
+    L.orc_analyze_cell_f32.restype = C.c_int
+    L.orc_neighbour_list_f32.argtypes = [_F, C.c_int64, _F, _U8, C.c_float, C.c_int, C.POINTER(_ResultF32)]
+    L.orc_neighbour_list_f32.restype = C.c_int
+    L.orc_free_f32.argtypes = [C.POINTER(_ResultF32)]
 
 
 def _colmajor(cell) -> np.ndarray:
@@ -340,4 +362,74 @@ def canonical(i, j, S, R=None):
     out = (i[order], j[order], S[order])
     if R is not None:
         out = out + (np.asarray(R).reshape(-1, 3)[order],)
+    return out
+
+
+# ------------------------------------------------------------ T = Float32 --
+@dataclass
+class OracleF32Result:
+    """build_cell_list + materialize_pairlist with T = Float32 (nl_oracle_f32.c)."""
+    perm: np.ndarray          # int64[nat], 1-based
+    cell_id: np.ndarray       # int64[nat], sorted
+    cell_offsets: np.ndarray  # int64[ncells+1]
+    X_sorted: np.ndarray      # float32[nat, 3]
+    i: np.ndarray
+    j: np.ndarray
+    S: np.ndarray             # int64[P, 3]
+    first: np.ndarray         # int64[nat+1]
+    R: np.ndarray             # float32[P, 3]
+
+    @property
+    def npairs(self) -> int:
+        return int(self.i.shape[0])
+
+
+def _f32_inputs(X, cutoff, cell):
+    X32 = np.ascontiguousarray(np.asarray(X).astype(np.float32).reshape(-1, 3))
+    cm32 = np.ascontiguousarray(np.asarray(cell, dtype=np.float64).reshape(3, 3).astype(np.float32).T).reshape(9)
+    return X32, cm32, np.float32(cutoff)
+
+
+def analyze_cell_f32(cell, cutoff, ti_bytes=4):
+    """analyze_cell + nxyz with T = Float32: (inv (3x3 float32), ncells, lens, nxyz)."""
+    L = lib()
+    _, cm, rc = _f32_inputs(np.zeros((0, 3)), cutoff, cell)
+    inv = np.zeros(9, dtype=np.float32)
+    ns = np.zeros(3, dtype=np.int64)
+    lens = np.zeros(3, dtype=np.float32)
+    nxyz = np.zeros(3, dtype=np.int64)
+    st = L.orc_analyze_cell_f32(_p(cm, _F), float(rc), int(ti_bytes), _p(inv, _F), _p(ns, _I), _p(lens, _F),
+                                _p(nxyz, _I))
+    if st:
+        raise OracleError(f"analyze_cell (Float32) failed with status {st}")
+    return inv.reshape(3, 3).T.copy(), ns, lens, nxyz
+
+
+def neighbour_list_f32(X, cutoff, cell, pbc, ti_bytes=4) -> OracleF32Result:
+    """The reference's sort-based path with positions, cell and cutoff in
+    Float32 (cell and cutoff converted as build_cell_list does, cell_list.jl:637-639)."""
+    L = lib()
+    X32, cm, rc = _f32_inputs(X, cutoff, cell)
+    nat = X32.shape[0]
+    pb = _pbc(pbc)
+    res = _ResultF32()
+    st = L.orc_neighbour_list_f32(_p(X32, _F), nat, _p(cm, _F), _p(pb, _U8), float(rc), int(ti_bytes), C.byref(res))
+    if st:
+        L.orc_free_f32(C.byref(res))
+        raise OracleError(f"neighbour_list (Float32) failed with status {st}")
+    try:
+        P = res.npairs
+        out = OracleF32Result(
+            perm=_arr(res.perm, nat, np.int64),
+            cell_id=_arr(res.cell_id, nat, np.int64),
+            cell_offsets=_arr(res.cell_offsets, res.ncells + 1, np.int64),
+            X_sorted=_arr(res.X_sorted, 3 * nat, np.float32, (nat, 3)),
+            i=_arr(res.i, P, np.int64),
+            j=_arr(res.j, P, np.int64),
+            S=_arr(res.S, 3 * P, np.int64, (P, 3)),
+            first=_arr(res.first, nat + 1, np.int64),
+            R=_arr(res.R, 3 * P, np.float32, (P, 3)),
+        )
+    finally:
+        L.orc_free_f32(C.byref(res))
     return out

@@ -1,0 +1,123 @@
+"""GPU parity of the single-precision path (positions, cell and cutoff in
+Float32) against the oracle's Float32 restatement of the reference
+(oracle/nl_oracle_f32.c): the SortedCellList arrays and i, j, S, first and
+the bits of R identical in the reference's order.  The reference runs its GPU
+tests for Float64 and Float32 (test/test_gpu.jl:14, test/test_utils.jl:239);
+the cases follow those tests plus atoms outside the cell (windings) and
+cutoff-boundary lattices."""
+import numpy as np
+import pytest
+import torch
+
+import configs as cf
+
+pytestmark = pytest.mark.gpu
+
+
+def to_np(t):
+    return t.detach().cpu().numpy()
+
+
+def run_both(nlpkg, orc, X, rc, cell, pbc, int_type=torch.int32):
+    X32 = np.ascontiguousarray(np.asarray(X).astype(np.float32).reshape(-1, 3))
+    clist = nlpkg.build_cell_list(torch.from_numpy(X32).cuda(), rc, cell, pbc, int_type=int_type)
+    g = nlpkg.materialize_pairlist(clist)
+    o = orc.neighbour_list_f32(X32, rc, cell, pbc, ti_bytes=4 if int_type == torch.int32 else 8)
+    return clist, g, o
+
+
+def assert_identical(clist, g, o):
+    np.testing.assert_array_equal(to_np(clist.perm).astype(np.int64), o.perm)
+    np.testing.assert_array_equal(to_np(clist.cell_id).astype(np.int64), o.cell_id)
+    np.testing.assert_array_equal(to_np(clist.cell_offsets).astype(np.int64), o.cell_offsets)
+    assert np.array_equal(to_np(clist.X).view(np.int32), o.X_sorted.view(np.int32))
+    assert g.R.dtype == torch.float32 and int(g.i.shape[0]) == o.npairs
+    np.testing.assert_array_equal(to_np(g.first).astype(np.int64), o.first)
+    np.testing.assert_array_equal(to_np(g.i).astype(np.int64), o.i)
+    np.testing.assert_array_equal(to_np(g.j).astype(np.int64), o.j)
+    np.testing.assert_array_equal(to_np(g.S).astype(np.int64), o.S)
+    assert np.array_equal(to_np(g.R).view(np.int32), o.R.view(np.int32)), "R bits differ"
+
+
+@pytest.mark.parametrize("seed", range(5))
+def test_random_configs(nlpkg, orc, seed):
+    N = 50 + 37 * seed
+    X, C, L = cf.rand_config(N, seed=500 + seed)
+    assert_identical(*run_both(nlpkg, orc, X, L / 3, C, (True, True, True)))
+
+
+@pytest.mark.parametrize("pbc", cf.ALL_PBC)
+def test_all_pbc(nlpkg, orc, pbc):
+    X, C, L = cf.rand_config(50, seed=57)
+    assert_identical(*run_both(nlpkg, orc, X, 0.33 * L, C, pbc))
+    X, C, L = cf.rand_config(3000, seed=58)
+    assert_identical(*run_both(nlpkg, orc, X, 5.0, C, pbc))
+
+
+def test_triclinic_and_elongated(nlpkg, orc):
+    X, C = cf.rand_config_triclinic(80, seed=59)
+    assert_identical(*run_both(nlpkg, orc, X, 3.0, C, (True, True, True)))
+    C2 = np.diag([5.0, 5.0, 20.0])
+    X2 = np.random.default_rng(60).random((80, 3)) @ C2
+    assert_identical(*run_both(nlpkg, orc, X2, 3.0, C2, (True, True, True)))
+    X3, C3 = cf.fcc_sheared(n=6, seed=61)[:2]
+    assert_identical(*run_both(nlpkg, orc, X3, 5.0, C3, (True, True, False)))
+
+
+def test_known_answers(nlpkg, orc):
+    X, C = cf.diamond_primitive()
+    clist, g, o = run_both(nlpkg, orc, X, 6.0, C, (True, True, True))
+    assert o.npairs == 92 and list(np.diff(to_np(g.first))) == [46, 46]
+    assert_identical(clist, g, o)
+    X, C = cf.fcc_cubic(3.61, (3, 3, 3))
+    clist, g, o = run_both(nlpkg, orc, X, 3.5, C, (True, True, True))
+    assert np.all(np.diff(to_np(g.first)) == 12)
+    assert_identical(clist, g, o)
+
+
+def test_atoms_outside_the_cell(nlpkg, orc):
+    X, C, L = cf.rand_config(600, seed=62)
+    X = X + np.random.default_rng(63).integers(-4, 5, X.shape) * L
+    for pbc in [(True, True, True), (True, False, True), (False, False, False)]:
+        assert_identical(*run_both(nlpkg, orc, X, 0.2 * L, C, pbc))
+
+
+def test_cutoff_boundary_lattice(nlpkg, orc):
+    X, C = cf.fcc_cubic(3.61, (4, 4, 4))
+    rc = np.float32(3.61) / np.sqrt(np.float32(2))
+    for r in (np.nextafter(rc, np.float32(0)), rc, np.nextafter(rc, np.float32(10))):
+        assert_identical(*run_both(nlpkg, orc, X, float(r), C, (True, True, True)))
+
+
+def test_int64_and_sizes(nlpkg, orc):
+    X, C, L = cf.rand_config(20000, seed=64)
+    assert_identical(*run_both(nlpkg, orc, X, 5.0, C, (True, True, True), int_type=torch.int64))
+    assert_identical(*run_both(nlpkg, orc, X, 5.0, C, (True, False, True)))
+
+
+def test_edge_cases(nlpkg, orc):
+    C = np.diag([10.0] * 3)
+    for X, pbc in [(np.zeros((0, 3)), (1, 1, 1)), (np.array([[5.0, 5.0, 5.0]]), (1, 1, 1)),
+                   (np.array([[5.0, 5.0, 5.0], [5.0, 5.0, 6.0]]), (1, 1, 1)),
+                   (np.array([[1.0, 1.0, 1.0], [8.0, 8.0, 8.0]]), (0, 0, 0))]:
+        assert_identical(*run_both(nlpkg, orc, X, 3.0, C, pbc))
+
+
+def test_lazy_and_unified_api(nlpkg, orc):
+    X, C, L = cf.rand_config(1000, seed=65)
+    X32 = X.astype(np.float32)
+    o = orc.neighbour_list_f32(X32, 0.25 * L, C, (1, 1, 1))
+    nl = nlpkg.neighbour_list(torch.from_numpy(X32).cuda(), 0.25 * L, C, (True, True, True))
+    np.testing.assert_array_equal(to_np(nl.j).astype(np.int64), o.j)
+    clist = nlpkg.neighbour_list(torch.from_numpy(X32).cuda(), 0.25 * L, C, (True, True, True), lazy=True)
+    np.testing.assert_array_equal(to_np(nlpkg.lazy_reduce(clist, "count")).astype(np.int64), np.diff(o.first))
+    js, Rs, Ss = nlpkg.neighbours(clist, 7)
+    a, b = o.first[6] - 1, o.first[7] - 1
+    np.testing.assert_array_equal(to_np(js).astype(np.int64), o.j[a:b])
+    assert np.array_equal(to_np(Rs).view(np.int32), o.R[a:b].view(np.int32))
+
+
+def test_bad_positions_raise(nlpkg):
+    X = torch.tensor([[1.0, 2.0, 3.0], [float("inf"), 0.0, 0.0]], dtype=torch.float32, device="cuda")
+    with pytest.raises(nlpkg.NLError):
+        nlpkg.build_cell_list(X, 2.0, np.diag([10.0] * 3), (True, True, True))

@@ -52,6 +52,21 @@ def test_analyze_cell_bit_equal_to_oracle(nlpkg, orc, k, rc):
     assert p.ncells_total == int(np.prod(o.ncells))
 
 
+@pytest.mark.parametrize("k,rc", [(0, 5.0), (1, 3.0), (2, 6.0), (3, 0.7), (4, 2.5)])
+def test_analyze_cell_f32_bit_equal_to_oracle(nlpkg, orc, k, rc):
+    """analyze_cell with T = Float32 (cell and cutoff converted to Float32,
+    every operation in single precision) equals the oracle's restatement."""
+    cells = [np.diag([58.48] * 3), cf.triclinic_cell(), np.array([[5.43 / 2 * a for a in r] for r in
+                                                                  [(0, 1, 1), (1, 0, 1), (1, 1, 0)]]),
+             np.array([[3.3, 0.4, 0.1], [0.2, 2.9, 0.7], [0.0, 0.3, 4.1]]), np.diag([72.2, 72.2, 92.2])]
+    plan = nlpkg.analyze_cell(cells[k], rc, float32=True)
+    inv, ns, lens, nxyz = orc.analyze_cell_f32(cells[k], rc)
+    assert plan.inv_cm.dtype == np.float32
+    assert np.array_equal(plan.inv_cell.view(np.int32), inv.view(np.int32))
+    assert np.array_equal(plan.lens.view(np.int32), lens.view(np.int32))
+    assert plan.ncells.tolist() == ns.tolist() and plan.nxyz.tolist() == nxyz.tolist()
+
+
 def test_too_many_cells_error(nlpkg):
     cell = np.diag([1e6, 1e6, 1e6])
     with pytest.raises(nlpkg.NLError) as e:
