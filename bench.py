@@ -292,6 +292,8 @@ def run_gpu(args):
         torch.cuda.empty_cache()
         extra.update(bench_half_and_verlet(nl, dev, stream, flush, extra_steps))
         torch.cuda.empty_cache()
+        extra.update(bench_float32_and_legacy(nl, dev, stream, flush, extra_steps))
+        torch.cuda.empty_cache()
         extra["serving"] = bench_serving(nl, dev)
     if rank != 0:
         return
@@ -486,6 +488,38 @@ def bench_half_and_verlet(nl, dev, stream, flush, steps):
             "verlet": {"workload": f"1M-atom workload, list at cutoff + {skin} A skin, atoms moved by up to 0.05 A",
                        "pairs": int(vpairs), "reuse_ms": reuse_ms, "rebuild_ms": rebuild_ms,
                        "reuses": v.reuses, "rebuilds": v.rebuilds}}
+
+
+def bench_float32_and_legacy(nl, dev, stream, flush, steps):
+    """The 1M-atom workload with Float32 positions (the reference with
+    T = Float32: build, count and fill with R in single precision), and the
+    reference's legacy linked-list PairList (cell fix, legacy screen, j sort)
+    timed as a whole synchronising call, as a user makes it."""
+    import time
+
+    import torch
+
+    X, C, pbc = workload()
+    X32 = torch.from_numpy(X.astype(np.float32)).to(dev)
+    eng = nl.NeighbourListEngine(X.shape[0], C, CUTOFF, pbc, device=dev, dtype=torch.float32)
+    total = eng.run(X32)
+    f32_ms = timed_steps(lambda: eng.launch(X32), steps, flush, stream)
+    eng.sync_status()
+    del eng
+    torch.cuda.empty_cache()
+    Xd = torch.from_numpy(X).to(dev)
+    lg = nl.legacy_pairlist(Xd, CUTOFF, C, pbc)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        lg = nl.legacy_pairlist(Xd, CUTOFF, C, pbc)
+    torch.cuda.synchronize(dev)
+    legacy_ms = (time.perf_counter() - t0) / steps * 1e3
+    return {"float32": {"workload": "1M-atom workload, Float32 positions, cell and cutoff", "pairs": int(total),
+                        "ms_per_step": f32_ms, "pairs_per_s": total / (f32_ms * 1e-3)},
+            "legacy": {"workload": "1M-atom workload, legacy linked-list PairList (fixcell = true)",
+                       "pairs": int(lg.i.numel()), "ms_per_call": legacy_ms,
+                       "timing": "host clock around the whole synchronising call (allocations included)"}}
 
 
 def bench_4m(nl, dev, stream, flush, steps):

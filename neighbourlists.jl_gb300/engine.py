@@ -19,28 +19,38 @@ from ._lib import check, lib
 from .api import PairList, SortedCellList, _index_bytes, _pbc, _ptr, _stream_handle, _tdtype, analyze_cell
 
 _D = C.POINTER(C.c_double)
+_F = C.POINTER(C.c_float)
 _I64 = C.POINTER(C.c_int64)
 _U8 = C.POINTER(C.c_uint8)
 
 
 class NeighbourListEngine:
+    """``dtype=torch.float32`` runs the single-precision path (positions, cell,
+    cutoff and R in Float32, the reference with T = Float32)."""
+
     def __init__(self, nat: int, cell, cutoff: float, pbc, int_type=torch.int32, with_R: bool = True,
-                 capacity: Optional[int] = None, device="cuda", half: bool = False):
+                 capacity: Optional[int] = None, device="cuda", half: bool = False, dtype=torch.float64):
+        if dtype not in (torch.float64, torch.float32):
+            raise TypeError("dtype must be torch.float64 or torch.float32")
+        self.f32 = dtype == torch.float32
+        if self.f32 and half:
+            raise TypeError("half lists take Float64 positions")
+        self.dtype = dtype
         self.nat = int(nat)
-        self.cell = np.asarray(cell, dtype=np.float64).reshape(3, 3).copy()
-        self.cutoff = float(cutoff)
+        self.cell = np.asarray(cell, dtype=np.float64).reshape(3, 3).astype(np.float32 if self.f32 else np.float64)
+        self.cutoff = np.float32(cutoff).item() if self.f32 else float(cutoff)
         self.pbc = _pbc(pbc)
         self.ib = _index_bytes(int_type)
         self.ti = _tdtype(self.ib)
         self.with_R = with_R
         self.half = bool(half)  # keep each unordered pair once (nl_neighbour_list_half)
         self.device = torch.device(device)
-        self.plan = analyze_cell(self.cell, self.cutoff, int_type)
+        self.plan = analyze_cell(self.cell, self.cutoff, int_type, float32=self.f32)
         p = self.plan
         nbytes = int(lib().nl_workspace_bytes(self.nat, p.ncells_total))
         self.ws = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
         self.perm = torch.empty(self.nat, dtype=self.ti, device=self.device)
-        self.Xs = torch.empty((self.nat, 3), dtype=torch.float64, device=self.device)
+        self.Xs = torch.empty((self.nat, 3), dtype=dtype, device=self.device)
         self.cid = torch.empty(self.nat, dtype=self.ti, device=self.device)
         self.offs = torch.empty(p.ncells_total + 1, dtype=self.ti, device=self.device)
         self.first = torch.empty(self.nat + 1, dtype=self.ti, device=self.device)
@@ -48,7 +58,7 @@ class NeighbourListEngine:
         self.i = self.j = self.S = self.R = None
         if capacity is None:
             # expected pairs for a homogeneous system plus headroom
-            vol = abs(float(np.linalg.det(self.cell)))
+            vol = abs(float(np.linalg.det(self.cell.astype(np.float64))))
             rho = self.nat / vol if vol > 0 else 0.0
             capacity = int(1.15 * self.nat * rho * 4.0 / 3.0 * np.pi * self.cutoff ** 3 / (2 if half else 1)) + 1024
         self._alloc(capacity)
@@ -62,15 +72,20 @@ class NeighbourListEngine:
         self.i = torch.empty(capacity, dtype=self.ti, device=self.device)
         self.j = torch.empty(capacity, dtype=self.ti, device=self.device)
         self.S = torch.empty((capacity, 3), dtype=self.ti, device=self.device)
-        self.R = torch.empty((capacity, 3), dtype=torch.float64, device=self.device) if self.with_R else None
+        self.R = torch.empty((capacity, 3), dtype=self.dtype, device=self.device) if self.with_R else None
 
     def _call(self, X: torch.Tensor, total_ptr, stream, outputs=None):
         p = self.plan
         check(lib().nl_set_tuning(C.byref(self.tuning)))
-        entry = lib().nl_neighbour_list_half if self.half else lib().nl_neighbour_list
+        if self.f32:
+            entry, fp = lib().nl_neighbour_list_f32, _F
+        else:
+            entry, fp = (lib().nl_neighbour_list_half if self.half else lib().nl_neighbour_list), _D
+        if X.dtype != self.dtype:
+            raise TypeError(f"positions must be {self.dtype}")
         i, j, S, R, cap = outputs if outputs is not None else (self.i, self.j, self.S, self.R, self.capacity)
         return entry(
-            _ptr(X), self.nat, p.cell_cm.ctypes.data_as(_D), p.inv_cm.ctypes.data_as(_D), p.ncells.ctypes.data_as(_I64),
+            _ptr(X), self.nat, p.cell_cm.ctypes.data_as(fp), p.inv_cm.ctypes.data_as(fp), p.ncells.ctypes.data_as(_I64),
             p.nxyz.ctypes.data_as(_I64), self.pbc.ctypes.data_as(_U8), self.cutoff, self.ib, _ptr(self.perm),
             _ptr(self.Xs), _ptr(self.cid), C.c_void_p(self.offs.data_ptr()), C.c_void_p(self.first.data_ptr()),
             cap, _ptr(i), _ptr(j), _ptr(S), _ptr(R), total_ptr, _ptr(self.ws),
@@ -127,7 +142,7 @@ class NeighbourListEngine:
         finished outputs."""
         main = stream if stream is not None else torch.cuda.current_stream(self.device)
         if getattr(self, "_Xdev", None) is None or self._Xdev.shape[0] != self.nat:
-            self._Xdev = torch.empty((self.nat, 3), dtype=torch.float64, device=self.device)
+            self._Xdev = torch.empty((self.nat, 3), dtype=self.dtype, device=self.device)
         if direct:
             P = out["i"].shape[0]
             for key in ("i", "j", "S", "R"):

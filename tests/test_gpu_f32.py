@@ -121,3 +121,26 @@ def test_bad_positions_raise(nlpkg):
     X = torch.tensor([[1.0, 2.0, 3.0], [float("inf"), 0.0, 0.0]], dtype=torch.float32, device="cuda")
     with pytest.raises(nlpkg.NLError):
         nlpkg.build_cell_list(X, 2.0, np.diag([10.0] * 3), (True, True, True))
+
+
+def test_engine_float32(nlpkg, orc):
+    """The resident pipeline (nl_neighbour_list_f32, no host synchronisation)
+    gives the same arrays, also when captured in a CUDA graph."""
+    X, C, L = cf.rand_config(5000, seed=66)
+    X32 = np.ascontiguousarray(X.astype(np.float32))
+    o = orc.neighbour_list_f32(X32, 5.0, C, (1, 1, 1))
+    Xd = torch.from_numpy(X32).cuda()
+    eng = nlpkg.NeighbourListEngine(X.shape[0], C, 5.0, (True, True, True), dtype=torch.float32)
+    assert eng.run(Xd) == o.npairs
+    for _ in range(2):
+        g = eng.pairlist(Xd)
+        np.testing.assert_array_equal(to_np(g.first).astype(np.int64), o.first)
+        np.testing.assert_array_equal(to_np(g.j).astype(np.int64), o.j)
+        np.testing.assert_array_equal(to_np(g.S).astype(np.int64), o.S)
+        assert np.array_equal(to_np(g.R).view(np.int32), o.R.view(np.int32))
+        eng.R.zero_()
+        eng.capture(Xd)
+        eng.replay()
+        torch.cuda.synchronize()
+    with pytest.raises(TypeError):
+        eng.launch(Xd.double())
