@@ -116,77 +116,209 @@ __global__ void __launch_bounds__(256) k_prepare32(Geo32 g, const float* __restr
   }
 }
 
-// One thread per sorted slot (home atom i): the reference's traversal of
-// _for_each_neighbor_pair -- stencil dz, dy, dx (dx fastest), each cell's
-// atoms in sorted order, skipping i itself at zero cell shift -- with
-// S = s_loop + wi - wj, R = (xj - xi) + C'S and dot(R, R) < cutoff^2 in FP32.
-// C'S is formed once per stencil cell for wj = 0 and again for the rare
-// candidates with a non-zero winding.  Count: pairs per atom.  Fill: i, j,
-// S, R at first[i] in traversal order.
+constexpr int kW32Warps = 4;    // warps per block of the pair kernel
+// candidates held per lane (a tile is 32 times that) and resident blocks per
+// SM the register budget is sized for, for the count and the fill kernels
+#ifndef NL_F32_PER_COUNT
+#define NL_F32_PER_COUNT 2
+#endif
+#ifndef NL_F32_MIN_COUNT
+#define NL_F32_MIN_COUNT 8
+#endif
+#ifndef NL_F32_PER_FILL
+#define NL_F32_PER_FILL 4
+#endif
+#ifndef NL_F32_MIN_FILL
+#define NL_F32_MIN_FILL 4
+#endif
+
+// A staged candidate's tag: s_loop + 128 in three 8-bit fields, bit 24 =
+// (s_loop == 0), bit 25 = (the candidate has a winding), bit 26 = valid.
+constexpr unsigned kTagLoopZero = 1u << 24;
+constexpr unsigned kTagWound = 1u << 25;
+constexpr unsigned kTagValid = 1u << 26;
+
+struct Shared32 {
+  float hx[32], hy[32], hz[32];  // home atoms of the group
+  int hw[32][3];                 // their windings
+  int hid[32];                   // their 1-based original indices
+  int incl[32];                  // stencil chunk: inclusive candidate counts
+  int start[32];                 // first sorted slot of the cell
+  unsigned loop[32];             // s_loop + 128 packed in 8-bit fields
+  float lc[3][32];               // C' s_loop
+};
+
+__device__ __forceinline__ int tag_s(unsigned t, int k) { return int((t >> (8 * k)) & 255u) - 128; }
+
+// One warp per home cell.  The candidates of the cell's stencil -- cells in
+// the reference's order dz, dy, dx (dx fastest), each cell's atoms in sorted
+// order -- are taken a tile at a time into registers (kW32Per per lane,
+// candidate r*32 + lane); every home atom of the cell (groups of 32, read by
+// broadcast from shared memory) is tested against them in that order:
+// S = s_loop + wi - wj, R = (xj - xi) + C'S, dot(R, R) < cutoff^2, all in
+// FP32 with the reference's operation order, skipping i itself at zero cell
+// shift (gpu_kernels.jl:58-101).  Count: pairs per atom.  Fill: accepted
+// pairs are ballot-compacted to consecutive positions from first[i], so each
+// atom's pairs are in the reference's traversal order.
 template <typename TI, bool FILL>
-__global__ void __launch_bounds__(256) k_pairs32(Pairs32Args<TI> a) {
+__global__ void __launch_bounds__(kW32Warps * 32, FILL ? NL_F32_MIN_FILL : NL_F32_MIN_COUNT)
+    k_pairs32(Pairs32Args<TI> a) {
+  constexpr int kW32Per = FILL ? NL_F32_PER_FILL : NL_F32_PER_COUNT;
+  constexpr int kW32Tile = 32 * kW32Per;
+  __shared__ Shared32 sh_all[kW32Warps];
+  const int lane = threadIdx.x & 31;
+  Shared32& W = sh_all[threadIdx.x >> 5];
   const Geo32& g = a.g;
-  const unsigned wzero = pack10(kW32Bias, kW32Bias, kW32Bias);
-  for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < g.nat;
-       s += (long long)gridDim.x * blockDim.x) {
-    const float4 ri = a.rec[s];
-    const unsigned mi = __float_as_uint(ri.w);
-    const int wi0 = field10(mi, 0) - kW32Bias, wi1 = field10(mi, 1) - kW32Bias, wi2 = field10(mi, 2) - kW32Bias;
-    const int c = a.scell[s];
-    const int ci0 = c % g.ns[0] + 1, ci1 = (c / g.ns[0]) % g.ns[1] + 1, ci2 = c / (g.ns[0] * g.ns[1]) + 1;
-    const TI iorig = a.perm[s];
-    long long pos = 0, end = 0;
-    bool write_ok = false;
-    int count = 0;
-    if constexpr (FILL) {
-      pos = (long long)a.first[iorig - 1] - 1;
-      end = (long long)a.first[iorig] - 1;
-      write_ok = pos >= 0 && end >= pos && end <= a.capacity;
-      if (!write_ok) atomicOr(a.err, kFlagCapacity);
-    }
-    for (int dz = -g.nxyz[2]; dz <= g.nxyz[2]; ++dz) {
-      if (!g.pbc[2] && (ci2 + dz < 1 || ci2 + dz > g.ns[2])) continue;
-      int sz;
-      const int cz = wrap_shift(ci2 + dz, g.ns[2], g.pbc[2], sz);
-      for (int dy = -g.nxyz[1]; dy <= g.nxyz[1]; ++dy) {
-        if (!g.pbc[1] && (ci1 + dy < 1 || ci1 + dy > g.ns[1])) continue;
-        int sy;
-        const int cy = wrap_shift(ci1 + dy, g.ns[1], g.pbc[1], sy);
-        for (int dx = -g.nxyz[0]; dx <= g.nxyz[0]; ++dx) {
-          if (!g.pbc[0] && (ci0 + dx < 1 || ci0 + dx > g.ns[0])) continue;
-          int sx;
-          const int cx = wrap_shift(ci0 + dx, g.ns[0], g.pbc[0], sx);
-          const int lin = (cx - 1) + g.ns[0] * ((cy - 1) + g.ns[1] * (cz - 1));
-          const long long beg = (long long)a.cell_offsets[lin] - 1, fin = (long long)a.cell_offsets[lin + 1] - 1;
-          if (beg >= fin) continue;
-          const int Sb0 = sx + wi0, Sb1 = sy + wi1, Sb2 = sz + wi2;
-          const float cb0 = cts32(g.C, Sb0, Sb1, Sb2, 0);
-          const float cb1 = cts32(g.C, Sb0, Sb1, Sb2, 1);
-          const float cb2 = cts32(g.C, Sb0, Sb1, Sb2, 2);
-          const bool zero_loop = (sx | sy | sz) == 0;
-          for (long long idx = beg; idx < fin; ++idx) {
-            if (zero_loop && idx == s) continue;
-            const float4 rj = a.rec[idx];
-            const unsigned mj = __float_as_uint(rj.w);
-            int S0 = Sb0, S1 = Sb1, S2 = Sb2;
-            float e0 = cb0, e1 = cb1, e2 = cb2;
-            if ((mj & kMetaFields) != wzero) {
-              S0 -= field10(mj, 0) - kW32Bias;
-              S1 -= field10(mj, 1) - kW32Bias;
-              S2 -= field10(mj, 2) - kW32Bias;
-              e0 = cts32(g.C, S0, S1, S2, 0);
-              e1 = cts32(g.C, S0, S1, S2, 1);
-              e2 = cts32(g.C, S0, S1, S2, 2);
+  const unsigned lt = lanemask_lt();
+  const int wx = 2 * g.nxyz[0] + 1, wy = 2 * g.nxyz[1] + 1;
+  const int nst = wx * wy * (2 * g.nxyz[2] + 1);
+  const int nwarps = gridDim.x * kW32Warps;
+
+  for (int cell = blockIdx.x * kW32Warps + (threadIdx.x >> 5); cell < g.ncells; cell += nwarps) {
+    const int hs = int(a.cell_offsets[cell]) - 1, he = int(a.cell_offsets[cell + 1]) - 1;
+    if (hs >= he) continue;
+    const int ci[3] = {cell % g.ns[0] + 1, (cell / g.ns[0]) % g.ns[1] + 1, cell / (g.ns[0] * g.ns[1]) + 1};
+    for (int h0 = hs; h0 < he; h0 += 32) {
+      const int nh = min(32, he - h0);
+      // this lane's home atom: running count (fill: write offset) and range
+      int hcount = 0, hn = 0;
+      long long hbase = 0;
+      bool hok = false;
+      __syncwarp();
+      if (lane < nh) {
+        const float4 rh = a.rec[h0 + lane];
+        const unsigned mh = __float_as_uint(rh.w);
+        const int id = int(a.perm[h0 + lane]);
+        W.hx[lane] = rh.x;
+        W.hy[lane] = rh.y;
+        W.hz[lane] = rh.z;
+        W.hw[lane][0] = field10(mh, 0) - kW32Bias;
+        W.hw[lane][1] = field10(mh, 1) - kW32Bias;
+        W.hw[lane][2] = field10(mh, 2) - kW32Bias;
+        W.hid[lane] = id;
+        if constexpr (FILL) {
+          hbase = (long long)a.first[id - 1] - 1;
+          hn = int((long long)a.first[id] - 1 - hbase);
+          hok = hbase >= 0 && hn >= 0 && hbase + hn <= a.capacity;
+          if (!hok) atomicOr(a.err, kFlagCapacity);
+        }
+      }
+      __syncwarp();
+      for (int q0 = 0; q0 < nst; q0 += 32) {
+        // stencil chunk: one cell per lane
+        const int q = q0 + lane;
+        bool valid = q < nst;
+        const int d[3] = {q % wx - g.nxyz[0], (q / wx) % wy - g.nxyz[1], q / (wx * wy) - g.nxyz[2]};
+        int cj[3], sl[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          if (!g.pbc[k] && (ci[k] + d[k] < 1 || ci[k] + d[k] > g.ns[k])) valid = false;
+          cj[k] = wrap_shift(ci[k] + d[k], g.ns[k], g.pbc[k], sl[k]);
+        }
+        int st = 0, cnt = 0;
+        if (valid) {
+          const int lin = (cj[0] - 1) + g.ns[0] * ((cj[1] - 1) + g.ns[1] * (cj[2] - 1));
+          st = int(a.cell_offsets[lin]) - 1;
+          cnt = int(a.cell_offsets[lin + 1]) - 1 - st;
+        }
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int v = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += v;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        if (total == 0) continue;
+        __syncwarp();
+        W.incl[lane] = incl;
+        W.start[lane] = st;
+        W.loop[lane] = (unsigned(sl[0] + 128) & 255u) | ((unsigned(sl[1] + 128) & 255u) << 8) |
+                       ((unsigned(sl[2] + 128) & 255u) << 16);
+        W.lc[0][lane] = valid ? cts32(g.C, sl[0], sl[1], sl[2], 0) : 0.f;
+        W.lc[1][lane] = valid ? cts32(g.C, sl[0], sl[1], sl[2], 1) : 0.f;
+        W.lc[2][lane] = valid ? cts32(g.C, sl[0], sl[1], sl[2], 2) : 0.f;
+        __syncwarp();
+        for (int t0 = 0; t0 < total; t0 += kW32Tile) {
+          // this lane's candidates t0 + r*32 + lane, in registers
+          float cxr[kW32Per], cyr[kW32Per], czr[kW32Per], ex[kW32Per], ey[kW32Per], ez[kW32Per];
+          unsigned tag[kW32Per];
+          int jor[kW32Per], jslot[kW32Per];
+#pragma unroll
+          for (int r = 0; r < kW32Per; ++r) {
+            const int p = t0 + r * 32 + lane;
+            tag[r] = 0u;
+            cxr[r] = cyr[r] = czr[r] = ex[r] = ey[r] = ez[r] = 0.f;
+            jor[r] = jslot[r] = 0;
+            if (p < total) {
+              int lo = 0, hi = 31;  // first stencil lane whose inclusive count exceeds p
+              while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (W.incl[mid] > p)
+                  hi = mid;
+                else
+                  lo = mid + 1;
+              }
+              const int js = W.start[lo] + (p - (lo ? W.incl[lo - 1] : 0));
+              const float4 rj = a.rec[js];
+              const unsigned lp = W.loop[lo];
+              const bool wound = (__float_as_uint(rj.w) & kMetaFields) != pack10(kW32Bias, kW32Bias, kW32Bias);
+              cxr[r] = rj.x;
+              cyr[r] = rj.y;
+              czr[r] = rj.z;
+              ex[r] = W.lc[0][lo];
+              ey[r] = W.lc[1][lo];
+              ez[r] = W.lc[2][lo];
+              jor[r] = int(a.perm[js]);
+              jslot[r] = js;
+              tag[r] = lp | (lp == 0x808080u ? kTagLoopZero : 0u) | (wound ? kTagWound : 0u) | kTagValid;
             }
-            const float R0 = fadd(fsub(rj.x, ri.x), e0);
-            const float R1 = fadd(fsub(rj.y, ri.y), e1);
-            const float R2 = fadd(fsub(rj.z, ri.z), e2);
-            const float r2 = fadd(fadd(fmul(R0, R0), fmul(R1, R1)), fmul(R2, R2));
-            if (r2 < g.cutoff_sq) {
+          }
+          for (int h = 0; h < nh; ++h) {
+            const float xi = W.hx[h], yi = W.hy[h], zi = W.hz[h];
+            const int wi0 = W.hw[h][0], wi1 = W.hw[h][1], wi2 = W.hw[h][2];
+            const int iid = W.hid[h];
+            const bool hwound = (wi0 | wi1 | wi2) != 0;
+            int off = 0, nmax = 0;
+            long long base = 0;
+            bool ok = false;
+            if constexpr (FILL) {
+              off = __shfl_sync(0xffffffffu, hcount, h);
+              nmax = __shfl_sync(0xffffffffu, hn, h);
+              base = __shfl_sync(0xffffffffu, hbase, h);
+              ok = __shfl_sync(0xffffffffu, hok ? 1 : 0, h) != 0;
+            }
+            int added = 0;
+#pragma unroll
+            for (int r = 0; r < kW32Per; ++r) {
+              if (t0 + r * 32 >= total) break;  // warp-uniform
+              const unsigned tg = tag[r];
+              bool acc = false;
+              float R0 = 0.f, R1 = 0.f, R2 = 0.f;
+              int S0 = tag_s(tg, 0), S1 = tag_s(tg, 1), S2 = tag_s(tg, 2);
+              if ((tg & kTagValid) && !((tg & kTagLoopZero) && jor[r] == iid)) {
+                float e0 = ex[r], e1 = ey[r], e2 = ez[r];
+                if (hwound || (tg & kTagWound)) {  // S = s_loop + wi - wj, C'S again
+                  const unsigned mj = __float_as_uint(a.rec[jslot[r]].w);
+                  S0 += wi0 - (field10(mj, 0) - kW32Bias);
+                  S1 += wi1 - (field10(mj, 1) - kW32Bias);
+                  S2 += wi2 - (field10(mj, 2) - kW32Bias);
+                  e0 = cts32(g.C, S0, S1, S2, 0);
+                  e1 = cts32(g.C, S0, S1, S2, 1);
+                  e2 = cts32(g.C, S0, S1, S2, 2);
+                }
+                R0 = fadd(fsub(cxr[r], xi), e0);
+                R1 = fadd(fsub(cyr[r], yi), e1);
+                R2 = fadd(fsub(czr[r], zi), e2);
+                const float r2 = fadd(fadd(fmul(R0, R0), fmul(R1, R1)), fmul(R2, R2));
+                acc = r2 < g.cutoff_sq;
+              }
+              const unsigned mask = __ballot_sync(0xffffffffu, acc);
               if constexpr (FILL) {
-                if (write_ok && pos < end) {
-                  a.oi[pos] = iorig;
-                  a.oj[pos] = a.perm[idx];
+                const int k = off + added + __popc(mask & lt);
+                if (acc && ok && k < nmax) {
+                  const long long pos = base + k;
+                  a.oi[pos] = TI(iid);
+                  a.oj[pos] = TI(jor[r]);
                   a.oS[3 * pos + 0] = TI(S0);
                   a.oS[3 * pos + 1] = TI(S1);
                   a.oS[3 * pos + 2] = TI(S2);
@@ -196,19 +328,20 @@ __global__ void __launch_bounds__(256) k_pairs32(Pairs32Args<TI> a) {
                     a.oR[3 * pos + 2] = R2;
                   }
                 }
-                ++pos;
-              } else {
-                ++count;
               }
+              added += __popc(mask);
             }
+            if (lane == h) hcount += added;
           }
         }
       }
-    }
-    if constexpr (FILL) {
-      if (write_ok && pos != end) atomicOr(a.err, kFlagInconsistent);
-    } else {
-      a.counts[iorig - 1] = count;
+      if (lane < nh) {
+        if constexpr (FILL) {
+          if (hok && hcount != hn) atomicOr(a.err, kFlagInconsistent);
+        } else {
+          a.counts[W.hid[lane] - 1] = hcount;
+        }
+      }
     }
   }
 }
@@ -231,11 +364,11 @@ void launch_prepare32(const Geo32& g, const float* Xs, const TI* cell_id, const 
 template <typename TI>
 void launch_pairs32(bool fill, const Pairs32Args<TI>& a, int num_sms, cudaStream_t st) {
   if (a.g.nat <= 0) return;
-  const int grid = grid_for(a.g.nat, 128, num_sms * 16);
+  const int grid = grid_for(a.g.ncells, kW32Warps, num_sms * 12);
   if (fill)
-    k_pairs32<TI, true><<<grid, 128, 0, st>>>(a);
+    k_pairs32<TI, true><<<grid, kW32Warps * 32, 0, st>>>(a);
   else
-    k_pairs32<TI, false><<<grid, 128, 0, st>>>(a);
+    k_pairs32<TI, false><<<grid, kW32Warps * 32, 0, st>>>(a);
 }
 
 #define NL_INST(TI)                                                                                                 \
