@@ -227,3 +227,36 @@ def test_golden_fixtures(orc):
         X, C, pbc, rc = golden_io.digest_input(dig)
         out = orc.neighbour_list(X, rc, C, pbc, nthreads=4)
         assert golden_io.digest(out) == dig["sha256"], dig["name"]
+
+
+# ------------------------------------------------------------ T = Float32 --
+def test_f32_known_answers(orc):
+    """The known answers of the reference's tests hold for the Float32
+    restatement: FCC Cu coordination 12, diamond primitive cell 92 pairs
+    (46 per atom) with rc larger than the cell, isolated H3."""
+    X, C = cf.fcc_cubic(3.61, (3, 3, 3))
+    assert np.all(np.diff(orc.neighbour_list_f32(X, 3.5, C, (1, 1, 1)).first) == 12)
+    assert orc.neighbour_list_f32(X, 1.0, C, (1, 1, 1)).npairs == 0
+    X, C = cf.diamond_primitive()
+    nl = orc.neighbour_list_f32(X, 6.0, C, (1, 1, 1))
+    assert nl.npairs == 92 and list(np.diff(nl.first)) == [46, 46]
+    X = np.array([[0.0, 0.0, 0.0], [0.0, 0.0, 2.0], [0.0, 10.0, 0.0]])
+    nl = orc.neighbour_list_f32(X, 5.0, np.diag(X.max(0) - X.min(0) + 1), (0, 0, 0))
+    assert nl.j.tolist() == [2, 1] and nl.R.tolist() == [[0.0, 0.0, 2.0], [0.0, 0.0, -2.0]]
+
+
+@pytest.mark.parametrize("pbc", cf.ALL_PBC)
+def test_f32_equals_f64_sets(orc, pbc):
+    """Away from the cutoff, the Float32 and Float64 lists hold the same
+    (i, j, S) for the same (Float32-representable) positions."""
+    X, C, L = cf.rand_config(400, seed=71)
+    X = X.astype(np.float32).astype(np.float64)
+    a = orc.neighbour_list_f32(X, 0.3 * L, C, pbc)
+    b = orc.neighbour_list(X, 0.3 * L, C, pbc)
+    r = np.linalg.norm(b.R, axis=1)
+    near = np.abs(r - 0.3 * L) < 1e-4 * L
+    key = lambda nl, m: set(zip(nl.i[m].tolist(), nl.j[m].tolist(), *[nl.S[m, k].tolist() for k in range(3)]))
+    ra = np.linalg.norm(a.R.astype(np.float64), axis=1)
+    assert key(a, np.abs(ra - 0.3 * L) >= 1e-4 * L) == key(b, ~near)
+    # the sorted cell lists agree too (binning away from cell faces)
+    assert np.array_equal(a.cell_offsets, orc.build_cell_list(X, 0.3 * L, C, pbc).cell_offsets)
