@@ -588,6 +588,47 @@ def measure_e2e(eng, X, Xd, total, stream, dev, args):
             "ms_per_step": e2e_ms, "api": "NeighbourListEngine.launch_host, two engines taking steps in turn"}
 
 
+def run_path(args):
+    """Profiling runs of the Float32 and legacy paths on the benchmark's
+    workload shape (``--atoms`` sets the size).  Prints one JSON line that is
+    not the benchmark line."""
+    import time
+
+    import torch
+
+    import __graft_entry__ as graft
+
+    nl = graft.load_package()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    X, C, pbc = workload(args.atoms)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    steps = max(args.steps, 1)
+    if args.path == "float32":
+        X32 = torch.from_numpy(X.astype(np.float32)).to(dev)
+        eng = nl.NeighbourListEngine(X.shape[0], C, CUTOFF, pbc, device=dev, dtype=torch.float32)
+        total = eng.run(X32)
+        for _ in range(args.warmup):
+            eng.launch(X32)
+        ms = timed_steps(lambda: eng.launch(X32), steps, flush, stream)
+        eng.sync_status()
+        out = {"pairs": int(total), "ms_per_step": ms, "timing": "CUDA events, L2 flushed before every step"}
+    else:
+        Xd = torch.from_numpy(X).to(dev)
+        for _ in range(args.warmup):
+            nl.legacy_pairlist(Xd, CUTOFF, C, pbc)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            lg = nl.legacy_pairlist(Xd, CUTOFF, C, pbc)
+        torch.cuda.synchronize(dev)
+        out = {"pairs": int(lg.i.numel()), "ms_per_call": (time.perf_counter() - t0) / steps * 1e3,
+               "timing": "host clock around the whole synchronising call"}
+    print(json.dumps({"metric": "profiling run (not the benchmark line)", "path": args.path, "atoms": args.atoms,
+                      **out}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -598,9 +639,13 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the lazy / batched / 4M sections")
     ap.add_argument("--atoms", type=int, default=N_ATOMS, help="system size (profiling runs use a smaller one)")
+    ap.add_argument("--path", default="headline", choices=["headline", "float32", "legacy"],
+                    help="float32 / legacy: profiling runs of those paths (not the benchmark line)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.path != "headline":
+        run_path(args)
     else:
         run_gpu(args)
 

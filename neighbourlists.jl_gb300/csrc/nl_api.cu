@@ -638,7 +638,10 @@ nl::LegacyGeo legacy_geo(const double* cell, const double* inv, const int64_t* n
   std::memcpy(g.inv, inv, sizeof(g.inv));
   double offmax = 0;
   for (int k = 0; k < 3; ++k)
-    for (int r = 0; r < 3; ++r) g.bins[r + 3 * k] = cell[k + 3 * r] / double(ns[k]);
+    for (int r = 0; r < 3; ++r) {
+      g.bins[r + 3 * k] = cell[k + 3 * r] / double(ns[k]);
+      g.binsf[r + 3 * k] = float(g.bins[r + 3 * k]);
+    }
   for (int r = 0; r < 3; ++r) {
     double m = 0;
     for (int k = 0; k < 3; ++k) m += std::fabs(g.bins[r + 3 * k]) * double(nxyz[k]);

@@ -187,7 +187,12 @@ __global__ void __launch_bounds__(256) k_legacy_prepare(LegacyArgs<TI> a) {
         const unsigned b = __float_as_uint(__double2float_ru(fabs(D[r])));
         m = b > m ? b : m;
       }
-      a.Df[s] = make_float4(__double2float_rn(D[0]), __double2float_rn(D[1]), __double2float_rn(D[2]), 0.f);
+      bool inbox = true;  // then bin_trunc(c0) is the bin the atom was listed in
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+        if (g.pbc[k] && (c0[k] < 1 || c0[k] > g.ns[k])) inbox = false;
+      a.Df[s] = make_float4(__double2float_rn(D[0]), __double2float_rn(D[1]), __double2float_rn(D[2]),
+                            inbox ? 1.f : 0.f);
       a.c0[s] = make_int4(c0[0], c0[1], c0[2], 0);
     }
     m = __reduce_max_sync(0xffffffffu, m);
@@ -201,6 +206,7 @@ struct LegacyChunk {
   int start[32];    // first sorted slot of the cell
   int q[32];        // stencil index (dx fastest, then dy, dz: CartesianIndices order)
   float off[3][32]; // bins * xyz in FP32
+  int S[3][32];     // (ci0 - cj + xyz) .÷ ns for the bin cj itself (S of the candidates inside the box)
 };
 struct LegacyStage {
   int j[kLegacyStage];     // 1-based original index of j (also the rank tile of long lists)
@@ -228,13 +234,14 @@ __global__ void __launch_bounds__(kLegacyWarps * 32) k_legacy_pairs(LegacyArgs<T
   const LegacyGeo& g = a.g;
 
   // FP32 screen band.  With u = 2^-24, M = max |D_r| and O = max |off_r|,
-  // each FP32 component of dx is within e = 4u (2M + O) of the exact
-  // (D_j - D_i) + off; a candidate whose FP32 r^2 is outside
-  // cutoff^2 -+ B, B = 2 (4u cutoff^2 + 2 sqrt(3) (cutoff + e) e + 3 e^2),
-  // is decided the same way by the reference's FP64 arithmetic.
+  // the FP32 offset (two FMAs on the FP32 bins) is within 4u O of the
+  // reference's FP64 bins * xyz, and each FP32 component of dx is within
+  // e = 6u (2M + O) of the exact (D_j - D_i) + off; a candidate whose FP32
+  // r^2 is outside cutoff^2 -+ B, B = 2 (4u cutoff^2 + 2 sqrt(3) (cutoff + e) e
+  // + 3 e^2), is decided the same way by the reference's FP64 arithmetic.
   const double u = 5.9604644775390625e-08;
   const double M = double(__uint_as_float(*a.dmax));
-  const double e = 4.0 * u * (2.0 * M + g.offmax) * 1.0001;
+  const double e = 6.0 * u * (2.0 * M + g.offmax) * 1.0001;
   const double B = 2.0 * (4.0 * u * g.cutoff_sq + 3.4641016151377544 * (g.cutoff + e) * e + 3.0 * e * e);
   const float lo = __double2float_rd(g.cutoff_sq - B);
   const float hi = __double2float_ru(g.cutoff_sq + B);
@@ -286,13 +293,18 @@ __global__ void __launch_bounds__(kLegacyWarps * 32) k_legacy_pairs(LegacyArgs<T
         }
         int st = 0, cnt = 0;
         float o0 = 0.f, o1 = 0.f, o2 = 0.f;
+        int s0 = 0, s1 = 0, s2 = 0;
         if (valid) {
           const int lin = (cj[0] - 1) + g.ns[0] * ((cj[1] - 1) + g.ns[1] * (cj[2] - 1));
           st = a.cell_start[lin];
           cnt = a.cell_start[lin + 1] - st;
-          o0 = __double2float_rn(bins_mul(g.bins, 0, x, y, z));
-          o1 = __double2float_rn(bins_mul(g.bins, 1, x, y, z));
-          o2 = __double2float_rn(bins_mul(g.bins, 2, x, y, z));
+          const float fx = float(x), fy = float(y), fz = float(z);
+          o0 = fmaf(g.binsf[6], fz, fmaf(g.binsf[3], fy, g.binsf[0] * fx));
+          o1 = fmaf(g.binsf[7], fz, fmaf(g.binsf[4], fy, g.binsf[1] * fx));
+          o2 = fmaf(g.binsf[8], fz, fmaf(g.binsf[5], fy, g.binsf[2] * fx));
+          s0 = (ci0[0] - cj[0] + x) / g.ns[0];
+          s1 = (ci0[1] - cj[1] + y) / g.ns[1];
+          s2 = (ci0[2] - cj[2] + z) / g.ns[2];
         }
         int incl = cnt;
 #pragma unroll
@@ -307,12 +319,15 @@ __global__ void __launch_bounds__(kLegacyWarps * 32) k_legacy_pairs(LegacyArgs<T
         W.off[0][lane] = o0;
         W.off[1][lane] = o1;
         W.off[2][lane] = o2;
+        W.S[0][lane] = s0;
+        W.S[1][lane] = s1;
+        W.S[2][lane] = s2;
         __syncwarp();
         const int total = __shfl_sync(0xffffffffu, incl, 31);
 
         for (int p0 = 0; p0 < total; p0 += 32) {
           const int p = p0 + lane;
-          bool acc = false, rechk = false;
+          bool acc = false, rechk = false, jin = false;
           int js = 0, owner = 0;
           if (p < total) {
             int lo_l = 0, hi_l = 31;  // first lane whose inclusive count exceeds p
@@ -327,6 +342,7 @@ __global__ void __launch_bounds__(kLegacyWarps * 32) k_legacy_pairs(LegacyArgs<T
             js = W.start[owner] + (p - (owner ? W.incl[owner - 1] : 0));
             if (!(js == slot && W.q[owner] == qcenter)) {
               const float4 dj = a.Df[js];
+              jin = dj.w != 0.f;
               const float d0 = (dj.x - dfi.x) + W.off[0][owner];
               const float d1 = (dj.y - dfi.y) + W.off[1][owner];
               const float d2 = (dj.z - dfi.z) + W.off[2][owner];
@@ -353,14 +369,20 @@ __global__ void __launch_bounds__(kLegacyWarps * 32) k_legacy_pairs(LegacyArgs<T
             const int pos = nacc + __popc(mask & lanemask_lt());
             if (acc) {
               jo = int(a.perm[js]);
-              const int qo = W.q[owner];
-              const int oxyz[3] = {qo % wx - g.nxyz[0], (qo / wx) % wy - g.nxyz[1], (qo / wx) / wy - g.nxyz[2]};
-              const int4 c0j = a.c0[js];
-              const int cjp[3] = {c0j.x, c0j.y, c0j.z};
+              if (jin) {  // bin_trunc(c0_j) is the bin itself
+                S[0] = W.S[0][owner];
+                S[1] = W.S[1][owner];
+                S[2] = W.S[2][owner];
+              } else {
+                const int qo = W.q[owner];
+                const int oxyz[3] = {qo % wx - g.nxyz[0], (qo / wx) % wy - g.nxyz[1], (qo / wx) / wy - g.nxyz[2]};
+                const int4 c0j = a.c0[js];
+                const int cjp[3] = {c0j.x, c0j.y, c0j.z};
 #pragma unroll
-              for (int k = 0; k < 3; ++k) {
-                const int ct = g.pbc[k] ? cjp[k] : clampi(cjp[k], 1, g.ns[k]);
-                S[k] = (ci0[k] - ct + oxyz[k]) / g.ns[k];  // truncating, like Julia's div (:358)
+                for (int k = 0; k < 3; ++k) {
+                  const int ct = g.pbc[k] ? cjp[k] : clampi(cjp[k], 1, g.ns[k]);
+                  S[k] = (ci0[k] - ct + oxyz[k]) / g.ns[k];  // truncating, like Julia's div (:358)
+                }
               }
             }
             if (staged) {

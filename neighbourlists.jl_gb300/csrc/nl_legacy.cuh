@@ -19,6 +19,7 @@ namespace nl {
 struct LegacyGeo {
   double inv[9];    // inv(cell), column-major
   double bins[9];   // bins[r + 3k] = cell[k, r] / ns[k]: column k is lattice vector k / ns[k]
+  float binsf[9];   // bins rounded to FP32 (the screen's stencil offsets)
   double cutoff_sq; // cutoff^2 (cutoff * cutoff)
   double cutoff;
   double offmax;    // bound on |(bins * xyz)_r| over the stencil
@@ -36,7 +37,7 @@ struct LegacyArgs {
   const TI* perm;          // sorted slot -> 1-based original index
   const int* cell_start;   // 0-based CSR over cells (ncells + 1)
   double* D;               // per slot: position relative to the lower corner of its (clamped) bin, 3 doubles
-  float4* Df;              // per slot: D rounded to FP32
+  float4* Df;              // per slot: D rounded to FP32; w = 1 when c0 lies in the box on every periodic axis
   int4* c0;                // per slot: unwrapped cell index floor(frac * ns + 1)
   unsigned* dmax;          // max |D_r| over the atoms, FP32 bits rounded up
   int* counts;             // count: pairs per original atom (0-based)

@@ -200,13 +200,13 @@ def test_screen_band_bounds_fp32_error(nlpkg, orc, case):
 
 # ---------------------------------------------------------- legacy screen --
 def _legacy_band(cell_cm, ns, nxyz, rc, Df):
-    """The legacy kernel's band (nl_legacy.cu): e = 4u(2M + O), B = 2(4u rc^2
+    """The legacy kernel's band (nl_legacy.cu): e = 6u(2M + O), B = 2(4u rc^2
     + 2 sqrt(3)(rc + e) e + 3 e^2), M = max |D| in FP32 rounded up."""
     u = 2.0 ** -24
     bins = np.array([[cell_cm[k + 3 * r] / ns[k] for k in range(3)] for r in range(3)])  # bins[r, k]
     O = max(sum(abs(bins[r, k]) * nxyz[k] for k in range(3)) for r in range(3)) * (1 + 1e-12)
     M = float(np.max(np.abs(Df))) if Df.size else 0.0
-    e = 4 * u * (2 * M + O) * 1.0001
+    e = 6 * u * (2 * M + O) * 1.0001
     return bins, 2 * (4 * u * rc * rc + 2 * np.sqrt(3) * (rc + e) * e + 3 * e * e)
 
 
@@ -244,7 +244,12 @@ def test_legacy_screen_band_bounds_fp32_error(nlpkg, case):
                 off = np.array([(bins[r, 0] * x + bins[r, 1] * y) + bins[r, 2] * z for r in range(3)])
                 d64 = (D[None, :, :] - D[:, None, :]) + off
                 r64 = (d64[..., 0] * d64[..., 0] + d64[..., 1] * d64[..., 1]) + d64[..., 2] * d64[..., 2]
-                d32 = (Df[None, :, :] - Df[:, None, :]) + off.astype(np.float32)
+                # the kernel's FP32 offset: fma(b6, z, fma(b3, y, b0 * x)) on the FP32 bins
+                bf = bins.astype(np.float32)
+                off32 = np.array([np.float32(np.float64(bf[r, 2]) * z + np.float64(
+                    np.float32(np.float64(bf[r, 1]) * y + np.float64(np.float32(bf[r, 0] * np.float32(x))))))
+                    for r in range(3)], dtype=np.float32)
+                d32 = (Df[None, :, :] - Df[:, None, :]) + off32
                 r32 = (d32[..., 0] * d32[..., 0] + d32[..., 1] * d32[..., 1]) + d32[..., 2] * d32[..., 2]
                 near = r64 < 4 * rc * rc
                 err = np.abs(r32[near].astype(np.float64) - r64[near])
