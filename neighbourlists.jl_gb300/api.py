@@ -156,6 +156,14 @@ class SortedCellList:
     def index_bytes(self) -> int:
         return 4 if self.perm.dtype == torch.int32 else 8
 
+    def to(self, device) -> "SortedCellList":
+        """The arrays on another device (Adapt.adapt_structure, adapt.jl:20-33);
+        scalar and matrix fields are kept.  A list moved off the GPU is data
+        only: the engine's calls take CUDA tensors."""
+        return SortedCellList(self.X.to(device), self.X_orig.to(device), self.perm.to(device), self.cell_id.to(device),
+                              self.cell_offsets.to(device), self.cell.copy(), self.inv_cell.copy(), self.pbc,
+                              self.cutoff, self.ncells.copy(), self.ncells_total, self._plan, None, False)
+
 
 @dataclass
 class PairList:
@@ -177,6 +185,12 @@ class PairList:
         if self._first_host is None:
             self._first_host = self.first.cpu().numpy().astype(np.int64)
         return self._first_host
+
+    def to(self, device) -> "PairList":
+        """The arrays on another device (Adapt.adapt_structure, adapt.jl:35-44)."""
+        mv = lambda t: t.to(device) if t is not None else None
+        return PairList(mv(self.X), self.C.copy(), self.cutoff, mv(self.i), mv(self.j), mv(self.S), mv(self.first),
+                        mv(self.R), self.rechecks)
 
 
 # --------------------------------------------------------------- building --

@@ -315,3 +315,16 @@ def test_batch_plan_on_host(nlpkg):
     assert L.nl_batch_create(arr, 2, 4, C.byref(h)) == nlpkg._lib.NL_ERR_ARG
     assert b"system 1" in L.nl_last_error()
     assert L.nl_batch_create(arr, 0, 4, C.byref(h)) == nlpkg._lib.NL_ERR_ARG
+
+
+def test_lists_move_between_devices(nlpkg):
+    """PairList / SortedCellList .to(device) (the reference's Adapt rules,
+    adapt.jl:20-44) move every array field and keep the rest."""
+    import torch
+
+    P = nlpkg.PairList(torch.zeros((3, 3), dtype=torch.float64), np.eye(3), 2.0, torch.tensor([1, 1, 2], dtype=torch.int32),
+                       torch.tensor([2, 3, 1], dtype=torch.int32), torch.zeros((3, 3), dtype=torch.int32),
+                       torch.tensor([1, 3, 4, 4], dtype=torch.int32), torch.ones((3, 3), dtype=torch.float64))
+    Q = P.to("cpu")
+    assert Q.i.tolist() == [1, 1, 2] and Q.first.tolist() == [1, 3, 4, 4] and Q.cutoff == 2.0
+    assert nlpkg.nneigs(Q, 1) == 2 and nlpkg.npairs(Q) == 3
