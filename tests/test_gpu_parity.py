@@ -344,6 +344,36 @@ def test_both_count_kernels(nlpkg, orc, count_kernel):
         assert_identical(eng.pairlist(None), o)
 
 
+def test_count_pass_edge_cases(nlpkg, orc):
+    """Exact atoms far outside an open axis, lists that overflow (> 64 pairs:
+    those cells go to the screening write pass) next to cells that do not, a
+    crowded cell, open boundaries, Int64; and the two count tilings giving
+    identical lists on 20k atoms."""
+    rng = np.random.default_rng(54)
+    X, C, L = cf.rand_config(4000, seed=55)
+    Xo = X.copy()
+    Xo[:30, 2] += rng.choice([-1, 1], 30) * rng.uniform(2.0, 40.0, 30) * L  # far outside the open z axis
+    dense = np.concatenate([X, rng.random((40, 3)) * 0.5 + L / 2])              # one crowded cell
+    cases = [(X, C, 5.0, (True, True, True)), (Xo, C, 5.0, (True, True, False)), (X, C, 6.0, (True, True, True)),
+             (dense, C, 5.0, (True, True, True)), (X, C, 5.0, (False, False, False))]
+    for X_, C_, rc, pbc in cases:
+        for it in (torch.int32, torch.int64):
+            g = nlpkg.neighbour_list(torch.from_numpy(np.ascontiguousarray(X_)).cuda(), rc, C_, pbc, int_type=it)
+            o = orc.neighbour_list(X_, rc, C_, pbc, nthreads=8)
+            assert_identical(g, o)
+    X, C, L = cf.rand_config(20000, seed=56)
+    Xd = torch.from_numpy(X).cuda()
+    lists = []
+    for k in (2, 1):
+        eng = nlpkg.NeighbourListEngine(X.shape[0], C, 5.0, (True, True, True))
+        eng.set_tuning(0, 0, k)
+        eng.run(Xd)
+        lists.append(eng.pairlist(Xd))
+    for key in ("first", "i", "j", "S"):
+        assert torch.equal(getattr(lists[0], key), getattr(lists[1], key))
+    assert torch.equal(lists[0].R.view(torch.int64), lists[1].R.view(torch.int64))
+
+
 def test_system_entry_points(nlpkg, orc):
     """AtomsBase-style systems (ext/NeighbourListsAtomsBaseExt.jl): periodic
     cell with a unit scale, and an isolated cluster whose cell is its
