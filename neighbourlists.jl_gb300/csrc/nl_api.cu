@@ -411,6 +411,8 @@ nl::PairArgs<TI> pair_args(const nl::Geometry& g, const TI* cell_offsets, const 
   a.cs_table = at<double>(ws, L.cs_table);
   a.screen_cells = at<int>(ws, L.screen_cells);
   a.n_screen_cells = at<int>(ws, L.pcount) + 4;  // zeroed with the pair scan state
+  a.sym_fail = at<int>(ws, L.pcount) + 6;        // likewise
+  a.sym_wound = at<int>(ws, L.pcount) + 7;       // likewise
   a.cell_flag = at<int>(ws, L.cell_flag);     // likewise
   a.count_kernel = g_tuning.count_kernel;
   a.pair_blocks_per_sm = g_tuning.pair_blocks_per_sm;
@@ -418,6 +420,18 @@ nl::PairArgs<TI> pair_args(const nl::Geometry& g, const TI* cell_offsets, const 
   a.stats = at<unsigned long long>(ws, L.stats);
   a.err = at<unsigned>(ws, L.err);
   return a;
+}
+
+// The symmetric count pass and the mask write pass (nl_pairs.cu) apply to a
+// full list of a single system with per-atom lists in the workspace and a
+// 27-cell stencil of distinct cells (nxyz = 1, periodic axes of at least 3
+// cells); count_kernel 1 or 2 selects the per-cell / per-atom pass instead.
+bool use_sym(const nl::Geometry& g, const Layout& L, int half) {
+  // masks (27 words per atom) and the stencil table (54 words per cell) share the list region
+  const bool fits = 27.0 * g.nat + 54.0 * g.ncells <= 2.0 * nl::kListCap * g.nat;
+  bool sym = L.use_lists && fits && !half && g_tuning.count_kernel != 1 && g_tuning.count_kernel != 2;
+  for (int k = 0; k < 3; ++k) sym = sym && g.nxyz[k] == 1 && (!g.pbc[k] || g.ns[k] >= 3);
+  return sym;
 }
 
 template <typename TI>
@@ -440,6 +454,11 @@ int count_impl(const nl::Geometry& g, const double* Xs, const TI* perm, const TI
   nl::PairArgs<TI> a = pair_args<TI>(g, cell_offsets, perm, Xs, ws, L);
   a.counts = at<int>(ws, L.counts);
   a.half = half;
+  a.sym = use_sym(g, L, half) ? 1 : 0;
+  if (a.sym) {  // the symmetric pass accumulates the counts
+    e = cudaMemsetAsync(a.counts, 0, sizeof(int) * size_t(g.nat), st);
+    if (e != cudaSuccess) return cuda_fail(e, "memset counts");
+  }
   nl::launch_pairs<TI>(nl::kModeCount, a, sms, st);
   nl::launch_scan<TI>(at<int>(ws, L.counts), g.nat, first, nullptr, at<unsigned long long>(ws, L.st_pairs),
                       at<int>(ws, L.pcount), at<long long>(ws, L.totals) + 1, at<unsigned>(ws, L.err), st);
@@ -454,6 +473,7 @@ int fill_impl(const nl::Geometry& g, const double* Xs, const TI* perm, const TI*
   if (g.nat == 0 || capacity <= 0) return NL_OK;
   nl::PairArgs<TI> a = pair_args<TI>(g, cell_offsets, perm, Xs, ws, L);
   a.half = half;
+  a.sym = use_sym(g, L, half) ? 1 : 0;
   a.first = first;
   a.oi = oi;
   a.oj = oj;
@@ -1218,8 +1238,8 @@ int nl_batch_neighbour_list(const nl_batch* batch, const double* d_X, void* d_pe
 
 static int check_tuning(const nl_tuning* t) {
   if (t && (t->pair_blocks_per_sm < 0 || t->pair_blocks_per_sm > 256 || t->emit_blocks_per_sm < 0 ||
-            t->emit_blocks_per_sm > 256 || t->count_kernel < 0 || t->count_kernel > 2))
-    return fail(NL_ERR_ARG, "tuning out of range (0..256 blocks per SM, count kernel 0..2)");
+            t->emit_blocks_per_sm > 256 || t->count_kernel < 0 || t->count_kernel > 3))
+    return fail(NL_ERR_ARG, "tuning out of range (0..256 blocks per SM, count kernel 0..3)");
   return NL_OK;
 }
 

@@ -362,6 +362,7 @@ __device__ __forceinline__ void load_system(const PairArgs<TI>& A, int s, Geomet
 
 template <typename TI, int MODE, bool BATCH>
 __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<TI> A) {
+  if (MODE == kModeCount && A.sym && *A.sym_fail == 0) return;  // the symmetric pass counted
   __shared__ WarpSmem sm[kPairWarps];
   __shared__ double cs_blk[BATCH ? 1 : 3 * kCsN * kCsN * kCsN];
   __shared__ unsigned dtab_blk[BATCH ? 32 * kPairWarps : kStencilTab];  // packed (d0, d1, d2) of stencil cell q
@@ -728,6 +729,282 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
 }
 
 // ------------------------------------------------------------------------
+// Symmetric count pass (single systems whose 27-cell stencil has distinct
+// cells).  The reference decides (i, j, S) and (j, i, -S) identically:
+// R(j, i, -S) = -R(i, j, S) bit for bit under round-to-nearest, so dot(R, R)
+// is the same.  Each unordered pair of cells (A, A + d) is therefore
+// screened once, by the warp of A, for the centre and the 13 stencil offsets
+// after it.  An atom's accepted neighbours in stencil cell q are a 32-bit
+// mask over that cell's atoms in sorted order, stored densely (27 words per
+// atom, in the list region): the warp of A writes its atoms' words for
+// q >= 13 (rows) and, for every atom j of A + d, j's word for the mirrored
+// cell 26 - q (column: which atoms of A accepted j); words whose mirrored
+// cell is empty or outside an open axis are written as 0 by the atom's own
+// warp, so every word is written exactly once.  Pair counts accumulate with
+// atomics; k_emit<masks> decodes the masks in the reference's order (stencil
+// order, then sorted order in each cell).  A cell of more than 32 atoms sets
+// sym_fail, and the per-cell count pass with per-atom lists runs instead.
+constexpr int kSymWarps = 4;
+constexpr int kSymChunk = 128;  // staged candidates per round of home atoms
+// record meta of an atom without windings that is not exact
+constexpr unsigned kPlainMeta = (128u) | (128u << 10) | (128u << 20);
+
+template <typename TI>
+__device__ __forceinline__ unsigned* sym_word(const PairArgs<TI>& A, int slot) {
+  return reinterpret_cast<unsigned*>(A.lists) + 27LL * slot;
+}
+// per non-empty home cell: first sorted slot (27 words) and loop-shift base
+// (27 words) of its stencil cells, after the masks (the host checks that
+// 27 nat + 54 ncells words fit the list region)
+template <typename TI>
+__device__ __forceinline__ unsigned* sym_table(const PairArgs<TI>& A, int cell) {
+  return reinterpret_cast<unsigned*>(A.lists) + 27LL * A.g.nat + 54LL * cell;
+}
+
+struct __align__(16) SymSmem {
+  float4 cv[kSymChunk];      // home-relative FP32 candidate (NaN exact, +inf padding); w = candidate word
+  int cslot[kSymChunk];      // sorted slot
+  int corig[kSymChunk];      // 0-based original index
+  unsigned cqb[kSymChunk];   // q << 8 | index of the candidate in its cell
+  unsigned ccol[kSymChunk];  // home atoms that accepted the candidate
+  unsigned rmask[32][15];    // rows of the home atoms, q = 13..26 (padded)
+  unsigned hmeta[32];
+  float box[6];
+  int prune;
+};
+
+template <typename TI>
+__global__ void __launch_bounds__(kSymWarps * 32, 8) k_pairs_sym(PairArgs<TI> A) {
+  __shared__ SymSmem sm[kSymWarps];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  SymSmem& W = sm[warp];
+  const Geometry& g = A.g;
+  const float lo = g.lo, hi = g.hi;
+  const unsigned lt = lt_mask();
+  unsigned rechecks = 0;
+  if (A.cap_rec && blockIdx.x == 0 && threadIdx.x == 0) *A.cap_rec = A.list_cap;
+  for (int h = blockIdx.x * kSymWarps + warp; h < A.ncells_total; h += gridDim.x * kSymWarps) {
+    const int hs = clampi(A.cell_offsets[h] - 1, g.nat), he = clampi(A.cell_offsets[h + 1] - 1, g.nat);
+    const int nb = he - hs;
+    if (nb <= 0) continue;
+    const int hc0 = h % g.ns[0] + 1, hc1 = (h / g.ns[0]) % g.ns[1] + 1, hc2 = h / (g.ns[0] * g.ns[1]) + 1;
+    // stencil cell q = lane
+    int cstart = 0, ccount = 0, lin = -1;
+    unsigned slp = 0;
+    float ox = 0.f, oy = 0.f, oz = 0.f;
+    if (lane < 27) {
+      lin = stencil_cell(g, nullptr, 0, 3, 3, hc0, hc1, hc2, lane, slp, ox, oy, oz);
+      if (lin >= 0) {
+        cstart = clampi(A.cell_offsets[lin] - 1, g.nat);
+        ccount = max(clampi(A.cell_offsets[lin + 1] - 1, g.nat) - cstart, 0);
+      }
+    }
+    if (nb > 32 || __any_sync(0xffffffffu, ccount > 32)) {
+      if (lane == 0) atomicOr(A.sym_fail, 1);
+      continue;
+    }
+    if (lane < 27) {  // the write pass reads the cell's stencil from here
+      unsigned* tab = sym_table(A, h);
+      tab[lane] = unsigned(cstart);
+      tab[27 + lane] = slp;
+    }
+    // words of the home atoms no other warp writes: mirrored cell empty or outside
+    const unsigned zq = __ballot_sync(0xffffffffu, lane < 13 && (lin < 0 || ccount == 0));
+    if (zq)
+      for (int t = lane; t < nb * 13; t += 32) {
+        const int a = t / 13, q = t - 13 * a;
+        if ((zq >> q) & 1u) sym_word(A, hs + a)[q] = 0u;
+      }
+    __syncwarp();
+    float ux = 0.f, uy = 0.f, uz = 0.f;
+    unsigned hm = kPlainMeta;
+    if (lane < nb) {
+      const float4 r = A.rec[hs + lane];
+      ux = r.x;
+      uy = r.y;
+      uz = r.z;
+      hm = __float_as_uint(r.w);
+      W.hmeta[lane] = hm;
+    }
+    if (__any_sync(0xffffffffu, hm != kPlainMeta) && lane == 0) atomicOr(A.sym_wound, 1);
+#pragma unroll
+    for (int k = 0; k < 14; ++k) W.rmask[lane][k] = 0u;
+    {
+      const float inf = __int_as_float(0x7f800000);
+      const bool in = lane < nb;
+      float bl[3] = {in ? ux : inf, in ? uy : inf, in ? uz : inf};
+      float bh[3] = {in ? ux : -inf, in ? uy : -inf, in ? uz : -inf};
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          bl[d] = fminf(bl[d], __shfl_xor_sync(0xffffffffu, bl[d], o));
+          bh[d] = fmaxf(bh[d], __shfl_xor_sync(0xffffffffu, bh[d], o));
+        }
+      const bool pr = !__any_sync(0xffffffffu, in && (W.hmeta[lane] & kExactBit) != 0);
+      if (lane == 0) {
+        W.box[0] = bl[0];
+        W.box[1] = bh[0];
+        W.box[2] = bl[1];
+        W.box[3] = bh[1];
+        W.box[4] = bl[2];
+        W.box[5] = bh[2];
+        W.prune = pr;
+      }
+    }
+    // candidates: the centre and the cells after it (lanes 13..26), flattened
+    const int scnt = lane >= 13 ? ccount : 0;
+    int incl = scnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    const int tg = __shfl_sync(0xffffffffu, incl, 31);
+    __syncwarp();
+    const bool prune = W.prune != 0;
+    for (int cb = 0; cb < tg; cb += kSymChunk) {
+      const int nch = min(kSymChunk, tg - cb);
+      // ---- stage: home-relative FP32 candidates, dropped when farther from
+      // the home atoms' box than the reject bound (their column words are 0)
+      int nkeep = 0;
+      for (int f0 = 0; f0 < nch; f0 += 32) {
+        const int f = f0 + lane;
+        const int gf = cb + min(f, nch - 1);
+        int q = 0;
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1) {
+          const int v = __shfl_sync(0xffffffffu, incl, q + step - 1);
+          if (v <= gf) q += step;
+        }
+        const int q_incl = __shfl_sync(0xffffffffu, incl, q);
+        const int q_cnt = __shfl_sync(0xffffffffu, scnt, q);
+        const int q_start = __shfl_sync(0xffffffffu, cstart, q);
+        const unsigned q_slp = __shfl_sync(0xffffffffu, slp, q);
+        const float qx = __shfl_sync(0xffffffffu, ox, q);
+        const float qy = __shfl_sync(0xffffffffu, oy, q);
+        const float qz = __shfl_sync(0xffffffffu, oz, q);
+        bool keep = false;
+        float4 cv;
+        int slot = 0, bit = 0;
+        if (f < nch) {
+          bit = gf - (q_incl - q_cnt);
+          slot = q_start + bit;
+          const float4 r = A.rec[slot];
+          const unsigned mj = __float_as_uint(r.w);
+          const unsigned cw = cand_word(q_slp, mj);
+          const float nan = __int_as_float(0x7fc00000);
+          const bool ex = (cw & kExactBit) != 0;
+          cv = make_float4(ex ? nan : r.x + qx, ex ? nan : r.y + qy, ex ? nan : r.z + qz, __uint_as_float(cw));
+          const float dx = fmaxf(fmaxf(W.box[0] - cv.x, cv.x - W.box[1]), 0.f);
+          const float dy = fmaxf(fmaxf(W.box[2] - cv.y, cv.y - W.box[3]), 0.f);
+          const float dz = fmaxf(fmaxf(W.box[4] - cv.z, cv.z - W.box[5]), 0.f);
+          const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+          keep = ex || !(prune && d2 > hi);
+          if (!keep && q > 13) sym_word(A, slot)[26 - q] = 0u;
+        }
+        const unsigned km = __ballot_sync(0xffffffffu, keep);
+        if (keep) {
+          const int pos = nkeep + __popc(km & lt);
+          W.cv[pos] = cv;
+          W.cslot[pos] = slot;
+          W.corig[pos] = clampi(A.perm[slot] - 1, g.nat - 1);
+          W.cqb[pos] = (unsigned(q) << 8) | unsigned(bit);
+          W.ccol[pos] = 0u;
+        }
+        nkeep += __popc(km);
+      }
+      {
+        const int pos = nkeep + lane;
+        if (pos < ((nkeep + 31) & ~31)) {
+          const float inf = __int_as_float(0x7f800000);
+          W.cv[pos] = make_float4(inf, inf, inf, 0.f);
+          W.cqb[pos] = 13u << 8;
+          W.ccol[pos] = 0u;
+        }
+      }
+      __syncwarp();
+      // ---- screen: kGroup home atoms per candidate load
+      const int nround = (nkeep + 31) & ~31;
+      for (int a0 = 0; a0 < nb; a0 += kGroup) {
+        float ax[kGroup], ay[kGroup], az[kGroup];
+#pragma unroll
+        for (int k = 0; k < kGroup; ++k) {
+          const int a = min(a0 + k, nb - 1);
+          const bool use = a0 + k < nb;
+          const float inf = __int_as_float(0x7f800000);
+          ax[k] = use ? __shfl_sync(0xffffffffu, ux, a) : inf;
+          ay[k] = use ? __shfl_sync(0xffffffffu, uy, a) : inf;
+          az[k] = use ? __shfl_sync(0xffffffffu, uz, a) : inf;
+        }
+        for (int r0 = 0; r0 < nround; r0 += 32) {
+          const int f = r0 + lane;
+          const float4 c = W.cv[f];
+          bool acc[kGroup], unc[kGroup];
+          bool any_unc = false;
+#pragma unroll
+          for (int k = 0; k < kGroup; ++k) {
+            const float rx = c.x - ax[k], ry = c.y - ay[k], rz = c.z - az[k];
+            const float r2 = fmaf(rz, rz, fmaf(ry, ry, rx * rx));
+            acc[k] = r2 < lo && r2 > 0.f;
+            unc[k] = !(r2 > hi) && !acc[k];
+            any_unc |= unc[k];
+          }
+          if (__any_sync(0xffffffffu, any_unc)) {
+#pragma unroll
+            for (int k = 0; k < kGroup; ++k)
+              if (unc[k]) {
+                const int a = a0 + k;
+                if (f >= nkeep || a >= nb || is_self(W.cslot[f], hs + a, __float_as_uint(c.w), W.hmeta[a])) {
+                  acc[k] = false;
+                } else {
+                  ++rechecks;
+                  acc[k] = exact_pair(g, A.Xs, hs + a, W.cslot[f], W.hmeta[a], __float_as_uint(c.w));
+                }
+              }
+          }
+          unsigned col = 0u;
+          const unsigned qb = W.cqb[f];
+#pragma unroll
+          for (int k = 0; k < kGroup; ++k)
+            if (acc[k]) {
+              atomicOr(&W.rmask[a0 + k][(qb >> 8) - 13], 1u << (qb & 255u));
+              col |= 1u << (a0 + k);
+            }
+          if (col) W.ccol[f] |= col;
+        }
+      }
+      __syncwarp();
+      // ---- columns: the mirrored cell's word of every kept candidate
+      for (int f = lane; f < nkeep; f += 32) {
+        const unsigned q = W.cqb[f] >> 8;
+        if (q > 13) {
+          const unsigned cc = W.ccol[f];
+          sym_word(A, W.cslot[f])[26 - q] = cc;
+          if (cc) atomicAdd(A.counts + W.corig[f], __popc(cc));
+        }
+      }
+      __syncwarp();
+    }
+    // ---- rows: words q = 13..26 of the home atoms, and their counts
+    for (int t = lane; t < nb * 14; t += 32) {
+      const int a = t / 14, k = t - 14 * a;
+      sym_word(A, hs + a)[13 + k] = W.rmask[a][k];
+    }
+    if (lane < nb) {
+      int c = 0;
+#pragma unroll
+      for (int k = 0; k < 14; ++k) c += __popc(W.rmask[lane][k]);
+      if (c) atomicAdd(A.counts + clampi(A.perm[hs + lane] - 1, g.nat - 1), c);
+    }
+    __syncwarp();
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) rechecks += __shfl_xor_sync(0xffffffffu, rechecks, o);
+  if (lane == 0 && rechecks) atomicAdd(A.stats, (unsigned long long)rechecks);
+}
+
+// ------------------------------------------------------------------------
 // Emit: writes i, j, S, R of every atom whose pairs the count pass listed --
 // no stencil, no staging and no screening.  One warp takes 32 consecutive
 // sorted slots; their per-atom data go to shared memory, then the warp walks
@@ -751,10 +1028,38 @@ struct __align__(16) EmitAtoms {
   unsigned mi[32];      // packed windings | exact bit
   int n[32];            // listed pairs (0 when written by the screening pass)
   int sys[32];          // batch: system of the slot
+  int cell[32];         // neighbour masks: 0-based home cell of the slot
 };
 
-template <typename TI, bool BATCH>
-__global__ void __launch_bounds__(kEmitWarps * 32, kEmitMinBlocks) k_emit(PairArgs<TI> A) {
+// k-th (0-based) set bit of m (m has more than k set bits)
+__device__ __forceinline__ int kth_bit(unsigned m, int k) {
+  int pos = 0;
+#pragma unroll
+  for (int w = 16; w > 0; w >>= 1) {
+    const int c = __popc(m & ((1u << w) - 1u));
+    if (c <= k) {
+      k -= c;
+      m >>= w;
+      pos += w;
+    }
+  }
+  return pos;
+}
+
+// MASKS: the pairs come from the symmetric count pass's neighbour masks
+// instead of lists; lane r of a pass finds the atom's r-th pair from the
+// prefix counts of its 27 mask words (stencil order, then sorted order in the
+// cell), so the output order is the same.  Atoms of more than list_cap pairs
+// are left to the screening write pass (their cells are listed here).
+#ifndef NL_EMIT_MASK_MIN_BLOCKS
+#define NL_EMIT_MIN_MASK_BLOCKS 6
+#else
+#define NL_EMIT_MIN_MASK_BLOCKS NL_EMIT_MASK_MIN_BLOCKS
+#endif
+template <typename TI, bool BATCH, bool MASKS>
+__global__ void __launch_bounds__(kEmitWarps * 32, MASKS ? NL_EMIT_MIN_MASK_BLOCKS : kEmitMinBlocks)
+    k_emit(PairArgs<TI> A) {
+  if (!BATCH && A.sym && ((*A.sym_fail == 0) != MASKS)) return;  // the other variant writes
   __shared__ EmitAtoms ea[kEmitWarps];
   __shared__ double cs_blk[BATCH ? 1 : 3 * kCsN * kCsN * kCsN];
   if (!BATCH) {
@@ -764,15 +1069,31 @@ __global__ void __launch_bounds__(kEmitWarps * 32, kEmitMinBlocks) k_emit(PairAr
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   EmitAtoms& E = ea[warp];
   const int K = A.list_cap;
+  const bool plain = MASKS && *A.sym_wound == 0;  // no atom has a winding: candidate words need no record
   const long long nwarps = (long long)gridDim.x * kEmitWarps;
   for (long long c0 = ((long long)blockIdx.x * kEmitWarps + warp) * 32; c0 < A.nat_total; c0 += nwarps * 32) {
     const int na = int(min(32LL, A.nat_total - c0));
     __syncwarp();
     if (lane < na) {
       const int slot = int(c0) + lane;
-      int n = A.lcount[slot];
-      E.n[lane] = n > K ? 0 : n;  // overflowed atoms belong to the screening pass
-      E.base[lane] = (long long)A.first[clampi(A.sorig[slot], A.nat_total - 1)] - 1;
+      if constexpr (MASKS) {
+        const unsigned* mw = reinterpret_cast<const unsigned*>(A.lists) + 27LL * slot;
+        int n = 0;
+#pragma unroll
+        for (int q = 0; q < 27; ++q) n += __popc(mw[q]);
+        const int hl = clampi(A.scell[slot], A.ncells_total - 1);
+        E.cell[lane] = hl;
+        E.n[lane] = n > K ? 0 : n;
+        if (n > K && atomicExch(A.cell_flag + hl, 1) == 0) {  // the screening write pass takes the cell
+          const int u = atomicAdd(A.n_screen_cells, 1);
+          if (u < A.ncells_total) A.screen_cells[u] = hl;
+        }
+        E.base[lane] = (long long)A.first[clampi(A.perm[slot] - 1, A.nat_total - 1)] - 1;
+      } else {
+        int n = A.lcount[slot];
+        E.n[lane] = n > K ? 0 : n;  // overflowed atoms belong to the screening pass
+        E.base[lane] = (long long)A.first[clampi(A.sorig[slot], A.nat_total - 1)] - 1;
+      }
       E.ti[lane] = (long long)A.perm[slot];
       E.mi[lane] = __float_as_uint(A.rec[slot].w);
       E.xi[lane][0] = A.Xs[3LL * slot + 0];
@@ -850,6 +1171,8 @@ __global__ void __launch_bounds__(kEmitWarps * 32, kEmitMinBlocks) k_emit(PairAr
         uint2 e;
         int a, r;
         bool v;
+        unsigned m, slp;  // masks: this lane's mask word and stencil cell of the pass's atom
+        int st;
       };
       struct StG {
         double x0, x1, x2;
@@ -864,18 +1187,53 @@ __global__ void __launch_bounds__(kEmitWarps * 32, kEmitMinBlocks) k_emit(PairAr
           const unsigned pd = E.pass[h];
           t.a = int(pd >> 8);
           t.r = 32 * int(pd & 255u) + lane;
-          t.e = __ldcs(A.lists + (c0 + t.a) * K + min(t.r, E.n[t.a] - 1));  // read once
+          if constexpr (MASKS) {
+            // the mask word and the stencil cell of lane `lane`; decoded in the gather stage
+            const unsigned* tab = sym_table(A, E.cell[t.a]);
+            t.st = lane < 27 ? int(tab[lane]) : 0;
+            t.slp = lane < 27 ? tab[27 + lane] : 0u;
+            t.m = lane < 27 ? __ldcs(reinterpret_cast<const unsigned*>(A.lists) + 27LL * (c0 + t.a) + lane) : 0u;
+          } else {
+            t.e = __ldcs(A.lists + (c0 + t.a) * K + min(t.r, E.n[t.a] - 1));  // read once
+          }
         }
       };
       auto stage_g = [&](const StE& t, StG& u) {
         u.v = t.v;
         if (u.v) {
-          const int slot_j = clampi(int(t.e.x), A.nat_total - 1);
+          uint2 e = t.e;
+          if constexpr (MASKS) {
+            // lane r takes the atom's r-th pair: stencil cell q from the prefix
+            // counts of the mask words, then the k-th atom of the cell's mask
+            const int c = __popc(t.m);
+            int pre = c;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+              const int v = __shfl_up_sync(0xffffffffu, pre, o);
+              if (lane >= o) pre += v;
+            }
+            const int r = min(t.r, E.n[t.a] - 1);
+            int q = 0;  // first stencil cell whose inclusive count exceeds r
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1) {
+              const int v = __shfl_sync(0xffffffffu, pre, q + step - 1);
+              if (v <= r) q += step;
+            }
+            const unsigned mq = __shfl_sync(0xffffffffu, t.m, q);
+            const int exq = __shfl_sync(0xffffffffu, pre - c, q);
+            const int stq = __shfl_sync(0xffffffffu, t.st, q);
+            const unsigned slq = __shfl_sync(0xffffffffu, t.slp, q);
+            e = make_uint2(unsigned(stq + kth_bit(mq, max(r - exq, 0))), slq);  // (slot of j, loop-shift base)
+          }
+          const int slot_j = clampi(int(e.x), A.nat_total - 1);
           u.x0 = __ldg(A.Xs + 3LL * slot_j + 0);
           u.x1 = __ldg(A.Xs + 3LL * slot_j + 1);
           u.x2 = __ldg(A.Xs + 3LL * slot_j + 2);
           u.oj = (long long)__ldg(A.perm + slot_j);
-          u.cw = t.e.y;
+          if constexpr (MASKS)
+            u.cw = cand_word(e.y, plain ? kPlainMeta : __float_as_uint(__ldg(&A.rec[slot_j].w)));
+          else
+            u.cw = e.y;
           u.a = t.a;
           u.r = t.r;
         }
@@ -928,6 +1286,7 @@ constexpr int kCountThreads = 128;
 
 template <typename TI, bool BATCH>
 __global__ void __launch_bounds__(kCountThreads, NL_COUNT_MIN_BLOCKS) k_count_atoms(PairArgs<TI> A) {
+  if (A.sym && *A.sym_fail == 0) return;  // the symmetric pass counted
   __shared__ unsigned dtab_blk[BATCH ? 1 : kStencilTab];
   if (!BATCH) {
     const int tx = 2 * A.g.nxyz[0] + 1, ty = 2 * A.g.nxyz[1] + 1;
@@ -1177,6 +1536,11 @@ static void launch_modes(int mode, const PairArgs<TI>& a, int num_sms, cudaStrea
   if (blocks < 1) blocks = 1;
   switch (mode) {
     case kModeCount:
+      if (!BATCH && a.sym) {  // symmetric pass; the per-cell pass below runs only if it gave up
+        long long sb = ((long long)a.ncells_total + kSymWarps - 1) / kSymWarps;
+        if (sb > (long long)num_sms * pbps) sb = (long long)num_sms * pbps;
+        k_pairs_sym<TI><<<int(sb), kSymWarps * 32, 0, st>>>(a);
+      }
       if (a.count_kernel != 2) {  // default: one warp per home cell
         k_pairs<TI, kModeCount, BATCH><<<int(blocks), kPairWarps * 32, 0, st>>>(a);
       } else {
@@ -1191,7 +1555,8 @@ static void launch_modes(int mode, const PairArgs<TI>& a, int num_sms, cudaStrea
       if (a.list_cap > 0) {
         long long eb = ((long long)a.nat_total + 32 * kEmitWarps - 1) / (32 * kEmitWarps);
         if (eb > (long long)num_sms * ebps) eb = (long long)num_sms * ebps;
-        k_emit<TI, BATCH><<<int(eb), kEmitWarps * 32, 0, st>>>(a);
+        k_emit<TI, BATCH, false><<<int(eb), kEmitWarps * 32, 0, st>>>(a);
+        if (!BATCH && a.sym) k_emit<TI, false, true><<<int(eb), kEmitWarps * 32, 0, st>>>(a);
       }
       k_pairs<TI, kModeFill, BATCH><<<int(blocks), kPairWarps * 32, 0, st>>>(a);
       break;

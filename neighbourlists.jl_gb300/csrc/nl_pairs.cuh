@@ -54,7 +54,10 @@ struct PairArgs {
   int* screen_cells;            // count pass: home cells left to the screening write pass
   int* n_screen_cells;          // length of that list
   int* cell_flag;           // per cell (zeroed per count): already in that list
-  int count_kernel;         // 0 / 1: one warp per home cell, 2: one thread per home atom
+  int count_kernel;         // 1: one warp per home cell, 2: one thread per home atom (0 / 3: see sym)
+  int sym;                  // count / write: each unordered cell pair screened once, neighbour masks
+  int* sym_fail;            // set when a cell has more than 32 atoms: lists and the per-cell pass instead
+  int* sym_wound;           // set when an atom has a winding or is exact (candidate words need its record)
   int half;                 // count / write: keep each unordered pair once (j > i, or j == i and S > 0)
   int pair_blocks_per_sm;   // launch tuning (0 = default): count / screening grids
   int emit_blocks_per_sm;   // launch tuning (0 = default): list write grid

@@ -322,11 +322,11 @@ def test_pair_and_site_iterators(nlpkg, orc):
         assert np.array_equal(to_np(R).view(np.int64), o.R[a:b].view(np.int64))
 
 
-@pytest.mark.parametrize("count_kernel", [1, 2])
+@pytest.mark.parametrize("count_kernel", [1, 2, 3])
 def test_both_count_kernels(nlpkg, orc, count_kernel):
-    """The warp-per-cell and thread-per-atom count passes give the same bits
-    (open and periodic axes, triclinic, a one-cell multi-image system, dense
-    cells that overflow the lists)."""
+    """The warp-per-cell, thread-per-atom and symmetric (neighbour masks)
+    count passes give the same bits (open and periodic axes, triclinic, a
+    one-cell multi-image system, dense cells that overflow the lists)."""
     Xd_, Cd = cf.diamond_primitive()
     Xf, Cf, pf = cf.fcc_sheared(n=5, seed=9)
     cases = [
@@ -347,7 +347,8 @@ def test_both_count_kernels(nlpkg, orc, count_kernel):
 def test_count_pass_edge_cases(nlpkg, orc):
     """Exact atoms far outside an open axis, lists that overflow (> 64 pairs:
     those cells go to the screening write pass) next to cells that do not, a
-    crowded cell, open boundaries, Int64; and the two count tilings giving
+    crowded cell (> 32 atoms: the symmetric pass falls back), open
+    boundaries, Int64; and the symmetric and per-atom count passes giving
     identical lists on 20k atoms."""
     rng = np.random.default_rng(54)
     X, C, L = cf.rand_config(4000, seed=55)
@@ -364,7 +365,7 @@ def test_count_pass_edge_cases(nlpkg, orc):
     X, C, L = cf.rand_config(20000, seed=56)
     Xd = torch.from_numpy(X).cuda()
     lists = []
-    for k in (2, 1):
+    for k in (3, 2):
         eng = nlpkg.NeighbourListEngine(X.shape[0], C, 5.0, (True, True, True))
         eng.set_tuning(0, 0, k)
         eng.run(Xd)
