@@ -745,7 +745,17 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
 // order, then sorted order in each cell).  A cell of more than 32 atoms sets
 // sym_fail, and the per-cell count pass with per-atom lists runs instead.
 constexpr int kSymWarps = 4;
-constexpr int kSymChunk = 128;  // staged candidates per round of home atoms
+#ifndef NL_SYM_CHUNK
+#define NL_SYM_CHUNK 128
+#endif
+#ifndef NL_SYM_GROUP
+#define NL_SYM_GROUP 2
+#endif
+#ifndef NL_SYM_MIN_BLOCKS
+#define NL_SYM_MIN_BLOCKS 8
+#endif
+constexpr int kSymChunk = NL_SYM_CHUNK;  // staged candidates per round of home atoms
+constexpr int kSymGroup = NL_SYM_GROUP;  // home atoms screened per candidate load
 // record meta of an atom without windings that is not exact
 constexpr unsigned kPlainMeta = (128u) | (128u << 10) | (128u << 20);
 
@@ -774,7 +784,7 @@ struct __align__(16) SymSmem {
 };
 
 template <typename TI>
-__global__ void __launch_bounds__(kSymWarps * 32, 8) k_pairs_sym(PairArgs<TI> A) {
+__global__ void __launch_bounds__(kSymWarps * 32, NL_SYM_MIN_BLOCKS) k_pairs_sym(PairArgs<TI> A) {
   __shared__ SymSmem sm[kSymWarps];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   SymSmem& W = sm[warp];
@@ -924,12 +934,12 @@ __global__ void __launch_bounds__(kSymWarps * 32, 8) k_pairs_sym(PairArgs<TI> A)
         }
       }
       __syncwarp();
-      // ---- screen: kGroup home atoms per candidate load
+      // ---- screen: kSymGroup home atoms per candidate load
       const int nround = (nkeep + 31) & ~31;
-      for (int a0 = 0; a0 < nb; a0 += kGroup) {
-        float ax[kGroup], ay[kGroup], az[kGroup];
+      for (int a0 = 0; a0 < nb; a0 += kSymGroup) {
+        float ax[kSymGroup], ay[kSymGroup], az[kSymGroup];
 #pragma unroll
-        for (int k = 0; k < kGroup; ++k) {
+        for (int k = 0; k < kSymGroup; ++k) {
           const int a = min(a0 + k, nb - 1);
           const bool use = a0 + k < nb;
           const float inf = __int_as_float(0x7f800000);
@@ -940,10 +950,10 @@ __global__ void __launch_bounds__(kSymWarps * 32, 8) k_pairs_sym(PairArgs<TI> A)
         for (int r0 = 0; r0 < nround; r0 += 32) {
           const int f = r0 + lane;
           const float4 c = W.cv[f];
-          bool acc[kGroup], unc[kGroup];
+          bool acc[kSymGroup], unc[kSymGroup];
           bool any_unc = false;
 #pragma unroll
-          for (int k = 0; k < kGroup; ++k) {
+          for (int k = 0; k < kSymGroup; ++k) {
             const float rx = c.x - ax[k], ry = c.y - ay[k], rz = c.z - az[k];
             const float r2 = fmaf(rz, rz, fmaf(ry, ry, rx * rx));
             acc[k] = r2 < lo && r2 > 0.f;
@@ -952,7 +962,7 @@ __global__ void __launch_bounds__(kSymWarps * 32, 8) k_pairs_sym(PairArgs<TI> A)
           }
           if (__any_sync(0xffffffffu, any_unc)) {
 #pragma unroll
-            for (int k = 0; k < kGroup; ++k)
+            for (int k = 0; k < kSymGroup; ++k)
               if (unc[k]) {
                 const int a = a0 + k;
                 if (f >= nkeep || a >= nb || is_self(W.cslot[f], hs + a, __float_as_uint(c.w), W.hmeta[a])) {
@@ -966,7 +976,7 @@ __global__ void __launch_bounds__(kSymWarps * 32, 8) k_pairs_sym(PairArgs<TI> A)
           unsigned col = 0u;
           const unsigned qb = W.cqb[f];
 #pragma unroll
-          for (int k = 0; k < kGroup; ++k)
+          for (int k = 0; k < kSymGroup; ++k)
             if (acc[k]) {
               atomicOr(&W.rmask[a0 + k][(qb >> 8) - 13], 1u << (qb & 255u));
               col |= 1u << (a0 + k);
@@ -1029,6 +1039,7 @@ struct __align__(16) EmitAtoms {
   int n[32];            // listed pairs (0 when written by the screening pass)
   int sys[32];          // batch: system of the slot
   int cell[32];         // neighbour masks: 0-based home cell of the slot
+  unsigned char qmap[32];  // neighbour masks: stencil cell of the k-th non-empty mask word
 };
 
 // k-th (0-based) set bit of m (m has more than k set bits)
@@ -1203,24 +1214,28 @@ __global__ void __launch_bounds__(kEmitWarps * 32, MASKS ? NL_EMIT_MIN_MASK_BLOC
         if (u.v) {
           uint2 e = t.e;
           if constexpr (MASKS) {
-            // lane r takes the atom's r-th pair: stencil cell q from the prefix
-            // counts of the mask words, then the k-th atom of the cell's mask
+            // lane r takes the atom's r-th pair.  Lane q holds mask word q
+            // (c_q pairs); its pairs are r in [ex_q, ex_q + c_q).  ex_q by
+            // bit-sliced ballots (c_q <= 32), the starts of the non-empty
+            // runs as a bit set, the run of r by a popcount, its stencil cell
+            // from qmap, then the k-th atom of that cell's mask.
+            const unsigned lt = lt_mask();
             const int c = __popc(t.m);
-            int pre = c;
+            int ex = 0;
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-              const int v = __shfl_up_sync(0xffffffffu, pre, o);
-              if (lane >= o) pre += v;
-            }
-            const int r = min(t.r, E.n[t.a] - 1);
-            int q = 0;  // first stencil cell whose inclusive count exceeds r
-#pragma unroll
-            for (int step = 16; step > 0; step >>= 1) {
-              const int v = __shfl_sync(0xffffffffu, pre, q + step - 1);
-              if (v <= r) q += step;
-            }
+            for (int b = 0; b < 6; ++b) ex += __popc(__ballot_sync(0xffffffffu, (c >> b) & 1) & lt) << b;
+            const unsigned ne = __ballot_sync(0xffffffffu, c != 0);
+            const unsigned starts_lo = __reduce_or_sync(0xffffffffu, c && ex < 32 ? 1u << ex : 0u);
+            const unsigned starts_hi = __reduce_or_sync(0xffffffffu, c && ex >= 32 ? 1u << (ex - 32) : 0u);
+            if (c) E.qmap[__popc(ne & lt)] = (unsigned char)lane;
+            __syncwarp();
+            const int r = min(t.r, E.n[t.a] - 1);  // 0 <= r < 64
+            const int j = r < 32 ? __popc(starts_lo & (0xffffffffu >> (31 - r))) - 1
+                                 : __popc(starts_lo) + __popc(starts_hi & (0xffffffffu >> (63 - r))) - 1;
+            const int q = E.qmap[j];
+            __syncwarp();
             const unsigned mq = __shfl_sync(0xffffffffu, t.m, q);
-            const int exq = __shfl_sync(0xffffffffu, pre - c, q);
+            const int exq = __shfl_sync(0xffffffffu, ex, q);
             const int stq = __shfl_sync(0xffffffffu, t.st, q);
             const unsigned slq = __shfl_sync(0xffffffffu, t.slp, q);
             e = make_uint2(unsigned(stq + kth_bit(mq, max(r - exq, 0))), slq);  // (slot of j, loop-shift base)
