@@ -45,7 +45,7 @@ ALGO_BYTES_PER_ATOM = 24  # positions read
 ALGO_BYTES_PER_PAIR = 44  # i 4 + j 4 + S 12 + R 24 written
 # kernels of one step: k_bin, k_scan_offsets (cells), k_scatter, k_fix, k_fix_big,
 # k_pairs<count>, k_scan_offsets (pairs), k_cs_table, k_emit, k_pairs<fill>
-LAUNCHES_PER_STEP = 10
+LAUNCHES_PER_STEP = 12  # kernels of one step: build 5, count 3 (with its scan), write 4
 
 
 def workload(n_atoms=N_ATOMS):
@@ -316,7 +316,7 @@ def run_gpu(args):
                    "cuda_graph": True, "ms_per_step_without_graph": launch_ms,
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_kind": peak_kind, "kernel": "write pass (k_emit + k_cs_table + k_pairs<fill>)",
+                     "peak_kind": peak_kind, "kernel": "write pass (k_emit<masks> + k_cs_table + k_pairs<fill>)",
                      "algorithmic_bytes": algo_bytes, "kernel_ms": fill_ms,
                      "traffic": (traffic or {}).get("dram_bytes_per_launch")},
         "step_roofline_frac": algo_bytes / (step_ms * 1e-3) / 1e9 / peak,
