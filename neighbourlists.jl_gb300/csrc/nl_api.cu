@@ -423,13 +423,13 @@ nl::PairArgs<TI> pair_args(const nl::Geometry& g, const TI* cell_offsets, const 
 }
 
 // The symmetric count pass and the mask write pass (nl_pairs.cu) apply to a
-// full list of a single system with per-atom lists in the workspace and a
-// 27-cell stencil of distinct cells (nxyz = 1, periodic axes of at least 3
-// cells); count_kernel 1 or 2 selects the per-cell / per-atom pass instead.
-bool use_sym(const nl::Geometry& g, const Layout& L, int half) {
+// full or half list of a single system with per-atom lists in the workspace
+// and a 27-cell stencil of distinct cells (nxyz = 1, periodic axes of at
+// least 3 cells); count_kernel 1 or 2 selects the per-cell / per-atom pass.
+bool use_sym(const nl::Geometry& g, const Layout& L) {
   // masks (27 words per atom) and the stencil table (54 words per cell) share the list region
   const bool fits = 27.0 * g.nat + 54.0 * g.ncells <= 2.0 * nl::kListCap * g.nat;
-  bool sym = L.use_lists && fits && !half && g_tuning.count_kernel != 1 && g_tuning.count_kernel != 2;
+  bool sym = L.use_lists && fits && g_tuning.count_kernel != 1 && g_tuning.count_kernel != 2;
   for (int k = 0; k < 3; ++k) sym = sym && g.nxyz[k] == 1 && (!g.pbc[k] || g.ns[k] >= 3);
   return sym;
 }
@@ -454,7 +454,7 @@ int count_impl(const nl::Geometry& g, const double* Xs, const TI* perm, const TI
   nl::PairArgs<TI> a = pair_args<TI>(g, cell_offsets, perm, Xs, ws, L);
   a.counts = at<int>(ws, L.counts);
   a.half = half;
-  a.sym = use_sym(g, L, half) ? 1 : 0;
+  a.sym = use_sym(g, L) ? 1 : 0;
   if (a.sym) {  // the symmetric pass accumulates the counts
     e = cudaMemsetAsync(a.counts, 0, sizeof(int) * size_t(g.nat), st);
     if (e != cudaSuccess) return cuda_fail(e, "memset counts");
@@ -473,7 +473,7 @@ int fill_impl(const nl::Geometry& g, const double* Xs, const TI* perm, const TI*
   if (g.nat == 0 || capacity <= 0) return NL_OK;
   nl::PairArgs<TI> a = pair_args<TI>(g, cell_offsets, perm, Xs, ws, L);
   a.half = half;
-  a.sym = use_sym(g, L, half) ? 1 : 0;
+  a.sym = use_sym(g, L) ? 1 : 0;
   a.first = first;
   a.oi = oi;
   a.oj = oj;

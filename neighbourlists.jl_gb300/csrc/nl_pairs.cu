@@ -779,6 +779,7 @@ struct __align__(16) SymSmem {
   unsigned ccol[kSymChunk];  // home atoms that accepted the candidate
   unsigned rmask[32][15];    // rows of the home atoms, q = 13..26 (padded)
   unsigned hmeta[32];
+  int horig[32];             // 0-based original index of the home atoms (half lists)
   float box[6];
   int prune;
 };
@@ -835,6 +836,7 @@ __global__ void __launch_bounds__(kSymWarps * 32, NL_SYM_MIN_BLOCKS) k_pairs_sym
       uz = r.z;
       hm = __float_as_uint(r.w);
       W.hmeta[lane] = hm;
+      W.horig[lane] = clampi(A.perm[hs + lane] - 1, g.nat - 1);
     }
     if (__any_sync(0xffffffffu, hm != kPlainMeta) && lane == 0) atomicOr(A.sym_wound, 1);
 #pragma unroll
@@ -978,8 +980,15 @@ __global__ void __launch_bounds__(kSymWarps * 32, NL_SYM_MIN_BLOCKS) k_pairs_sym
 #pragma unroll
           for (int k = 0; k < kSymGroup; ++k)
             if (acc[k]) {
-              atomicOr(&W.rmask[a0 + k][(qb >> 8) - 13], 1u << (qb & 255u));
-              col |= 1u << (a0 + k);
+              // full lists keep both directions; a half list keeps the one
+              // half_keep selects: the home atom's row or the candidate's column
+              bool row = true, column = (qb >> 8) > 13u;
+              if (A.half) {
+                row = half_keep(W.horig[a0 + k], W.corig[f], __float_as_uint(c.w), W.hmeta[a0 + k]);
+                column = column && !row;
+              }
+              if (row) atomicOr(&W.rmask[a0 + k][(qb >> 8) - 13], 1u << (qb & 255u));
+              if (column) col |= 1u << (a0 + k);
             }
           if (col) W.ccol[f] |= col;
         }

@@ -426,12 +426,14 @@ def half_of(o):
     return keep, first
 
 
-@pytest.mark.parametrize("case", ["10k", "fcc", "diamond", "dense", "triclinic"])
-@pytest.mark.parametrize("count_kernel", [1, 2])
+@pytest.mark.parametrize("case", ["10k", "fcc", "diamond", "dense", "triclinic", "crowded"])
+@pytest.mark.parametrize("count_kernel", [1, 2, 3])
 def test_half_lists(nlpkg, orc, case, count_kernel):
     """nl_neighbour_list_half == the full list filtered to j > i (or the
     periodic images of an atom itself with S > 0), in the reference's order;
-    both count tilings; dense cells take the screening write pass."""
+    the per-cell, per-atom and symmetric count passes (the last keeps one
+    direction of each pair in the masks); dense cells take the screening
+    write pass."""
     if case == "10k":
         X, C, L = cf.rand_config(10000, seed=0)
         rc, pbc = 5.0, (True, True, True)
@@ -443,9 +445,12 @@ def test_half_lists(nlpkg, orc, case, count_kernel):
         rc, pbc = 6.0, (True, True, True)
     elif case == "dense":
         X, C, pbc, rc = np.random.default_rng(81).random((400, 3)) * 6.0, np.diag([6.0] * 3), (True, True, True), 2.2
-    else:
+    elif case == "triclinic":
         X, C = cf.rand_config_triclinic(300, seed=82)
         rc, pbc = 3.0, (True, False, True)
+    else:  # > 64 pairs for some atoms, cells of <= 32 atoms: masks plus the screening write pass
+        X, C, L = cf.rand_config(4000, seed=55)
+        rc, pbc = 6.0, (True, True, False)
     eng = nlpkg.NeighbourListEngine(X.shape[0], C, rc, pbc, half=True)
     eng.set_tuning(0, 0, count_kernel)
     t = eng.run(torch.from_numpy(np.ascontiguousarray(X)).cuda())
