@@ -562,6 +562,14 @@ int build_impl32(const float* X, int64_t nat, const nl::Geo32& g, TI* perm, floa
   return e == cudaSuccess ? NL_OK : cuda_fail(e, "launch build kernels");
 }
 
+// the symmetric count / mask write pass of the Float32 path: as use_sym
+bool use_sym32(const nl::Geo32& g, const Layout& L) {
+  const bool fits = 27.0 * g.nat + 54.0 * g.ncells <= 2.0 * nl::kListCap * g.nat;
+  bool sym = L.use_lists && fits && g_tuning.count_kernel != 1 && g_tuning.count_kernel != 2;
+  for (int k = 0; k < 3; ++k) sym = sym && g.nxyz[k] == 1 && (!g.pbc[k] || g.ns[k] >= 3);
+  return sym;
+}
+
 template <typename TI>
 nl::Pairs32Args<TI> pairs32_args(const nl::Geo32& g, const TI* cell_offsets, const TI* perm, void* ws,
                                  const Layout& L) {
@@ -574,6 +582,9 @@ nl::Pairs32Args<TI> pairs32_args(const nl::Geo32& g, const TI* cell_offsets, con
   a.perm = perm;
   a.counts = at<int>(ws, L.counts);
   a.err = at<unsigned>(ws, L.err);
+  a.sym = use_sym32(g, L) ? 1 : 0;
+  a.masks = reinterpret_cast<unsigned*>(at<uint2>(ws, L.lists));
+  a.sym_fail = at<int>(ws, L.pcount) + 6;  // zeroed with the pair scan state
   return a;
 }
 
@@ -593,6 +604,10 @@ int count_impl32(const nl::Geo32& g, const float* Xs, const TI* perm, const TI* 
     nl::launch_prepare32<TI>(g, Xs, cell_id, perm, g.nat, at<float4>(ws, L.rec_sorted), at<int>(ws, L.scell),
                              at<unsigned>(ws, L.err), sms, st);
   const nl::Pairs32Args<TI> a = pairs32_args<TI>(g, cell_offsets, perm, ws, L);
+  if (a.sym) {  // the symmetric pass accumulates the counts
+    e = cudaMemsetAsync(a.counts, 0, sizeof(int) * size_t(g.nat), st);
+    if (e != cudaSuccess) return cuda_fail(e, "memset counts");
+  }
   nl::launch_pairs32<TI>(false, a, sms, st);
   nl::launch_scan<TI>(a.counts, g.nat, first, nullptr, at<unsigned long long>(ws, L.st_pairs), at<int>(ws, L.pcount),
                       at<long long>(ws, L.totals) + 1, a.err, st);

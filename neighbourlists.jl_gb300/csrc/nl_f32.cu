@@ -163,6 +163,7 @@ __device__ __forceinline__ int tag_s(unsigned t, int k) { return int((t >> (8 * 
 template <typename TI, bool FILL>
 __global__ void __launch_bounds__(kW32Warps * 32, FILL ? NL_F32_MIN_FILL : NL_F32_MIN_COUNT)
     k_pairs32(Pairs32Args<TI> a) {
+  if (a.sym && *a.sym_fail == 0) return;  // the symmetric count and the mask write pass ran
   constexpr int kW32Per = FILL ? NL_F32_PER_FILL : NL_F32_PER_COUNT;
   constexpr int kW32Tile = 32 * kW32Per;
   __shared__ Shared32 sh_all[kW32Warps];
@@ -346,6 +347,301 @@ __global__ void __launch_bounds__(kW32Warps * 32, FILL ? NL_F32_MIN_FILL : NL_F3
   }
 }
 
+// ------------------------------------------------------------------------
+// Symmetric count pass in Float32 (27-cell stencils of distinct cells).  The
+// reference's FP32 decision for (i, j, S) and (j, i, -S) is the same:
+// R(j, i, -S) = -R(i, j, S) bit for bit under round-to-nearest.  As in the
+// Float64 engine, the warp of home cell A tests its atoms against the
+// centre and the 13 stencil cells after it, with the exact FP32 test, and
+// stores every atom's accepted neighbours as one 32-bit mask per stencil
+// cell (27 words per atom: rows for A's atoms, mirrored columns for the
+// candidates; words whose mirrored cell is empty or outside an open axis are
+// written as 0 by the atom's own warp), counts with atomics, and the cell's
+// stencil table (first slot and loop shift of each stencil cell) for the
+// write pass.  A cell of more than 32 atoms sets sym_fail: the per-cell
+// passes run instead.
+constexpr int kSym32Warps = 4;
+constexpr int kSym32Chunk = 128;
+
+struct Sym32Smem {
+  float cx[kSym32Chunk], cy[kSym32Chunk], cz[kSym32Chunk];  // candidate coordinates
+  float ex[kSym32Chunk], ey[kSym32Chunk], ez[kSym32Chunk];  // C' s_loop of its stencil cell
+  unsigned ctag[kSym32Chunk];  // s_loop + 128 in 8-bit fields | q << 24 (bits 24-28) | wound << 29
+  int cjor[kSym32Chunk];       // 1-based original index
+  int cslot[kSym32Chunk];      // sorted slot
+  unsigned char cbit[kSym32Chunk];  // index of the candidate in its cell
+  unsigned ccol[kSym32Chunk];  // home atoms that accepted the candidate
+  unsigned rmask[32][15];      // rows of the home atoms, q = 13..26
+  float hx[32], hy[32], hz[32];
+  int hw[32][3];
+  int hid[32];                 // 1-based original index
+};
+
+__device__ __forceinline__ unsigned* sym32_table(unsigned* masks, int nat, int cell) {
+  return masks + 27LL * nat + 54LL * cell;
+}
+
+template <typename TI>
+__global__ void __launch_bounds__(kSym32Warps * 32, 8) k_pairs32_sym(Pairs32Args<TI> a) {
+  __shared__ Sym32Smem sm_all[kSym32Warps];
+  const int lane = threadIdx.x & 31;
+  Sym32Smem& W = sm_all[threadIdx.x >> 5];
+  const Geo32& g = a.g;
+  const unsigned lt = lanemask_lt();
+  const unsigned wzero = pack10(kW32Bias, kW32Bias, kW32Bias);
+  for (int h = blockIdx.x * kSym32Warps + (threadIdx.x >> 5); h < g.ncells; h += gridDim.x * kSym32Warps) {
+    const int hs = int(a.cell_offsets[h]) - 1, he = int(a.cell_offsets[h + 1]) - 1;
+    const int nb = he - hs;
+    if (nb <= 0) continue;
+    const int ci[3] = {h % g.ns[0] + 1, (h / g.ns[0]) % g.ns[1] + 1, h / (g.ns[0] * g.ns[1]) + 1};
+    // stencil cell q = lane (dx fastest, then dy, dz)
+    int cstart = 0, ccount = 0, sl[3] = {0, 0, 0};
+    bool valid = lane < 27;
+    if (valid) {
+      const int d[3] = {lane % 3 - 1, (lane / 3) % 3 - 1, lane / 9 - 1};
+      int cj[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        if (!g.pbc[k] && (ci[k] + d[k] < 1 || ci[k] + d[k] > g.ns[k])) valid = false;
+        cj[k] = wrap_shift(ci[k] + d[k], g.ns[k], g.pbc[k], sl[k]);
+      }
+      if (valid) {
+        const int lin = (cj[0] - 1) + g.ns[0] * ((cj[1] - 1) + g.ns[1] * (cj[2] - 1));
+        cstart = int(a.cell_offsets[lin]) - 1;
+        ccount = int(a.cell_offsets[lin + 1]) - 1 - cstart;
+      }
+    }
+    if (nb > 32 || __any_sync(0xffffffffu, ccount > 32)) {
+      if (lane == 0) atomicOr(a.sym_fail, 1);
+      continue;
+    }
+    const unsigned slp = (unsigned(sl[0] + 128) & 255u) | ((unsigned(sl[1] + 128) & 255u) << 8) |
+                         ((unsigned(sl[2] + 128) & 255u) << 16);
+    const float lc0 = cts32(g.C, sl[0], sl[1], sl[2], 0), lc1 = cts32(g.C, sl[0], sl[1], sl[2], 1),
+                lc2 = cts32(g.C, sl[0], sl[1], sl[2], 2);
+    if (lane < 27) {
+      unsigned* tab = sym32_table(a.masks, g.nat, h);
+      tab[lane] = unsigned(cstart);
+      tab[27 + lane] = slp;
+    }
+    // words of the home atoms that no other warp writes
+    const unsigned zq = __ballot_sync(0xffffffffu, lane < 13 && (!valid || ccount == 0));
+    if (zq)
+      for (int t = lane; t < nb * 13; t += 32) {
+        const int at = t / 13, q = t - 13 * at;
+        if ((zq >> q) & 1u) a.masks[27LL * (hs + at) + q] = 0u;
+      }
+    __syncwarp();
+    if (lane < nb) {
+      const float4 r = a.rec[hs + lane];
+      const unsigned m = __float_as_uint(r.w);
+      W.hx[lane] = r.x;
+      W.hy[lane] = r.y;
+      W.hz[lane] = r.z;
+      W.hw[lane][0] = field10(m, 0) - kW32Bias;
+      W.hw[lane][1] = field10(m, 1) - kW32Bias;
+      W.hw[lane][2] = field10(m, 2) - kW32Bias;
+      W.hid[lane] = int(a.perm[hs + lane]);
+    }
+#pragma unroll
+    for (int k = 0; k < 14; ++k) W.rmask[lane][k] = 0u;
+    // candidates: the centre and the cells after it (lanes 13..26), flattened
+    const int scnt = lane >= 13 ? ccount : 0;
+    int incl = scnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    const int tg = __shfl_sync(0xffffffffu, incl, 31);
+    __syncwarp();
+    for (int cb = 0; cb < tg; cb += kSym32Chunk) {
+      const int nch = min(kSym32Chunk, tg - cb);
+      for (int f0 = 0; f0 < nch; f0 += 32) {
+        const int f = f0 + lane;
+        const int gf = cb + min(f, nch - 1);
+        int q = 0;
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1) {
+          const int v = __shfl_sync(0xffffffffu, incl, q + step - 1);
+          if (v <= gf) q += step;
+        }
+        const int q_incl = __shfl_sync(0xffffffffu, incl, q);
+        const int q_cnt = __shfl_sync(0xffffffffu, scnt, q);
+        const int q_start = __shfl_sync(0xffffffffu, cstart, q);
+        const unsigned q_slp = __shfl_sync(0xffffffffu, slp, q);
+        const float q0 = __shfl_sync(0xffffffffu, lc0, q), q1 = __shfl_sync(0xffffffffu, lc1, q),
+                    q2 = __shfl_sync(0xffffffffu, lc2, q);
+        if (f < nch) {
+          const int bit = gf - (q_incl - q_cnt);
+          const int js = q_start + bit;
+          const float4 r = a.rec[js];
+          const bool wound = (__float_as_uint(r.w) & kMetaFields) != wzero;
+          W.cx[f] = r.x;
+          W.cy[f] = r.y;
+          W.cz[f] = r.z;
+          W.ex[f] = q0;
+          W.ey[f] = q1;
+          W.ez[f] = q2;
+          W.ctag[f] = (q_slp & 0xFFFFFFu) | (unsigned(q) << 24) | (wound ? (1u << 29) : 0u);
+          W.cjor[f] = int(a.perm[js]);
+          W.cslot[f] = js;
+          W.cbit[f] = (unsigned char)bit;
+          W.ccol[f] = 0u;
+        }
+      }
+      __syncwarp();
+      for (int at = 0; at < nb; ++at) {
+        const float xi = W.hx[at], yi = W.hy[at], zi = W.hz[at];
+        const int wi0 = W.hw[at][0], wi1 = W.hw[at][1], wi2 = W.hw[at][2];
+        const int iid = W.hid[at];
+        const bool hwound = (wi0 | wi1 | wi2) != 0;
+        for (int c0 = 0; c0 < nch; c0 += 32) {
+          const int f = c0 + lane;
+          bool acc = false;
+          unsigned tg2 = 0;
+          if (f < nch) {
+            tg2 = W.ctag[f];
+            const int q = int((tg2 >> 24) & 31u);
+            if (!(q == 13 && W.cjor[f] == iid)) {  // i itself at zero loop shift (the centre)
+              float e0 = W.ex[f], e1 = W.ey[f], e2 = W.ez[f];
+              if (hwound || (tg2 & (1u << 29))) {
+                const unsigned mj = __float_as_uint(a.rec[W.cslot[f]].w);
+                const int S0 = tag_s(tg2, 0) + wi0 - (field10(mj, 0) - kW32Bias);
+                const int S1 = tag_s(tg2, 1) + wi1 - (field10(mj, 1) - kW32Bias);
+                const int S2 = tag_s(tg2, 2) + wi2 - (field10(mj, 2) - kW32Bias);
+                e0 = cts32(g.C, S0, S1, S2, 0);
+                e1 = cts32(g.C, S0, S1, S2, 1);
+                e2 = cts32(g.C, S0, S1, S2, 2);
+              }
+              const float R0 = fadd(fsub(W.cx[f], xi), e0);
+              const float R1 = fadd(fsub(W.cy[f], yi), e1);
+              const float R2 = fadd(fsub(W.cz[f], zi), e2);
+              acc = fadd(fadd(fmul(R0, R0), fmul(R1, R1)), fmul(R2, R2)) < g.cutoff_sq;
+            }
+          }
+          if (acc) {
+            const int q = int((tg2 >> 24) & 31u);
+            atomicOr(&W.rmask[at][q - 13], 1u << W.cbit[f]);
+            if (q > 13) W.ccol[f] |= 1u << at;
+          }
+        }
+      }
+      __syncwarp();
+      for (int f = lane; f < nch; f += 32) {
+        const int q = int((W.ctag[f] >> 24) & 31u);
+        if (q > 13) {
+          const unsigned cc = W.ccol[f];
+          a.masks[27LL * W.cslot[f] + (26 - q)] = cc;
+          if (cc) atomicAdd(a.counts + (W.cjor[f] - 1), __popc(cc));
+        }
+      }
+      __syncwarp();
+    }
+    for (int t = lane; t < nb * 14; t += 32) {
+      const int at = t / 14, k = t - 14 * at;
+      a.masks[27LL * (hs + at) + 13 + k] = W.rmask[at][k];
+    }
+    if (lane < nb) {
+      int c = 0;
+#pragma unroll
+      for (int k = 0; k < 14; ++k) c += __popc(W.rmask[lane][k]);
+      if (c) atomicAdd(a.counts + (W.hid[lane] - 1), c);
+    }
+    __syncwarp();
+  }
+}
+
+// k-th (0-based) set bit of m (m has more than k set bits)
+__device__ __forceinline__ int kth_bit32(unsigned m, int k) {
+  int pos = 0;
+#pragma unroll
+  for (int w = 16; w > 0; w >>= 1) {
+    const int c = __popc(m & ((1u << w) - 1u));
+    if (c <= k) {
+      k -= c;
+      m >>= w;
+      pos += w;
+    }
+  }
+  return pos;
+}
+
+// Write pass from the masks: one warp per atom at a time.  Lane q holds the
+// atom's mask word q; lane r of a pass takes the atom's r-th pair (stencil
+// cell by a shuffle search over the prefix counts, atom by a popcount
+// select), gathers it and writes i, j, S, R (FP32, the reference's
+// arithmetic) at first[i] + r.
+template <typename TI>
+__global__ void __launch_bounds__(128) k_emit32_masks(Pairs32Args<TI> a) {
+  if (*a.sym_fail) return;
+  const Geo32& g = a.g;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = lanemask_lt();
+  for (int s = blockIdx.x * 4 + (threadIdx.x >> 5); s < g.nat; s += gridDim.x * 4) {
+    const float4 ri = a.rec[s];
+    const unsigned mi = __float_as_uint(ri.w);
+    const int wi0 = field10(mi, 0) - kW32Bias, wi1 = field10(mi, 1) - kW32Bias, wi2 = field10(mi, 2) - kW32Bias;
+    const TI iid = a.perm[s];
+    const long long base = (long long)a.first[iid - 1] - 1;
+    const long long nexp = (long long)a.first[iid] - 1 - base;
+    const unsigned m = lane < 27 ? a.masks[27LL * s + lane] : 0u;
+    const unsigned* tab = sym32_table(a.masks, g.nat, a.scell[s]);
+    const int st = lane < 27 ? int(tab[lane]) : 0;
+    const unsigned slp = lane < 27 ? tab[27 + lane] : 0u;
+    const int c = __popc(m);
+    int ex = 0;
+#pragma unroll
+    for (int b = 0; b < 6; ++b) ex += __popc(__ballot_sync(0xffffffffu, (c >> b) & 1) & lt) << b;
+    const int incl = ex + c;
+    const int n = __shfl_sync(0xffffffffu, incl, 31);
+    if (n != nexp) {
+      if (lane == 0) atomicOr(a.err, kFlagInconsistent);
+      continue;
+    }
+    if (base < 0 || base + n > a.capacity) {
+      if (lane == 0) atomicOr(a.err, kFlagCapacity);
+      continue;
+    }
+    for (int r0 = 0; r0 < n; r0 += 32) {
+      const int r = r0 + lane;
+      const int rr = min(r, n - 1);
+      int q = 0;  // first stencil cell whose inclusive count exceeds rr
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const int v = __shfl_sync(0xffffffffu, incl, q + step - 1);
+        if (v <= rr) q += step;
+      }
+      const unsigned mq = __shfl_sync(0xffffffffu, m, q);
+      const int exq = __shfl_sync(0xffffffffu, ex, q);
+      const int stq = __shfl_sync(0xffffffffu, st, q);
+      const unsigned slq = __shfl_sync(0xffffffffu, slp, q);
+      if (r < n) {
+        const int js = stq + kth_bit32(mq, rr - exq);
+        const float4 rj = a.rec[js];
+        const unsigned mj = __float_as_uint(rj.w);
+        const int S0 = tag_s(slq, 0) + wi0 - (field10(mj, 0) - kW32Bias);
+        const int S1 = tag_s(slq, 1) + wi1 - (field10(mj, 1) - kW32Bias);
+        const int S2 = tag_s(slq, 2) + wi2 - (field10(mj, 2) - kW32Bias);
+        const float R0 = fadd(fsub(rj.x, ri.x), cts32(g.C, S0, S1, S2, 0));
+        const float R1 = fadd(fsub(rj.y, ri.y), cts32(g.C, S0, S1, S2, 1));
+        const float R2 = fadd(fsub(rj.z, ri.z), cts32(g.C, S0, S1, S2, 2));
+        const long long pos = base + r;
+        a.oi[pos] = iid;
+        a.oj[pos] = a.perm[js];
+        a.oS[3 * pos + 0] = TI(S0);
+        a.oS[3 * pos + 1] = TI(S1);
+        a.oS[3 * pos + 2] = TI(S2);
+        if (a.oR) {
+          a.oR[3 * pos + 0] = R0;
+          a.oR[3 * pos + 1] = R1;
+          a.oR[3 * pos + 2] = R2;
+        }
+      }
+    }
+  }
+}
+
 }  // namespace
 
 void launch_bin32(const Geo32& g, const float* X, int nat, int* cid, int* ticket, float4* rec, int* cell_count,
@@ -365,10 +661,13 @@ template <typename TI>
 void launch_pairs32(bool fill, const Pairs32Args<TI>& a, int num_sms, cudaStream_t st) {
   if (a.g.nat <= 0) return;
   const int grid = grid_for(a.g.ncells, kW32Warps, num_sms * 12);
-  if (fill)
+  if (fill) {
+    if (a.sym) k_emit32_masks<TI><<<grid_for(a.g.nat, 4, num_sms * 16), 128, 0, st>>>(a);
     k_pairs32<TI, true><<<grid, kW32Warps * 32, 0, st>>>(a);
-  else
+  } else {
+    if (a.sym) k_pairs32_sym<TI><<<grid_for(a.g.ncells, kSym32Warps, num_sms * 16), kSym32Warps * 32, 0, st>>>(a);
     k_pairs32<TI, false><<<grid, kW32Warps * 32, 0, st>>>(a);
+  }
 }
 
 #define NL_INST(TI)                                                                                                 \

@@ -43,6 +43,11 @@ struct Pairs32Args {
   float* oR;                 // may be null
   long long capacity;
   unsigned* err;
+  // symmetric count (27-cell stencils of distinct cells): 27 neighbour-mask
+  // words per atom, then 54 words of stencil table per cell, in `masks`
+  int sym;
+  unsigned* masks;
+  int* sym_fail;             // a cell of more than 32 atoms: the per-cell passes run instead
 };
 
 // binning of the caller's positions (cell id, ticket, record, histogram)

@@ -144,3 +144,20 @@ def test_engine_float32(nlpkg, orc):
         torch.cuda.synchronize()
     with pytest.raises(TypeError):
         eng.launch(Xd.double())
+
+
+def test_symmetric_pass_and_fallback(nlpkg, orc):
+    """The symmetric count with neighbour masks (distinct 27-cell stencils),
+    atoms with more than 64 pairs, and crowded cells (> 32 atoms: the
+    per-cell passes run instead), all identical to the oracle."""
+    X, C, L = cf.rand_config(4000, seed=55)
+    assert_identical(*run_both(nlpkg, orc, X, 6.0, C, (True, True, False)))
+    Xd = np.random.default_rng(7).random((3000, 3)) * 4.0
+    assert_identical(*run_both(nlpkg, orc, Xd, 1.1, np.diag([4.0] * 3), (True, True, True)))
+    for k in (1, 2):  # per-cell passes forced
+        X32 = np.ascontiguousarray(X.astype(np.float32))
+        eng = nlpkg.NeighbourListEngine(X.shape[0], C, 5.0, (True, True, True), dtype=torch.float32)
+        eng.set_tuning(0, 0, k)
+        eng.run(torch.from_numpy(X32).cuda())
+        o = orc.neighbour_list_f32(X32, 5.0, C, (True, True, True))
+        np.testing.assert_array_equal(to_np(eng.pairlist(None).j).astype(np.int64), o.j)
