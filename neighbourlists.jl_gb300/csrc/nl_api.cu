@@ -455,10 +455,11 @@ int count_impl(const nl::Geometry& g, const double* Xs, const TI* perm, const TI
   a.counts = at<int>(ws, L.counts);
   a.half = half;
   a.sym = use_sym(g, L) ? 1 : 0;
-  if (a.sym) {  // the symmetric pass accumulates the counts
-    e = cudaMemsetAsync(a.counts, 0, sizeof(int) * size_t(g.nat), st);
-    if (e != cudaSuccess) return cuda_fail(e, "memset counts");
-  }
+  // the symmetric pass accumulates the counts; without it, sym_fail records
+  // for the write pass that the lists are to be used
+  e = a.sym ? cudaMemsetAsync(a.counts, 0, sizeof(int) * size_t(g.nat), st)
+            : cudaMemsetAsync(a.sym_fail, 0xFF, sizeof(int), st);
+  if (e != cudaSuccess) return cuda_fail(e, "memset counts");
   nl::launch_pairs<TI>(nl::kModeCount, a, sms, st);
   nl::launch_scan<TI>(at<int>(ws, L.counts), g.nat, first, nullptr, at<unsigned long long>(ws, L.st_pairs),
                       at<int>(ws, L.pcount), at<long long>(ws, L.totals) + 1, at<unsigned>(ws, L.err), st);
@@ -473,7 +474,6 @@ int fill_impl(const nl::Geometry& g, const double* Xs, const TI* perm, const TI*
   if (g.nat == 0 || capacity <= 0) return NL_OK;
   nl::PairArgs<TI> a = pair_args<TI>(g, cell_offsets, perm, Xs, ws, L);
   a.half = half;
-  a.sym = use_sym(g, L) ? 1 : 0;
   a.first = first;
   a.oi = oi;
   a.oj = oj;
@@ -604,10 +604,10 @@ int count_impl32(const nl::Geo32& g, const float* Xs, const TI* perm, const TI* 
     nl::launch_prepare32<TI>(g, Xs, cell_id, perm, g.nat, at<float4>(ws, L.rec_sorted), at<int>(ws, L.scell),
                              at<unsigned>(ws, L.err), sms, st);
   const nl::Pairs32Args<TI> a = pairs32_args<TI>(g, cell_offsets, perm, ws, L);
-  if (a.sym) {  // the symmetric pass accumulates the counts
-    e = cudaMemsetAsync(a.counts, 0, sizeof(int) * size_t(g.nat), st);
-    if (e != cudaSuccess) return cuda_fail(e, "memset counts");
-  }
+  // as count_impl: counts accumulated by the symmetric pass, else the record
+  e = a.sym ? cudaMemsetAsync(a.counts, 0, sizeof(int) * size_t(g.nat), st)
+            : cudaMemsetAsync(a.sym_fail, 0xFF, sizeof(int), st);
+  if (e != cudaSuccess) return cuda_fail(e, "memset counts");
   nl::launch_pairs32<TI>(false, a, sms, st);
   nl::launch_scan<TI>(a.counts, g.nat, first, nullptr, at<unsigned long long>(ws, L.st_pairs), at<int>(ws, L.pcount),
                       at<long long>(ws, L.totals) + 1, a.err, st);

@@ -163,7 +163,9 @@ __device__ __forceinline__ int tag_s(unsigned t, int k) { return int((t >> (8 * 
 template <typename TI, bool FILL>
 __global__ void __launch_bounds__(kW32Warps * 32, FILL ? NL_F32_MIN_FILL : NL_F32_MIN_COUNT)
     k_pairs32(Pairs32Args<TI> a) {
-  if (a.sym && *a.sym_fail == 0) return;  // the symmetric count and the mask write pass ran
+  // count: the symmetric pass counted; fill: the count recorded in the
+  // workspace that the mask write pass takes over (sym_fail == 0)
+  if ((FILL || a.sym) && *a.sym_fail == 0) return;
   constexpr int kW32Per = FILL ? NL_F32_PER_FILL : NL_F32_PER_COUNT;
   constexpr int kW32Tile = 32 * kW32Per;
   __shared__ Shared32 sh_all[kW32Warps];
@@ -662,7 +664,7 @@ void launch_pairs32(bool fill, const Pairs32Args<TI>& a, int num_sms, cudaStream
   if (a.g.nat <= 0) return;
   const int grid = grid_for(a.g.ncells, kW32Warps, num_sms * 12);
   if (fill) {
-    if (a.sym) k_emit32_masks<TI><<<grid_for(a.g.nat, 4, num_sms * 16), 128, 0, st>>>(a);
+    k_emit32_masks<TI><<<grid_for(a.g.nat, 4, num_sms * 16), 128, 0, st>>>(a);
     k_pairs32<TI, true><<<grid, kW32Warps * 32, 0, st>>>(a);
   } else {
     if (a.sym) k_pairs32_sym<TI><<<grid_for(a.g.ncells, kSym32Warps, num_sms * 16), kSym32Warps * 32, 0, st>>>(a);

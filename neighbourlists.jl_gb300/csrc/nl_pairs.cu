@@ -1067,7 +1067,8 @@ __device__ __forceinline__ int kth_bit(unsigned m, int k) {
 }
 
 // MASKS: the pairs come from the symmetric count pass's neighbour masks
-// instead of lists; lane r of a pass finds the atom's r-th pair from the
+// instead of lists (single systems; both variants are launched and the count's
+// record in the workspace selects one); lane r of a pass finds the atom's r-th pair from the
 // prefix counts of its 27 mask words (stencil order, then sorted order in the
 // cell), so the output order is the same.  Atoms of more than list_cap pairs
 // are left to the screening write pass (their cells are listed here).
@@ -1079,7 +1080,9 @@ __device__ __forceinline__ int kth_bit(unsigned m, int k) {
 template <typename TI, bool BATCH, bool MASKS>
 __global__ void __launch_bounds__(kEmitWarps * 32, MASKS ? NL_EMIT_MIN_MASK_BLOCKS : kEmitMinBlocks)
     k_emit(PairArgs<TI> A) {
-  if (!BATCH && A.sym && ((*A.sym_fail == 0) != MASKS)) return;  // the other variant writes
+  // the count recorded its choice in the workspace: sym_fail == 0 after a
+  // successful symmetric count (masks), non-zero otherwise (lists)
+  if (!BATCH && ((*A.sym_fail == 0) != MASKS)) return;
   __shared__ EmitAtoms ea[kEmitWarps];
   __shared__ double cs_blk[BATCH ? 1 : 3 * kCsN * kCsN * kCsN];
   if (!BATCH) {
@@ -1108,7 +1111,12 @@ __global__ void __launch_bounds__(kEmitWarps * 32, MASKS ? NL_EMIT_MIN_MASK_BLOC
           const int u = atomicAdd(A.n_screen_cells, 1);
           if (u < A.ncells_total) A.screen_cells[u] = hl;
         }
-        E.base[lane] = (long long)A.first[clampi(A.perm[slot] - 1, A.nat_total - 1)] - 1;
+        const int orig = clampi(A.perm[slot] - 1, A.nat_total - 1);
+        E.base[lane] = (long long)A.first[orig] - 1;
+        if ((long long)A.first[orig + 1] - 1 - E.base[lane] != n) {  // counts and masks disagree
+          atomicOr(A.err, kFlagInconsistent);
+          E.n[lane] = 0;
+        }
       } else {
         int n = A.lcount[slot];
         E.n[lane] = n > K ? 0 : n;  // overflowed atoms belong to the screening pass
@@ -1580,7 +1588,7 @@ static void launch_modes(int mode, const PairArgs<TI>& a, int num_sms, cudaStrea
         long long eb = ((long long)a.nat_total + 32 * kEmitWarps - 1) / (32 * kEmitWarps);
         if (eb > (long long)num_sms * ebps) eb = (long long)num_sms * ebps;
         k_emit<TI, BATCH, false><<<int(eb), kEmitWarps * 32, 0, st>>>(a);
-        if (!BATCH && a.sym) k_emit<TI, false, true><<<int(eb), kEmitWarps * 32, 0, st>>>(a);
+        if (!BATCH) k_emit<TI, false, true><<<int(eb), kEmitWarps * 32, 0, st>>>(a);
       }
       k_pairs<TI, kModeFill, BATCH><<<int(blocks), kPairWarps * 32, 0, st>>>(a);
       break;

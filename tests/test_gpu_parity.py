@@ -529,3 +529,46 @@ def test_half_int64_and_verlet_half(nlpkg, orc):
     got = set(zip(i[inside].tolist(), j[inside].tolist(), map(tuple, S[inside].tolist())))
     want = set(zip(o2.i[keep2].tolist(), o2.j[keep2].tolist(), map(tuple, o2.S[keep2].tolist())))
     assert got == want
+
+
+def test_fill_follows_the_count_choice(nlpkg, orc):
+    """The write pass follows the count pass recorded in the workspace, even
+    when the calling thread's tuning changed in between (symmetric count then
+    list-mode tuning, and the reverse)."""
+    import ctypes as C
+
+    from neighbourlists_gb300 import _lib
+    from neighbourlists_gb300.api import _plan_args, _pbc, _ptr, _stream_handle
+
+    X, Cm, L = cf.rand_config(6000, seed=91)
+    o = orc.neighbour_list(X, 5.0, Cm, (True, True, True), nthreads=8)
+    L_ = nlpkg.lib()
+    for before, after in ((3, 1), (1, 3), (2, 0)):
+        clist = nlpkg.build_cell_list(torch.from_numpy(X).cuda(), 5.0, Cm, (True, True, True))
+        nat = X.shape[0]
+        first = torch.empty(nat + 1, dtype=torch.int32, device="cuda")
+        total = C.c_int64(0)
+        cm, im, nc, nx = _plan_args(clist)
+        pb = _pbc(clist.pbc)
+        sh = _stream_handle(None)
+        _lib.check(L_.nl_set_tuning(C.byref(_lib.Tuning(0, 0, before))))
+        _lib.check(L_.nl_count_pairs(_ptr(clist.X), _ptr(clist.perm), _ptr(clist.cell_id),
+                                     C.c_void_p(clist.cell_offsets.data_ptr()), nat, cm, im, nc, nx,
+                                     pb.ctypes.data_as(C.POINTER(C.c_uint8)), 5.0, 4, 1,
+                                     C.c_void_p(first.data_ptr()), C.byref(total), _ptr(clist._ws), clist._ws.numel(), sh))
+        P = int(total.value)
+        i = torch.empty(P, dtype=torch.int32, device="cuda")
+        j = torch.empty_like(i)
+        S = torch.empty((P, 3), dtype=torch.int32, device="cuda")
+        R = torch.empty((P, 3), dtype=torch.float64, device="cuda")
+        _lib.check(L_.nl_set_tuning(C.byref(_lib.Tuning(0, 0, after))))
+        _lib.check(L_.nl_fill_pairs(_ptr(clist.X), _ptr(clist.perm), C.c_void_p(clist.cell_offsets.data_ptr()), nat,
+                                    cm, im, nc, nx, pb.ctypes.data_as(C.POINTER(C.c_uint8)), 5.0, 4,
+                                    C.c_void_p(first.data_ptr()), P, _ptr(i), _ptr(j), _ptr(S), _ptr(R), _ptr(clist._ws),
+                                    clist._ws.numel(), sh))
+        _lib.check(L_.nl_sync_status(_ptr(clist._ws), sh))
+        _lib.check(L_.nl_set_tuning(None))
+        assert P == o.npairs
+        np.testing.assert_array_equal(to_np(j).astype(np.int64), o.j)
+        np.testing.assert_array_equal(to_np(S).astype(np.int64), o.S)
+        assert np.array_equal(to_np(R).view(np.int64), o.R.view(np.int64))
