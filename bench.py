@@ -590,8 +590,8 @@ def measure_e2e(eng, X, Xd, total, stream, dev, args):
 
 def run_path(args):
     """Profiling runs of the Float32 and legacy paths on the benchmark's
-    workload shape (``--atoms`` sets the size).  Prints one JSON line that is
-    not the benchmark line."""
+    workload shape (``--atoms`` sets the size) and of the 4,096-system batch.
+    Prints one JSON line that is not the benchmark line."""
     import time
 
     import torch
@@ -605,7 +605,20 @@ def run_path(args):
     stream = torch.cuda.current_stream(dev)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
     steps = max(args.steps, 1)
-    if args.path == "float32":
+    if args.path == "batched":
+        import configs as cf
+
+        systems = cf.batch_systems(4096, seed=0)
+        Xb = torch.from_numpy(np.ascontiguousarray(np.concatenate([x for (x, _, _, _) in systems]))).to(dev)
+        b = nl.BatchNeighbourList([(x.shape[0], c, rc, p) for (x, c, rc, p) in systems], device=dev)
+        total = b.run(Xb)
+        for _ in range(args.warmup):
+            b.launch(Xb)
+        ms = timed_steps(lambda: b.launch(Xb), steps, flush, stream)
+        b.sync_status()
+        out = {"pairs": int(total), "ms_per_batch": ms, "systems": len(systems),
+               "timing": "CUDA events, default launch shapes, no graph, L2 flushed before every batch"}
+    elif args.path == "float32":
         X32 = torch.from_numpy(X.astype(np.float32)).to(dev)
         eng = nl.NeighbourListEngine(X.shape[0], C, CUTOFF, pbc, device=dev, dtype=torch.float32)
         total = eng.run(X32)
@@ -639,8 +652,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the lazy / batched / 4M sections")
     ap.add_argument("--atoms", type=int, default=N_ATOMS, help="system size (profiling runs use a smaller one)")
-    ap.add_argument("--path", default="headline", choices=["headline", "float32", "legacy"],
-                    help="float32 / legacy: profiling runs of those paths (not the benchmark line)")
+    ap.add_argument("--path", default="headline", choices=["headline", "float32", "legacy", "batched"],
+                    help="float32 / legacy / batched: profiling runs of those paths (not the benchmark line)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -1039,7 +1039,7 @@ constexpr int kEmitMinBlocks = NL_EMIT_MIN_BLOCKS;  // resident blocks per SM th
 
 struct __align__(16) EmitAtoms {
   long long sbuf[96];   // a pass's S, three words per pair, staged for contiguous stores
-  unsigned short pass[64];  // the chunk's passes: atom << 8 | pass within the atom
+  unsigned short pass[kListCap];  // the chunk's passes (32 atoms, kListCap / 32 each): atom << 8 | pass
   double rbuf[96];      // a pass's R, likewise
   double xi[32][3];     // FP64 position
   long long base[32];   // first output slot (0-based)
@@ -1233,22 +1233,24 @@ __global__ void __launch_bounds__(kEmitWarps * 32, MASKS ? NL_EMIT_MIN_MASK_BLOC
           if constexpr (MASKS) {
             // lane r takes the atom's r-th pair.  Lane q holds mask word q
             // (c_q pairs); its pairs are r in [ex_q, ex_q + c_q).  ex_q by
-            // bit-sliced ballots (c_q <= 32), the starts of the non-empty
-            // runs as a bit set, the run of r by a popcount, its stencil cell
-            // from qmap, then the k-th atom of that cell's mask.
+            // bit-sliced ballots (c_q <= 32); the pass covers r in
+            // [base, base + 32): the non-empty runs starting before base are
+            // counted by a ballot, those starting in the window form a bit
+            // set, so the run of r is a popcount; its stencil cell comes from
+            // qmap, then the k-th atom of that cell's mask.
             const unsigned lt = lt_mask();
             const int c = __popc(t.m);
             int ex = 0;
 #pragma unroll
             for (int b = 0; b < 6; ++b) ex += __popc(__ballot_sync(0xffffffffu, (c >> b) & 1) & lt) << b;
             const unsigned ne = __ballot_sync(0xffffffffu, c != 0);
-            const unsigned starts_lo = __reduce_or_sync(0xffffffffu, c && ex < 32 ? 1u << ex : 0u);
-            const unsigned starts_hi = __reduce_or_sync(0xffffffffu, c && ex >= 32 ? 1u << (ex - 32) : 0u);
+            const int base = t.r - lane;  // the pass's first pair (a multiple of 32)
+            const unsigned before = __ballot_sync(0xffffffffu, c != 0 && ex < base);
+            const unsigned win = __reduce_or_sync(0xffffffffu, c && ex >= base && ex < base + 32 ? 1u << (ex - base) : 0u);
             if (c) E.qmap[__popc(ne & lt)] = (unsigned char)lane;
             __syncwarp();
-            const int r = min(t.r, E.n[t.a] - 1);  // 0 <= r < 64
-            const int j = r < 32 ? __popc(starts_lo & (0xffffffffu >> (31 - r))) - 1
-                                 : __popc(starts_lo) + __popc(starts_hi & (0xffffffffu >> (63 - r))) - 1;
+            const int r = min(t.r, E.n[t.a] - 1);  // base <= r < base + 32
+            const int j = __popc(before) + __popc(win & (0xffffffffu >> (31 - (r - base)))) - 1;
             const int q = E.qmap[j];
             __syncwarp();
             const unsigned mq = __shfl_sync(0xffffffffu, t.m, q);

@@ -11,7 +11,10 @@ enum PairMode : int { kModeCount = 0, kModeFill = 1, kModeLazyR6 = 2 };
 // list of kListCap entries.  The write pass (k_emit) turns the lists into
 // i, j, S, R without screening again; cells with an atom of more than
 // kListCap pairs are listed for the screening write pass instead.
-constexpr int kListCap = 64;
+#ifndef NL_LIST_CAP
+#define NL_LIST_CAP 192
+#endif
+constexpr int kListCap = NL_LIST_CAP;  // at most 255 * 32 (the write pass numbers passes in 8 bits)
 
 // doubles in one C'S table (|S_k| <= 2)
 constexpr int kCsTableDoubles = 3 * 125;

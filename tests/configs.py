@@ -29,6 +29,23 @@ def rand_config(N, density=0.05, seed=0):
     return X, np.diag([L, L, L]), L
 
 
+def corner_clump(N, cutoff, per_octant=28, density=0.05, seed=0):
+    """A uniform cubic box whose 8 cells around one interior corner of the
+    cell grid (floor(L / cutoff) cells per axis) hold only a clump of
+    8 * per_octant atoms within 0.9 A of that corner, per_octant in each cell:
+    the clump's atoms have more than 8 * per_octant - 1 pairs while no cell
+    holds more than max(per_octant, background) atoms.  Returns X, cell, L."""
+    X, C, L = rand_config(N, density, seed)
+    ns = int(np.floor(L / cutoff))
+    w = L / ns
+    corner = np.full(3, (ns // 2) * w)
+    X = X[np.any(np.abs(X - corner) >= w, axis=1)]
+    rng = np.random.default_rng(seed + 1)
+    signs = np.array([[sx, sy, sz] for sx in (-1, 1) for sy in (-1, 1) for sz in (-1, 1)], dtype=float)
+    clump = corner + np.repeat(signs, per_octant, axis=0) * rng.uniform(0.05, 0.9 / np.sqrt(3), (8 * per_octant, 3))
+    return np.concatenate([X, clump]), C, L
+
+
 def triclinic_cell():
     """rand_non_cubic_cell (test_utils.jl:297-299); rows are lattice vectors."""
     return np.array([[10.0, 2.0, 1.0], [0.0, 9.0, 1.5], [0.0, 0.0, 8.0]])

@@ -286,10 +286,12 @@ def test_minimal_workspace_screening_write(nlpkg, orc, case):
 @pytest.mark.parametrize("case", ["dense", "fcc", "min_workspace"])
 def test_lazy_inv_r6_paths(nlpkg, orc, case):
     """Lazy sum 1/r^6: from the per-atom lists, through the screening pass for
-    overflowed cells (dense: > 64 pairs per atom), and with no lists at all
-    (minimal workspace) -- bit-identical to the oracle in every case."""
+    overflowed cells (dense, with a clump of atoms of more than 192 pairs),
+    and with no lists at all (minimal workspace) -- bit-identical to the
+    oracle in every case."""
     if case == "dense":
-        X = np.random.default_rng(6).random((400, 3)) * 6.0
+        rng = np.random.default_rng(6)
+        X = np.concatenate([rng.random((400, 3)) * 6.0, 3.0 + (rng.random((150, 3)) - 0.5) * 1.2])
         C, pbc, rc = np.diag([6.0] * 3), (True, True, True), 2.2
     else:
         X, C, pbc = cf.fcc_sheared(n=5, seed=4)
@@ -345,9 +347,10 @@ def test_both_count_kernels(nlpkg, orc, count_kernel):
 
 
 def test_count_pass_edge_cases(nlpkg, orc):
-    """Exact atoms far outside an open axis, lists that overflow (> 64 pairs:
-    those cells go to the screening write pass) next to cells that do not, a
-    crowded cell (> 32 atoms: the symmetric pass falls back), open
+    """Exact atoms far outside an open axis, lists that overflow (> 192
+    pairs: those cells go to the screening write pass) next to cells that do
+    not, in cells of at most 32 atoms (symmetric pass) and in crowded cells
+    (> 32 atoms: the symmetric pass falls back), open
     boundaries, Int64; and the symmetric and per-atom count passes giving
     identical lists on 20k atoms."""
     rng = np.random.default_rng(54)
@@ -355,8 +358,14 @@ def test_count_pass_edge_cases(nlpkg, orc):
     Xo = X.copy()
     Xo[:30, 2] += rng.choice([-1, 1], 30) * rng.uniform(2.0, 40.0, 30) * L  # far outside the open z axis
     dense = np.concatenate([X, rng.random((40, 3)) * 0.5 + L / 2])              # one crowded cell
+    Xc5, Cc, _ = cf.corner_clump(4000, 5.0, seed=55)
+    Xc6 = cf.corner_clump(4000, 6.0, seed=55)[0]
+    Xm = cf.corner_clump(4000, 5.0, per_octant=20, seed=57)[0]  # 65..192 pairs decoded from the masks
+    clump = np.concatenate([X, L / 3 + (rng.random((250, 3)) - 0.5) * 1.5])  # > 192 pairs, one crowded cell
     cases = [(X, C, 5.0, (True, True, True)), (Xo, C, 5.0, (True, True, False)), (X, C, 6.0, (True, True, True)),
-             (dense, C, 5.0, (True, True, True)), (X, C, 5.0, (False, False, False))]
+             (dense, C, 5.0, (True, True, True)), (X, C, 5.0, (False, False, False)),
+             (Xc5, Cc, 5.0, (True, True, True)), (Xc6, Cc, 6.0, (True, True, False)), (clump, C, 5.0, (True, True, True)),
+             (Xm, Cc, 5.0, (True, True, True))]
     for X_, C_, rc, pbc in cases:
         for it in (torch.int32, torch.int64):
             g = nlpkg.neighbour_list(torch.from_numpy(np.ascontiguousarray(X_)).cuda(), rc, C_, pbc, int_type=it)
@@ -448,8 +457,8 @@ def test_half_lists(nlpkg, orc, case, count_kernel):
     elif case == "triclinic":
         X, C = cf.rand_config_triclinic(300, seed=82)
         rc, pbc = 3.0, (True, False, True)
-    else:  # > 64 pairs for some atoms, cells of <= 32 atoms: masks plus the screening write pass
-        X, C, L = cf.rand_config(4000, seed=55)
+    else:  # > 192 pairs for some atoms, cells of <= 32 atoms: masks plus the screening write pass
+        X, C, L = cf.corner_clump(4000, 6.0, seed=55)
         rc, pbc = 6.0, (True, True, False)
     eng = nlpkg.NeighbourListEngine(X.shape[0], C, rc, pbc, half=True)
     eng.set_tuning(0, 0, count_kernel)
