@@ -616,7 +616,7 @@ def run_path(args):
             b.launch(Xb)
         ms = timed_steps(lambda: b.launch(Xb), steps, flush, stream)
         b.sync_status()
-        out = {"pairs": int(total), "ms_per_batch": ms, "systems": len(systems),
+        out = {"atoms": int(Xb.shape[0]), "pairs": int(total), "ms_per_batch": ms, "systems": len(systems),
                "timing": "CUDA events, default launch shapes, no graph, L2 flushed before every batch"}
     elif args.path == "float32":
         X32 = torch.from_numpy(X.astype(np.float32)).to(dev)
@@ -638,8 +638,8 @@ def run_path(args):
         torch.cuda.synchronize(dev)
         out = {"pairs": int(lg.i.numel()), "ms_per_call": (time.perf_counter() - t0) / steps * 1e3,
                "timing": "host clock around the whole synchronising call"}
-    print(json.dumps({"metric": "profiling run (not the benchmark line)", "path": args.path, "atoms": args.atoms,
-                      **out}))
+    print(json.dumps({"metric": "profiling run (not the benchmark line)", "path": args.path,
+                      **{"atoms": args.atoms, **out}}))
 
 
 def main():
