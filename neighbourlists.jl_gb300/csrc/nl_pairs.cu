@@ -362,7 +362,7 @@ __device__ __forceinline__ void load_system(const PairArgs<TI>& A, int s, Geomet
 
 template <typename TI, int MODE, bool BATCH>
 __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<TI> A) {
-  if (MODE == kModeCount && A.sym && *A.sym_fail == 0) return;  // the symmetric pass counted
+  if (MODE == kModeCount && !BATCH && A.sym && *A.sym_fail == 0) return;  // the symmetric pass counted
   __shared__ WarpSmem sm[kPairWarps];
   __shared__ double cs_blk[BATCH ? 1 : 3 * kCsN * kCsN * kCsN];
   __shared__ unsigned dtab_blk[BATCH ? 32 * kPairWarps : kStencilTab];  // packed (d0, d1, d2) of stencil cell q
@@ -435,6 +435,8 @@ __global__ void __launch_bounds__(kPairWarps * 32, kMinBlocks) k_pairs(PairArgs<
     sv.hl = h;
     if constexpr (BATCH) {
       sv.s = batch_system(A.sys_cell, A.nsys, h);
+      // systems the symmetric pass counted
+      if (MODE == kModeCount && A.sym && A.sys_sym[sv.s] && !A.sys_fail[sv.s]) continue;
       if (sv.s != cur_sys) {
         load_system<TI, BATCH>(A, sv.s, geo_w[warp], dtab_blk + 32 * warp, lane);
         set_stencil();
@@ -754,21 +756,30 @@ constexpr int kSymWarps = 4;
 #ifndef NL_SYM_MIN_BLOCKS
 #define NL_SYM_MIN_BLOCKS 8
 #endif
+#ifndef NL_SYM_BATCH_MIN_BLOCKS
+#define NL_SYM_BATCH_MIN_BLOCKS 6  // the batch variant keeps a per-system view in registers
+#endif
 constexpr int kSymChunk = NL_SYM_CHUNK;  // staged candidates per round of home atoms
 constexpr int kSymGroup = NL_SYM_GROUP;  // home atoms screened per candidate load
 // record meta of an atom without windings that is not exact
 constexpr unsigned kPlainMeta = (128u) | (128u << 10) | (128u << 20);
 
-template <typename TI>
-__device__ __forceinline__ unsigned* sym_word(const PairArgs<TI>& A, int slot) {
-  return reinterpret_cast<unsigned*>(A.lists) + 27LL * slot;
+// The 27 mask words of a sorted slot: single systems store them densely;
+// batches, whose systems mix masks and lists, at the start of the slot's own
+// list region (2 list_cap words), so the two never overlap.
+template <typename TI, bool BATCH>
+__device__ __forceinline__ unsigned* sym_word(const PairArgs<TI>& A, long long slot) {
+  return BATCH ? reinterpret_cast<unsigned*>(A.lists + slot * A.list_cap)
+               : reinterpret_cast<unsigned*>(A.lists) + 27LL * slot;
 }
 // per non-empty home cell: first sorted slot (27 words) and loop-shift base
-// (27 words) of its stencil cells, after the masks (the host checks that
-// 27 nat + 54 ncells words fit the list region)
-template <typename TI>
-__device__ __forceinline__ unsigned* sym_table(const PairArgs<TI>& A, int cell) {
-  return reinterpret_cast<unsigned*>(A.lists) + 27LL * A.g.nat + 54LL * cell;
+// (27 words) of its stencil cells.  Single systems: after the masks (the
+// host checks that 27 nat + 54 ncells words fit the list region); batches:
+// after the masks in the list region of the cell's first slot.
+template <typename TI, bool BATCH>
+__device__ __forceinline__ unsigned* sym_table(const PairArgs<TI>& A, int cell, int first_slot) {
+  return BATCH ? sym_word<TI, true>(A, first_slot) + 27
+               : reinterpret_cast<unsigned*>(A.lists) + 27LL * A.g.nat + 54LL * cell;
 }
 
 struct __align__(16) SymSmem {
@@ -784,21 +795,46 @@ struct __align__(16) SymSmem {
   int prune;
 };
 
-template <typename TI>
-__global__ void __launch_bounds__(kSymWarps * 32, NL_SYM_MIN_BLOCKS) k_pairs_sym(PairArgs<TI> A) {
+// Batches run it over the cells of the systems flagged in sys_sym, with each
+// system's geometry and its cells and slots offset to the launch's; a system
+// with a crowded cell sets its sys_fail and the per-cell pass counts it.
+template <typename TI, bool BATCH>
+__global__ void __launch_bounds__(kSymWarps * 32, BATCH ? NL_SYM_BATCH_MIN_BLOCKS : NL_SYM_MIN_BLOCKS)
+    k_pairs_sym(PairArgs<TI> A) {
   __shared__ SymSmem sm[kSymWarps];
+  __shared__ Geometry geo_w[BATCH ? kSymWarps : 1];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   SymSmem& W = sm[warp];
-  const Geometry& g = A.g;
-  const float lo = g.lo, hi = g.hi;
+  const Geometry& g = BATCH ? geo_w[warp] : A.g;
+  const int nat = A.nat_total;  // slot bound (g.nat for a single system)
   const unsigned lt = lt_mask();
   unsigned rechecks = 0;
+  int cur_sys = -1;
   if (A.cap_rec && blockIdx.x == 0 && threadIdx.x == 0) *A.cap_rec = A.list_cap;
   for (int h = blockIdx.x * kSymWarps + warp; h < A.ncells_total; h += gridDim.x * kSymWarps) {
-    const int hs = clampi(A.cell_offsets[h] - 1, g.nat), he = clampi(A.cell_offsets[h + 1] - 1, g.nat);
+    // system view: first slot / original atom, index of cell 0 in cell_offsets, home cell in the system
+    int sys = 0, abase = 0, coff = 0, hl = h;
+    if constexpr (BATCH) {
+      sys = batch_system(A.sys_cell, A.nsys, h);
+      if (!A.sys_sym[sys]) continue;
+      if (sys != cur_sys) {
+        __syncwarp();
+        const int* src = reinterpret_cast<const int*>(A.geo + sys);
+        int* dst = reinterpret_cast<int*>(&geo_w[warp]);
+        for (int k = lane; k < int(sizeof(Geometry) / 4); k += 32) dst[k] = src[k];
+        __syncwarp();
+        cur_sys = sys;
+      }
+      abase = A.sys_atom[sys];
+      coff = A.sys_cell[sys] + sys;
+      hl = h - A.sys_cell[sys];
+    }
+    const float lo = g.lo, hi = g.hi;
+    const int hs = clampi(A.cell_offsets[coff + hl] - 1 + abase, nat);
+    const int he = clampi(A.cell_offsets[coff + hl + 1] - 1 + abase, nat);
     const int nb = he - hs;
     if (nb <= 0) continue;
-    const int hc0 = h % g.ns[0] + 1, hc1 = (h / g.ns[0]) % g.ns[1] + 1, hc2 = h / (g.ns[0] * g.ns[1]) + 1;
+    const int hc0 = hl % g.ns[0] + 1, hc1 = (hl / g.ns[0]) % g.ns[1] + 1, hc2 = hl / (g.ns[0] * g.ns[1]) + 1;
     // stencil cell q = lane
     int cstart = 0, ccount = 0, lin = -1;
     unsigned slp = 0;
@@ -806,16 +842,16 @@ __global__ void __launch_bounds__(kSymWarps * 32, NL_SYM_MIN_BLOCKS) k_pairs_sym
     if (lane < 27) {
       lin = stencil_cell(g, nullptr, 0, 3, 3, hc0, hc1, hc2, lane, slp, ox, oy, oz);
       if (lin >= 0) {
-        cstart = clampi(A.cell_offsets[lin] - 1, g.nat);
-        ccount = max(clampi(A.cell_offsets[lin + 1] - 1, g.nat) - cstart, 0);
+        cstart = clampi(A.cell_offsets[coff + lin] - 1 + abase, nat);
+        ccount = max(clampi(A.cell_offsets[coff + lin + 1] - 1 + abase, nat) - cstart, 0);
       }
     }
     if (nb > 32 || __any_sync(0xffffffffu, ccount > 32)) {
-      if (lane == 0) atomicOr(A.sym_fail, 1);
+      if (lane == 0) atomicOr(BATCH ? A.sys_fail + sys : A.sym_fail, 1);
       continue;
     }
     if (lane < 27) {  // the write pass reads the cell's stencil from here
-      unsigned* tab = sym_table(A, h);
+      unsigned* tab = sym_table<TI, BATCH>(A, h, hs);
       tab[lane] = unsigned(cstart);
       tab[27 + lane] = slp;
     }
@@ -824,7 +860,7 @@ __global__ void __launch_bounds__(kSymWarps * 32, NL_SYM_MIN_BLOCKS) k_pairs_sym
     if (zq)
       for (int t = lane; t < nb * 13; t += 32) {
         const int a = t / 13, q = t - 13 * a;
-        if ((zq >> q) & 1u) sym_word(A, hs + a)[q] = 0u;
+        if ((zq >> q) & 1u) sym_word<TI, BATCH>(A, hs + a)[q] = 0u;
       }
     __syncwarp();
     float ux = 0.f, uy = 0.f, uz = 0.f;
@@ -836,9 +872,9 @@ __global__ void __launch_bounds__(kSymWarps * 32, NL_SYM_MIN_BLOCKS) k_pairs_sym
       uz = r.z;
       hm = __float_as_uint(r.w);
       W.hmeta[lane] = hm;
-      W.horig[lane] = clampi(A.perm[hs + lane] - 1, g.nat - 1);
+      W.horig[lane] = abase + clampi(A.perm[hs + lane] - 1, g.nat - 1);  // original index in the launch
     }
-    if (__any_sync(0xffffffffu, hm != kPlainMeta) && lane == 0) atomicOr(A.sym_wound, 1);
+    if (!BATCH && __any_sync(0xffffffffu, hm != kPlainMeta) && lane == 0) atomicOr(A.sym_wound, 1);
 #pragma unroll
     for (int k = 0; k < 14; ++k) W.rmask[lane][k] = 0u;
     {
@@ -913,14 +949,14 @@ __global__ void __launch_bounds__(kSymWarps * 32, NL_SYM_MIN_BLOCKS) k_pairs_sym
           const float dz = fmaxf(fmaxf(W.box[4] - cv.z, cv.z - W.box[5]), 0.f);
           const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
           keep = ex || !(prune && d2 > hi);
-          if (!keep && q > 13) sym_word(A, slot)[26 - q] = 0u;
+          if (!keep && q > 13) sym_word<TI, BATCH>(A, slot)[26 - q] = 0u;
         }
         const unsigned km = __ballot_sync(0xffffffffu, keep);
         if (keep) {
           const int pos = nkeep + __popc(km & lt);
           W.cv[pos] = cv;
           W.cslot[pos] = slot;
-          W.corig[pos] = clampi(A.perm[slot] - 1, g.nat - 1);
+          W.corig[pos] = abase + clampi(A.perm[slot] - 1, g.nat - 1);
           W.cqb[pos] = (unsigned(q) << 8) | unsigned(bit);
           W.ccol[pos] = 0u;
         }
@@ -999,7 +1035,7 @@ __global__ void __launch_bounds__(kSymWarps * 32, NL_SYM_MIN_BLOCKS) k_pairs_sym
         const unsigned q = W.cqb[f] >> 8;
         if (q > 13) {
           const unsigned cc = W.ccol[f];
-          sym_word(A, W.cslot[f])[26 - q] = cc;
+          sym_word<TI, BATCH>(A, W.cslot[f])[26 - q] = cc;
           if (cc) atomicAdd(A.counts + W.corig[f], __popc(cc));
         }
       }
@@ -1008,13 +1044,13 @@ __global__ void __launch_bounds__(kSymWarps * 32, NL_SYM_MIN_BLOCKS) k_pairs_sym
     // ---- rows: words q = 13..26 of the home atoms, and their counts
     for (int t = lane; t < nb * 14; t += 32) {
       const int a = t / 14, k = t - 14 * a;
-      sym_word(A, hs + a)[13 + k] = W.rmask[a][k];
+      sym_word<TI, BATCH>(A, hs + a)[13 + k] = W.rmask[a][k];
     }
     if (lane < nb) {
       int c = 0;
 #pragma unroll
       for (int k = 0; k < 14; ++k) c += __popc(W.rmask[lane][k]);
-      if (c) atomicAdd(A.counts + clampi(A.perm[hs + lane] - 1, g.nat - 1), c);
+      if (c) atomicAdd(A.counts + W.horig[lane], c);
     }
     __syncwarp();
   }
@@ -1047,7 +1083,7 @@ struct __align__(16) EmitAtoms {
   unsigned mi[32];      // packed windings | exact bit
   int n[32];            // listed pairs (0 when written by the screening pass)
   int sys[32];          // batch: system of the slot
-  int cell[32];         // neighbour masks: 0-based home cell of the slot
+  int cell[32];         // neighbour masks: 0-based home cell of the slot (batches: the cell's first slot)
   unsigned char qmap[32];  // neighbour masks: stencil cell of the k-th non-empty mask word
 };
 
@@ -1067,18 +1103,17 @@ __device__ __forceinline__ int kth_bit(unsigned m, int k) {
 }
 
 // MASKS: the pairs come from the symmetric count pass's neighbour masks
-// instead of lists (single systems; both variants are launched and the count's
-// record in the workspace selects one); lane r of a pass finds the atom's r-th pair from the
+// instead of lists (both variants are launched; for a single system the
+// count's record in the workspace selects one, in a batch each takes the
+// atoms of its systems); lane r of a pass finds the atom's r-th pair from the
 // prefix counts of its 27 mask words (stencil order, then sorted order in the
 // cell), so the output order is the same.  Atoms of more than list_cap pairs
 // are left to the screening write pass (their cells are listed here).
 #ifndef NL_EMIT_MASK_MIN_BLOCKS
-#define NL_EMIT_MIN_MASK_BLOCKS 6
-#else
-#define NL_EMIT_MIN_MASK_BLOCKS NL_EMIT_MASK_MIN_BLOCKS
+#define NL_EMIT_MASK_MIN_BLOCKS 6  // resident blocks per SM the mask variant is compiled for
 #endif
 template <typename TI, bool BATCH, bool MASKS>
-__global__ void __launch_bounds__(kEmitWarps * 32, MASKS ? NL_EMIT_MIN_MASK_BLOCKS : kEmitMinBlocks)
+__global__ void __launch_bounds__(kEmitWarps * 32, MASKS ? NL_EMIT_MASK_MIN_BLOCKS : kEmitMinBlocks)
     k_emit(PairArgs<TI> A) {
   // the count recorded its choice in the workspace: sym_fail == 0 after a
   // successful symmetric count (masks), non-zero otherwise (lists)
@@ -1092,26 +1127,41 @@ __global__ void __launch_bounds__(kEmitWarps * 32, MASKS ? NL_EMIT_MIN_MASK_BLOC
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   EmitAtoms& E = ea[warp];
   const int K = A.list_cap;
-  const bool plain = MASKS && *A.sym_wound == 0;  // no atom has a winding: candidate words need no record
+  // no atom has a winding (single systems record it): candidate words need no record
+  const bool plain = MASKS && !BATCH && *A.sym_wound == 0;
   const long long nwarps = (long long)gridDim.x * kEmitWarps;
   for (long long c0 = ((long long)blockIdx.x * kEmitWarps + warp) * 32; c0 < A.nat_total; c0 += nwarps * 32) {
     const int na = int(min(32LL, A.nat_total - c0));
     __syncwarp();
     if (lane < na) {
       const int slot = int(c0) + lane;
-      if constexpr (MASKS) {
-        const unsigned* mw = reinterpret_cast<const unsigned*>(A.lists) + 27LL * slot;
+      const int sys = BATCH ? batch_system(A.sys_atom, A.nsys, slot) : 0;
+      E.sys[lane] = sys;
+      // batches: the mask variant writes the atoms of the systems the
+      // symmetric pass counted, the list variant the others
+      const bool own = !BATCH || ((A.sym && A.sys_sym[sys] && !A.sys_fail[sys]) == MASKS);
+      if (!own) {
+        E.n[lane] = 0;
+      } else if (MASKS) {
+        const unsigned* mw = sym_word<TI, BATCH>(A, slot);
         int n = 0;
 #pragma unroll
         for (int q = 0; q < 27; ++q) n += __popc(mw[q]);
         const int hl = clampi(A.scell[slot], A.ncells_total - 1);
-        E.cell[lane] = hl;
+        int abase = 0;
+        if (BATCH) {  // the home cell's first slot holds its stencil table
+          abase = A.sys_atom[sys];
+          const int coff = A.sys_cell[sys] + sys;
+          E.cell[lane] = clampi(A.cell_offsets[coff + hl - A.sys_cell[sys]] - 1 + abase, A.nat_total - 1);
+        } else {
+          E.cell[lane] = hl;
+        }
         E.n[lane] = n > K ? 0 : n;
         if (n > K && atomicExch(A.cell_flag + hl, 1) == 0) {  // the screening write pass takes the cell
           const int u = atomicAdd(A.n_screen_cells, 1);
           if (u < A.ncells_total) A.screen_cells[u] = hl;
         }
-        const int orig = clampi(A.perm[slot] - 1, A.nat_total - 1);
+        const int orig = clampi(abase + A.perm[slot] - 1, A.nat_total - 1);
         E.base[lane] = (long long)A.first[orig] - 1;
         if ((long long)A.first[orig + 1] - 1 - E.base[lane] != n) {  // counts and masks disagree
           atomicOr(A.err, kFlagInconsistent);
@@ -1127,7 +1177,6 @@ __global__ void __launch_bounds__(kEmitWarps * 32, MASKS ? NL_EMIT_MIN_MASK_BLOC
       E.xi[lane][0] = A.Xs[3LL * slot + 0];
       E.xi[lane][1] = A.Xs[3LL * slot + 1];
       E.xi[lane][2] = A.Xs[3LL * slot + 2];
-      E.sys[lane] = BATCH ? batch_system(A.sys_atom, A.nsys, slot) : 0;
     }
     __syncwarp();
 
@@ -1215,12 +1264,12 @@ __global__ void __launch_bounds__(kEmitWarps * 32, MASKS ? NL_EMIT_MIN_MASK_BLOC
           const unsigned pd = E.pass[h];
           t.a = int(pd >> 8);
           t.r = 32 * int(pd & 255u) + lane;
-          if constexpr (MASKS) {
+          if (MASKS) {
             // the mask word and the stencil cell of lane `lane`; decoded in the gather stage
-            const unsigned* tab = sym_table(A, E.cell[t.a]);
+            const unsigned* tab = sym_table<TI, BATCH>(A, E.cell[t.a], E.cell[t.a]);
             t.st = lane < 27 ? int(tab[lane]) : 0;
             t.slp = lane < 27 ? tab[27 + lane] : 0u;
-            t.m = lane < 27 ? __ldcs(reinterpret_cast<const unsigned*>(A.lists) + 27LL * (c0 + t.a) + lane) : 0u;
+            t.m = lane < 27 ? __ldcs(sym_word<TI, BATCH>(A, c0 + t.a) + lane) : 0u;
           } else {
             t.e = __ldcs(A.lists + (c0 + t.a) * K + min(t.r, E.n[t.a] - 1));  // read once
           }
@@ -1230,7 +1279,7 @@ __global__ void __launch_bounds__(kEmitWarps * 32, MASKS ? NL_EMIT_MIN_MASK_BLOC
         u.v = t.v;
         if (u.v) {
           uint2 e = t.e;
-          if constexpr (MASKS) {
+          if (MASKS) {
             // lane r takes the atom's r-th pair.  Lane q holds mask word q
             // (c_q pairs); its pairs are r in [ex_q, ex_q + c_q).  ex_q by
             // bit-sliced ballots (c_q <= 32); the pass covers r in
@@ -1264,7 +1313,7 @@ __global__ void __launch_bounds__(kEmitWarps * 32, MASKS ? NL_EMIT_MIN_MASK_BLOC
           u.x1 = __ldg(A.Xs + 3LL * slot_j + 1);
           u.x2 = __ldg(A.Xs + 3LL * slot_j + 2);
           u.oj = (long long)__ldg(A.perm + slot_j);
-          if constexpr (MASKS)
+          if (MASKS)
             u.cw = cand_word(e.y, plain ? kPlainMeta : __float_as_uint(__ldg(&A.rec[slot_j].w)));
           else
             u.cw = e.y;
@@ -1320,7 +1369,8 @@ constexpr int kCountThreads = 128;
 
 template <typename TI, bool BATCH>
 __global__ void __launch_bounds__(kCountThreads, NL_COUNT_MIN_BLOCKS) k_count_atoms(PairArgs<TI> A) {
-  if (A.sym && *A.sym_fail == 0) return;  // the symmetric pass counted
+  // the symmetric pass counted (batches run this pass only without it)
+  if (!BATCH && A.sym && *A.sym_fail == 0) return;
   __shared__ unsigned dtab_blk[BATCH ? 1 : kStencilTab];
   if (!BATCH) {
     const int tx = 2 * A.g.nxyz[0] + 1, ty = 2 * A.g.nxyz[1] + 1;
@@ -1570,10 +1620,10 @@ static void launch_modes(int mode, const PairArgs<TI>& a, int num_sms, cudaStrea
   if (blocks < 1) blocks = 1;
   switch (mode) {
     case kModeCount:
-      if (!BATCH && a.sym) {  // symmetric pass; the per-cell pass below runs only if it gave up
+      if (a.sym) {  // symmetric pass; the per-cell pass below counts what it gave up (or left)
         long long sb = ((long long)a.ncells_total + kSymWarps - 1) / kSymWarps;
         if (sb > (long long)num_sms * pbps) sb = (long long)num_sms * pbps;
-        k_pairs_sym<TI><<<int(sb), kSymWarps * 32, 0, st>>>(a);
+        k_pairs_sym<TI, BATCH><<<int(sb), kSymWarps * 32, 0, st>>>(a);
       }
       if (a.count_kernel != 2) {  // default: one warp per home cell
         k_pairs<TI, kModeCount, BATCH><<<int(blocks), kPairWarps * 32, 0, st>>>(a);
@@ -1590,7 +1640,7 @@ static void launch_modes(int mode, const PairArgs<TI>& a, int num_sms, cudaStrea
         long long eb = ((long long)a.nat_total + 32 * kEmitWarps - 1) / (32 * kEmitWarps);
         if (eb > (long long)num_sms * ebps) eb = (long long)num_sms * ebps;
         k_emit<TI, BATCH, false><<<int(eb), kEmitWarps * 32, 0, st>>>(a);
-        if (!BATCH) k_emit<TI, false, true><<<int(eb), kEmitWarps * 32, 0, st>>>(a);
+        if (!BATCH || a.sym) k_emit<TI, BATCH, true><<<int(eb), kEmitWarps * 32, 0, st>>>(a);
       }
       k_pairs<TI, kModeFill, BATCH><<<int(blocks), kPairWarps * 32, 0, st>>>(a);
       break;

@@ -61,6 +61,8 @@ struct PairArgs {
   int sym;                  // count / write: each unordered cell pair screened once, neighbour masks
   int* sym_fail;            // set when a cell has more than 32 atoms: lists and the per-cell pass instead
   int* sym_wound;           // set when an atom has a winding or is exact (candidate words need its record)
+  const int* sys_sym;       // batch: 1 for the systems the symmetric pass takes (27 distinct stencil cells)
+  int* sys_fail;            // batch: per system, like sym_fail (zeroed per call)
   int half;                 // count / write: keep each unordered pair once (j > i, or j == i and S > 0)
   int pair_blocks_per_sm;   // launch tuning (0 = default): count / screening grids
   int emit_blocks_per_sm;   // launch tuning (0 = default): list write grid

@@ -28,8 +28,6 @@ class NeighbourListEngine:
     """``dtype=torch.float32`` runs the single-precision path (positions, cell,
     cutoff and R in Float32, the reference with T = Float32)."""
 
-    single_system = True  # the symmetric count pass (tuning count_kernel 3) applies
-
     def __init__(self, nat: int, cell, cutoff: float, pbc, int_type=torch.int32, with_R: bool = True,
                  capacity: Optional[int] = None, device="cuda", half: bool = False, dtype=torch.float64):
         if dtype not in (torch.float64, torch.float32):

@@ -3,9 +3,9 @@
 The cell grid is not a free parameter here: it fixes the reference's output
 order (stencil order over the reference's cells), so the tuner varies what
 does not change results -- the count pass (each unordered cell pair once
-into neighbour masks, where a single system's stencil allows it; one warp per
-home cell, staging the stencil in shared memory; or one thread per home
-atom), the blocks per SM of the count / screening kernels and of the list
+into neighbour masks, for the systems whose 27-cell stencil has distinct
+cells; one warp per home cell, staging the stencil in shared memory; or one
+thread per home atom), the blocks per SM of the count / screening kernels and of the list
 write kernel (how many home cells / atoms each warp walks) -- times every
 candidate on the caller's own input with CUDA events, and keeps the fastest.
 """
@@ -16,7 +16,7 @@ from typing import Dict, Iterable, Optional, Tuple
 
 import torch
 
-COUNT_KERNELS = (3, 1, 2)   # 3: symmetric (single systems), 1: warp per home cell, 2: thread per home atom
+COUNT_KERNELS = (3, 1, 2)   # 3: symmetric where it applies, 1: warp per home cell, 2: thread per home atom
 PAIR_BLOCKS = (4, 7, 14)
 EMIT_BLOCKS = (8, 16, 32)
 
@@ -41,9 +41,8 @@ def autotune(runner, X: torch.Tensor, candidates: Optional[Iterable[Tuple[int, .
     [, count_kernel]) and leaves the fastest set on the runner (a
     NeighbourListEngine or a BatchNeighbourList).  Returns the choice and
     every trial."""
-    kernels = COUNT_KERNELS if getattr(runner, "single_system", False) else tuple(k for k in COUNT_KERNELS if k != 3)
     cands = list(candidates) if candidates is not None else list(
-        itertools.product(PAIR_BLOCKS, EMIT_BLOCKS, kernels))
+        itertools.product(PAIR_BLOCKS, EMIT_BLOCKS, COUNT_KERNELS))
     runner.run(X)  # sizes the pair buffers
     trials = []
     for c in cands:

@@ -14,9 +14,11 @@ def to_np(t):
     return t.detach().cpu().numpy()
 
 
-def check_batch(nlpkg, orc, systems, int_type=torch.int32, capacity=None):
+def check_batch(nlpkg, orc, systems, int_type=torch.int32, capacity=None, count_kernel=None):
     b = nlpkg.BatchNeighbourList([(x.shape[0], c, rc, p) for (x, c, rc, p) in systems], int_type=int_type,
                                  capacity=capacity)
+    if count_kernel is not None:
+        b.set_tuning(0, 0, count_kernel)
     X = np.concatenate([x for (x, _, _, _) in systems]) if systems else np.zeros((0, 3))
     Xd = torch.from_numpy(np.ascontiguousarray(X, dtype=np.float64)).cuda()
     total = b.run(Xd)
@@ -129,7 +131,7 @@ def test_engine_graph_replay(nlpkg, orc):
     assert np.array_equal(eng.R[:t].cpu().numpy().view(np.int64), o.R.view(np.int64))
 
 
-@pytest.mark.parametrize("count_kernel", [1, 2])
+@pytest.mark.parametrize("count_kernel", [1, 2, 3])
 def test_batch_both_count_kernels(nlpkg, orc, count_kernel):
     systems = cf.batch_systems(30, seed=17, nmax=600)
     b = nlpkg.BatchNeighbourList([(x.shape[0], c, rc, p) for (x, c, rc, p) in systems])
@@ -142,3 +144,35 @@ def test_batch_both_count_kernels(nlpkg, orc, count_kernel):
         assert np.array_equal(to_np(pl.j).astype(np.int64), o.j), s
         assert np.array_equal(to_np(pl.S).astype(np.int64), o.S), s
         assert np.array_equal(to_np(pl.R).view(np.int64), o.R.view(np.int64)), s
+
+
+@pytest.mark.parametrize("count_kernel", [0, 1, 3])
+def test_batch_symmetric_count_mixed(nlpkg, orc, count_kernel):
+    """Systems that take the symmetric count pass (27 distinct stencil cells)
+    next to systems that cannot (fewer than 3 cells on a periodic axis) and
+    one that gives it up (a cell of more than 32 atoms): atoms of more than
+    192 pairs (screening write pass), of 65..192 pairs decoded from the masks,
+    open axes and windings, all equal to the oracle."""
+    rng = np.random.default_rng(60)
+    Xc, Cc, Lc = cf.corner_clump(4000, 5.0, seed=55)
+    Xm = cf.corner_clump(4000, 5.0, per_octant=20, seed=57)[0]
+    X6 = cf.corner_clump(4000, 6.0, seed=55)[0]
+    Xr, Cr, Lr = cf.rand_config(3000, seed=61)
+    crowded = np.concatenate([Xr, Lr / 2 + rng.random((40, 3)) * 0.5])
+    Xo, Co, Lo = cf.rand_config(2000, seed=62)
+    Xw, Cw, Lw = cf.rand_config(600, seed=63)
+    Xw = Xw + rng.integers(-3, 4, Xw.shape) * Lw
+    Xs, Cs, Ls = cf.rand_config(100, seed=64)
+    Xt, Ct = cf.rand_config_triclinic(300, seed=65)
+    systems = [
+        (Xc, Cc, 5.0, (True, True, True)),
+        (np.zeros((0, 3)), np.diag([10.0] * 3), 3.0, (True, True, True)),
+        (Xm, Cc, 5.0, (True, True, True)),
+        (crowded, Cr, 5.0, (True, True, True)),
+        (Xs, Cs, 0.4 * Ls, (True, True, True)),
+        (Xo, Co, 5.0, (True, True, False)),
+        (Xw, Cw, 0.2 * Lw, (True, True, True)),
+        (Xt, Ct, 3.0, (True, False, True)),
+        (X6, Cc, 6.0, (True, True, False)),
+    ]
+    check_batch(nlpkg, orc, systems, count_kernel=count_kernel)
