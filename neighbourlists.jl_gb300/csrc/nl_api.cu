@@ -766,7 +766,7 @@ int legacy_check(int64_t nat, const int64_t* ncells, const int64_t* nxyz, int in
 // --------------------------------------------------------------- batches --
 struct BatchLayout {
   Layout L;  // the single-system layout for all atoms and cells of the batch
-  size_t geo, atom0, cell0, cs, first_all, sys_sym, sys_fail, end;
+  size_t geo, atom0, cell0, cs, first_all, sys_sym, sys_fail, cell_sys, end;
 };
 
 BatchLayout batch_layout(int64_t nat, int64_t ncells, int nsys) {
@@ -788,6 +788,8 @@ BatchLayout batch_layout(int64_t nat, int64_t ncells, int nsys) {
   o += up(sizeof(int) * size_t(nsys));
   B.sys_fail = o;
   o += up(sizeof(int) * size_t(nsys));
+  B.cell_sys = o;
+  o += up(sizeof(int) * size_t(ncells > 0 ? ncells : 1));
   B.end = o;
   return B;
 }
@@ -852,6 +854,7 @@ int batch_impl(const nl_batch& b, const double* X, TI* perm, double* Xs, TI* cel
   a.geo = si.geo;
   a.sys_atom = si.atom0;
   a.sys_cell = si.cell0;
+  a.cell_sys = at<int>(ws, b.B.cell_sys);
   a.cs_sys = at<double>(ws, b.B.cs);
   a.nsys = b.nsys;
   a.nat_total = na;
@@ -1249,6 +1252,7 @@ int nl_batch_upload(const nl_batch* batch, void* d_workspace, size_t workspace_b
                         cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) return cuda_fail(e, "upload batch tables");
   nl::launch_cs_tables(at<nl::Geometry>(d_workspace, B.geo), batch->nsys, at<double>(d_workspace, B.cs), st);
+  nl::launch_cell_systems(at<int>(d_workspace, B.cell0), batch->nsys, at<int>(d_workspace, B.cell_sys), st);
   e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   return e == cudaSuccess ? NL_OK : cuda_fail(e, "upload batch tables");

@@ -438,7 +438,7 @@ __global__ void __launch_bounds__(kPairWarps * 32, BATCH ? NL_PAIR_BATCH_MIN_BLO
     SysView<BATCH> sv;
     sv.hl = h;
     if constexpr (BATCH) {
-      sv.s = batch_system(A.sys_cell, A.nsys, h);
+      sv.s = clampi(A.cell_sys[h], A.nsys - 1);
       // systems the symmetric pass counted
       if (MODE == kModeCount && A.sym && A.sys_sym[sv.s] && !A.sys_fail[sv.s]) continue;
       if (sv.s != cur_sys) {
@@ -819,7 +819,7 @@ __global__ void __launch_bounds__(kSymWarps * 32, BATCH ? NL_SYM_BATCH_MIN_BLOCK
     // system view: first slot / original atom, index of cell 0 in cell_offsets, home cell in the system
     int sys = 0, abase = 0, coff = 0, hl = h;
     if constexpr (BATCH) {
-      sys = batch_system(A.sys_cell, A.nsys, h);
+      sys = clampi(A.cell_sys[h], A.nsys - 1);
       if (!A.sys_sym[sys]) continue;
       if (sys != cur_sys) {
         __syncwarp();
@@ -1143,7 +1143,7 @@ __global__ void __launch_bounds__(kEmitWarps * 32,
     __syncwarp();
     if (lane < na) {
       const int slot = int(c0) + lane;
-      const int sys = BATCH ? batch_system(A.sys_atom, A.nsys, slot) : 0;
+      const int sys = BATCH ? clampi(A.cell_sys[clampi(A.scell[slot], A.ncells_total - 1)], A.nsys - 1) : 0;
       E.sys[lane] = sys;
       // batches: the mask variant writes the atoms of the systems the
       // symmetric pass counted, the list variant the others
@@ -1393,7 +1393,7 @@ __global__ void __launch_bounds__(kCountThreads, NL_COUNT_MIN_BLOCKS) k_count_at
   for (long long sl = (long long)blockIdx.x * blockDim.x + threadIdx.x; sl < A.nat_total;
        sl += (long long)gridDim.x * blockDim.x) {
     const int slot = int(sl);
-    const int sys = BATCH ? batch_system(A.sys_atom, A.nsys, slot) : 0;
+    const int sys = BATCH ? clampi(A.cell_sys[clampi(A.scell[slot], A.ncells_total - 1)], A.nsys - 1) : 0;
     const Geometry& g = BATCH ? A.geo[sys] : A.g;
     const int abase = BATCH ? A.sys_atom[sys] : 0;
     const int coff = BATCH ? A.sys_cell[sys] + sys : 0;
@@ -1675,6 +1675,16 @@ void launch_pairs(int mode, const PairArgs<TI>& a, int num_sms, cudaStream_t st)
 
 void launch_cs_tables(const Geometry* geo, int nsys, double* out, cudaStream_t st) {
   if (nsys > 0) k_cs_tables<<<nsys, 128, 0, st>>>(geo, out);
+}
+
+// Batches: the system of every cell (one block per system).
+__global__ void k_cell_systems(const int* __restrict__ sys_cell, int* __restrict__ out) {
+  const int s = blockIdx.x;
+  for (int c = sys_cell[s] + threadIdx.x; c < sys_cell[s + 1]; c += blockDim.x) out[c] = s;
+}
+
+void launch_cell_systems(const int* sys_cell, int nsys, int* out, cudaStream_t st) {
+  if (nsys > 0) k_cell_systems<<<nsys, 128, 0, st>>>(sys_cell, out);
 }
 
 template void launch_pairs<int32_t>(int, const PairArgs<int32_t>&, int, cudaStream_t);

@@ -31,6 +31,7 @@ struct PairArgs {
   const Geometry* geo;      // batch: geometry of each system
   const int* sys_atom;      // batch: nsys+1 slot offsets
   const int* sys_cell;      // batch: nsys+1 cell offsets
+  const int* cell_sys;      // batch: system of each cell
   const double* cs_sys;     // batch: C'S table of each system
   int nsys;                 // 0 for a single system
   int nat_total;            // slots of the whole launch
@@ -93,7 +94,8 @@ void launch_pair_vectors(const Geometry& g, const double* X, const TI* pi, const
 void launch_max_disp_sq(const double* X, const double* Xref, long long nat, unsigned long long* out, int num_sms,
                         cudaStream_t st);
 
-// batches: the C'S table of every system
+// batches: the C'S table of every system, the system of every cell
 void launch_cs_tables(const Geometry* geo, int nsys, double* out, cudaStream_t st);
+void launch_cell_systems(const int* sys_cell, int nsys, int* out, cudaStream_t st);
 
 }  // namespace nl
