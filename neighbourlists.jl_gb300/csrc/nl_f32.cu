@@ -580,15 +580,34 @@ __global__ void __launch_bounds__(128) k_emit32_masks(Pairs32Args<TI> a) {
   const Geo32& g = a.g;
   const int lane = threadIdx.x & 31;
   const unsigned lt = lanemask_lt();
-  for (int s = blockIdx.x * 4 + (threadIdx.x >> 5); s < g.nat; s += gridDim.x * 4) {
-    const float4 ri = a.rec[s];
+  const int stride = gridDim.x * 4;
+  // the next atom's own loads (record, index, mask word, cell) are issued
+  // before this atom's pairs, so their latency overlaps its work
+  int s = blockIdx.x * 4 + (threadIdx.x >> 5);
+  float4 nx_ri = make_float4(0.f, 0.f, 0.f, 0.f);
+  TI nx_iid = 1;
+  unsigned nx_m = 0u;
+  int nx_cell = 0;
+  auto fetch = [&](int t) {
+    if (t < g.nat) {
+      nx_ri = a.rec[t];
+      nx_iid = a.perm[t];
+      nx_m = lane < 27 ? a.masks[27LL * t + lane] : 0u;
+      nx_cell = a.scell[t];
+    }
+  };
+  fetch(s);
+  for (; s < g.nat; s += stride) {
+    const float4 ri = nx_ri;
+    const TI iid = nx_iid;
+    const unsigned m = nx_m;
+    const int cell = nx_cell;
+    fetch(s + stride);
     const unsigned mi = __float_as_uint(ri.w);
     const int wi0 = field10(mi, 0) - kW32Bias, wi1 = field10(mi, 1) - kW32Bias, wi2 = field10(mi, 2) - kW32Bias;
-    const TI iid = a.perm[s];
     const long long base = (long long)a.first[iid - 1] - 1;
     const long long nexp = (long long)a.first[iid] - 1 - base;
-    const unsigned m = lane < 27 ? a.masks[27LL * s + lane] : 0u;
-    const unsigned* tab = sym32_table(a.masks, g.nat, a.scell[s]);
+    const unsigned* tab = sym32_table(a.masks, g.nat, cell);
     const int st = lane < 27 ? int(tab[lane]) : 0;
     const unsigned slp = lane < 27 ? tab[27 + lane] : 0u;
     const int c = __popc(m);
