@@ -367,6 +367,9 @@ template <typename TI, int MODE, bool BATCH>
 __global__ void __launch_bounds__(kPairWarps * 32, BATCH ? NL_PAIR_BATCH_MIN_BLOCKS : kMinBlocks)
     k_pairs(PairArgs<TI> A) {
   if (MODE == kModeCount && !BATCH && A.sym && *A.sym_fail == 0) return;  // the symmetric pass counted
+  // the screening passes visit only listed cells: none listed, nothing to do
+  // (the same value for every thread, so no block stops at a barrier alone)
+  if ((MODE == kModeFill || (MODE == kModeLazyR6 && A.list_cap > 0)) && *A.n_screen_cells <= 0) return;
   __shared__ WarpSmem sm[kPairWarps];
   __shared__ double cs_blk[BATCH ? 1 : 3 * kCsN * kCsN * kCsN];
   __shared__ unsigned dtab_blk[BATCH ? 32 * kPairWarps : kStencilTab];  // packed (d0, d1, d2) of stencil cell q
