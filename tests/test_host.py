@@ -309,7 +309,8 @@ def test_batch_plan_on_host(nlpkg):
     na, nc = C.c_int64(), C.c_int64()
     assert L.nl_batch_sizes(h, C.byref(na), C.byref(nc)) == 0
     assert na.value == 10 and nc.value == 2 * 3 * 4 * 4
-    assert L.nl_batch_workspace_bytes(h) >= L.nl_workspace_bytes(10, nc.value)
+    # the single-system layout for all atoms and cells, plus the system of every cell
+    assert L.nl_batch_workspace_bytes(h) >= L.nl_workspace_bytes(10, nc.value) + 4 * nc.value
     L.nl_batch_destroy(h)
     arr[1].nxyz[0] = 63
     assert L.nl_batch_create(arr, 2, 4, C.byref(h)) == nlpkg._lib.NL_ERR_ARG
@@ -328,3 +329,41 @@ def test_lists_move_between_devices(nlpkg):
     Q = P.to("cpu")
     assert Q.i.tolist() == [1, 1, 2] and Q.first.tolist() == [1, 3, 4, 4] and Q.cutoff == 2.0
     assert nlpkg.nneigs(Q, 1) == 2 and nlpkg.npairs(Q) == 3
+
+
+def test_autotune_candidates_and_choice(nlpkg, monkeypatch):
+    """The tuner times every (pair blocks, emit blocks, count kernel) set --
+    the symmetric count pass among them for any runner, single system or
+    batch -- and leaves the fastest on the runner (the CUDA-event timer is
+    replaced by a fixed cost per set here)."""
+    import sys
+
+    tuning = sys.modules[nlpkg.__name__ + ".tuning"]
+
+    class Runner:
+        def __init__(self):
+            self.t = None
+
+        def run(self, X):
+            return 0
+
+        def set_tuning(self, p, e, k):
+            self.t = (p, e, k)
+
+        def launch(self, X):
+            pass
+
+        def sync_status(self):
+            pass
+
+    r = Runner()
+    cost = lambda t: abs(t[0] - 7) + abs(t[1] - 16) / 8 + (0 if t[2] == 3 else 1)  # noqa: E731
+    monkeypatch.setattr(tuning, "_time_ms", lambda fn, reps: (fn(), cost(r.t))[1])
+    res = tuning.autotune(r, None, reps=1)
+    assert len(res["trials"]) == len(tuning.PAIR_BLOCKS) * len(tuning.EMIT_BLOCKS) * len(tuning.COUNT_KERNELS)
+    assert {t["count_kernel"] for t in res["trials"]} == {1, 2, 3}
+    assert r.t == (7, 16, 3)
+    assert (res["pair_blocks_per_sm"], res["emit_blocks_per_sm"], res["count_kernel"]) == (7, 16, 3)
+    res = tuning.autotune(r, None, candidates=[(4, 8), (14, 32, 2)], reps=1)
+    assert [(t["pair_blocks_per_sm"], t["emit_blocks_per_sm"], t["count_kernel"]) for t in res["trials"]] == \
+        [(4, 8, 0), (14, 32, 2)]
