@@ -107,6 +107,10 @@ class NeighbourListEngine:
         return self.last_total
 
     def set_tuning(self, pair_blocks_per_sm: int = 0, emit_blocks_per_sm: int = 0, count_kernel: int = 0) -> None:
+        """Launch shapes of this engine's calls (nl_set_tuning; 0 = default).
+        count_kernel: 0 the symmetric pass where the stencil allows it, else 1;
+        1 one warp per home cell; 2 one thread per home atom; 3 symmetric where
+        it applies.  Results never depend on them."""
         self.tuning = _lib.Tuning(int(pair_blocks_per_sm), int(emit_blocks_per_sm), int(count_kernel))
 
     def capture(self, X: torch.Tensor) -> torch.cuda.CUDAGraph:
