@@ -608,7 +608,7 @@ def run_path(args):
     if args.path == "batched":
         import configs as cf
 
-        systems = cf.batch_systems(4096, seed=0)
+        systems = cf.batch_systems(args.systems, seed=0)
         Xb = torch.from_numpy(np.ascontiguousarray(np.concatenate([x for (x, _, _, _) in systems]))).to(dev)
         b = nl.BatchNeighbourList([(x.shape[0], c, rc, p) for (x, c, rc, p) in systems], device=dev)
         total = b.run(Xb)
@@ -652,6 +652,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the lazy / batched / 4M sections")
     ap.add_argument("--atoms", type=int, default=N_ATOMS, help="system size (profiling runs use a smaller one)")
+    ap.add_argument("--systems", type=int, default=4096, help="batched profiling runs: systems in the batch")
     ap.add_argument("--path", default="headline", choices=["headline", "float32", "legacy", "batched"],
                     help="float32 / legacy / batched: profiling runs of those paths (not the benchmark line)")
     args = ap.parse_args()
