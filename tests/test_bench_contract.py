@@ -1,0 +1,41 @@
+"""The benchmark's reference arm (bench.py --impl reference) on the host: one
+JSON line with the GPU arm's metric, workload and keys, the reference's CPU
+path (the C restatement) timed on all host threads; ranks other than 0 of a
+multi-rank launch print nothing and exit 0."""
+import json
+import os
+import subprocess
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def run_bench(*args, env=None):
+    e = dict(os.environ)
+    e.update(env or {})
+    return subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), *args], capture_output=True, text=True,
+                          cwd=ROOT, env=e, timeout=600)
+
+
+def test_reference_arm_line():
+    sys.path.insert(0, ROOT)
+    import bench
+
+    r = run_bench("--impl", "reference", "--steps", "1", "--warmup", "0")
+    assert r.returncode == 0, r.stderr
+    d = json.loads(r.stdout.strip().splitlines()[-1])
+    assert d["impl"] == "reference" and d["metric"] == bench.METRIC and d["unit"] == "pairs/s"
+    assert d["higher_is_better"] is True and d["steps"] == 1 and d["warmup"] == 0 and d["n_gpus"] == 1
+    assert d["config"]["workload"] == bench.WORKLOAD and d["config"]["atoms"] == bench.N_ATOMS
+    assert d["config"]["pairs"] == 26173098  # the 1M-atom workload's pair count, as on the GPU
+    assert d["value"] > 0 and abs(d["ms_per_step"] * 1e-3 * d["value"] - d["config"]["pairs"]) < 1e-6 * d["value"] + 1
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    assert d["cpu_baseline"]["value"] == d["value"]
+    assert d["e2e"] == {"value": d["value"], "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+def test_reference_arm_other_ranks_print_nothing():
+    r = run_bench("--impl", "reference", "--steps", "1", "--warmup", "0", "--gpus", "2",
+                  env={"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"})
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.strip() == ""
