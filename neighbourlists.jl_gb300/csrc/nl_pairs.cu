@@ -1080,9 +1080,14 @@ __global__ void __launch_bounds__(kSymWarps * 32, BATCH ? NL_SYM_BATCH_MIN_BLOCK
 constexpr int kEmitWarps = 4;
 constexpr int kEmitMinBlocks = NL_EMIT_MIN_BLOCKS;  // resident blocks per SM the register budget targets
 
+// passes of a chunk of 32 atoms of at most kListCap listed pairs each; a
+// pass number within an atom is kept in 8 bits
+constexpr int kChunkPasses = 32 * ((kListCap + 31) / 32);
+static_assert((kListCap + 31) / 32 <= 255, "pass numbers within an atom are 8-bit");
+
 struct __align__(16) EmitAtoms {
   long long sbuf[96];   // a pass's S, three words per pair, staged for contiguous stores
-  unsigned short pass[kListCap];  // the chunk's passes (32 atoms, kListCap / 32 each): atom << 8 | pass
+  unsigned short pass[kChunkPasses];  // the chunk's passes (32 atoms, up to kListCap / 32 each): atom << 8 | pass
   double rbuf[96];      // a pass's R, likewise
   double xi[32][3];     // FP64 position
   long long base[32];   // first output slot (0-based)
