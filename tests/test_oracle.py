@@ -260,3 +260,22 @@ def test_f32_equals_f64_sets(orc, pbc):
     assert key(a, np.abs(ra - 0.3 * L) >= 1e-4 * L) == key(b, ~near)
     # the sorted cell lists agree too (binning away from cell faces)
     assert np.array_equal(a.cell_offsets, orc.build_cell_list(X, 0.3 * L, C, pbc).cell_offsets)
+
+
+@pytest.mark.parametrize("rc,per_octant,pbc,lo,hi", [
+    (5.0, 28, (True, True, True), 193, 10**9),    # lists overflow the 192-entry capacity
+    (6.0, 28, (True, True, False), 193, 10**9),
+    (5.0, 20, (True, True, True), 65, 192),       # more than 64 pairs, decoded from the masks
+])
+def test_corner_clump_generator(orc, rc, per_octant, pbc, lo, hi):
+    """The GPU overflow cases rest on these properties of the corner-clump
+    generator: its clump atoms have lo..hi pairs and no cell holds more than
+    32 atoms (so the symmetric count pass still applies)."""
+    X, C, L = cf.corner_clump(4000, rc, per_octant=per_octant, seed=55 if per_octant == 28 else 57)
+    o = orc.neighbour_list(X, rc, C, pbc, nthreads=8)
+    cl = orc.build_cell_list(X, rc, C, pbc)
+    npair = np.diff(o.first)
+    assert np.diff(cl.cell_offsets).max() <= 32
+    clump = npair[-8 * per_octant:]
+    assert clump.min() >= lo and clump.max() <= hi
+    assert npair[:-8 * per_octant].max() < lo  # the background stays below
