@@ -48,6 +48,15 @@ ALGO_BYTES_PER_PAIR = 44  # i 4 + j 4 + S 12 + R 24 written
 LAUNCHES_PER_STEP = 12  # kernels of one step: build 5, count 3 (with its scan), write 4
 
 
+def bench_config(n_atoms, pairs):
+    """The workload description both arms print (identical dicts)."""
+    return {"workload": WORKLOAD if n_atoms == N_ATOMS else f"uniform {n_atoms} atoms (profiling size)",
+            "atoms": int(n_atoms), "pairs": int(pairs), "cutoff": CUTOFF, "density": DENSITY, "pbc": "TTT",
+            "index_type": "Int32", "with_R": True,
+            "l2": "GPU arm: 256 MiB write (untimed) before every timed step; CPU arm: positions and pair "
+                  "arrays far larger than the host caches"}
+
+
 def workload(n_atoms=N_ATOMS):
     import configs as cf
 
@@ -174,7 +183,7 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": val, "unit": "pairs/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "atoms": N_ATOMS, "pairs": int(pairs)},
+        "config": bench_config(N_ATOMS, pairs),
         "cpu_baseline": {"value": val, "unit": "pairs/s", "cores": threads, "kind": "port",
                          "sample": f"{args.steps} timed full runs of the workload after {args.warmup} warm-up runs"},
         "e2e": {"value": val, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -309,11 +318,8 @@ def run_gpu(args):
         "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD if n_atoms == N_ATOMS else f"uniform {n_atoms} atoms (profiling size)",
-                   "atoms": n_atoms, "pairs": int(total), "cutoff": CUTOFF,
-                   "density": DENSITY, "pbc": "TTT", "index_type": "Int32", "with_R": True,
-                   "l2": "flushed before every timed step (256 MiB write, untimed)",
-                   "cuda_graph": True, "ms_per_step_without_graph": launch_ms,
+        "config": bench_config(n_atoms, total),
+        "timing": {"cuda_graph": True, "ms_per_step_without_graph": launch_ms,
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "kernel": "write pass (k_emit<masks> + k_cs_table + k_pairs<fill>)",

@@ -173,6 +173,14 @@ int nl_neighbour_list_static(const double* d_X, int64_t nat, const double cell[9
                              void* d_first, int64_t capacity, void* d_i, void* d_j, void* d_S, double* d_R,
                              int64_t* total_pairs, void* stream);
 
+/* Status of the last nl_neighbour_list_static call on the current device,
+ * for callers that made it asynchronously (total_pairs = NULL): synchronises
+ * `stream`, then returns the result of that call's device-side checks
+ * (NL_ERR_CAPACITY, NL_ERR_BAD_POSITION, NL_ERR_INDEX_OVERFLOW, ...) and, if
+ * total_pairs is not NULL, its pair count.  Like the call it reports on, it
+ * allocates nothing.  No counterpart in the reference. */
+int nl_static_sync_status(int64_t* total_pairs, void* stream);
+
 /* ---- batches of independent systems -------------------------------------
  * No counterpart in the reference, which handles one system per call: a
  * batch replaces a loop of neighbour_list(X_s, cutoff_s, cell_s, pbc_s)

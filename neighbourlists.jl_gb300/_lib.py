@@ -37,6 +37,7 @@ EXPORTED = [
     "nl_fill_pairs",
     "nl_neighbour_list",
     "nl_neighbour_list_static",
+    "nl_static_sync_status",
     "nl_neighbour_list_half",
     "nl_lazy_reduce",
     "nl_pair_vectors",
@@ -146,6 +147,8 @@ def _declare(L):
     L.nl_neighbour_list_static.argtypes = [_vp, C.c_int64, _D, _D, _I64, _I64, _U8, C.c_double, C.c_int, _vp, _vp,
                                            _vp, _vp, _vp, C.c_int64, _vp, _vp, _vp, _vp, _I64, _vp]
     L.nl_neighbour_list_static.restype = C.c_int
+    L.nl_static_sync_status.argtypes = [_I64, _vp]
+    L.nl_static_sync_status.restype = C.c_int
     L.nl_lazy_reduce.argtypes = [_vp, _vp, _vp, _vp, C.c_int64, _D, _D, _I64, _I64, _U8, C.c_double, C.c_int, C.c_int,
                                  C.c_int, _vp, _vp, C.c_size_t, _vp]
     L.nl_lazy_reduce.restype = C.c_int

@@ -9,6 +9,7 @@
 // operation): the build passes -ffp-contract=off to the host compiler.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -253,15 +254,18 @@ T* at(void* ws, size_t off) {
 }
 
 int num_sms() {
-  static int cache[64] = {0};
+  // per device, filled on first use; concurrent first calls store the same value
+  static std::atomic<int> cache[64];
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 148;
-  if (!cache[dev]) {
+  int v = cache[dev].load(std::memory_order_relaxed);
+  if (!v) {
     int n = 0;
     cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    cache[dev] = n > 0 ? n : 148;
+    v = n > 0 ? n : 148;
+    cache[dev].store(v, std::memory_order_relaxed);
   }
-  return cache[dev];
+  return v;
 }
 
 struct Pinned {
@@ -909,6 +913,9 @@ int status_from_device_flags(unsigned flags) { return status_from_flags(flags); 
 size_t workspace_min_bytes(int64_t nat, int64_t ncells_total) {
   if (nat < 0 || ncells_total < 1) return 0;
   return layout(nat, ncells_total).base_end;
+}
+size_t workspace_total_offset(int64_t nat, int64_t ncells_total) {
+  return layout(nat, ncells_total).totals + sizeof(long long);
 }
 }  // namespace nl
 

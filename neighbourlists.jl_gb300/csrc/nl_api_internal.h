@@ -13,4 +13,8 @@ int status_from_device_flags(unsigned flags);
 // then written by the screening write pass); nl_workspace_bytes is the size
 // with the lists.
 size_t workspace_min_bytes(int64_t nat, int64_t ncells_total);
+// Byte offset in a workspace of the int64 pair total the count pass writes
+// (the last entry of its scan), for a system of nat atoms and ncells_total
+// cells; the error word sits at offset 0.
+size_t workspace_total_offset(int64_t nat, int64_t ncells_total);
 }  // namespace nl

@@ -38,9 +38,14 @@ class VerletList:
         self.reuses = 0
 
     def max_displacement(self, X: torch.Tensor, stream=None) -> float:
+        """Largest displacement since the build, measured on ``stream`` (default:
+        the current stream) and read back on that same stream."""
+        st = stream if stream is not None else torch.cuda.current_stream(self.engine.device)
         check(lib().nl_max_displacement_sq(_ptr(X), _ptr(self.X_ref), int(X.shape[0]), _ptr(self._d2),
-                                           _stream_handle(stream)))
-        return float(self._d2.item()) ** 0.5
+                                           _stream_handle(st)))
+        with torch.cuda.stream(st):
+            d2 = float(self._d2.item())
+        return d2 ** 0.5
 
     def update(self, X: torch.Tensor, stream=None) -> bool:
         """Brings the list to positions X; returns True if it was rebuilt."""

@@ -28,6 +28,7 @@ def test_reference_arm_line():
     assert d["higher_is_better"] is True and d["steps"] == 1 and d["warmup"] == 0 and d["n_gpus"] == 1
     assert d["config"]["workload"] == bench.WORKLOAD and d["config"]["atoms"] == bench.N_ATOMS
     assert d["config"]["pairs"] == 26173098  # the 1M-atom workload's pair count, as on the GPU
+    assert d["config"] == bench.bench_config(bench.N_ATOMS, 26173098)  # the GPU arm prints the same dict
     assert d["value"] > 0 and abs(d["ms_per_step"] * 1e-3 * d["value"] - d["config"]["pairs"]) < 1e-6 * d["value"] + 1
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
     assert d["cpu_baseline"]["value"] == d["value"]

@@ -514,6 +514,24 @@ def test_verlet_reuse(nlpkg, orc):
         X = X + rng.uniform(-0.12, 0.12, size=X.shape) * (1.0 if step < 2 else 4.0)
 
 
+def test_verlet_displacement_on_a_side_stream(nlpkg):
+    """The displacement test launched on a non-current stream is read back on
+    that stream: it sees the new positions, not a stale value."""
+    X0, C, L = cf.rand_config(20000, seed=94)
+    v = nlpkg.VerletList(X0.shape[0], C, 4.0, 1.0, (True, True, True))
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):
+        Xd0 = torch.from_numpy(X0).cuda()
+    side.synchronize()
+    v.update(Xd0, stream=side)
+    X1 = X0.copy()
+    X1[123] += 0.3  # one atom moves by 0.3 * sqrt(3)
+    with torch.cuda.stream(side):
+        Xd1 = torch.from_numpy(X1).cuda()
+    d = v.max_displacement(Xd1, stream=side)  # launched on side, the current stream is the default one
+    assert abs(d - 0.3 * np.sqrt(3.0)) < 1e-12
+
+
 def test_half_int64_and_verlet_half(nlpkg, orc):
     """Half lists in Int64, and Verlet reuse of a half list."""
     X, C, L = cf.rand_config(5000, seed=101)

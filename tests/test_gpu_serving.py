@@ -37,10 +37,13 @@ def test_same_alone_and_in_mix(nlpkg, orc):
     for r in mix:
         alone, _, _ = serve(nlpkg, [(r.X, r.cell, r.cutoff, r.pbc)], slots=1)
         assert same(alone[0].result, r.result), r.rid
-    for r in mix[::7]:
+    for r in mix:  # every request, every field, against the oracle
         o = orc.neighbour_list(r.X, r.cutoff, r.cell, r.pbc, nthreads=8)
-        assert np.array_equal(r.result["i"].cpu().numpy().astype(np.int64), o.i)
-        assert np.array_equal(r.result["R"].cpu().numpy().view(np.int64), o.R.view(np.int64))
+        res = r.result
+        assert np.array_equal(res["first"].cpu().numpy().astype(np.int64), o.first), r.rid
+        for k in ("i", "j", "S"):
+            assert np.array_equal(res[k].cpu().numpy().astype(np.int64), getattr(o, k)), (r.rid, k)
+        assert np.array_equal(res["R"].cpu().numpy().view(np.int64), o.R.view(np.int64)), r.rid
 
 
 def test_plain_mode_matches_batched(nlpkg):

@@ -4,8 +4,12 @@ library instead of a caller-provided workspace).
 
 Checked through the C ABI against the workspace entry point nl_neighbour_list
 on the same inputs, bit for bit, on two calls in a row with different systems
-(the second call reuses the shared scratch the first one left behind).  This
-file is collected last so that a failure here cannot hide other failures."""
+(the second call reuses the shared scratch the first one left behind), for
+Int32 and Int64 indices; plus the empty system, pair buffers that are too
+small (status and pair count), the asynchronous form read back with
+nl_static_sync_status, and that a warmed-up call leaves the device's free
+memory unchanged.  This file is collected last so that a failure here cannot
+hide other failures."""
 import ctypes as C
 
 import numpy as np
@@ -19,46 +23,55 @@ pytestmark = pytest.mark.gpu
 _D = C.POINTER(C.c_double)
 _I64 = C.POINTER(C.c_int64)
 _U8 = C.POINTER(C.c_uint8)
+NL_ERR_CAPACITY = 7
 
 
 def _p(t):
     return C.c_void_p(t.data_ptr()) if t is not None and t.numel() else C.c_void_p(0)
 
 
-def _run(nlpkg, X, cell, rc, pbc, static):
-    L = nlpkg.lib()
-    plan = nlpkg.analyze_cell(cell, rc)
-    nat = X.shape[0]
+def _buffers(nat, ncells_total, cap, ti):
     dev = torch.device("cuda")
-    ti = torch.int32
-    Xd = torch.from_numpy(np.ascontiguousarray(X)).to(dev)
-    out = {
+    return {
         "perm": torch.empty(nat, dtype=ti, device=dev),
         "X_sorted": torch.empty((nat, 3), dtype=torch.float64, device=dev),
         "cell_id": torch.empty(nat, dtype=ti, device=dev),
-        "cell_offsets": torch.empty(plan.ncells_total + 1, dtype=ti, device=dev),
+        "cell_offsets": torch.empty(ncells_total + 1, dtype=ti, device=dev),
         "first": torch.empty(nat + 1, dtype=ti, device=dev),
+        "i": torch.empty(cap, dtype=ti, device=dev), "j": torch.empty(cap, dtype=ti, device=dev),
+        "S": torch.empty((cap, 3), dtype=ti, device=dev), "R": torch.empty((cap, 3), dtype=torch.float64, device=dev),
     }
-    cap = 200 * nat + 1024
-    out.update(i=torch.empty(cap, dtype=ti, device=dev), j=torch.empty(cap, dtype=ti, device=dev),
-               S=torch.empty((cap, 3), dtype=ti, device=dev), R=torch.empty((cap, 3), dtype=torch.float64, device=dev))
+
+
+def _call(nlpkg, X, cell, rc, pbc, static, ti=torch.int32, cap=None, total=True, out=None, Xd=None):
+    """One call through the C ABI; returns (status, pair count, buffers)."""
+    L = nlpkg.lib()
+    plan = nlpkg.analyze_cell(cell, rc, ti)
+    nat = X.shape[0]
+    if Xd is None:
+        Xd = torch.from_numpy(np.ascontiguousarray(X)).cuda()
+    cap = 200 * nat + 1024 if cap is None else cap
+    out = _buffers(nat, plan.ncells_total, cap, ti) if out is None else out
     pb = np.array([1 if p else 0 for p in pbc], dtype=np.uint8)
-    total = C.c_int64(-1)
+    tot = C.c_int64(-1)
     stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    ib = 4 if ti == torch.int32 else 8
     args = [_p(Xd), nat, plan.cell_cm.ctypes.data_as(_D), plan.inv_cm.ctypes.data_as(_D),
-            plan.ncells.ctypes.data_as(_I64), plan.nxyz.ctypes.data_as(_I64), pb.ctypes.data_as(_U8), float(rc), 4,
+            plan.ncells.ctypes.data_as(_I64), plan.nxyz.ctypes.data_as(_I64), pb.ctypes.data_as(_U8), float(rc), ib,
             _p(out["perm"]), _p(out["X_sorted"]), _p(out["cell_id"]), _p(out["cell_offsets"]), _p(out["first"]),
-            cap, _p(out["i"]), _p(out["j"]), _p(out["S"]), _p(out["R"]), C.byref(total)]
+            cap, _p(out["i"]), _p(out["j"]), _p(out["S"]), _p(out["R"]), C.byref(tot) if total else None]
     if static:
         st = L.nl_neighbour_list_static(*args, stream)
     else:
-        ws = torch.empty(int(L.nl_workspace_bytes(nat, plan.ncells_total)), dtype=torch.uint8, device=dev)
+        ws = torch.empty(int(L.nl_workspace_bytes(nat, plan.ncells_total)), dtype=torch.uint8, device="cuda")
         st = L.nl_neighbour_list(*args, _p(ws), ws.numel(), stream)
-    assert st == 0, L.nl_last_error().decode()
-    P = int(total.value)
-    for k in ("i", "j", "S", "R"):
-        out[k] = out[k][:P]
-    return {k: v.cpu().numpy() for k, v in out.items()}
+    return st, int(tot.value), out
+
+
+def _host(out, P):
+    h = {k: v.cpu().numpy() for k, v in out.items() if k not in ("i", "j", "S", "R")}
+    h.update({k: out[k][:P].cpu().numpy() for k in ("i", "j", "S", "R")})
+    return h
 
 
 def _same(a, b):
@@ -69,26 +82,94 @@ def _same(a, b):
         assert np.array_equal(x, y), k
 
 
-def test_static_scratch_matches_workspace_path_twice(nlpkg):
+def _cases():
     X1, C1, _ = cf.rand_config(20000, seed=41)
     X2, C2, pbc2 = cf.fcc_sheared(n=8, seed=42)
-    cases = [(X1, C1, 5.0, (True, True, True)), (X2, C2, 5.0, pbc2)]
-    refs = [_run(nlpkg, *c, static=False) for c in cases]
-    for (case, ref) in zip(cases, refs):  # two calls in a row on the shared scratch
-        got = _run(nlpkg, *case, static=True)
-        assert got["i"].shape[0] > 0
-        _same(got, ref)
+    return [(X1, C1, 5.0, (True, True, True)), (X2, C2, 5.0, pbc2)]
 
 
-def test_static_scratch_rejects_oversize_systems(nlpkg):
+@pytest.mark.parametrize("ti", [torch.int32, torch.int64])
+def test_static_scratch_matches_workspace_path_twice(nlpkg, ti):
+    cases = _cases()
+    refs = []
+    for c in cases:
+        st, P, out = _call(nlpkg, *c, static=False, ti=ti)
+        assert st == 0, nlpkg.lib().nl_last_error().decode()
+        refs.append(_host(out, P))
+    for case, ref in zip(cases, refs):  # two calls in a row on the shared scratch
+        st, P, out = _call(nlpkg, *case, static=True, ti=ti)
+        assert st == 0, nlpkg.lib().nl_last_error().decode()
+        assert P == ref["i"].shape[0] > 0
+        _same(_host(out, P), ref)
+
+
+def test_static_async_form_and_sync_status(nlpkg):
+    L = nlpkg.lib()
+    case = _cases()[0]
+    st, P_ref, out_ref = _call(nlpkg, *case, static=False)
+    assert st == 0
+    ref = _host(out_ref, P_ref)
+    st, _, out = _call(nlpkg, *case, static=True, total=False)  # no host synchronisation
+    assert st == 0, L.nl_last_error().decode()
+    tot = C.c_int64(-1)
+    assert L.nl_static_sync_status(C.byref(tot), C.c_void_p(torch.cuda.current_stream().cuda_stream)) == 0
+    assert tot.value == P_ref
+    _same(_host(out, P_ref), ref)
+
+
+def test_static_capacity_too_small_reports_status_and_count(nlpkg):
+    L = nlpkg.lib()
+    case = _cases()[1]
+    st, P_ref, _ = _call(nlpkg, *case, static=False)
+    assert st == 0
+    small = P_ref // 2
+    st, P, _ = _call(nlpkg, *case, static=True, cap=small)
+    assert st == NL_ERR_CAPACITY and P == P_ref
+    st, _, _ = _call(nlpkg, *case, static=True, cap=small, total=False)
+    assert st == 0  # asynchronous: the device-side check is read back later
+    tot = C.c_int64(-1)
+    s2 = L.nl_static_sync_status(C.byref(tot), C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert s2 == NL_ERR_CAPACITY and tot.value == P_ref
+
+
+def test_static_empty_system(nlpkg):
+    X = np.zeros((0, 3))
+    st, P, out = _call(nlpkg, X, np.diag([10.0, 10.0, 10.0]), 3.0, (True, True, True), static=True, cap=16)
+    assert st == 0 and P == 0
+    assert out["first"].cpu().tolist() == [1]
+    assert torch.all(out["cell_offsets"].cpu() == 1)
+
+
+def test_static_call_allocates_nothing(nlpkg):
+    case = _cases()[0]
+    X, cell, rc, pbc = case
+    Xd = torch.from_numpy(np.ascontiguousarray(X)).cuda()
+    plan = nlpkg.analyze_cell(cell, rc)
+    out = _buffers(X.shape[0], plan.ncells_total, 200 * X.shape[0] + 1024, torch.int32)
+    st, P0, _ = _call(nlpkg, *case, static=True, out=out, Xd=Xd)  # warm-up: module and symbol loaded
+    assert st == 0
+    torch.cuda.synchronize()
+    free0, alloc0 = torch.cuda.mem_get_info()[0], torch.cuda.memory_allocated()
+    st, P1, _ = _call(nlpkg, *case, static=True, out=out, Xd=Xd)
+    torch.cuda.synchronize()
+    assert st == 0 and P1 == P0
+    assert torch.cuda.mem_get_info()[0] == free0 and torch.cuda.memory_allocated() == alloc0
+
+
+def test_static_scratch_rejects_oversize_and_bad_sizes(nlpkg):
     L = nlpkg.lib()
     cell = np.diag([300.0] * 3)
     plan = nlpkg.analyze_cell(cell, 5.0)
     pb = np.ones(3, dtype=np.uint8)
     total = C.c_int64(-1)
-    st = L.nl_neighbour_list_static(C.c_void_p(0), 5_000_000, plan.cell_cm.ctypes.data_as(_D),
-                                    plan.inv_cm.ctypes.data_as(_D), plan.ncells.ctypes.data_as(_I64),
-                                    plan.nxyz.ctypes.data_as(_I64), pb.ctypes.data_as(_U8), 5.0, 4, None, None, None,
-                                    None, None, 0, None, None, None, None, C.byref(total), None)
-    assert st == 3  # NL_ERR_NOMEM
+
+    def call(nat):
+        return L.nl_neighbour_list_static(C.c_void_p(0), nat, plan.cell_cm.ctypes.data_as(_D),
+                                          plan.inv_cm.ctypes.data_as(_D), plan.ncells.ctypes.data_as(_I64),
+                                          plan.nxyz.ctypes.data_as(_I64), pb.ctypes.data_as(_U8), 5.0, 4, None, None,
+                                          None, None, None, 0, None, None, None, None, C.byref(total), None)
+
+    assert call(5_000_000) == 3  # NL_ERR_NOMEM
     assert "32 MiB" in L.nl_last_error().decode()
+    assert call(-1) == 1  # NL_ERR_ARG
+    assert call(2**31) == 1
