@@ -185,7 +185,8 @@ struct Layout {
   // [err 64 | stats 64] [pairs zero region: counters 64 | st_pairs | cell_flag]
   // [build zero region: counters 64 | st_cells | cell_count] [arrays...]
   size_t err, stats, pcount, st_pairs, cell_flag, pend, bcount, st_cells, cell_count, bend;
-  size_t totals, cell_start, cid, ticket, rec, tmp, rec_sorted, scell, counts, lcount, sorig, cs_table, screen_cells,
+  size_t totals, cell_start, cid, ticket, rec, tmp, rec_sorted, scell, counts, lcount, sorig, islot, cs_table,
+      screen_cells,
       big_list, base_end, lists, end;
   bool use_lists = true;  // the workspace holds the pair lists (it reaches `end`)
 };
@@ -232,6 +233,8 @@ Layout layout(int64_t nat, int64_t ncells) {
   L.lcount = o;
   o += up(sizeof(int) * n);
   L.sorig = o;
+  o += up(sizeof(int) * n);
+  L.islot = o;
   o += up(sizeof(int) * n);
   L.cs_table = o;
   o += up(sizeof(double) * 3 * 125);
@@ -411,6 +414,7 @@ nl::PairArgs<TI> pair_args(const nl::Geometry& g, const TI* cell_offsets, const 
   a.lists = L.use_lists ? at<uint2>(ws, L.lists) : nullptr;
   a.lcount = at<int>(ws, L.lcount);
   a.sorig = at<int>(ws, L.sorig);
+  a.islot = at<int>(ws, L.islot);
   a.cap_rec = at<int>(ws, L.pcount) + 2;  // the count pass's list_cap, checked by the write pass
   a.cs_table = at<double>(ws, L.cs_table);
   a.screen_cells = at<int>(ws, L.screen_cells);
@@ -484,6 +488,7 @@ int fill_impl(const nl::Geometry& g, const double* Xs, const TI* perm, const TI*
   a.oS = oS;
   a.oR = oR;
   a.capacity = capacity;
+  a.vec_ok = (reinterpret_cast<uintptr_t>(oS) % 16 == 0) && (reinterpret_cast<uintptr_t>(oR) % 16 == 0);
   nl::launch_pairs<TI>(nl::kModeFill, a, num_sms(), st);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? NL_OK : cuda_fail(e, "launch fill kernel");
@@ -1021,7 +1026,9 @@ static int fill_pairs_entry(const double* d_X_sorted, const void* d_perm, const 
                             void* d_workspace, size_t workspace_bytes, void* stream, int half) {
   if (!cell || !inv_cell || !ncells || !nxyz || !pbc || !d_first || !d_cell_offsets)
     return fail(NL_ERR_ARG, "null argument");
-  if (capacity > 0 && (!d_i || !d_j || !d_S || !d_X_sorted || !d_perm)) return fail(NL_ERR_ARG, "null argument");
+  // an empty system writes no pairs: its (empty) arrays may be null
+  if (capacity > 0 && nat > 0 && (!d_i || !d_j || !d_S || !d_X_sorted || !d_perm))
+    return fail(NL_ERR_ARG, "null argument");
   Layout L;
   int64_t nct;
   int s = check_common(nat, ncells, nxyz, index_bytes, d_workspace, workspace_bytes, L, nct);
@@ -1414,7 +1421,8 @@ int nl_fill_pairs_f32(const float* d_X_sorted, const void* d_perm, const void* d
                       void* stream) {
   if (!cell || !inv_cell || !ncells || !nxyz || !pbc || !d_first || !d_cell_offsets)
     return fail(NL_ERR_ARG, "null argument");
-  if (capacity > 0 && (!d_i || !d_j || !d_S || !d_X_sorted || !d_perm)) return fail(NL_ERR_ARG, "null argument");
+  if (capacity > 0 && nat > 0 && (!d_i || !d_j || !d_S || !d_X_sorted || !d_perm))
+    return fail(NL_ERR_ARG, "null argument");
   Layout L;
   int64_t nct;
   int s = check_common(nat, ncells, nxyz, index_bytes, d_workspace, workspace_bytes, L, nct);

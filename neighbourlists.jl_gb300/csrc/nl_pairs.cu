@@ -880,6 +880,7 @@ __global__ void __launch_bounds__(kSymWarps * 32, BATCH ? NL_SYM_BATCH_MIN_BLOCK
       hm = __float_as_uint(r.w);
       W.hmeta[lane] = hm;
       W.horig[lane] = abase + clampi(A.perm[hs + lane] - 1, g.nat - 1);  // original index in the launch
+      if (!BATCH) A.islot[W.horig[lane]] = hs + lane;  // the write pass walks atoms in original order
     }
     if (!BATCH && __any_sync(0xffffffffu, hm != kPlainMeta) && lane == 0) atomicOr(A.sym_wound, 1);
 #pragma unroll
@@ -1369,6 +1370,246 @@ __global__ void __launch_bounds__(kEmitWarps * 32,
 }
 
 // ------------------------------------------------------------------------
+// Write pass for the symmetric count pass's neighbour masks, in ORIGINAL atom
+// order (single systems).  Atom o's pairs occupy [first[o], first[o+1]) and
+// atoms follow one another in original order, so a warp that takes 32
+// consecutive original atoms writes one contiguous run of every output array:
+// its stores cover whole lines, and only the run's two ends share a sector
+// with another warp's atoms.  (Walking atoms in cell order instead scatters
+// ~26-pair runs over the arrays; the partial sectors at both ends of every
+// run cost extra DRAM traffic.)
+//
+// Per batch of 32 atoms: lane a loads atom a's sorted slot (islot, written
+// by the count pass), position, meta and output range; the warp copies the
+// atoms' 27 mask words to shared memory (one 108-byte read per atom); lane a
+// expands its own masks -- stencil order (dz, dy, dx), then sorted order in
+// each stencil cell, the reference's traversal order -- into a table of
+// (slot of j, loop-shift base, atom) entries at the pair's output position.
+// The stencil cell starts come from cell_offsets (interior cells: a fixed
+// offset per stencil cell; boundary cells: the wrap of stencil_cell).  The
+// table holds kEOEnt entries; a batch with more pairs is cut at atom
+// boundaries (an atom has at most 27 * 32 pairs on this path).  The warp
+// then walks the output positions 32 at a time, passes aligned to multiples
+// of 32 in the output arrays, lane r writing pair base + r: j, S from the
+// packed fields (windings and exact atoms as everywhere) and
+// R = (xj - xi) + C'S with the reference's operations.  i and j are stored per
+// lane; S and R are staged in shared memory and stored as 16-byte vectors
+// (scalar stores for the vectors that straddle the run's ends, or when the
+// arrays are not 16-byte aligned).  The gathers of the next pass are issued
+// before the current pass is finished.
+#ifndef NL_EO_MIN_BLOCKS
+#define NL_EO_MIN_BLOCKS 6  // resident blocks per SM (shared memory holds six)
+#endif
+constexpr int kEOWarps = 2;
+constexpr int kEOEnt = 1024;  // pair entries per warp
+static_assert(kEOEnt >= 27 * 32, "an atom of the symmetric pass has at most 27 * 32 pairs");
+
+template <typename TI>
+struct __align__(16) EOSmem {
+  double rbuf[96];           // R of one pass, three words per pair
+  TI sbuf[96];               // S of one pass
+  unsigned mw[32][27];       // mask words of the batch's atoms
+  unsigned eslot[kEOEnt];    // entry: sorted slot of j
+  unsigned eslp[kEOEnt];     // entry: loop-shift base (cand_base) of j's stencil cell
+  unsigned char ea[kEOEnt];  // entry: atom of the batch
+  double xi[32][3];          // the batch's atoms: FP64 position
+  long long ti[32];          //   output value of i (1-based)
+  unsigned mi[32];           //   record meta (windings, exact bit)
+};
+
+// Stores the pass's staged words [lo, hi) of one output array (96 words per
+// pass at dst = the pass's first word) with 16-byte vectors where a whole
+// vector lies inside [lo, hi), else word by word.
+template <typename T>
+__device__ __forceinline__ void store_staged(T* __restrict__ dst, const T* __restrict__ buf, int lo, int hi, bool vec,
+                                             int lane) {
+  constexpr int V = 16 / int(sizeof(T));
+  if (vec) {
+    for (int v = lane; v < 96 / V; v += 32) {
+      const int e0 = v * V;
+      if (e0 >= lo && e0 + V <= hi) {
+        if constexpr (sizeof(T) == 4) {
+          __stcs(reinterpret_cast<int4*>(dst + e0), *reinterpret_cast<const int4*>(buf + e0));
+        } else {
+          __stcs(reinterpret_cast<longlong2*>(dst + e0), *reinterpret_cast<const longlong2*>(buf + e0));
+        }
+      } else {
+        for (int e = max(e0, lo); e < min(e0 + V, hi); ++e) __stcs(dst + e, buf[e]);
+      }
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int e = lane + 32 * k;
+      if (e >= lo && e < hi) __stcs(dst + e, buf[e]);
+    }
+  }
+}
+
+template <typename TI>
+__global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(PairArgs<TI> A) {
+  if (*A.sym_fail != 0) return;  // the count pass used lists: k_emit writes them
+  __shared__ EOSmem<TI> sm[kEOWarps];
+  __shared__ double cs_blk[3 * kCsN * kCsN * kCsN];
+  __shared__ int qoff[27];  // linear offset of stencil cell q from an interior home cell
+  const Geometry& g = A.g;
+  for (int t = threadIdx.x; t < 3 * kCsN * kCsN * kCsN; t += blockDim.x) cs_blk[t] = A.cs_table[t];
+  if (threadIdx.x < 27) {
+    const int q = threadIdx.x;
+    qoff[q] = (q % 3 - 1) + g.ns[0] * ((q / 3) % 3 - 1 + g.ns[1] * (q / 9 - 1));
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  EOSmem<TI>& E = sm[warp];
+  const int nat = g.nat;
+  const bool plain = *A.sym_wound == 0;  // no atom has a winding or is exact
+  const bool vec = A.vec_ok != 0;
+  const unsigned* masks = reinterpret_cast<const unsigned*>(A.lists);
+  const long long cap = A.capacity;
+  unsigned bad = 0;  // error flags of this lane
+  const long long nwarps = (long long)gridDim.x * kEOWarps;
+  for (long long o0 = ((long long)blockIdx.x * kEOWarps + warp) * 32; o0 < nat; o0 += nwarps * 32) {
+    const int na = int(min(32LL, nat - o0));
+    // ---- the batch's atoms (lane a = atom o0 + a)
+    int slot = 0, hc = 0;
+    long long f = 0, n = 0;
+    __syncwarp();
+    if (lane < na) {
+      const long long o = o0 + lane;
+      slot = clampi(A.islot[o], nat - 1);
+      f = (long long)A.first[o] - 1;
+      n = (long long)A.first[o + 1] - 1 - f;
+      hc = clampi(A.scell[slot], g.ncells - 1);
+      E.xi[lane][0] = A.Xs[3LL * slot + 0];
+      E.xi[lane][1] = A.Xs[3LL * slot + 1];
+      E.xi[lane][2] = A.Xs[3LL * slot + 2];
+      E.mi[lane] = __float_as_uint(A.rec[slot].w);
+      E.ti[lane] = o + 1;
+    }
+    for (int a = 0; a < na; ++a) {  // mask words: one 108-byte read per atom
+      const int sa = __shfl_sync(0xffffffffu, slot, a);
+      if (lane < 27) E.mw[a][lane] = __ldcs(masks + 27LL * sa + lane);
+    }
+    __syncwarp();
+    const int c0 = hc % g.ns[0] + 1, c1 = (hc / g.ns[0]) % g.ns[1] + 1, c2 = hc / (g.ns[0] * g.ns[1]) + 1;
+    const bool interior = c0 >= 2 && c0 < g.ns[0] && c1 >= 2 && c1 < g.ns[1] && c2 >= 2 && c2 < g.ns[2];
+    // ---- chunks of at most kEOEnt pairs, cut at atom boundaries
+    int l0 = 0;
+    while (l0 < na) {
+      const long long G = __shfl_sync(0xffffffffu, f, l0);
+      const unsigned inch = __ballot_sync(0xffffffffu, lane >= l0 && lane < na && f + n - G <= kEOEnt);
+      const int l1 = l0 + __popc(inch >> l0);
+      if (l1 == l0) {  // an atom with more pairs than its masks can hold: counts and masks disagree
+        bad |= kFlagInconsistent;
+        break;
+      }
+      const long long Gend = __shfl_sync(0xffffffffu, f + n, l1 - 1);
+      // ---- expansion: lane a writes its entries at [f - G, f - G + n)
+      if (lane >= l0 && lane < l1) {
+        int e = int(f - G);
+        const int eend = e + int(n);
+        for (int q = 0; q < 27; ++q) {
+          unsigned m = E.mw[lane][q];
+          if (!m) continue;
+          int lin;
+          unsigned slp;
+          if (interior) {
+            lin = hc + qoff[q];
+            slp = cand_base(0, 0, 0);
+          } else {
+            float ox, oy, oz;
+            lin = stencil_cell(g, nullptr, 0, 3, 3, c0, c1, c2, q, slp, ox, oy, oz);
+          }
+          if (lin < 0) {  // a neighbour in a cell outside an open axis
+            bad |= kFlagInconsistent;
+            continue;
+          }
+          const unsigned start = unsigned(clampi(A.cell_offsets[lin] - 1, nat));
+          while (m) {
+            const int b = __ffs(m) - 1;
+            m &= m - 1u;
+            if (e >= 0 && e < eend && e < kEOEnt) {  // (bounds hold for consistent counts)
+              E.eslot[e] = start + unsigned(b);
+              E.eslp[e] = slp;
+              E.ea[e] = (unsigned char)lane;
+            }
+            ++e;
+          }
+        }
+        if (e != eend) bad |= kFlagInconsistent;  // counts and masks disagree
+      }
+      __syncwarp();
+      // ---- emission, passes aligned to 32 output positions
+      const long long hi = min(Gend, cap);
+      if (Gend > cap && lane == l0) bad |= kFlagCapacity;
+      struct Ld {
+        double x0, x1, x2;
+        long long oj;
+        unsigned mj, slp;
+        int a;
+        bool act;
+      };
+      auto load = [&](long long b, Ld& u) {
+        const long long p = b + lane;
+        u.act = p >= G && p < hi && p - G < kEOEnt;
+        u.a = 0;
+        u.slp = 0;
+        u.mj = kPlainMeta;
+        u.x0 = u.x1 = u.x2 = 0.0;
+        u.oj = 0;
+        if (u.act) {
+          const int k = int(p - G);
+          const int sj = clampi(int(E.eslot[k]), nat - 1);
+          u.slp = E.eslp[k];
+          u.a = E.ea[k] & 31;
+          u.x0 = __ldg(A.Xs + 3LL * sj + 0);
+          u.x1 = __ldg(A.Xs + 3LL * sj + 1);
+          u.x2 = __ldg(A.Xs + 3LL * sj + 2);
+          u.oj = (long long)__ldg(A.perm + sj);
+          if (!plain) u.mj = __float_as_uint(__ldg(&A.rec[sj].w));
+        }
+      };
+      auto finish = [&](long long b, const Ld& u) {
+        const double* xi = E.xi[u.a];
+        const double xj[3] = {u.x0, u.x1, u.x2};
+        int S[3];
+        pair_S(g, xi, xj, E.mi[u.a], cand_word(u.slp, u.mj), S);
+        double R[3] = {0.0, 0.0, 0.0};
+        if (A.oR) pair_R(g, cs_blk, xi, xj, S[0], S[1], S[2], u.act, R);
+        const long long p = b + lane;
+        if (u.act) {
+          __stcs(A.oi + p, TI(E.ti[u.a]));
+          __stcs(A.oj + p, TI(u.oj));
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          E.sbuf[3 * lane + k] = TI(S[k]);
+          E.rbuf[3 * lane + k] = R[k];
+        }
+        __syncwarp();
+        const int lo = 3 * int(max(G - b, 0LL)), hw = 3 * int(min(hi - b, 32LL));
+        store_staged<TI>(A.oS + 3 * b, E.sbuf, lo, hw, vec, lane);
+        if (A.oR) store_staged<double>(A.oR + 3 * b, E.rbuf, lo, hw, vec, lane);
+        __syncwarp();
+      };
+      const long long b0 = G & ~31LL;
+      if (b0 < hi) {
+        Ld cur, nxt;
+        load(b0, cur);
+        for (long long b = b0; b < hi; b += 32) {
+          load(b + 32, nxt);  // in flight while this pass is finished
+          finish(b, cur);
+          cur = nxt;
+        }
+      }
+      __syncwarp();
+      l0 = l1;
+    }
+  }
+  if (bad) atomicOr(A.err, bad);
+}
+
+// ------------------------------------------------------------------------
 // Count pass with one thread per home atom.  Each thread walks its own
 // stencil in the reference's order (dz, dy, dx; then the cell's atoms in
 // sorted order), screens every candidate with the same FP32 arithmetic as
@@ -1656,7 +1897,14 @@ static void launch_modes(int mode, const PairArgs<TI>& a, int num_sms, cudaStrea
         long long eb = ((long long)a.nat_total + 32 * kEmitWarps - 1) / (32 * kEmitWarps);
         if (eb > (long long)num_sms * ebps) eb = (long long)num_sms * ebps;
         k_emit<TI, BATCH, false><<<int(eb), kEmitWarps * 32, 0, st>>>(a);
-        if (!BATCH || a.sym) k_emit<TI, BATCH, true><<<int(eb), kEmitWarps * 32, 0, st>>>(a);
+        if (!BATCH) {  // masks: written in original atom order
+          const int obps = a.emit_blocks_per_sm > 0 ? a.emit_blocks_per_sm : 2 * NL_EO_MIN_BLOCKS;
+          long long ob = ((long long)a.nat_total + 32 * kEOWarps - 1) / (32 * kEOWarps);
+          if (ob > (long long)num_sms * obps) ob = (long long)num_sms * obps;
+          k_emit_orig<TI><<<int(ob), kEOWarps * 32, 0, st>>>(a);
+        } else if (a.sym) {
+          k_emit<TI, BATCH, true><<<int(eb), kEmitWarps * 32, 0, st>>>(a);
+        }
       }
       k_pairs<TI, kModeFill, BATCH><<<int(blocks), kPairWarps * 32, 0, st>>>(a);
       break;
