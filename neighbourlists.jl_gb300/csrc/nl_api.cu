@@ -185,7 +185,7 @@ struct Layout {
   // [err 64 | stats 64] [pairs zero region: counters 64 | st_pairs | cell_flag]
   // [build zero region: counters 64 | st_cells | cell_count] [arrays...]
   size_t err, stats, pcount, st_pairs, cell_flag, pend, bcount, st_cells, cell_count, bend;
-  size_t totals, cell_start, cid, ticket, rec, tmp, rec_sorted, scell, counts, lcount, sorig, islot, cs_table,
+  size_t totals, cell_start, cid, ticket, rec, tmp, rec_sorted, scell, counts, lcount, sorig, hdr, cs_table,
       screen_cells,
       big_list, base_end, lists, end;
   bool use_lists = true;  // the workspace holds the pair lists (it reaches `end`)
@@ -234,8 +234,8 @@ Layout layout(int64_t nat, int64_t ncells) {
   o += up(sizeof(int) * n);
   L.sorig = o;
   o += up(sizeof(int) * n);
-  L.islot = o;
-  o += up(sizeof(int) * n);
+  L.hdr = o;
+  o += up(sizeof(int2) * n);
   L.cs_table = o;
   o += up(sizeof(double) * 3 * 125);
   L.screen_cells = o;
@@ -414,7 +414,7 @@ nl::PairArgs<TI> pair_args(const nl::Geometry& g, const TI* cell_offsets, const 
   a.lists = L.use_lists ? at<uint2>(ws, L.lists) : nullptr;
   a.lcount = at<int>(ws, L.lcount);
   a.sorig = at<int>(ws, L.sorig);
-  a.islot = at<int>(ws, L.islot);
+  a.hdr = at<int2>(ws, L.hdr);
   a.cap_rec = at<int>(ws, L.pcount) + 2;  // the count pass's list_cap, checked by the write pass
   a.cs_table = at<double>(ws, L.cs_table);
   a.screen_cells = at<int>(ws, L.screen_cells);

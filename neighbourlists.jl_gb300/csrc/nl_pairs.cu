@@ -880,7 +880,6 @@ __global__ void __launch_bounds__(kSymWarps * 32, BATCH ? NL_SYM_BATCH_MIN_BLOCK
       hm = __float_as_uint(r.w);
       W.hmeta[lane] = hm;
       W.horig[lane] = abase + clampi(A.perm[hs + lane] - 1, g.nat - 1);  // original index in the launch
-      if (!BATCH) A.islot[W.horig[lane]] = hs + lane;  // the write pass walks atoms in original order
     }
     if (!BATCH && __any_sync(0xffffffffu, hm != kPlainMeta) && lane == 0) atomicOr(A.sym_wound, 1);
 #pragma unroll
@@ -1061,6 +1060,249 @@ __global__ void __launch_bounds__(kSymWarps * 32, BATCH ? NL_SYM_BATCH_MIN_BLOCK
       if (c) atomicAdd(A.counts + W.horig[lane], c);
     }
     __syncwarp();
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) rechecks += __shfl_xor_sync(0xffffffffu, rechecks, o);
+  if (lane == 0 && rechecks) atomicAdd(A.stats, (unsigned long long)rechecks);
+}
+
+// ------------------------------------------------------------------------
+// Symmetric count pass of single systems, candidate-parallel.  It makes the
+// same decisions and writes the same neighbour masks and counts as
+// k_pairs_sym: each unordered pair of cells (A, A + d), d the centre or one
+// of the 13 stencil offsets after it, is screened once, by the warp of A.
+// Lanes hold the candidates -- the atoms of stencil cells q = 13..26 in
+// stencil order (centre first), 32 per round -- and the warp walks the home
+// atoms two at a time with packed FP32 pair arithmetic (f32x2: the same IEEE
+// operations, rounded per element, so the screen's r2 is bit for bit the
+// scalar fmaf(rz, rz, fmaf(ry, ry, rx * rx))).  A home atom's accepted
+// candidates of one round are a ballot; its row word for stencil cell q is
+// the run of ballot bits of q's candidates (a funnel shift across two
+// rounds).  A candidate's column word -- the home atoms that accepted it,
+// stored as its word for the mirrored cell 26 - q -- accumulates in a
+// register.  The next cell's stencil ranges are loaded one cell ahead.  The
+// write pass finds stencil cells from cell_offsets, so no per-cell stencil
+// table is written; each home atom's (sorted slot, home cell) goes to hdr,
+// indexed by its original index, for the original-order write pass.  Mask
+// words are kMaskStride per atom (27 used) so that they load as 16-byte
+// vectors.
+constexpr int kSCWarps = 4;
+constexpr long long kMaskStride = 28;  // mask words per atom (27 used; 16-byte rows)
+constexpr int kSCMaxRounds = 14;  // 14 stencil cells of at most 32 atoms
+#ifndef NL_SC_MIN_BLOCKS
+#define NL_SC_MIN_BLOCKS 6
+#endif
+
+struct __align__(16) SCSmem {
+  float hx[32], hy[32], hz[32];      // home atoms: FP32 record (+inf beyond the cell's atoms)
+  unsigned hmeta[32];
+  int horig[32];
+  int hcnt[32];                      // pairs in the rows written by this warp
+  unsigned B[32][kSCMaxRounds + 1];  // ballot of home atom a in round r
+};
+
+__device__ __forceinline__ unsigned long long f2pack(float a, float b) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void f2unpack(unsigned long long v, float& a, float& b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ unsigned long long f2sub(unsigned long long a, unsigned long long b) {
+  unsigned long long r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ unsigned long long f2mul(unsigned long long a, unsigned long long b) {
+  unsigned long long r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ unsigned long long f2fma(unsigned long long a, unsigned long long b, unsigned long long c) {
+  unsigned long long r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+
+template <typename TI>
+__global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(PairArgs<TI> A) {
+  __shared__ SCSmem sm[kSCWarps];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  SCSmem& W = sm[warp];
+  const Geometry& g = A.g;
+  const int nat = g.nat;
+  const float lo = g.lo, hi = g.hi;
+  const float inf = __int_as_float(0x7f800000), nan = __int_as_float(0x7fc00000);
+  unsigned rechecks = 0;
+  if (A.cap_rec && blockIdx.x == 0 && threadIdx.x == 0) *A.cap_rec = A.list_cap;
+  unsigned* masks = reinterpret_cast<unsigned*>(A.lists);
+  const int nwarps = gridDim.x * kSCWarps;
+  // stencil cell q = lane of home cell h: sorted range, loop-shift base, FP32 corner offset
+  struct St {
+    int start, cnt, lin;
+    unsigned slp;
+    float ox, oy, oz;
+  };
+  auto stencil = [&](int h, St& s) {
+    s.start = s.cnt = 0;
+    s.lin = -1;
+    s.slp = 0;
+    s.ox = s.oy = s.oz = 0.f;
+    if (h < A.ncells_total && lane < 27) {
+      const int c0 = h % g.ns[0] + 1, c1 = (h / g.ns[0]) % g.ns[1] + 1, c2 = h / (g.ns[0] * g.ns[1]) + 1;
+      s.lin = stencil_cell(g, nullptr, 0, 3, 3, c0, c1, c2, lane, s.slp, s.ox, s.oy, s.oz);
+      if (s.lin >= 0) {
+        s.start = clampi(A.cell_offsets[s.lin] - 1, nat);
+        s.cnt = max(clampi(A.cell_offsets[s.lin + 1] - 1, nat) - s.start, 0);
+      }
+    }
+  };
+  int h = blockIdx.x * kSCWarps + warp;
+  St cur;
+  stencil(h, cur);
+  for (; h < A.ncells_total; h += nwarps) {
+    St nxt;
+    stencil(h + nwarps, nxt);  // the next cell's ranges are loaded while this one is screened
+    const int hs = __shfl_sync(0xffffffffu, cur.start, 13), nb = __shfl_sync(0xffffffffu, cur.cnt, 13);
+    if (nb > 32 || __any_sync(0xffffffffu, cur.cnt > 32)) {
+      if (lane == 0) atomicOr(A.sym_fail, 1);  // a crowded cell: the per-cell pass with lists counts instead
+    } else if (nb > 0) {
+      // words q < 13 of the home atoms that no other warp writes: their cell is empty or outside
+      const unsigned zq = __ballot_sync(0xffffffffu, lane < 13 && (cur.lin < 0 || cur.cnt == 0));
+      if (zq)
+        for (int t = lane; t < nb * 13; t += 32) {
+          const int a = t / 13, q = t - 13 * a;
+          if ((zq >> q) & 1u) masks[kMaskStride * (hs + a) + q] = 0u;
+        }
+      unsigned hm = kPlainMeta;
+      {
+        float x = inf, y = inf, z = inf;
+        if (lane < nb) {
+          const float4 r = A.rec[hs + lane];  // exact atoms carry NaN coordinates
+          x = r.x;
+          y = r.y;
+          z = r.z;
+          hm = __float_as_uint(r.w);
+          const int o = clampi(A.perm[hs + lane] - 1, nat - 1);
+          W.horig[lane] = o;
+          A.hdr[o] = make_int2(hs + lane, h);  // the write pass walks atoms in original order
+        }
+        W.hx[lane] = x;
+        W.hy[lane] = y;
+        W.hz[lane] = z;
+        W.hmeta[lane] = hm;
+        W.hcnt[lane] = 0;
+      }
+      if (__any_sync(0xffffffffu, hm != kPlainMeta) && lane == 0) atomicOr(A.sym_wound, 1);
+      // candidates: stencil cells 13..26 in stencil order, flattened
+      const int scnt = lane >= 13 ? cur.cnt : 0;
+      int incl = scnt;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+      }
+      const int T = __shfl_sync(0xffffffffu, incl, 31);
+      const int nr = (T + 31) >> 5;  // <= kSCMaxRounds
+      __syncwarp();
+      for (int rr = 0; rr < nr; ++rr) {
+        const int f = 32 * rr + lane;
+        const bool valid = f < T;
+        const int gf = min(f, T - 1);
+        int qq = 0;
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1) {
+          const int v = __shfl_sync(0xffffffffu, incl, qq + step - 1);
+          if (v <= gf) qq += step;
+        }
+        const int q_incl = __shfl_sync(0xffffffffu, incl, qq);
+        const int q_cnt = __shfl_sync(0xffffffffu, scnt, qq);
+        const int q_start = __shfl_sync(0xffffffffu, cur.start, qq);
+        const unsigned q_slp = __shfl_sync(0xffffffffu, cur.slp, qq);
+        const float qx = __shfl_sync(0xffffffffu, cur.ox, qq);
+        const float qy = __shfl_sync(0xffffffffu, cur.oy, qq);
+        const float qz = __shfl_sync(0xffffffffu, cur.oz, qq);
+        const int slot = clampi(q_start + gf - (q_incl - q_cnt), nat - 1);
+        const float4 r = A.rec[slot];
+        const unsigned cw = cand_word(q_slp, __float_as_uint(r.w));
+        const bool ex = (cw & kExactBit) != 0;
+        const float cx = ex ? nan : r.x + qx, cy = ex ? nan : r.y + qy, cz = ex ? nan : r.z + qz;
+        const int corig = clampi(A.perm[slot] - 1, nat - 1);
+        const unsigned long long px = f2pack(cx, cx), py = f2pack(cy, cy), pz = f2pack(cz, cz);
+        const bool fwd = qq > 13;  // a forward cell: this warp writes the candidate's column word
+        unsigned col = 0u;
+        for (int a = 0; a < nb; a += 2) {
+          // home atoms a and a + 1 (+inf beyond the cell): packed (a, a + 1) pairs
+          const unsigned long long hx2 = *reinterpret_cast<const unsigned long long*>(&W.hx[a]);
+          const unsigned long long hy2 = *reinterpret_cast<const unsigned long long*>(&W.hy[a]);
+          const unsigned long long hz2 = *reinterpret_cast<const unsigned long long*>(&W.hz[a]);
+          const unsigned long long rx = f2sub(px, hx2), ry = f2sub(py, hy2), rz = f2sub(pz, hz2);
+          const unsigned long long r2p = f2fma(rz, rz, f2fma(ry, ry, f2mul(rx, rx)));
+          float r20, r21;
+          f2unpack(r2p, r20, r21);
+          const bool v0 = valid && f != a, v1 = valid && a + 1 < nb && f != a + 1;  // the centre holds the home atom itself at f == a
+          bool acc0 = v0 && r20 < lo, acc1 = v1 && r21 < lo;
+          const bool unc0 = v0 && !(r20 < lo) && !(r20 > hi), unc1 = v1 && !(r21 < lo) && !(r21 > hi);
+          if (__any_sync(0xffffffffu, unc0 || unc1)) {  // the band, and exact atoms (NaN): FP64 with the reference's arithmetic
+            if (unc0) {
+              ++rechecks;
+              acc0 = exact_pair(g, A.Xs, hs + a, slot, W.hmeta[a], cw);
+            }
+            if (unc1) {
+              ++rechecks;
+              acc1 = exact_pair(g, A.Xs, hs + a + 1, slot, W.hmeta[a + 1], cw);
+            }
+          }
+          // full lists keep both directions (row and, for forward cells, column);
+          // a half list keeps the one half_keep selects
+          bool row0 = acc0, row1 = acc1, col0 = acc0 && fwd, col1 = acc1 && fwd;
+          if (A.half) {
+            if (acc0) {
+              const bool k = half_keep(W.horig[a], corig, cw, W.hmeta[a]);
+              row0 = k;
+              col0 = col0 && !k;
+            }
+            if (acc1) {
+              const bool k = half_keep(W.horig[a + 1], corig, cw, W.hmeta[a + 1]);
+              row1 = k;
+              col1 = col1 && !k;
+            }
+          }
+          const unsigned b0 = __ballot_sync(0xffffffffu, row0), b1 = __ballot_sync(0xffffffffu, row1);
+          if (lane == 0) {
+            W.B[a][rr] = b0;
+            W.B[a + 1][rr] = b1;  // a + 1 <= 31: nb <= 32 and a is even
+          }
+          col |= (col0 ? 1u << a : 0u) | (col1 ? 2u << a : 0u);
+        }
+        if (valid && fwd) {  // the candidate's word for its mirrored cell
+          masks[kMaskStride * slot + (26 - qq)] = col;
+          if (col) atomicAdd(A.counts + corig, __popc(col));
+        }
+      }
+      __syncwarp();
+      // rows: word q = 13..26 of every home atom, from its ballots
+      for (int t0 = 0; t0 < nb * 14; t0 += 32) {
+        const int t = t0 + lane;
+        const int a = t / 14, k = t - 14 * (t / 14);
+        const int off = __shfl_sync(0xffffffffu, incl - scnt, 13 + k);
+        const int cnt = __shfl_sync(0xffffffffu, scnt, 13 + k);
+        if (t < nb * 14) {
+          unsigned w = 0u;
+          if (cnt > 0) {  // then off + cnt <= 32 nr: both ballot words exist
+            w = __funnelshift_r(W.B[a][off >> 5], W.B[a][(off >> 5) + 1], off & 31);
+            if (cnt < 32) w &= (1u << cnt) - 1u;
+          }
+          masks[kMaskStride * (hs + a) + 13 + k] = w;
+          if (w) atomicAdd(&W.hcnt[a], __popc(w));
+        }
+      }
+      __syncwarp();
+      if (lane < nb && W.hcnt[lane]) atomicAdd(A.counts + W.horig[lane], W.hcnt[lane]);
+      __syncwarp();
+    }
+    cur = nxt;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) rechecks += __shfl_xor_sync(0xffffffffu, rechecks, o);
@@ -1377,28 +1619,30 @@ __global__ void __launch_bounds__(kEmitWarps * 32,
 // its stores cover whole lines, and only the run's two ends share a sector
 // with another warp's atoms.  (Walking atoms in cell order instead scatters
 // ~26-pair runs over the arrays; the partial sectors at both ends of every
-// run cost extra DRAM traffic.)
+// run cost extra DRAM traffic.)  The price is that the neighbours' positions
+// are gathered from anywhere in the sorted arrays (L2, not L1), so the
+// kernel keeps many loads in flight:
 //
-// Per batch of 32 atoms: lane a loads atom a's sorted slot (islot, written
-// by the count pass), position, meta and output range; the warp copies the
-// atoms' 27 mask words to shared memory (one 108-byte read per atom); lane a
-// expands its own masks -- stencil order (dz, dy, dx), then sorted order in
-// each stencil cell, the reference's traversal order -- into a table of
-// (slot of j, loop-shift base, atom) entries at the pair's output position.
-// The stencil cell starts come from cell_offsets (interior cells: a fixed
-// offset per stencil cell; boundary cells: the wrap of stencil_cell).  The
+// Per batch of 32 atoms, lane a holds atom o0 + a: its header (sorted slot,
+// home cell) and output range, then -- loads issued together -- its 27 mask
+// words (16-byte vector loads), position, record meta and the sorted start of
+// each of its 27 stencil cells (from cell_offsets; the wrapped cell and loop
+// shift per axis follow from the home cell).  Lane a expands its own masks,
+// in stencil order (dz, dy, dx) and sorted order within each stencil cell --
+// the reference's traversal order -- into a shared-memory table of (slot of
+// j, loop-shift base, atom) entries at the pairs' output positions.  The
 // table holds kEOEnt entries; a batch with more pairs is cut at atom
-// boundaries (an atom has at most 27 * 32 pairs on this path).  The warp
-// then walks the output positions 32 at a time, passes aligned to multiples
-// of 32 in the output arrays, lane r writing pair base + r: j, S from the
-// packed fields (windings and exact atoms as everywhere) and
-// R = (xj - xi) + C'S with the reference's operations.  i and j are stored per
-// lane; S and R are staged in shared memory and stored as 16-byte vectors
-// (scalar stores for the vectors that straddle the run's ends, or when the
-// arrays are not 16-byte aligned).  The gathers of the next pass are issued
-// before the current pass is finished.
+// boundaries (an atom has at most 27 * 32 pairs on this path).  The warp then
+// walks the output positions 32 at a time, passes aligned to multiples of 32
+// in the output arrays, lane r writing pair base + r: j, S from the packed
+// fields (windings and exact atoms as everywhere) and R = (xj - xi) + C'S
+// with the reference's operations.  i and j are stored per lane; S and R are
+// staged in shared memory and stored as 16-byte vectors (scalar stores for
+// the vectors that straddle the run's ends, or when the arrays are not
+// 16-byte aligned).  The gathers of the next two passes are in flight while
+// two passes are finished.
 #ifndef NL_EO_MIN_BLOCKS
-#define NL_EO_MIN_BLOCKS 6  // resident blocks per SM (shared memory holds six)
+#define NL_EO_MIN_BLOCKS 6  // resident blocks per SM the register budget targets (168 registers, no spills)
 #endif
 constexpr int kEOWarps = 2;
 constexpr int kEOEnt = 1024;  // pair entries per warp
@@ -1406,15 +1650,14 @@ static_assert(kEOEnt >= 27 * 32, "an atom of the symmetric pass has at most 27 *
 
 template <typename TI>
 struct __align__(16) EOSmem {
-  double rbuf[96];           // R of one pass, three words per pair
-  TI sbuf[96];               // S of one pass
-  unsigned mw[32][27];       // mask words of the batch's atoms
-  unsigned eslot[kEOEnt];    // entry: sorted slot of j
-  unsigned eslp[kEOEnt];     // entry: loop-shift base (cand_base) of j's stencil cell
-  unsigned char ea[kEOEnt];  // entry: atom of the batch
-  double xi[32][3];          // the batch's atoms: FP64 position
-  long long ti[32];          //   output value of i (1-based)
-  unsigned mi[32];           //   record meta (windings, exact bit)
+  double rbuf[96];            // R of one pass, three words per pair
+  TI sbuf[96];                // S of one pass
+  unsigned eslot[kEOEnt];     // entry: sorted slot of j
+  unsigned short einfo[kEOEnt];  // entry: atom of the batch | loop shifts of j's stencil cell (2 bits per axis)
+  unsigned st[32][27];        // the batch's atoms: sorted start of each stencil cell
+  double xi[32][3];           //   FP64 position
+  long long ti[32];           //   output value of i (1-based)
+  unsigned mi[32];            //   record meta (windings, exact bit)
 };
 
 // Stores the pass's staged words [lo, hi) of one output array (96 words per
@@ -1446,18 +1689,42 @@ __device__ __forceinline__ void store_staged(T* __restrict__ dst, const T* __res
   }
 }
 
+// The three cells c - 1, c, c + 1 along one axis (c 1-based): 0-based wrapped
+// index, loop shift and whether the cell exists (wrap_and_shift,
+// cell_list.jl:105-120; periodic axes of the symmetric path have n >= 3).
+__device__ __forceinline__ void axis3(int c, int n, int pbc, int* w, int* s, bool* ok) {
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    int i = c + d - 1, sh = 0;
+    bool v = true;
+    if (i < 1) {
+      if (pbc) {
+        i += n;
+        sh = -1;
+      } else {
+        v = false;
+      }
+    } else if (i > n) {
+      if (pbc) {
+        i -= n;
+        sh = 1;
+      } else {
+        v = false;
+      }
+    }
+    w[d] = i - 1;
+    s[d] = sh;
+    ok[d] = v;
+  }
+}
+
 template <typename TI>
 __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(PairArgs<TI> A) {
   if (*A.sym_fail != 0) return;  // the count pass used lists: k_emit writes them
   __shared__ EOSmem<TI> sm[kEOWarps];
   __shared__ double cs_blk[3 * kCsN * kCsN * kCsN];
-  __shared__ int qoff[27];  // linear offset of stencil cell q from an interior home cell
   const Geometry& g = A.g;
   for (int t = threadIdx.x; t < 3 * kCsN * kCsN * kCsN; t += blockDim.x) cs_blk[t] = A.cs_table[t];
-  if (threadIdx.x < 27) {
-    const int q = threadIdx.x;
-    qoff[q] = (q % 3 - 1) + g.ns[0] * ((q / 3) % 3 - 1 + g.ns[1] * (q / 9 - 1));
-  }
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   EOSmem<TI>& E = sm[warp];
@@ -1470,34 +1737,59 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
   const long long nwarps = (long long)gridDim.x * kEOWarps;
   for (long long o0 = ((long long)blockIdx.x * kEOWarps + warp) * 32; o0 < nat; o0 += nwarps * 32) {
     const int na = int(min(32LL, nat - o0));
-    // ---- the batch's atoms (lane a = atom o0 + a)
-    int slot = 0, hc = 0;
+    const bool own = lane < na;
+    // ---- lane a: atom o0 + a.  Header and output range first ...
+    int2 hd = make_int2(0, 0);
     long long f = 0, n = 0;
-    __syncwarp();
-    if (lane < na) {
+    if (own) {
       const long long o = o0 + lane;
-      slot = clampi(A.islot[o], nat - 1);
+      hd = A.hdr[o];
       f = (long long)A.first[o] - 1;
       n = (long long)A.first[o + 1] - 1 - f;
-      hc = clampi(A.scell[slot], g.ncells - 1);
+    }
+    const int slot = clampi(hd.x, nat - 1), hc = clampi(hd.y, g.ncells - 1);
+    int wx[3], wy[3], wz[3], sx[3], sy[3], sz[3];
+    bool okx[3], oky[3], okz[3];
+    axis3(hc % g.ns[0] + 1, g.ns[0], g.pbc[0], wx, sx, okx);
+    axis3((hc / g.ns[0]) % g.ns[1] + 1, g.ns[1], g.pbc[1], wy, sy, oky);
+    axis3(hc / (g.ns[0] * g.ns[1]) + 1, g.ns[2], g.pbc[2], wz, sz, okz);
+    // ... then masks, position, meta and the 27 stencil cell starts, all in flight together
+    uint4 mv[7];
+    const uint4* mrow = reinterpret_cast<const uint4*>(masks + kMaskStride * slot);
+#pragma unroll
+    for (int k = 0; k < 7; ++k) mv[k] = own ? __ldg(mrow + k) : make_uint4(0u, 0u, 0u, 0u);
+    {
+      TI st[27];
+#pragma unroll
+      for (int q = 0; q < 27; ++q) {
+        const int dx = q % 3, dy = (q / 3) % 3, dz = q / 9;
+        const int lin = wx[dx] + g.ns[0] * (wy[dy] + g.ns[1] * wz[dz]);
+        st[q] = own && okx[dx] && oky[dy] && okz[dz] ? A.cell_offsets[lin] : TI(1);
+      }
+#pragma unroll
+      for (int q = 0; q < 27; ++q) E.st[lane][q] = unsigned(clampi(st[q] - 1, nat));
+    }
+    if (own) {
       E.xi[lane][0] = A.Xs[3LL * slot + 0];
       E.xi[lane][1] = A.Xs[3LL * slot + 1];
       E.xi[lane][2] = A.Xs[3LL * slot + 2];
       E.mi[lane] = __float_as_uint(A.rec[slot].w);
-      E.ti[lane] = o + 1;
+      E.ti[lane] = o0 + lane + 1;
     }
-    for (int a = 0; a < na; ++a) {  // mask words: one 108-byte read per atom
-      const int sa = __shfl_sync(0xffffffffu, slot, a);
-      if (lane < 27) E.mw[a][lane] = __ldcs(masks + 27LL * sa + lane);
+    unsigned m[27];
+#pragma unroll
+    for (int k = 0; k < 7; ++k) {
+      m[4 * k] = mv[k].x;
+      if (4 * k + 1 < 27) m[4 * k + 1] = mv[k].y;
+      if (4 * k + 2 < 27) m[4 * k + 2] = mv[k].z;
+      if (4 * k + 3 < 27) m[4 * k + 3] = mv[k].w;
     }
     __syncwarp();
-    const int c0 = hc % g.ns[0] + 1, c1 = (hc / g.ns[0]) % g.ns[1] + 1, c2 = hc / (g.ns[0] * g.ns[1]) + 1;
-    const bool interior = c0 >= 2 && c0 < g.ns[0] && c1 >= 2 && c1 < g.ns[1] && c2 >= 2 && c2 < g.ns[2];
     // ---- chunks of at most kEOEnt pairs, cut at atom boundaries
     int l0 = 0;
     while (l0 < na) {
       const long long G = __shfl_sync(0xffffffffu, f, l0);
-      const unsigned inch = __ballot_sync(0xffffffffu, lane >= l0 && lane < na && f + n - G <= kEOEnt);
+      const unsigned inch = __ballot_sync(0xffffffffu, lane >= l0 && own && f + n - G <= kEOEnt);
       const int l1 = l0 + __popc(inch >> l0);
       if (l1 == l0) {  // an atom with more pairs than its masks can hold: counts and masks disagree
         bad |= kFlagInconsistent;
@@ -1508,32 +1800,27 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
       if (lane >= l0 && lane < l1) {
         int e = int(f - G);
         const int eend = e + int(n);
+#pragma unroll
         for (int q = 0; q < 27; ++q) {
-          unsigned m = E.mw[lane][q];
-          if (!m) continue;
-          int lin;
-          unsigned slp;
-          if (interior) {
-            lin = hc + qoff[q];
-            slp = cand_base(0, 0, 0);
-          } else {
-            float ox, oy, oz;
-            lin = stencil_cell(g, nullptr, 0, 3, 3, c0, c1, c2, q, slp, ox, oy, oz);
-          }
-          if (lin < 0) {  // a neighbour in a cell outside an open axis
-            bad |= kFlagInconsistent;
-            continue;
-          }
-          const unsigned start = unsigned(clampi(A.cell_offsets[lin] - 1, nat));
-          while (m) {
-            const int b = __ffs(m) - 1;
-            m &= m - 1u;
-            if (e >= 0 && e < eend && e < kEOEnt) {  // (bounds hold for consistent counts)
-              E.eslot[e] = start + unsigned(b);
-              E.eslp[e] = slp;
-              E.ea[e] = (unsigned char)lane;
+          unsigned mq = m[q];
+          if (mq) {
+            const int dx = q % 3, dy = (q / 3) % 3, dz = q / 9;
+            if (!(okx[dx] && oky[dy] && okz[dz])) {  // a neighbour in a cell outside an open axis
+              bad |= kFlagInconsistent;
+              mq = 0u;
             }
-            ++e;
+            const unsigned info = unsigned(lane) | unsigned(sx[dx] + 1) << 5 | unsigned(sy[dy] + 1) << 7 |
+                                  unsigned(sz[dz] + 1) << 9;
+            const unsigned start = E.st[lane][q];
+            while (mq) {
+              const int b = __ffs(mq) - 1;
+              mq &= mq - 1u;
+              if (e >= 0 && e < eend && e < kEOEnt) {  // (bounds hold for consistent counts)
+                E.eslot[e] = start + unsigned(b);
+                E.einfo[e] = (unsigned short)info;
+              }
+              ++e;
+            }
           }
         }
         if (e != eend) bad |= kFlagInconsistent;  // counts and masks disagree
@@ -1544,7 +1831,7 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
       if (Gend > cap && lane == l0) bad |= kFlagCapacity;
       struct Ld {
         double x0, x1, x2;
-        long long oj;
+        int oj;  // perm value (<= 2^31 - 2)
         unsigned mj, slp;
         int a;
         bool act;
@@ -1560,12 +1847,13 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
         if (u.act) {
           const int k = int(p - G);
           const int sj = clampi(int(E.eslot[k]), nat - 1);
-          u.slp = E.eslp[k];
-          u.a = E.ea[k] & 31;
+          const unsigned info = E.einfo[k];
+          u.slp = cand_base(int((info >> 5) & 3u) - 1, int((info >> 7) & 3u) - 1, int((info >> 9) & 3u) - 1);
+          u.a = int(info & 31u);
           u.x0 = __ldg(A.Xs + 3LL * sj + 0);
           u.x1 = __ldg(A.Xs + 3LL * sj + 1);
           u.x2 = __ldg(A.Xs + 3LL * sj + 2);
-          u.oj = (long long)__ldg(A.perm + sj);
+          u.oj = int(__ldg(A.perm + sj));
           if (!plain) u.mj = __float_as_uint(__ldg(&A.rec[sj].w));
         }
       };
@@ -1594,12 +1882,16 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
       };
       const long long b0 = G & ~31LL;
       if (b0 < hi) {
-        Ld cur, nxt;
-        load(b0, cur);
-        for (long long b = b0; b < hi; b += 32) {
-          load(b + 32, nxt);  // in flight while this pass is finished
-          finish(b, cur);
-          cur = nxt;
+        Ld c0, c1, n0, n1;
+        load(b0, c0);
+        load(b0 + 32, c1);
+        for (long long b = b0; b < hi; b += 64) {
+          load(b + 64, n0);  // two passes' gathers in flight while two are finished
+          load(b + 96, n1);
+          finish(b, c0);
+          if (b + 32 < hi) finish(b + 32, c1);
+          c0 = n0;
+          c1 = n1;
         }
       }
       __syncwarp();
@@ -1878,9 +2170,16 @@ static void launch_modes(int mode, const PairArgs<TI>& a, int num_sms, cudaStrea
   switch (mode) {
     case kModeCount:
       if (a.sym) {  // symmetric pass; the per-cell pass below counts what it gave up (or left)
-        long long sb = ((long long)a.ncells_total + kSymWarps - 1) / kSymWarps;
-        if (sb > (long long)num_sms * pbps) sb = (long long)num_sms * pbps;
-        k_pairs_sym<TI, BATCH><<<int(sb), kSymWarps * 32, 0, st>>>(a);
+        if (BATCH) {
+          long long sb = ((long long)a.ncells_total + kSymWarps - 1) / kSymWarps;
+          if (sb > (long long)num_sms * pbps) sb = (long long)num_sms * pbps;
+          k_pairs_sym<TI, BATCH><<<int(sb), kSymWarps * 32, 0, st>>>(a);
+        } else {
+          const int sbps = a.pair_blocks_per_sm > 0 ? a.pair_blocks_per_sm : 2 * NL_SC_MIN_BLOCKS;
+          long long sb = ((long long)a.ncells_total + kSCWarps - 1) / kSCWarps;
+          if (sb > (long long)num_sms * sbps) sb = (long long)num_sms * sbps;
+          k_sym_count<TI><<<int(sb), kSCWarps * 32, 0, st>>>(a);
+        }
       }
       if (a.count_kernel != 2) {  // default: one warp per home cell
         k_pairs<TI, kModeCount, BATCH><<<int(blocks), kPairWarps * 32, 0, st>>>(a);

@@ -52,7 +52,7 @@ struct PairArgs {
   uint2* lists;             // per sorted slot: list_cap accepted (slot_j, candidate word)
   int* lcount;              // per sorted slot: pairs of the atom (count pass)
   int* sorig;               // per sorted slot: original atom index within the launch (0-based)
-  int* islot;               // per original atom of the launch: its sorted slot (symmetric count pass)
+  int2* hdr;                // per original atom: (sorted slot, home cell), written by the symmetric count pass
   int list_cap;             // kListCap, or 0: no lists (every cell takes the screening write pass)
   int* cap_rec;             // list_cap of the count pass (the write pass checks it)
   double* cs_table;         // C'S for |S_k| <= 2 (built once per call by k_cs_table)
