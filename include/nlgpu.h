@@ -155,6 +155,27 @@ int nl_lazy_reduce(const double* d_X_sorted, const void* d_perm, const void* d_c
                    const int64_t nxyz[3], const uint8_t pbc[3], double cutoff, int index_bytes, int reuse_records,
                    int op, void* d_out, void* d_workspace, size_t workspace_bytes, void* stream);
 
+/* Lazy per-atom traversal for a set of query atoms, without materialising
+ * the system's list.  Replaces neighbours(clist, i) and
+ * count_neighbours(clist, i) (cell_list.jl:808-833), i.e. for_each_neighbour
+ * (cell_list.jl:779-801) / _for_each_neighbor_pair (gpu_kernels.jl:58-101)
+ * for each atom of d_atoms[0 .. nq-1] (1-based original indices, TI).
+ * d_X is the cell list's X_orig, d_X_sorted / d_perm / d_cell_offsets its
+ * sorted arrays.  Count mode (d_j == NULL): d_counts[k] (int64) = the number
+ * of neighbours of atom d_atoms[k].  Fill mode: the neighbours of d_atoms[k]
+ * -- j (1-based), S (3 x TI) and, if d_R is not NULL, R (3 doubles) -- are
+ * written from pair d_offsets[k] (int64, 0-based) in the reference's
+ * traversal order; pairs at or beyond capacity are not written
+ * (NL_ERR_CAPACITY).  Every decision is the reference's FP64 arithmetic.
+ * The device-side error word is the first word of d_workspace (any
+ * workspace of at least 128 bytes; read it with nl_sync_status).
+ * Asynchronous. */
+int nl_query_neighbours(const double* d_X, const double* d_X_sorted, const void* d_perm, const void* d_cell_offsets,
+                        int64_t nat, const double cell[9], const double inv_cell[9], const int64_t ncells[3],
+                        const int64_t nxyz[3], const uint8_t pbc[3], double cutoff, int index_bytes,
+                        const void* d_atoms, int64_t nq, int64_t* d_counts, const int64_t* d_offsets, int64_t capacity,
+                        void* d_j, void* d_S, double* d_R, void* d_workspace, size_t workspace_bytes, void* stream);
+
 /* nl_neighbour_list without a workspace, for callers that cannot allocate
  * device memory (a framework pool owns the device, a real-time loop forbids
  * allocation after start-up, or the host code may not call cudaMalloc).  No

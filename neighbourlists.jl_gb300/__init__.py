@@ -26,6 +26,7 @@ from .api import (  # noqa: F401
     num_neighbours,
     pair_vectors,
     pairs,
+    query_neighbours,
     sites,
 )
 from .atoms import System, build_cell_list_system, isolated_cell, neighbour_list_system  # noqa: F401

@@ -40,6 +40,7 @@ EXPORTED = [
     "nl_static_sync_status",
     "nl_neighbour_list_half",
     "nl_lazy_reduce",
+    "nl_query_neighbours",
     "nl_pair_vectors",
     "nl_max_displacement_sq",
     "nl_batch_create",
@@ -152,6 +153,9 @@ def _declare(L):
     L.nl_lazy_reduce.argtypes = [_vp, _vp, _vp, _vp, C.c_int64, _D, _D, _I64, _I64, _U8, C.c_double, C.c_int, C.c_int,
                                  C.c_int, _vp, _vp, C.c_size_t, _vp]
     L.nl_lazy_reduce.restype = C.c_int
+    L.nl_query_neighbours.argtypes = [_vp, _vp, _vp, _vp, C.c_int64, _D, _D, _I64, _I64, _U8, C.c_double, C.c_int, _vp,
+                                      C.c_int64, _vp, _vp, C.c_int64, _vp, _vp, _vp, _vp, C.c_size_t, _vp]
+    L.nl_query_neighbours.restype = C.c_int
     L.nl_batch_create.argtypes = [C.POINTER(System), C.c_int, C.c_int, C.POINTER(_vp)]
     L.nl_batch_create.restype = C.c_int
     L.nl_batch_create_auto.argtypes = [_vp, _vp, _vp, _vp, C.c_int, C.c_int, C.POINTER(_vp)]

@@ -36,7 +36,7 @@ __all__ = [
     "SortedCellList", "PairList", "NLError", "analyze_cell", "build_cell_list", "materialize_pairlist",
     "neighbour_list", "npairs", "nsites", "nneigs", "maxneigs", "max_neighbours", "neigs", "neigss", "neighbours",
     "num_neighbours", "count_neighbours", "for_each_neighbour", "lazy_reduce", "cutoff", "pairs", "sites",
-    "PairIterator", "SiteIterator", "pair_vectors", "legacy_pairlist",
+    "PairIterator", "SiteIterator", "pair_vectors", "legacy_pairlist", "query_neighbours",
 ]
 
 _D = C.POINTER(C.c_double)
@@ -531,18 +531,78 @@ def _getR(nlist: PairList, a: int, b: int) -> torch.Tensor:
     return pair_vectors(X, nlist.C, nlist.i[a:b], nlist.j[a:b], nlist.S[a:b].contiguous())
 
 
+def query_neighbours(clist: SortedCellList, atoms, with_R: bool = True, stream=None):
+    """Neighbours of a set of atoms (1-based original indices) by the lazy
+    traversal on the device (nl_query_neighbours: for_each_neighbour,
+    cell_list.jl:779-833, per atom), without materialising the system's list.
+    Returns (first, j, S, R): first[k] .. first[k+1]-1 (1-based, int64) are the
+    pairs of atoms[k], in the reference's traversal order."""
+    if _is_f32(clist):
+        raise TypeError("the per-atom lazy traversal takes a Float64 cell list")
+    dev = clist.X.device
+    ti = clist.perm.dtype
+    at = torch.as_tensor(np.asarray(atoms, dtype=np.int64).reshape(-1), device=dev).to(ti).contiguous()
+    nq = int(at.numel())
+    ws = _query_workspace(clist)
+    pb = _pbc(clist.pbc)
+    cm, im, nc, nx = _plan_args(clist)
+    sh = _stream_handle(stream)
+    nat = int(clist.X.shape[0])
+    counts = torch.zeros(nq, dtype=torch.int64, device=dev)
+
+    def call(offsets, cap, j, S, R, cnt):
+        return lib().nl_query_neighbours(
+            _ptr(clist.X_orig), _ptr(clist.X), _ptr(clist.perm), C.c_void_p(clist.cell_offsets.data_ptr()), nat, cm,
+            im, nc, nx, pb.ctypes.data_as(_U8), clist.cutoff, clist.index_bytes, _ptr(at), nq, _ptr(cnt),
+            _ptr(offsets), int(cap), _ptr(j), _ptr(S), _ptr(R), _ptr(ws), ws.numel(), sh)
+
+    with torch.cuda.device(dev):
+        check(call(None, 0, None, None, None, counts))
+        check(lib().nl_sync_status(_ptr(ws), sh))
+        first = torch.zeros(nq + 1, dtype=torch.int64, device=dev)
+        torch.cumsum(counts, 0, out=first[1:])
+        P = int(first[-1].item())
+        j = torch.empty(P, dtype=ti, device=dev)
+        S = torch.empty((P, 3), dtype=ti, device=dev)
+        R = torch.empty((P, 3), dtype=torch.float64, device=dev) if with_R else None
+        if P:
+            check(call(first, P, j, S, R, None))
+            check(lib().nl_sync_status(_ptr(ws), sh))
+    return first + 1, j, S, R
+
+
+def _query_workspace(clist: SortedCellList) -> torch.Tensor:
+    """The error word of the per-atom traversal: the cell list's workspace
+    when it has one (the traversal touches only its first word), else a small
+    buffer of its own."""
+    if clist._ws is not None:
+        return clist._ws
+    w = getattr(clist, "_qws", None)
+    if w is None:
+        w = torch.zeros(128, dtype=torch.uint8, device=clist.X.device)
+        object.__setattr__(clist, "_qws", w)
+    return w
+
+
 def count_neighbours(clist: SortedCellList, i: int) -> int:
-    """count_neighbours(clist, i) (cell_list.jl:808-814), i 1-based."""
-    return int(lazy_reduce(clist, "count")[i - 1].item())
+    """count_neighbours(clist, i) (cell_list.jl:808-814), i 1-based: the lazy
+    traversal of atom i alone on the device."""
+    if _is_f32(clist):
+        return int(lazy_reduce(clist, "count")[i - 1].item())
+    first, _, _, _ = query_neighbours(clist, [i], with_R=False)
+    return int(first[1].item() - first[0].item())
 
 
 def neighbours(x, i: int):
     """neighbours(nlist, i) = neigss; neighbours(clist, i) -> (js, Rs, Ss)
-    (cell_list.jl:606, 821-833)."""
+    (cell_list.jl:606, 821-833): for a SortedCellList, the lazy traversal of
+    atom i alone on the device, in the reference's order."""
     if isinstance(x, PairList):
         return neigss(x, i)
-    nl = _lazy_pairlist(x)
-    return neigss(nl, i)
+    if _is_f32(x):
+        return neigss(_lazy_pairlist(x), i)
+    _, j, S, R = query_neighbours(x, [i])
+    return j, R, S
 
 
 def _lazy_pairlist(clist: SortedCellList) -> PairList:

@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libnlgpu.so")
-SOURCES = ["nl_build.cu", "nl_pairs.cu", "nl_api.cu", "nl_static.cu", "nl_legacy.cu", "nl_f32.cu"]
+SOURCES = ["nl_build.cu", "nl_pairs.cu", "nl_api.cu", "nl_static.cu", "nl_legacy.cu", "nl_f32.cu", "nl_query.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

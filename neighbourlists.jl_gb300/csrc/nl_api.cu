@@ -185,7 +185,7 @@ struct Layout {
   // [err 64 | stats 64] [pairs zero region: counters 64 | st_pairs | cell_flag]
   // [build zero region: counters 64 | st_cells | cell_count] [arrays...]
   size_t err, stats, pcount, st_pairs, cell_flag, pend, bcount, st_cells, cell_count, bend;
-  size_t totals, cell_start, cid, ticket, rec, tmp, rec_sorted, scell, counts, lcount, sorig, hdr, cs_table,
+  size_t totals, cell_start, cid, ticket, rec, tmp, rec_sorted, scell, counts, lcount, sorig, hdr, xpk, cs_table,
       screen_cells,
       big_list, base_end, lists, end;
   bool use_lists = true;  // the workspace holds the pair lists (it reaches `end`)
@@ -236,6 +236,8 @@ Layout layout(int64_t nat, int64_t ncells) {
   o += up(sizeof(int) * n);
   L.hdr = o;
   o += up(sizeof(int2) * n);
+  L.xpk = o;
+  o += up(sizeof(nl::XPack) * n);
   L.cs_table = o;
   o += up(sizeof(double) * 3 * 125);
   L.screen_cells = o;
@@ -346,6 +348,7 @@ int status_from_flags(unsigned f) {
   if (f & nl::kFlagInconsistent) return fail(NL_ERR_INCONSISTENT, "cell list ids do not match its positions");
   if (f & nl::kFlagTimeout) return fail(NL_ERR_TIMEOUT, "a bounded device-side wait timed out");
   if (f & nl::kFlagIndexOverflow) return fail(NL_ERR_INDEX_OVERFLOW, "pair count does not fit the index type");
+  if (f & nl::kFlagBadIndex) return fail(NL_ERR_ARG, "an atom index given to the call is out of range");
   if (f & nl::kFlagCapacity) return fail(NL_ERR_CAPACITY, "pair buffers are smaller than the pair count");
   return NL_OK;
 }
@@ -415,6 +418,7 @@ nl::PairArgs<TI> pair_args(const nl::Geometry& g, const TI* cell_offsets, const 
   a.lcount = at<int>(ws, L.lcount);
   a.sorig = at<int>(ws, L.sorig);
   a.hdr = at<int2>(ws, L.hdr);
+  a.xpk = at<nl::XPack>(ws, L.xpk);
   a.cap_rec = at<int>(ws, L.pcount) + 2;  // the count pass's list_cap, checked by the write pass
   a.cs_table = at<double>(ws, L.cs_table);
   a.screen_cells = at<int>(ws, L.screen_cells);
@@ -918,6 +922,10 @@ int status_from_device_flags(unsigned flags) { return status_from_flags(flags); 
 size_t workspace_min_bytes(int64_t nat, int64_t ncells_total) {
   if (nat < 0 || ncells_total < 1) return 0;
   return layout(nat, ncells_total).base_end;
+}
+Geometry geometry_for(const double* cell, const double* inv, const int64_t* ns, const int64_t* nxyz,
+                      const uint8_t* pbc, double cutoff, int64_t nat) {
+  return make_geometry(cell, inv, ns, nxyz, pbc, cutoff, nat);
 }
 size_t workspace_total_offset(int64_t nat, int64_t ncells_total) {
   return layout(nat, ncells_total).totals + sizeof(long long);

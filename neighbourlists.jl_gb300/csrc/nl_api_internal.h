@@ -4,6 +4,8 @@
 #include <cstdint>
 #include <string>
 
+#include "nl_common.cuh"
+
 namespace nl {
 // Records msg as the calling thread's nl_last_error() text and returns status.
 int report(int status, const std::string& msg);
@@ -17,4 +19,8 @@ size_t workspace_min_bytes(int64_t nat, int64_t ncells_total);
 // (the last entry of its scan), for a system of nat atoms and ncells_total
 // cells; the error word sits at offset 0.
 size_t workspace_total_offset(int64_t nat, int64_t ncells_total);
+// The kernels' view of one system (cell, inverse, grid, stencil, FP32 screen
+// band, binning constants); nxyz may be null where no stencil is needed.
+Geometry geometry_for(const double* cell, const double* inv, const int64_t* ns, const int64_t* nxyz,
+                      const uint8_t* pbc, double cutoff, int64_t nat);
 }  // namespace nl

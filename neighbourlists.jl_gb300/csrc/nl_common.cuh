@@ -32,6 +32,7 @@ enum : unsigned {
   kFlagCapacity = 4u,
   kFlagInconsistent = 8u,
   kFlagIndexOverflow = 16u,
+  kFlagBadIndex = 32u,  // an atom index given to the call is out of range
 };
 
 // ---------------------------------------------------------------- geometry --

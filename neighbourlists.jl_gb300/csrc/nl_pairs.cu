@@ -1187,6 +1187,18 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
           const int o = clampi(A.perm[hs + lane] - 1, nat - 1);
           W.horig[lane] = o;
           A.hdr[o] = make_int2(hs + lane, h);  // the write pass walks atoms in original order
+          const double X0 = A.Xs[3LL * (hs + lane) + 0], X1 = A.Xs[3LL * (hs + lane) + 1],
+                       X2 = A.Xs[3LL * (hs + lane) + 2];
+          XPack xp;
+          xp.x = X0;
+          xp.y = X1;
+          xp.z = X2;
+          xp.perm = o + 1;
+          xp.meta = hm;
+          A.xpk[hs + lane] = xp;
+          const long long nz = (long long)0x8000000000000000ULL;
+          if (__double_as_longlong(X0) == nz || __double_as_longlong(X1) == nz || __double_as_longlong(X2) == nz)
+            atomicOr(A.sym_wound, 2);
         }
         W.hx[lane] = x;
         W.hy[lane] = y;
@@ -1619,65 +1631,57 @@ __global__ void __launch_bounds__(kEmitWarps * 32,
 // its stores cover whole lines, and only the run's two ends share a sector
 // with another warp's atoms.  (Walking atoms in cell order instead scatters
 // ~26-pair runs over the arrays; the partial sectors at both ends of every
-// run cost extra DRAM traffic.)  The price is that the neighbours' positions
-// are gathered from anywhere in the sorted arrays (L2, not L1), so the
-// kernel keeps many loads in flight:
+// run cost extra DRAM traffic.)  The neighbours' data are gathered from
+// anywhere in the sorted arrays, so they come from L2: one 32-byte row per
+// neighbour (XPack: position, perm, meta, written by the count pass).
 //
 // Per batch of 32 atoms, lane a holds atom o0 + a: its header (sorted slot,
 // home cell) and output range, then -- loads issued together -- its 27 mask
 // words (16-byte vector loads), position, record meta and the sorted start of
-// each of its 27 stencil cells (from cell_offsets; the wrapped cell and loop
-// shift per axis follow from the home cell).  Lane a expands its own masks,
-// in stencil order (dz, dy, dx) and sorted order within each stencil cell --
-// the reference's traversal order -- into a shared-memory table of (slot of
-// j, loop-shift base, atom) entries at the pairs' output positions.  The
-// table holds kEOEnt entries; a batch with more pairs is cut at atom
-// boundaries (an atom has at most 27 * 32 pairs on this path).  The warp then
-// walks the output positions 32 at a time, passes aligned to multiples of 32
-// in the output arrays, lane r writing pair base + r: j, S from the packed
-// fields (windings and exact atoms as everywhere) and R = (xj - xi) + C'S
-// with the reference's operations.  i and j are stored per lane; S and R are
-// staged in shared memory and stored as 16-byte vectors (scalar stores for
-// the vectors that straddle the run's ends, or when the arrays are not
-// 16-byte aligned).  The gathers of the next two passes are in flight while
-// two passes are finished.
+// each of its 27 stencil cells (cell_offsets; the wrapped cell and loop shift
+// per axis follow from the home cell).  Lane a expands its own masks, in
+// stencil order (dz, dy, dx) and sorted order within each stencil cell -- the
+// reference's traversal order -- into a shared-memory table of 8-byte
+// entries (slot of j; atom and the three loop shifts) at the pairs' output
+// positions.  The table holds kEOEnt entries; a batch with more pairs is cut
+// at atom boundaries (an atom has at most 27 * 32 - 1 pairs on this path).
+// The warp then walks the output positions 32 at a time, passes aligned to
+// multiples of 32 in the output arrays, lane r writing pair base + r: i, j,
+// S (the loop shifts, or with windings s_loop + wi - wj) and
+// R = (xj - xi) + C'S with the reference's operations.  i and j are stored
+// per lane; S and R are staged in shared memory and stored as 16-byte
+// vectors (a chunk's first and last passes, and arrays that are not 16-byte
+// aligned, store word by word).  The gathers of the next two passes are in
+// flight while two passes are finished.
 #ifndef NL_EO_MIN_BLOCKS
-#define NL_EO_MIN_BLOCKS 6  // resident blocks per SM the register budget targets (168 registers, no spills)
+#define NL_EO_MIN_BLOCKS 8  // resident blocks per SM the register budget targets
 #endif
 constexpr int kEOWarps = 2;
 constexpr int kEOEnt = 1024;  // pair entries per warp
-static_assert(kEOEnt >= 27 * 32, "an atom of the symmetric pass has at most 27 * 32 pairs");
+static_assert(kEOEnt >= 27 * 32, "an atom of the symmetric pass has fewer than 27 * 32 pairs");
 
 template <typename TI>
 struct __align__(16) EOSmem {
-  double rbuf[96];            // R of one pass, three words per pair
-  TI sbuf[96];                // S of one pass
-  unsigned eslot[kEOEnt];     // entry: sorted slot of j
-  unsigned short einfo[kEOEnt];  // entry: atom of the batch | loop shifts of j's stencil cell (2 bits per axis)
-  unsigned st[32][27];        // the batch's atoms: sorted start of each stencil cell
-  double xi[32][3];           //   FP64 position
-  long long ti[32];           //   output value of i (1-based)
-  unsigned mi[32];            //   record meta (windings, exact bit)
+  double rbuf[96];      // R of one pass, three words per pair
+  TI sbuf[96];          // S of one pass
+  uint2 ent[kEOEnt];    // entry: (sorted slot of j, atom | loop shift + 1 per axis << 5 + 2k)
+  double xi[32][3];     // the batch's atoms: FP64 position
+  unsigned mi[32];      //   record meta (windings, exact bit)
 };
 
-// Stores the pass's staged words [lo, hi) of one output array (96 words per
-// pass at dst = the pass's first word) with 16-byte vectors where a whole
-// vector lies inside [lo, hi), else word by word.
+// One pass's staged S and R words [lo, hi) (96 per pass; dst = the pass's
+// first word): whole 16-byte vectors where vec, else word by word.
 template <typename T>
 __device__ __forceinline__ void store_staged(T* __restrict__ dst, const T* __restrict__ buf, int lo, int hi, bool vec,
                                              int lane) {
   constexpr int V = 16 / int(sizeof(T));
-  if (vec) {
+  if (vec) {  // the whole pass: 96 / V vectors
+#pragma unroll
     for (int v = lane; v < 96 / V; v += 32) {
-      const int e0 = v * V;
-      if (e0 >= lo && e0 + V <= hi) {
-        if constexpr (sizeof(T) == 4) {
-          __stcs(reinterpret_cast<int4*>(dst + e0), *reinterpret_cast<const int4*>(buf + e0));
-        } else {
-          __stcs(reinterpret_cast<longlong2*>(dst + e0), *reinterpret_cast<const longlong2*>(buf + e0));
-        }
+      if constexpr (sizeof(T) == 4) {
+        __stcs(reinterpret_cast<int4*>(dst) + v, reinterpret_cast<const int4*>(buf)[v]);
       } else {
-        for (int e = max(e0, lo); e < min(e0 + V, hi); ++e) __stcs(dst + e, buf[e]);
+        __stcs(reinterpret_cast<longlong2*>(dst) + v, reinterpret_cast<const longlong2*>(buf)[v]);
       }
     }
   } else {
@@ -1729,10 +1733,13 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   EOSmem<TI>& E = sm[warp];
   const int nat = g.nat;
-  const bool plain = *A.sym_wound == 0;  // no atom has a winding or is exact
-  const bool vec = A.vec_ok != 0;
+  const int sw = *A.sym_wound;
+  const bool plain = (sw & 1) == 0;   // no atom has a winding or is exact: S = the loop shift
+  const bool negzero = (sw & 2) != 0;  // a coordinate is -0: R needs the signed-zero rule for S = 0
+  const bool vec_ok = A.vec_ok != 0;
   const unsigned* masks = reinterpret_cast<const unsigned*>(A.lists);
   const long long cap = A.capacity;
+  const double* zc = cs_blk + 3 * ((kCsN * kCsN + kCsN + 1) * kCsR);  // C'(0,0,0): signed zeros
   unsigned bad = 0;  // error flags of this lane
   const long long nwarps = (long long)gridDim.x * kEOWarps;
   for (long long o0 = ((long long)blockIdx.x * kEOWarps + warp) * 32; o0 < nat; o0 += nwarps * 32) {
@@ -1748,44 +1755,9 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
       n = (long long)A.first[o + 1] - 1 - f;
     }
     const int slot = clampi(hd.x, nat - 1), hc = clampi(hd.y, g.ncells - 1);
-    int wx[3], wy[3], wz[3], sx[3], sy[3], sz[3];
-    bool okx[3], oky[3], okz[3];
-    axis3(hc % g.ns[0] + 1, g.ns[0], g.pbc[0], wx, sx, okx);
-    axis3((hc / g.ns[0]) % g.ns[1] + 1, g.ns[1], g.pbc[1], wy, sy, oky);
-    axis3(hc / (g.ns[0] * g.ns[1]) + 1, g.ns[2], g.pbc[2], wz, sz, okz);
-    // ... then masks, position, meta and the 27 stencil cell starts, all in flight together
-    uint4 mv[7];
-    const uint4* mrow = reinterpret_cast<const uint4*>(masks + kMaskStride * slot);
-#pragma unroll
-    for (int k = 0; k < 7; ++k) mv[k] = own ? __ldg(mrow + k) : make_uint4(0u, 0u, 0u, 0u);
-    {
-      TI st[27];
-#pragma unroll
-      for (int q = 0; q < 27; ++q) {
-        const int dx = q % 3, dy = (q / 3) % 3, dz = q / 9;
-        const int lin = wx[dx] + g.ns[0] * (wy[dy] + g.ns[1] * wz[dz]);
-        st[q] = own && okx[dx] && oky[dy] && okz[dz] ? A.cell_offsets[lin] : TI(1);
-      }
-#pragma unroll
-      for (int q = 0; q < 27; ++q) E.st[lane][q] = unsigned(clampi(st[q] - 1, nat));
-    }
-    if (own) {
-      E.xi[lane][0] = A.Xs[3LL * slot + 0];
-      E.xi[lane][1] = A.Xs[3LL * slot + 1];
-      E.xi[lane][2] = A.Xs[3LL * slot + 2];
-      E.mi[lane] = __float_as_uint(A.rec[slot].w);
-      E.ti[lane] = o0 + lane + 1;
-    }
-    unsigned m[27];
-#pragma unroll
-    for (int k = 0; k < 7; ++k) {
-      m[4 * k] = mv[k].x;
-      if (4 * k + 1 < 27) m[4 * k + 1] = mv[k].y;
-      if (4 * k + 2 < 27) m[4 * k + 2] = mv[k].z;
-      if (4 * k + 3 < 27) m[4 * k + 3] = mv[k].w;
-    }
-    __syncwarp();
-    // ---- chunks of at most kEOEnt pairs, cut at atom boundaries
+    // ---- chunks of at most kEOEnt pairs, cut at atom boundaries; each chunk
+    // loads, expands and writes its own atoms, so that the masks and cell
+    // starts held for the expansion are dead while the chunk is written
     int l0 = 0;
     while (l0 < na) {
       const long long G = __shfl_sync(0xffffffffu, f, l0);
@@ -1795,101 +1767,169 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
         bad |= kFlagInconsistent;
         break;
       }
-      const long long Gend = __shfl_sync(0xffffffffu, f + n, l1 - 1);
-      // ---- expansion: lane a writes its entries at [f - G, f - G + n)
-      if (lane >= l0 && lane < l1) {
-        int e = int(f - G);
-        const int eend = e + int(n);
+      const int cnt = int(__shfl_sync(0xffffffffu, f + n, l1 - 1) - G);
+      const bool mine = lane >= l0 && lane < l1;
+      {
+        int wx[3], wy[3], wz[3], sx[3], sy[3], sz[3];
+        bool okx[3], oky[3], okz[3];
+        axis3(hc % g.ns[0] + 1, g.ns[0], g.pbc[0], wx, sx, okx);
+        axis3((hc / g.ns[0]) % g.ns[1] + 1, g.ns[1], g.pbc[1], wy, sy, oky);
+        axis3(hc / (g.ns[0] * g.ns[1]) + 1, g.ns[2], g.pbc[2], wz, sz, okz);
+        // masks, position, meta and the 27 stencil cell starts, all in flight together
+        uint4 mv[7];
+        const uint4* mrow = reinterpret_cast<const uint4*>(masks + kMaskStride * slot);
 #pragma unroll
-        for (int q = 0; q < 27; ++q) {
-          unsigned mq = m[q];
-          if (mq) {
-            const int dx = q % 3, dy = (q / 3) % 3, dz = q / 9;
-            if (!(okx[dx] && oky[dy] && okz[dz])) {  // a neighbour in a cell outside an open axis
-              bad |= kFlagInconsistent;
-              mq = 0u;
-            }
-            const unsigned info = unsigned(lane) | unsigned(sx[dx] + 1) << 5 | unsigned(sy[dy] + 1) << 7 |
-                                  unsigned(sz[dz] + 1) << 9;
-            const unsigned start = E.st[lane][q];
-            while (mq) {
-              const int b = __ffs(mq) - 1;
-              mq &= mq - 1u;
-              if (e >= 0 && e < eend && e < kEOEnt) {  // (bounds hold for consistent counts)
-                E.eslot[e] = start + unsigned(b);
-                E.einfo[e] = (unsigned short)info;
+        for (int k = 0; k < 7; ++k) mv[k] = mine ? __ldg(mrow + k) : make_uint4(0u, 0u, 0u, 0u);
+        unsigned st[27];
+#pragma unroll
+        for (int r = 0; r < 9; ++r) {
+          const int dy = r % 3, dz = r / 3;
+          const int rb = g.ns[0] * (wy[dy] + g.ns[1] * wz[dz]);
+          const bool rok = mine && oky[dy] && okz[dz];
+#pragma unroll
+          for (int dx = 0; dx < 3; ++dx)
+            st[3 * r + dx] = unsigned(clampi((rok && okx[dx] ? A.cell_offsets[rb + wx[dx]] : TI(1)) - 1, nat));
+        }
+        if (mine) {
+          E.xi[lane][0] = A.Xs[3LL * slot + 0];
+          E.xi[lane][1] = A.Xs[3LL * slot + 1];
+          E.xi[lane][2] = A.Xs[3LL * slot + 2];
+          E.mi[lane] = __float_as_uint(A.rec[slot].w);
+        }
+        // ---- expansion: lane a writes its entries at [f - G, f - G + n)
+        if (mine) {
+          int e = int(f - G);
+          const int eend = e + int(n);
+#pragma unroll
+          for (int q = 0; q < 27; ++q) {
+            unsigned mq = (&mv[q >> 2].x)[q & 3];
+            if (mq) {
+              const int dx = q % 3, dy = (q / 3) % 3, dz = q / 9;
+              if (!(okx[dx] && oky[dy] && okz[dz])) {  // a neighbour in a cell outside an open axis
+                bad |= kFlagInconsistent;
+                mq = 0u;
               }
-              ++e;
+              const unsigned info = unsigned(lane) | unsigned(sx[dx] + 1) << 5 | unsigned(sy[dy] + 1) << 7 |
+                                    unsigned(sz[dz] + 1) << 9;
+              while (mq) {
+                const int b = __ffs(mq) - 1;
+                mq &= mq - 1u;
+                if (e >= 0 && e < eend && e < kEOEnt) E.ent[e] = make_uint2(st[q] + unsigned(b), info);
+                ++e;
+              }
             }
           }
+          if (e != eend) bad |= kFlagInconsistent;  // counts and masks disagree
         }
-        if (e != eend) bad |= kFlagInconsistent;  // counts and masks disagree
       }
       __syncwarp();
-      // ---- emission, passes aligned to 32 output positions
-      const long long hi = min(Gend, cap);
-      if (Gend > cap && lane == l0) bad |= kFlagCapacity;
+      // ---- emission: pass j covers output positions G - off + 32 j + lane
+      const int off = int(G & 31);
+      const int lim = int(max(min((long long)cnt, cap - G), 0LL));  // entries that fit the buffers
+      if ((long long)cnt > cap - G && lane == l0) bad |= kFlagCapacity;
+      const int npass = (lim + off + 31) >> 5;
+      const long long p0 = G - off;  // first output position of pass 0 (a multiple of 32)
+      const long long ti0 = o0 + 1;  // i of atom a is ti0 + a
       struct Ld {
         double x0, x1, x2;
-        int oj;  // perm value (<= 2^31 - 2)
-        unsigned mj, slp;
-        int a;
+        int pj;
+        unsigned mj, info;
         bool act;
       };
-      auto load = [&](long long b, Ld& u) {
-        const long long p = b + lane;
-        u.act = p >= G && p < hi && p - G < kEOEnt;
-        u.a = 0;
-        u.slp = 0;
-        u.mj = kPlainMeta;
+      auto load = [&](int j, Ld& u) {
+        const int k = 32 * j - off + lane;
+        u.act = k >= 0 && k < lim;
+        u.info = 0u;
         u.x0 = u.x1 = u.x2 = 0.0;
-        u.oj = 0;
+        u.pj = 0;
+        u.mj = kPlainMeta;
         if (u.act) {
-          const int k = int(p - G);
-          const int sj = clampi(int(E.eslot[k]), nat - 1);
-          const unsigned info = E.einfo[k];
-          u.slp = cand_base(int((info >> 5) & 3u) - 1, int((info >> 7) & 3u) - 1, int((info >> 9) & 3u) - 1);
-          u.a = int(info & 31u);
-          u.x0 = __ldg(A.Xs + 3LL * sj + 0);
-          u.x1 = __ldg(A.Xs + 3LL * sj + 1);
-          u.x2 = __ldg(A.Xs + 3LL * sj + 2);
-          u.oj = int(__ldg(A.perm + sj));
-          if (!plain) u.mj = __float_as_uint(__ldg(&A.rec[sj].w));
+          const uint2 en = E.ent[k];
+          u.info = en.y;
+          const XPack* xp = A.xpk + clampi(int(en.x), nat - 1);
+          const double2 v0 = __ldg(reinterpret_cast<const double2*>(xp));
+          const int4 v1 = __ldg(reinterpret_cast<const int4*>(xp) + 1);
+          u.x0 = v0.x;
+          u.x1 = v0.y;
+          u.x2 = __hiloint2double(v1.y, v1.x);
+          u.pj = v1.z;
+          u.mj = unsigned(v1.w);
         }
       };
-      auto finish = [&](long long b, const Ld& u) {
-        const double* xi = E.xi[u.a];
-        const double xj[3] = {u.x0, u.x1, u.x2};
+      auto finish = [&](int j, const Ld& u) {
+        const int a = int(u.info & 31u);
+        const double* xi = E.xi[a];
         int S[3];
-        pair_S(g, xi, xj, E.mi[u.a], cand_word(u.slp, u.mj), S);
-        double R[3] = {0.0, 0.0, 0.0};
-        if (A.oR) pair_R(g, cs_blk, xi, xj, S[0], S[1], S[2], u.act, R);
-        const long long p = b + lane;
-        if (u.act) {
-          __stcs(A.oi + p, TI(E.ti[u.a]));
-          __stcs(A.oj + p, TI(u.oj));
+        if (plain) {
+          S[0] = int((u.info >> 5) & 3u) - 1;
+          S[1] = int((u.info >> 7) & 3u) - 1;
+          S[2] = int((u.info >> 9) & 3u) - 1;
+        } else {
+          const double xj[3] = {u.x0, u.x1, u.x2};
+          const unsigned slp = cand_base(int((u.info >> 5) & 3u) - 1, int((u.info >> 7) & 3u) - 1,
+                                         int((u.info >> 9) & 3u) - 1);
+          pair_S(g, xi, xj, E.mi[a], cand_word(slp, u.mj), S);
         }
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          E.sbuf[3 * lane + k] = TI(S[k]);
-          E.rbuf[3 * lane + k] = R[k];
+        double R0 = 0.0, R1 = 0.0, R2 = 0.0;
+        if (A.oR) {
+          R0 = dsub(u.x0, xi[0]);
+          R1 = dsub(u.x1, xi[1]);
+          R2 = dsub(u.x2, xi[2]);
+          const bool nz = u.act && (S[0] | S[1] | S[2]) != 0;
+          if (__any_sync(0xffffffffu, nz)) {
+            if (nz) {
+              double c0, c1, c2;
+              if (abs(S[0]) <= kCsR && abs(S[1]) <= kCsR && abs(S[2]) <= kCsR) {
+                const double* t = cs_blk + 3 * ((S[0] + kCsR) + kCsN * ((S[1] + kCsR) + kCsN * (S[2] + kCsR)));
+                c0 = t[0];
+                c1 = t[1];
+                c2 = t[2];
+              } else {
+                c0 = cts_k(g.C, S[0], S[1], S[2], 0);
+                c1 = cts_k(g.C, S[0], S[1], S[2], 1);
+                c2 = cts_k(g.C, S[0], S[1], S[2], 2);
+              }
+              R0 = dadd(R0, c0);
+              R1 = dadd(R1, c1);
+              R2 = dadd(R2, c2);
+            }
+          }
+          if (negzero && !nz) {  // a -0 coordinate: RN(d + C'(0,0,0)) differs from d when d is -0
+            R0 = add_signed_zero(R0, zc[0]);
+            R1 = add_signed_zero(R1, zc[1]);
+            R2 = add_signed_zero(R2, zc[2]);
+          }
+        }
+        const long long pb = p0 + 32LL * j;  // this pass's first output position
+        if (u.act) {
+          __stcs(A.oi + pb + lane, TI(ti0 + a));
+          __stcs(A.oj + pb + lane, TI(u.pj));
+        }
+        E.sbuf[3 * lane + 0] = TI(S[0]);
+        E.sbuf[3 * lane + 1] = TI(S[1]);
+        E.sbuf[3 * lane + 2] = TI(S[2]);
+        if (A.oR) {
+          E.rbuf[3 * lane + 0] = R0;
+          E.rbuf[3 * lane + 1] = R1;
+          E.rbuf[3 * lane + 2] = R2;
         }
         __syncwarp();
-        const int lo = 3 * int(max(G - b, 0LL)), hw = 3 * int(min(hi - b, 32LL));
-        store_staged<TI>(A.oS + 3 * b, E.sbuf, lo, hw, vec, lane);
-        if (A.oR) store_staged<double>(A.oR + 3 * b, E.rbuf, lo, hw, vec, lane);
+        const int k0 = 32 * j - off;  // entry of lane 0
+        const bool full = vec_ok && k0 >= 0 && k0 + 32 <= lim;
+        const int lo = 3 * max(-k0, 0), hw = 3 * min(lim - k0, 32);
+        store_staged<TI>(A.oS + 3 * pb, E.sbuf, lo, hw, full, lane);
+        if (A.oR) store_staged<double>(A.oR + 3 * pb, E.rbuf, lo, hw, full, lane);
         __syncwarp();
       };
-      const long long b0 = G & ~31LL;
-      if (b0 < hi) {
+      if (npass > 0) {
         Ld c0, c1, n0, n1;
-        load(b0, c0);
-        load(b0 + 32, c1);
-        for (long long b = b0; b < hi; b += 64) {
-          load(b + 64, n0);  // two passes' gathers in flight while two are finished
-          load(b + 96, n1);
-          finish(b, c0);
-          if (b + 32 < hi) finish(b + 32, c1);
+        load(0, c0);
+        load(1, c1);
+        for (int j = 0; j < npass; j += 2) {
+          load(j + 2, n0);  // two passes' gathers in flight while two are finished
+          load(j + 3, n1);
+          finish(j, c0);
+          if (j + 1 < npass) finish(j + 1, c1);
           c0 = n0;
           c1 = n1;
         }

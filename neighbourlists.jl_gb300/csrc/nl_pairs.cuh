@@ -25,6 +25,16 @@ constexpr int kCsTableDoubles = 3 * 125;
 // the reference's per-system arrays placed one after another: perm and
 // cell_id hold system-local 1-based values, and its cell_offsets (ncells+1
 // entries) start at sys_cell[s] + s.
+// Per sorted slot, what the original-order write pass gathers for a
+// neighbour: its FP64 position, 1-based original index (perm) and record
+// meta (windings, exact bit), in one 32-byte row (two 16-byte loads).
+struct __align__(16) XPack {
+  double x, y, z;
+  int perm;
+  unsigned meta;
+};
+static_assert(sizeof(XPack) == 32, "one 32-byte row per slot");
+
 template <typename TI>
 struct PairArgs {
   Geometry g;               // single system (nsys == 0)
@@ -53,6 +63,7 @@ struct PairArgs {
   int* lcount;              // per sorted slot: pairs of the atom (count pass)
   int* sorig;               // per sorted slot: original atom index within the launch (0-based)
   int2* hdr;                // per original atom: (sorted slot, home cell), written by the symmetric count pass
+  XPack* xpk;               // per sorted slot: gather row of the original-order write pass (symmetric count pass)
   int list_cap;             // kListCap, or 0: no lists (every cell takes the screening write pass)
   int* cap_rec;             // list_cap of the count pass (the write pass checks it)
   double* cs_table;         // C'S for |S_k| <= 2 (built once per call by k_cs_table)
@@ -62,7 +73,8 @@ struct PairArgs {
   int count_kernel;         // 1: one warp per home cell, 2: one thread per home atom (0 / 3: see sym)
   int sym;                  // count / write: each unordered cell pair screened once, neighbour masks
   int* sym_fail;            // set when a cell has more than 32 atoms: lists and the per-cell pass instead
-  int* sym_wound;           // set when an atom has a winding or is exact (candidate words need its record)
+  int* sym_wound;           // bit 0: an atom has a winding or is exact (candidate words need its record);
+                            // bit 1: a coordinate is -0 (R needs the signed-zero rule of C'S with S = 0)
   const int* sys_sym;       // batch: 1 for the systems the symmetric pass takes (27 distinct stencil cells)
   int* sys_fail;            // batch: per system, like sym_fail (zeroed per call)
   int half;                 // count / write: keep each unordered pair once (j > i, or j == i and S > 0)

@@ -1,0 +1,76 @@
+"""The lazy per-atom traversal on the device (nl_query_neighbours):
+neighbours(clist, i), count_neighbours(clist, i) and for_each_neighbour
+(cell_list.jl:779-833) for single atoms and for sets of atoms, against the
+oracle's traversal of the same cell list -- j, S and the bits of R in the
+reference's order -- without the system's list being materialised.  Cases:
+cubic, triclinic, mixed and open boundaries, a one-cell system whose
+stencil reaches several periodic images (diamond primitive, rc 6), atoms
+far outside an open axis, Int64, and an out-of-range atom index."""
+import numpy as np
+import pytest
+import torch
+
+import configs as cf
+
+pytestmark = pytest.mark.gpu
+
+
+def _cases():
+    Xd, Cd = cf.diamond_primitive()
+    Xf, Cf, pf = cf.fcc_sheared(n=5, seed=11)
+    X, C, L = cf.rand_config(3000, seed=12)
+    Xo = X.copy()
+    Xo[:20, 2] += np.random.default_rng(13).uniform(2.0, 30.0, 20) * L  # far outside the open z axis
+    Xt, Ct = cf.rand_config_triclinic(400, seed=14)
+    return [
+        (X, C, 5.0, (True, True, True)),
+        (Xo, C, 5.0, (True, True, False)),
+        (Xf, Cf, 5.0, pf),
+        (Xd, Cd, 6.0, (True, True, True)),
+        (Xt, Ct, 3.0, (False, True, False)),
+        (X[:500], C, 5.0, (False, False, False)),
+    ]
+
+
+@pytest.mark.parametrize("case", range(6))
+def test_neighbours_of_single_atoms(nlpkg, orc, case):
+    X, C, rc, pbc = _cases()[case]
+    clist = nlpkg.build_cell_list(torch.from_numpy(np.ascontiguousarray(X)).cuda(), rc, C, pbc)
+    oc = orc.build_cell_list(X, rc, C, pbc)
+    for i in sorted({1, 2, X.shape[0], (X.shape[0] + 1) // 2, min(17, X.shape[0])}):
+        js, Rs, Ss = nlpkg.neighbours(clist, i)
+        oj, oR, oS = orc.neighbours(oc, i)
+        assert np.array_equal(js.cpu().numpy().astype(np.int64), oj), i
+        assert np.array_equal(Ss.cpu().numpy().astype(np.int64), oS), i
+        assert np.array_equal(Rs.cpu().numpy().view(np.int64), oR.view(np.int64)), i
+        assert nlpkg.count_neighbours(clist, i) == oj.shape[0]
+        seen = []
+        nlpkg.for_each_neighbour(lambda j, R, S: seen.append((j, tuple(S))), clist, i)
+        assert seen == [(int(a), tuple(int(v) for v in b)) for a, b in zip(oj, oS)]
+
+
+@pytest.mark.parametrize("int_type", [torch.int32, torch.int64])
+def test_query_sets_match_the_full_list(nlpkg, orc, int_type):
+    X, C, L = cf.rand_config(20000, seed=15)
+    pbc = (True, False, True)
+    clist = nlpkg.build_cell_list(torch.from_numpy(X).cuda(), 5.0, C, pbc, int_type=int_type)
+    o = orc.neighbour_list(X, 5.0, C, pbc, ti_bytes=4 if int_type == torch.int32 else 8, nthreads=8)
+    atoms = np.random.default_rng(16).choice(X.shape[0], 500, replace=False) + 1
+    first, j, S, R = nlpkg.query_neighbours(clist, atoms)
+    first = first.cpu().numpy()
+    j, S, R = j.cpu().numpy().astype(np.int64), S.cpu().numpy().astype(np.int64), R.cpu().numpy()
+    assert j.dtype == np.int64 and first[0] == 1
+    for k, a in enumerate(atoms):
+        lo, hi = o.first[a - 1] - 1, o.first[a] - 1
+        g0, g1 = first[k] - 1, first[k + 1] - 1
+        assert np.array_equal(j[g0:g1], o.j[lo:hi]), a
+        assert np.array_equal(S[g0:g1], o.S[lo:hi]), a
+        assert np.array_equal(R[g0:g1].view(np.int64), o.R[lo:hi].view(np.int64)), a
+
+
+def test_query_rejects_out_of_range_atoms(nlpkg):
+    X, C, L = cf.rand_config(1000, seed=17)
+    clist = nlpkg.build_cell_list(torch.from_numpy(X).cuda(), 5.0, C, (True, True, True))
+    with pytest.raises(nlpkg.NLError):
+        nlpkg.query_neighbours(clist, [1, 1001])
+    assert nlpkg.count_neighbours(clist, 1000) >= 0  # the error word was cleared
