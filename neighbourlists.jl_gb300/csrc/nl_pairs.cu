@@ -1243,6 +1243,8 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
         const int corig = clampi(A.perm[slot] - 1, nat - 1);
         const unsigned long long px = f2pack(cx, cx), py = f2pack(cy, cy), pz = f2pack(cz, cz);
         const bool fwd = qq > 13;  // a forward cell: this warp writes the candidate's column word
+        // warp-uniform masks of the round: valid candidates, forward-cell candidates
+        const unsigned vmask = __ballot_sync(0xffffffffu, valid), fmask = __ballot_sync(0xffffffffu, valid && fwd);
         unsigned col = 0u;
         for (int a = 0; a < nb; a += 2) {
           // home atoms a and a + 1 (+inf beyond the cell): packed (a, a + 1) pairs
@@ -1253,40 +1255,43 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
           const unsigned long long r2p = f2fma(rz, rz, f2fma(ry, ry, f2mul(rx, rx)));
           float r20, r21;
           f2unpack(r2p, r20, r21);
-          const bool v0 = valid && f != a, v1 = valid && a + 1 < nb && f != a + 1;  // the centre holds the home atom itself at f == a
-          bool acc0 = v0 && r20 < lo, acc1 = v1 && r21 < lo;
-          const bool unc0 = v0 && !(r20 < lo) && !(r20 > hi), unc1 = v1 && !(r21 < lo) && !(r21 > hi);
-          if (__any_sync(0xffffffffu, unc0 || unc1)) {  // the band, and exact atoms (NaN): FP64 with the reference's arithmetic
-            if (unc0) {
+          // accepted (r2 < lo) and not rejected (!(r2 > hi): the band and NaN) as ballots;
+          // the centre holds the home atom itself at candidate f == a (round 0, lane a)
+          const unsigned lo0 = __ballot_sync(0xffffffffu, r20 < lo), lo1 = __ballot_sync(0xffffffffu, r21 < lo);
+          const unsigned in0 = __ballot_sync(0xffffffffu, !(r20 > hi)), in1 = __ballot_sync(0xffffffffu, !(r21 > hi));
+          const unsigned m0 = vmask & ~(rr == 0 ? 1u << a : 0u);
+          const unsigned m1 = a + 1 < nb ? vmask & ~(rr == 0 ? 2u << a : 0u) : 0u;
+          unsigned acc0 = lo0 & m0, acc1 = lo1 & m1;
+          const unsigned unc0 = in0 & ~lo0 & m0, unc1 = in1 & ~lo1 & m1;
+          if (unc0 | unc1) {  // the band, and exact atoms (NaN): FP64 with the reference's arithmetic
+            bool x0 = false, x1 = false;
+            if ((unc0 >> lane) & 1u) {
               ++rechecks;
-              acc0 = exact_pair(g, A.Xs, hs + a, slot, W.hmeta[a], cw);
+              x0 = exact_pair(g, A.Xs, hs + a, slot, W.hmeta[a], cw);
             }
-            if (unc1) {
+            if ((unc1 >> lane) & 1u) {
               ++rechecks;
-              acc1 = exact_pair(g, A.Xs, hs + a + 1, slot, W.hmeta[a + 1], cw);
+              x1 = exact_pair(g, A.Xs, hs + a + 1, slot, W.hmeta[a + 1], cw);
             }
+            acc0 |= __ballot_sync(0xffffffffu, x0);
+            acc1 |= __ballot_sync(0xffffffffu, x1);
           }
           // full lists keep both directions (row and, for forward cells, column);
           // a half list keeps the one half_keep selects
-          bool row0 = acc0, row1 = acc1, col0 = acc0 && fwd, col1 = acc1 && fwd;
+          unsigned row0 = acc0, row1 = acc1, cm0 = acc0 & fmask, cm1 = acc1 & fmask;
           if (A.half) {
-            if (acc0) {
-              const bool k = half_keep(W.horig[a], corig, cw, W.hmeta[a]);
-              row0 = k;
-              col0 = col0 && !k;
-            }
-            if (acc1) {
-              const bool k = half_keep(W.horig[a + 1], corig, cw, W.hmeta[a + 1]);
-              row1 = k;
-              col1 = col1 && !k;
-            }
+            const bool k0 = ((acc0 >> lane) & 1u) && half_keep(W.horig[a], corig, cw, W.hmeta[a]);
+            const bool k1 = ((acc1 >> lane) & 1u) && half_keep(W.horig[a + 1], corig, cw, W.hmeta[a + 1]);
+            row0 = __ballot_sync(0xffffffffu, k0);
+            row1 = __ballot_sync(0xffffffffu, k1);
+            cm0 &= ~row0;
+            cm1 &= ~row1;
           }
-          const unsigned b0 = __ballot_sync(0xffffffffu, row0), b1 = __ballot_sync(0xffffffffu, row1);
           if (lane == 0) {
-            W.B[a][rr] = b0;
-            W.B[a + 1][rr] = b1;  // a + 1 <= 31: nb <= 32 and a is even
+            W.B[a][rr] = row0;
+            W.B[a + 1][rr] = row1;  // a + 1 <= 31: nb <= 32 and a is even
           }
-          col |= (col0 ? 1u << a : 0u) | (col1 ? 2u << a : 0u);
+          col |= (((cm0 >> lane) & 1u) << a) | (((cm1 >> lane) & 1u) << (a + 1));
         }
         if (valid && fwd) {  // the candidate's word for its mirrored cell
           masks[kMaskStride * slot + (26 - qq)] = col;
@@ -1669,30 +1674,6 @@ struct __align__(16) EOSmem {
   unsigned mi[32];      //   record meta (windings, exact bit)
 };
 
-// One pass's staged S and R words [lo, hi) (96 per pass; dst = the pass's
-// first word): whole 16-byte vectors where vec, else word by word.
-template <typename T>
-__device__ __forceinline__ void store_staged(T* __restrict__ dst, const T* __restrict__ buf, int lo, int hi, bool vec,
-                                             int lane) {
-  constexpr int V = 16 / int(sizeof(T));
-  if (vec) {  // the whole pass: 96 / V vectors
-#pragma unroll
-    for (int v = lane; v < 96 / V; v += 32) {
-      if constexpr (sizeof(T) == 4) {
-        __stcs(reinterpret_cast<int4*>(dst) + v, reinterpret_cast<const int4*>(buf)[v]);
-      } else {
-        __stcs(reinterpret_cast<longlong2*>(dst) + v, reinterpret_cast<const longlong2*>(buf)[v]);
-      }
-    }
-  } else {
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const int e = lane + 32 * k;
-      if (e >= lo && e < hi) __stcs(dst + e, buf[e]);
-    }
-  }
-}
-
 // The three cells c - 1, c, c + 1 along one axis (c 1-based): 0-based wrapped
 // index, loop shift and whether the cell exists (wrap_and_shift,
 // cell_list.jl:105-120; periodic axes of the symmetric path have n >= 3).
@@ -1796,57 +1777,73 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
           E.xi[lane][2] = A.Xs[3LL * slot + 2];
           E.mi[lane] = __float_as_uint(A.rec[slot].w);
         }
-        // ---- expansion: lane a writes its entries at [f - G, f - G + n)
-        if (mine) {
-          int e = int(f - G);
-          const int eend = e + int(n);
+        // ---- expansion: lane a writes its entries at [f - G, f - G + n); a
+        // word has about one bit on average, so the first two bits of every
+        // word are taken without a loop and the rest by a rare one
+        {
+          int e = mine ? int(f - G) : 0;
+          const int eend = mine ? e + int(n) : 0;
+          const int emax = min(eend, kEOEnt);  // (bounds hold for consistent counts)
 #pragma unroll
           for (int q = 0; q < 27; ++q) {
-            unsigned mq = (&mv[q >> 2].x)[q & 3];
+            const int dx = q % 3, dy = (q / 3) % 3, dz = q / 9;
+            unsigned mq = mine ? (&mv[q >> 2].x)[q & 3] : 0u;
+            if (mq && !(okx[dx] && oky[dy] && okz[dz])) {  // a neighbour in a cell outside an open axis
+              bad |= kFlagInconsistent;
+              mq = 0u;
+            }
+            const unsigned info = unsigned(lane) | unsigned(sx[dx] + 1) << 5 | unsigned(sy[dy] + 1) << 7 |
+                                  unsigned(sz[dz] + 1) << 9;
+            const int c = __popc(mq);
             if (mq) {
-              const int dx = q % 3, dy = (q / 3) % 3, dz = q / 9;
-              if (!(okx[dx] && oky[dy] && okz[dz])) {  // a neighbour in a cell outside an open axis
-                bad |= kFlagInconsistent;
-                mq = 0u;
-              }
-              const unsigned info = unsigned(lane) | unsigned(sx[dx] + 1) << 5 | unsigned(sy[dy] + 1) << 7 |
-                                    unsigned(sz[dz] + 1) << 9;
-              while (mq) {
-                const int b = __ffs(mq) - 1;
+              if (e >= 0 && e < emax) E.ent[e] = make_uint2(st[q] + unsigned(__ffs(mq) - 1), info);
+              mq &= mq - 1u;
+              if (mq) {
+                if (e + 1 >= 0 && e + 1 < emax) E.ent[e + 1] = make_uint2(st[q] + unsigned(__ffs(mq) - 1), info);
                 mq &= mq - 1u;
-                if (e >= 0 && e < eend && e < kEOEnt) E.ent[e] = make_uint2(st[q] + unsigned(b), info);
-                ++e;
               }
             }
+            if (__any_sync(0xffffffffu, mq != 0u)) {  // words of three or more bits
+              int ee = e + 2;
+              while (mq) {
+                if (ee >= 0 && ee < emax) E.ent[ee] = make_uint2(st[q] + unsigned(__ffs(mq) - 1), info);
+                mq &= mq - 1u;
+                ++ee;
+              }
+            }
+            e += c;
           }
-          if (e != eend) bad |= kFlagInconsistent;  // counts and masks disagree
+          if (mine && e != eend) bad |= kFlagInconsistent;  // counts and masks disagree
         }
       }
       __syncwarp();
-      // ---- emission: pass j covers output positions G - off + 32 j + lane
+      // ---- emission: pass j covers output positions p0 + 32 j + lane, p0 =
+      // G rounded down to a multiple of 32; lane r of pass j takes entry
+      // k = 32 j + r - off
       const int off = int(G & 31);
       const int lim = int(max(min((long long)cnt, cap - G), 0LL));  // entries that fit the buffers
       if ((long long)cnt > cap - G && lane == l0) bad |= kFlagCapacity;
       const int npass = (lim + off + 31) >> 5;
-      const long long p0 = G - off;  // first output position of pass 0 (a multiple of 32)
-      const long long ti0 = o0 + 1;  // i of atom a is ti0 + a
+      const long long p0 = G - off;
+      TI* __restrict__ oi = A.oi + p0;
+      TI* __restrict__ oj = A.oj + p0;
+      TI* __restrict__ oS = A.oS + 3 * p0;
+      double* __restrict__ oR = A.oR ? A.oR + 3 * p0 : nullptr;
+      const TI ti0 = TI(o0 + 1);  // i of atom a is ti0 + a
       struct Ld {
         double x0, x1, x2;
         int pj;
         unsigned mj, info;
-        bool act;
       };
-      auto load = [&](int j, Ld& u) {
-        const int k = 32 * j - off + lane;
-        u.act = k >= 0 && k < lim;
+      auto load = [&](int k, Ld& u) {
         u.info = 0u;
         u.x0 = u.x1 = u.x2 = 0.0;
         u.pj = 0;
         u.mj = kPlainMeta;
-        if (u.act) {
+        if (unsigned(k) < unsigned(lim)) {
           const uint2 en = E.ent[k];
           u.info = en.y;
-          const XPack* xp = A.xpk + clampi(int(en.x), nat - 1);
+          const XPack* xp = A.xpk + min(en.x, unsigned(nat - 1));
           const double2 v0 = __ldg(reinterpret_cast<const double2*>(xp));
           const int4 v1 = __ldg(reinterpret_cast<const int4*>(xp) + 1);
           u.x0 = v0.x;
@@ -1857,37 +1854,42 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
         }
       };
       auto finish = [&](int j, const Ld& u) {
+        const int k = 32 * j + lane - off;
+        const bool act = unsigned(k) < unsigned(lim);
         const int a = int(u.info & 31u);
         const double* xi = E.xi[a];
-        int S[3];
-        if (plain) {
-          S[0] = int((u.info >> 5) & 3u) - 1;
-          S[1] = int((u.info >> 7) & 3u) - 1;
-          S[2] = int((u.info >> 9) & 3u) - 1;
-        } else {
+        int S0 = int((u.info >> 5) & 3u) - 1, S1 = int((u.info >> 7) & 3u) - 1, S2 = int((u.info >> 9) & 3u) - 1;
+        if (!plain) {  // windings or exact atoms: S = s_loop + wi - wj
           const double xj[3] = {u.x0, u.x1, u.x2};
-          const unsigned slp = cand_base(int((u.info >> 5) & 3u) - 1, int((u.info >> 7) & 3u) - 1,
-                                         int((u.info >> 9) & 3u) - 1);
-          pair_S(g, xi, xj, E.mi[a], cand_word(slp, u.mj), S);
+          int S[3];
+          pair_S(g, xi, xj, E.mi[a], cand_word(cand_base(S0, S1, S2), u.mj), S);
+          S0 = S[0];
+          S1 = S[1];
+          S2 = S[2];
         }
-        double R0 = 0.0, R1 = 0.0, R2 = 0.0;
-        if (A.oR) {
-          R0 = dsub(u.x0, xi[0]);
-          R1 = dsub(u.x1, xi[1]);
-          R2 = dsub(u.x2, xi[2]);
-          const bool nz = u.act && (S[0] | S[1] | S[2]) != 0;
+        const int t = 32 * j + lane;  // output position relative to p0
+        if (act) {
+          __stcs(oi + t, TI(ti0 + a));
+          __stcs(oj + t, TI(u.pj));
+        }
+        E.sbuf[3 * lane + 0] = TI(S0);
+        E.sbuf[3 * lane + 1] = TI(S1);
+        E.sbuf[3 * lane + 2] = TI(S2);
+        if (oR) {
+          double R0 = dsub(u.x0, xi[0]), R1 = dsub(u.x1, xi[1]), R2 = dsub(u.x2, xi[2]);
+          const bool nz = act && (S0 | S1 | S2) != 0;
           if (__any_sync(0xffffffffu, nz)) {
             if (nz) {
               double c0, c1, c2;
-              if (abs(S[0]) <= kCsR && abs(S[1]) <= kCsR && abs(S[2]) <= kCsR) {
-                const double* t = cs_blk + 3 * ((S[0] + kCsR) + kCsN * ((S[1] + kCsR) + kCsN * (S[2] + kCsR)));
-                c0 = t[0];
-                c1 = t[1];
-                c2 = t[2];
+              if (abs(S0) <= kCsR && abs(S1) <= kCsR && abs(S2) <= kCsR) {
+                const double* tb = cs_blk + 3 * ((S0 + kCsR) + kCsN * ((S1 + kCsR) + kCsN * (S2 + kCsR)));
+                c0 = tb[0];
+                c1 = tb[1];
+                c2 = tb[2];
               } else {
-                c0 = cts_k(g.C, S[0], S[1], S[2], 0);
-                c1 = cts_k(g.C, S[0], S[1], S[2], 1);
-                c2 = cts_k(g.C, S[0], S[1], S[2], 2);
+                c0 = cts_k(g.C, S0, S1, S2, 0);
+                c1 = cts_k(g.C, S0, S1, S2, 1);
+                c2 = cts_k(g.C, S0, S1, S2, 2);
               }
               R0 = dadd(R0, c0);
               R1 = dadd(R1, c1);
@@ -1899,35 +1901,49 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
             R1 = add_signed_zero(R1, zc[1]);
             R2 = add_signed_zero(R2, zc[2]);
           }
-        }
-        const long long pb = p0 + 32LL * j;  // this pass's first output position
-        if (u.act) {
-          __stcs(A.oi + pb + lane, TI(ti0 + a));
-          __stcs(A.oj + pb + lane, TI(u.pj));
-        }
-        E.sbuf[3 * lane + 0] = TI(S[0]);
-        E.sbuf[3 * lane + 1] = TI(S[1]);
-        E.sbuf[3 * lane + 2] = TI(S[2]);
-        if (A.oR) {
           E.rbuf[3 * lane + 0] = R0;
           E.rbuf[3 * lane + 1] = R1;
           E.rbuf[3 * lane + 2] = R2;
         }
         __syncwarp();
         const int k0 = 32 * j - off;  // entry of lane 0
-        const bool full = vec_ok && k0 >= 0 && k0 + 32 <= lim;
-        const int lo = 3 * max(-k0, 0), hw = 3 * min(lim - k0, 32);
-        store_staged<TI>(A.oS + 3 * pb, E.sbuf, lo, hw, full, lane);
-        if (A.oR) store_staged<double>(A.oR + 3 * pb, E.rbuf, lo, hw, full, lane);
+        if (vec_ok && k0 >= 0 && k0 + 32 <= lim) {  // a full pass: 16-byte vectors
+          constexpr int VS = 16 / int(sizeof(TI));
+          if (lane < 96 / VS) {
+            if constexpr (sizeof(TI) == 4)
+              __stcs(reinterpret_cast<int4*>(oS + 96 * j) + lane, reinterpret_cast<const int4*>(E.sbuf)[lane]);
+            else
+              __stcs(reinterpret_cast<longlong2*>(oS + 96 * j) + lane, reinterpret_cast<const longlong2*>(E.sbuf)[lane]);
+          }
+          if (sizeof(TI) == 8 && lane < 48 - 32)
+            __stcs(reinterpret_cast<longlong2*>(oS + 96 * j) + 32 + lane,
+                   reinterpret_cast<const longlong2*>(E.sbuf)[32 + lane]);
+          if (oR) {
+            __stcs(reinterpret_cast<double2*>(oR + 96 * j) + lane, reinterpret_cast<const double2*>(E.rbuf)[lane]);
+            if (lane < 16)
+              __stcs(reinterpret_cast<double2*>(oR + 96 * j) + 32 + lane,
+                     reinterpret_cast<const double2*>(E.rbuf)[32 + lane]);
+          }
+        } else {  // the chunk's ends: the words of this pass's own pairs only
+          const int lo = 3 * max(-k0, 0), hw = 3 * min(lim - k0, 32);
+#pragma unroll
+          for (int w = 0; w < 3; ++w) {
+            const int e = lane + 32 * w;
+            if (e >= lo && e < hw) {
+              __stcs(oS + 96 * j + e, E.sbuf[e]);
+              if (oR) __stcs(oR + 96 * j + e, E.rbuf[e]);
+            }
+          }
+        }
         __syncwarp();
       };
       if (npass > 0) {
         Ld c0, c1, n0, n1;
-        load(0, c0);
-        load(1, c1);
+        load(lane - off, c0);
+        load(32 + lane - off, c1);
         for (int j = 0; j < npass; j += 2) {
-          load(j + 2, n0);  // two passes' gathers in flight while two are finished
-          load(j + 3, n1);
+          load(32 * (j + 2) + lane - off, n0);  // two passes' gathers in flight while two are finished
+          load(32 * (j + 3) + lane - off, n1);
           finish(j, c0);
           if (j + 1 < npass) finish(j + 1, c1);
           c0 = n0;
