@@ -47,7 +47,9 @@ extern "C" {
 
 /* lazy reductions (nl_lazy_reduce) */
 #define NL_REDUCE_COUNT 0         /* int32 per atom: count_neighbours (cell_list.jl:808-814) */
-#define NL_REDUCE_INV_R6 1        /* double per atom: sum over neighbours of 1/r^6 */
+#define NL_REDUCE_INV_R6 1        /* double per atom: sum over neighbours of 1/r^6, in traversal order (bit-exact) */
+#define NL_REDUCE_INV_R6_FAST 2   /* the same sum by the fused symmetric pass: relative error <= 1e-12, last bits
+                                     vary with the order of the atomic additions */
 
 /* Cell analysis: the reference's analyze_cell (cell_list.jl:152-170) plus the
  * stencil half-width nxyz of materialize_pairlist (gpu_kernels.jl:315-316),
@@ -149,7 +151,13 @@ int nl_max_displacement_sq(const double* d_X, const double* d_Xref, int64_t nat,
 /* Lazy mode (for_each_neighbour over every atom, cell_list.jl:779-814) with a
  * built-in per-atom reduction: NL_REDUCE_COUNT -> int32 d_out[nat];
  * NL_REDUCE_INV_R6 -> double d_out[nat] = sum_j 1/((r2*r2)*r2), r2 = dot(R,R),
- * accumulated in the reference's traversal order.  Asynchronous. */
+ * accumulated in the reference's traversal order (bit-identical to a
+ * sequential for_each_neighbour sum); NL_REDUCE_INV_R6_FAST -> the same sum
+ * screened and reduced in one pass that visits each unordered pair once (R
+ * with the reference's FP64 operations, 1/r^6 in double-float, atomic
+ * accumulation): relative error at most 1e-12.  Where the stencil is not 27
+ * distinct cells, or a cell holds more than 32 atoms, the fast op computes
+ * the traversal-order sum.  Asynchronous. */
 int nl_lazy_reduce(const double* d_X_sorted, const void* d_perm, const void* d_cell_id, const void* d_cell_offsets,
                    int64_t nat, const double cell[9], const double inv_cell[9], const int64_t ncells[3],
                    const int64_t nxyz[3], const uint8_t pbc[3], double cutoff, int index_bytes, int reuse_records,

@@ -26,6 +26,7 @@ NL_LEGACY_FIX_WORKSPACE_BYTES = 256
 
 NL_REDUCE_COUNT = 0
 NL_REDUCE_INV_R6 = 1
+NL_REDUCE_INV_R6_FAST = 2
 
 # every symbol include/nlgpu.h declares
 EXPORTED = [

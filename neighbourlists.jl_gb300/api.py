@@ -419,7 +419,10 @@ def lazy_reduce(clist: SortedCellList, op: str = "count", stream=None, out: Opti
                 sync: bool = True) -> torch.Tensor:
     """Built-in reductions of the lazy traversal over every atom:
     "count" -> int32 neighbour count per atom (count_neighbours for all i);
-    "inv_r6" -> float64 per-atom sum of 1/r^6 in the reference's order.
+    "inv_r6" -> float64 per-atom sum of 1/r^6 in the reference's order
+    (bit-identical to a sequential for_each_neighbour sum);
+    "inv_r6_fast" -> the same sums from one fused pass over unordered pairs
+    (relative error at most 1e-12, last bits not reproducible run to run).
     ``out`` reuses an output tensor; ``sync=False`` leaves the error check to
     a later nl_sync_status on the cell list's workspace."""
     nat = int(clist.X.shape[0])
@@ -438,8 +441,10 @@ def lazy_reduce(clist: SortedCellList, op: str = "count", stream=None, out: Opti
         code, dt = _lib.NL_REDUCE_COUNT, torch.int32
     elif op == "inv_r6":
         code, dt = _lib.NL_REDUCE_INV_R6, torch.float64
+    elif op == "inv_r6_fast":
+        code, dt = _lib.NL_REDUCE_INV_R6_FAST, torch.float64
     else:
-        raise ValueError("op must be 'count' or 'inv_r6'")
+        raise ValueError("op must be 'count', 'inv_r6' or 'inv_r6_fast'")
     if out is None:
         out = torch.zeros(nat, dtype=dt, device=dev)
     elif out.dtype != dt or out.numel() != nat or not out.is_cuda:

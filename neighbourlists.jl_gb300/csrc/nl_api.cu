@@ -438,6 +438,14 @@ nl::PairArgs<TI> pair_args(const nl::Geometry& g, const TI* cell_offsets, const 
 // full or half list of a single system with per-atom lists in the workspace
 // and a 27-cell stencil of distinct cells (nxyz = 1, periodic axes of at
 // least 3 cells); count_kernel 1 or 2 selects the per-cell / per-atom pass.
+// The stencil is 27 distinct cells: nxyz = 1 on every axis and periodic axes
+// of at least 3 cells (the symmetric passes' condition on the geometry).
+bool sym_geometry(const nl::Geometry& g) {
+  bool sym = true;
+  for (int k = 0; k < 3; ++k) sym = sym && g.nxyz[k] == 1 && (!g.pbc[k] || g.ns[k] >= 3);
+  return sym;
+}
+
 bool use_sym(const nl::Geometry& g, const Layout& L) {
   // masks (27 words per atom) and the stencil table (54 words per cell) share the list region
   const bool fits = 27.0 * g.nat + 54.0 * g.ncells <= 2.0 * nl::kListCap * g.nat;
@@ -492,7 +500,8 @@ int fill_impl(const nl::Geometry& g, const double* Xs, const TI* perm, const TI*
   a.oS = oS;
   a.oR = oR;
   a.capacity = capacity;
-  a.vec_ok = (reinterpret_cast<uintptr_t>(oS) % 16 == 0) && (reinterpret_cast<uintptr_t>(oR) % 16 == 0);
+  a.vec_ok = (reinterpret_cast<uintptr_t>(oi) % 16 == 0) && (reinterpret_cast<uintptr_t>(oj) % 16 == 0) &&
+             (reinterpret_cast<uintptr_t>(oS) % 16 == 0) && (reinterpret_cast<uintptr_t>(oR) % 16 == 0);
   nl::launch_pairs<TI>(nl::kModeFill, a, num_sms(), st);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? NL_OK : cuda_fail(e, "launch fill kernel");
@@ -1124,7 +1133,8 @@ int nl_lazy_reduce(const double* d_X_sorted, const void* d_perm, const void* d_c
   if (!cell || !inv_cell || !ncells || !nxyz || !pbc || !d_cell_offsets ||
       (nat > 0 && (!d_X_sorted || !d_perm || !d_cell_id || !d_out)))
     return fail(NL_ERR_ARG, "null argument");
-  if (op != NL_REDUCE_COUNT && op != NL_REDUCE_INV_R6) return fail(NL_ERR_ARG, "unknown reduction");
+  if (op != NL_REDUCE_COUNT && op != NL_REDUCE_INV_R6 && op != NL_REDUCE_INV_R6_FAST)
+    return fail(NL_ERR_ARG, "unknown reduction");
   Layout L;
   int64_t nct;
   int s = check_common(nat, ncells, nxyz, index_bytes, d_workspace, workspace_bytes, L, nct);
@@ -1147,6 +1157,21 @@ int nl_lazy_reduce(const double* d_X_sorted, const void* d_perm, const void* d_c
     nl::PairArgs<TI> a =
         pair_args<TI>(g, static_cast<const TI*>(d_cell_offsets), static_cast<const TI*>(d_perm), d_X_sorted, d_workspace, L);
     a.cap_rec = nullptr;  // a later nl_fill_pairs must not take these lists for its own
+    // the fused symmetric passes where the stencil is 27 distinct cells; the
+    // per-cell passes below are gated on their success and redo the whole
+    // reduction when a cell holds more than 32 atoms
+    a.sym = (op == NL_REDUCE_COUNT || op == NL_REDUCE_INV_R6_FAST) && sym_geometry(g) ? 1 : 0;
+    if (a.sym) {
+      const size_t bytes = op == NL_REDUCE_COUNT ? sizeof(int) : sizeof(double);
+      cudaError_t me = cudaMemsetAsync(d_out, 0, bytes * size_t(g.nat), st);
+      if (me != cudaSuccess) e = me;
+      if (op == NL_REDUCE_COUNT) {
+        a.counts = static_cast<int*>(d_out);
+      } else {
+        a.per_atom = static_cast<double*>(d_out);
+      }
+      nl::launch_sym_lazy<TI>(op == NL_REDUCE_COUNT ? nl::kLazyCounts : nl::kLazyInvR6, a, sms, st);
+    }
     if (op == NL_REDUCE_COUNT) {
       a.list_cap = 0;  // the counts are the result: no lists
       a.lists = nullptr;
@@ -1169,6 +1194,7 @@ int nl_lazy_reduce(const double* d_X_sorted, const void* d_perm, const void* d_c
     run(int32_t(0));
   else
     run(int64_t(0));
+  if (e != cudaSuccess) return cuda_fail(e, "memset lazy output");
   e = cudaGetLastError();
   return e == cudaSuccess ? NL_OK : cuda_fail(e, "launch lazy kernel");
 }

@@ -366,7 +366,8 @@ __device__ __forceinline__ void load_system(const PairArgs<TI>& A, int s, Geomet
 template <typename TI, int MODE, bool BATCH>
 __global__ void __launch_bounds__(kPairWarps * 32, BATCH ? NL_PAIR_BATCH_MIN_BLOCKS : kMinBlocks)
     k_pairs(PairArgs<TI> A) {
-  if (MODE == kModeCount && !BATCH && A.sym && *A.sym_fail == 0) return;  // the symmetric pass counted
+  if ((MODE == kModeCount || MODE == kModeLazyR6) && !BATCH && A.sym && *A.sym_fail == 0)
+    return;  // the symmetric pass counted (or summed)
   // the screening passes visit only listed cells: none listed, nothing to do
   // (the same value for every thread, so no block stops at a barrier alone)
   if ((MODE == kModeFill || (MODE == kModeLazyR6 && A.list_cap > 0)) && *A.n_screen_cells <= 0) return;
@@ -1125,11 +1126,131 @@ __device__ __forceinline__ unsigned long long f2fma(unsigned long long a, unsign
   return r;
 }
 
+// What the candidate-parallel symmetric pass produces: the neighbour masks
+// (and headers and gather rows) of the write pass, only the per-atom counts
+// (the lazy count), or the per-atom sums of 1/r^6 (the lazy reduction).
+constexpr int kSymMasks = 0, kSymCounts = 1, kSymInvR6 = 2;
+
+// The lazy reduction's view of one warp: home atoms, every candidate of the
+// home cell's forward stencil (up to 14 cells of 32 atoms), and the queue of
+// accepted pairs (home atom | forward flag << 5 | candidate << 6).
+struct __align__(16) LZSmem {
+  float hx[32], hy[32], hz[32];
+  unsigned hmeta[32];
+  int horig[32];
+  int hcnt[32];
+  double hX[32][3];        // home atoms: FP64 positions
+  double hsum[32];         //   sum over their rows
+  int cslot[14 * 32];      // candidate: sorted slot
+  unsigned ccw[14 * 32];   //   candidate word (loop shift, windings)
+  double csum[14 * 32];    //   sum over its column (forward cells)
+  unsigned q[128];         // queued pairs
+};
+
+// Double-float (unevaluated FP32 pairs, hi + lo): Dekker's and Knuth's
+// error-free products and sums (about 48 significant bits).
+struct dfloat {
+  float hi, lo;
+};
+__device__ __forceinline__ dfloat df_quick(float a, float b) {  // |a| >= |b|
+  const float s = a + b;
+  return {s, b - (s - a)};
+}
+__device__ __forceinline__ dfloat df_sq(float h, float l) {  // (h + l)^2
+  const float p = h * h;
+  float e = fmaf(h, h, -p);
+  e = fmaf(2.f * h, l, e);
+  return df_quick(p, e);
+}
+__device__ __forceinline__ dfloat df_add(dfloat a, dfloat b) {
+  const float s = a.hi + b.hi;
+  const float bb = s - a.hi;
+  const float e = (a.hi - (s - bb)) + (b.hi - bb) + (a.lo + b.lo);
+  return df_quick(s, e);
+}
+__device__ __forceinline__ dfloat df_mul(dfloat a, dfloat b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e));
+  return df_quick(p, e);
+}
+__device__ __forceinline__ dfloat df_rcp(dfloat a) {  // one Newton step from the FP32 reciprocal
+  const float y = __fdividef(1.0f, a.hi);
+  float e = fmaf(-a.hi, y, 1.0f);
+  e = fmaf(-a.lo, y, e);
+  return df_quick(y, y * e);
+}
+// A normal float (or zero) as a double, with integer operations.
+__device__ __forceinline__ double f2d_exact(float x) {
+  const unsigned u = __float_as_uint(x);
+  const unsigned ex = (u >> 23) & 0xFFu;
+  if (ex == 0u) return __longlong_as_double((long long)(u & 0x80000000u) << 32);  // +-0 (subnormals to zero)
+  const unsigned hi = (u & 0x80000000u) | ((ex + 896u) << 20) | ((u & 0x7FFFFFu) >> 3);
+  return __hiloint2double(int(hi), int((u & 0x7u) << 29));
+}
+
+// Evaluates n <= 32 queued pairs of the lazy reduction, one per lane: R with
+// the reference's FP64 operations (gpu_kernels.jl:88-91), r2 and 1/r2^3 in
+// double-float (relative error far below 1e-12), then the atom's row sum and,
+// for a forward candidate, its column sum.  r2 below 1e-12 (where 1/r2^3
+// leaves the FP32 range: coincident or nearly coincident atoms) is evaluated
+// in FP64 with the reference's formula.
 template <typename TI>
+__device__ __forceinline__ void lazy_flush(const PairArgs<TI>& A, const Geometry& g, const double* cs_tab, LZSmem& W,
+                                           int n, int lane) {
+  const bool act = lane < n;
+  const unsigned e = act ? W.q[lane] : 0u;
+  const int a = int(e & 31u), fi = int(e >> 6);
+  const double* xi = W.hX[a];
+  const int sj = W.cslot[fi];
+  const double xj[3] = {A.Xs[3LL * sj + 0], A.Xs[3LL * sj + 1], A.Xs[3LL * sj + 2]};
+  int S[3];
+  pair_S(g, xi, xj, W.hmeta[a], W.ccw[fi], S);
+  double R[3];
+  pair_R(g, cs_tab, xi, xj, S[0], S[1], S[2], act, R);
+  dfloat r2 = {0.f, 0.f};
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    float h, l, c;
+    if (!split3(R[k], h, l, c)) {  // |R_k| outside [2^-60, 2^60]
+      h = __double2float_rn(R[k]);
+      l = 0.f;
+    }
+    r2 = df_add(r2, df_sq(h, l));
+  }
+  double fd;
+  if (__any_sync(0xffffffffu, act && !(r2.hi >= 1e-12f))) {
+    if (!(r2.hi >= 1e-12f)) {
+      const double r2d = dot_ref(R);
+      fd = __ddiv_rn(1.0, dmul(dmul(r2d, r2d), r2d));
+    } else {
+      const dfloat y = df_rcp(r2);
+      const dfloat f = df_mul(df_mul(y, y), y);
+      fd = dadd(f2d_exact(f.hi), f2d_exact(f.lo));
+    }
+  } else {
+    const dfloat y = df_rcp(r2);
+    const dfloat f = df_mul(df_mul(y, y), y);
+    fd = dadd(f2d_exact(f.hi), f2d_exact(f.lo));
+  }
+  if (act) {
+    atomicAdd(&W.hsum[a], fd);
+    if ((e >> 5) & 1u) atomicAdd(&W.csum[fi], fd);
+  }
+  __syncwarp();
+}
+
+template <typename TI, int SM>
 __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(PairArgs<TI> A) {
-  __shared__ SCSmem sm[kSCWarps];
+  using Smem = std::conditional_t<SM == kSymInvR6, LZSmem, SCSmem>;
+  __shared__ Smem sm[kSCWarps];
+  __shared__ double cs_blk[SM == kSymInvR6 ? 3 * kCsN * kCsN * kCsN : 1];
+  if constexpr (SM == kSymInvR6) {
+    for (int t = threadIdx.x; t < 3 * kCsN * kCsN * kCsN; t += blockDim.x) cs_blk[t] = A.cs_table[t];
+    __syncthreads();
+  }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  SCSmem& W = sm[warp];
+  Smem& W = sm[warp];
   const Geometry& g = A.g;
   const int nat = g.nat;
   const float lo = g.lo, hi = g.hi;
@@ -1169,7 +1290,7 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
       if (lane == 0) atomicOr(A.sym_fail, 1);  // a crowded cell: the per-cell pass with lists counts instead
     } else if (nb > 0) {
       // words q < 13 of the home atoms that no other warp writes: their cell is empty or outside
-      const unsigned zq = __ballot_sync(0xffffffffu, lane < 13 && (cur.lin < 0 || cur.cnt == 0));
+      const unsigned zq = SM == kSymMasks ? __ballot_sync(0xffffffffu, lane < 13 && (cur.lin < 0 || cur.cnt == 0)) : 0u;
       if (zq)
         for (int t = lane; t < nb * 13; t += 32) {
           const int a = t / 13, q = t - 13 * a;
@@ -1186,19 +1307,27 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
           hm = __float_as_uint(r.w);
           const int o = clampi(A.perm[hs + lane] - 1, nat - 1);
           W.horig[lane] = o;
-          A.hdr[o] = make_int2(hs + lane, h);  // the write pass walks atoms in original order
           const double X0 = A.Xs[3LL * (hs + lane) + 0], X1 = A.Xs[3LL * (hs + lane) + 1],
                        X2 = A.Xs[3LL * (hs + lane) + 2];
-          XPack xp;
-          xp.x = X0;
-          xp.y = X1;
-          xp.z = X2;
-          xp.perm = o + 1;
-          xp.meta = hm;
-          A.xpk[hs + lane] = xp;
-          const long long nz = (long long)0x8000000000000000ULL;
-          if (__double_as_longlong(X0) == nz || __double_as_longlong(X1) == nz || __double_as_longlong(X2) == nz)
-            atomicOr(A.sym_wound, 2);
+          if constexpr (SM == kSymMasks) {
+            A.hdr[o] = make_int2(hs + lane, h);  // the write pass walks atoms in original order
+            XPack xp;
+            xp.x = X0;
+            xp.y = X1;
+            xp.z = X2;
+            xp.perm = o + 1;
+            xp.meta = hm;
+            A.xpk[hs + lane] = xp;
+            const long long nz = (long long)0x8000000000000000ULL;
+            if (__double_as_longlong(X0) == nz || __double_as_longlong(X1) == nz || __double_as_longlong(X2) == nz)
+              atomicOr(A.sym_wound, 2);
+          }
+          if constexpr (SM == kSymInvR6) {
+            W.hX[lane][0] = X0;
+            W.hX[lane][1] = X1;
+            W.hX[lane][2] = X2;
+            W.hsum[lane] = 0.0;
+          }
         }
         W.hx[lane] = x;
         W.hy[lane] = y;
@@ -1206,7 +1335,7 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
         W.hmeta[lane] = hm;
         W.hcnt[lane] = 0;
       }
-      if (__any_sync(0xffffffffu, hm != kPlainMeta) && lane == 0) atomicOr(A.sym_wound, 1);
+      if (SM == kSymMasks && __any_sync(0xffffffffu, hm != kPlainMeta) && lane == 0) atomicOr(A.sym_wound, 1);
       // candidates: stencil cells 13..26 in stencil order, flattened
       const int scnt = lane >= 13 ? cur.cnt : 0;
       int incl = scnt;
@@ -1217,6 +1346,7 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
       }
       const int T = __shfl_sync(0xffffffffu, incl, 31);
       const int nr = (T + 31) >> 5;  // <= kSCMaxRounds
+      int qn = 0;  // sum of 1/r^6: accepted pairs queued (flushed 32 at a time with full lanes)
       __syncwarp();
       for (int rr = 0; rr < nr; ++rr) {
         const int f = 32 * rr + lane;
@@ -1241,6 +1371,13 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
         const bool ex = (cw & kExactBit) != 0;
         const float cx = ex ? nan : r.x + qx, cy = ex ? nan : r.y + qy, cz = ex ? nan : r.z + qz;
         const int corig = clampi(A.perm[slot] - 1, nat - 1);
+        if constexpr (SM == kSymInvR6) {  // the candidate, for the queue's pair evaluation
+          if (valid) {
+            W.cslot[f] = slot;
+            W.ccw[f] = cw;
+            W.csum[f] = 0.0;
+          }
+        }
         const unsigned long long px = f2pack(cx, cx), py = f2pack(cy, cy), pz = f2pack(cz, cz);
         const bool fwd = qq > 13;  // a forward cell: this warp writes the candidate's column word
         // warp-uniform masks of the round: valid candidates, forward-cell candidates
@@ -1287,18 +1424,65 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
             cm0 &= ~row0;
             cm1 &= ~row1;
           }
-          if (lane == 0) {
-            W.B[a][rr] = row0;
-            W.B[a + 1][rr] = row1;  // a + 1 <= 31: nb <= 32 and a is even
+          if constexpr (SM == kSymMasks) {
+            if (lane == 0) {
+              W.B[a][rr] = row0;
+              W.B[a + 1][rr] = row1;  // a + 1 <= 31: nb <= 32 and a is even
+            }
+          } else if constexpr (SM == kSymCounts) {
+            if (lane == 0) {
+              W.hcnt[a] += __popc(row0);
+              W.hcnt[a + 1] += __popc(row1);
+            }
+          } else {
+            // queue every accepted pair: (home atom, candidate, forward flag); a
+            // pair of the centre is met from both of its atoms and added to
+            // each atom's own row, a forward pair to the row and the column
+            const unsigned lt = lt_mask();
+            if ((row0 >> lane) & 1u)
+              W.q[qn + __popc(row0 & lt)] = unsigned(a) | (((cm0 >> lane) & 1u) << 5) | (unsigned(f) << 6);
+            qn += __popc(row0);
+            if ((row1 >> lane) & 1u)
+              W.q[qn + __popc(row1 & lt)] = unsigned(a + 1) | (((cm1 >> lane) & 1u) << 5) | (unsigned(f) << 6);
+            qn += __popc(row1);
+            if (qn >= 32) {
+              __syncwarp();
+              lazy_flush<TI>(A, g, cs_blk, W, 32, lane);
+              const unsigned rest = lane + 32 < qn ? W.q[lane + 32] : 0u;  // qn <= 96
+              const unsigned rest2 = lane + 64 < qn ? W.q[lane + 64] : 0u;
+              __syncwarp();
+              if (lane + 32 < qn) W.q[lane] = rest;
+              if (lane + 64 < qn) W.q[lane + 32] = rest2;
+              qn -= 32;
+              __syncwarp();
+            }
           }
-          col |= (((cm0 >> lane) & 1u) << a) | (((cm1 >> lane) & 1u) << (a + 1));
+          if constexpr (SM != kSymInvR6) col |= (((cm0 >> lane) & 1u) << a) | (((cm1 >> lane) & 1u) << (a + 1));
         }
-        if (valid && fwd) {  // the candidate's word for its mirrored cell
-          masks[kMaskStride * slot + (26 - qq)] = col;
-          if (col) atomicAdd(A.counts + corig, __popc(col));
+        if constexpr (SM == kSymMasks) {
+          if (valid && fwd) {  // the candidate's word for its mirrored cell
+            masks[kMaskStride * slot + (26 - qq)] = col;
+            if (col) atomicAdd(A.counts + corig, __popc(col));
+          }
+        } else if constexpr (SM == kSymCounts) {
+          if (valid && fwd && col) atomicAdd(A.counts + corig, __popc(col));
         }
       }
       __syncwarp();
+      if constexpr (SM == kSymInvR6) {
+        if (qn > 0) lazy_flush<TI>(A, g, cs_blk, W, qn, lane);
+        __syncwarp();
+        // the cell's sums: its atoms' rows and its forward candidates' columns
+        if (lane < nb) atomicAdd(A.per_atom + W.horig[lane], W.hsum[lane]);
+        for (int fc = lane; fc < T; fc += 32)
+          if (W.csum[fc] != 0.0) atomicAdd(A.per_atom + clampi(A.perm[W.cslot[fc]] - 1, nat - 1), W.csum[fc]);
+        __syncwarp();
+      }
+      if constexpr (SM == kSymCounts) {
+        if (lane < nb && W.hcnt[lane]) atomicAdd(A.counts + W.horig[lane], W.hcnt[lane]);
+        __syncwarp();
+      }
+      if constexpr (SM == kSymMasks) {
       // rows: word q = 13..26 of every home atom, from its ballots
       for (int t0 = 0; t0 < nb * 14; t0 += 32) {
         const int t = t0 + lane;
@@ -1318,6 +1502,7 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
       __syncwarp();
       if (lane < nb && W.hcnt[lane]) atomicAdd(A.counts + W.horig[lane], W.hcnt[lane]);
       __syncwarp();
+      }
     }
     cur = nxt;
   }
@@ -1667,8 +1852,6 @@ static_assert(kEOEnt >= 27 * 32, "an atom of the symmetric pass has fewer than 2
 
 template <typename TI>
 struct __align__(16) EOSmem {
-  double rbuf[96];      // R of one pass, three words per pair
-  TI sbuf[96];          // S of one pass
   uint2 ent[kEOEnt];    // entry: (sorted slot of j, atom | loop shift + 1 per axis << 5 + 2k)
   double xi[32][3];     // the batch's atoms: FP64 position
   unsigned mi[32];      //   record meta (windings, exact bit)
@@ -1742,7 +1925,8 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
     int l0 = 0;
     while (l0 < na) {
       const long long G = __shfl_sync(0xffffffffu, f, l0);
-      const unsigned inch = __ballot_sync(0xffffffffu, lane >= l0 && own && f + n - G <= kEOEnt);
+      // (entries are stored from index G mod 32: kEOEnt - 32 pairs per chunk)
+      const unsigned inch = __ballot_sync(0xffffffffu, lane >= l0 && own && f + n - G <= kEOEnt - 32);
       const int l1 = l0 + __popc(inch >> l0);
       if (l1 == l0) {  // an atom with more pairs than its masks can hold: counts and masks disagree
         bad |= kFlagInconsistent;
@@ -1781,7 +1965,7 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
         // word has about one bit on average, so the first two bits of every
         // word are taken without a loop and the rest by a rare one
         {
-          int e = mine ? int(f - G) : 0;
+          int e = mine ? int(f - G) + int(G & 31) : 0;  // the entry of output position p sits at p - (G - G mod 32)
           const int eend = mine ? e + int(n) : 0;
           const int emax = min(eend, kEOEnt);  // (bounds hold for consistent counts)
 #pragma unroll
@@ -1817,137 +2001,137 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
         }
       }
       __syncwarp();
-      // ---- emission: pass j covers output positions p0 + 32 j + lane, p0 =
-      // G rounded down to a multiple of 32; lane r of pass j takes entry
-      // k = 32 j + r - off
+      // ---- emission: lane r of round t writes the four output positions
+      // p0 + 4 (32 t + r) .. + 3 (p0 = G rounded down to a multiple of 32):
+      // entries [4 g, 4 g + 4) with two 16-byte shared loads, four gathers in
+      // flight, and i, j, S, R of the four pairs as 16-byte vector stores
+      // (word by word at the chunk's ends or for unaligned arrays)
       const int off = int(G & 31);
       const int lim = int(max(min((long long)cnt, cap - G), 0LL));  // entries that fit the buffers
       if ((long long)cnt > cap - G && lane == l0) bad |= kFlagCapacity;
-      const int npass = (lim + off + 31) >> 5;
+      const int hix = off + lim;  // entries [off, hix) are this chunk's pairs
       const long long p0 = G - off;
       TI* __restrict__ oi = A.oi + p0;
       TI* __restrict__ oj = A.oj + p0;
       TI* __restrict__ oS = A.oS + 3 * p0;
       double* __restrict__ oR = A.oR ? A.oR + 3 * p0 : nullptr;
       const TI ti0 = TI(o0 + 1);  // i of atom a is ti0 + a
-      struct Ld {
-        double x0, x1, x2;
-        int pj;
-        unsigned mj, info;
-      };
-      auto load = [&](int k, Ld& u) {
-        u.info = 0u;
-        u.x0 = u.x1 = u.x2 = 0.0;
-        u.pj = 0;
-        u.mj = kPlainMeta;
-        if (unsigned(k) < unsigned(lim)) {
-          const uint2 en = E.ent[k];
-          u.info = en.y;
-          const XPack* xp = A.xpk + min(en.x, unsigned(nat - 1));
-          const double2 v0 = __ldg(reinterpret_cast<const double2*>(xp));
-          const int4 v1 = __ldg(reinterpret_cast<const int4*>(xp) + 1);
-          u.x0 = v0.x;
-          u.x1 = v0.y;
-          u.x2 = __hiloint2double(v1.y, v1.x);
-          u.pj = v1.z;
-          u.mj = unsigned(v1.w);
+      const int ngroups = (hix + 3) >> 2;
+      for (int g0 = 0; g0 < ngroups; g0 += 32) {
+        const int b = 4 * (g0 + lane);
+        const bool any = b < hix;
+        uint4 e01 = make_uint4(0u, 0u, 0u, 0u), e23 = e01;
+        if (any) {
+          e01 = reinterpret_cast<const uint4*>(E.ent)[b >> 1];
+          e23 = reinterpret_cast<const uint4*>(E.ent)[(b >> 1) + 1];
         }
-      };
-      auto finish = [&](int j, const Ld& u) {
-        const int k = 32 * j + lane - off;
-        const bool act = unsigned(k) < unsigned(lim);
-        const int a = int(u.info & 31u);
-        const double* xi = E.xi[a];
-        int S0 = int((u.info >> 5) & 3u) - 1, S1 = int((u.info >> 7) & 3u) - 1, S2 = int((u.info >> 9) & 3u) - 1;
-        if (!plain) {  // windings or exact atoms: S = s_loop + wi - wj
-          const double xj[3] = {u.x0, u.x1, u.x2};
-          int S[3];
-          pair_S(g, xi, xj, E.mi[a], cand_word(cand_base(S0, S1, S2), u.mj), S);
-          S0 = S[0];
-          S1 = S[1];
-          S2 = S[2];
-        }
-        const int t = 32 * j + lane;  // output position relative to p0
-        if (act) {
-          __stcs(oi + t, TI(ti0 + a));
-          __stcs(oj + t, TI(u.pj));
-        }
-        E.sbuf[3 * lane + 0] = TI(S0);
-        E.sbuf[3 * lane + 1] = TI(S1);
-        E.sbuf[3 * lane + 2] = TI(S2);
-        if (oR) {
-          double R0 = dsub(u.x0, xi[0]), R1 = dsub(u.x1, xi[1]), R2 = dsub(u.x2, xi[2]);
-          const bool nz = act && (S0 | S1 | S2) != 0;
-          if (__any_sync(0xffffffffu, nz)) {
-            if (nz) {
-              double c0, c1, c2;
-              if (abs(S0) <= kCsR && abs(S1) <= kCsR && abs(S2) <= kCsR) {
-                const double* tb = cs_blk + 3 * ((S0 + kCsR) + kCsN * ((S1 + kCsR) + kCsN * (S2 + kCsR)));
-                c0 = tb[0];
-                c1 = tb[1];
-                c2 = tb[2];
-              } else {
-                c0 = cts_k(g.C, S0, S1, S2, 0);
-                c1 = cts_k(g.C, S0, S1, S2, 1);
-                c2 = cts_k(g.C, S0, S1, S2, 2);
-              }
-              R0 = dadd(R0, c0);
-              R1 = dadd(R1, c1);
-              R2 = dadd(R2, c2);
-            }
-          }
-          if (negzero && !nz) {  // a -0 coordinate: RN(d + C'(0,0,0)) differs from d when d is -0
-            R0 = add_signed_zero(R0, zc[0]);
-            R1 = add_signed_zero(R1, zc[1]);
-            R2 = add_signed_zero(R2, zc[2]);
-          }
-          E.rbuf[3 * lane + 0] = R0;
-          E.rbuf[3 * lane + 1] = R1;
-          E.rbuf[3 * lane + 2] = R2;
-        }
-        __syncwarp();
-        const int k0 = 32 * j - off;  // entry of lane 0
-        if (vec_ok && k0 >= 0 && k0 + 32 <= lim) {  // a full pass: 16-byte vectors
-          constexpr int VS = 16 / int(sizeof(TI));
-          if (lane < 96 / VS) {
-            if constexpr (sizeof(TI) == 4)
-              __stcs(reinterpret_cast<int4*>(oS + 96 * j) + lane, reinterpret_cast<const int4*>(E.sbuf)[lane]);
-            else
-              __stcs(reinterpret_cast<longlong2*>(oS + 96 * j) + lane, reinterpret_cast<const longlong2*>(E.sbuf)[lane]);
-          }
-          if (sizeof(TI) == 8 && lane < 48 - 32)
-            __stcs(reinterpret_cast<longlong2*>(oS + 96 * j) + 32 + lane,
-                   reinterpret_cast<const longlong2*>(E.sbuf)[32 + lane]);
-          if (oR) {
-            __stcs(reinterpret_cast<double2*>(oR + 96 * j) + lane, reinterpret_cast<const double2*>(E.rbuf)[lane]);
-            if (lane < 16)
-              __stcs(reinterpret_cast<double2*>(oR + 96 * j) + 32 + lane,
-                     reinterpret_cast<const double2*>(E.rbuf)[32 + lane]);
-          }
-        } else {  // the chunk's ends: the words of this pass's own pairs only
-          const int lo = 3 * max(-k0, 0), hw = 3 * min(lim - k0, 32);
+        const unsigned slot4[4] = {e01.x, e01.z, e23.x, e23.z}, info[4] = {e01.y, e01.w, e23.y, e23.w};
+        double X0[4], X1[4], X2[4];
+        int pj[4];
+        unsigned mj[4];
+        bool v[4];
 #pragma unroll
-          for (int w = 0; w < 3; ++w) {
-            const int e = lane + 32 * w;
-            if (e >= lo && e < hw) {
-              __stcs(oS + 96 * j + e, E.sbuf[e]);
-              if (oR) __stcs(oR + 96 * j + e, E.rbuf[e]);
-            }
+        for (int u = 0; u < 4; ++u) {
+          v[u] = b + u >= off && b + u < hix;
+          X0[u] = X1[u] = X2[u] = 0.0;
+          pj[u] = 0;
+          mj[u] = kPlainMeta;
+          if (v[u]) {
+            const XPack* xp = A.xpk + min(slot4[u], unsigned(nat - 1));
+            const double2 w0 = __ldg(reinterpret_cast<const double2*>(xp));
+            const int4 w1 = __ldg(reinterpret_cast<const int4*>(xp) + 1);
+            X0[u] = w0.x;
+            X1[u] = w0.y;
+            X2[u] = __hiloint2double(w1.y, w1.x);
+            pj[u] = w1.z;
+            mj[u] = unsigned(w1.w);
           }
         }
-        __syncwarp();
-      };
-      if (npass > 0) {
-        Ld c0, c1, n0, n1;
-        load(lane - off, c0);
-        load(32 + lane - off, c1);
-        for (int j = 0; j < npass; j += 2) {
-          load(32 * (j + 2) + lane - off, n0);  // two passes' gathers in flight while two are finished
-          load(32 * (j + 3) + lane - off, n1);
-          finish(j, c0);
-          if (j + 1 < npass) finish(j + 1, c1);
-          c0 = n0;
-          c1 = n1;
+        TI Iv[4], Jv[4], Sv[12];
+        double Rv[12];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int a = int(info[u] & 31u);
+          const double* xi = E.xi[a];
+          int S0 = int((info[u] >> 5) & 3u) - 1, S1 = int((info[u] >> 7) & 3u) - 1, S2 = int((info[u] >> 9) & 3u) - 1;
+          if (!plain) {  // windings or exact atoms: S = s_loop + wi - wj
+            const double xj[3] = {X0[u], X1[u], X2[u]};
+            int S[3];
+            pair_S(g, xi, xj, E.mi[a], cand_word(cand_base(S0, S1, S2), mj[u]), S);
+            S0 = S[0];
+            S1 = S[1];
+            S2 = S[2];
+          }
+          Iv[u] = TI(ti0 + a);
+          Jv[u] = TI(pj[u]);
+          Sv[3 * u + 0] = TI(S0);
+          Sv[3 * u + 1] = TI(S1);
+          Sv[3 * u + 2] = TI(S2);
+          if (oR) {
+            double R0 = dsub(X0[u], xi[0]), R1 = dsub(X1[u], xi[1]), R2 = dsub(X2[u], xi[2]);
+            const bool nz = v[u] && (S0 | S1 | S2) != 0;
+            if (__any_sync(0xffffffffu, nz)) {
+              if (nz) {
+                double c0, c1, c2;
+                if (abs(S0) <= kCsR && abs(S1) <= kCsR && abs(S2) <= kCsR) {
+                  const double* tb = cs_blk + 3 * ((S0 + kCsR) + kCsN * ((S1 + kCsR) + kCsN * (S2 + kCsR)));
+                  c0 = tb[0];
+                  c1 = tb[1];
+                  c2 = tb[2];
+                } else {
+                  c0 = cts_k(g.C, S0, S1, S2, 0);
+                  c1 = cts_k(g.C, S0, S1, S2, 1);
+                  c2 = cts_k(g.C, S0, S1, S2, 2);
+                }
+                R0 = dadd(R0, c0);
+                R1 = dadd(R1, c1);
+                R2 = dadd(R2, c2);
+              }
+            }
+            if (negzero && !nz) {  // a -0 coordinate: RN(d + C'(0,0,0)) differs from d when d is -0
+              R0 = add_signed_zero(R0, zc[0]);
+              R1 = add_signed_zero(R1, zc[1]);
+              R2 = add_signed_zero(R2, zc[2]);
+            }
+            Rv[3 * u + 0] = R0;
+            Rv[3 * u + 1] = R1;
+            Rv[3 * u + 2] = R2;
+          }
+        }
+        if (vec_ok && b >= off && b + 4 <= hix) {  // four whole pairs: 16-byte vectors
+          if constexpr (sizeof(TI) == 4) {
+            __stcs(reinterpret_cast<int4*>(oi + b), make_int4(Iv[0], Iv[1], Iv[2], Iv[3]));
+            __stcs(reinterpret_cast<int4*>(oj + b), make_int4(Jv[0], Jv[1], Jv[2], Jv[3]));
+#pragma unroll
+            for (int w = 0; w < 3; ++w)
+              __stcs(reinterpret_cast<int4*>(oS + 3 * b) + w, make_int4(Sv[4 * w], Sv[4 * w + 1], Sv[4 * w + 2], Sv[4 * w + 3]));
+          } else {
+#pragma unroll
+            for (int w = 0; w < 2; ++w) {
+              __stcs(reinterpret_cast<longlong2*>(oi + b) + w, make_longlong2(Iv[2 * w], Iv[2 * w + 1]));
+              __stcs(reinterpret_cast<longlong2*>(oj + b) + w, make_longlong2(Jv[2 * w], Jv[2 * w + 1]));
+            }
+#pragma unroll
+            for (int w = 0; w < 6; ++w)
+              __stcs(reinterpret_cast<longlong2*>(oS + 3 * b) + w, make_longlong2(Sv[2 * w], Sv[2 * w + 1]));
+          }
+          if (oR) {
+#pragma unroll
+            for (int w = 0; w < 6; ++w)
+              __stcs(reinterpret_cast<double2*>(oR + 3 * b) + w, make_double2(Rv[2 * w], Rv[2 * w + 1]));
+          }
+        } else if (any) {  // the chunk's ends: this lane's pairs word by word
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+            if (v[u]) {
+              __stcs(oi + b + u, Iv[u]);
+              __stcs(oj + b + u, Jv[u]);
+#pragma unroll
+              for (int k = 0; k < 3; ++k) {
+                __stcs(oS + 3 * (b + u) + k, Sv[3 * u + k]);
+                if (oR) __stcs(oR + 3 * (b + u) + k, Rv[3 * u + k]);
+              }
+            }
         }
       }
       __syncwarp();
@@ -2109,6 +2293,7 @@ __device__ __forceinline__ void pair_R_lane(const Geometry& g, const double* cs_
 
 template <typename TI, bool BATCH>
 __global__ void __launch_bounds__(128) k_lazy_lists(PairArgs<TI> A) {
+  if (!BATCH && A.sym && *A.sym_fail == 0) return;  // the fused symmetric pass summed
   __shared__ double cs_blk[BATCH ? 1 : 3 * kCsN * kCsN * kCsN];
   if (!BATCH) {
     for (int t = threadIdx.x; t < 3 * kCsN * kCsN * kCsN; t += blockDim.x) cs_blk[t] = A.cs_table[t];
@@ -2234,7 +2419,7 @@ static void launch_modes(int mode, const PairArgs<TI>& a, int num_sms, cudaStrea
           const int sbps = a.pair_blocks_per_sm > 0 ? a.pair_blocks_per_sm : 2 * NL_SC_MIN_BLOCKS;
           long long sb = ((long long)a.ncells_total + kSCWarps - 1) / kSCWarps;
           if (sb > (long long)num_sms * sbps) sb = (long long)num_sms * sbps;
-          k_sym_count<TI><<<int(sb), kSCWarps * 32, 0, st>>>(a);
+          k_sym_count<TI, kSymMasks><<<int(sb), kSCWarps * 32, 0, st>>>(a);
         }
       }
       if (a.count_kernel != 2) {  // default: one warp per home cell
@@ -2275,6 +2460,22 @@ static void launch_modes(int mode, const PairArgs<TI>& a, int num_sms, cudaStrea
       break;
   }
 }
+
+template <typename TI>
+void launch_sym_lazy(int what, const PairArgs<TI>& a, int num_sms, cudaStream_t st) {
+  if (a.nat_total <= 0 || a.ncells_total <= 0) return;
+  const int sbps = a.pair_blocks_per_sm > 0 ? a.pair_blocks_per_sm : 2 * NL_SC_MIN_BLOCKS;
+  long long sb = ((long long)a.ncells_total + kSCWarps - 1) / kSCWarps;
+  if (sb > (long long)num_sms * sbps) sb = (long long)num_sms * sbps;
+  if (what == kLazyCounts) {
+    k_sym_count<TI, kSymCounts><<<int(sb), kSCWarps * 32, 0, st>>>(a);
+  } else {
+    k_cs_table<<<1, 128, 0, st>>>(a.g, a.cs_table, nullptr, 0, a.err);
+    k_sym_count<TI, kSymInvR6><<<int(sb), kSCWarps * 32, 0, st>>>(a);
+  }
+}
+template void launch_sym_lazy<int32_t>(int, const PairArgs<int32_t>&, int, cudaStream_t);
+template void launch_sym_lazy<int64_t>(int, const PairArgs<int64_t>&, int, cudaStream_t);
 
 template <typename TI>
 void launch_pairs(int mode, const PairArgs<TI>& a, int num_sms, cudaStream_t st) {

@@ -101,6 +101,15 @@ __device__ __forceinline__ int batch_system(const int* __restrict__ first, int n
 template <typename TI>
 void launch_pairs(int mode, const PairArgs<TI>& a, int num_sms, cudaStream_t st);
 
+// The fused symmetric lazy passes of single systems whose 27-cell stencil has
+// distinct cells: per-atom counts (into a.counts, zeroed by the caller) or
+// per-atom sums of 1/r^6 (into a.per_atom, zeroed by the caller).  A cell of
+// more than 32 atoms sets a.sym_fail; the caller's per-cell passes (gated on
+// it) then redo the whole reduction.
+enum LazyWhat : int { kLazyCounts = 0, kLazyInvR6 = 1 };
+template <typename TI>
+void launch_sym_lazy(int what, const PairArgs<TI>& a, int num_sms, cudaStream_t st);
+
 // R = (X[j] - X[i]) + C'S of an existing list; largest squared displacement
 template <typename TI>
 void launch_pair_vectors(const Geometry& g, const double* X, const TI* pi, const TI* pj, const TI* pS,

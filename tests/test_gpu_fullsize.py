@@ -73,6 +73,9 @@ def test_lazy_r6_1m_against_fp64_oracle(nlpkg, orc):
     ref = orc.lazy_sum_r6(orc.build_cell_list(X, 5.0, C, (True, True, True)), nthreads=THREADS)
     rel = np.abs(got - ref) / np.maximum(np.abs(ref), 1e-300)
     assert rel.max() <= LAZY_RTOL, rel.max()
+    fast = nlpkg.lazy_reduce(clist, "inv_r6_fast").cpu().numpy()  # the fused symmetric pass
+    rel = np.abs(fast - ref) / np.maximum(np.abs(ref), 1e-300)
+    assert rel.max() <= LAZY_RTOL, rel.max()
     cnt = nlpkg.lazy_reduce(clist, "count").cpu().numpy().astype(np.int64)
     assert np.array_equal(cnt, np.diff(eng.first.cpu().numpy().astype(np.int64)))
     del eng

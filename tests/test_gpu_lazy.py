@@ -74,3 +74,57 @@ def test_query_rejects_out_of_range_atoms(nlpkg):
     with pytest.raises(nlpkg.NLError):
         nlpkg.query_neighbours(clist, [1, 1001])
     assert nlpkg.count_neighbours(clist, 1000) >= 0  # the error word was cleared
+
+
+LAZY_RTOL = 1e-12  # the fused pass's stated relative tolerance on the per-atom sums
+
+
+@pytest.mark.parametrize("case", range(6))
+def test_fused_lazy_sum_and_count(nlpkg, orc, case):
+    """The fused symmetric lazy pass (NL_REDUCE_INV_R6_FAST): per-atom sums of
+    1/r^6 within 1e-12 of the oracle's FP64 traversal, per-atom counts equal
+    to the oracle's, on geometries it takes (cubic, mixed and open boundaries,
+    sheared triclinic, atoms far outside an open axis) and on ones it hands
+    to the traversal-order passes (the diamond cell's 5x5x5 stencil)."""
+    X, C, rc, pbc = _cases()[case]
+    clist = nlpkg.build_cell_list(torch.from_numpy(np.ascontiguousarray(X)).cuda(), rc, C, pbc)
+    oc = orc.build_cell_list(X, rc, C, pbc)
+    ref = orc.lazy_sum_r6(oc)
+    got = nlpkg.lazy_reduce(clist, "inv_r6_fast").cpu().numpy()
+    rel = np.abs(got - ref) / np.maximum(np.abs(ref), 1e-300)
+    assert rel.max() <= LAZY_RTOL, rel.max()
+    o = orc.neighbour_list(X, rc, C, pbc, nthreads=8)
+    cnt = nlpkg.lazy_reduce(clist, "count").cpu().numpy().astype(np.int64)
+    assert np.array_equal(cnt, np.diff(o.first))
+
+
+def test_fused_lazy_crowded_cell_falls_back(nlpkg, orc):
+    """A cell of more than 32 atoms: the fused pass gives up and the
+    traversal-order passes produce every sum (then bit-identical)."""
+    rng = np.random.default_rng(18)
+    X, C, L = cf.rand_config(3000, seed=19)
+    X = np.concatenate([X, L / 2 + (rng.random((60, 3)) - 0.5) * 0.8])
+    clist = nlpkg.build_cell_list(torch.from_numpy(X).cuda(), 5.0, C, (True, True, True))
+    ref = orc.lazy_sum_r6(orc.build_cell_list(X, 5.0, C, (True, True, True)))
+    got = nlpkg.lazy_reduce(clist, "inv_r6_fast").cpu().numpy()
+    assert np.array_equal(got.view(np.int64), ref.view(np.int64))
+    o = orc.neighbour_list(X, 5.0, C, (True, True, True), nthreads=8)
+    assert np.array_equal(nlpkg.lazy_reduce(clist, "count").cpu().numpy().astype(np.int64), np.diff(o.first))
+
+
+def test_fused_lazy_close_pairs(nlpkg, orc):
+    """Pairs at distances down to 1e-9 A and coincident atoms: the close ones
+    are evaluated in FP64 with the reference's formula (an exact zero
+    distance gives +Inf, as 1/0 does in the reference)."""
+    X, C, L = cf.rand_config(4000, seed=20)
+    X = X.copy()
+    for k, d in enumerate([1e-9, 1e-6, 1e-3, 0.05, 0.5]):
+        X[2 * k + 1] = X[2 * k] + np.array([d, 0.0, 0.0])
+    X[20] = X[21]  # coincident
+    clist = nlpkg.build_cell_list(torch.from_numpy(X).cuda(), 5.0, C, (True, True, True))
+    ref = orc.lazy_sum_r6(orc.build_cell_list(X, 5.0, C, (True, True, True)))
+    got = nlpkg.lazy_reduce(clist, "inv_r6_fast").cpu().numpy()
+    fin = np.isfinite(ref)
+    assert np.array_equal(np.isfinite(got), fin) and np.all(got[~fin] == ref[~fin])
+    rel = np.abs(got[fin] - ref[fin]) / np.abs(ref[fin])
+    assert rel.max() <= LAZY_RTOL, rel.max()
