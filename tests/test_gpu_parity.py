@@ -599,3 +599,49 @@ def test_fill_follows_the_count_choice(nlpkg, orc):
         np.testing.assert_array_equal(to_np(j).astype(np.int64), o.j)
         np.testing.assert_array_equal(to_np(S).astype(np.int64), o.S)
         assert np.array_equal(to_np(R).view(np.int64), o.R.view(np.int64))
+
+
+@pytest.mark.parametrize("int_type", [torch.int32, torch.int64])
+def test_unaligned_output_arrays(nlpkg, orc, int_type):
+    """Pair arrays that do not start on 16-byte boundaries (views one element
+    into larger buffers) take the write pass's word-by-word stores: same
+    bits as the oracle, nothing written outside the views."""
+    import ctypes as C
+    X, Cm, L = cf.rand_config(20000, seed=95)
+    pbc = (True, True, True)
+    plan = nlpkg.analyze_cell(Cm, 5.0, int_type)
+    nat = X.shape[0]
+    dev = torch.device("cuda")
+    ib = 4 if int_type == torch.int32 else 8
+    o = orc.neighbour_list(X, 5.0, Cm, pbc, ti_bytes=ib, nthreads=8)
+    P = o.npairs
+    bufs = {k: torch.zeros((P + 8) * w, dtype=dt, device=dev) for k, w, dt in
+            (("i", 1, int_type), ("j", 1, int_type), ("S", 3, int_type), ("R", 3, torch.float64))}
+    views = {"i": bufs["i"][1:P + 1], "j": bufs["j"][1:P + 1], "S": bufs["S"][3:3 * P + 3],
+             "R": bufs["R"][3:3 * P + 3]}
+    ws = torch.empty(int(nlpkg.lib().nl_workspace_bytes(nat, plan.ncells_total)), dtype=torch.uint8, device=dev)
+    perm, cid = torch.empty(nat, dtype=int_type, device=dev), torch.empty(nat, dtype=int_type, device=dev)
+    Xs = torch.empty((nat, 3), dtype=torch.float64, device=dev)
+    offs = torch.empty(plan.ncells_total + 1, dtype=int_type, device=dev)
+    first = torch.empty(nat + 1, dtype=int_type, device=dev)
+    pb = np.ones(3, dtype=np.uint8)
+    total = C.c_int64(-1)
+    D, I64, U8 = C.POINTER(C.c_double), C.POINTER(C.c_int64), C.POINTER(C.c_uint8)
+    Xd = torch.from_numpy(X).cuda()
+    torch.cuda.synchronize()
+
+    def p(t):
+        return C.c_void_p(t.data_ptr())
+
+    st = nlpkg.lib().nl_neighbour_list(p(Xd), nat, plan.cell_cm.ctypes.data_as(D), plan.inv_cm.ctypes.data_as(D),
+                                       plan.ncells.ctypes.data_as(I64), plan.nxyz.ctypes.data_as(I64),
+                                       pb.ctypes.data_as(U8), 5.0, ib, p(perm), p(Xs), p(cid), p(offs), p(first), P,
+                                       p(views["i"]), p(views["j"]), p(views["S"]), p(views["R"]), C.byref(total),
+                                       p(ws), ws.numel(), C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert st == 0 and total.value == P
+    assert np.array_equal(views["i"].cpu().numpy().astype(np.int64), o.i)
+    assert np.array_equal(views["j"].cpu().numpy().astype(np.int64), o.j)
+    assert np.array_equal(views["S"].cpu().numpy().reshape(-1, 3).astype(np.int64), o.S)
+    assert np.array_equal(views["R"].cpu().numpy().reshape(-1, 3).view(np.int64), o.R.view(np.int64))
+    for k, w in (("i", 1), ("j", 1), ("S", 3), ("R", 3)):  # nothing written outside the views
+        assert torch.all(bufs[k][:w] == 0) and torch.all(bufs[k][w * (P + 1):] == 0), k
