@@ -384,6 +384,31 @@ def bench_batched(nl, dev, stream, flush, steps):
 
     plain_steps = max(1, min(steps, 2))
     plain_ms = timed_steps(plain, plain_steps, flush, stream)
+    # the same per-system calls with the host out of the way: every system's
+    # call captured in its own CUDA graph, the graphs replayed one after
+    # another on one stream, and round-robin on eight streams (systems overlap
+    # on the device)
+    for e, v in zip(engines, views):
+        e.capture(v)
+    torch.cuda.synchronize(dev)
+
+    def plain_graphs():
+        for e in engines:
+            e.replay()
+
+    plain_graph_ms = timed_steps(plain_graphs, plain_steps, flush, stream)
+    side = [torch.cuda.Stream(device=dev) for _ in range(8)]
+
+    def plain_streams():
+        for st in side:
+            st.wait_stream(stream)
+        for k, e in enumerate(engines):
+            with torch.cuda.stream(side[k % 8]):
+                e.replay()
+        for st in side:
+            stream.wait_stream(st)
+
+    plain_streams_ms = timed_steps(plain_streams, plain_steps, flush, stream)
     # bit-identical outputs (every system)
     po = b.pair_offsets_host()
     same = True
@@ -400,7 +425,13 @@ def bench_batched(nl, dev, stream, flush, steps):
             "systems_per_s": nsys / (batch_ms * 1e-3), "ms_per_batch": batch_ms,
             "pairs_per_s": total / (batch_ms * 1e-3),
             "plain_systems_per_s": nsys / (plain_ms * 1e-3), "plain_ms": plain_ms,
-            "speedup_vs_plain": plain_ms / batch_ms, "identical_to_plain": bool(same),
+            "plain_graphs_ms": plain_graph_ms, "plain_graphs_8_streams_ms": plain_streams_ms,
+            "plain_note": "plain_ms: one engine.launch per system from Python; plain_graphs_ms: each system's "
+                          "call as its own CUDA graph, replayed back to back on one stream; "
+                          "plain_graphs_8_streams_ms: the same graphs round-robin on eight streams",
+            "speedup_vs_plain": plain_ms / batch_ms,
+            "speedup_vs_plain_graphs": min(plain_graph_ms, plain_streams_ms) / batch_ms,
+            "identical_to_plain": bool(same),
             "cuda_graph": True, "autotune": {k: tune[k] for k in ("pair_blocks_per_sm", "emit_blocks_per_sm", "count_kernel", "ms")},
             "l2": "flushed before every timed step"}
 
@@ -450,20 +481,27 @@ def bench_serving(nl, dev, rates=(1_000, 5_000, 20_000, 50_000), n_req=1_500):
     systems = [(torch.from_numpy(x).pin_memory(), c, rc, p) for (x, c, rc, p) in serving_requests(n_req)]
     out = {"workload": f"{n_req} requests per rate: the batched distribution (4,096-system config) with 5% "
                        "large systems of 50k-200k atoms (density 0.05, rc 5 A); Poisson arrivals; 40 GB pair "
-                       "budget; pinned request buffers; latency = arrival to results on the device",
+                       "budget; pinned request buffers; latency = arrival to results on the device, and for the "
+                       "*_to_host modes arrival to results (first, i, j, S, R) copied into pinned host memory",
            "rates": {}}
     for mode in ("batched", "plain"):
-        srv = nl.NeighbourListServer(device=dev, mode=mode)
-        # warm-up at the highest rate: the arenas grow to their working size once
-        srv.run_trace(nl.poisson_trace(systems, rates[-1], seed=1))
-        for rate in rates:
-            srv.batches = srv.reruns = 0
-            st = srv.run_trace(nl.poisson_trace(systems, rate, seed=int(rate)))
-            out["rates"].setdefault(str(rate), {})[mode] = {k: st[k] for k in (
-                "p50_ms", "p99_ms", "systems_per_s", "pairs_per_s", "batches", "reruns")}
-        srv.close()
+        for host in (False, True):
+            srv = nl.NeighbourListServer(device=dev, mode=mode, host_results=host)
+            key = mode + ("_to_host" if host else "")
+            # warm-up at the highest rate: the arenas grow to their working size once
+            srv.run_trace(nl.poisson_trace(systems, rates[-1], seed=1))
+            for rate in rates:
+                srv.batches = srv.reruns = 0
+                st = srv.run_trace(nl.poisson_trace(systems, rate, seed=int(rate)))
+                out["rates"].setdefault(str(rate), {})[key] = {k: st[k] for k in (
+                    "p50_ms", "p99_ms", "systems_per_s", "pairs_per_s", "batches", "reruns")}
+            srv.close()
+            del srv
+            torch.cuda.empty_cache()
     top = out["rates"][str(rates[-1])]
     out["speedup_vs_plain_at_max_rate"] = top["batched"]["systems_per_s"] / top["plain"]["systems_per_s"]
+    out["speedup_vs_plain_at_max_rate_to_host"] = (top["batched_to_host"]["systems_per_s"] /
+                                                   top["plain_to_host"]["systems_per_s"])
     return out
 
 
@@ -549,15 +587,19 @@ def measure_e2e(eng, X, Xd, total, stream, dev, args):
     next step's kernels; each step still moves its own inputs and outputs."""
     import torch
 
+    from neighbourlists_gb300 import numa
+
     n_atoms = X.shape[0]
     ti = eng.ti
-    hX = torch.from_numpy(X).pin_memory()
+    node = numa.gpu_numa_node(dev)  # host buffers on the GPU's own NUMA node
+    hX = numa.pinned_on_node((n_atoms, 3), torch.float64, node)
+    hX.copy_(torch.from_numpy(X))
 
     def host_outputs():
-        return {"first": torch.empty(n_atoms + 1, dtype=ti).pin_memory(),
-                "i": torch.empty(total, dtype=ti).pin_memory(), "j": torch.empty(total, dtype=ti).pin_memory(),
-                "S": torch.empty((total, 3), dtype=ti).pin_memory(),
-                "R": torch.empty((total, 3), dtype=torch.float64).pin_memory()}
+        return {"first": numa.pinned_on_node(n_atoms + 1, ti, node),
+                "i": numa.pinned_on_node(total, ti, node), "j": numa.pinned_on_node(total, ti, node),
+                "S": numa.pinned_on_node((total, 3), ti, node),
+                "R": numa.pinned_on_node((total, 3), torch.float64, node)}
 
     eng2 = type(eng)(n_atoms, eng.cell, eng.cutoff, tuple(bool(b) for b in eng.pbc), int_type=ti, device=dev,
                      capacity=eng.capacity)
@@ -591,7 +633,41 @@ def measure_e2e(eng, X, Xd, total, stream, dev, args):
     d2h = (h_i.numel() * h_i.element_size() + h_j.numel() * h_j.element_size() + h_S.numel() * h_S.element_size()
            + h_R.numel() * 8 + h_f.numel() * h_f.element_size())
     return {"value": None, "unit": "pairs/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-            "ms_per_step": e2e_ms, "api": "NeighbourListEngine.launch_host, two engines taking steps in turn"}
+            "ms_per_step": e2e_ms, "api": "NeighbourListEngine.launch_host, two engines taking steps in turn",
+            "placement": {"gpu_numa_node": node, "output_R_pages_by_node": numa.page_nodes(h_R),
+                          "d2h_gbs_by_host_node": d2h_by_node(dev, stream)}}
+
+
+def d2h_bandwidth(dev, stream, host):
+    """GB/s of one device-to-host copy of 1 GiB into a pinned buffer."""
+    import torch
+
+    src = torch.empty(host.numel(), dtype=torch.uint8, device=dev)
+    host.copy_(src, non_blocking=True)
+    torch.cuda.synchronize(dev)
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record(stream)
+    for _ in range(3):
+        host.copy_(src, non_blocking=True)
+    e.record(stream)
+    torch.cuda.synchronize(dev)
+    return 3 * host.numel() / (s.elapsed_time(e) * 1e-3) / 1e9
+
+
+def d2h_by_node(dev, stream):
+    """Device-to-host copy bandwidth into pinned memory placed on each NUMA
+    node that has CPUs (the placement the end-to-end number depends on)."""
+    import torch
+    from neighbourlists_gb300 import numa
+
+    out = {}
+    for node in sorted(numa.cpu_nodes()):
+        h = numa.pinned_on_node(1 << 30, torch.uint8, node)
+        out[str(node)] = {"gbs": d2h_bandwidth(dev, stream, h), "pages_by_node": numa.page_nodes(h)}
+        del h
+    if not out:
+        out["unknown"] = {"gbs": d2h_bandwidth(dev, stream, torch.empty(1 << 30, dtype=torch.uint8).pin_memory())}
+    return out
 
 
 def run_path(args):

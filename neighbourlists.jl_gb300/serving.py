@@ -51,9 +51,10 @@ class Request:
 
     @property
     def result(self) -> Optional[dict]:
-        """first, i, j, S, R of this request (device tensors).  Views into the
-        slot's arenas are valid until that slot runs its next batch; a server
-        with ``copy_results`` hands out copies."""
+        """first, i, j, S, R of this request (device tensors; host tensors from
+        a server with ``host_results``).  Views into the slot's arenas are
+        valid until that slot runs its next batch; a server with
+        ``copy_results`` hands out copies."""
         if self._res is None:
             return None
         if isinstance(self._res, dict):
@@ -79,18 +80,29 @@ class Request:
 
 
 class _Slot:
-    """One in-flight batch: stream, completion event and resident arenas."""
+    """One in-flight batch: stream, completion events and resident arenas
+    (device buffers, and pinned host buffers for results copied back)."""
 
     def __init__(self, device):
         self.device = device
         self.stream = torch.cuda.Stream(device=device)
         self.event = torch.cuda.Event()
+        self.copy_event = torch.cuda.Event()
         self.bufs = {}
+        self.hbufs = {}
         self.h_X = None
         self.reqs: List[Request] = []
         self.handle = None
         self.pred_bytes = 0
         self.busy = False
+        self.copying = False  # the batch's results are on their way to the host
+
+    def hbuf(self, name, numel, dtype):
+        t = self.hbufs.get(name)
+        if t is None or t.numel() < numel or t.dtype != dtype:
+            t = torch.empty(max(int(numel * 1.25), 1), dtype=dtype).pin_memory()
+            self.hbufs[name] = t
+        return t
 
     def buf(self, name, numel, dtype):
         t = self.bufs.get(name)
@@ -108,7 +120,11 @@ class _Slot:
 class NeighbourListServer:
     def __init__(self, pair_budget_bytes: float = 40e9, slots: int = 3, max_batch_atoms: int = 4_000_000,
                  max_batch_systems: int = 8192, int_type=torch.int32, with_R: bool = True, device="cuda",
-                 mode: str = "batched", copy_results: bool = False):
+                 mode: str = "batched", copy_results: bool = False, host_results: bool = False):
+        """host_results: every batch's results (first, i, j, S, R) are copied
+        into pinned host memory on the slot's stream, and a request is done --
+        its latency stops -- when its results are on the host; the request's
+        ``result`` is then host tensors."""
         if mode not in ("batched", "plain"):
             raise ValueError("mode must be 'batched' or 'plain'")
         self.ib = _index_bytes(int_type)
@@ -117,6 +133,7 @@ class NeighbourListServer:
         self.device = torch.device(device)
         self.mode = mode
         self.copy_results = copy_results
+        self.host_results = host_results
         self.direct_copy_atoms = 8192  # pinned requests at least this large skip the staging copy
         self.budget = float(pair_budget_bytes)
         self.max_atoms = int(max_batch_atoms)
@@ -136,10 +153,13 @@ class NeighbourListServer:
         return bool(self.queue) or any(s.busy for s in self.slots)
 
     def poll(self, now_fn=time.perf_counter) -> List[Request]:
-        """Finishes every slot whose batch completed; returns its requests."""
+        """Finishes every slot whose batch completed (with host_results: whose
+        results reached the host); returns its requests."""
         done = []
         for s in self.slots:
-            if s.busy and s.event.query():
+            if s.busy and s.copying and s.copy_event.query():
+                done.extend(self._release(s, now_fn()))
+            elif s.busy and not s.copying and s.event.query():
                 done.extend(self._finish(s, now_fn()))
         return done
 
@@ -288,6 +308,26 @@ class NeighbourListServer:
             return self._finish(s, t_done)
         check(status)
         i, j, S, R = s.bufs["i"], s.bufs["j"], s.bufs["S"], s.bufs.get("R")
+        if self.host_results:
+            # one copy per array for the whole batch into the slot's pinned arenas
+            nf = sum(r.nat for r in s.reqs) + (len(s.reqs) if self.mode == "batched" else 1)
+            hf = s.hbuf("first", nf, self.ti)
+            hi, hj = s.hbuf("i", max(total, 1), self.ti), s.hbuf("j", max(total, 1), self.ti)
+            hS = s.hbuf("S", 3 * max(total, 1), self.ti)
+            hR = s.hbuf("R", 3 * max(total, 1), torch.float64) if R is not None else None
+            with torch.cuda.stream(s.stream):
+                hf[:nf].copy_(first[:nf], non_blocking=True)
+                if total:
+                    hi[:total].copy_(i[:total], non_blocking=True)
+                    hj[:total].copy_(j[:total], non_blocking=True)
+                    hS[:3 * total].copy_(S[:3 * total], non_blocking=True)
+                    if hR is not None:
+                        hR[:3 * total].copy_(R[:3 * total], non_blocking=True)
+                s.copy_event.record(s.stream)
+            s.copying = True
+            s.po_h = po_h
+            s.host = (hf, hi, hj, hS, hR)
+            return []
         a0 = 0
         for k, r in enumerate(s.reqs):
             p0, p1 = int(po_h[k]), int(po_h[k + 1])
@@ -297,6 +337,24 @@ class NeighbourListServer:
                 r._res = {key: (v.clone() if v is not None else None) for key, v in r.result.items()}
             r.npairs, r.t_done = p1 - p0, t_done
             a0 += r.nat
+        return self._free(s)
+
+    def _release(self, s: _Slot, t_done: float) -> List[Request]:
+        """The batch's results are on the host: hand each request its slices."""
+        hf, hi, hj, hS, hR = s.host
+        a0 = 0
+        for k, r in enumerate(s.reqs):
+            p0, p1 = int(s.po_h[k]), int(s.po_h[k + 1])
+            f0 = a0 + k if self.mode == "batched" else 0
+            r._res = (hf, hi, hj, hS, hR, f0, p0, p1)
+            if self.copy_results:  # the pinned arenas are reused by the slot's next batch
+                r._res = {key: (v.clone() if v is not None else None) for key, v in r.result.items()}
+            r.npairs, r.t_done = p1 - p0, t_done
+            a0 += r.nat
+        s.copying = False
+        return self._free(s)
+
+    def _free(self, s: _Slot) -> List[Request]:
         done = s.reqs
         s.reqs, s.busy = [], False
         self.inflight_bytes -= s.pred_bytes

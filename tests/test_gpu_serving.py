@@ -68,3 +68,18 @@ def test_budget_bounds_admission_and_reruns(nlpkg, monkeypatch):
     assert stats["reruns"] > 0
     for x, y in zip(ref, got):
         assert same(x.result, y.result)
+
+
+def test_host_results_match_device_results(nlpkg):
+    """With host_results the latency stops when a request's results are in
+    pinned host memory: the same bits as the device results, every request."""
+    systems = mixed_systems()[:14]
+    dev, _, _ = serve(nlpkg, systems, slots=2)
+    host, stats, _ = serve(nlpkg, systems, slots=2, host_results=True)
+    assert stats["requests"] == len(systems)
+    for a, b in zip(dev, host):
+        assert not b.result["i"].is_cuda
+        assert same({k: v.cpu() for k, v in a.result.items()}, b.result), a.rid
+    plain, _, _ = serve(nlpkg, systems, slots=2, mode="plain", host_results=True)
+    for a, b in zip(dev, plain):
+        assert same({k: v.cpu() for k, v in a.result.items()}, b.result), a.rid

@@ -367,3 +367,20 @@ def test_autotune_candidates_and_choice(nlpkg, monkeypatch):
     res = tuning.autotune(r, None, candidates=[(4, 8), (14, 32, 2)], reps=1)
     assert [(t["pair_blocks_per_sm"], t["emit_blocks_per_sm"], t["count_kernel"]) for t in res["trials"]] == \
         [(4, 8, 0), (14, 32, 2)]
+
+
+def test_numa_helpers_on_the_host(nlpkg):
+    """The NUMA helpers of the end-to-end buffers: CPU lists parse, and a
+    buffer's pages are reported on an existing node."""
+    import torch
+    from neighbourlists_gb300 import numa
+
+    nodes = numa.cpu_nodes()
+    if not nodes:
+        pytest.skip("no NUMA information on this host")
+    for node, cpus in nodes.items():
+        assert cpus and cpus == numa.node_cpus(node)
+    t = torch.zeros(1 << 22, dtype=torch.uint8)
+    where = numa.page_nodes(t)
+    assert where and sum(where.values()) > 0
+    assert numa.node_cpus(10**6) == set()
