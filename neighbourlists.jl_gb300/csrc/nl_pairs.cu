@@ -1144,8 +1144,9 @@ struct __align__(16) LZSmem {
   int cslot[14 * 32];      // candidate: sorted slot
   unsigned ccw[14 * 32];   //   candidate word (loop shift, windings)
   double csum[14 * 32];    //   sum over its column (forward cells)
-  unsigned q[128];         // queued pairs
+  unsigned q[128];         // queued pairs (a ring)
 };
+constexpr int kLZRing = 128;
 
 // Double-float (unevaluated FP32 pairs, hi + lo): Dekker's and Knuth's
 // error-free products and sums (about 48 significant bits).
@@ -1189,7 +1190,8 @@ __device__ __forceinline__ double f2d_exact(float x) {
   return __hiloint2double(int(hi), int((u & 0x7u) << 29));
 }
 
-// Evaluates n <= 32 queued pairs of the lazy reduction, one per lane: R with
+// Evaluates the n <= 32 queued pairs from ring position head of the lazy
+// reduction, one per lane: R with
 // the reference's FP64 operations (gpu_kernels.jl:88-91), r2 and 1/r2^3 in
 // double-float (relative error far below 1e-12), then the atom's row sum and,
 // for a forward candidate, its column sum.  r2 below 1e-12 (where 1/r2^3
@@ -1197,9 +1199,9 @@ __device__ __forceinline__ double f2d_exact(float x) {
 // in FP64 with the reference's formula.
 template <typename TI>
 __device__ __forceinline__ void lazy_flush(const PairArgs<TI>& A, const Geometry& g, const double* cs_tab, LZSmem& W,
-                                           int n, int lane) {
+                                           int head, int n, int lane) {
   const bool act = lane < n;
-  const unsigned e = act ? W.q[lane] : 0u;
+  const unsigned e = act ? W.q[(head + lane) & (kLZRing - 1)] : 0u;
   const int a = int(e & 31u), fi = int(e >> 6);
   const double* xi = W.hX[a];
   const int sj = W.cslot[fi];
@@ -1346,7 +1348,7 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
       }
       const int T = __shfl_sync(0xffffffffu, incl, 31);
       const int nr = (T + 31) >> 5;  // <= kSCMaxRounds
-      int qn = 0;  // sum of 1/r^6: accepted pairs queued (flushed 32 at a time with full lanes)
+      int qh = 0, qt = 0;  // sum of 1/r^6: ring of accepted pairs (flushed 32 at a time with full lanes)
       __syncwarp();
       for (int rr = 0; rr < nr; ++rr) {
         const int f = 32 * rr + lane;
@@ -1438,23 +1440,20 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
             // queue every accepted pair: (home atom, candidate, forward flag); a
             // pair of the centre is met from both of its atoms and added to
             // each atom's own row, a forward pair to the row and the column
+            // (a ring of kLZRing entries: at most 31 + 64 are queued before a flush)
             const unsigned lt = lt_mask();
             if ((row0 >> lane) & 1u)
-              W.q[qn + __popc(row0 & lt)] = unsigned(a) | (((cm0 >> lane) & 1u) << 5) | (unsigned(f) << 6);
-            qn += __popc(row0);
+              W.q[(qt + __popc(row0 & lt)) & (kLZRing - 1)] =
+                  unsigned(a) | (((cm0 >> lane) & 1u) << 5) | (unsigned(f) << 6);
+            qt += __popc(row0);
             if ((row1 >> lane) & 1u)
-              W.q[qn + __popc(row1 & lt)] = unsigned(a + 1) | (((cm1 >> lane) & 1u) << 5) | (unsigned(f) << 6);
-            qn += __popc(row1);
-            if (qn >= 32) {
+              W.q[(qt + __popc(row1 & lt)) & (kLZRing - 1)] =
+                  unsigned(a + 1) | (((cm1 >> lane) & 1u) << 5) | (unsigned(f) << 6);
+            qt += __popc(row1);
+            while (qt - qh >= 32) {
               __syncwarp();
-              lazy_flush<TI>(A, g, cs_blk, W, 32, lane);
-              const unsigned rest = lane + 32 < qn ? W.q[lane + 32] : 0u;  // qn <= 96
-              const unsigned rest2 = lane + 64 < qn ? W.q[lane + 64] : 0u;
-              __syncwarp();
-              if (lane + 32 < qn) W.q[lane] = rest;
-              if (lane + 64 < qn) W.q[lane + 32] = rest2;
-              qn -= 32;
-              __syncwarp();
+              lazy_flush<TI>(A, g, cs_blk, W, qh, 32, lane);
+              qh += 32;
             }
           }
           if constexpr (SM != kSymInvR6) col |= (((cm0 >> lane) & 1u) << a) | (((cm1 >> lane) & 1u) << (a + 1));
@@ -1470,7 +1469,8 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
       }
       __syncwarp();
       if constexpr (SM == kSymInvR6) {
-        if (qn > 0) lazy_flush<TI>(A, g, cs_blk, W, qn, lane);
+        __syncwarp();
+        if (qt > qh) lazy_flush<TI>(A, g, cs_blk, W, qh, qt - qh, lane);
         __syncwarp();
         // the cell's sums: its atoms' rows and its forward candidates' columns
         if (lane < nb) atomicAdd(A.per_atom + W.horig[lane], W.hsum[lane]);
@@ -1900,7 +1900,6 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
   const int sw = *A.sym_wound;
   const bool plain = (sw & 1) == 0;   // no atom has a winding or is exact: S = the loop shift
   const bool negzero = (sw & 2) != 0;  // a coordinate is -0: R needs the signed-zero rule for S = 0
-  const bool vec_ok = A.vec_ok != 0;
   const unsigned* masks = reinterpret_cast<const unsigned*>(A.lists);
   const long long cap = A.capacity;
   const double* zc = cs_blk + 3 * ((kCsN * kCsN + kCsN + 1) * kCsR);  // C'(0,0,0): signed zeros
@@ -2001,137 +2000,109 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
         }
       }
       __syncwarp();
-      // ---- emission: lane r of round t writes the four output positions
-      // p0 + 4 (32 t + r) .. + 3 (p0 = G rounded down to a multiple of 32):
-      // entries [4 g, 4 g + 4) with two 16-byte shared loads, four gathers in
-      // flight, and i, j, S, R of the four pairs as 16-byte vector stores
-      // (word by word at the chunk's ends or for unaligned arrays)
+      // ---- emission: lane r of pass j writes output position p0 + 32 j + r
+      // (p0 = G rounded down to a multiple of 32), entry 32 j + r: i and j as
+      // one word per lane, S and R as three words per lane (each store
+      // instruction covers a contiguous run of the arrays).  The gathers of
+      // the next two passes are in flight while two passes are written.
       const int off = int(G & 31);
       const int lim = int(max(min((long long)cnt, cap - G), 0LL));  // entries that fit the buffers
       if ((long long)cnt > cap - G && lane == l0) bad |= kFlagCapacity;
       const int hix = off + lim;  // entries [off, hix) are this chunk's pairs
+      const int npass = (hix + 31) >> 5;
       const long long p0 = G - off;
       TI* __restrict__ oi = A.oi + p0;
       TI* __restrict__ oj = A.oj + p0;
       TI* __restrict__ oS = A.oS + 3 * p0;
       double* __restrict__ oR = A.oR ? A.oR + 3 * p0 : nullptr;
       const TI ti0 = TI(o0 + 1);  // i of atom a is ti0 + a
-      const int ngroups = (hix + 3) >> 2;
-      for (int g0 = 0; g0 < ngroups; g0 += 32) {
-        const int b = 4 * (g0 + lane);
-        const bool any = b < hix;
-        uint4 e01 = make_uint4(0u, 0u, 0u, 0u), e23 = e01;
-        if (any) {
-          e01 = reinterpret_cast<const uint4*>(E.ent)[b >> 1];
-          e23 = reinterpret_cast<const uint4*>(E.ent)[(b >> 1) + 1];
+      struct Ld {
+        double x0, x1, x2;
+        int pj;
+        unsigned mj, info;
+      };
+      auto load = [&](int k, Ld& u) {
+        u.info = 0u;
+        u.x0 = u.x1 = u.x2 = 0.0;
+        u.pj = 0;
+        u.mj = kPlainMeta;
+        if (k >= off && k < hix) {
+          const uint2 en = E.ent[k];
+          u.info = en.y;
+          const XPack* xp = A.xpk + min(en.x, unsigned(nat - 1));
+          const double2 w0 = __ldg(reinterpret_cast<const double2*>(xp));
+          const int4 w1 = __ldg(reinterpret_cast<const int4*>(xp) + 1);
+          u.x0 = w0.x;
+          u.x1 = w0.y;
+          u.x2 = __hiloint2double(w1.y, w1.x);
+          u.pj = w1.z;
+          u.mj = unsigned(w1.w);
         }
-        const unsigned slot4[4] = {e01.x, e01.z, e23.x, e23.z}, info[4] = {e01.y, e01.w, e23.y, e23.w};
-        double X0[4], X1[4], X2[4];
-        int pj[4];
-        unsigned mj[4];
-        bool v[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          v[u] = b + u >= off && b + u < hix;
-          X0[u] = X1[u] = X2[u] = 0.0;
-          pj[u] = 0;
-          mj[u] = kPlainMeta;
-          if (v[u]) {
-            const XPack* xp = A.xpk + min(slot4[u], unsigned(nat - 1));
-            const double2 w0 = __ldg(reinterpret_cast<const double2*>(xp));
-            const int4 w1 = __ldg(reinterpret_cast<const int4*>(xp) + 1);
-            X0[u] = w0.x;
-            X1[u] = w0.y;
-            X2[u] = __hiloint2double(w1.y, w1.x);
-            pj[u] = w1.z;
-            mj[u] = unsigned(w1.w);
-          }
+      };
+      auto write = [&](int k, const Ld& u) {
+        const bool act = k >= off && k < hix;
+        const int a = int(u.info & 31u);
+        const double* xi = E.xi[a];
+        int S0 = int((u.info >> 5) & 3u) - 1, S1 = int((u.info >> 7) & 3u) - 1, S2 = int((u.info >> 9) & 3u) - 1;
+        if (!plain) {  // windings or exact atoms: S = s_loop + wi - wj
+          const double xj[3] = {u.x0, u.x1, u.x2};
+          int S[3];
+          pair_S(g, xi, xj, E.mi[a], cand_word(cand_base(S0, S1, S2), u.mj), S);
+          S0 = S[0];
+          S1 = S[1];
+          S2 = S[2];
         }
-        TI Iv[4], Jv[4], Sv[12];
-        double Rv[12];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int a = int(info[u] & 31u);
-          const double* xi = E.xi[a];
-          int S0 = int((info[u] >> 5) & 3u) - 1, S1 = int((info[u] >> 7) & 3u) - 1, S2 = int((info[u] >> 9) & 3u) - 1;
-          if (!plain) {  // windings or exact atoms: S = s_loop + wi - wj
-            const double xj[3] = {X0[u], X1[u], X2[u]};
-            int S[3];
-            pair_S(g, xi, xj, E.mi[a], cand_word(cand_base(S0, S1, S2), mj[u]), S);
-            S0 = S[0];
-            S1 = S[1];
-            S2 = S[2];
-          }
-          Iv[u] = TI(ti0 + a);
-          Jv[u] = TI(pj[u]);
-          Sv[3 * u + 0] = TI(S0);
-          Sv[3 * u + 1] = TI(S1);
-          Sv[3 * u + 2] = TI(S2);
-          if (oR) {
-            double R0 = dsub(X0[u], xi[0]), R1 = dsub(X1[u], xi[1]), R2 = dsub(X2[u], xi[2]);
-            const bool nz = v[u] && (S0 | S1 | S2) != 0;
-            if (__any_sync(0xffffffffu, nz)) {
-              if (nz) {
-                double c0, c1, c2;
-                if (abs(S0) <= kCsR && abs(S1) <= kCsR && abs(S2) <= kCsR) {
-                  const double* tb = cs_blk + 3 * ((S0 + kCsR) + kCsN * ((S1 + kCsR) + kCsN * (S2 + kCsR)));
-                  c0 = tb[0];
-                  c1 = tb[1];
-                  c2 = tb[2];
-                } else {
-                  c0 = cts_k(g.C, S0, S1, S2, 0);
-                  c1 = cts_k(g.C, S0, S1, S2, 1);
-                  c2 = cts_k(g.C, S0, S1, S2, 2);
-                }
-                R0 = dadd(R0, c0);
-                R1 = dadd(R1, c1);
-                R2 = dadd(R2, c2);
+        if (act) {
+          __stcs(oi + k, TI(ti0 + a));
+          __stcs(oj + k, TI(u.pj));
+          __stcs(oS + 3 * k + 0, TI(S0));
+          __stcs(oS + 3 * k + 1, TI(S1));
+          __stcs(oS + 3 * k + 2, TI(S2));
+        }
+        if (oR) {
+          double R0 = dsub(u.x0, xi[0]), R1 = dsub(u.x1, xi[1]), R2 = dsub(u.x2, xi[2]);
+          const bool nz = act && (S0 | S1 | S2) != 0;
+          if (__any_sync(0xffffffffu, nz)) {
+            if (nz) {
+              double c0, c1, c2;
+              if (abs(S0) <= kCsR && abs(S1) <= kCsR && abs(S2) <= kCsR) {
+                const double* tb = cs_blk + 3 * ((S0 + kCsR) + kCsN * ((S1 + kCsR) + kCsN * (S2 + kCsR)));
+                c0 = tb[0];
+                c1 = tb[1];
+                c2 = tb[2];
+              } else {
+                c0 = cts_k(g.C, S0, S1, S2, 0);
+                c1 = cts_k(g.C, S0, S1, S2, 1);
+                c2 = cts_k(g.C, S0, S1, S2, 2);
               }
+              R0 = dadd(R0, c0);
+              R1 = dadd(R1, c1);
+              R2 = dadd(R2, c2);
             }
-            if (negzero && !nz) {  // a -0 coordinate: RN(d + C'(0,0,0)) differs from d when d is -0
-              R0 = add_signed_zero(R0, zc[0]);
-              R1 = add_signed_zero(R1, zc[1]);
-              R2 = add_signed_zero(R2, zc[2]);
-            }
-            Rv[3 * u + 0] = R0;
-            Rv[3 * u + 1] = R1;
-            Rv[3 * u + 2] = R2;
+          }
+          if (negzero && !nz) {  // a -0 coordinate: RN(d + C'(0,0,0)) differs from d when d is -0
+            R0 = add_signed_zero(R0, zc[0]);
+            R1 = add_signed_zero(R1, zc[1]);
+            R2 = add_signed_zero(R2, zc[2]);
+          }
+          if (act) {
+            __stcs(oR + 3 * k + 0, R0);
+            __stcs(oR + 3 * k + 1, R1);
+            __stcs(oR + 3 * k + 2, R2);
           }
         }
-        if (vec_ok && b >= off && b + 4 <= hix) {  // four whole pairs: 16-byte vectors
-          if constexpr (sizeof(TI) == 4) {
-            __stcs(reinterpret_cast<int4*>(oi + b), make_int4(Iv[0], Iv[1], Iv[2], Iv[3]));
-            __stcs(reinterpret_cast<int4*>(oj + b), make_int4(Jv[0], Jv[1], Jv[2], Jv[3]));
-#pragma unroll
-            for (int w = 0; w < 3; ++w)
-              __stcs(reinterpret_cast<int4*>(oS + 3 * b) + w, make_int4(Sv[4 * w], Sv[4 * w + 1], Sv[4 * w + 2], Sv[4 * w + 3]));
-          } else {
-#pragma unroll
-            for (int w = 0; w < 2; ++w) {
-              __stcs(reinterpret_cast<longlong2*>(oi + b) + w, make_longlong2(Iv[2 * w], Iv[2 * w + 1]));
-              __stcs(reinterpret_cast<longlong2*>(oj + b) + w, make_longlong2(Jv[2 * w], Jv[2 * w + 1]));
-            }
-#pragma unroll
-            for (int w = 0; w < 6; ++w)
-              __stcs(reinterpret_cast<longlong2*>(oS + 3 * b) + w, make_longlong2(Sv[2 * w], Sv[2 * w + 1]));
-          }
-          if (oR) {
-#pragma unroll
-            for (int w = 0; w < 6; ++w)
-              __stcs(reinterpret_cast<double2*>(oR + 3 * b) + w, make_double2(Rv[2 * w], Rv[2 * w + 1]));
-          }
-        } else if (any) {  // the chunk's ends: this lane's pairs word by word
-#pragma unroll
-          for (int u = 0; u < 4; ++u)
-            if (v[u]) {
-              __stcs(oi + b + u, Iv[u]);
-              __stcs(oj + b + u, Jv[u]);
-#pragma unroll
-              for (int k = 0; k < 3; ++k) {
-                __stcs(oS + 3 * (b + u) + k, Sv[3 * u + k]);
-                if (oR) __stcs(oR + 3 * (b + u) + k, Rv[3 * u + k]);
-              }
-            }
+      };
+      if (npass > 0) {
+        Ld c0, c1, n0, n1;
+        load(lane, c0);
+        load(32 + lane, c1);
+        for (int j = 0; j < npass; j += 2) {
+          load(32 * (j + 2) + lane, n0);  // two passes' gathers in flight while two are written
+          load(32 * (j + 3) + lane, n1);
+          write(32 * j + lane, c0);
+          if (j + 1 < npass) write(32 * (j + 1) + lane, c1);
+          c0 = n0;
+          c1 = n1;
         }
       }
       __syncwarp();
