@@ -1160,8 +1160,10 @@ int nl_lazy_reduce(const double* d_X_sorted, const void* d_perm, const void* d_c
     // the fused symmetric passes where the stencil is 27 distinct cells; the
     // per-cell passes below are gated on their success and redo the whole
     // reduction when a cell holds more than 32 atoms
-    a.sym = (op == NL_REDUCE_COUNT || op == NL_REDUCE_INV_R6_FAST) && sym_geometry(g) ? 1 : 0;
-    if (a.sym) {
+    // (sym_gate, not sym: the count launcher reads sym as "launch the mask pass")
+    a.sym = 0;
+    a.sym_gate = (op == NL_REDUCE_COUNT || op == NL_REDUCE_INV_R6_FAST) && sym_geometry(g) ? 1 : 0;
+    if (a.sym_gate) {
       const size_t bytes = op == NL_REDUCE_COUNT ? sizeof(int) : sizeof(double);
       cudaError_t me = cudaMemsetAsync(d_out, 0, bytes * size_t(g.nat), st);
       if (me != cudaSuccess) e = me;

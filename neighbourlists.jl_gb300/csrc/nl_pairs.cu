@@ -366,7 +366,7 @@ __device__ __forceinline__ void load_system(const PairArgs<TI>& A, int s, Geomet
 template <typename TI, int MODE, bool BATCH>
 __global__ void __launch_bounds__(kPairWarps * 32, BATCH ? NL_PAIR_BATCH_MIN_BLOCKS : kMinBlocks)
     k_pairs(PairArgs<TI> A) {
-  if ((MODE == kModeCount || MODE == kModeLazyR6) && !BATCH && A.sym && *A.sym_fail == 0)
+  if ((MODE == kModeCount || MODE == kModeLazyR6) && !BATCH && (A.sym || A.sym_gate) && *A.sym_fail == 0)
     return;  // the symmetric pass counted (or summed)
   // the screening passes visit only listed cells: none listed, nothing to do
   // (the same value for every thread, so no block stops at a barrier alone)
@@ -2130,7 +2130,7 @@ constexpr int kCountThreads = 128;
 template <typename TI, bool BATCH>
 __global__ void __launch_bounds__(kCountThreads, NL_COUNT_MIN_BLOCKS) k_count_atoms(PairArgs<TI> A) {
   // the symmetric pass counted (batches run this pass only without it)
-  if (!BATCH && A.sym && *A.sym_fail == 0) return;
+  if (!BATCH && (A.sym || A.sym_gate) && *A.sym_fail == 0) return;
   __shared__ unsigned dtab_blk[BATCH ? 1 : kStencilTab];
   if (!BATCH) {
     const int tx = 2 * A.g.nxyz[0] + 1, ty = 2 * A.g.nxyz[1] + 1;
@@ -2264,7 +2264,7 @@ __device__ __forceinline__ void pair_R_lane(const Geometry& g, const double* cs_
 
 template <typename TI, bool BATCH>
 __global__ void __launch_bounds__(128) k_lazy_lists(PairArgs<TI> A) {
-  if (!BATCH && A.sym && *A.sym_fail == 0) return;  // the fused symmetric pass summed
+  if (!BATCH && (A.sym || A.sym_gate) && *A.sym_fail == 0) return;  // the fused symmetric pass summed
   __shared__ double cs_blk[BATCH ? 1 : 3 * kCsN * kCsN * kCsN];
   if (!BATCH) {
     for (int t = threadIdx.x; t < 3 * kCsN * kCsN * kCsN; t += blockDim.x) cs_blk[t] = A.cs_table[t];

@@ -73,6 +73,8 @@ struct PairArgs {
   int count_kernel;         // 1: one warp per home cell, 2: one thread per home atom (0 / 3: see sym)
   int sym;                  // count / write: each unordered cell pair screened once, neighbour masks
   int* sym_fail;            // set when a cell has more than 32 atoms: lists and the per-cell pass instead
+  int sym_gate;             // a fused symmetric lazy pass already ran (launched by the caller, not by the
+                            // count launcher): the per-cell passes run only if it set sym_fail
   int* sym_wound;           // bit 0: an atom has a winding or is exact (candidate words need its record);
                             // bit 1: a coordinate is -0 (R needs the signed-zero rule of C'S with S = 0)
   const int* sys_sym;       // batch: 1 for the systems the symmetric pass takes (27 distinct stencil cells)
