@@ -1093,6 +1093,9 @@ constexpr int kSCMaxRounds = 14;  // 14 stencil cells of at most 32 atoms
 #ifndef NL_SC_MIN_BLOCKS
 #define NL_SC_MIN_BLOCKS 6
 #endif
+#ifndef NL_SC_PACKED
+#define NL_SC_PACKED 1  // packed f32x2 pair arithmetic (0: the same operations as scalar FP32)
+#endif
 
 struct __align__(16) SCSmem {
   float hx[32], hy[32], hz[32];      // home atoms: FP32 record (+inf beyond the cell's atoms)
@@ -1380,20 +1383,34 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
             W.csum[f] = 0.0;
           }
         }
+#if NL_SC_PACKED
         const unsigned long long px = f2pack(cx, cx), py = f2pack(cy, cy), pz = f2pack(cz, cz);
+#endif
         const bool fwd = qq > 13;  // a forward cell: this warp writes the candidate's column word
         // warp-uniform masks of the round: valid candidates, forward-cell candidates
         const unsigned vmask = __ballot_sync(0xffffffffu, valid), fmask = __ballot_sync(0xffffffffu, valid && fwd);
         unsigned col = 0u;
         for (int a = 0; a < nb; a += 2) {
           // home atoms a and a + 1 (+inf beyond the cell): packed (a, a + 1) pairs
+          float r20, r21;
+#if NL_SC_PACKED
           const unsigned long long hx2 = *reinterpret_cast<const unsigned long long*>(&W.hx[a]);
           const unsigned long long hy2 = *reinterpret_cast<const unsigned long long*>(&W.hy[a]);
           const unsigned long long hz2 = *reinterpret_cast<const unsigned long long*>(&W.hz[a]);
           const unsigned long long rx = f2sub(px, hx2), ry = f2sub(py, hy2), rz = f2sub(pz, hz2);
           const unsigned long long r2p = f2fma(rz, rz, f2fma(ry, ry, f2mul(rx, rx)));
-          float r20, r21;
           f2unpack(r2p, r20, r21);
+#else
+          {
+            const float2 hx2 = *reinterpret_cast<const float2*>(&W.hx[a]);
+            const float2 hy2 = *reinterpret_cast<const float2*>(&W.hy[a]);
+            const float2 hz2 = *reinterpret_cast<const float2*>(&W.hz[a]);
+            const float rx0 = cx - hx2.x, ry0 = cy - hy2.x, rz0 = cz - hz2.x;
+            const float rx1 = cx - hx2.y, ry1 = cy - hy2.y, rz1 = cz - hz2.y;
+            r20 = fmaf(rz0, rz0, fmaf(ry0, ry0, rx0 * rx0));
+            r21 = fmaf(rz1, rz1, fmaf(ry1, ry1, rx1 * rx1));
+          }
+#endif
           // accepted (r2 < lo) and not rejected (!(r2 > hi): the band and NaN) as ballots;
           // the centre holds the home atom itself at candidate f == a (round 0, lane a)
           const unsigned lo0 = __ballot_sync(0xffffffffu, r20 < lo), lo1 = __ballot_sync(0xffffffffu, r21 < lo);
@@ -2003,8 +2020,7 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
       // ---- emission: lane r of pass j writes output position p0 + 32 j + r
       // (p0 = G rounded down to a multiple of 32), entry 32 j + r: i and j as
       // one word per lane, S and R as three words per lane (each store
-      // instruction covers a contiguous run of the arrays).  The gathers of
-      // the next two passes are in flight while two passes are written.
+      // instruction covers a contiguous run of the arrays).
       const int off = int(G & 31);
       const int lim = int(max(min((long long)cnt, cap - G), 0LL));  // entries that fit the buffers
       if ((long long)cnt > cap - G && lane == l0) bad |= kFlagCapacity;
@@ -2092,18 +2108,12 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
           }
         }
       };
-      if (npass > 0) {
-        Ld c0, c1, n0, n1;
-        load(lane, c0);
-        load(32 + lane, c1);
-        for (int j = 0; j < npass; j += 2) {
-          load(32 * (j + 2) + lane, n0);  // two passes' gathers in flight while two are written
-          load(32 * (j + 3) + lane, n1);
-          write(32 * j + lane, c0);
-          if (j + 1 < npass) write(32 * (j + 1) + lane, c1);
-          c0 = n0;
-          c1 = n1;
-        }
+      for (int j = 0; j < npass; j += 2) {  // two passes' gathers in flight, then both written
+        Ld u0, u1;
+        load(32 * j + lane, u0);
+        load(32 * j + 32 + lane, u1);
+        write(32 * j + lane, u0);
+        if (j + 1 < npass) write(32 * j + 32 + lane, u1);
       }
       __syncwarp();
       l0 = l1;
