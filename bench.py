@@ -446,16 +446,28 @@ def bench_lazy(nl, eng, Xd, X, C, pbc, stream, flush, steps):
 
     eng.launch(Xd)
     clist = eng.cell_list(Xd)
-    out = nl.lazy_reduce(clist, "inv_r6")
-    ms = timed_steps(lambda: nl.lazy_reduce(clist, "inv_r6", out=out, sync=False), steps, flush, stream)
-    eng.sync_status()
-    got = out.cpu().numpy()
     ref = orc.lazy_sum_r6(orc.build_cell_list(X, CUTOFF, C, pbc), nthreads=os.cpu_count() or 1)
-    rel = np.abs(got - ref) / np.maximum(np.abs(ref), 1e-300)
-    return {"workload": "lazy sum_j 1/r^6 per atom, same 1M-atom cell list", "ms": ms,
-            "pairs_per_s": eng.last_total / (ms * 1e-3), "max_rel_err_vs_oracle": float(rel.max()),
-            "bit_identical": bool(np.array_equal(got.view(np.int64), ref.view(np.int64))),
-            "tolerance": 1e-12}
+    res = {"workload": "lazy per-atom reductions over the same 1M-atom cell list, no pair list written",
+           "tolerance": 1e-12}
+    # "inv_r6": traversal-order passes (bit-identical sums); "inv_r6_fast": the
+    # fused symmetric screen-and-reduce pass; "count": neighbours per atom
+    for kind in ("inv_r6", "inv_r6_fast", "count"):
+        out = nl.lazy_reduce(clist, kind)
+        ms = timed_steps(lambda: nl.lazy_reduce(clist, kind, out=out, sync=False), steps, flush, stream)
+        eng.sync_status()
+        leg = {"ms": ms, "pairs_per_s": eng.last_total / (ms * 1e-3)}
+        if kind == "count":
+            leg["equal_to_list_counts"] = bool(np.array_equal(
+                out.cpu().numpy().astype(np.int64), np.diff(eng.first.cpu().numpy().astype(np.int64))))
+        else:
+            got = out.cpu().numpy()
+            rel = np.abs(got - ref) / np.maximum(np.abs(ref), 1e-300)
+            leg["max_rel_err_vs_oracle"] = float(rel.max())
+            leg["bit_identical"] = bool(np.array_equal(got.view(np.int64), ref.view(np.int64)))
+        res[kind] = leg
+    # the first leg's figures stay at the top level as well
+    res.update({k: res["inv_r6"][k] for k in ("ms", "pairs_per_s", "max_rel_err_vs_oracle", "bit_identical")})
+    return res
 
 
 def serving_requests(n_req, seed=7):
@@ -700,6 +712,20 @@ def run_path(args):
         b.sync_status()
         out = {"atoms": int(Xb.shape[0]), "pairs": int(total), "ms_per_batch": ms, "systems": len(systems),
                "timing": "CUDA events, default launch shapes, no graph, L2 flushed before every batch"}
+    elif args.path == "lazy":
+        Xd = torch.from_numpy(X).to(dev)
+        eng = nl.NeighbourListEngine(X.shape[0], C, CUTOFF, pbc, device=dev)
+        total = eng.run(Xd)
+        clist = eng.cell_list(Xd)
+        out = {"pairs": int(total)}
+        for kind in ("inv_r6_fast", "count", "inv_r6"):
+            res = nl.lazy_reduce(clist, kind)
+            for _ in range(args.warmup):
+                nl.lazy_reduce(clist, kind, out=res, sync=False)
+            out[kind + "_ms"] = timed_steps(lambda: nl.lazy_reduce(clist, kind, out=res, sync=False), steps, flush,
+                                            stream)
+            eng.sync_status()
+        out["timing"] = "CUDA events, L2 flushed before every call"
     elif args.path == "float32":
         X32 = torch.from_numpy(X.astype(np.float32)).to(dev)
         eng = nl.NeighbourListEngine(X.shape[0], C, CUTOFF, pbc, device=dev, dtype=torch.float32)
@@ -735,8 +761,8 @@ def main():
     ap.add_argument("--no-extra", action="store_true", help="skip the lazy / batched / 4M sections")
     ap.add_argument("--atoms", type=int, default=N_ATOMS, help="system size (profiling runs use a smaller one)")
     ap.add_argument("--systems", type=int, default=4096, help="batched profiling runs: systems in the batch")
-    ap.add_argument("--path", default="headline", choices=["headline", "float32", "legacy", "batched"],
-                    help="float32 / legacy / batched: profiling runs of those paths (not the benchmark line)")
+    ap.add_argument("--path", default="headline", choices=["headline", "float32", "legacy", "batched", "lazy"],
+                    help="float32 / legacy / batched / lazy: profiling runs of those paths (not the benchmark line)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -1080,8 +1080,12 @@ __global__ void __launch_bounds__(kSymWarps * 32, BATCH ? NL_SYM_BATCH_MIN_BLOCK
 // candidates of one round are a ballot; its row word for stencil cell q is
 // the run of ballot bits of q's candidates (a funnel shift across two
 // rounds).  A candidate's column word -- the home atoms that accepted it,
-// stored as its word for the mirrored cell 26 - q -- accumulates in a
-// register.  The next cell's stencil ranges are loaded one cell ahead.  The
+// stored as its word for the mirrored cell 26 - q -- accumulates in the
+// candidate lane's register from its own decisions.  Lanes beyond the round's
+// candidates and atoms beyond the home cell get infinite coordinates, so the
+// screen needs no masks; the home atom itself (its own candidate in the
+// centre) is taken out of its row afterwards.  The next cell's stencil ranges
+// are loaded one cell ahead.  The
 // write pass finds stencil cells from cell_offsets, so no per-cell stencil
 // table is written; each home atom's (sorted slot, home cell) goes to hdr,
 // indexed by its original index, for the original-order write pass.  Mask
@@ -1374,7 +1378,10 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
         const float4 r = A.rec[slot];
         const unsigned cw = cand_word(q_slp, __float_as_uint(r.w));
         const bool ex = (cw & kExactBit) != 0;
-        const float cx = ex ? nan : r.x + qx, cy = ex ? nan : r.y + qy, cz = ex ? nan : r.z + qz;
+        // exact atoms carry NaN (always rechecked); lanes beyond the candidates -inf
+        // (r2 = +inf against every home atom, +inf ones included: never accepted or rechecked)
+        const float cx = !valid ? -inf : ex ? nan : r.x + qx, cy = !valid ? -inf : ex ? nan : r.y + qy,
+                    cz = !valid ? -inf : ex ? nan : r.z + qz;
         const int corig = clampi(A.perm[slot] - 1, nat - 1);
         if constexpr (SM == kSymInvR6) {  // the candidate, for the queue's pair evaluation
           if (valid) {
@@ -1387,8 +1394,7 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
         const unsigned long long px = f2pack(cx, cx), py = f2pack(cy, cy), pz = f2pack(cz, cz);
 #endif
         const bool fwd = qq > 13;  // a forward cell: this warp writes the candidate's column word
-        // warp-uniform masks of the round: valid candidates, forward-cell candidates
-        const unsigned vmask = __ballot_sync(0xffffffffu, valid), fmask = __ballot_sync(0xffffffffu, valid && fwd);
+        const unsigned vmask = __ballot_sync(0xffffffffu, valid);  // the round's candidates
         unsigned col = 0u;
         for (int a = 0; a < nb; a += 2) {
           // home atoms a and a + 1 (+inf beyond the cell): packed (a, a + 1) pairs
@@ -1411,37 +1417,44 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
             r21 = fmaf(rz1, rz1, fmaf(ry1, ry1, rx1 * rx1));
           }
 #endif
-          // accepted (r2 < lo) and not rejected (!(r2 > hi): the band and NaN) as ballots;
-          // the centre holds the home atom itself at candidate f == a (round 0, lane a)
-          const unsigned lo0 = __ballot_sync(0xffffffffu, r20 < lo), lo1 = __ballot_sync(0xffffffffu, r21 < lo);
-          const unsigned in0 = __ballot_sync(0xffffffffu, !(r20 > hi)), in1 = __ballot_sync(0xffffffffu, !(r21 > hi));
-          const unsigned m0 = vmask & ~(rr == 0 ? 1u << a : 0u);
-          const unsigned m1 = a + 1 < nb ? vmask & ~(rr == 0 ? 2u << a : 0u) : 0u;
-          unsigned acc0 = lo0 & m0, acc1 = lo1 & m1;
-          const unsigned unc0 = in0 & ~lo0 & m0, unc1 = in1 & ~lo1 & m1;
-          if (unc0 | unc1) {  // the band, and exact atoms (NaN): FP64 with the reference's arithmetic
-            bool x0 = false, x1 = false;
-            if ((unc0 >> lane) & 1u) {
+          // accepted: r2 < lo; the band and NaN (exact atoms) are decided in FP64
+          // with the reference's arithmetic.  The centre holds the home atom
+          // itself at candidate f == a (round 0, lane a): accepted here (r2 = 0)
+          // and taken out of its row word after the rounds (masks) or below.
+          bool l0 = r20 < lo, l1 = r21 < lo;
+          const bool u0 = !l0 && !(r20 > hi), u1 = !l1 && !(r21 > hi);
+          if (__any_sync(0xffffffffu, u0 || u1)) {
+            const unsigned sb = rr == 0 ? 1u << a : 0u;  // the home atom itself
+            const bool v0 = ((vmask & ~sb) >> lane) & 1u;
+            const bool v1 = a + 1 < nb && (((vmask & ~(sb << 1)) >> lane) & 1u);
+            if (u0 && v0) {
               ++rechecks;
-              x0 = exact_pair(g, A.Xs, hs + a, slot, W.hmeta[a], cw);
+              l0 = exact_pair(g, A.Xs, hs + a, slot, W.hmeta[a], cw);
             }
-            if ((unc1 >> lane) & 1u) {
+            if (u1 && v1) {
               ++rechecks;
-              x1 = exact_pair(g, A.Xs, hs + a + 1, slot, W.hmeta[a + 1], cw);
+              l1 = exact_pair(g, A.Xs, hs + a + 1, slot, W.hmeta[a + 1], cw);
             }
-            acc0 |= __ballot_sync(0xffffffffu, x0);
-            acc1 |= __ballot_sync(0xffffffffu, x1);
+          }
+          unsigned acc0 = __ballot_sync(0xffffffffu, l0), acc1 = __ballot_sync(0xffffffffu, l1);
+          if constexpr (SM != kSymMasks) {  // the home atom itself is no pair
+            const unsigned sb = rr == 0 ? 1u << a : 0u;
+            acc0 &= ~sb;
+            acc1 &= ~(sb << 1);
+            l0 = l0 && ((acc0 >> lane) & 1u);
+            l1 = l1 && ((acc1 >> lane) & 1u);
           }
           // full lists keep both directions (row and, for forward cells, column);
           // a half list keeps the one half_keep selects
-          unsigned row0 = acc0, row1 = acc1, cm0 = acc0 & fmask, cm1 = acc1 & fmask;
+          unsigned row0 = acc0, row1 = acc1;
+          bool c0 = l0, c1 = l1;  // this lane's candidate joins the column of home atom a / a + 1
           if (A.half) {
-            const bool k0 = ((acc0 >> lane) & 1u) && half_keep(W.horig[a], corig, cw, W.hmeta[a]);
-            const bool k1 = ((acc1 >> lane) & 1u) && half_keep(W.horig[a + 1], corig, cw, W.hmeta[a + 1]);
+            const bool k0 = l0 && half_keep(W.horig[a], corig, cw, W.hmeta[a]);
+            const bool k1 = l1 && half_keep(W.horig[a + 1], corig, cw, W.hmeta[a + 1]);
             row0 = __ballot_sync(0xffffffffu, k0);
             row1 = __ballot_sync(0xffffffffu, k1);
-            cm0 &= ~row0;
-            cm1 &= ~row1;
+            c0 = l0 && !k0;
+            c1 = l1 && !k1;
           }
           if constexpr (SM == kSymMasks) {
             if (lane == 0) {
@@ -1461,11 +1474,11 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
             const unsigned lt = lt_mask();
             if ((row0 >> lane) & 1u)
               W.q[(qt + __popc(row0 & lt)) & (kLZRing - 1)] =
-                  unsigned(a) | (((cm0 >> lane) & 1u) << 5) | (unsigned(f) << 6);
+                  unsigned(a) | (unsigned(c0 && fwd) << 5) | (unsigned(f) << 6);
             qt += __popc(row0);
             if ((row1 >> lane) & 1u)
               W.q[(qt + __popc(row1 & lt)) & (kLZRing - 1)] =
-                  unsigned(a + 1) | (((cm1 >> lane) & 1u) << 5) | (unsigned(f) << 6);
+                  unsigned(a + 1) | (unsigned(c1 && fwd) << 5) | (unsigned(f) << 6);
             qt += __popc(row1);
             while (qt - qh >= 32) {
               __syncwarp();
@@ -1473,7 +1486,7 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
               qh += 32;
             }
           }
-          if constexpr (SM != kSymInvR6) col |= (((cm0 >> lane) & 1u) << a) | (((cm1 >> lane) & 1u) << (a + 1));
+          if constexpr (SM != kSymInvR6) col |= (c0 ? 1u << a : 0u) | (c1 ? 2u << a : 0u);
         }
         if constexpr (SM == kSymMasks) {
           if (valid && fwd) {  // the candidate's word for its mirrored cell
@@ -1485,6 +1498,10 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
         }
       }
       __syncwarp();
+      if constexpr (SM == kSymMasks) {  // the home atom itself (round 0, candidate a) is no pair
+        if (lane < nb) W.B[lane][0] &= ~(1u << lane);
+        __syncwarp();
+      }
       if constexpr (SM == kSymInvR6) {
         __syncwarp();
         if (qt > qh) lazy_flush<TI>(A, g, cs_blk, W, qh, qt - qh, lane);
@@ -1846,20 +1863,26 @@ __global__ void __launch_bounds__(kEmitWarps * 32,
 // home cell) and output range, then -- loads issued together -- its 27 mask
 // words (16-byte vector loads), position, record meta and the sorted start of
 // each of its 27 stencil cells (cell_offsets; the wrapped cell and loop shift
-// per axis follow from the home cell).  Lane a expands its own masks, in
-// stencil order (dz, dy, dx) and sorted order within each stencil cell -- the
-// reference's traversal order -- into a shared-memory table of 8-byte
-// entries (slot of j; atom and the three loop shifts) at the pairs' output
-// positions.  The table holds kEOEnt entries; a batch with more pairs is cut
-// at atom boundaries (an atom has at most 27 * 32 - 1 pairs on this path).
-// The warp then walks the output positions 32 at a time, passes aligned to
-// multiples of 32 in the output arrays, lane r writing pair base + r: i, j,
-// S (the loop shifts, or with windings s_loop + wi - wj) and
-// R = (xj - xi) + C'S with the reference's operations.  i and j are stored
-// per lane; S and R are staged in shared memory and stored as 16-byte
-// vectors (a chunk's first and last passes, and arrays that are not 16-byte
-// aligned, store word by word).  The gathers of the next two passes are in
-// flight while two passes are finished.
+// per axis follow from the home cell).  The masks are expanded into a
+// shared-memory table of 8-byte entries (slot of j; atom and the three loop
+// shifts) at the pairs' output positions, in stencil order (dz, dy, dx) and
+// sorted order within each stencil cell -- the reference's traversal order.
+// The expansion is balanced over the warp: each lane lists its non-empty
+// words (word, stencil cell start, loop-shift code) at the end of its own
+// stretch of the table, then takes one set bit per step, reading the next
+// listed word when a word is used up.  The warp takes as many steps as its
+// busiest lane has pairs (about 37 for 26 pairs per atom) instead of, word by
+// word, as many as the fullest word of any lane has bits (about 120).  A
+// listed word is read before the entries reach it: when the entry at stretch
+// position s is written, every unread listed word still holds a bit, so the
+// unread part of the list lies beyond s.  The table holds kEOEnt entries; a
+// batch with more pairs is cut at atom boundaries (an atom has at most
+// 27 * 32 - 1 pairs on this path).  The warp then walks the output positions
+// 32 at a time, passes aligned to multiples of 32 in the output arrays, lane
+// r writing pair base + r: i, j, S (the loop shifts, or with windings
+// s_loop + wi - wj) and R = (xj - xi) + C'S with the reference's operations,
+// one word per lane and array in each store instruction.  The gathers of two
+// passes are in flight before either pass is written.
 #ifndef NL_EO_MIN_BLOCKS
 #define NL_EO_MIN_BLOCKS 8  // resident blocks per SM the register budget targets
 #endif
@@ -1869,9 +1892,11 @@ static_assert(kEOEnt >= 27 * 32, "an atom of the symmetric pass has fewer than 2
 
 template <typename TI>
 struct __align__(16) EOSmem {
-  uint2 ent[kEOEnt];    // entry: (sorted slot of j, atom | loop shift + 1 per axis << 5 + 2k)
-  double xi[32][3];     // the batch's atoms: FP64 position
-  unsigned mi[32];      //   record meta (windings, exact bit)
+  uint2 ent[kEOEnt];           // entry: (sorted slot of j, atom | loop shift + 1 per axis << 5 + 2k);
+                               // while the masks are expanded also the listed words (word, cell start)
+  unsigned char code[kEOEnt];  // loop-shift code (bits 5.. of an entry's second word) of a listed word
+  double xi[32][4];            // the batch's atoms: FP64 position (and padding)
+  unsigned mi[32];             //   record meta (windings, exact bit)
 };
 
 // The three cells c - 1, c, c + 1 along one axis (c 1-based): 0-based wrapped
@@ -1977,43 +2002,58 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
           E.xi[lane][2] = A.Xs[3LL * slot + 2];
           E.mi[lane] = __float_as_uint(A.rec[slot].w);
         }
-        // ---- expansion: lane a writes its entries at [f - G, f - G + n); a
-        // word has about one bit on average, so the first two bits of every
-        // word are taken without a loop and the rest by a rare one
-        {
-          int e = mine ? int(f - G) + int(G & 31) : 0;  // the entry of output position p sits at p - (G - G mod 32)
-          const int eend = mine ? e + int(n) : 0;
-          const int emax = min(eend, kEOEnt);  // (bounds hold for consistent counts)
+        // ---- the lane's non-empty words, listed at the end of its stretch
+        // [e0, e0 + nn) of the table (each holds a bit: nnz <= nn), written
+        // from the last word down so that each mask word and cell start dies
+        // as soon as it is listed
+        const int e0 = mine ? int(f - G) + int(G & 31) : 0;  // the entry of output position p sits at p - (G - G mod 32)
+        const int nn = mine ? int(n) : 0;
+        int nnz = 0, tot = 0;
 #pragma unroll
-          for (int q = 0; q < 27; ++q) {
-            const int dx = q % 3, dy = (q / 3) % 3, dz = q / 9;
-            unsigned mq = mine ? (&mv[q >> 2].x)[q & 3] : 0u;
-            if (mq && !(okx[dx] && oky[dy] && okz[dz])) {  // a neighbour in a cell outside an open axis
-              bad |= kFlagInconsistent;
-              mq = 0u;
-            }
-            const unsigned info = unsigned(lane) | unsigned(sx[dx] + 1) << 5 | unsigned(sy[dy] + 1) << 7 |
-                                  unsigned(sz[dz] + 1) << 9;
-            const int c = __popc(mq);
-            if (mq) {
-              if (e >= 0 && e < emax) E.ent[e] = make_uint2(st[q] + unsigned(__ffs(mq) - 1), info);
-              mq &= mq - 1u;
-              if (mq) {
-                if (e + 1 >= 0 && e + 1 < emax) E.ent[e + 1] = make_uint2(st[q] + unsigned(__ffs(mq) - 1), info);
-                mq &= mq - 1u;
-              }
-            }
-            if (__any_sync(0xffffffffu, mq != 0u)) {  // words of three or more bits
-              int ee = e + 2;
-              while (mq) {
-                if (ee >= 0 && ee < emax) E.ent[ee] = make_uint2(st[q] + unsigned(__ffs(mq) - 1), info);
-                mq &= mq - 1u;
-                ++ee;
-              }
-            }
-            e += c;
+        for (int q = 26; q >= 0; --q) {
+          unsigned mq = (&mv[q >> 2].x)[q & 3];
+          if (mq && !(okx[q % 3] && oky[(q / 3) % 3] && okz[q / 9])) {  // a neighbour in a cell outside an open axis
+            bad |= kFlagInconsistent;
+            mq = 0u;
           }
-          if (mine && e != eend) bad |= kFlagInconsistent;  // counts and masks disagree
+          if (mq) {
+            if (nnz < nn && e0 >= 0) {
+              const int k = e0 + nn - 1 - nnz;
+              E.ent[k] = make_uint2(mq, st[q]);
+              E.code[k] = (unsigned char)(unsigned(sx[q % 3] + 1) | unsigned(sy[(q / 3) % 3] + 1) << 2 |
+                                          unsigned(sz[q / 9] + 1) << 4);
+            }
+            ++nnz;
+            tot += __popc(mq);
+          }
+        }
+        const bool lok = mine && tot == nn && e0 >= 0;
+        if (mine && !lok) bad |= kFlagInconsistent;  // counts and masks disagree
+        const int li = e0 + nn - nnz;  // the first listed word
+        // ---- one set bit per step: entry e0 + s is the lane's pair s
+        unsigned w = 0u, stq = 0u, inf = 0u;
+        int kk = 0;
+        if (lok && nnz > 0) {
+          const uint2 it = E.ent[li];
+          w = it.x;
+          stq = it.y;
+          inf = unsigned(lane) | unsigned(E.code[li]) << 5;
+          kk = 1;
+        }
+        const int smax = __reduce_max_sync(0xffffffffu, lok ? nn : 0);
+        for (int s = 0; s < smax; ++s) {
+          const bool on = lok && s < nn;
+          const unsigned bit = unsigned(__ffs(w) - 1);
+          if (on) E.ent[e0 + s] = make_uint2(stq + bit, inf);
+          w &= w - 1u;
+          if (on && w == 0u && s + 1 < nn && kk < nnz) {  // the word is used up: the next listed one
+            const int p = li + kk;
+            const uint2 it = E.ent[p];
+            w = it.x;
+            stq = it.y;
+            inf = unsigned(lane) | unsigned(E.code[p]) << 5;
+            ++kk;
+          }
         }
       }
       __syncwarp();
@@ -2033,50 +2073,41 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
       double* __restrict__ oR = A.oR ? A.oR + 3 * p0 : nullptr;
       const TI ti0 = TI(o0 + 1);  // i of atom a is ti0 + a
       struct Ld {
-        double x0, x1, x2;
-        int pj;
-        unsigned mj, info;
+        uint2 en;
+        double2 w0;
+        int4 w1;
       };
+      // every lane loads (entries outside [off, hix) repeat an edge entry; their stores are off)
       auto load = [&](int k, Ld& u) {
-        u.info = 0u;
-        u.x0 = u.x1 = u.x2 = 0.0;
-        u.pj = 0;
-        u.mj = kPlainMeta;
-        if (k >= off && k < hix) {
-          const uint2 en = E.ent[k];
-          u.info = en.y;
-          const XPack* xp = A.xpk + min(en.x, unsigned(nat - 1));
-          const double2 w0 = __ldg(reinterpret_cast<const double2*>(xp));
-          const int4 w1 = __ldg(reinterpret_cast<const int4*>(xp) + 1);
-          u.x0 = w0.x;
-          u.x1 = w0.y;
-          u.x2 = __hiloint2double(w1.y, w1.x);
-          u.pj = w1.z;
-          u.mj = unsigned(w1.w);
-        }
+        u.en = E.ent[min(max(k, off), hix - 1)];
+        const XPack* xp = A.xpk + min(u.en.x, unsigned(nat - 1));
+        u.w0 = __ldg(reinterpret_cast<const double2*>(xp));
+        u.w1 = __ldg(reinterpret_cast<const int4*>(xp) + 1);
       };
       auto write = [&](int k, const Ld& u) {
         const bool act = k >= off && k < hix;
-        const int a = int(u.info & 31u);
+        const unsigned info = u.en.y;
+        const int a = int(info & 31u);
         const double* xi = E.xi[a];
-        int S0 = int((u.info >> 5) & 3u) - 1, S1 = int((u.info >> 7) & 3u) - 1, S2 = int((u.info >> 9) & 3u) - 1;
+        const double x0 = u.w0.x, x1 = u.w0.y, x2 = __hiloint2double(u.w1.y, u.w1.x);
+        int S0 = int((info >> 5) & 3u) - 1, S1 = int((info >> 7) & 3u) - 1, S2 = int((info >> 9) & 3u) - 1;
         if (!plain) {  // windings or exact atoms: S = s_loop + wi - wj
-          const double xj[3] = {u.x0, u.x1, u.x2};
+          const double xj[3] = {x0, x1, x2};
           int S[3];
-          pair_S(g, xi, xj, E.mi[a], cand_word(cand_base(S0, S1, S2), u.mj), S);
+          pair_S(g, xi, xj, E.mi[a], cand_word(cand_base(S0, S1, S2), unsigned(u.w1.w)), S);
           S0 = S[0];
           S1 = S[1];
           S2 = S[2];
         }
         if (act) {
           __stcs(oi + k, TI(ti0 + a));
-          __stcs(oj + k, TI(u.pj));
+          __stcs(oj + k, TI(u.w1.z));
           __stcs(oS + 3 * k + 0, TI(S0));
           __stcs(oS + 3 * k + 1, TI(S1));
           __stcs(oS + 3 * k + 2, TI(S2));
         }
         if (oR) {
-          double R0 = dsub(u.x0, xi[0]), R1 = dsub(u.x1, xi[1]), R2 = dsub(u.x2, xi[2]);
+          double R0 = dsub(x0, xi[0]), R1 = dsub(x1, xi[1]), R2 = dsub(x2, xi[2]);
           const bool nz = act && (S0 | S1 | S2) != 0;
           if (__any_sync(0xffffffffu, nz)) {
             if (nz) {
