@@ -1147,10 +1147,10 @@ struct __align__(16) LZSmem {
   int horig[32];
   int hcnt[32];
   double hX[32][3];        // home atoms: FP64 positions
-  double hsum[32];         //   sum over their rows
+  float2 hsum[32];         //   sum over their rows (double-float)
   int cslot[14 * 32];      // candidate: sorted slot
   unsigned ccw[14 * 32];   //   candidate word (loop shift, windings)
-  double csum[14 * 32];    //   sum over its column (forward cells)
+  float2 csum[14 * 32];    //   sum over its column (forward cells; double-float)
   unsigned q[128];         // queued pairs (a ring)
 };
 constexpr int kLZRing = 128;
@@ -1198,12 +1198,13 @@ __device__ __forceinline__ double f2d_exact(float x) {
 }
 
 // Evaluates the n <= 32 queued pairs from ring position head of the lazy
-// reduction, one per lane: R with
-// the reference's FP64 operations (gpu_kernels.jl:88-91), r2 and 1/r2^3 in
-// double-float (relative error far below 1e-12), then the atom's row sum and,
-// for a forward candidate, its column sum.  r2 below 1e-12 (where 1/r2^3
-// leaves the FP32 range: coincident or nearly coincident atoms) is evaluated
-// in FP64 with the reference's formula.
+// reduction, one per lane: R with the reference's FP64 operations
+// (gpu_kernels.jl:88-91), r2 and 1/r2^3 in double-float (relative error far
+// below 1e-12), then the home atom's row sum and, for a forward candidate, its
+// column sum, both kept in double-float in shared memory (FP64 only for the
+// cell's final per-atom additions).  r2 below 1e-12 (where 1/r2^3 leaves the
+// FP32 range: coincident or nearly coincident atoms) is evaluated in FP64
+// with the reference's formula and added to the per-atom sums directly.
 template <typename TI>
 __device__ __forceinline__ void lazy_flush(const PairArgs<TI>& A, const Geometry& g, const double* cs_tab, LZSmem& W,
                                            int head, int n, int lane) {
@@ -1227,26 +1228,57 @@ __device__ __forceinline__ void lazy_flush(const PairArgs<TI>& A, const Geometry
     }
     r2 = df_add(r2, df_sq(h, l));
   }
-  double fd;
-  if (__any_sync(0xffffffffu, act && !(r2.hi >= 1e-12f))) {
-    if (!(r2.hi >= 1e-12f)) {
-      const double r2d = dot_ref(R);
-      fd = __ddiv_rn(1.0, dmul(dmul(r2d, r2d), r2d));
-    } else {
-      const dfloat y = df_rcp(r2);
-      const dfloat f = df_mul(df_mul(y, y), y);
-      fd = dadd(f2d_exact(f.hi), f2d_exact(f.lo));
-    }
-  } else {
+  // 1/r2^3 in double-float; r2 below 1e-12 (rare) in FP64, added to the
+  // per-atom sums at once
+  const bool rare = act && !(r2.hi >= 1e-12f);
+  dfloat f = {0.f, 0.f};
+  if (act && !rare) {
     const dfloat y = df_rcp(r2);
-    const dfloat f = df_mul(df_mul(y, y), y);
-    fd = dadd(f2d_exact(f.hi), f2d_exact(f.lo));
+    f = df_mul(df_mul(y, y), y);
   }
-  if (act) {
-    atomicAdd(&W.hsum[a], fd);
-    if ((e >> 5) & 1u) atomicAdd(&W.csum[fi], fd);
+  const bool fwd = act && ((e >> 5) & 1u);
+  if (__any_sync(0xffffffffu, rare)) {
+    if (rare) {
+      const double r2d = dot_ref(R);
+      const double fd = __ddiv_rn(1.0, dmul(dmul(r2d, r2d), r2d));
+      atomicAdd(A.per_atom + W.horig[a], fd);
+      if (fwd) atomicAdd(A.per_atom + clampi(A.perm[sj] - 1, g.nat - 1), fd);
+    }
   }
-  __syncwarp();
+  // Runs of one home atom sit on consecutive lanes (the queue's order).  A
+  // segmented double-float scan leaves each run's row sum on its last lane;
+  // then the runs update the shared sums one run after another, without
+  // atomics: within a run the candidates are distinct, and a home atom or a
+  // candidate recurs only in another run.
+  const int key = act ? a : -1;
+  const int kp = __shfl_up_sync(0xffffffffu, key, 1);
+  const unsigned heads = __ballot_sync(0xffffffffu, !act || lane == 0 || kp != key);
+  const int sstart = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));  // first lane of this lane's run
+  dfloat rs = f;
+  for (int d = 1; d < 32 && __any_sync(0xffffffffu, lane - d >= sstart); d <<= 1) {
+    const float th = __shfl_up_sync(0xffffffffu, rs.hi, d), tl = __shfl_up_sync(0xffffffffu, rs.lo, d);
+    if (lane - d >= sstart) rs = df_add(rs, dfloat{th, tl});
+  }
+  const int kn = __shfl_down_sync(0xffffffffu, key, 1);
+  const bool tail = act && (lane == 31 || kn != key);
+  unsigned pending = __ballot_sync(0xffffffffu, act) & heads;
+  while (pending) {
+    const int h0 = __ffs(pending) - 1;
+    pending &= pending - 1u;
+    const int h1 = pending ? __ffs(pending) - 1 : n;
+    const bool in = lane >= h0 && lane < h1;
+    if (in && fwd && (f.hi != 0.f || f.lo != 0.f)) {
+      const float2 c = W.csum[fi];
+      const dfloat t = df_add(dfloat{c.x, c.y}, f);
+      W.csum[fi] = make_float2(t.hi, t.lo);
+    }
+    if (in && tail && (rs.hi != 0.f || rs.lo != 0.f)) {
+      const float2 c = W.hsum[a];
+      const dfloat t = df_add(dfloat{c.x, c.y}, rs);
+      W.hsum[a] = make_float2(t.hi, t.lo);
+    }
+    __syncwarp();
+  }
 }
 
 template <typename TI, int SM>
@@ -1335,7 +1367,7 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
             W.hX[lane][0] = X0;
             W.hX[lane][1] = X1;
             W.hX[lane][2] = X2;
-            W.hsum[lane] = 0.0;
+            W.hsum[lane] = make_float2(0.f, 0.f);
           }
         }
         W.hx[lane] = x;
@@ -1387,7 +1419,7 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
           if (valid) {
             W.cslot[f] = slot;
             W.ccw[f] = cw;
-            W.csum[f] = 0.0;
+            W.csum[f] = make_float2(0.f, 0.f);
           }
         }
 #if NL_SC_PACKED
@@ -1507,9 +1539,15 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
         if (qt > qh) lazy_flush<TI>(A, g, cs_blk, W, qh, qt - qh, lane);
         __syncwarp();
         // the cell's sums: its atoms' rows and its forward candidates' columns
-        if (lane < nb) atomicAdd(A.per_atom + W.horig[lane], W.hsum[lane]);
-        for (int fc = lane; fc < T; fc += 32)
-          if (W.csum[fc] != 0.0) atomicAdd(A.per_atom + clampi(A.perm[W.cslot[fc]] - 1, nat - 1), W.csum[fc]);
+        if (lane < nb) {
+          const float2 h = W.hsum[lane];
+          if (h.x != 0.f || h.y != 0.f) atomicAdd(A.per_atom + W.horig[lane], dadd(f2d_exact(h.x), f2d_exact(h.y)));
+        }
+        for (int fc = lane; fc < T; fc += 32) {
+          const float2 c = W.csum[fc];
+          if (c.x != 0.f || c.y != 0.f)
+            atomicAdd(A.per_atom + clampi(A.perm[W.cslot[fc]] - 1, nat - 1), dadd(f2d_exact(c.x), f2d_exact(c.y)));
+        }
         __syncwarp();
       }
       if constexpr (SM == kSymCounts) {
@@ -1881,13 +1919,17 @@ __global__ void __launch_bounds__(kEmitWarps * 32,
 // 32 at a time, passes aligned to multiples of 32 in the output arrays, lane
 // r writing pair base + r: i, j, S (the loop shifts, or with windings
 // s_loop + wi - wj) and R = (xj - xi) + C'S with the reference's operations,
-// one word per lane and array in each store instruction.  The gathers of two
-// passes are in flight before either pass is written.
+// one word per lane and array in each store instruction.  The gathers of
+// kEOPasses passes are in flight before the first of them is written.
 #ifndef NL_EO_MIN_BLOCKS
 #define NL_EO_MIN_BLOCKS 8  // resident blocks per SM the register budget targets
 #endif
+#ifndef NL_EO_PASSES
+#define NL_EO_PASSES 2  // passes whose gathers are in flight together
+#endif
 constexpr int kEOWarps = 2;
 constexpr int kEOEnt = 1024;  // pair entries per warp
+constexpr int kEOPasses = NL_EO_PASSES;
 static_assert(kEOEnt >= 27 * 32, "an atom of the symmetric pass has fewer than 27 * 32 pairs");
 
 template <typename TI>
@@ -2091,6 +2133,7 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
         const double* xi = E.xi[a];
         const double x0 = u.w0.x, x1 = u.w0.y, x2 = __hiloint2double(u.w1.y, u.w1.x);
         int S0 = int((info >> 5) & 3u) - 1, S1 = int((info >> 7) & 3u) - 1, S2 = int((info >> 9) & 3u) - 1;
+        bool snz = (info & (63u << 5)) != (21u << 5);  // (S0, S1, S2) != 0: the codes are not 1, 1, 1
         if (!plain) {  // windings or exact atoms: S = s_loop + wi - wj
           const double xj[3] = {x0, x1, x2};
           int S[3];
@@ -2098,6 +2141,7 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
           S0 = S[0];
           S1 = S[1];
           S2 = S[2];
+          snz = (S0 | S1 | S2) != 0;
         }
         if (act) {
           __stcs(oi + k, TI(ti0 + a));
@@ -2108,7 +2152,7 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
         }
         if (oR) {
           double R0 = dsub(x0, xi[0]), R1 = dsub(x1, xi[1]), R2 = dsub(x2, xi[2]);
-          const bool nz = act && (S0 | S1 | S2) != 0;
+          const bool nz = act && snz;
           if (__any_sync(0xffffffffu, nz)) {
             if (nz) {
               double c0, c1, c2;
@@ -2139,12 +2183,13 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
           }
         }
       };
-      for (int j = 0; j < npass; j += 2) {  // two passes' gathers in flight, then both written
-        Ld u0, u1;
-        load(32 * j + lane, u0);
-        load(32 * j + 32 + lane, u1);
-        write(32 * j + lane, u0);
-        if (j + 1 < npass) write(32 * j + 32 + lane, u1);
+      for (int j = 0; j < npass; j += kEOPasses) {  // kEOPasses passes' gathers in flight, then all written
+        Ld u[kEOPasses];
+#pragma unroll
+        for (int t = 0; t < kEOPasses; ++t) load(32 * (j + t) + lane, u[t]);
+#pragma unroll
+        for (int t = 0; t < kEOPasses; ++t)
+          if (t == 0 || j + t < npass) write(32 * (j + t) + lane, u[t]);
       }
       __syncwarp();
       l0 = l1;
