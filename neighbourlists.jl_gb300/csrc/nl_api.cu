@@ -1161,8 +1161,12 @@ int nl_lazy_reduce(const double* d_X_sorted, const void* d_perm, const void* d_c
     // per-cell passes below are gated on their success and redo the whole
     // reduction when a cell holds more than 32 atoms
     // (sym_gate, not sym: the count launcher reads sym as "launch the mask pass")
+    // (the fast sum reads the neighbour masks, which need the list region)
     a.sym = 0;
-    a.sym_gate = (op == NL_REDUCE_COUNT || op == NL_REDUCE_INV_R6_FAST) && sym_geometry(g) ? 1 : 0;
+    a.sym_gate = (op == NL_REDUCE_COUNT && sym_geometry(g)) ||
+                         (op == NL_REDUCE_INV_R6_FAST && sym_geometry(g) && use_sym(g, L))
+                     ? 1
+                     : 0;
     if (a.sym_gate) {
       const size_t bytes = op == NL_REDUCE_COUNT ? sizeof(int) : sizeof(double);
       cudaError_t me = cudaMemsetAsync(d_out, 0, bytes * size_t(g.nat), st);
@@ -1171,6 +1175,9 @@ int nl_lazy_reduce(const double* d_X_sorted, const void* d_perm, const void* d_c
         a.counts = static_cast<int*>(d_out);
       } else {
         a.per_atom = static_cast<double*>(d_out);
+        a.counts = at<int>(d_workspace, L.counts);  // the mask pass's counts (not the result)
+        me = cudaMemsetAsync(a.counts, 0, sizeof(int) * size_t(g.nat), st);
+        if (me != cudaSuccess) e = me;
       }
       nl::launch_sym_lazy<TI>(op == NL_REDUCE_COUNT ? nl::kLazyCounts : nl::kLazyInvR6, a, sms, st);
     }

@@ -1135,25 +1135,13 @@ __device__ __forceinline__ unsigned long long f2fma(unsigned long long a, unsign
 
 // What the candidate-parallel symmetric pass produces: the neighbour masks
 // (and headers and gather rows) of the write pass, only the per-atom counts
-// (the lazy count), or the per-atom sums of 1/r^6 (the lazy reduction).
-constexpr int kSymMasks = 0, kSymCounts = 1, kSymInvR6 = 2;
-
-// The lazy reduction's view of one warp: home atoms, every candidate of the
-// home cell's forward stencil (up to 14 cells of 32 atoms), and the queue of
-// accepted pairs (home atom | forward flag << 5 | candidate << 6).
-struct __align__(16) LZSmem {
-  float hx[32], hy[32], hz[32];
-  unsigned hmeta[32];
-  int horig[32];
-  int hcnt[32];
-  double hX[32][3];        // home atoms: FP64 positions
-  float2 hsum[32];         //   sum over their rows (double-float)
-  int cslot[14 * 32];      // candidate: sorted slot
-  unsigned ccw[14 * 32];   //   candidate word (loop shift, windings)
-  float2 csum[14 * 32];    //   sum over its column (forward cells; double-float)
-  unsigned q[128];         // queued pairs (a ring)
-};
-constexpr int kLZRing = 128;
+// (the lazy count), or the masks with gather rows whose positions are fixed
+// point (the lazy sum of 1/r^6, k_lazy_rows).
+constexpr int kSymMasks = 0, kSymCounts = 1, kSymMasksFix = 2;
+// Fixed-point positions of the lazy sum: x * 2^52 as a 64-bit integer
+// (|x| < 2^11 A; below 1 A the position loses bits under 2^-53 A).
+constexpr double kFixScale = 4503599627370496.0;  // 2^52
+constexpr double kFixMax = 2000.0;
 
 // Double-float (unevaluated FP32 pairs, hi + lo): Dekker's and Knuth's
 // error-free products and sums (about 48 significant bits).
@@ -1197,101 +1185,12 @@ __device__ __forceinline__ double f2d_exact(float x) {
   return __hiloint2double(int(hi), int((u & 0x7u) << 29));
 }
 
-// Evaluates the n <= 32 queued pairs from ring position head of the lazy
-// reduction, one per lane: R with the reference's FP64 operations
-// (gpu_kernels.jl:88-91), r2 and 1/r2^3 in double-float (relative error far
-// below 1e-12), then the home atom's row sum and, for a forward candidate, its
-// column sum, both kept in double-float in shared memory (FP64 only for the
-// cell's final per-atom additions).  r2 below 1e-12 (where 1/r2^3 leaves the
-// FP32 range: coincident or nearly coincident atoms) is evaluated in FP64
-// with the reference's formula and added to the per-atom sums directly.
-template <typename TI>
-__device__ __forceinline__ void lazy_flush(const PairArgs<TI>& A, const Geometry& g, const double* cs_tab, LZSmem& W,
-                                           int head, int n, int lane) {
-  const bool act = lane < n;
-  const unsigned e = act ? W.q[(head + lane) & (kLZRing - 1)] : 0u;
-  const int a = int(e & 31u), fi = int(e >> 6);
-  const double* xi = W.hX[a];
-  const int sj = W.cslot[fi];
-  const double xj[3] = {A.Xs[3LL * sj + 0], A.Xs[3LL * sj + 1], A.Xs[3LL * sj + 2]};
-  int S[3];
-  pair_S(g, xi, xj, W.hmeta[a], W.ccw[fi], S);
-  double R[3];
-  pair_R(g, cs_tab, xi, xj, S[0], S[1], S[2], act, R);
-  dfloat r2 = {0.f, 0.f};
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    float h, l, c;
-    if (!split3(R[k], h, l, c)) {  // |R_k| outside [2^-60, 2^60]
-      h = __double2float_rn(R[k]);
-      l = 0.f;
-    }
-    r2 = df_add(r2, df_sq(h, l));
-  }
-  // 1/r2^3 in double-float; r2 below 1e-12 (rare) in FP64, added to the
-  // per-atom sums at once
-  const bool rare = act && !(r2.hi >= 1e-12f);
-  dfloat f = {0.f, 0.f};
-  if (act && !rare) {
-    const dfloat y = df_rcp(r2);
-    f = df_mul(df_mul(y, y), y);
-  }
-  const bool fwd = act && ((e >> 5) & 1u);
-  if (__any_sync(0xffffffffu, rare)) {
-    if (rare) {
-      const double r2d = dot_ref(R);
-      const double fd = __ddiv_rn(1.0, dmul(dmul(r2d, r2d), r2d));
-      atomicAdd(A.per_atom + W.horig[a], fd);
-      if (fwd) atomicAdd(A.per_atom + clampi(A.perm[sj] - 1, g.nat - 1), fd);
-    }
-  }
-  // Runs of one home atom sit on consecutive lanes (the queue's order).  A
-  // segmented double-float scan leaves each run's row sum on its last lane;
-  // then the runs update the shared sums one run after another, without
-  // atomics: within a run the candidates are distinct, and a home atom or a
-  // candidate recurs only in another run.
-  const int key = act ? a : -1;
-  const int kp = __shfl_up_sync(0xffffffffu, key, 1);
-  const unsigned heads = __ballot_sync(0xffffffffu, !act || lane == 0 || kp != key);
-  const int sstart = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));  // first lane of this lane's run
-  dfloat rs = f;
-  for (int d = 1; d < 32 && __any_sync(0xffffffffu, lane - d >= sstart); d <<= 1) {
-    const float th = __shfl_up_sync(0xffffffffu, rs.hi, d), tl = __shfl_up_sync(0xffffffffu, rs.lo, d);
-    if (lane - d >= sstart) rs = df_add(rs, dfloat{th, tl});
-  }
-  const int kn = __shfl_down_sync(0xffffffffu, key, 1);
-  const bool tail = act && (lane == 31 || kn != key);
-  unsigned pending = __ballot_sync(0xffffffffu, act) & heads;
-  while (pending) {
-    const int h0 = __ffs(pending) - 1;
-    pending &= pending - 1u;
-    const int h1 = pending ? __ffs(pending) - 1 : n;
-    const bool in = lane >= h0 && lane < h1;
-    if (in && fwd && (f.hi != 0.f || f.lo != 0.f)) {
-      const float2 c = W.csum[fi];
-      const dfloat t = df_add(dfloat{c.x, c.y}, f);
-      W.csum[fi] = make_float2(t.hi, t.lo);
-    }
-    if (in && tail && (rs.hi != 0.f || rs.lo != 0.f)) {
-      const float2 c = W.hsum[a];
-      const dfloat t = df_add(dfloat{c.x, c.y}, rs);
-      W.hsum[a] = make_float2(t.hi, t.lo);
-    }
-    __syncwarp();
-  }
-}
-
 template <typename TI, int SM>
 __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(PairArgs<TI> A) {
-  using Smem = std::conditional_t<SM == kSymInvR6, LZSmem, SCSmem>;
-  __shared__ Smem sm[kSCWarps];
-  __shared__ double cs_blk[SM == kSymInvR6 ? 3 * kCsN * kCsN * kCsN : 1];
-  if constexpr (SM == kSymInvR6) {
-    for (int t = threadIdx.x; t < 3 * kCsN * kCsN * kCsN; t += blockDim.x) cs_blk[t] = A.cs_table[t];
-    __syncthreads();
-  }
+  constexpr bool kMask = SM == kSymMasks || SM == kSymMasksFix;  // neighbour masks written
+  __shared__ SCSmem sm[kSCWarps];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  Smem& W = sm[warp];
+  SCSmem& W = sm[warp];
   const Geometry& g = A.g;
   const int nat = g.nat;
   const float lo = g.lo, hi = g.hi;
@@ -1331,7 +1230,7 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
       if (lane == 0) atomicOr(A.sym_fail, 1);  // a crowded cell: the per-cell pass with lists counts instead
     } else if (nb > 0) {
       // words q < 13 of the home atoms that no other warp writes: their cell is empty or outside
-      const unsigned zq = SM == kSymMasks ? __ballot_sync(0xffffffffu, lane < 13 && (cur.lin < 0 || cur.cnt == 0)) : 0u;
+      const unsigned zq = kMask ? __ballot_sync(0xffffffffu, lane < 13 && (cur.lin < 0 || cur.cnt == 0)) : 0u;
       if (zq)
         for (int t = lane; t < nb * 13; t += 32) {
           const int a = t / 13, q = t - 13 * a;
@@ -1363,11 +1262,16 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
             if (__double_as_longlong(X0) == nz || __double_as_longlong(X1) == nz || __double_as_longlong(X2) == nz)
               atomicOr(A.sym_wound, 2);
           }
-          if constexpr (SM == kSymInvR6) {
-            W.hX[lane][0] = X0;
-            W.hX[lane][1] = X1;
-            W.hX[lane][2] = X2;
-            W.hsum[lane] = make_float2(0.f, 0.f);
+          if constexpr (SM == kSymMasksFix) {  // the lazy sum's gather row: fixed-point position
+            XPack xp;
+            xp.x = __longlong_as_double(__double2ll_rn(dmul(X0, kFixScale)));
+            xp.y = __longlong_as_double(__double2ll_rn(dmul(X1, kFixScale)));
+            xp.z = __longlong_as_double(__double2ll_rn(dmul(X2, kFixScale)));
+            xp.perm = o + 1;
+            xp.meta = hm;
+            A.xpk[hs + lane] = xp;
+            if (!(fabs(X0) < kFixMax && fabs(X1) < kFixMax && fabs(X2) < kFixMax) || (hm & kExactBit))
+              atomicOr(A.sym_wound, 4);  // out of the fixed-point range, or exact: FP64 pairs instead
           }
         }
         W.hx[lane] = x;
@@ -1376,7 +1280,7 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
         W.hmeta[lane] = hm;
         W.hcnt[lane] = 0;
       }
-      if (SM == kSymMasks && __any_sync(0xffffffffu, hm != kPlainMeta) && lane == 0) atomicOr(A.sym_wound, 1);
+      if (kMask && __any_sync(0xffffffffu, hm != kPlainMeta) && lane == 0) atomicOr(A.sym_wound, 1);
       // candidates: stencil cells 13..26 in stencil order, flattened
       const int scnt = lane >= 13 ? cur.cnt : 0;
       int incl = scnt;
@@ -1387,7 +1291,6 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
       }
       const int T = __shfl_sync(0xffffffffu, incl, 31);
       const int nr = (T + 31) >> 5;  // <= kSCMaxRounds
-      int qh = 0, qt = 0;  // sum of 1/r^6: ring of accepted pairs (flushed 32 at a time with full lanes)
       __syncwarp();
       for (int rr = 0; rr < nr; ++rr) {
         const int f = 32 * rr + lane;
@@ -1415,13 +1318,6 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
         const float cx = !valid ? -inf : ex ? nan : r.x + qx, cy = !valid ? -inf : ex ? nan : r.y + qy,
                     cz = !valid ? -inf : ex ? nan : r.z + qz;
         const int corig = clampi(A.perm[slot] - 1, nat - 1);
-        if constexpr (SM == kSymInvR6) {  // the candidate, for the queue's pair evaluation
-          if (valid) {
-            W.cslot[f] = slot;
-            W.ccw[f] = cw;
-            W.csum[f] = make_float2(0.f, 0.f);
-          }
-        }
 #if NL_SC_PACKED
         const unsigned long long px = f2pack(cx, cx), py = f2pack(cy, cy), pz = f2pack(cz, cz);
 #endif
@@ -1469,7 +1365,7 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
             }
           }
           unsigned acc0 = __ballot_sync(0xffffffffu, l0), acc1 = __ballot_sync(0xffffffffu, l1);
-          if constexpr (SM != kSymMasks) {  // the home atom itself is no pair
+          if constexpr (!kMask) {  // the home atom itself is no pair
             const unsigned sb = rr == 0 ? 1u << a : 0u;
             acc0 &= ~sb;
             acc1 &= ~(sb << 1);
@@ -1488,73 +1384,38 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
             c0 = l0 && !k0;
             c1 = l1 && !k1;
           }
-          if constexpr (SM == kSymMasks) {
+          if constexpr (kMask) {
             if (lane == 0) {
               W.B[a][rr] = row0;
               W.B[a + 1][rr] = row1;  // a + 1 <= 31: nb <= 32 and a is even
             }
-          } else if constexpr (SM == kSymCounts) {
+          } else {
             if (lane == 0) {
               W.hcnt[a] += __popc(row0);
               W.hcnt[a + 1] += __popc(row1);
             }
-          } else {
-            // queue every accepted pair: (home atom, candidate, forward flag); a
-            // pair of the centre is met from both of its atoms and added to
-            // each atom's own row, a forward pair to the row and the column
-            // (a ring of kLZRing entries: at most 31 + 64 are queued before a flush)
-            const unsigned lt = lt_mask();
-            if ((row0 >> lane) & 1u)
-              W.q[(qt + __popc(row0 & lt)) & (kLZRing - 1)] =
-                  unsigned(a) | (unsigned(c0 && fwd) << 5) | (unsigned(f) << 6);
-            qt += __popc(row0);
-            if ((row1 >> lane) & 1u)
-              W.q[(qt + __popc(row1 & lt)) & (kLZRing - 1)] =
-                  unsigned(a + 1) | (unsigned(c1 && fwd) << 5) | (unsigned(f) << 6);
-            qt += __popc(row1);
-            while (qt - qh >= 32) {
-              __syncwarp();
-              lazy_flush<TI>(A, g, cs_blk, W, qh, 32, lane);
-              qh += 32;
-            }
           }
-          if constexpr (SM != kSymInvR6) col |= (c0 ? 1u << a : 0u) | (c1 ? 2u << a : 0u);
+          col |= (c0 ? 1u << a : 0u) | (c1 ? 2u << a : 0u);
         }
-        if constexpr (SM == kSymMasks) {
+        if constexpr (kMask) {
           if (valid && fwd) {  // the candidate's word for its mirrored cell
             masks[kMaskStride * slot + (26 - qq)] = col;
             if (col) atomicAdd(A.counts + corig, __popc(col));
           }
-        } else if constexpr (SM == kSymCounts) {
+        } else {
           if (valid && fwd && col) atomicAdd(A.counts + corig, __popc(col));
         }
       }
       __syncwarp();
-      if constexpr (SM == kSymMasks) {  // the home atom itself (round 0, candidate a) is no pair
+      if constexpr (kMask) {  // the home atom itself (round 0, candidate a) is no pair
         if (lane < nb) W.B[lane][0] &= ~(1u << lane);
-        __syncwarp();
-      }
-      if constexpr (SM == kSymInvR6) {
-        __syncwarp();
-        if (qt > qh) lazy_flush<TI>(A, g, cs_blk, W, qh, qt - qh, lane);
-        __syncwarp();
-        // the cell's sums: its atoms' rows and its forward candidates' columns
-        if (lane < nb) {
-          const float2 h = W.hsum[lane];
-          if (h.x != 0.f || h.y != 0.f) atomicAdd(A.per_atom + W.horig[lane], dadd(f2d_exact(h.x), f2d_exact(h.y)));
-        }
-        for (int fc = lane; fc < T; fc += 32) {
-          const float2 c = W.csum[fc];
-          if (c.x != 0.f || c.y != 0.f)
-            atomicAdd(A.per_atom + clampi(A.perm[W.cslot[fc]] - 1, nat - 1), dadd(f2d_exact(c.x), f2d_exact(c.y)));
-        }
         __syncwarp();
       }
       if constexpr (SM == kSymCounts) {
         if (lane < nb && W.hcnt[lane]) atomicAdd(A.counts + W.horig[lane], W.hcnt[lane]);
         __syncwarp();
       }
-      if constexpr (SM == kSymMasks) {
+      if constexpr (kMask) {
       // rows: word q = 13..26 of every home atom, from its ballots
       for (int t0 = 0; t0 < nb * 14; t0 += 32) {
         const int t = t0 + lane;
@@ -2199,6 +2060,276 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
 }
 
 // ------------------------------------------------------------------------
+// Lazy sum of 1/r^6 per atom (NL_REDUCE_INV_R6_FAST) from the neighbour
+// masks of the symmetric count pass (k_sym_count<kSymMasksFix>, whose gather
+// rows carry fixed-point positions: x * 2^52 as 64-bit integers).  One lane
+// per sorted atom walks the atom's own pairs in the reference's traversal
+// order (stencil order, sorted order within each stencil cell), one set bit
+// per step, and sums 1/r2^3 over them.  R = Xj - Xi + C'S is exact in fixed
+// point (two integer subtractions and the C'S table in fixed point), then a
+// double-float; r2 and 1/r2^3 are double-float (relative error far below
+// 1e-12), and so is the sum.  No FP64 instruction is issued per pair: FP64
+// runs at a small fraction of the FP32 rate on this GPU.  When a position is
+// outside the fixed-point range (|x| >= 2000 A) or an atom is exact, R takes
+// the reference's FP64 operations (gpu_kernels.jl:88-91) from the sorted
+// positions instead.  r2 below 1e-12 (1/r2^3 beyond the FP32 range:
+// coincident or nearly coincident atoms) is evaluated in FP64 with the
+// reference's formula.  Each lane stores its atom's sum: no atomics, no pair
+// list, and the same result on every run.  A warp takes 32 consecutive sorted
+// atoms -- a few neighbouring cells, so the neighbours' 32-byte gather rows
+// mostly come from L1 -- keeps each lane's 27 mask words, stencil cell starts
+// and loop-shift codes in shared memory (rows of 33 words: lanes reading the
+// same word index hit distinct banks), and takes as many steps as its
+// busiest lane has pairs, two pairs per lane per step.
+constexpr int kLRWarps = 2;
+constexpr int kLRRow = 33;
+#ifndef NL_LR_MIN_BLOCKS
+#define NL_LR_MIN_BLOCKS 10
+#endif
+struct LRSmem {
+  unsigned m[32 * kLRRow];       // mask word q of lane a at a * kLRRow + q
+  unsigned st[32 * kLRRow];      // the sorted start of stencil cell q
+  unsigned char cd[32 * kLRRow];  // loop shift + 1 per axis of stencil cell q (2 bits each)
+};
+
+// v * 2^-52 (v a fixed-point value of magnitude below 2^63) as a double-float:
+// three 24-bit chunks are exact floats; their sum is formed with an
+// error-free two-sum and the smallest chunk added to the error term.
+__device__ __forceinline__ dfloat fix_to_df(long long v) {
+  const int a = int(v >> 48);
+  const unsigned b = unsigned((unsigned long long)v >> 24) & 0xFFFFFFu;
+  const unsigned c = unsigned(v) & 0xFFFFFFu;
+  const float fa = float(a) * 0x1p-4f, fb = float(b) * 0x1p-28f, fc = float(c) * 0x1p-52f;
+  const float s = fa + fb;
+  const float bb = s - fa;
+  const float e = ((fa - (s - bb)) + (fb - bb)) + fc;
+  return df_quick(s, e);
+}
+
+template <typename TI>
+__global__ void __launch_bounds__(kLRWarps * 32, NL_LR_MIN_BLOCKS) k_lazy_rows(PairArgs<TI> A) {
+  if (*A.sym_fail != 0) return;  // a crowded cell: the per-cell passes sum instead
+  __shared__ LRSmem sm[kLRWarps];
+  __shared__ double cs_blk[3 * kCsN * kCsN * kCsN];
+  __shared__ long long cs_fix[3 * kCsN * kCsN * kCsN];
+  const Geometry& g = A.g;
+  for (int t = threadIdx.x; t < 3 * kCsN * kCsN * kCsN; t += blockDim.x) {
+    const double c = A.cs_table[t];
+    cs_blk[t] = c;
+    cs_fix[t] = __double2ll_rn(dmul(c, kFixScale));
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  LRSmem& W = sm[warp];
+  unsigned* wm = W.m + lane * kLRRow;
+  unsigned* wst = W.st + lane * kLRRow;
+  unsigned char* wcd = W.cd + lane * kLRRow;
+  const int nat = g.nat;
+  const int sw = *A.sym_wound;
+  const bool plain = (sw & 1) == 0;   // no atom has a winding or is exact: S = the loop shift
+  const bool negzero = (sw & 2) != 0;  // a coordinate is -0 (FP64 pairs: the signed-zero rule for S = 0)
+  const bool fixed = (sw & 4) == 0;    // every position is in the fixed-point range, no atom is exact
+  const unsigned* masks = reinterpret_cast<const unsigned*>(A.lists);
+  const double* zc = cs_blk + 3 * ((kCsN * kCsN + kCsN + 1) * kCsR);  // C'(0,0,0): signed zeros
+  unsigned bad = 0;
+  const long long nwarps = (long long)gridDim.x * kLRWarps;
+  for (long long s0 = ((long long)blockIdx.x * kLRWarps + warp) * 32; s0 < nat; s0 += nwarps * 32) {
+    const bool own = s0 + lane < nat;
+    const int slot = int(min(s0 + lane, (long long)nat - 1));
+    const int hc = clampi(A.scell[slot], g.ncells - 1);
+    int n = 0;        // the atom's pairs
+    unsigned ne = 0;  // its non-empty words
+    {
+      int wx[3], wy[3], wz[3], sx[3], sy[3], sz[3];
+      bool okx[3], oky[3], okz[3];
+      axis3(hc % g.ns[0] + 1, g.ns[0], g.pbc[0], wx, sx, okx);
+      axis3((hc / g.ns[0]) % g.ns[1] + 1, g.ns[1], g.pbc[1], wy, sy, oky);
+      axis3(hc / (g.ns[0] * g.ns[1]) + 1, g.ns[2], g.pbc[2], wz, sz, okz);
+      uint4 mv[7];
+      const uint4* mrow = reinterpret_cast<const uint4*>(masks + kMaskStride * slot);
+#pragma unroll
+      for (int k = 0; k < 7; ++k) mv[k] = own ? __ldg(mrow + k) : make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+      for (int r = 0; r < 9; ++r) {
+        const int dy = r % 3, dz = r / 3;
+        const int rb = g.ns[0] * (wy[dy] + g.ns[1] * wz[dz]);
+        const bool rok = own && oky[dy] && okz[dz];
+#pragma unroll
+        for (int dx = 0; dx < 3; ++dx) {
+          const int q = 3 * r + dx;
+          wst[q] = unsigned(clampi((rok && okx[dx] ? A.cell_offsets[rb + wx[dx]] : TI(1)) - 1, nat));
+          wcd[q] = (unsigned char)(unsigned(sx[dx] + 1) | unsigned(sy[dy] + 1) << 2 | unsigned(sz[dz] + 1) << 4);
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 27; ++q) {
+        unsigned mq = (&mv[q >> 2].x)[q & 3];
+        if (mq && !(okx[q % 3] && oky[(q / 3) % 3] && okz[q / 9])) {  // a neighbour in a cell outside an open axis
+          bad |= kFlagInconsistent;
+          mq = 0u;
+        }
+        wm[q] = mq;
+        ne |= unsigned(mq != 0u) << q;
+        n += __popc(mq);
+      }
+    }
+    const XPack xp = A.xpk[slot];
+    const unsigned mi = xp.meta;
+    long long xf[3];  // fixed-point position
+    double xi[3];     // FP64 position (FP64 pairs)
+    xf[0] = __double_as_longlong(xp.x);
+    xf[1] = __double_as_longlong(xp.y);
+    xf[2] = __double_as_longlong(xp.z);
+    xi[0] = xi[1] = xi[2] = 0.0;
+    if (!fixed) {
+      xi[0] = A.Xs[3LL * slot + 0];
+      xi[1] = A.Xs[3LL * slot + 1];
+      xi[2] = A.Xs[3LL * slot + 2];
+    }
+    // the current word of the walk
+    unsigned w = 0u, stq = 0u, cq = 0u;
+    auto next_word = [&]() {
+      const int q = __ffs(ne) - 1;
+      ne &= ne - 1u;
+      w = wm[q];
+      stq = wst[q];
+      cq = wcd[q];
+    };
+    if (ne) next_word();
+    auto take = [&](bool on, int& j, unsigned& c) {
+      j = 0;
+      c = 21u;  // no loop shift
+      if (on) {
+        j = int(stq) + __ffs(w) - 1;
+        c = cq;
+        w &= w - 1u;
+        if (w == 0u && ne) next_word();
+      }
+    };
+    dfloat acc = {0.f, 0.f};
+    double accd = 0.0;  // the FP64-evaluated terms
+    // 1/r2^3 of the pair (atom, j) with loop-shift code c (0 when !on)
+    auto term = [&](bool on, int j, unsigned c, const double2& w0, const int4& w1) -> dfloat {
+      int S[3] = {int(c & 3u) - 1, int((c >> 2) & 3u) - 1, int((c >> 4) & 3u) - 1};
+      dfloat r2 = {0.f, 0.f};
+      double R[3];
+      if (fixed) {
+        if (!plain) {  // windings (no exact atoms here): S = s_loop + wi - wj
+          const unsigned cw = cand_word(cand_base(S[0], S[1], S[2]), unsigned(w1.w));
+#pragma unroll
+          for (int k = 0; k < 3; ++k) S[k] = field10(cw, k) + field10(mi, k) - 640;
+        }
+        long long rf[3];
+        rf[0] = __double_as_longlong(w0.x) - xf[0];
+        rf[1] = __double_as_longlong(w0.y) - xf[1];
+        rf[2] = (long long)(((unsigned long long)unsigned(w1.y) << 32) | unsigned(w1.x)) - xf[2];
+        const bool nz = on && (S[0] | S[1] | S[2]) != 0;
+        if (__any_sync(0xffffffffu, nz)) {
+          if (nz) {
+            if (abs(S[0]) <= kCsR && abs(S[1]) <= kCsR && abs(S[2]) <= kCsR) {
+              const long long* tb = cs_fix + 3 * ((S[0] + kCsR) + kCsN * ((S[1] + kCsR) + kCsN * (S[2] + kCsR)));
+              rf[0] += tb[0];
+              rf[1] += tb[1];
+              rf[2] += tb[2];
+            } else {
+#pragma unroll
+              for (int k = 0; k < 3; ++k) rf[k] += __double2ll_rn(dmul(cts_k(g.C, S[0], S[1], S[2], k), kFixScale));
+            }
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const dfloat d = fix_to_df(rf[k]);
+          r2 = df_add(r2, df_sq(d.hi, d.lo));
+        }
+        if (__any_sync(0xffffffffu, on && !(r2.hi >= 1e-12f))) {  // (rare) the FP64 positions for the formula
+          const double xj0 = A.Xs[3LL * min(unsigned(j), unsigned(nat - 1)) + 0];
+          const double xj1 = A.Xs[3LL * min(unsigned(j), unsigned(nat - 1)) + 1];
+          const double xj2 = A.Xs[3LL * min(unsigned(j), unsigned(nat - 1)) + 2];
+          const double xs0 = A.Xs[3LL * slot + 0], xs1 = A.Xs[3LL * slot + 1], xs2 = A.Xs[3LL * slot + 2];
+          const double xa[3] = {xs0, xs1, xs2}, xb[3] = {xj0, xj1, xj2};
+          pair_R(g, cs_blk, xa, xb, S[0], S[1], S[2], on, R);
+        }
+      } else {
+        const double xj[3] = {A.Xs[3LL * min(unsigned(j), unsigned(nat - 1)) + 0],
+                              A.Xs[3LL * min(unsigned(j), unsigned(nat - 1)) + 1],
+                              A.Xs[3LL * min(unsigned(j), unsigned(nat - 1)) + 2]};
+        if (!plain) {  // windings or exact atoms: S = s_loop + wi - wj
+          int T[3];
+          pair_S(g, xi, xj, mi, cand_word(cand_base(S[0], S[1], S[2]), unsigned(w1.w)), T);
+          S[0] = T[0];
+          S[1] = T[1];
+          S[2] = T[2];
+        }
+        R[0] = dsub(xj[0], xi[0]);
+        R[1] = dsub(xj[1], xi[1]);
+        R[2] = dsub(xj[2], xi[2]);
+        const bool nz = on && (S[0] | S[1] | S[2]) != 0;
+        if (__any_sync(0xffffffffu, nz)) {
+          if (nz) {
+            double c0, c1, c2;
+            if (abs(S[0]) <= kCsR && abs(S[1]) <= kCsR && abs(S[2]) <= kCsR) {
+              const double* tb = cs_blk + 3 * ((S[0] + kCsR) + kCsN * ((S[1] + kCsR) + kCsN * (S[2] + kCsR)));
+              c0 = tb[0];
+              c1 = tb[1];
+              c2 = tb[2];
+            } else {
+              c0 = cts_k(g.C, S[0], S[1], S[2], 0);
+              c1 = cts_k(g.C, S[0], S[1], S[2], 1);
+              c2 = cts_k(g.C, S[0], S[1], S[2], 2);
+            }
+            R[0] = dadd(R[0], c0);
+            R[1] = dadd(R[1], c1);
+            R[2] = dadd(R[2], c2);
+          }
+        }
+        if (negzero && !nz) {
+          R[0] = add_signed_zero(R[0], zc[0]);
+          R[1] = add_signed_zero(R[1], zc[1]);
+          R[2] = add_signed_zero(R[2], zc[2]);
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          float h, l, cc;
+          if (!split3(R[k], h, l, cc)) {  // |R_k| outside [2^-60, 2^60]
+            h = __double2float_rn(R[k]);
+            l = 0.f;
+          }
+          r2 = df_add(r2, df_sq(h, l));
+        }
+      }
+      dfloat f = {0.f, 0.f};
+      if (!on) return f;
+      if (!(r2.hi >= 1e-12f)) {
+        const double r2d = dot_ref(R);
+        accd += __ddiv_rn(1.0, dmul(dmul(r2d, r2d), r2d));
+        return f;
+      }
+      const dfloat y = df_rcp(r2);
+      return df_mul(df_mul(y, y), y);
+    };
+    const int smax = __reduce_max_sync(0xffffffffu, own ? n : 0);
+    for (int s = 0; s < smax; s += 2) {  // two pairs per lane: their gathers in flight together
+      int j0, j1;
+      unsigned c0, c1;
+      const bool on0 = own && s < n, on1 = own && s + 1 < n;
+      take(on0, j0, c0);
+      take(on1, j1, c1);
+      const XPack* p0 = A.xpk + min(unsigned(j0), unsigned(nat - 1));
+      const XPack* p1 = A.xpk + min(unsigned(j1), unsigned(nat - 1));
+      const double2 a0 = __ldg(reinterpret_cast<const double2*>(p0));
+      const int4 b0 = __ldg(reinterpret_cast<const int4*>(p0) + 1);
+      const double2 a1 = __ldg(reinterpret_cast<const double2*>(p1));
+      const int4 b1 = __ldg(reinterpret_cast<const int4*>(p1) + 1);
+      acc = df_add(acc, term(on0, j0, c0, a0, b0));
+      acc = df_add(acc, term(on1, j1, c1, a1, b1));
+    }
+    if (own) A.per_atom[clampi(int(xp.perm) - 1, nat - 1)] = dadd(dadd(f2d_exact(acc.hi), f2d_exact(acc.lo)), accd);
+  }
+  if (bad) atomicOr(A.err, bad);
+}
+
+// ------------------------------------------------------------------------
 // Count pass with one thread per home atom.  Each thread walks its own
 // stencil in the reference's order (dz, dy, dx; then the cell's atoms in
 // sorted order), screens every candidate with the same FP32 arithmetic as
@@ -2528,7 +2659,11 @@ void launch_sym_lazy(int what, const PairArgs<TI>& a, int num_sms, cudaStream_t 
     k_sym_count<TI, kSymCounts><<<int(sb), kSCWarps * 32, 0, st>>>(a);
   } else {
     k_cs_table<<<1, 128, 0, st>>>(a.g, a.cs_table, nullptr, 0, a.err);
-    k_sym_count<TI, kSymInvR6><<<int(sb), kSCWarps * 32, 0, st>>>(a);
+    // the neighbour masks with fixed-point gather rows, then each atom's sum from its masks
+    k_sym_count<TI, kSymMasksFix><<<int(sb), kSCWarps * 32, 0, st>>>(a);
+    long long lb = ((long long)a.nat_total + 32 * kLRWarps - 1) / (32 * kLRWarps);
+    if (lb > (long long)num_sms * 2 * NL_LR_MIN_BLOCKS) lb = (long long)num_sms * 2 * NL_LR_MIN_BLOCKS;
+    k_lazy_rows<TI><<<int(lb), kLRWarps * 32, 0, st>>>(a);
   }
 }
 template void launch_sym_lazy<int32_t>(int, const PairArgs<int32_t>&, int, cudaStream_t);
