@@ -48,8 +48,8 @@ extern "C" {
 /* lazy reductions (nl_lazy_reduce) */
 #define NL_REDUCE_COUNT 0         /* int32 per atom: count_neighbours (cell_list.jl:808-814) */
 #define NL_REDUCE_INV_R6 1        /* double per atom: sum over neighbours of 1/r^6, in traversal order (bit-exact) */
-#define NL_REDUCE_INV_R6_FAST 2   /* the same sum by the fused symmetric pass: relative error <= 1e-12, last bits
-                                     vary with the order of the atomic additions */
+#define NL_REDUCE_INV_R6_FAST 2   /* the same sum from the neighbour masks, each unordered pair once: relative
+                                     error <= 1e-12, last bits vary with the order of the atomic additions */
 
 /* Cell analysis: the reference's analyze_cell (cell_list.jl:152-170) plus the
  * stencil half-width nxyz of materialize_pairlist (gpu_kernels.jl:315-316),

@@ -421,8 +421,9 @@ def lazy_reduce(clist: SortedCellList, op: str = "count", stream=None, out: Opti
     "count" -> int32 neighbour count per atom (count_neighbours for all i);
     "inv_r6" -> float64 per-atom sum of 1/r^6 in the reference's order
     (bit-identical to a sequential for_each_neighbour sum);
-    "inv_r6_fast" -> the same sums from one fused pass over unordered pairs
-    (relative error at most 1e-12, last bits not reproducible run to run).
+    "inv_r6_fast" -> the same sums from the neighbour masks, each unordered
+    pair once with exact fixed-point R (relative error at most 1e-12, last bits
+    not reproducible run to run).
     ``out`` reuses an output tensor; ``sync=False`` leaves the error check to
     a later nl_sync_status on the cell list's workspace."""
     nat = int(clist.X.shape[0])

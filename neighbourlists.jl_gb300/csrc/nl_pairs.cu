@@ -2084,7 +2084,10 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
 constexpr int kLRWarps = 2;
 constexpr int kLRRow = 33;
 #ifndef NL_LR_MIN_BLOCKS
-#define NL_LR_MIN_BLOCKS 10
+#define NL_LR_MIN_BLOCKS 8
+#endif
+#ifndef NL_LR_HALF
+#define NL_LR_HALF 1  // each unordered pair once (0: every atom walks all its pairs, no atomics)
 #endif
 struct LRSmem {
   unsigned m[32 * kLRRow];       // mask word q of lane a at a * kLRRow + q
@@ -2161,12 +2164,17 @@ __global__ void __launch_bounds__(kLRWarps * 32, NL_LR_MIN_BLOCKS) k_lazy_rows(P
           wcd[q] = (unsigned char)(unsigned(sx[dx] + 1) | unsigned(sy[dy] + 1) << 2 | unsigned(sz[dz] + 1) << 4);
         }
       }
+      const int me = slot - int(wst[13]);  // the atom's place in its own cell (bit of the centre word)
 #pragma unroll
       for (int q = 0; q < 27; ++q) {
         unsigned mq = (&mv[q >> 2].x)[q & 3];
         if (mq && !(okx[q % 3] && oky[(q / 3) % 3] && okz[q / 9])) {  // a neighbour in a cell outside an open axis
           bad |= kFlagInconsistent;
           mq = 0u;
+        }
+        if (NL_LR_HALF) {  // each unordered pair from one side: forward cells, and later atoms of the centre
+          if (q < 13) mq = 0u;
+          if (q == 13) mq &= me >= 0 && me < 32 ? ~((2u << me) - 1u) : 0u;
         }
         wm[q] = mq;
         ne |= unsigned(mq != 0u) << q;
@@ -2208,8 +2216,10 @@ __global__ void __launch_bounds__(kLRWarps * 32, NL_LR_MIN_BLOCKS) k_lazy_rows(P
     };
     dfloat acc = {0.f, 0.f};
     double accd = 0.0;  // the FP64-evaluated terms
-    // 1/r2^3 of the pair (atom, j) with loop-shift code c (0 when !on)
-    auto term = [&](bool on, int j, unsigned c, const double2& w0, const int4& w1) -> dfloat {
+    // 1/r2^3 of the pair (atom, j) with loop-shift code c (0 when !on): a
+    // double-float, or (r2 below 1e-12) an FP64 value in fr
+    auto term = [&](bool on, int j, unsigned c, const double2& w0, const int4& w1, double& fr) -> dfloat {
+      fr = 0.0;
       int S[3] = {int(c & 3u) - 1, int((c >> 2) & 3u) - 1, int((c >> 4) & 3u) - 1};
       dfloat r2 = {0.f, 0.f};
       double R[3];
@@ -2302,7 +2312,7 @@ __global__ void __launch_bounds__(kLRWarps * 32, NL_LR_MIN_BLOCKS) k_lazy_rows(P
       if (!on) return f;
       if (!(r2.hi >= 1e-12f)) {
         const double r2d = dot_ref(R);
-        accd += __ddiv_rn(1.0, dmul(dmul(r2d, r2d), r2d));
+        fr = __ddiv_rn(1.0, dmul(dmul(r2d, r2d), r2d));
         return f;
       }
       const dfloat y = df_rcp(r2);
@@ -2321,10 +2331,22 @@ __global__ void __launch_bounds__(kLRWarps * 32, NL_LR_MIN_BLOCKS) k_lazy_rows(P
       const int4 b0 = __ldg(reinterpret_cast<const int4*>(p0) + 1);
       const double2 a1 = __ldg(reinterpret_cast<const double2*>(p1));
       const int4 b1 = __ldg(reinterpret_cast<const int4*>(p1) + 1);
-      acc = df_add(acc, term(on0, j0, c0, a0, b0));
-      acc = df_add(acc, term(on1, j1, c1, a1, b1));
+      double r0, r1;
+      const dfloat f0 = term(on0, j0, c0, a0, b0, r0), f1 = term(on1, j1, c1, a1, b1, r1);
+      acc = df_add(df_add(acc, f0), f1);
+      accd += r0 + r1;
+      if (NL_LR_HALF) {  // the neighbour's share of the pair
+        if (on0) atomicAdd(A.per_atom + clampi(b0.z - 1, nat - 1), dadd(dadd(f2d_exact(f0.hi), f2d_exact(f0.lo)), r0));
+        if (on1) atomicAdd(A.per_atom + clampi(b1.z - 1, nat - 1), dadd(dadd(f2d_exact(f1.hi), f2d_exact(f1.lo)), r1));
+      }
     }
-    if (own) A.per_atom[clampi(int(xp.perm) - 1, nat - 1)] = dadd(dadd(f2d_exact(acc.hi), f2d_exact(acc.lo)), accd);
+    if (own) {
+      const double tot = dadd(dadd(f2d_exact(acc.hi), f2d_exact(acc.lo)), accd);
+      if (NL_LR_HALF)
+        atomicAdd(A.per_atom + clampi(int(xp.perm) - 1, nat - 1), tot);
+      else
+        A.per_atom[clampi(int(xp.perm) - 1, nat - 1)] = tot;
+    }
   }
   if (bad) atomicOr(A.err, bad);
 }

@@ -76,16 +76,18 @@ def test_query_rejects_out_of_range_atoms(nlpkg):
     assert nlpkg.count_neighbours(clist, 1000) >= 0  # the error word was cleared
 
 
-LAZY_RTOL = 1e-12  # the fused pass's stated relative tolerance on the per-atom sums
+LAZY_RTOL = 1e-12  # the fast sum's stated relative tolerance on the per-atom sums
 
 
 @pytest.mark.parametrize("case", range(6))
 def test_fused_lazy_sum_and_count(nlpkg, orc, case):
-    """The fused symmetric lazy pass (NL_REDUCE_INV_R6_FAST): per-atom sums of
-    1/r^6 within 1e-12 of the oracle's FP64 traversal, per-atom counts equal
-    to the oracle's, on geometries it takes (cubic, mixed and open boundaries,
-    sheared triclinic, atoms far outside an open axis) and on ones it hands
-    to the traversal-order passes (the diamond cell's 5x5x5 stencil)."""
+    """The fast lazy sum (NL_REDUCE_INV_R6_FAST: the mask pass, then each
+    unordered pair once with fixed-point R) and the fused lazy count: per-atom
+    sums of 1/r^6 within 1e-12 of the oracle's FP64 traversal, per-atom
+    counts equal to the oracle's, on geometries they take (cubic, mixed and
+    open boundaries, sheared triclinic, atoms far outside an open axis: FP64
+    R) and on ones they hand to the traversal-order passes (the diamond
+    cell's 5x5x5 stencil)."""
     X, C, rc, pbc = _cases()[case]
     clist = nlpkg.build_cell_list(torch.from_numpy(np.ascontiguousarray(X)).cuda(), rc, C, pbc)
     oc = orc.build_cell_list(X, rc, C, pbc)
@@ -99,7 +101,7 @@ def test_fused_lazy_sum_and_count(nlpkg, orc, case):
 
 
 def test_fused_lazy_crowded_cell_falls_back(nlpkg, orc):
-    """A cell of more than 32 atoms: the fused pass gives up and the
+    """A cell of more than 32 atoms: the mask pass gives up and the
     traversal-order passes produce every sum (then bit-identical)."""
     rng = np.random.default_rng(18)
     X, C, L = cf.rand_config(3000, seed=19)
@@ -128,3 +130,24 @@ def test_fused_lazy_close_pairs(nlpkg, orc):
     assert np.array_equal(np.isfinite(got), fin) and np.all(got[~fin] == ref[~fin])
     rel = np.abs(got[fin] - ref[fin]) / np.abs(ref[fin])
     assert rel.max() <= LAZY_RTOL, rel.max()
+
+
+def test_fast_lazy_sum_windings_and_far_positions(nlpkg, orc):
+    """The fast sum's two position paths: atoms wound once around periodic
+    axes (fixed-point R, S from the windings) and a chain of atoms reaching
+    beyond 2000 A along an open axis (outside the fixed-point range: R with
+    the reference's FP64 operations)."""
+    X, C, L = cf.rand_config(3000, seed=21)
+    Xw = X.copy()
+    Xw[:200, 0] += L          # winding +1 on x
+    Xw[200:400, 1] -= 2 * L   # winding -2 on y
+    rng = np.random.default_rng(22)
+    n = 1300
+    Xc = np.stack([np.arange(n) * 2.0 + rng.uniform(-0.3, 0.3, n), rng.uniform(0, 16, n), rng.uniform(0, 16, n)], 1)
+    Cc = np.diag([2.0 * n, 16.0, 16.0])  # 3 cells across y and z: the mask pass takes it
+    for Xs, Cs, pbc in ((Xw, C, (True, True, True)), (Xc, Cc, (False, True, True))):
+        clist = nlpkg.build_cell_list(torch.from_numpy(np.ascontiguousarray(Xs)).cuda(), 5.0, Cs, pbc)
+        ref = orc.lazy_sum_r6(orc.build_cell_list(Xs, 5.0, Cs, pbc))
+        got = nlpkg.lazy_reduce(clist, "inv_r6_fast").cpu().numpy()
+        rel = np.abs(got - ref) / np.maximum(np.abs(ref), 1e-300)
+        assert rel.max() <= LAZY_RTOL, rel.max()
