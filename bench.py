@@ -43,8 +43,10 @@ METRIC = "pairs/s (1M atoms, rc 5 A, density 0.05, full pbc, Float64, build_cell
 WORKLOAD = "uniform 1,000,000 atoms, density 0.05 A^-3, cubic pbc box (L=271.44 A), cutoff 5 A, Float64, Int32 indices"
 ALGO_BYTES_PER_ATOM = 24  # positions read
 ALGO_BYTES_PER_PAIR = 44  # i 4 + j 4 + S 12 + R 24 written
-# kernels of one step: k_bin, k_scan_offsets (cells), k_scatter, k_fix, k_fix_big,
-# k_pairs<count>, k_scan_offsets (pairs), k_cs_table, k_emit, k_pairs<fill>
+# kernels of one step: k_bin, k_scan_offsets (cells), k_scatter, k_fix, k_fix_big (build);
+# k_sym_count, k_pairs<count> (returns at once after the symmetric pass), k_scan_offsets
+# (pairs) (count); k_cs_table, k_emit<lists> and k_pairs<fill> (both return at once),
+# k_emit_orig (write)
 LAUNCHES_PER_STEP = 12  # kernels of one step: build 5, count 3 (with its scan), write 4
 
 
@@ -78,8 +80,9 @@ def measured_peaks():
 
 
 def ncu_traffic():
-    """Per-launch DRAM bytes of the fill kernel from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "k_emit_1M_traffic.json")
+    """Per-launch DRAM bytes of the write kernel (k_emit_orig) at 1M atoms from the
+    committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "k_emit_orig_1M_traffic.json")
     if os.path.exists(p):
         with open(p) as f:
             return json.load(f)
@@ -322,7 +325,7 @@ def run_gpu(args):
         "timing": {"cuda_graph": True, "ms_per_step_without_graph": launch_ms,
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_kind": peak_kind, "kernel": "write pass (k_emit<masks> + k_cs_table + k_pairs<fill>)",
+                     "peak_kind": peak_kind, "kernel": "write pass (k_emit_orig + k_cs_table; k_emit<lists>, k_pairs<fill> return at once)",
                      "algorithmic_bytes": algo_bytes, "kernel_ms": fill_ms,
                      "traffic": (traffic or {}).get("dram_bytes_per_launch")},
         "step_roofline_frac": algo_bytes / (step_ms * 1e-3) / 1e9 / peak,

@@ -2336,8 +2336,13 @@ __global__ void __launch_bounds__(kLRWarps * 32, NL_LR_MIN_BLOCKS) k_lazy_rows(P
       acc = df_add(df_add(acc, f0), f1);
       accd += r0 + r1;
       if (NL_LR_HALF) {  // the neighbour's share of the pair
-        if (on0) atomicAdd(A.per_atom + clampi(b0.z - 1, nat - 1), dadd(dadd(f2d_exact(f0.hi), f2d_exact(f0.lo)), r0));
-        if (on1) atomicAdd(A.per_atom + clampi(b1.z - 1, nat - 1), dadd(dadd(f2d_exact(f1.hi), f2d_exact(f1.lo)), r1));
+        double v0 = dadd(f2d_exact(f0.hi), f2d_exact(f0.lo)), v1 = dadd(f2d_exact(f1.hi), f2d_exact(f1.lo));
+        if (__any_sync(0xffffffffu, r0 != 0.0 || r1 != 0.0)) {  // (rare) FP64-evaluated terms
+          v0 = dadd(v0, r0);
+          v1 = dadd(v1, r1);
+        }
+        if (on0) atomicAdd(A.per_atom + clampi(b0.z - 1, nat - 1), v0);
+        if (on1) atomicAdd(A.per_atom + clampi(b1.z - 1, nat - 1), v1);
       }
     }
     if (own) {
