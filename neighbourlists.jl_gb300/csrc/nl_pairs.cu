@@ -97,6 +97,66 @@ __device__ __forceinline__ double add_signed_zero(double d, double z) {
   return (bd << 1) != 0 ? d : __longlong_as_double(bd & __double_as_longlong(z));
 }
 
+// L2 residency of the 32-byte gather rows (XPack): the write pass gathers
+// each row ~26 times from anywhere in the array while it streams the masks
+// and headers in and the pair arrays out, so the gathers load with an
+// evict-last L2 policy and the read-once data with evict-first (cache-
+// streaming) loads.  At 1M atoms this took the write pass's DRAM reads from
+// 724 to 585 MB per launch (NL_L2_HINTS=0 builds plain loads).  Storing the
+// rows with the same policy in the count pass slowed the count pass down.
+#ifndef NL_L2_HINTS
+#define NL_L2_HINTS 1
+#endif
+#ifndef NL_L2_HINTS_STORE
+#define NL_L2_HINTS_STORE 0  // 1: the count pass stores the rows with the same policy (slower count pass)
+#endif
+__device__ __forceinline__ unsigned long long l2_keep_policy() {
+  unsigned long long p = 0;
+#if NL_L2_HINTS
+  asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+#endif
+  return p;
+}
+__device__ __forceinline__ double2 ld_keep(const double2* ptr, unsigned long long pol) {
+#if NL_L2_HINTS
+  double2 v;
+  asm("ld.global.nc.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;" : "=d"(v.x), "=d"(v.y) : "l"(ptr), "l"(pol));
+  return v;
+#else
+  return __ldg(ptr);
+#endif
+}
+__device__ __forceinline__ int4 ld_keep(const int4* ptr, unsigned long long pol) {
+#if NL_L2_HINTS
+  int4 v;
+  asm("ld.global.nc.L2::cache_hint.v4.s32 {%0, %1, %2, %3}, [%4], %5;"
+      : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+      : "l"(ptr), "l"(pol));
+  return v;
+#else
+  return __ldg(ptr);
+#endif
+}
+__device__ __forceinline__ void st_keep(XPack* dst, const XPack& v, unsigned long long pol) {
+#if NL_L2_HINTS && NL_L2_HINTS_STORE
+  double2* d = reinterpret_cast<double2*>(dst);
+  asm volatile("st.global.L2::cache_hint.v2.f64 [%0], {%1, %2}, %3;" ::"l"(d), "d"(v.x), "d"(v.y), "l"(pol));
+  asm volatile("st.global.L2::cache_hint.v4.s32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(d + 1),
+               "r"(__double2loint(v.z)), "r"(__double2hiint(v.z)), "r"(v.perm), "r"(int(v.meta)), "l"(pol));
+#else
+  *dst = v;
+#endif
+}
+// read-once data: evict first from L1 and L2
+template <typename T>
+__device__ __forceinline__ T ld_stream(const T* ptr) {
+#if NL_L2_HINTS
+  return __ldcs(ptr);
+#else
+  return __ldg(ptr);
+#endif
+}
+
 // R = (xj - xi) + C'S with the reference's operation order.  The three sums
 // with C'S are only issued when the warp holds a pair with S != 0 (for S == 0
 // C'S is a vector of signed zeros and the sum is exact, see add_signed_zero).
@@ -1257,7 +1317,7 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
             xp.z = X2;
             xp.perm = o + 1;
             xp.meta = hm;
-            A.xpk[hs + lane] = xp;
+            st_keep(A.xpk + hs + lane, xp, l2_keep_policy());
             const long long nz = (long long)0x8000000000000000ULL;
             if (__double_as_longlong(X0) == nz || __double_as_longlong(X1) == nz || __double_as_longlong(X2) == nz)
               atomicOr(A.sym_wound, 2);
@@ -1269,7 +1329,7 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
             xp.z = __longlong_as_double(__double2ll_rn(dmul(X2, kFixScale)));
             xp.perm = o + 1;
             xp.meta = hm;
-            A.xpk[hs + lane] = xp;
+            st_keep(A.xpk + hs + lane, xp, l2_keep_policy());
             if (!(fabs(X0) < kFixMax && fabs(X1) < kFixMax && fabs(X2) < kFixMax) || (hm & kExactBit))
               atomicOr(A.sym_wound, 4);  // out of the fixed-point range, or exact: FP64 pairs instead
           }
@@ -1788,6 +1848,9 @@ __global__ void __launch_bounds__(kEmitWarps * 32,
 #ifndef NL_EO_PASSES
 #define NL_EO_PASSES 2  // passes whose gathers are in flight together
 #endif
+#ifndef NL_EO_PLANES
+#define NL_EO_PLANES 0  // 1: masks and cell starts loaded one stencil plane at a time (fewer registers)
+#endif
 constexpr int kEOWarps = 2;
 constexpr int kEOEnt = 1024;  // pair entries per warp
 constexpr int kEOPasses = NL_EO_PASSES;
@@ -1848,6 +1911,7 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
   const unsigned* masks = reinterpret_cast<const unsigned*>(A.lists);
   const long long cap = A.capacity;
   const double* zc = cs_blk + 3 * ((kCsN * kCsN + kCsN + 1) * kCsR);  // C'(0,0,0): signed zeros
+  const unsigned long long keep = l2_keep_policy();
   unsigned bad = 0;  // error flags of this lane
   const long long nwarps = (long long)gridDim.x * kEOWarps;
   for (long long o0 = ((long long)blockIdx.x * kEOWarps + warp) * 32; o0 < nat; o0 += nwarps * 32) {
@@ -1858,7 +1922,7 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
     long long f = 0, n = 0;
     if (own) {
       const long long o = o0 + lane;
-      hd = A.hdr[o];
+      hd = ld_stream(A.hdr + o);
       f = (long long)A.first[o] - 1;
       n = (long long)A.first[o + 1] - 1 - f;
     }
@@ -1884,11 +1948,62 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
         axis3(hc % g.ns[0] + 1, g.ns[0], g.pbc[0], wx, sx, okx);
         axis3((hc / g.ns[0]) % g.ns[1] + 1, g.ns[1], g.pbc[1], wy, sy, oky);
         axis3(hc / (g.ns[0] * g.ns[1]) + 1, g.ns[2], g.pbc[2], wz, sz, okz);
+#if NL_EO_PLANES
+        if (mine) {
+          E.xi[lane][0] = A.Xs[3LL * slot + 0];
+          E.xi[lane][1] = A.Xs[3LL * slot + 1];
+          E.xi[lane][2] = A.Xs[3LL * slot + 2];
+          E.mi[lane] = __float_as_uint(A.rec[slot].w);
+        }
+        // ---- the lane's non-empty words, listed at the end of its stretch
+        // [e0, e0 + nn) of the table (each holds a bit: nnz <= nn), written
+        // from the last word down.  The mask words and cell starts are
+        // loaded one stencil plane (dz) at a time, so that at most one
+        // plane's nine words and starts are held at once.
+        const uint4* mrow = reinterpret_cast<const uint4*>(masks + kMaskStride * slot);
+        const int e0 = mine ? int(f - G) + int(G & 31) : 0;  // the entry of output position p sits at p - (G - G mod 32)
+        const int nn = mine ? int(n) : 0;
+        int nnz = 0, tot = 0;
+#pragma unroll
+        for (int dz = 2; dz >= 0; --dz) {
+          const int u0 = (9 * dz) >> 2;  // the 16-byte words holding mask words 9 dz .. 9 dz + 8
+          uint4 mv[3];
+#pragma unroll
+          for (int k = 0; k < 3; ++k) mv[k] = mine ? __ldg(mrow + u0 + k) : make_uint4(0u, 0u, 0u, 0u);
+          unsigned st[9];
+#pragma unroll
+          for (int dy = 0; dy < 3; ++dy) {
+            const int rb = g.ns[0] * (wy[dy] + g.ns[1] * wz[dz]);
+            const bool rok = mine && oky[dy] && okz[dz];
+#pragma unroll
+            for (int dx = 0; dx < 3; ++dx)
+              st[3 * dy + dx] = unsigned(clampi((rok && okx[dx] ? A.cell_offsets[rb + wx[dx]] : TI(1)) - 1, nat));
+          }
+#pragma unroll
+          for (int r = 8; r >= 0; --r) {
+            const int q = 9 * dz + r, dx = r % 3, dy = r / 3;
+            unsigned mq = (&mv[(q >> 2) - u0].x)[q & 3];
+            if (mq && !(okx[dx] && oky[dy] && okz[dz])) {  // a neighbour in a cell outside an open axis
+              bad |= kFlagInconsistent;
+              mq = 0u;
+            }
+            if (mq) {
+              if (nnz < nn && e0 >= 0) {
+                const int k = e0 + nn - 1 - nnz;
+                E.ent[k] = make_uint2(mq, st[r]);
+                E.code[k] = (unsigned char)(unsigned(sx[dx] + 1) | unsigned(sy[dy] + 1) << 2 | unsigned(sz[dz] + 1) << 4);
+              }
+              ++nnz;
+              tot += __popc(mq);
+            }
+          }
+        }
+#else
         // masks, position, meta and the 27 stencil cell starts, all in flight together
         uint4 mv[7];
         const uint4* mrow = reinterpret_cast<const uint4*>(masks + kMaskStride * slot);
 #pragma unroll
-        for (int k = 0; k < 7; ++k) mv[k] = mine ? __ldg(mrow + k) : make_uint4(0u, 0u, 0u, 0u);
+        for (int k = 0; k < 7; ++k) mv[k] = mine ? ld_stream(mrow + k) : make_uint4(0u, 0u, 0u, 0u);
         unsigned st[27];
 #pragma unroll
         for (int r = 0; r < 9; ++r) {
@@ -1930,6 +2045,7 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
             tot += __popc(mq);
           }
         }
+#endif
         const bool lok = mine && tot == nn && e0 >= 0;
         if (mine && !lok) bad |= kFlagInconsistent;  // counts and masks disagree
         const int li = e0 + nn - nnz;  // the first listed word
@@ -1984,8 +2100,8 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
       auto load = [&](int k, Ld& u) {
         u.en = E.ent[min(max(k, off), hix - 1)];
         const XPack* xp = A.xpk + min(u.en.x, unsigned(nat - 1));
-        u.w0 = __ldg(reinterpret_cast<const double2*>(xp));
-        u.w1 = __ldg(reinterpret_cast<const int4*>(xp) + 1);
+        u.w0 = ld_keep(reinterpret_cast<const double2*>(xp), keep);
+        u.w1 = ld_keep(reinterpret_cast<const int4*>(xp) + 1, keep);
       };
       auto write = [&](int k, const Ld& u) {
         const bool act = k >= off && k < hix;
@@ -2133,6 +2249,7 @@ __global__ void __launch_bounds__(kLRWarps * 32, NL_LR_MIN_BLOCKS) k_lazy_rows(P
   const bool negzero = (sw & 2) != 0;  // a coordinate is -0 (FP64 pairs: the signed-zero rule for S = 0)
   const bool fixed = (sw & 4) == 0;    // every position is in the fixed-point range, no atom is exact
   const unsigned* masks = reinterpret_cast<const unsigned*>(A.lists);
+  const unsigned long long keep = l2_keep_policy();
   const double* zc = cs_blk + 3 * ((kCsN * kCsN + kCsN + 1) * kCsR);  // C'(0,0,0): signed zeros
   unsigned bad = 0;
   const long long nwarps = (long long)gridDim.x * kLRWarps;
@@ -2151,7 +2268,7 @@ __global__ void __launch_bounds__(kLRWarps * 32, NL_LR_MIN_BLOCKS) k_lazy_rows(P
       uint4 mv[7];
       const uint4* mrow = reinterpret_cast<const uint4*>(masks + kMaskStride * slot);
 #pragma unroll
-      for (int k = 0; k < 7; ++k) mv[k] = own ? __ldg(mrow + k) : make_uint4(0u, 0u, 0u, 0u);
+      for (int k = 0; k < 7; ++k) mv[k] = own ? ld_stream(mrow + k) : make_uint4(0u, 0u, 0u, 0u);
 #pragma unroll
       for (int r = 0; r < 9; ++r) {
         const int dy = r % 3, dz = r / 3;
@@ -2327,10 +2444,10 @@ __global__ void __launch_bounds__(kLRWarps * 32, NL_LR_MIN_BLOCKS) k_lazy_rows(P
       take(on1, j1, c1);
       const XPack* p0 = A.xpk + min(unsigned(j0), unsigned(nat - 1));
       const XPack* p1 = A.xpk + min(unsigned(j1), unsigned(nat - 1));
-      const double2 a0 = __ldg(reinterpret_cast<const double2*>(p0));
-      const int4 b0 = __ldg(reinterpret_cast<const int4*>(p0) + 1);
-      const double2 a1 = __ldg(reinterpret_cast<const double2*>(p1));
-      const int4 b1 = __ldg(reinterpret_cast<const int4*>(p1) + 1);
+      const double2 a0 = ld_keep(reinterpret_cast<const double2*>(p0), keep);
+      const int4 b0 = ld_keep(reinterpret_cast<const int4*>(p0) + 1, keep);
+      const double2 a1 = ld_keep(reinterpret_cast<const double2*>(p1), keep);
+      const int4 b1 = ld_keep(reinterpret_cast<const int4*>(p1) + 1, keep);
       double r0, r1;
       const dfloat f0 = term(on0, j0, c0, a0, b0, r0), f1 = term(on1, j1, c1, a1, b1, r1);
       acc = df_add(df_add(acc, f0), f1);
