@@ -306,6 +306,32 @@ int nl_neighbour_list_f32(const float* d_X, int64_t nat, const float cell[9], co
                           void* d_first, int64_t capacity, void* d_i, void* d_j, void* d_S, float* d_R,
                           int64_t* total_pairs, void* d_workspace, size_t workspace_bytes, void* stream);
 
+/* Float32 batches: as nl_batch_create / nl_batch_neighbour_list with
+ * T = Float32 for every system (cell, cutoff and the nl_analyze_cell_f32
+ * results in Float32; positions, sorted positions and R in Float32).
+ * nl_batch_workspace_bytes, nl_batch_sizes, nl_batch_upload, nl_batch_destroy
+ * and nl_batch_set_tuning take either kind of batch; each run entry takes
+ * only its own kind (NL_ERR_ARG otherwise).  Every per-system output equals a
+ * single-system nl_neighbour_list_f32 call. */
+typedef struct nl_system_f32 {
+  int64_t nat;
+  float cell[9];        /* column-major, rows = lattice vectors */
+  float inv_cell[9];    /* the nl_analyze_cell_f32 results */
+  int64_t ncells[3];
+  int64_t nxyz[3];
+  uint8_t pbc[3];
+  float cutoff;
+} nl_system_f32;
+int nl_batch_create_f32(const nl_system_f32* systems, int nsys, int index_bytes, nl_batch** batch);
+/* Same from raw systems (cells[9*s..] column-major, cutoffs[s] in Float32):
+ * the Float32 cell analysis runs inside, as nl_batch_create_auto. */
+int nl_batch_create_auto_f32(const float* cells, const float* cutoffs, const uint8_t* pbc, const int64_t* nat,
+                             int nsys, int index_bytes, nl_batch** batch);
+int nl_batch_neighbour_list_f32(const nl_batch* batch, const float* d_X, void* d_perm, float* d_X_sorted,
+                                void* d_cell_id, void* d_cell_offsets, void* d_first, int64_t* d_pair_offsets,
+                                int64_t capacity, void* d_i, void* d_j, void* d_S, float* d_R, int64_t* total_pairs,
+                                void* d_workspace, size_t workspace_bytes, void* stream);
+
 /* ---- legacy linked-list PairList -----------------------------------------
  * The reference's legacy constructor PairList(X::Vector{SVec}, cutoff, cell,
  * pbc; int_type, fixcell) (cell_list.jl:11-20, _pairlist_ :369-385), kept

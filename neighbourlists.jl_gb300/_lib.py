@@ -51,6 +51,9 @@ EXPORTED = [
     "nl_batch_sizes",
     "nl_batch_upload",
     "nl_batch_neighbour_list",
+    "nl_batch_create_f32",
+    "nl_batch_create_auto_f32",
+    "nl_batch_neighbour_list_f32",
     "nl_analyze_cell_f32",
     "nl_build_cell_list_f32",
     "nl_count_pairs_f32",
@@ -101,6 +104,19 @@ class System(C.Structure):
         ("nxyz", C.c_int64 * 3),
         ("pbc", C.c_uint8 * 3),
         ("cutoff", C.c_double),
+    ]
+
+
+class SystemF32(C.Structure):
+    """nl_system_f32: one system of a Float32 batch."""
+    _fields_ = [
+        ("nat", C.c_int64),
+        ("cell", C.c_float * 9),
+        ("inv_cell", C.c_float * 9),
+        ("ncells", C.c_int64 * 3),
+        ("nxyz", C.c_int64 * 3),
+        ("pbc", C.c_uint8 * 3),
+        ("cutoff", C.c_float),
     ]
 
 
@@ -172,6 +188,13 @@ def _declare(L):
     L.nl_batch_neighbour_list.argtypes = [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int64, _vp, _vp, _vp, _vp, _I64,
                                           _vp, C.c_size_t, _vp]
     L.nl_batch_neighbour_list.restype = C.c_int
+    L.nl_batch_create_f32.argtypes = [C.POINTER(SystemF32), C.c_int, C.c_int, C.POINTER(_vp)]
+    L.nl_batch_create_f32.restype = C.c_int
+    L.nl_batch_create_auto_f32.argtypes = [_vp, _vp, _vp, _vp, C.c_int, C.c_int, C.POINTER(_vp)]
+    L.nl_batch_create_auto_f32.restype = C.c_int
+    L.nl_batch_neighbour_list_f32.argtypes = [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int64, _vp, _vp, _vp, _vp,
+                                              _I64, _vp, C.c_size_t, _vp]
+    L.nl_batch_neighbour_list_f32.restype = C.c_int
     _F = C.POINTER(C.c_float)
     L.nl_analyze_cell_f32.argtypes = [_F, C.c_float, C.c_int, C.POINTER(CellPlanF32)]
     L.nl_analyze_cell_f32.restype = C.c_int

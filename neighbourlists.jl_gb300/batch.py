@@ -28,22 +28,30 @@ class BatchNeighbourList:
 
     ``systems`` is a sequence of (nat, cell, cutoff, pbc); the positions of
     all systems are passed concatenated, system after system, as one (N, 3)
-    float64 CUDA tensor.
+    CUDA tensor of ``dtype``: float64, or float32 for the reference with
+    T = Float32 (cell and cutoff converted to Float32, every operation in
+    single precision, R in float32; test/test_gpu.jl:14).
     """
 
     def __init__(self, systems: Sequence[Tuple[int, object, float, object]], int_type=torch.int32,
-                 with_R: bool = True, capacity: Optional[int] = None, device="cuda"):
+                 with_R: bool = True, capacity: Optional[int] = None, device="cuda", dtype=torch.float64):
+        if dtype not in (torch.float64, torch.float32):
+            raise TypeError("positions must be float64 or float32")
         self.ib = _index_bytes(int_type)
         self.ti = _tdtype(self.ib)
         self.with_R = with_R
         self.device = torch.device(device)
+        self.dtype = dtype
+        self.f32 = dtype == torch.float32
         n = len(systems)
-        arr = (_lib.System * max(n, 1))()
+        arr = ((_lib.SystemF32 if self.f32 else _lib.System) * max(n, 1))()
         self.cells, self.cutoffs, self.pbcs, self.nats = [], [], [], []
         exp_pairs = 0.0
         for s, (nat, cell, cutoff, pbc) in enumerate(systems):
             cellm = np.asarray(cell, dtype=np.float64).reshape(3, 3).copy()
-            plan = analyze_cell(cellm, cutoff, int_type)
+            if self.f32:
+                cellm = cellm.astype(np.float32)
+            plan = analyze_cell(cellm, cutoff, int_type, float32=self.f32)
             pb = _pbc(pbc)
             y = arr[s]
             y.nat = int(nat)
@@ -52,7 +60,7 @@ class BatchNeighbourList:
             y.ncells[:] = plan.ncells.tolist()
             y.nxyz[:] = plan.nxyz.tolist()
             y.pbc[:] = pb.tolist()
-            y.cutoff = float(cutoff)
+            y.cutoff = float(np.float32(cutoff)) if self.f32 else float(cutoff)
             self.cells.append(cellm)
             self.cutoffs.append(float(cutoff))
             self.pbcs.append(tuple(bool(b) for b in pb))
@@ -61,7 +69,8 @@ class BatchNeighbourList:
             if vol > 0:
                 exp_pairs += nat * (nat / vol) * 4.0 / 3.0 * np.pi * float(cutoff) ** 3
         h = C.c_void_p()
-        check(lib().nl_batch_create(arr, n, self.ib, C.byref(h)))
+        create = lib().nl_batch_create_f32 if self.f32 else lib().nl_batch_create
+        check(create(arr, n, self.ib, C.byref(h)))
         self._h = h
         self.nsys = n
         na, nc = C.c_int64(), C.c_int64()
@@ -76,7 +85,7 @@ class BatchNeighbourList:
             check(lib().nl_batch_upload(h, _ptr(self.ws), self.ws.numel(), _stream_handle(None)))
         N = self.nat_total
         self.perm = torch.empty(N, dtype=self.ti, device=dev)
-        self.Xs = torch.empty((N, 3), dtype=torch.float64, device=dev)
+        self.Xs = torch.empty((N, 3), dtype=dtype, device=dev)
         self.cid = torch.empty(N, dtype=self.ti, device=dev)
         self.offs = torch.empty(self.ncells_total + n, dtype=self.ti, device=dev)
         self.first = torch.empty(N + n, dtype=self.ti, device=dev)
@@ -103,13 +112,14 @@ class BatchNeighbourList:
         self.i = torch.empty(capacity, dtype=self.ti, device=dev)
         self.j = torch.empty(capacity, dtype=self.ti, device=dev)
         self.S = torch.empty((capacity, 3), dtype=self.ti, device=dev)
-        self.R = torch.empty((capacity, 3), dtype=torch.float64, device=dev) if self.with_R else None
+        self.R = torch.empty((capacity, 3), dtype=self.dtype, device=dev) if self.with_R else None
 
     def _call(self, X: torch.Tensor, total_ptr, stream):
-        if X.dtype != torch.float64 or tuple(X.shape) != (self.nat_total, 3) or not X.is_cuda:
-            raise ValueError(f"positions must be a ({self.nat_total}, 3) float64 CUDA tensor")
+        if X.dtype != self.dtype or tuple(X.shape) != (self.nat_total, 3) or not X.is_cuda:
+            raise ValueError(f"positions must be a ({self.nat_total}, 3) {str(self.dtype)[6:]} CUDA tensor")
         X = X.contiguous()
-        return lib().nl_batch_neighbour_list(
+        run = lib().nl_batch_neighbour_list_f32 if self.f32 else lib().nl_batch_neighbour_list
+        return run(
             self._h, _ptr(X), _ptr(self.perm), _ptr(self.Xs), _ptr(self.cid), C.c_void_p(self.offs.data_ptr()),
             C.c_void_p(self.first.data_ptr()), C.c_void_p(self.pair_offsets.data_ptr()), self.capacity, _ptr(self.i),
             _ptr(self.j), _ptr(self.S), _ptr(self.R), total_ptr, _ptr(self.ws), self.ws.numel(),
@@ -175,7 +185,7 @@ class BatchNeighbourList:
         po = self.pair_offsets_host()
         p0, p1 = int(po[s]), int(po[s + 1])
         Xo = X[a0:a1] if X is not None else None
-        plan = analyze_cell(self.cells[s], self.cutoffs[s], self.ti)
+        plan = analyze_cell(self.cells[s], self.cutoffs[s], self.ti, float32=self.f32)
         clist = SortedCellList(self.Xs[a0:a1], Xo, self.perm[a0:a1], self.cid[a0:a1], self.offs[c0:c1],
                                self.cells[s], plan.inv_cell, self.pbcs[s], self.cutoffs[s], plan.ncells,
                                plan.ncells_total, plan)

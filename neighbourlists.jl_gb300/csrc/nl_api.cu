@@ -788,7 +788,7 @@ int legacy_check(int64_t nat, const int64_t* ncells, const int64_t* nxyz, int in
 // --------------------------------------------------------------- batches --
 struct BatchLayout {
   Layout L;  // the single-system layout for all atoms and cells of the batch
-  size_t geo, atom0, cell0, cs, first_all, sys_sym, sys_fail, cell_sys, end;
+  size_t geo, atom0, cell0, cs, first_all, sys_sym, sys_fail, cell_sys, geo32, end;
 };
 
 BatchLayout batch_layout(int64_t nat, int64_t ncells, int nsys) {
@@ -812,6 +812,8 @@ BatchLayout batch_layout(int64_t nat, int64_t ncells, int nsys) {
   o += up(sizeof(int) * size_t(nsys));
   B.cell_sys = o;
   o += up(sizeof(int) * size_t(ncells > 0 ? ncells : 1));
+  B.geo32 = o;  // Float32 batches: the per-system single-precision geometry
+  o += up(sizeof(nl::Geo32) * size_t(nsys));
   B.end = o;
   return B;
 }
@@ -832,8 +834,10 @@ bool batch_system_sym(const nl::Geometry& g) {
 struct nl_batch {
   int nsys = 0;
   int index_bytes = 4;
+  bool f32 = false;  // Float32 positions (nl_batch_create_f32): geo32 instead of geo
   int64_t nat = 0, ncells = 0;
   std::vector<nl::Geometry> geo;
+  std::vector<nl::Geo32> geo32;
   std::vector<int> atom0, cell0;
   std::vector<int> sym;  // per system: the symmetric count pass applies
   bool any_sym = false;
@@ -918,6 +922,79 @@ int batch_impl(const nl_batch& b, const double* X, TI* perm, double* Xs, TI* cel
     a.oR = oR;
     a.capacity = capacity;
     nl::launch_pairs<TI>(nl::kModeFill, a, sms, st);
+  }
+  e = cudaGetLastError();
+  return e == cudaSuccess ? NL_OK : cuda_fail(e, "launch batch kernels");
+}
+
+// A Float32 batch: the single-precision kernels over all systems at once --
+// binning with each atom's system geometry, the counting sort of the launch's
+// cells, then the per-cell count and fill passes, each warp taking the
+// geometry of its home cell's system (no symmetric pass for batches).
+template <typename TI>
+int batch_impl32(const nl_batch& b, const float* X, TI* perm, float* Xs, TI* cell_id, TI* cell_offsets, TI* first,
+                 long long* pair_offsets, int64_t capacity, TI* oi, TI* oj, TI* oS, float* oR, void* ws,
+                 cudaStream_t st) {
+  const Layout& L = b.B.L;
+  const int sms = num_sms();
+  const int na = int(b.nat), nc = int(b.ncells);
+  cudaError_t e = cudaMemsetAsync(ws, 0, L.bend, st);
+  if (e != cudaSuccess) return cuda_fail(e, "memset workspace");
+  const nl::SysIndex si{nullptr, at<int>(ws, b.B.atom0), at<int>(ws, b.B.cell0), b.nsys};
+  const nl::Geo32* geos = at<nl::Geo32>(ws, b.B.geo32);
+  int* cid = at<int>(ws, L.cid);
+  int* ticket = at<int>(ws, L.ticket);
+  float4* rec = at<float4>(ws, L.rec);
+  int* cell_count = at<int>(ws, L.cell_count);
+  int* cell_start = at<int>(ws, L.cell_start);
+  unsigned* err = at<unsigned>(ws, L.err);
+  int* bcount = at<int>(ws, L.bcount);
+  TI* first_all = at<TI>(ws, b.B.first_all);
+  nl::launch_bin32_batch(geos, si.atom0, si.cell0, b.nsys, X, na, cid, ticket, rec, cell_count, err, sms, st);
+  nl::launch_scan<TI>(cell_count, nc, nullptr, cell_start, at<unsigned long long>(ws, L.st_cells), bcount,
+                      at<long long>(ws, L.totals), err, st);
+  nl::launch_scatter(na, cid, ticket, cell_start, at<int>(ws, L.tmp), sms, st);
+  nl::launch_fix<TI, float>(si, na, at<int>(ws, L.tmp), cid, cell_start, X, rec, perm, cell_id, Xs,
+                            at<float4>(ws, L.rec_sorted), at<int>(ws, L.scell), at<int>(ws, L.big_list), bcount + 1,
+                            sms, st);
+  nl::launch_batch_cell_offsets<TI>(si, nc, cell_start, cell_offsets, sms, st);
+  nl::Pairs32Args<TI> a;
+  std::memset(&a, 0, sizeof(a));
+  a.rec = at<float4>(ws, L.rec_sorted);
+  a.scell = at<int>(ws, L.scell);
+  a.cell_offsets = cell_offsets;
+  a.perm = perm;
+  a.counts = at<int>(ws, L.counts);
+  a.err = err;
+  a.sym = 0;
+  a.sym_fail = at<int>(ws, L.pcount) + 6;  // set: the per-cell fill writes every pair
+  a.geos = geos;
+  a.sys_atom = si.atom0;
+  a.sys_cell = si.cell0;
+  a.cell_sys = at<int>(ws, b.B.cell_sys);
+  a.nsys = b.nsys;
+  a.nat_total = na;
+  a.ncells_total = nc;
+  e = cudaMemsetAsync(a.sym_fail, 0xFF, sizeof(int), st);
+  if (e != cudaSuccess) return cuda_fail(e, "memset workspace");
+  if (na > 0) {
+    nl::launch_pairs32<TI>(false, a, sms, st);
+    nl::launch_scan<TI>(a.counts, na, first_all, nullptr, at<unsigned long long>(ws, L.st_pairs),
+                        at<int>(ws, L.pcount), at<long long>(ws, L.totals) + 1, err, st);
+  } else {
+    static const TI one = 1;
+    e = cudaMemcpyAsync(first_all, &one, sizeof(TI), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(e, "empty batch");
+  }
+  nl::launch_batch_first<TI>(si, na, first_all, first, pair_offsets, sms, st);
+  if (na > 0 && capacity > 0) {
+    a.first = first_all;
+    a.oi = oi;
+    a.oj = oj;
+    a.oS = oS;
+    a.oR = oR;
+    a.capacity = capacity;
+    nl::launch_pairs32<TI>(true, a, sms, st);
   }
   e = cudaGetLastError();
   return e == cudaSuccess ? NL_OK : cuda_fail(e, "launch batch kernels");
@@ -1279,6 +1356,76 @@ int nl_batch_create_auto(const double* cells, const double* cutoffs, const uint8
   return nl_batch_create(sys.data(), nsys, index_bytes, batch);
 }
 
+int nl_batch_create_f32(const nl_system_f32* systems, int nsys, int index_bytes, nl_batch** batch) {
+  if (!batch || (nsys > 0 && !systems)) return fail(NL_ERR_ARG, "null argument");
+  *batch = nullptr;
+  if (nsys < 1) return fail(NL_ERR_ARG, "a batch needs at least one system");
+  if (index_bytes != 4 && index_bytes != 8) return fail(NL_ERR_ARG, "index_bytes must be 4 or 8");
+  nl_batch* b = new (std::nothrow) nl_batch;
+  if (!b) return fail(NL_ERR_NOMEM, "cannot allocate the batch plan");
+  b->nsys = nsys;
+  b->index_bytes = index_bytes;
+  b->f32 = true;
+  b->geo32.resize(size_t(nsys));
+  b->atom0.resize(size_t(nsys) + 1);
+  b->cell0.resize(size_t(nsys) + 1);
+  b->sym.assign(size_t(nsys), 0);
+  int64_t na = 0, nc = 0;
+  for (int s = 0; s < nsys; ++s) {
+    const nl_system_f32& y = systems[s];
+    Layout Ls;
+    int64_t nct;
+    int st = check_common(y.nat, y.ncells, y.nxyz, index_bytes, reinterpret_cast<void*>(1), ~size_t(0), Ls, nct);
+    if (st == NL_OK && (!(y.cutoff > 0) || !std::isfinite(y.cutoff))) st = fail(NL_ERR_ARG, "cutoff must be positive");
+    if (st) {
+      g_last_error = "system " + std::to_string(s) + ": " + g_last_error;
+      delete b;
+      return st;
+    }
+    b->atom0[size_t(s)] = int(na);
+    b->cell0[size_t(s)] = int(nc);
+    b->geo32[size_t(s)] = make_geo32(y.cell, y.inv_cell, y.ncells, y.nxyz, y.pbc, y.cutoff, y.nat);
+    na += y.nat;
+    nc += nct;
+    if (na > 2147483646LL || nc + nsys > 2147483646LL) {
+      delete b;
+      return fail(NL_ERR_ARG, "a batch holds at most 2^31-2 atoms and 2^31-2 cells");
+    }
+  }
+  b->atom0[size_t(nsys)] = int(na);
+  b->cell0[size_t(nsys)] = int(nc);
+  b->nat = na;
+  b->ncells = nc;
+  b->B = batch_layout(na, nc, nsys);
+  *batch = b;
+  return NL_OK;
+}
+
+int nl_batch_create_auto_f32(const float* cells, const float* cutoffs, const uint8_t* pbc, const int64_t* nat,
+                             int nsys, int index_bytes, nl_batch** batch) {
+  if (!batch || (nsys > 0 && (!cells || !cutoffs || !pbc || !nat))) return fail(NL_ERR_ARG, "null argument");
+  if (nsys < 1) return fail(NL_ERR_ARG, "a batch needs at least one system");
+  std::vector<nl_system_f32> sys(static_cast<size_t>(nsys));
+  for (int s = 0; s < nsys; ++s) {
+    nl_system_f32& y = sys[size_t(s)];
+    nl_cell_plan_f32 p;
+    if (int st = analyze_f32(cells + 9 * size_t(s), cutoffs[s], index_bytes, &p)) {
+      g_last_error = "system " + std::to_string(s) + ": " + g_last_error;
+      return st;
+    }
+    y.nat = nat[s];
+    std::memcpy(y.cell, cells + 9 * size_t(s), sizeof(y.cell));
+    std::memcpy(y.inv_cell, p.inv_cell, sizeof(y.inv_cell));
+    for (int k = 0; k < 3; ++k) {
+      y.ncells[k] = p.ncells[k];
+      y.nxyz[k] = p.nxyz[k];
+      y.pbc[k] = pbc[3 * size_t(s) + k] ? 1 : 0;
+    }
+    y.cutoff = cutoffs[s];
+  }
+  return nl_batch_create_f32(sys.data(), nsys, index_bytes, batch);
+}
+
 void nl_batch_destroy(nl_batch* batch) { delete batch; }
 
 size_t nl_batch_workspace_bytes(const nl_batch* batch) { return batch ? batch->B.end : 0; }
@@ -1296,8 +1443,10 @@ int nl_batch_upload(const nl_batch* batch, void* d_workspace, size_t workspace_b
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const BatchLayout& B = batch->B;
   // pageable sources: each copy returns once its source has been consumed
-  cudaError_t e = cudaMemcpyAsync(at<char>(d_workspace, B.geo), batch->geo.data(),
-                                  sizeof(nl::Geometry) * batch->geo.size(), cudaMemcpyHostToDevice, st);
+  cudaError_t e = batch->f32 ? cudaMemcpyAsync(at<char>(d_workspace, B.geo32), batch->geo32.data(),
+                                               sizeof(nl::Geo32) * batch->geo32.size(), cudaMemcpyHostToDevice, st)
+                             : cudaMemcpyAsync(at<char>(d_workspace, B.geo), batch->geo.data(),
+                                               sizeof(nl::Geometry) * batch->geo.size(), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(at<char>(d_workspace, B.atom0), batch->atom0.data(), sizeof(int) * batch->atom0.size(),
                         cudaMemcpyHostToDevice, st);
@@ -1308,7 +1457,7 @@ int nl_batch_upload(const nl_batch* batch, void* d_workspace, size_t workspace_b
     e = cudaMemcpyAsync(at<char>(d_workspace, B.sys_sym), batch->sym.data(), sizeof(int) * batch->sym.size(),
                         cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) return cuda_fail(e, "upload batch tables");
-  nl::launch_cs_tables(at<nl::Geometry>(d_workspace, B.geo), batch->nsys, at<double>(d_workspace, B.cs), st);
+  if (!batch->f32) nl::launch_cs_tables(at<nl::Geometry>(d_workspace, B.geo), batch->nsys, at<double>(d_workspace, B.cs), st);
   nl::launch_cell_systems(at<int>(d_workspace, B.cell0), batch->nsys, at<int>(d_workspace, B.cell_sys), st);
   e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -1320,6 +1469,7 @@ int nl_batch_neighbour_list(const nl_batch* batch, const double* d_X, void* d_pe
                             int64_t capacity, void* d_i, void* d_j, void* d_S, double* d_R, int64_t* total_pairs,
                             void* d_workspace, size_t workspace_bytes, void* stream) {
   if (!batch || !d_cell_offsets || !d_first || !d_pair_offsets || !d_workspace) return fail(NL_ERR_ARG, "null argument");
+  if (batch->f32) return fail(NL_ERR_ARG, "a Float32 batch runs through nl_batch_neighbour_list_f32");
   if (batch->nat > 0 && (!d_X || !d_perm || !d_X_sorted || !d_cell_id)) return fail(NL_ERR_ARG, "null argument");
   if (capacity > 0 && (!d_i || !d_j || !d_S)) return fail(NL_ERR_ARG, "null argument");
   if (workspace_bytes < batch->B.end) return fail(NL_ERR_NOMEM, "workspace too small (see nl_batch_workspace_bytes)");
@@ -1335,6 +1485,40 @@ int nl_batch_neighbour_list(const nl_batch* batch, const double* d_X, void* d_pe
                             static_cast<int64_t*>(d_cell_offsets), static_cast<int64_t*>(d_first),
                             reinterpret_cast<long long*>(d_pair_offsets), capacity, static_cast<int64_t*>(d_i),
                             static_cast<int64_t*>(d_j), static_cast<int64_t*>(d_S), d_R, d_workspace, st);
+  if (s) return s;
+  if (total_pairs) {
+    if (batch->nat == 0) {
+      *total_pairs = 0;
+      return sync_read(d_workspace, st, nullptr, nullptr);
+    }
+    s = sync_read(d_workspace, st, at<long long>(d_workspace, batch->B.L.totals) + 1, total_pairs);
+    if (s == NL_OK && *total_pairs > capacity) return fail(NL_ERR_CAPACITY, "pair buffers are smaller than the pair count");
+    return s;
+  }
+  return NL_OK;
+}
+
+int nl_batch_neighbour_list_f32(const nl_batch* batch, const float* d_X, void* d_perm, float* d_X_sorted,
+                                void* d_cell_id, void* d_cell_offsets, void* d_first, int64_t* d_pair_offsets,
+                                int64_t capacity, void* d_i, void* d_j, void* d_S, float* d_R, int64_t* total_pairs,
+                                void* d_workspace, size_t workspace_bytes, void* stream) {
+  if (!batch || !d_cell_offsets || !d_first || !d_pair_offsets || !d_workspace) return fail(NL_ERR_ARG, "null argument");
+  if (!batch->f32) return fail(NL_ERR_ARG, "a Float64 batch runs through nl_batch_neighbour_list");
+  if (batch->nat > 0 && (!d_X || !d_perm || !d_X_sorted || !d_cell_id)) return fail(NL_ERR_ARG, "null argument");
+  if (capacity > 0 && (!d_i || !d_j || !d_S)) return fail(NL_ERR_ARG, "null argument");
+  if (workspace_bytes < batch->B.end) return fail(NL_ERR_NOMEM, "workspace too small (see nl_batch_workspace_bytes)");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int s;
+  if (batch->index_bytes == 4)
+    s = batch_impl32<int32_t>(*batch, d_X, static_cast<int32_t*>(d_perm), d_X_sorted, static_cast<int32_t*>(d_cell_id),
+                              static_cast<int32_t*>(d_cell_offsets), static_cast<int32_t*>(d_first),
+                              reinterpret_cast<long long*>(d_pair_offsets), capacity, static_cast<int32_t*>(d_i),
+                              static_cast<int32_t*>(d_j), static_cast<int32_t*>(d_S), d_R, d_workspace, st);
+  else
+    s = batch_impl32<int64_t>(*batch, d_X, static_cast<int64_t*>(d_perm), d_X_sorted, static_cast<int64_t*>(d_cell_id),
+                              static_cast<int64_t*>(d_cell_offsets), static_cast<int64_t*>(d_first),
+                              reinterpret_cast<long long*>(d_pair_offsets), capacity, static_cast<int64_t*>(d_i),
+                              static_cast<int64_t*>(d_j), static_cast<int64_t*>(d_S), d_R, d_workspace, st);
   if (s) return s;
   if (total_pairs) {
     if (batch->nat == 0) {

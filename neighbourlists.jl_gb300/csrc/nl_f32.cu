@@ -71,10 +71,15 @@ __device__ __forceinline__ float4 record32(float x0, float x1, float x2, const i
 }
 
 // One thread per atom (original order): cell id, ticket, record, histogram
-// (the same outputs as the double-precision binning).
-__global__ void __launch_bounds__(256) k_bin32(Geo32 g, const float* __restrict__ X, int nat, int* __restrict__ cid,
-                                               int* __restrict__ ticket, float4* __restrict__ rec,
-                                               int* __restrict__ cell_count, unsigned* __restrict__ err) {
+// (the same outputs as the double-precision binning).  Batches: the atom's
+// system by a binary search over the atom offsets, its geometry from the
+// table, its cell index offset by the system's first cell.
+template <bool BATCH>
+__global__ void __launch_bounds__(256) k_bin32(Geo32 g1, const Geo32* __restrict__ geos, const int* __restrict__ atom0,
+                                               const int* __restrict__ cell0, int nsys, const float* __restrict__ X,
+                                               int nat, int* __restrict__ cid, int* __restrict__ ticket,
+                                               float4* __restrict__ rec, int* __restrict__ cell_count,
+                                               unsigned* __restrict__ err) {
   const int lane = threadIdx.x & 31;
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < nat; base += stride) {
@@ -82,10 +87,12 @@ __global__ void __launch_bounds__(256) k_bin32(Geo32 g, const float* __restrict_
     const bool valid = i < nat;
     int c = 0;
     if (valid) {
+      const int sys = BATCH ? batch_system(atom0, nsys, int(i)) : 0;
+      const Geo32& g = BATCH ? geos[sys] : g1;
       const float x0 = X[3 * i + 0], x1 = X[3 * i + 1], x2 = X[3 * i + 2];
       int cc[3], w[3];
       if (!bin32(g, x0, x1, x2, cc, w)) atomicOr(err, kFlagBadPosition);
-      c = (cc[0] - 1) + g.ns[0] * ((cc[1] - 1) + g.ns[1] * (cc[2] - 1));
+      c = (cc[0] - 1) + g.ns[0] * ((cc[1] - 1) + g.ns[1] * (cc[2] - 1)) + (BATCH ? cell0[sys] : 0);
       rec[i] = record32(x0, x1, x2, w);
       cid[i] = c;
     }
@@ -159,8 +166,11 @@ __device__ __forceinline__ int tag_s(unsigned t, int k) { return int((t >> (8 * 
 // FP32 with the reference's operation order, skipping i itself at zero cell
 // shift (gpu_kernels.jl:58-101).  Count: pairs per atom.  Fill: accepted
 // pairs are ballot-compacted to consecutive positions from first[i], so each
-// atom's pairs are in the reference's traversal order.
-template <typename TI, bool FILL>
+// atom's pairs are in the reference's traversal order.  Batches: the warp
+// takes the system of its home cell from the per-cell table, copies the
+// system's geometry to shared memory when the system changes, and adds the
+// system's first slot to its (system-local) cell offsets and atom indices.
+template <typename TI, bool FILL, bool BATCH>
 __global__ void __launch_bounds__(kW32Warps * 32, FILL ? NL_F32_MIN_FILL : NL_F32_MIN_COUNT)
     k_pairs32(Pairs32Args<TI> a) {
   // count: the symmetric pass counted; fill: the count recorded in the
@@ -169,18 +179,39 @@ __global__ void __launch_bounds__(kW32Warps * 32, FILL ? NL_F32_MIN_FILL : NL_F3
   constexpr int kW32Per = FILL ? NL_F32_PER_FILL : NL_F32_PER_COUNT;
   constexpr int kW32Tile = 32 * kW32Per;
   __shared__ Shared32 sh_all[kW32Warps];
+  __shared__ Geo32 geo_w[BATCH ? kW32Warps : 1];
   const int lane = threadIdx.x & 31;
   Shared32& W = sh_all[threadIdx.x >> 5];
-  const Geo32& g = a.g;
+  const Geo32& g = BATCH ? geo_w[threadIdx.x >> 5] : a.g;
   const unsigned lt = lanemask_lt();
-  const int wx = 2 * g.nxyz[0] + 1, wy = 2 * g.nxyz[1] + 1;
-  const int nst = wx * wy * (2 * g.nxyz[2] + 1);
+  int wx = 2 * g.nxyz[0] + 1, wy = 2 * g.nxyz[1] + 1;
+  int nst = wx * wy * (2 * g.nxyz[2] + 1);
   const int nwarps = gridDim.x * kW32Warps;
+  const int ncells = BATCH ? a.ncells_total : g.ncells;
+  int cur_sys = -1, abase = 0, coff = 0;
 
-  for (int cell = blockIdx.x * kW32Warps + (threadIdx.x >> 5); cell < g.ncells; cell += nwarps) {
-    const int hs = int(a.cell_offsets[cell]) - 1, he = int(a.cell_offsets[cell + 1]) - 1;
+  for (int cell = blockIdx.x * kW32Warps + (threadIdx.x >> 5); cell < ncells; cell += nwarps) {
+    int hl = cell;  // the cell within its system
+    if constexpr (BATCH) {
+      const int sys = max(min(a.cell_sys[cell], a.nsys - 1), 0);
+      if (sys != cur_sys) {  // the system's geometry to shared memory
+        __syncwarp();
+        const int* src = reinterpret_cast<const int*>(a.geos + sys);
+        int* dst = reinterpret_cast<int*>(&geo_w[threadIdx.x >> 5]);
+        for (int k = lane; k < int(sizeof(Geo32) / 4); k += 32) dst[k] = src[k];
+        __syncwarp();
+        wx = 2 * g.nxyz[0] + 1;
+        wy = 2 * g.nxyz[1] + 1;
+        nst = wx * wy * (2 * g.nxyz[2] + 1);
+        cur_sys = sys;
+      }
+      abase = a.sys_atom[sys];
+      coff = a.sys_cell[sys] + sys;  // the system's cell_offsets: ncells_s + 1 entries
+      hl = cell - a.sys_cell[sys];
+    }
+    const int hs = int(a.cell_offsets[coff + hl]) - 1 + abase, he = int(a.cell_offsets[coff + hl + 1]) - 1 + abase;
     if (hs >= he) continue;
-    const int ci[3] = {cell % g.ns[0] + 1, (cell / g.ns[0]) % g.ns[1] + 1, cell / (g.ns[0] * g.ns[1]) + 1};
+    const int ci[3] = {hl % g.ns[0] + 1, (hl / g.ns[0]) % g.ns[1] + 1, hl / (g.ns[0] * g.ns[1]) + 1};
     for (int h0 = hs; h0 < he; h0 += 32) {
       const int nh = min(32, he - h0);
       // this lane's home atom: running count (fill: write offset) and range
@@ -200,8 +231,8 @@ __global__ void __launch_bounds__(kW32Warps * 32, FILL ? NL_F32_MIN_FILL : NL_F3
         W.hw[lane][2] = field10(mh, 2) - kW32Bias;
         W.hid[lane] = id;
         if constexpr (FILL) {
-          hbase = (long long)a.first[id - 1] - 1;
-          hn = int((long long)a.first[id] - 1 - hbase);
+          hbase = (long long)a.first[abase + id - 1] - 1;
+          hn = int((long long)a.first[abase + id] - 1 - hbase);
           hok = hbase >= 0 && hn >= 0 && hbase + hn <= a.capacity;
           if (!hok) atomicOr(a.err, kFlagCapacity);
         }
@@ -221,8 +252,8 @@ __global__ void __launch_bounds__(kW32Warps * 32, FILL ? NL_F32_MIN_FILL : NL_F3
         int st = 0, cnt = 0;
         if (valid) {
           const int lin = (cj[0] - 1) + g.ns[0] * ((cj[1] - 1) + g.ns[1] * (cj[2] - 1));
-          st = int(a.cell_offsets[lin]) - 1;
-          cnt = int(a.cell_offsets[lin + 1]) - 1 - st;
+          st = int(a.cell_offsets[coff + lin]) - 1 + abase;
+          cnt = int(a.cell_offsets[coff + lin + 1]) - 1 + abase - st;
         }
         int incl = cnt;
 #pragma unroll
@@ -342,7 +373,7 @@ __global__ void __launch_bounds__(kW32Warps * 32, FILL ? NL_F32_MIN_FILL : NL_F3
         if constexpr (FILL) {
           if (hok && hcount != hn) atomicOr(a.err, kFlagInconsistent);
         } else {
-          a.counts[W.hid[lane] - 1] = hcount;
+          a.counts[abase + W.hid[lane] - 1] = hcount;
         }
       }
     }
@@ -668,7 +699,18 @@ __global__ void __launch_bounds__(128) k_emit32_masks(Pairs32Args<TI> a) {
 void launch_bin32(const Geo32& g, const float* X, int nat, int* cid, int* ticket, float4* rec, int* cell_count,
                   unsigned* err, int num_sms, cudaStream_t st) {
   if (nat <= 0) return;
-  k_bin32<<<grid_for(nat, 256, num_sms * 8), 256, 0, st>>>(g, X, nat, cid, ticket, rec, cell_count, err);
+  k_bin32<false><<<grid_for(nat, 256, num_sms * 8), 256, 0, st>>>(g, nullptr, nullptr, nullptr, 0, X, nat, cid, ticket,
+                                                                   rec, cell_count, err);
+}
+
+void launch_bin32_batch(const Geo32* geos, const int* atom0, const int* cell0, int nsys, const float* X, int nat,
+                        int* cid, int* ticket, float4* rec, int* cell_count, unsigned* err, int num_sms,
+                        cudaStream_t st) {
+  if (nat <= 0 || nsys <= 0) return;
+  Geo32 g0;
+  memset(&g0, 0, sizeof(g0));
+  k_bin32<true><<<grid_for(nat, 256, num_sms * 8), 256, 0, st>>>(g0, geos, atom0, cell0, nsys, X, nat, cid, ticket,
+                                                                  rec, cell_count, err);
 }
 
 template <typename TI>
@@ -680,14 +722,23 @@ void launch_prepare32(const Geo32& g, const float* Xs, const TI* cell_id, const 
 
 template <typename TI>
 void launch_pairs32(bool fill, const Pairs32Args<TI>& a, int num_sms, cudaStream_t st) {
+  if (a.nsys > 0) {  // batches: the per-cell passes (count, then the screening fill)
+    if (a.nat_total <= 0 || a.ncells_total <= 0) return;
+    const int grid = grid_for(a.ncells_total, kW32Warps, num_sms * 12);
+    if (fill)
+      k_pairs32<TI, true, true><<<grid, kW32Warps * 32, 0, st>>>(a);
+    else
+      k_pairs32<TI, false, true><<<grid, kW32Warps * 32, 0, st>>>(a);
+    return;
+  }
   if (a.g.nat <= 0) return;
   const int grid = grid_for(a.g.ncells, kW32Warps, num_sms * 12);
   if (fill) {
     k_emit32_masks<TI><<<grid_for(a.g.nat, 4, num_sms * 16), 128, 0, st>>>(a);
-    k_pairs32<TI, true><<<grid, kW32Warps * 32, 0, st>>>(a);
+    k_pairs32<TI, true, false><<<grid, kW32Warps * 32, 0, st>>>(a);
   } else {
     if (a.sym) k_pairs32_sym<TI><<<grid_for(a.g.ncells, kSym32Warps, num_sms * 16), kSym32Warps * 32, 0, st>>>(a);
-    k_pairs32<TI, false><<<grid, kW32Warps * 32, 0, st>>>(a);
+    k_pairs32<TI, false, false><<<grid, kW32Warps * 32, 0, st>>>(a);
   }
 }
 

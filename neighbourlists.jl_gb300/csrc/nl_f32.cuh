@@ -48,11 +48,28 @@ struct Pairs32Args {
   int sym;
   unsigned* masks;
   int* sym_fail;             // a cell of more than 32 atoms: the per-cell passes run instead
+  // batches (nsys > 0): per-system geometry, slot and cell offsets of each
+  // system in the launch, the system of every cell; cell_offsets, perm and
+  // the pair outputs hold system-local values, counts and first are
+  // launch-wide (index: the system's first slot + local index)
+  const Geo32* geos;
+  const int* sys_atom;       // nsys + 1
+  const int* sys_cell;       // nsys + 1
+  const int* cell_sys;       // ncells_total
+  int nsys;
+  int nat_total;
+  int ncells_total;
 };
 
 // binning of the caller's positions (cell id, ticket, record, histogram)
 void launch_bin32(const Geo32& g, const float* X, int nat, int* cid, int* ticket, float4* rec, int* cell_count,
                   unsigned* err, int num_sms, cudaStream_t st);
+// the same for a batch: atom i of the launch belongs to the system s with
+// atom0[s] <= i < atom0[s + 1] and is binned with geos[s]; its cell index is
+// offset by cell0[s]
+void launch_bin32_batch(const Geo32* geos, const int* atom0, const int* cell0, int nsys, const float* X, int nat,
+                        int* cid, int* ticket, float4* rec, int* cell_count, unsigned* err, int num_sms,
+                        cudaStream_t st);
 // records of an existing sorted cell list (checks its cell ids)
 template <typename TI>
 void launch_prepare32(const Geo32& g, const float* Xs, const TI* cell_id, const TI* perm, int nat, float4* rec_sorted,

@@ -40,7 +40,7 @@ _U8 = C.POINTER(C.c_uint8)
 @dataclass
 class Request:
     rid: int
-    X: object                  # (n, 3) float64 positions: numpy array, or a pinned torch tensor (copied directly)
+    X: object                  # (n, 3) positions of the server's dtype: numpy array, or a pinned torch tensor
     cell: np.ndarray           # 3x3, rows are lattice vectors
     cutoff: float
     pbc: tuple
@@ -83,8 +83,9 @@ class _Slot:
     """One in-flight batch: stream, completion events and resident arenas
     (device buffers, and pinned host buffers for results copied back)."""
 
-    def __init__(self, device):
+    def __init__(self, device, dtype=torch.float64):
         self.device = device
+        self.dtype = dtype  # positions
         self.stream = torch.cuda.Stream(device=device)
         self.event = torch.cuda.Event()
         self.copy_event = torch.cuda.Event()
@@ -113,20 +114,26 @@ class _Slot:
 
     def host_X(self, n):
         if self.h_X is None or self.h_X.shape[0] < n:
-            self.h_X = torch.empty((max(int(n * 1.25), 1), 3), dtype=torch.float64).pin_memory()
+            self.h_X = torch.empty((max(int(n * 1.25), 1), 3), dtype=self.dtype).pin_memory()
         return self.h_X
 
 
 class NeighbourListServer:
     def __init__(self, pair_budget_bytes: float = 40e9, slots: int = 3, max_batch_atoms: int = 4_000_000,
                  max_batch_systems: int = 8192, int_type=torch.int32, with_R: bool = True, device="cuda",
-                 mode: str = "batched", copy_results: bool = False, host_results: bool = False):
+                 mode: str = "batched", copy_results: bool = False, host_results: bool = False,
+                 dtype=torch.float64):
         """host_results: every batch's results (first, i, j, S, R) are copied
         into pinned host memory on the slot's stream, and a request is done --
         its latency stops -- when its results are on the host; the request's
-        ``result`` is then host tensors."""
+        ``result`` is then host tensors.  dtype: float64, or float32 for the
+        reference with T = Float32 (positions, cell, cutoff and R in Float32)."""
         if mode not in ("batched", "plain"):
             raise ValueError("mode must be 'batched' or 'plain'")
+        if dtype not in (torch.float64, torch.float32):
+            raise TypeError("positions must be float64 or float32")
+        self.fdt = dtype
+        self.f32 = dtype == torch.float32
         self.ib = _index_bytes(int_type)
         self.ti = _tdtype(self.ib)
         self.with_R = with_R
@@ -138,8 +145,8 @@ class NeighbourListServer:
         self.budget = float(pair_budget_bytes)
         self.max_atoms = int(max_batch_atoms)
         self.max_systems = int(max_batch_systems) if mode == "batched" else 1
-        self.bytes_per_pair = 2 * self.ib + 3 * self.ib + (24 if with_R else 0)
-        self.slots = [_Slot(self.device) for _ in range(slots)]
+        self.bytes_per_pair = 2 * self.ib + 3 * self.ib + ((12 if self.f32 else 24) if with_R else 0)
+        self.slots = [_Slot(self.device, dtype) for _ in range(slots)]
         self.queue: Deque[Request] = deque()
         self.inflight_bytes = 0
         self.batches = 0
@@ -192,7 +199,7 @@ class NeighbourListServer:
         self.inflight_bytes += pred_bytes
         self.batches += 1
         nat = sum(r.nat for r in reqs)
-        Xd = s.buf("X", 3 * max(nat, 1), torch.float64)
+        Xd = s.buf("X", 3 * max(nat, 1), self.fdt)
         with torch.cuda.stream(s.stream):
             if nat:
                 # small requests are gathered into the slot's pinned staging
@@ -224,22 +231,24 @@ class NeighbourListServer:
         i = s.buf("i", cap, self.ti)
         j = s.buf("j", cap, self.ti)
         S = s.buf("S", 3 * cap, self.ti)
-        R = s.buf("R", 3 * cap, torch.float64) if self.with_R else None
+        R = s.buf("R", 3 * cap, self.fdt) if self.with_R else None
         return i, j, S, R, min(i.numel(), j.numel(), S.numel() // 3, R.numel() // 3 if R is not None else 1 << 62)
 
     def _launch_batched(self, s: _Slot, reqs: List[Request], nat: int, cap: int) -> None:
         L = lib()
         n = len(reqs)
-        cells = np.concatenate([_colmajor(r.cell) for r in reqs])
-        cut = np.array([r.cutoff for r in reqs], dtype=np.float64)
+        fnp = np.float32 if self.f32 else np.float64
+        cells = np.ascontiguousarray(np.concatenate([_colmajor(r.cell) for r in reqs]).astype(fnp))
+        cut = np.array([r.cutoff for r in reqs], dtype=fnp)
         pb = np.concatenate([_pbc(r.pbc) for r in reqs])
         nats = np.array([r.nat for r in reqs], dtype=np.int64)
         if s.handle is not None:
             L.nl_batch_destroy(s.handle)
             s.handle = None
         h = C.c_void_p()
-        check(L.nl_batch_create_auto(cells.ctypes.data_as(_D), cut.ctypes.data_as(_D), pb.ctypes.data_as(_U8),
-                                     nats.ctypes.data_as(_I64), n, self.ib, C.byref(h)))
+        create = L.nl_batch_create_auto_f32 if self.f32 else L.nl_batch_create_auto
+        check(create(C.c_void_p(cells.ctypes.data), C.c_void_p(cut.ctypes.data), pb.ctypes.data_as(_U8),
+                     nats.ctypes.data_as(_I64), n, self.ib, C.byref(h)))
         s.handle = h
         na, nc = C.c_int64(), C.c_int64()
         check(L.nl_batch_sizes(h, C.byref(na), C.byref(nc)))
@@ -248,7 +257,7 @@ class NeighbourListServer:
         check(L.nl_batch_upload(h, _ptr(ws), ws.numel(), st))
         s.nc = int(nc.value)
         perm = s.buf("perm", max(nat, 1), self.ti)
-        Xs = s.buf("Xs", 3 * max(nat, 1), torch.float64)
+        Xs = s.buf("Xs", 3 * max(nat, 1), self.fdt)
         cid = s.buf("cid", max(nat, 1), self.ti)
         offs = s.buf("offs", s.nc + n, self.ti)
         first = s.buf("first", nat + n, self.ti)
@@ -256,18 +265,18 @@ class NeighbourListServer:
         i, j, S, R, capacity = self._outputs(s, cap)
         s.launch_args = (perm, Xs, cid, offs, first, po, ws)
         s.capacity = capacity
-        check(L.nl_batch_neighbour_list(h, _ptr(s.bufs["X"]), _ptr(perm), _ptr(Xs), _ptr(cid),
-                                        C.c_void_p(offs.data_ptr()), C.c_void_p(first.data_ptr()),
-                                        C.c_void_p(po.data_ptr()), capacity, _ptr(i), _ptr(j), _ptr(S), _ptr(R),
-                                        None, _ptr(ws), ws.numel(), st))
+        run = L.nl_batch_neighbour_list_f32 if self.f32 else L.nl_batch_neighbour_list
+        check(run(h, _ptr(s.bufs["X"]), _ptr(perm), _ptr(Xs), _ptr(cid), C.c_void_p(offs.data_ptr()),
+                  C.c_void_p(first.data_ptr()), C.c_void_p(po.data_ptr()), capacity, _ptr(i), _ptr(j), _ptr(S), _ptr(R),
+                  None, _ptr(ws), ws.numel(), st))
 
     def _launch_plain(self, s: _Slot, r: Request, cap: int) -> None:
         L = lib()
-        plan = analyze_cell(r.cell, r.cutoff, self.ti)
+        plan = analyze_cell(r.cell, r.cutoff, self.ti, float32=self.f32)
         nat = r.nat
         ws = s.buf("ws", int(L.nl_workspace_bytes(nat, plan.ncells_total)), torch.uint8)
         perm = s.buf("perm", max(nat, 1), self.ti)
-        Xs = s.buf("Xs", 3 * max(nat, 1), torch.float64)
+        Xs = s.buf("Xs", 3 * max(nat, 1), self.fdt)
         cid = s.buf("cid", max(nat, 1), self.ti)
         offs = s.buf("offs", plan.ncells_total + 1, self.ti)
         first = s.buf("first", nat + 1, self.ti)
@@ -275,12 +284,13 @@ class NeighbourListServer:
         pb = _pbc(r.pbc)
         s.launch_args = (plan, ws, first)
         s.capacity = capacity
-        check(L.nl_neighbour_list(_ptr(s.bufs["X"]), nat, plan.cell_cm.ctypes.data_as(_D),
-                                  plan.inv_cm.ctypes.data_as(_D), plan.ncells.ctypes.data_as(_I64),
-                                  plan.nxyz.ctypes.data_as(_I64), pb.ctypes.data_as(_U8), float(r.cutoff), self.ib,
-                                  _ptr(perm), _ptr(Xs), _ptr(cid), C.c_void_p(offs.data_ptr()),
-                                  C.c_void_p(first.data_ptr()), capacity, _ptr(i), _ptr(j), _ptr(S), _ptr(R), None,
-                                  _ptr(ws), ws.numel(), C.c_void_p(s.stream.cuda_stream)))
+        one = L.nl_neighbour_list_f32 if self.f32 else L.nl_neighbour_list
+        rc = float(np.float32(r.cutoff)) if self.f32 else float(r.cutoff)
+        check(one(_ptr(s.bufs["X"]), nat, C.c_void_p(plan.cell_cm.ctypes.data), C.c_void_p(plan.inv_cm.ctypes.data),
+                  plan.ncells.ctypes.data_as(_I64), plan.nxyz.ctypes.data_as(_I64), pb.ctypes.data_as(_U8), rc,
+                  self.ib, _ptr(perm), _ptr(Xs), _ptr(cid), C.c_void_p(offs.data_ptr()), C.c_void_p(first.data_ptr()),
+                  capacity, _ptr(i), _ptr(j), _ptr(S), _ptr(R), None, _ptr(ws), ws.numel(),
+                  C.c_void_p(s.stream.cuda_stream)))
 
     def _finish(self, s: _Slot, t_done: float) -> List[Request]:
         L = lib()
@@ -314,7 +324,7 @@ class NeighbourListServer:
             hf = s.hbuf("first", nf, self.ti)
             hi, hj = s.hbuf("i", max(total, 1), self.ti), s.hbuf("j", max(total, 1), self.ti)
             hS = s.hbuf("S", 3 * max(total, 1), self.ti)
-            hR = s.hbuf("R", 3 * max(total, 1), torch.float64) if R is not None else None
+            hR = s.hbuf("R", 3 * max(total, 1), self.fdt) if R is not None else None
             with torch.cuda.stream(s.stream):
                 hf[:nf].copy_(first[:nf], non_blocking=True)
                 if total:

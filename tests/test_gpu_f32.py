@@ -161,3 +161,43 @@ def test_symmetric_pass_and_fallback(nlpkg, orc):
         eng.run(torch.from_numpy(X32).cuda())
         o = orc.neighbour_list_f32(X32, 5.0, C, (True, True, True))
         np.testing.assert_array_equal(to_np(eng.pairlist(None).j).astype(np.int64), o.j)
+
+
+def test_batch_float32_every_system(nlpkg, orc):
+    """A Float32 batch (nl_batch_create_f32 / nl_batch_neighbour_list_f32):
+    uneven triclinic systems with mixed boundaries, a one-atom and an empty
+    system, atoms outside their cell -- every system's SortedCellList arrays,
+    first, i, j, S and the bits of R equal the oracle's Float32 restatement,
+    as for a single-system call; Int32 and Int64 indices."""
+    systems = cf.batch_systems(60, seed=31, nmin=1, nmax=700)
+    rng = np.random.default_rng(32)
+    systems[3] = (np.zeros((0, 3)), systems[3][1], systems[3][2], systems[3][3])
+    x, c, rc, p = systems[7]
+    x = x.copy()
+    x[: max(1, len(x) // 5)] += rng.uniform(-1.5, 1.5, (max(1, len(x) // 5), 3)) @ np.asarray(c)  # windings
+    systems[7] = (x, c, rc, p)
+    X32 = [np.ascontiguousarray(np.asarray(x, dtype=np.float32).reshape(-1, 3)) for (x, _, _, _) in systems]
+    for int_type in (torch.int32, torch.int64):
+        b = nlpkg.BatchNeighbourList([(len(x), c, rc, p) for (x, (_, c, rc, p)) in zip(X32, systems)],
+                                     int_type=int_type, dtype=torch.float32)
+        b.run(torch.from_numpy(np.concatenate(X32)).cuda())
+        po = b.pair_offsets_host().astype(np.int64)
+        h = {k: to_np(getattr(b, k)) for k in ("perm", "Xs", "cid", "offs", "first", "i", "j", "S", "R")}
+        assert h["Xs"].dtype == np.float32 and h["R"].dtype == np.float32
+        for s, (x, (_, c, rc, p)) in enumerate(zip(X32, systems)):
+            o = orc.neighbour_list_f32(x, rc, c, p, ti_bytes=4 if int_type == torch.int32 else 8)
+            a0, a1 = int(b.atom0[s]), int(b.atom0[s + 1])
+            c0, c1 = int(b.cell0[s]) + s, int(b.cell0[s + 1]) + s + 1
+            p0, p1 = int(po[s]), int(po[s + 1])
+            assert p1 - p0 == o.npairs, s
+            np.testing.assert_array_equal(h["perm"][a0:a1].astype(np.int64), o.perm)
+            np.testing.assert_array_equal(h["cid"][a0:a1].astype(np.int64), o.cell_id)
+            np.testing.assert_array_equal(h["offs"][c0:c1].astype(np.int64), o.cell_offsets)
+            assert np.array_equal(h["Xs"][a0:a1].view(np.int32), o.X_sorted.view(np.int32)), s
+            np.testing.assert_array_equal(h["first"][a0 + s:a1 + s + 1].astype(np.int64), o.first)
+            np.testing.assert_array_equal(h["i"][p0:p1].astype(np.int64), o.i)
+            np.testing.assert_array_equal(h["j"][p0:p1].astype(np.int64), o.j)
+            np.testing.assert_array_equal(h["S"][p0:p1].astype(np.int64), o.S)
+            assert np.array_equal(h["R"][p0:p1].view(np.int32), o.R.view(np.int32)), s
+        clist, pl = b.system(7)  # the per-system views carry the Float32 plan
+        assert clist.X.dtype == torch.float32 and pl.R.dtype == torch.float32

@@ -83,3 +83,21 @@ def test_host_results_match_device_results(nlpkg):
     plain, _, _ = serve(nlpkg, systems, slots=2, mode="plain", host_results=True)
     for a, b in zip(dev, plain):
         assert same({k: v.cpu() for k, v in a.result.items()}, b.result), a.rid
+
+
+def test_float32_server_batched_and_plain(nlpkg, orc):
+    """A Float32 server (dtype=torch.float32: Float32 batches, or plain
+    nl_neighbour_list_f32 calls): every request, every field and the bits of
+    R equal the oracle's Float32 restatement, in both modes."""
+    systems = [(np.asarray(x, dtype=np.float32), c, rc, p) for (x, c, rc, p) in mixed_systems()[:24]]
+    a, _, srv = serve(nlpkg, systems, slots=2, dtype=torch.float32)
+    assert srv.batches < len(systems)
+    b, _, _ = serve(nlpkg, systems, slots=2, mode="plain", dtype=torch.float32)
+    for ra, rb in zip(a, b):
+        o = orc.neighbour_list_f32(ra.X, ra.cutoff, ra.cell, ra.pbc)
+        for res in (ra.result, rb.result):
+            assert res["R"].dtype == torch.float32
+            assert np.array_equal(res["first"].cpu().numpy().astype(np.int64), o.first), ra.rid
+            for k in ("i", "j", "S"):
+                assert np.array_equal(res[k].cpu().numpy().astype(np.int64), getattr(o, k)), (ra.rid, k)
+            assert np.array_equal(res["R"].cpu().numpy().view(np.int32), o.R.view(np.int32)), ra.rid
