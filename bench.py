@@ -422,6 +422,16 @@ def bench_batched(nl, dev, stream, flush, steps):
                  and torch.equal(e.S[:t], b.S[p0:p1])
                  and torch.equal(e.R[:t].view(torch.int64), b.R[p0:p1].view(torch.int64)))
     nsys = len(systems)
+    # the same systems with Float32 positions, cells and cutoffs (one CUDA graph)
+    del engines, views
+    X32 = torch.from_numpy(X.astype(np.float32)).to(dev)
+    b32 = nl.BatchNeighbourList([(x.shape[0], c, rc, p) for (x, c, rc, p) in systems], device=dev,
+                                dtype=torch.float32)
+    total32 = b32.run(X32)
+    b32.capture(X32)
+    f32_ms = timed_steps(b32.replay, steps, flush, stream)
+    b32.sync_status()
+    del b32
     return {"workload": "4,096 systems, atoms log-uniform [8, 4096] (2,740,812 atoms), triclinic, density "
                         "U[0.03,0.10], off-diagonals U(+-0.15 diag), pbc per axis p=0.8, cutoff U[3,6] A, seed 0",
             "systems": nsys, "atoms": int(X.shape[0]), "pairs": int(total),
@@ -436,6 +446,9 @@ def bench_batched(nl, dev, stream, flush, steps):
             "speedup_vs_plain_graphs": min(plain_graph_ms, plain_streams_ms) / batch_ms,
             "identical_to_plain": bool(same),
             "cuda_graph": True, "autotune": {k: tune[k] for k in ("pair_blocks_per_sm", "emit_blocks_per_sm", "count_kernel", "ms")},
+            "float32": {"ms_per_batch": f32_ms, "systems_per_s": nsys / (f32_ms * 1e-3), "pairs": int(total32),
+                        "note": "the same systems in Float32 (cell, cutoff, positions, R), CUDA graph, default "
+                                "launch shapes"},
             "l2": "flushed before every timed step"}
 
 
