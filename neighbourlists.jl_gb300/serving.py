@@ -286,7 +286,8 @@ class NeighbourListServer:
         s.capacity = capacity
         one = L.nl_neighbour_list_f32 if self.f32 else L.nl_neighbour_list
         rc = float(np.float32(r.cutoff)) if self.f32 else float(r.cutoff)
-        check(one(_ptr(s.bufs["X"]), nat, C.c_void_p(plan.cell_cm.ctypes.data), C.c_void_p(plan.inv_cm.ctypes.data),
+        fp = C.POINTER(C.c_float) if self.f32 else _D
+        check(one(_ptr(s.bufs["X"]), nat, plan.cell_cm.ctypes.data_as(fp), plan.inv_cm.ctypes.data_as(fp),
                   plan.ncells.ctypes.data_as(_I64), plan.nxyz.ctypes.data_as(_I64), pb.ctypes.data_as(_U8), rc,
                   self.ib, _ptr(perm), _ptr(Xs), _ptr(cid), C.c_void_p(offs.data_ptr()), C.c_void_p(first.data_ptr()),
                   capacity, _ptr(i), _ptr(j), _ptr(S), _ptr(R), None, _ptr(ws), ws.numel(),
