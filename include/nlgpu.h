@@ -306,6 +306,19 @@ int nl_neighbour_list_f32(const float* d_X, int64_t nat, const float cell[9], co
                           void* d_first, int64_t capacity, void* d_i, void* d_j, void* d_S, float* d_R,
                           int64_t* total_pairs, void* d_workspace, size_t workspace_bytes, void* stream);
 
+/* nl_pair_vectors and nl_max_displacement_sq for Float32 positions (R by
+ * the reference's single-precision operations; the displacement in FP32). */
+int nl_pair_vectors_f32(const float* d_X, int64_t nat, const float cell[9], int index_bytes, const void* d_i,
+                        const void* d_j, const void* d_S, int64_t npairs, float* d_R, void* stream);
+int nl_max_displacement_sq_f32(const float* d_X, const float* d_Xref, int64_t nat, float* d_out, void* stream);
+/* nl_neighbour_list_half for Float32 positions: each unordered pair once
+ * (j > i, or j == i and S > 0 lexicographically), in the reference's order. */
+int nl_neighbour_list_half_f32(const float* d_X, int64_t nat, const float cell[9], const float inv_cell[9],
+                               const int64_t ncells[3], const int64_t nxyz[3], const uint8_t pbc[3], float cutoff,
+                               int index_bytes, void* d_perm, float* d_X_sorted, void* d_cell_id, void* d_cell_offsets,
+                               void* d_first, int64_t capacity, void* d_i, void* d_j, void* d_S, float* d_R,
+                               int64_t* total_pairs, void* d_workspace, size_t workspace_bytes, void* stream);
+
 /* Float32 batches: as nl_batch_create / nl_batch_neighbour_list with
  * T = Float32 for every system (cell, cutoff and the nl_analyze_cell_f32
  * results in Float32; positions, sorted positions and R in Float32).

@@ -44,6 +44,8 @@ EXPORTED = [
     "nl_query_neighbours",
     "nl_pair_vectors",
     "nl_max_displacement_sq",
+    "nl_pair_vectors_f32",
+    "nl_max_displacement_sq_f32",
     "nl_batch_create",
     "nl_batch_create_auto",
     "nl_batch_destroy",
@@ -51,6 +53,7 @@ EXPORTED = [
     "nl_batch_sizes",
     "nl_batch_upload",
     "nl_batch_neighbour_list",
+    "nl_neighbour_list_half_f32",
     "nl_batch_create_f32",
     "nl_batch_create_auto_f32",
     "nl_batch_neighbour_list_f32",
@@ -210,6 +213,8 @@ def _declare(L):
     L.nl_neighbour_list_f32.argtypes = [_vp, C.c_int64, _F, _F, _I64, _I64, _U8, C.c_float, C.c_int, _vp, _vp, _vp,
                                         _vp, _vp, C.c_int64, _vp, _vp, _vp, _vp, _I64, _vp, C.c_size_t, _vp]
     L.nl_neighbour_list_f32.restype = C.c_int
+    L.nl_neighbour_list_half_f32.argtypes = L.nl_neighbour_list_f32.argtypes
+    L.nl_neighbour_list_half_f32.restype = C.c_int
     L.nl_legacy_fix_cell.argtypes = [_vp, C.c_int64, _D, _U8, _vp, _D, _vp, C.c_size_t, _vp]
     L.nl_legacy_fix_cell.restype = C.c_int
     L.nl_legacy_workspace_bytes.argtypes = [C.c_int64, C.c_int64, C.c_int]
@@ -228,6 +233,11 @@ def _declare(L):
     L.nl_pair_vectors.restype = C.c_int
     L.nl_max_displacement_sq.argtypes = [_vp, _vp, C.c_int64, _vp, _vp]
     L.nl_max_displacement_sq.restype = C.c_int
+    L.nl_pair_vectors_f32.argtypes = [_vp, C.c_int64, C.POINTER(C.c_float), C.c_int, _vp, _vp, _vp, C.c_int64, _vp,
+                                      _vp]
+    L.nl_pair_vectors_f32.restype = C.c_int
+    L.nl_max_displacement_sq_f32.argtypes = [_vp, _vp, C.c_int64, _vp, _vp]
+    L.nl_max_displacement_sq_f32.restype = C.c_int
     L.nl_sync_status.argtypes = [_vp, _vp]
     L.nl_sync_status.restype = C.c_int
     L.nl_last_recheck_count.argtypes = [_vp, _vp, _I64]

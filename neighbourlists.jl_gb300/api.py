@@ -324,9 +324,9 @@ def neighbour_list(X, cutoff: float, cell, pbc, lazy: bool = False, int_type=tor
             raise ValueError("a half list is a materialised list (lazy=False)")
         from .engine import NeighbourListEngine
 
-        Xd = _device_positions(X)
+        Xd = _device_positions(X, f32_ok=True)
         eng = NeighbourListEngine(int(Xd.shape[0]), cell, cutoff, pbc, int_type=int_type, with_R=with_R,
-                                  device=Xd.device, half=True)
+                                  device=Xd.device, half=True, dtype=Xd.dtype)
         eng.run(Xd, stream)
         return eng.pairlist(Xd)
     clist = build_cell_list(X, cutoff, cell, pbc, int_type=int_type, stream=stream)
@@ -516,14 +516,21 @@ def neigs(nlist: PairList, i0: int):
 def pair_vectors(X: torch.Tensor, cell, i: torch.Tensor, j: torch.Tensor, S: torch.Tensor,
                  out: Optional[torch.Tensor] = None, stream=None) -> torch.Tensor:
     """R = (X[j] - X[i]) + C'S for every pair (the reference's _getR,
-    cell_list.jl:525-531), bit-equal to the R of a materialised list."""
+    cell_list.jl:525-531), bit-equal to the R of a materialised list; float32
+    positions take the reference's single-precision operations (T = Float32)."""
     P = int(i.shape[0])
+    f32 = X.dtype == torch.float32
     if out is None:
-        out = torch.empty((P, 3), dtype=torch.float64, device=X.device)
+        out = torch.empty((P, 3), dtype=X.dtype, device=X.device)
     cm = _colmajor(cell)
     ib = 4 if i.dtype == torch.int32 else 8
-    check(lib().nl_pair_vectors(_ptr(X), int(X.shape[0]), cm.ctypes.data_as(_D), ib, _ptr(i), _ptr(j), _ptr(S), P,
-                                _ptr(out), _stream_handle(stream)))
+    if f32:
+        cm32 = np.ascontiguousarray(cm.astype(np.float32))
+        check(lib().nl_pair_vectors_f32(_ptr(X), int(X.shape[0]), cm32.ctypes.data_as(_F), ib, _ptr(i), _ptr(j),
+                                        _ptr(S), P, _ptr(out), _stream_handle(stream)))
+    else:
+        check(lib().nl_pair_vectors(_ptr(X), int(X.shape[0]), cm.ctypes.data_as(_D), ib, _ptr(i), _ptr(j), _ptr(S),
+                                    P, _ptr(out), _stream_handle(stream)))
     return out
 
 

@@ -594,9 +594,10 @@ bool use_sym32(const nl::Geo32& g, const Layout& L) {
 
 template <typename TI>
 nl::Pairs32Args<TI> pairs32_args(const nl::Geo32& g, const TI* cell_offsets, const TI* perm, void* ws,
-                                 const Layout& L) {
+                                 const Layout& L, int half = 0) {
   nl::Pairs32Args<TI> a;
   std::memset(&a, 0, sizeof(a));
+  a.half = half;
   a.g = g;
   a.rec = at<float4>(ws, L.rec_sorted);
   a.scell = at<int>(ws, L.scell);
@@ -604,7 +605,7 @@ nl::Pairs32Args<TI> pairs32_args(const nl::Geo32& g, const TI* cell_offsets, con
   a.perm = perm;
   a.counts = at<int>(ws, L.counts);
   a.err = at<unsigned>(ws, L.err);
-  a.sym = use_sym32(g, L) ? 1 : 0;
+  a.sym = !half && use_sym32(g, L) ? 1 : 0;  // half lists: the per-cell passes (they filter every pair)
   a.masks = reinterpret_cast<unsigned*>(at<uint2>(ws, L.lists));
   a.sym_fail = at<int>(ws, L.pcount) + 6;  // zeroed with the pair scan state
   return a;
@@ -612,7 +613,7 @@ nl::Pairs32Args<TI> pairs32_args(const nl::Geo32& g, const TI* cell_offsets, con
 
 template <typename TI>
 int count_impl32(const nl::Geo32& g, const float* Xs, const TI* perm, const TI* cell_id, const TI* cell_offsets,
-                 int reuse, TI* first, void* ws, const Layout& L, cudaStream_t st) {
+                 int reuse, TI* first, void* ws, const Layout& L, cudaStream_t st, int half = 0) {
   const int sms = num_sms();
   const size_t z0 = reuse ? L.stats : L.err;
   cudaError_t e = cudaMemsetAsync(static_cast<char*>(ws) + z0, 0, L.pend - z0, st);
@@ -625,7 +626,7 @@ int count_impl32(const nl::Geo32& g, const float* Xs, const TI* perm, const TI* 
   if (!reuse)
     nl::launch_prepare32<TI>(g, Xs, cell_id, perm, g.nat, at<float4>(ws, L.rec_sorted), at<int>(ws, L.scell),
                              at<unsigned>(ws, L.err), sms, st);
-  const nl::Pairs32Args<TI> a = pairs32_args<TI>(g, cell_offsets, perm, ws, L);
+  const nl::Pairs32Args<TI> a = pairs32_args<TI>(g, cell_offsets, perm, ws, L, half);
   // as count_impl: counts accumulated by the symmetric pass, else the record
   e = a.sym ? cudaMemsetAsync(a.counts, 0, sizeof(int) * size_t(g.nat), st)
             : cudaMemsetAsync(a.sym_fail, 0xFF, sizeof(int), st);
@@ -639,9 +640,9 @@ int count_impl32(const nl::Geo32& g, const float* Xs, const TI* perm, const TI* 
 
 template <typename TI>
 int fill_impl32(const nl::Geo32& g, const TI* perm, const TI* cell_offsets, const TI* first, int64_t capacity, TI* oi,
-                TI* oj, TI* oS, float* oR, void* ws, const Layout& L, cudaStream_t st) {
+                TI* oj, TI* oS, float* oR, void* ws, const Layout& L, cudaStream_t st, int half = 0) {
   if (g.nat == 0 || capacity <= 0) return NL_OK;
-  nl::Pairs32Args<TI> a = pairs32_args<TI>(g, cell_offsets, perm, ws, L);
+  nl::Pairs32Args<TI> a = pairs32_args<TI>(g, cell_offsets, perm, ws, L, half);
   a.first = first;
   a.oi = oi;
   a.oj = oj;
@@ -1584,6 +1585,38 @@ int nl_max_displacement_sq(const double* d_X, const double* d_Xref, int64_t nat,
   return e == cudaSuccess ? NL_OK : cuda_fail(e, "launch max displacement");
 }
 
+int nl_pair_vectors_f32(const float* d_X, int64_t nat, const float cell[9], int index_bytes, const void* d_i,
+                        const void* d_j, const void* d_S, int64_t npairs, float* d_R, void* stream) {
+  if (!cell || npairs < 0 || nat < 0) return fail(NL_ERR_ARG, "invalid argument");
+  if (index_bytes != 4 && index_bytes != 8) return fail(NL_ERR_ARG, "index_bytes must be 4 or 8");
+  if (npairs == 0) return NL_OK;
+  if (!d_X || !d_i || !d_j || !d_S || !d_R || nat == 0) return fail(NL_ERR_ARG, "null argument");
+  if (nat > 2147483646LL) return fail(NL_ERR_ARG, "nat must be in [0, 2^31-2]");
+  nl::Geo32 g;
+  std::memset(&g, 0, sizeof(g));
+  std::memcpy(g.C, cell, sizeof(g.C));
+  g.nat = int(nat);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (index_bytes == 4)
+    nl::launch_pair_vectors32<int32_t>(g, d_X, static_cast<const int32_t*>(d_i), static_cast<const int32_t*>(d_j),
+                                       static_cast<const int32_t*>(d_S), npairs, d_R, num_sms(), st);
+  else
+    nl::launch_pair_vectors32<int64_t>(g, d_X, static_cast<const int64_t*>(d_i), static_cast<const int64_t*>(d_j),
+                                       static_cast<const int64_t*>(d_S), npairs, d_R, num_sms(), st);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? NL_OK : cuda_fail(e, "launch pair vectors");
+}
+
+int nl_max_displacement_sq_f32(const float* d_X, const float* d_Xref, int64_t nat, float* d_out, void* stream) {
+  if (!d_out || nat < 0 || (nat > 0 && (!d_X || !d_Xref))) return fail(NL_ERR_ARG, "null argument");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaMemsetAsync(d_out, 0, sizeof(float), st);
+  if (e != cudaSuccess) return cuda_fail(e, "memset");
+  nl::launch_max_disp_sq32(d_X, d_Xref, nat, reinterpret_cast<unsigned*>(d_out), num_sms(), st);
+  e = cudaGetLastError();
+  return e == cudaSuccess ? NL_OK : cuda_fail(e, "launch max displacement");
+}
+
 int nl_analyze_cell_f32(const float cell[9], float cutoff, int index_bytes, nl_cell_plan_f32* plan) {
   if (!cell || !plan) return fail(NL_ERR_ARG, "null argument");
   return analyze_f32(cell, cutoff, index_bytes, plan);
@@ -1609,10 +1642,11 @@ int nl_build_cell_list_f32(const float* d_X, int64_t nat, const float cell[9], c
                                static_cast<int64_t*>(d_cell_offsets), d_workspace, L, st);
 }
 
-int nl_count_pairs_f32(const float* d_X_sorted, const void* d_perm, const void* d_cell_id, const void* d_cell_offsets,
-                       int64_t nat, const float cell[9], const float inv_cell[9], const int64_t ncells[3],
-                       const int64_t nxyz[3], const uint8_t pbc[3], float cutoff, int index_bytes, int reuse_records,
-                       void* d_first, int64_t* total_pairs, void* d_workspace, size_t workspace_bytes, void* stream) {
+static int count_pairs_f32_entry(const float* d_X_sorted, const void* d_perm, const void* d_cell_id,
+                                 const void* d_cell_offsets, int64_t nat, const float cell[9], const float inv_cell[9],
+                                 const int64_t ncells[3], const int64_t nxyz[3], const uint8_t pbc[3], float cutoff,
+                                 int index_bytes, int reuse_records, void* d_first, int64_t* total_pairs,
+                                 void* d_workspace, size_t workspace_bytes, void* stream, int half) {
   if (!cell || !inv_cell || !ncells || !nxyz || !pbc || !d_first || !d_cell_offsets ||
       (nat > 0 && (!d_X_sorted || !d_perm || !d_cell_id)))
     return fail(NL_ERR_ARG, "null argument");
@@ -1625,11 +1659,11 @@ int nl_count_pairs_f32(const float* d_X_sorted, const void* d_perm, const void* 
   if (index_bytes == 4)
     s = count_impl32<int32_t>(g, d_X_sorted, static_cast<const int32_t*>(d_perm),
                               static_cast<const int32_t*>(d_cell_id), static_cast<const int32_t*>(d_cell_offsets),
-                              reuse_records, static_cast<int32_t*>(d_first), d_workspace, L, st);
+                              reuse_records, static_cast<int32_t*>(d_first), d_workspace, L, st, half);
   else
     s = count_impl32<int64_t>(g, d_X_sorted, static_cast<const int64_t*>(d_perm),
                               static_cast<const int64_t*>(d_cell_id), static_cast<const int64_t*>(d_cell_offsets),
-                              reuse_records, static_cast<int64_t*>(d_first), d_workspace, L, st);
+                              reuse_records, static_cast<int64_t*>(d_first), d_workspace, L, st, half);
   if (s) return s;
   if (total_pairs) {
     if (nat == 0) {
@@ -1641,11 +1675,20 @@ int nl_count_pairs_f32(const float* d_X_sorted, const void* d_perm, const void* 
   return NL_OK;
 }
 
-int nl_fill_pairs_f32(const float* d_X_sorted, const void* d_perm, const void* d_cell_offsets, int64_t nat,
-                      const float cell[9], const float inv_cell[9], const int64_t ncells[3], const int64_t nxyz[3],
-                      const uint8_t pbc[3], float cutoff, int index_bytes, const void* d_first, int64_t capacity,
-                      void* d_i, void* d_j, void* d_S, float* d_R, void* d_workspace, size_t workspace_bytes,
-                      void* stream) {
+int nl_count_pairs_f32(const float* d_X_sorted, const void* d_perm, const void* d_cell_id, const void* d_cell_offsets,
+                       int64_t nat, const float cell[9], const float inv_cell[9], const int64_t ncells[3],
+                       const int64_t nxyz[3], const uint8_t pbc[3], float cutoff, int index_bytes, int reuse_records,
+                       void* d_first, int64_t* total_pairs, void* d_workspace, size_t workspace_bytes, void* stream) {
+  return count_pairs_f32_entry(d_X_sorted, d_perm, d_cell_id, d_cell_offsets, nat, cell, inv_cell, ncells, nxyz, pbc,
+                               cutoff, index_bytes, reuse_records, d_first, total_pairs, d_workspace, workspace_bytes,
+                               stream, 0);
+}
+
+static int fill_pairs_f32_entry(const float* d_X_sorted, const void* d_perm, const void* d_cell_offsets, int64_t nat,
+                                const float cell[9], const float inv_cell[9], const int64_t ncells[3],
+                                const int64_t nxyz[3], const uint8_t pbc[3], float cutoff, int index_bytes,
+                                const void* d_first, int64_t capacity, void* d_i, void* d_j, void* d_S, float* d_R,
+                                void* d_workspace, size_t workspace_bytes, void* stream, int half) {
   if (!cell || !inv_cell || !ncells || !nxyz || !pbc || !d_first || !d_cell_offsets)
     return fail(NL_ERR_ARG, "null argument");
   if (capacity > 0 && nat > 0 && (!d_i || !d_j || !d_S || !d_X_sorted || !d_perm))
@@ -1659,25 +1702,37 @@ int nl_fill_pairs_f32(const float* d_X_sorted, const void* d_perm, const void* d
   if (index_bytes == 4)
     return fill_impl32<int32_t>(g, static_cast<const int32_t*>(d_perm), static_cast<const int32_t*>(d_cell_offsets),
                                 static_cast<const int32_t*>(d_first), capacity, static_cast<int32_t*>(d_i),
-                                static_cast<int32_t*>(d_j), static_cast<int32_t*>(d_S), d_R, d_workspace, L, st);
+                                static_cast<int32_t*>(d_j), static_cast<int32_t*>(d_S), d_R, d_workspace, L, st, half);
   return fill_impl32<int64_t>(g, static_cast<const int64_t*>(d_perm), static_cast<const int64_t*>(d_cell_offsets),
                               static_cast<const int64_t*>(d_first), capacity, static_cast<int64_t*>(d_i),
-                              static_cast<int64_t*>(d_j), static_cast<int64_t*>(d_S), d_R, d_workspace, L, st);
+                              static_cast<int64_t*>(d_j), static_cast<int64_t*>(d_S), d_R, d_workspace, L, st, half);
 }
 
-int nl_neighbour_list_f32(const float* d_X, int64_t nat, const float cell[9], const float inv_cell[9],
-                          const int64_t ncells[3], const int64_t nxyz[3], const uint8_t pbc[3], float cutoff,
-                          int index_bytes, void* d_perm, float* d_X_sorted, void* d_cell_id, void* d_cell_offsets,
-                          void* d_first, int64_t capacity, void* d_i, void* d_j, void* d_S, float* d_R,
-                          int64_t* total_pairs, void* d_workspace, size_t workspace_bytes, void* stream) {
+int nl_fill_pairs_f32(const float* d_X_sorted, const void* d_perm, const void* d_cell_offsets, int64_t nat,
+                      const float cell[9], const float inv_cell[9], const int64_t ncells[3], const int64_t nxyz[3],
+                      const uint8_t pbc[3], float cutoff, int index_bytes, const void* d_first, int64_t capacity,
+                      void* d_i, void* d_j, void* d_S, float* d_R, void* d_workspace, size_t workspace_bytes,
+                      void* stream) {
+  return fill_pairs_f32_entry(d_X_sorted, d_perm, d_cell_offsets, nat, cell, inv_cell, ncells, nxyz, pbc, cutoff,
+                              index_bytes, d_first, capacity, d_i, d_j, d_S, d_R, d_workspace, workspace_bytes, stream,
+                              0);
+}
+
+static int neighbour_list_f32_entry(const float* d_X, int64_t nat, const float cell[9], const float inv_cell[9],
+                                    const int64_t ncells[3], const int64_t nxyz[3], const uint8_t pbc[3],
+                                    float cutoff, int index_bytes, void* d_perm, float* d_X_sorted, void* d_cell_id,
+                                    void* d_cell_offsets, void* d_first, int64_t capacity, void* d_i, void* d_j,
+                                    void* d_S, float* d_R, int64_t* total_pairs, void* d_workspace,
+                                    size_t workspace_bytes, void* stream, int half) {
   int s = nl_build_cell_list_f32(d_X, nat, cell, inv_cell, ncells, pbc, cutoff, index_bytes, d_perm, d_X_sorted,
                                  d_cell_id, d_cell_offsets, d_workspace, workspace_bytes, stream);
   if (s) return s;
-  s = nl_count_pairs_f32(d_X_sorted, d_perm, d_cell_id, d_cell_offsets, nat, cell, inv_cell, ncells, nxyz, pbc, cutoff,
-                         index_bytes, 1, d_first, nullptr, d_workspace, workspace_bytes, stream);
+  s = count_pairs_f32_entry(d_X_sorted, d_perm, d_cell_id, d_cell_offsets, nat, cell, inv_cell, ncells, nxyz, pbc,
+                            cutoff, index_bytes, 1, d_first, nullptr, d_workspace, workspace_bytes, stream, half);
   if (s) return s;
-  s = nl_fill_pairs_f32(d_X_sorted, d_perm, d_cell_offsets, nat, cell, inv_cell, ncells, nxyz, pbc, cutoff, index_bytes,
-                        d_first, capacity, d_i, d_j, d_S, d_R, d_workspace, workspace_bytes, stream);
+  s = fill_pairs_f32_entry(d_X_sorted, d_perm, d_cell_offsets, nat, cell, inv_cell, ncells, nxyz, pbc, cutoff,
+                           index_bytes, d_first, capacity, d_i, d_j, d_S, d_R, d_workspace, workspace_bytes, stream,
+                           half);
   if (s) return s;
   if (total_pairs) {
     Layout L = layout(nat, ncells[0] * ncells[1] * ncells[2]);
@@ -1691,6 +1746,26 @@ int nl_neighbour_list_f32(const float* d_X, int64_t nat, const float cell[9], co
     return s;
   }
   return NL_OK;
+}
+
+int nl_neighbour_list_f32(const float* d_X, int64_t nat, const float cell[9], const float inv_cell[9],
+                          const int64_t ncells[3], const int64_t nxyz[3], const uint8_t pbc[3], float cutoff,
+                          int index_bytes, void* d_perm, float* d_X_sorted, void* d_cell_id, void* d_cell_offsets,
+                          void* d_first, int64_t capacity, void* d_i, void* d_j, void* d_S, float* d_R,
+                          int64_t* total_pairs, void* d_workspace, size_t workspace_bytes, void* stream) {
+  return neighbour_list_f32_entry(d_X, nat, cell, inv_cell, ncells, nxyz, pbc, cutoff, index_bytes, d_perm, d_X_sorted,
+                                  d_cell_id, d_cell_offsets, d_first, capacity, d_i, d_j, d_S, d_R, total_pairs,
+                                  d_workspace, workspace_bytes, stream, 0);
+}
+
+int nl_neighbour_list_half_f32(const float* d_X, int64_t nat, const float cell[9], const float inv_cell[9],
+                               const int64_t ncells[3], const int64_t nxyz[3], const uint8_t pbc[3], float cutoff,
+                               int index_bytes, void* d_perm, float* d_X_sorted, void* d_cell_id, void* d_cell_offsets,
+                               void* d_first, int64_t capacity, void* d_i, void* d_j, void* d_S, float* d_R,
+                               int64_t* total_pairs, void* d_workspace, size_t workspace_bytes, void* stream) {
+  return neighbour_list_f32_entry(d_X, nat, cell, inv_cell, ncells, nxyz, pbc, cutoff, index_bytes, d_perm, d_X_sorted,
+                                  d_cell_id, d_cell_offsets, d_first, capacity, d_i, d_j, d_S, d_R, total_pairs,
+                                  d_workspace, workspace_bytes, stream, 1);
 }
 
 size_t nl_legacy_workspace_bytes(int64_t nat, int64_t ncells_total, int index_bytes) {

@@ -345,6 +345,8 @@ __global__ void __launch_bounds__(kW32Warps * 32, FILL ? NL_F32_MIN_FILL : NL_F3
                 R2 = fadd(fsub(czr[r], zi), e2);
                 const float r2 = fadd(fadd(fmul(R0, R0), fmul(R1, R1)), fmul(R2, R2));
                 acc = r2 < g.cutoff_sq;
+                if (a.half && acc)  // half list: j > i, or the atom's own image with S > 0 lexicographically
+                  acc = jor[r] != iid ? jor[r] > iid : (S0 > 0 || (S0 == 0 && (S1 > 0 || (S1 == 0 && S2 > 0))));
               }
               const unsigned mask = __ballot_sync(0xffffffffu, acc);
               if constexpr (FILL) {
@@ -694,7 +696,56 @@ __global__ void __launch_bounds__(128) k_emit32_masks(Pairs32Args<TI> a) {
   }
 }
 
+// _getR (cell_list.jl:525-531) with T = Float32 over a whole list: R =
+// (xj - xi) + C'S with the single-precision operations of the pair passes.
+template <typename TI>
+__global__ void __launch_bounds__(256) k_pair_vectors32(Geo32 g, const float* __restrict__ X,
+                                                        const TI* __restrict__ pi, const TI* __restrict__ pj,
+                                                        const TI* __restrict__ pS, long long npairs,
+                                                        float* __restrict__ R) {
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < npairs;
+       p += (long long)gridDim.x * blockDim.x) {
+    const long long i = min(max((long long)pi[p] - 1, 0LL), (long long)g.nat - 1);
+    const long long j = min(max((long long)pj[p] - 1, 0LL), (long long)g.nat - 1);
+    const int s0 = int(pS[3 * p + 0]), s1 = int(pS[3 * p + 1]), s2 = int(pS[3 * p + 2]);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) R[3 * p + k] = fadd(fsub(X[3 * j + k], X[3 * i + k]), cts32(g.C, s0, s1, s2, k));
+  }
+}
+
+// Largest squared displacement in FP32 (the Verlet skin test); NaN wins.
+__global__ void __launch_bounds__(256) k_max_disp_sq32(const float* __restrict__ X, const float* __restrict__ Xref,
+                                                       long long nat, unsigned* __restrict__ out) {
+  float m = 0.f;
+  for (long long a = (long long)blockIdx.x * blockDim.x + threadIdx.x; a < nat; a += (long long)gridDim.x * blockDim.x) {
+    const float d0 = X[3 * a + 0] - Xref[3 * a + 0], d1 = X[3 * a + 1] - Xref[3 * a + 1],
+                d2 = X[3 * a + 2] - Xref[3 * a + 2];
+    const float d = d0 * d0 + d1 * d1 + d2 * d2;
+    m = (d > m || d != d) ? d : m;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float v = __shfl_xor_sync(0xffffffffu, m, o);
+    m = (v > m || v != v) ? v : m;
+  }
+  // non-negative floats (and NaN) order like their bit patterns
+  if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));
+}
+
 }  // namespace
+
+template <typename TI>
+void launch_pair_vectors32(const Geo32& g, const float* X, const TI* pi, const TI* pj, const TI* pS, long long npairs,
+                           float* R, int num_sms, cudaStream_t st) {
+  if (npairs <= 0) return;
+  k_pair_vectors32<TI><<<grid_for(npairs, 256, num_sms * 8), 256, 0, st>>>(g, X, pi, pj, pS, npairs, R);
+}
+
+void launch_max_disp_sq32(const float* X, const float* Xref, long long nat, unsigned* out, int num_sms,
+                          cudaStream_t st) {
+  if (nat <= 0) return;
+  k_max_disp_sq32<<<grid_for(nat, 256, num_sms * 8), 256, 0, st>>>(X, Xref, nat, out);
+}
 
 void launch_bin32(const Geo32& g, const float* X, int nat, int* cid, int* ticket, float4* rec, int* cell_count,
                   unsigned* err, int num_sms, cudaStream_t st) {
@@ -745,7 +796,9 @@ void launch_pairs32(bool fill, const Pairs32Args<TI>& a, int num_sms, cudaStream
 #define NL_INST(TI)                                                                                                 \
   template void launch_prepare32<TI>(const Geo32&, const float*, const TI*, const TI*, int, float4*, int*,         \
                                      unsigned*, int, cudaStream_t);                                                \
-  template void launch_pairs32<TI>(bool, const Pairs32Args<TI>&, int, cudaStream_t);
+  template void launch_pairs32<TI>(bool, const Pairs32Args<TI>&, int, cudaStream_t);                              \
+  template void launch_pair_vectors32<TI>(const Geo32&, const float*, const TI*, const TI*, const TI*, long long,   \
+                                          float*, int, cudaStream_t);
 NL_INST(int32_t)
 NL_INST(int64_t)
 #undef NL_INST

@@ -48,6 +48,7 @@ struct Pairs32Args {
   int sym;
   unsigned* masks;
   int* sym_fail;             // a cell of more than 32 atoms: the per-cell passes run instead
+  int half;                  // keep each unordered pair once: j > i, or j == i and S > 0 lexicographically
   // batches (nsys > 0): per-system geometry, slot and cell offsets of each
   // system in the launch, the system of every cell; cell_offsets, perm and
   // the pair outputs hold system-local values, counts and first are
@@ -77,5 +78,12 @@ void launch_prepare32(const Geo32& g, const float* Xs, const TI* cell_id, const 
 // count (fill = false) or fill (fill = true) pass
 template <typename TI>
 void launch_pairs32(bool fill, const Pairs32Args<TI>& a, int num_sms, cudaStream_t st);
+// R of a whole list at new positions (Verlet reuse), and the largest squared
+// displacement since a reference configuration (bits of a non-negative float)
+template <typename TI>
+void launch_pair_vectors32(const Geo32& g, const float* X, const TI* pi, const TI* pj, const TI* pS, long long npairs,
+                           float* R, int num_sms, cudaStream_t st);
+void launch_max_disp_sq32(const float* X, const float* Xref, long long nat, unsigned* out, int num_sms,
+                          cudaStream_t st);
 
 }  // namespace nl

@@ -33,8 +33,6 @@ class NeighbourListEngine:
         if dtype not in (torch.float64, torch.float32):
             raise TypeError("dtype must be torch.float64 or torch.float32")
         self.f32 = dtype == torch.float32
-        if self.f32 and half:
-            raise TypeError("half lists take Float64 positions")
         self.dtype = dtype
         self.nat = int(nat)
         self.cell = np.asarray(cell, dtype=np.float64).reshape(3, 3).astype(np.float32 if self.f32 else np.float64)
@@ -43,7 +41,7 @@ class NeighbourListEngine:
         self.ib = _index_bytes(int_type)
         self.ti = _tdtype(self.ib)
         self.with_R = with_R
-        self.half = bool(half)  # keep each unordered pair once (nl_neighbour_list_half)
+        self.half = bool(half)  # keep each unordered pair once (nl_neighbour_list_half[_f32])
         self.device = torch.device(device)
         self.plan = analyze_cell(self.cell, self.cutoff, int_type, float32=self.f32)
         p = self.plan
@@ -78,7 +76,7 @@ class NeighbourListEngine:
         p = self.plan
         check(lib().nl_set_tuning(C.byref(self.tuning)))
         if self.f32:
-            entry, fp = lib().nl_neighbour_list_f32, _F
+            entry, fp = (lib().nl_neighbour_list_half_f32 if self.half else lib().nl_neighbour_list_f32), _F
         else:
             entry, fp = (lib().nl_neighbour_list_half if self.half else lib().nl_neighbour_list), _D
         if X.dtype != self.dtype:

@@ -26,14 +26,17 @@ __all__ = ["VerletList"]
 
 class VerletList:
     def __init__(self, nat: int, cell, cutoff: float, skin: float, pbc, int_type=torch.int32, half: bool = False,
-                 device="cuda"):
+                 device="cuda", dtype=torch.float64):
+        """dtype=torch.float32: Float32 positions (list, R and the skin test
+        in single precision, the reference with T = Float32)."""
         if not skin > 0:
             raise ValueError("skin must be positive")
         self.cutoff, self.skin = float(cutoff), float(skin)
         self.engine = NeighbourListEngine(nat, cell, self.cutoff + self.skin, pbc, int_type=int_type,
-                                          device=device, half=half)
+                                          device=device, half=half, dtype=dtype)
+        self.f32 = dtype == torch.float32
         self.X_ref = None
-        self._d2 = torch.zeros(1, dtype=torch.float64, device=self.engine.device)
+        self._d2 = torch.zeros(1, dtype=dtype, device=self.engine.device)
         self.rebuilds = 0
         self.reuses = 0
 
@@ -41,8 +44,8 @@ class VerletList:
         """Largest displacement since the build, measured on ``stream`` (default:
         the current stream) and read back on that same stream."""
         st = stream if stream is not None else torch.cuda.current_stream(self.engine.device)
-        check(lib().nl_max_displacement_sq(_ptr(X), _ptr(self.X_ref), int(X.shape[0]), _ptr(self._d2),
-                                           _stream_handle(st)))
+        disp = lib().nl_max_displacement_sq_f32 if self.f32 else lib().nl_max_displacement_sq
+        check(disp(_ptr(X), _ptr(self.X_ref), int(X.shape[0]), _ptr(self._d2), _stream_handle(st)))
         with torch.cuda.stream(st):
             d2 = float(self._d2.item())
         return d2 ** 0.5

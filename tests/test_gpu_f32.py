@@ -201,3 +201,65 @@ def test_batch_float32_every_system(nlpkg, orc):
             assert np.array_equal(h["R"][p0:p1].view(np.int32), o.R.view(np.int32)), s
         clist, pl = b.system(7)  # the per-system views carry the Float32 plan
         assert clist.X.dtype == torch.float32 and pl.R.dtype == torch.float32
+
+
+def _half_keep(i, j, S):
+    s = S.astype(np.int64)
+    return (j > i) | ((j == i) & ((s[:, 0] > 0) | ((s[:, 0] == 0) & ((s[:, 1] > 0) | ((s[:, 1] == 0) & (s[:, 2] > 0))))))
+
+
+@pytest.mark.parametrize("case", range(3))
+def test_half_list_float32(nlpkg, orc, case):
+    """Float32 half lists (nl_neighbour_list_half_f32): the oracle's Float32
+    full list filtered by the half rule (j > i, or j == i and S > 0
+    lexicographically), in the reference's order, bits of R included."""
+    if case == 0:
+        X, C, L = cf.rand_config(3000, seed=61)
+        rc, pbc = 5.0, (True, True, True)
+    elif case == 1:
+        X, C = cf.rand_config_triclinic(400, seed=62)
+        rc, pbc = 3.0, (True, False, True)
+    else:
+        X, C = cf.diamond_primitive()
+        rc, pbc = 6.0, (True, True, True)
+    X32 = np.ascontiguousarray(np.asarray(X, dtype=np.float32).reshape(-1, 3))
+    pl = nlpkg.neighbour_list(torch.from_numpy(X32).cuda(), rc, C, pbc, half=True)
+    o = orc.neighbour_list_f32(X32, rc, C, pbc)
+    keep = _half_keep(o.i, o.j, o.S)
+    assert pl.R.dtype == torch.float32 and int(pl.i.shape[0]) == int(keep.sum())
+    np.testing.assert_array_equal(to_np(pl.i).astype(np.int64), o.i[keep])
+    np.testing.assert_array_equal(to_np(pl.j).astype(np.int64), o.j[keep])
+    np.testing.assert_array_equal(to_np(pl.S).astype(np.int64), o.S[keep])
+    assert np.array_equal(to_np(pl.R).view(np.int32), o.R[keep].view(np.int32))
+    counts = np.bincount(o.i[keep] - 1, minlength=X32.shape[0])
+    np.testing.assert_array_equal(np.diff(to_np(pl.first).astype(np.int64)), counts)
+
+
+def test_verlet_reuse_float32(nlpkg, orc):
+    """Verlet reuse with Float32 positions: R of the kept pairs recomputed with
+    the reference's single-precision operations (bit-equal to a numpy float32
+    restatement of _getR), every pair within the cutoff equal to the oracle's
+    Float32 list, rebuild once atoms moved beyond skin / 2."""
+    X0, C, L = cf.rand_config(5000, seed=95)
+    rc, skin, pbc = 5.0, 1.0, (True, True, True)
+    v = nlpkg.VerletList(X0.shape[0], C, rc, skin, pbc, dtype=torch.float32)
+    C32 = np.asarray(C, dtype=np.float32)
+    rng = np.random.default_rng(96)
+    X = X0.astype(np.float32)
+    for step in range(4):
+        rebuilt = v.update(torch.from_numpy(X).cuda())
+        assert rebuilt == (step in (0, 3))
+        P = v.engine.total_pairs()
+        i, j, S = (t[:P].cpu().numpy().astype(np.int64) for t in (v.engine.i, v.engine.j, v.engine.S))
+        R = v.engine.R[:P].cpu().numpy()
+        assert R.dtype == np.float32
+        Sf = S.astype(np.float32)
+        cs = (Sf[:, 0:1] * C32[0] + Sf[:, 1:2] * C32[1]) + Sf[:, 2:3] * C32[2]  # float32, left fold, no FMA
+        ref = (X[j - 1] - X[i - 1]) + cs
+        assert np.array_equal(R.view(np.int32), ref.view(np.int32))
+        o = orc.neighbour_list_f32(X, rc, C, pbc)
+        inside = ((R[:, 0] * R[:, 0] + R[:, 1] * R[:, 1]) + R[:, 2] * R[:, 2]) < np.float32(rc) * np.float32(rc)
+        got = set(zip(i[inside].tolist(), j[inside].tolist(), map(tuple, S[inside].tolist())))
+        want = set(zip(o.i.tolist(), o.j.tolist(), map(tuple, o.S.tolist())))
+        assert got == want
+        X = (X + rng.uniform(-0.12, 0.12, size=X.shape) * (1.0 if step < 2 else 4.0)).astype(np.float32)
