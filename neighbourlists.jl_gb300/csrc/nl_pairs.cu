@@ -2451,11 +2451,10 @@ __global__ void __launch_bounds__(kLRWarps * 32, NL_LR_MIN_BLOCKS) k_lazy_rows(P
       double r0, r1;
       const dfloat f0 = term(on0, j0, c0, a0, b0, r0), f1 = term(on1, j1, c1, a1, b1, r1);
       acc = df_add(df_add(acc, f0), f1);
-      const bool rare = __any_sync(0xffffffffu, r0 != 0.0 || r1 != 0.0);  // FP64-evaluated terms (r2 < 1e-12)
-      if (rare) accd = dadd(accd, dadd(r0, r1));
+      accd += r0 + r1;
       if (NL_LR_HALF) {  // the neighbour's share of the pair
         double v0 = dadd(f2d_exact(f0.hi), f2d_exact(f0.lo)), v1 = dadd(f2d_exact(f1.hi), f2d_exact(f1.lo));
-        if (rare) {
+        if (__any_sync(0xffffffffu, r0 != 0.0 || r1 != 0.0)) {  // (rare) FP64-evaluated terms
           v0 = dadd(v0, r0);
           v1 = dadd(v1, r1);
         }
