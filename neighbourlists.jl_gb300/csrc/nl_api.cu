@@ -883,6 +883,7 @@ int batch_impl(const nl_batch& b, const double* X, TI* perm, double* Xs, TI* cel
   a.sys_cell = si.cell0;
   a.cell_sys = at<int>(ws, b.B.cell_sys);
   a.cs_sys = at<double>(ws, b.B.cs);
+  a.work = at<int>(ws, L.pcount) + 12;  // zeroed with the workspace's first region
   a.nsys = b.nsys;
   a.nat_total = na;
   a.ncells_total = nc;

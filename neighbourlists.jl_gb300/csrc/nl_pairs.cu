@@ -423,6 +423,11 @@ __device__ __forceinline__ void load_system(const PairArgs<TI>& A, int s, Geomet
   __syncwarp();
 }
 
+#ifndef NL_BATCH_RUN
+#define NL_BATCH_RUN 4
+#endif
+constexpr int kBatchRun = NL_BATCH_RUN;  // consecutive cells a warp takes per counter increment (batches)
+
 template <typename TI, int MODE, bool BATCH>
 __global__ void __launch_bounds__(kPairWarps * 32, BATCH ? NL_PAIR_BATCH_MIN_BLOCKS : kMinBlocks)
     k_pairs(PairArgs<TI> A) {
@@ -477,7 +482,24 @@ __global__ void __launch_bounds__(kPairWarps * 32, BATCH ? NL_PAIR_BATCH_MIN_BLO
   const bool listed = MODE == kModeFill || (MODE == kModeLazyR6 && A.list_cap > 0);
   const int ncell_iter = listed ? min(*A.n_screen_cells, A.ncells_total) : A.ncells_total;
   auto cell_at = [&](int idx) { return listed ? clampi(A.screen_cells[idx], A.ncells_total - 1) : idx; };
-  int idx = blockIdx.x * kPairWarps + warp;
+  // Batches: warps take runs of kBatchRun consecutive cells from a counter
+  // (one system's cells follow one another, so a run mostly stays in one
+  // system and its geometry is loaded once; taking runs as warps free up
+  // keeps uneven cells balanced).  Single systems: a grid stride.
+  int* work = BATCH ? A.work + (MODE == kModeCount ? 0 : 1) : nullptr;
+  int run_left = 0;
+  auto next_idx = [&](int cur) -> int {
+    if (!BATCH) return cur + nwarps;
+    if (run_left > 1) {
+      --run_left;
+      return cur + 1;
+    }
+    int b = 0;
+    if (lane == 0) b = atomicAdd(work, kBatchRun);
+    run_left = kBatchRun;
+    return __shfl_sync(0xffffffffu, b, 0);
+  };
+  int idx = BATCH ? next_idx(0) : blockIdx.x * kPairWarps + warp;
   // (0-based slot offsets, clamped to [0, nat])
   int pf_hs = 0, pf_he = 0, pf_lo = 0, pf_hi = 0;
   auto prefetch = [&](int pidx) {
@@ -493,7 +515,7 @@ __global__ void __launch_bounds__(kPairWarps * 32, BATCH ? NL_PAIR_BATCH_MIN_BLO
     pf_hi = lin >= 0 ? clampi(A.cell_offsets[lin + 1] - 1, g.nat) : 0;
   };
   prefetch(idx);
-  for (; idx < ncell_iter; idx += nwarps) {
+  for (; idx < ncell_iter; idx = next_idx(idx)) {
     const int h = cell_at(idx);
     // offsets are clamped to [0, nat] so that a malformed cell list (which
     // the prepare pass reports as inconsistent) never indexes out of bounds

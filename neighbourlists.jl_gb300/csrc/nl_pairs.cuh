@@ -83,6 +83,7 @@ struct PairArgs {
   int pair_blocks_per_sm;   // launch tuning (0 = default): count / screening grids
   int emit_blocks_per_sm;   // launch tuning (0 = default): list write grid
   int vec_ok;               // S and R start on 16-byte boundaries: the write pass stores 16-byte vectors
+  int* work;                // batch: cell counters of the count and screening passes (zeroed per call)
   unsigned long long* stats;  // [0] += FP64 rechecks
   unsigned* err;
 };
