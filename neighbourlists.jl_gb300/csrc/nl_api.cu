@@ -974,6 +974,7 @@ int batch_impl32(const nl_batch& b, const float* X, TI* perm, float* Xs, TI* cel
   a.sys_atom = si.atom0;
   a.sys_cell = si.cell0;
   a.cell_sys = at<int>(ws, b.B.cell_sys);
+  a.work = at<int>(ws, L.pcount) + 12;  // zeroed with the workspace's first region
   a.nsys = b.nsys;
   a.nat_total = na;
   a.ncells_total = nc;

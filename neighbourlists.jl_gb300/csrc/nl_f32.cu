@@ -190,7 +190,15 @@ __global__ void __launch_bounds__(kW32Warps * 32, FILL ? NL_F32_MIN_FILL : NL_F3
   const int ncells = BATCH ? a.ncells_total : g.ncells;
   int cur_sys = -1, abase = 0, coff = 0;
 
-  for (int cell = blockIdx.x * kW32Warps + (threadIdx.x >> 5); cell < ncells; cell += nwarps) {
+  // batches: the next cell from a counter as warps free up (uneven cells)
+  auto next_cell = [&](int cur) -> int {
+    if (!BATCH) return cur + nwarps;
+    int b = 0;
+    if (lane == 0) b = atomicAdd(a.work + (FILL ? 1 : 0), 1);
+    return __shfl_sync(0xffffffffu, b, 0);
+  };
+  for (int cell = BATCH ? next_cell(0) : blockIdx.x * kW32Warps + (threadIdx.x >> 5); cell < ncells;
+       cell = next_cell(cell)) {
     int hl = cell;  // the cell within its system
     if constexpr (BATCH) {
       const int sys = max(min(a.cell_sys[cell], a.nsys - 1), 0);

@@ -57,6 +57,7 @@ struct Pairs32Args {
   const int* sys_atom;       // nsys + 1
   const int* sys_cell;       // nsys + 1
   const int* cell_sys;       // ncells_total
+  int* work;                 // cell counters of the count and fill passes (zeroed per call)
   int nsys;
   int nat_total;
   int ncells_total;

@@ -1607,7 +1607,17 @@ __global__ void __launch_bounds__(kEmitWarps * 32,
   // no atom has a winding (single systems record it): candidate words need no record
   const bool plain = MASKS && !BATCH && *A.sym_wound == 0;
   const long long nwarps = (long long)gridDim.x * kEmitWarps;
-  for (long long c0 = ((long long)blockIdx.x * kEmitWarps + warp) * 32; c0 < A.nat_total; c0 += nwarps * 32) {
+  // batches: the next 32 atoms from a counter as warps free up (uneven pair
+  // counts); single systems: a grid stride
+  unsigned* ework = BATCH ? reinterpret_cast<unsigned*>(A.work) + (MASKS ? 3 : 2) : nullptr;
+  auto next_c0 = [&](long long cur) -> long long {
+    if (!BATCH) return cur + nwarps * 32;
+    unsigned b = 0;
+    if (lane == 0) b = atomicAdd(ework, 32u);
+    return (long long)__shfl_sync(0xffffffffu, b, 0);
+  };
+  for (long long c0 = BATCH ? next_c0(0) : ((long long)blockIdx.x * kEmitWarps + warp) * 32; c0 < A.nat_total;
+       c0 = next_c0(c0)) {
     const int na = int(min(32LL, A.nat_total - c0));
     __syncwarp();
     if (lane < na) {
