@@ -2244,6 +2244,16 @@ struct LRSmem {
   unsigned char cd[32 * kLRRow];  // loop shift + 1 per axis of stencil cell q (2 bits each)
 };
 
+// A C'S value in the positions' fixed point, modulo 2^64: the pair vector
+// Xj - Xi + C'S is formed in wrapping 64-bit arithmetic and is small (|R| <
+// 2^11 A), so only C'S modulo 2^12 A matters (2^12 * 2^52 = 2^64); the
+// remainder is exact in FP64 and scaled into [-2^63, 2^63).
+__device__ __forceinline__ unsigned long long fix_mod(double c) {
+  double r = remainder(c, 4096.0);  // exact, in [-2048, 2048]
+  if (r >= 2048.0) r -= 4096.0;
+  return (unsigned long long)__double2ll_rn(dmul(r, kFixScale));
+}
+
 // v * 2^-52 (v a fixed-point value of magnitude below 2^63) as a double-float:
 // three 24-bit chunks are exact floats; their sum is formed with an
 // error-free two-sum and the smallest chunk added to the error term.
@@ -2263,12 +2273,12 @@ __global__ void __launch_bounds__(kLRWarps * 32, NL_LR_MIN_BLOCKS) k_lazy_rows(P
   if (*A.sym_fail != 0) return;  // a crowded cell: the per-cell passes sum instead
   __shared__ LRSmem sm[kLRWarps];
   __shared__ double cs_blk[3 * kCsN * kCsN * kCsN];
-  __shared__ long long cs_fix[3 * kCsN * kCsN * kCsN];
+  __shared__ unsigned long long cs_fix[3 * kCsN * kCsN * kCsN];
   const Geometry& g = A.g;
   for (int t = threadIdx.x; t < 3 * kCsN * kCsN * kCsN; t += blockDim.x) {
     const double c = A.cs_table[t];
     cs_blk[t] = c;
-    cs_fix[t] = __double2ll_rn(dmul(c, kFixScale));
+    cs_fix[t] = fix_mod(c);
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -2379,27 +2389,28 @@ __global__ void __launch_bounds__(kLRWarps * 32, NL_LR_MIN_BLOCKS) k_lazy_rows(P
 #pragma unroll
           for (int k = 0; k < 3; ++k) S[k] = field10(cw, k) + field10(mi, k) - 640;
         }
-        long long rf[3];
-        rf[0] = __double_as_longlong(w0.x) - xf[0];
-        rf[1] = __double_as_longlong(w0.y) - xf[1];
-        rf[2] = (long long)(((unsigned long long)unsigned(w1.y) << 32) | unsigned(w1.x)) - xf[2];
+        // (unsigned: the differences and sums wrap modulo 2^64, the result is exact)
+        unsigned long long rf[3];
+        rf[0] = (unsigned long long)__double_as_longlong(w0.x) - (unsigned long long)xf[0];
+        rf[1] = (unsigned long long)__double_as_longlong(w0.y) - (unsigned long long)xf[1];
+        rf[2] = (((unsigned long long)unsigned(w1.y) << 32) | unsigned(w1.x)) - (unsigned long long)xf[2];
         const bool nz = on && (S[0] | S[1] | S[2]) != 0;
         if (__any_sync(0xffffffffu, nz)) {
           if (nz) {
             if (abs(S[0]) <= kCsR && abs(S[1]) <= kCsR && abs(S[2]) <= kCsR) {
-              const long long* tb = cs_fix + 3 * ((S[0] + kCsR) + kCsN * ((S[1] + kCsR) + kCsN * (S[2] + kCsR)));
+              const unsigned long long* tb = cs_fix + 3 * ((S[0] + kCsR) + kCsN * ((S[1] + kCsR) + kCsN * (S[2] + kCsR)));
               rf[0] += tb[0];
               rf[1] += tb[1];
               rf[2] += tb[2];
             } else {
 #pragma unroll
-              for (int k = 0; k < 3; ++k) rf[k] += __double2ll_rn(dmul(cts_k(g.C, S[0], S[1], S[2], k), kFixScale));
+              for (int k = 0; k < 3; ++k) rf[k] += fix_mod(cts_k(g.C, S[0], S[1], S[2], k));
             }
           }
         }
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-          const dfloat d = fix_to_df(rf[k]);
+          const dfloat d = fix_to_df((long long)rf[k]);
           r2 = df_add(r2, df_sq(d.hi, d.lo));
         }
         if (__any_sync(0xffffffffu, on && !(r2.hi >= 1e-12f))) {  // (rare) the FP64 positions for the formula

@@ -134,9 +134,10 @@ def test_fused_lazy_close_pairs(nlpkg, orc):
 
 def test_fast_lazy_sum_windings_and_far_positions(nlpkg, orc):
     """The fast sum's two position paths: atoms wound once around periodic
-    axes (fixed-point R, S from the windings) and a chain of atoms reaching
+    axes (fixed-point R, S from the windings), a chain of atoms reaching
     beyond 2000 A along an open axis (outside the fixed-point range: R with
-    the reference's FP64 operations)."""
+    the reference's FP64 operations), and a long periodic box whose wound
+    atoms give shifts C'S beyond 2048 A (fixed point modulo 2^64)."""
     X, C, L = cf.rand_config(3000, seed=21)
     Xw = X.copy()
     Xw[:200, 0] += L          # winding +1 on x
@@ -145,9 +146,49 @@ def test_fast_lazy_sum_windings_and_far_positions(nlpkg, orc):
     n = 1300
     Xc = np.stack([np.arange(n) * 2.0 + rng.uniform(-0.3, 0.3, n), rng.uniform(0, 16, n), rng.uniform(0, 16, n)], 1)
     Cc = np.diag([2.0 * n, 16.0, 16.0])  # 3 cells across y and z: the mask pass takes it
+    # a 1100 A periodic chain whose ends are wound +1 and -2: pairs across the
+    # x boundary have C'S = 2200 A (beyond 2^11 A: the fixed-point shift
+    # wraps modulo 2^64 together with Xj - Xi)
+    m = 2200
+    Xl = np.stack([np.arange(m) * 0.5 + rng.uniform(-0.2, 0.2, m), rng.uniform(0, 16, m), rng.uniform(0, 16, m)], 1)
+    Xl[Xl[:, 0] < 50.0, 0] += 1100.0
+    Xl[Xl[:, 0] > 1050.0, 0] -= 2200.0
+    Xl[(np.arange(m) % 7 == 3) & (Xl[:, 0] > 100.0) & (Xl[:, 0] < 800.0), 0] += 1100.0
+    Cl = np.diag([1100.0, 16.0, 16.0])
     for Xs, Cs, pbc in ((Xw, C, (True, True, True)), (Xc, Cc, (False, True, True))):
         clist = nlpkg.build_cell_list(torch.from_numpy(np.ascontiguousarray(Xs)).cuda(), 5.0, Cs, pbc)
         ref = orc.lazy_sum_r6(orc.build_cell_list(Xs, 5.0, Cs, pbc))
         got = nlpkg.lazy_reduce(clist, "inv_r6_fast").cpu().numpy()
         rel = np.abs(got - ref) / np.maximum(np.abs(ref), 1e-300)
         assert rel.max() <= LAZY_RTOL, rel.max()
+    # at |X| ~ 1900 A and C'S = 2200 A the reference's own FP64 R is off by a
+    # few 1e-13 A (about 1.4e-12 on the sums): the fast sum is held to 1e-12 of
+    # the exact sums, and to the oracle within 1e-12 plus the oracle's own error
+    clist = nlpkg.build_cell_list(torch.from_numpy(np.ascontiguousarray(Xl)).cuda(), 5.0, Cl, (True, True, True))
+    ref = orc.lazy_sum_r6(orc.build_cell_list(Xl, 5.0, Cl, (True, True, True)))
+    got = nlpkg.lazy_reduce(clist, "inv_r6_fast").cpu().numpy()
+    ex = _exact_sum_r6(Xl, Cl, orc.neighbour_list(Xl, 5.0, Cl, (True, True, True), nthreads=8))
+    den = np.maximum(np.abs(ex), 1e-300)
+    assert (np.abs(got - ex) / den).max() <= LAZY_RTOL
+    assert (np.abs(got - ref) / den).max() <= LAZY_RTOL + (np.abs(ref - ex) / den).max()
+
+
+def _exact_sum_r6(X, C, o):
+    """Per-atom sums of 1/r^6 over the list's pairs with R = Xj - Xi + C'S and
+    r^2 in exact rational arithmetic (each term correctly rounded, summed
+    with math.fsum)."""
+    from fractions import Fraction
+    import math
+
+    I, J, S = np.asarray(o.i) - 1, np.asarray(o.j) - 1, np.asarray(o.S)
+    Xf = [[Fraction(float(v)) for v in row] for row in X]
+    Cf = [[Fraction(float(v)) for v in row] for row in C]
+    terms = [[] for _ in range(len(X))]
+    for p in range(len(I)):
+        i, j, s = int(I[p]), int(J[p]), [int(v) for v in S[p]]
+        r2 = Fraction(0)
+        for k in range(3):
+            d = Xf[j][k] - Xf[i][k] + sum(Cf[l][k] * s[l] for l in range(3))
+            r2 += d * d
+        terms[i].append(float(1 / r2 ** 3))
+    return np.array([math.fsum(t) for t in terms])
