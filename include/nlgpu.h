@@ -402,7 +402,7 @@ int nl_legacy_fill_pairs(int64_t nat, const double cell[9], const double inv_cel
 typedef struct nl_tuning {
   int pair_blocks_per_sm;   /* count / screening write / lazy kernels, 1..256 */
   int emit_blocks_per_sm;   /* list write kernel, 1..256 */
-  int count_kernel;         /* 0 default (single systems: 3 where it applies, else 1; batches: 1);
+  int count_kernel;         /* 0 default (3 where it applies, else 1);
                                1 one warp per home cell; 2 one thread per home atom; 3 each unordered
                                pair of cells screened once with neighbour masks (systems whose 27-cell
                                stencil has distinct cells, single or in a batch; a system with a cell

@@ -143,10 +143,10 @@ class BatchNeighbourList:
         return self.last_total
 
     def set_tuning(self, pair_blocks_per_sm: int = 0, emit_blocks_per_sm: int = 0, count_kernel: int = 0) -> None:
-        """Launch shapes (nl_batch_set_tuning; 0 = default).  count_kernel: 0 or
-        1 one warp per home cell, 2 one thread per home atom, 3 the symmetric
-        pass for the systems whose 27-cell stencil has distinct cells (the
-        per-cell pass for the others).  Results never depend on them."""
+        """Launch shapes (nl_batch_set_tuning; 0 = default).  count_kernel: 1
+        one warp per home cell, 2 one thread per home atom, 0 or 3 the
+        symmetric pass for the systems whose 27-cell stencil has distinct cells
+        (the per-cell pass for the others).  Results never depend on them."""
         t = _lib.Tuning(int(pair_blocks_per_sm), int(emit_blocks_per_sm), int(count_kernel))
         check(lib().nl_batch_set_tuning(self._h, C.byref(t)))
 

@@ -789,10 +789,14 @@ int legacy_check(int64_t nat, const int64_t* ncells, const int64_t* nxyz, int in
 // --------------------------------------------------------------- batches --
 struct BatchLayout {
   Layout L;  // the single-system layout for all atoms and cells of the batch
-  size_t geo, atom0, cell0, cs, first_all, sys_sym, sys_fail, cell_sys, geo32, end;
+  size_t geo, atom0, cell0, cs, first_all, sys_sym, sys_fail, cell_sys, geo32, nonsym_cells, nonsym_chunks, rounds,
+      end;
 };
 
-BatchLayout batch_layout(int64_t nat, int64_t ncells, int nsys) {
+// n_chunks: the 32-slot chunks of the systems that the symmetric count pass
+// does not take; the lists of cells and chunks the per-cell passes walk have
+// room for every system failing the pass as well
+BatchLayout batch_layout(int64_t nat, int64_t ncells, int nsys, size_t n_chunks = 0) {
   BatchLayout B;
   B.L = layout(nat, ncells);
   B.L.use_lists = (unsigned long long)nat * nl::kListCap < (1ull << 32);
@@ -815,6 +819,12 @@ BatchLayout batch_layout(int64_t nat, int64_t ncells, int nsys) {
   o += up(sizeof(int) * size_t(ncells > 0 ? ncells : 1));
   B.geo32 = o;  // Float32 batches: the per-system single-precision geometry
   o += up(sizeof(nl::Geo32) * size_t(nsys));
+  B.nonsym_cells = o;
+  o += up(sizeof(int) * size_t(ncells > 0 ? ncells : 1));
+  B.nonsym_chunks = o;
+  o += up(sizeof(int) * (n_chunks + size_t(nat / 32) + 2 * size_t(nsys) + 2));
+  B.rounds = o;  // rounds of 32 home atoms of those cells (at most nat / 32 + 2)
+  o += up(sizeof(int2) * (size_t(nat / 32) + 2));
   B.end = o;
   return B;
 }
@@ -842,6 +852,10 @@ struct nl_batch {
   std::vector<int> atom0, cell0;
   std::vector<int> sym;  // per system: the symmetric count pass applies
   bool any_sym = false;
+  // the cells, and the 32-slot chunks of sorted slots, of the systems the
+  // symmetric pass does not take: the per-cell count and list write passes
+  // walk these and those of the systems that fail the pass
+  std::vector<int> nonsym_cells, nonsym_chunks;
   BatchLayout B;
   nl_tuning tuning = {0, 0, 0};
 };
@@ -891,15 +905,23 @@ int batch_impl(const nl_batch& b, const double* X, TI* perm, double* Xs, TI* cel
   a.pair_blocks_per_sm = b.tuning.pair_blocks_per_sm;
   a.emit_blocks_per_sm = b.tuning.emit_blocks_per_sm;
   a.count_kernel = b.tuning.count_kernel;
-  // count kernel 3: the symmetric pass for the systems it applies to (it
-  // accumulates their counts), the per-cell pass for the rest.  Not the
-  // default here: on batches of small systems (a few atoms per cell) its
-  // per-cell overhead and the mask decode cost more than screening every
-  // ordered pair -- 5.6 against 4.9 ms for 4,096 systems of 8 to 4,096 atoms
-  // -- so the autotuner decides.
-  a.sym = b.any_sym && a.list_cap > 0 && a.count_kernel == 3 ? 1 : 0;
+  // count kernel 0 (default) or 3: the symmetric pass for the systems it
+  // applies to (it accumulates their counts; their pairs are written from the
+  // masks in original order), the per-cell pass for the rest -- 3.87 against
+  // 4.16 ms with the per-cell pass for all (count kernel 1) on 4,096 systems
+  // of 8 to 4,096 atoms.
+  a.sym = b.any_sym && a.list_cap > 0 && (a.count_kernel == 0 || a.count_kernel == 3) ? 1 : 0;
   a.sys_sym = at<int>(ws, b.B.sys_sym);
   a.sys_fail = at<int>(ws, b.B.sys_fail);
+  a.extra_cells = at<int>(ws, L.pcount) + 9;    // zeroed with the workspace's first region
+  a.extra_chunks = at<int>(ws, L.pcount) + 10;  // likewise
+  a.n_rounds = at<int>(ws, L.pcount) + 3;       // likewise
+  a.round_work = at<int>(ws, L.pcount) + 11;    // likewise
+  a.rounds = at<int2>(ws, b.B.rounds);
+  a.nonsym_cells = at<int>(ws, b.B.nonsym_cells);
+  a.n_nonsym_cells = int(b.nonsym_cells.size());
+  a.nonsym_chunks = at<int>(ws, b.B.nonsym_chunks);
+  a.n_nonsym_chunks = int(b.nonsym_chunks.size());
   if (a.sym && na > 0) {
     e = cudaMemsetAsync(a.counts, 0, sizeof(int) * size_t(na), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(a.sys_fail, 0, sizeof(int) * size_t(b.nsys), st);
@@ -1329,7 +1351,13 @@ int nl_batch_create(const nl_system* systems, int nsys, int index_bytes, nl_batc
   b->cell0[size_t(nsys)] = int(nc);
   b->nat = na;
   b->ncells = nc;
-  b->B = batch_layout(na, nc, nsys);
+  for (int s = 0; s < nsys; ++s) {
+    if (b->sym[size_t(s)]) continue;
+    for (int c = b->cell0[size_t(s)]; c < b->cell0[size_t(s) + 1]; ++c) b->nonsym_cells.push_back(c);
+    for (int c0 = b->atom0[size_t(s)] & ~31; c0 < b->atom0[size_t(s) + 1]; c0 += 32)
+      if (b->nonsym_chunks.empty() || b->nonsym_chunks.back() != c0) b->nonsym_chunks.push_back(c0);
+  }
+  b->B = batch_layout(na, nc, nsys, b->nonsym_chunks.size());
   *batch = b;
   return NL_OK;
 }
@@ -1459,6 +1487,12 @@ int nl_batch_upload(const nl_batch* batch, void* d_workspace, size_t workspace_b
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(at<char>(d_workspace, B.sys_sym), batch->sym.data(), sizeof(int) * batch->sym.size(),
                         cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && !batch->nonsym_cells.empty())
+    e = cudaMemcpyAsync(at<char>(d_workspace, B.nonsym_cells), batch->nonsym_cells.data(),
+                        sizeof(int) * batch->nonsym_cells.size(), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && !batch->nonsym_chunks.empty())
+    e = cudaMemcpyAsync(at<char>(d_workspace, B.nonsym_chunks), batch->nonsym_chunks.data(),
+                        sizeof(int) * batch->nonsym_chunks.size(), cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) return cuda_fail(e, "upload batch tables");
   if (!batch->f32) nl::launch_cs_tables(at<nl::Geometry>(d_workspace, B.geo), batch->nsys, at<double>(d_workspace, B.cs), st);
   nl::launch_cell_systems(at<int>(d_workspace, B.cell0), batch->nsys, at<int>(d_workspace, B.cell_sys), st);

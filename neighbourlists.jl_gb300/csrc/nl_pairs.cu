@@ -480,14 +480,30 @@ __global__ void __launch_bounds__(kPairWarps * 32, BATCH ? NL_PAIR_BATCH_MIN_BLO
   // (k_emit writes the others); count and lazy visit every cell.
   // (so does the lazy pass when the per-atom lists cover the other cells)
   const bool listed = MODE == kModeFill || (MODE == kModeLazyR6 && A.list_cap > 0);
-  const int ncell_iter = listed ? min(*A.n_screen_cells, A.ncells_total) : A.ncells_total;
-  auto cell_at = [&](int idx) { return listed ? clampi(A.screen_cells[idx], A.ncells_total - 1) : idx; };
+  // a batch's count pass after the symmetric one: only the cells of the
+  // systems it did not take or that failed it
+  const bool nonsym = BATCH && MODE == kModeCount && A.sym && A.nonsym_cells;
+  // ... in rounds of 32 home atoms, so that a cell of many atoms (a small
+  // system's only cell, a crowded one) does not hold one warp alone
+  const bool split = nonsym && A.rounds;
+  const bool rpass = split && A.round_pass;
+  const int rcap = A.nat_total / 32 + 2;  // rounds the list holds
+  const int ncell_iter = listed   ? min(*A.n_screen_cells, A.ncells_total)
+                         : rpass  ? min(*A.n_rounds, rcap)
+                         : nonsym ? min(A.n_nonsym_cells + *A.extra_cells, A.ncells_total)
+                                  : A.ncells_total;
+  auto cell_at = [&](int idx) {
+    return listed ? clampi(A.screen_cells[idx], A.ncells_total - 1)
+           : rpass  ? clampi(A.rounds[idx].x, A.ncells_total - 1)
+           : nonsym ? clampi(A.nonsym_cells[idx], A.ncells_total - 1)
+                    : idx;
+  };
   // Batches: warps take their next cell (runs of kBatchRun cells) from a
   // counter as they free up, which balances the uneven cells of a batch
   // (4.69 -> 4.33 ms per 4,096-system batch against a grid stride; runs of
   // 2, 4 and 8 consecutive cells, fewer geometry loads, were slower: 4.59,
   // 5.26, 5.65 ms).  Single systems: a grid stride.
-  int* work = BATCH ? A.work + (MODE == kModeCount ? 0 : 1) : nullptr;
+  int* work = BATCH ? (rpass ? A.round_work : A.work + (MODE == kModeCount ? 0 : 1)) : nullptr;
   int run_left = 0;
   auto next_idx = [&](int cur) -> int {
     if (!BATCH) return cur + nwarps;
@@ -545,8 +561,21 @@ __global__ void __launch_bounds__(kPairWarps * 32, BATCH ? NL_PAIR_BATCH_MIN_BLO
     const int hl = sv.hl;
     bool overflow = false;  // count: an atom of this cell has more than list_cap pairs
     const int hc0 = hl % g.ns[0] + 1, hc1 = (hl / g.ns[0]) % g.ns[1] + 1, hc2 = hl / (g.ns[0] * g.ns[1]) + 1;
+    int hb0 = hs, hb1 = he;  // the home atoms this warp takes
+    if (rpass) {
+      hb0 = min(hs + 32 * max(A.rounds[idx].y, 0), he);
+      hb1 = min(hb0 + 32, he);
+    } else if (split && he - hs > 32) {  // the first 32 here, the other rounds listed
+      hb1 = hs + 32;
+      const int nr = ((he - hs + 31) >> 5) - 1;
+      int base = 0;
+      if (lane == 0) base = atomicAdd(A.n_rounds, nr);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      for (int k = lane; k < nr; k += 32)
+        if (base + k < rcap) A.rounds[base + k] = make_int2(h, k + 1);
+    }
 
-    for (int hb = hs; hb < he; hb += 32) {
+    for (int hb = hb0; hb < hb1; hb += 32) {
       const int nb = min(32, he - hb);
       float ux = 0.f, uy = 0.f, uz = 0.f;
 
@@ -809,8 +838,9 @@ __global__ void __launch_bounds__(kPairWarps * 32, BATCH ? NL_PAIR_BATCH_MIN_BLO
       __syncwarp();
     }
     // a cell with an atom whose list overflowed (or with no lists at all) is
-    // written by the screening write pass
-    if (MODE == kModeCount && __any_sync(0xffffffffu, overflow) && lane == 0) {
+    // written by the screening write pass (once: its rounds may all overflow)
+    if (MODE == kModeCount && __any_sync(0xffffffffu, overflow) && lane == 0 &&
+        (!split || atomicExch(A.cell_flag + h, 1) == 0)) {
       const int u = atomicAdd(A.n_screen_cells, 1);
       if (u < A.ncells_total) A.screen_cells[u] = h;
     }
@@ -822,7 +852,7 @@ __global__ void __launch_bounds__(kPairWarps * 32, BATCH ? NL_PAIR_BATCH_MIN_BLO
 }
 
 // ------------------------------------------------------------------------
-// Symmetric count pass (single systems whose 27-cell stencil has distinct
+// Symmetric count pass (systems whose 27-cell stencil has distinct
 // cells).  The reference decides (i, j, S) and (j, i, -S) identically:
 // R(j, i, -S) = -R(i, j, S) bit for bit under round-to-nearest, so dot(R, R)
 // is the same.  Each unordered pair of cells (A, A + d) is therefore
@@ -834,327 +864,16 @@ __global__ void __launch_bounds__(kPairWarps * 32, BATCH ? NL_PAIR_BATCH_MIN_BLO
 // cell 26 - q (column: which atoms of A accepted j); words whose mirrored
 // cell is empty or outside an open axis are written as 0 by the atom's own
 // warp, so every word is written exactly once.  Pair counts accumulate with
-// atomics; k_emit<masks> decodes the masks in the reference's order (stencil
+// atomics; the write pass decodes the masks in the reference's order (stencil
 // order, then sorted order in each cell).  A cell of more than 32 atoms sets
 // sym_fail, and the per-cell count pass with per-atom lists runs instead.
-constexpr int kSymWarps = 4;
-#ifndef NL_SYM_CHUNK
-#define NL_SYM_CHUNK 128
-#endif
-#ifndef NL_SYM_GROUP
-#define NL_SYM_GROUP 2
-#endif
-#ifndef NL_SYM_MIN_BLOCKS
-#define NL_SYM_MIN_BLOCKS 8
-#endif
-#ifndef NL_SYM_BATCH_MIN_BLOCKS
-#define NL_SYM_BATCH_MIN_BLOCKS 6  // the batch variant keeps a per-system view in registers
-#endif
-constexpr int kSymChunk = NL_SYM_CHUNK;  // staged candidates per round of home atoms
-constexpr int kSymGroup = NL_SYM_GROUP;  // home atoms screened per candidate load
 // record meta of an atom without windings that is not exact
 constexpr unsigned kPlainMeta = (128u) | (128u << 10) | (128u << 20);
 
-// The 27 mask words of a sorted slot: single systems store them densely;
-// batches, whose systems mix masks and lists, at the start of the slot's own
-// list region (2 list_cap words), so the two never overlap.
-template <typename TI, bool BATCH>
-__device__ __forceinline__ unsigned* sym_word(const PairArgs<TI>& A, long long slot) {
-  return BATCH ? reinterpret_cast<unsigned*>(A.lists + slot * A.list_cap)
-               : reinterpret_cast<unsigned*>(A.lists) + 27LL * slot;
-}
-// per non-empty home cell: first sorted slot (27 words) and loop-shift base
-// (27 words) of its stencil cells.  Single systems: after the masks (the
-// host checks that 27 nat + 54 ncells words fit the list region); batches:
-// after the masks in the list region of the cell's first slot.
-template <typename TI, bool BATCH>
-__device__ __forceinline__ unsigned* sym_table(const PairArgs<TI>& A, int cell, int first_slot) {
-  return BATCH ? sym_word<TI, true>(A, first_slot) + 27
-               : reinterpret_cast<unsigned*>(A.lists) + 27LL * A.g.nat + 54LL * cell;
-}
-
-struct __align__(16) SymSmem {
-  float4 cv[kSymChunk];      // home-relative FP32 candidate (NaN exact, +inf padding); w = candidate word
-  int cslot[kSymChunk];      // sorted slot
-  int corig[kSymChunk];      // 0-based original index
-  unsigned cqb[kSymChunk];   // q << 8 | index of the candidate in its cell
-  unsigned ccol[kSymChunk];  // home atoms that accepted the candidate
-  unsigned rmask[32][15];    // rows of the home atoms, q = 13..26 (padded)
-  unsigned hmeta[32];
-  int horig[32];             // 0-based original index of the home atoms (half lists)
-  float box[6];
-  int prune;
-};
-
-// Batches run it over the cells of the systems flagged in sys_sym, with each
-// system's geometry and its cells and slots offset to the launch's; a system
-// with a crowded cell sets its sys_fail and the per-cell pass counts it.
-template <typename TI, bool BATCH>
-__global__ void __launch_bounds__(kSymWarps * 32, BATCH ? NL_SYM_BATCH_MIN_BLOCKS : NL_SYM_MIN_BLOCKS)
-    k_pairs_sym(PairArgs<TI> A) {
-  __shared__ SymSmem sm[kSymWarps];
-  __shared__ Geometry geo_w[BATCH ? kSymWarps : 1];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  SymSmem& W = sm[warp];
-  const Geometry& g = BATCH ? geo_w[warp] : A.g;
-  const int nat = A.nat_total;  // slot bound (g.nat for a single system)
-  const unsigned lt = lt_mask();
-  unsigned rechecks = 0;
-  int cur_sys = -1;
-  if (A.cap_rec && blockIdx.x == 0 && threadIdx.x == 0) *A.cap_rec = A.list_cap;
-  for (int h = blockIdx.x * kSymWarps + warp; h < A.ncells_total; h += gridDim.x * kSymWarps) {
-    // system view: first slot / original atom, index of cell 0 in cell_offsets, home cell in the system
-    int sys = 0, abase = 0, coff = 0, hl = h;
-    if constexpr (BATCH) {
-      sys = clampi(A.cell_sys[h], A.nsys - 1);
-      if (!A.sys_sym[sys]) continue;
-      if (sys != cur_sys) {
-        __syncwarp();
-        const int* src = reinterpret_cast<const int*>(A.geo + sys);
-        int* dst = reinterpret_cast<int*>(&geo_w[warp]);
-        for (int k = lane; k < int(sizeof(Geometry) / 4); k += 32) dst[k] = src[k];
-        __syncwarp();
-        cur_sys = sys;
-      }
-      abase = A.sys_atom[sys];
-      coff = A.sys_cell[sys] + sys;
-      hl = h - A.sys_cell[sys];
-    }
-    const float lo = g.lo, hi = g.hi;
-    const int hs = clampi(A.cell_offsets[coff + hl] - 1 + abase, nat);
-    const int he = clampi(A.cell_offsets[coff + hl + 1] - 1 + abase, nat);
-    const int nb = he - hs;
-    if (nb <= 0) continue;
-    const int hc0 = hl % g.ns[0] + 1, hc1 = (hl / g.ns[0]) % g.ns[1] + 1, hc2 = hl / (g.ns[0] * g.ns[1]) + 1;
-    // stencil cell q = lane
-    int cstart = 0, ccount = 0, lin = -1;
-    unsigned slp = 0;
-    float ox = 0.f, oy = 0.f, oz = 0.f;
-    if (lane < 27) {
-      lin = stencil_cell(g, nullptr, 0, 3, 3, hc0, hc1, hc2, lane, slp, ox, oy, oz);
-      if (lin >= 0) {
-        cstart = clampi(A.cell_offsets[coff + lin] - 1 + abase, nat);
-        ccount = max(clampi(A.cell_offsets[coff + lin + 1] - 1 + abase, nat) - cstart, 0);
-      }
-    }
-    if (nb > 32 || __any_sync(0xffffffffu, ccount > 32)) {
-      if (lane == 0) atomicOr(BATCH ? A.sys_fail + sys : A.sym_fail, 1);
-      continue;
-    }
-    if (lane < 27) {  // the write pass reads the cell's stencil from here
-      unsigned* tab = sym_table<TI, BATCH>(A, h, hs);
-      tab[lane] = unsigned(cstart);
-      tab[27 + lane] = slp;
-    }
-    // words of the home atoms no other warp writes: mirrored cell empty or outside
-    const unsigned zq = __ballot_sync(0xffffffffu, lane < 13 && (lin < 0 || ccount == 0));
-    if (zq)
-      for (int t = lane; t < nb * 13; t += 32) {
-        const int a = t / 13, q = t - 13 * a;
-        if ((zq >> q) & 1u) sym_word<TI, BATCH>(A, hs + a)[q] = 0u;
-      }
-    __syncwarp();
-    float ux = 0.f, uy = 0.f, uz = 0.f;
-    unsigned hm = kPlainMeta;
-    if (lane < nb) {
-      const float4 r = A.rec[hs + lane];
-      ux = r.x;
-      uy = r.y;
-      uz = r.z;
-      hm = __float_as_uint(r.w);
-      W.hmeta[lane] = hm;
-      W.horig[lane] = abase + clampi(A.perm[hs + lane] - 1, g.nat - 1);  // original index in the launch
-    }
-    if (!BATCH && __any_sync(0xffffffffu, hm != kPlainMeta) && lane == 0) atomicOr(A.sym_wound, 1);
-#pragma unroll
-    for (int k = 0; k < 14; ++k) W.rmask[lane][k] = 0u;
-    {
-      const float inf = __int_as_float(0x7f800000);
-      const bool in = lane < nb;
-      float bl[3] = {in ? ux : inf, in ? uy : inf, in ? uz : inf};
-      float bh[3] = {in ? ux : -inf, in ? uy : -inf, in ? uz : -inf};
-#pragma unroll
-      for (int d = 0; d < 3; ++d)
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          bl[d] = fminf(bl[d], __shfl_xor_sync(0xffffffffu, bl[d], o));
-          bh[d] = fmaxf(bh[d], __shfl_xor_sync(0xffffffffu, bh[d], o));
-        }
-      const bool pr = !__any_sync(0xffffffffu, in && (W.hmeta[lane] & kExactBit) != 0);
-      if (lane == 0) {
-        W.box[0] = bl[0];
-        W.box[1] = bh[0];
-        W.box[2] = bl[1];
-        W.box[3] = bh[1];
-        W.box[4] = bl[2];
-        W.box[5] = bh[2];
-        W.prune = pr;
-      }
-    }
-    // candidates: the centre and the cells after it (lanes 13..26), flattened
-    const int scnt = lane >= 13 ? ccount : 0;
-    int incl = scnt;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int v = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += v;
-    }
-    const int tg = __shfl_sync(0xffffffffu, incl, 31);
-    __syncwarp();
-    const bool prune = W.prune != 0;
-    for (int cb = 0; cb < tg; cb += kSymChunk) {
-      const int nch = min(kSymChunk, tg - cb);
-      // ---- stage: home-relative FP32 candidates, dropped when farther from
-      // the home atoms' box than the reject bound (their column words are 0)
-      int nkeep = 0;
-      for (int f0 = 0; f0 < nch; f0 += 32) {
-        const int f = f0 + lane;
-        const int gf = cb + min(f, nch - 1);
-        int q = 0;
-#pragma unroll
-        for (int step = 16; step > 0; step >>= 1) {
-          const int v = __shfl_sync(0xffffffffu, incl, q + step - 1);
-          if (v <= gf) q += step;
-        }
-        const int q_incl = __shfl_sync(0xffffffffu, incl, q);
-        const int q_cnt = __shfl_sync(0xffffffffu, scnt, q);
-        const int q_start = __shfl_sync(0xffffffffu, cstart, q);
-        const unsigned q_slp = __shfl_sync(0xffffffffu, slp, q);
-        const float qx = __shfl_sync(0xffffffffu, ox, q);
-        const float qy = __shfl_sync(0xffffffffu, oy, q);
-        const float qz = __shfl_sync(0xffffffffu, oz, q);
-        bool keep = false;
-        float4 cv;
-        int slot = 0, bit = 0;
-        if (f < nch) {
-          bit = gf - (q_incl - q_cnt);
-          slot = q_start + bit;
-          const float4 r = A.rec[slot];
-          const unsigned mj = __float_as_uint(r.w);
-          const unsigned cw = cand_word(q_slp, mj);
-          const float nan = __int_as_float(0x7fc00000);
-          const bool ex = (cw & kExactBit) != 0;
-          cv = make_float4(ex ? nan : r.x + qx, ex ? nan : r.y + qy, ex ? nan : r.z + qz, __uint_as_float(cw));
-          const float dx = fmaxf(fmaxf(W.box[0] - cv.x, cv.x - W.box[1]), 0.f);
-          const float dy = fmaxf(fmaxf(W.box[2] - cv.y, cv.y - W.box[3]), 0.f);
-          const float dz = fmaxf(fmaxf(W.box[4] - cv.z, cv.z - W.box[5]), 0.f);
-          const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-          keep = ex || !(prune && d2 > hi);
-          if (!keep && q > 13) sym_word<TI, BATCH>(A, slot)[26 - q] = 0u;
-        }
-        const unsigned km = __ballot_sync(0xffffffffu, keep);
-        if (keep) {
-          const int pos = nkeep + __popc(km & lt);
-          W.cv[pos] = cv;
-          W.cslot[pos] = slot;
-          W.corig[pos] = abase + clampi(A.perm[slot] - 1, g.nat - 1);
-          W.cqb[pos] = (unsigned(q) << 8) | unsigned(bit);
-          W.ccol[pos] = 0u;
-        }
-        nkeep += __popc(km);
-      }
-      {
-        const int pos = nkeep + lane;
-        if (pos < ((nkeep + 31) & ~31)) {
-          const float inf = __int_as_float(0x7f800000);
-          W.cv[pos] = make_float4(inf, inf, inf, 0.f);
-          W.cqb[pos] = 13u << 8;
-          W.ccol[pos] = 0u;
-        }
-      }
-      __syncwarp();
-      // ---- screen: kSymGroup home atoms per candidate load
-      const int nround = (nkeep + 31) & ~31;
-      for (int a0 = 0; a0 < nb; a0 += kSymGroup) {
-        float ax[kSymGroup], ay[kSymGroup], az[kSymGroup];
-#pragma unroll
-        for (int k = 0; k < kSymGroup; ++k) {
-          const int a = min(a0 + k, nb - 1);
-          const bool use = a0 + k < nb;
-          const float inf = __int_as_float(0x7f800000);
-          ax[k] = use ? __shfl_sync(0xffffffffu, ux, a) : inf;
-          ay[k] = use ? __shfl_sync(0xffffffffu, uy, a) : inf;
-          az[k] = use ? __shfl_sync(0xffffffffu, uz, a) : inf;
-        }
-        for (int r0 = 0; r0 < nround; r0 += 32) {
-          const int f = r0 + lane;
-          const float4 c = W.cv[f];
-          bool acc[kSymGroup], unc[kSymGroup];
-          bool any_unc = false;
-#pragma unroll
-          for (int k = 0; k < kSymGroup; ++k) {
-            const float rx = c.x - ax[k], ry = c.y - ay[k], rz = c.z - az[k];
-            const float r2 = fmaf(rz, rz, fmaf(ry, ry, rx * rx));
-            acc[k] = r2 < lo && r2 > 0.f;
-            unc[k] = !(r2 > hi) && !acc[k];
-            any_unc |= unc[k];
-          }
-          if (__any_sync(0xffffffffu, any_unc)) {
-#pragma unroll
-            for (int k = 0; k < kSymGroup; ++k)
-              if (unc[k]) {
-                const int a = a0 + k;
-                if (f >= nkeep || a >= nb || is_self(W.cslot[f], hs + a, __float_as_uint(c.w), W.hmeta[a])) {
-                  acc[k] = false;
-                } else {
-                  ++rechecks;
-                  acc[k] = exact_pair(g, A.Xs, hs + a, W.cslot[f], W.hmeta[a], __float_as_uint(c.w));
-                }
-              }
-          }
-          unsigned col = 0u;
-          const unsigned qb = W.cqb[f];
-#pragma unroll
-          for (int k = 0; k < kSymGroup; ++k)
-            if (acc[k]) {
-              // full lists keep both directions; a half list keeps the one
-              // half_keep selects: the home atom's row or the candidate's column
-              bool row = true, column = (qb >> 8) > 13u;
-              if (A.half) {
-                row = half_keep(W.horig[a0 + k], W.corig[f], __float_as_uint(c.w), W.hmeta[a0 + k]);
-                column = column && !row;
-              }
-              if (row) atomicOr(&W.rmask[a0 + k][(qb >> 8) - 13], 1u << (qb & 255u));
-              if (column) col |= 1u << (a0 + k);
-            }
-          if (col) W.ccol[f] |= col;
-        }
-      }
-      __syncwarp();
-      // ---- columns: the mirrored cell's word of every kept candidate
-      for (int f = lane; f < nkeep; f += 32) {
-        const unsigned q = W.cqb[f] >> 8;
-        if (q > 13) {
-          const unsigned cc = W.ccol[f];
-          sym_word<TI, BATCH>(A, W.cslot[f])[26 - q] = cc;
-          if (cc) atomicAdd(A.counts + W.corig[f], __popc(cc));
-        }
-      }
-      __syncwarp();
-    }
-    // ---- rows: words q = 13..26 of the home atoms, and their counts
-    for (int t = lane; t < nb * 14; t += 32) {
-      const int a = t / 14, k = t - 14 * a;
-      sym_word<TI, BATCH>(A, hs + a)[13 + k] = W.rmask[a][k];
-    }
-    if (lane < nb) {
-      int c = 0;
-#pragma unroll
-      for (int k = 0; k < 14; ++k) c += __popc(W.rmask[lane][k]);
-      if (c) atomicAdd(A.counts + W.horig[lane], c);
-    }
-    __syncwarp();
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) rechecks += __shfl_xor_sync(0xffffffffu, rechecks, o);
-  if (lane == 0 && rechecks) atomicAdd(A.stats, (unsigned long long)rechecks);
-}
-
 // ------------------------------------------------------------------------
-// Symmetric count pass of single systems, candidate-parallel.  It makes the
-// same decisions and writes the same neighbour masks and counts as
-// k_pairs_sym: each unordered pair of cells (A, A + d), d the centre or one
-// of the 13 stencil offsets after it, is screened once, by the warp of A.
+// The symmetric count pass, candidate-parallel: each unordered pair of cells
+// (A, A + d), d the centre or one of the 13 stencil offsets after it, is
+// screened once, by the warp of A.
 // Lanes hold the candidates -- the atoms of stencil cells q = 13..26 in
 // stencil order (centre first), 32 per round -- and the warp walks the home
 // atoms two at a time with packed FP32 pair arithmetic (f32x2: the same IEEE
@@ -1268,19 +987,32 @@ __device__ __forceinline__ double f2d_exact(float x) {
   return __hiloint2double(int(hi), int((u & 0x7u) << 29));
 }
 
-template <typename TI, int SM>
+// BATCH (masks only): the cells of the systems flagged in sys_sym, each warp
+// with its home cell's system geometry in shared memory, slots and original
+// indices offset to the launch's; a system with a crowded cell sets its
+// sys_fail, and the per-cell pass then counts all of it.  A batch keeps an
+// atom's mask words at the start of its own list region.
+template <typename TI, int SM, bool BATCH = false>
 __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(PairArgs<TI> A) {
   constexpr bool kMask = SM == kSymMasks || SM == kSymMasksFix;  // neighbour masks written
+  static_assert(!BATCH || SM == kSymMasks, "batches take the mask variant only");
   __shared__ SCSmem sm[kSCWarps];
+  __shared__ Geometry geo_w[BATCH ? kSCWarps : 1];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   SCSmem& W = sm[warp];
-  const Geometry& g = A.g;
-  const int nat = g.nat;
-  const float lo = g.lo, hi = g.hi;
+  const Geometry& g = BATCH ? geo_w[warp] : A.g;
+  const int nat = BATCH ? A.nat_total : A.g.nat;  // bound of sorted slots and original indices
+  float lo = A.g.lo, hi = A.g.hi;
+  // batches: the home cell's system, its first slot / original atom and the
+  // index of its cell 0 in cell_offsets (zero for a single system)
+  int sys = 0, abase = 0, coff = 0, cur_sys = -1;
   const float inf = __int_as_float(0x7f800000), nan = __int_as_float(0x7fc00000);
   unsigned rechecks = 0;
   if (A.cap_rec && blockIdx.x == 0 && threadIdx.x == 0) *A.cap_rec = A.list_cap;
   unsigned* masks = reinterpret_cast<unsigned*>(A.lists);
+  auto mrow = [&](long long slot) -> unsigned* {  // the mask words of a sorted slot
+    return BATCH ? reinterpret_cast<unsigned*>(A.lists + slot * A.list_cap) : masks + kMaskStride * slot;
+  };
   const int nwarps = gridDim.x * kSCWarps;
   // stencil cell q = lane of home cell h: sorted range, loop-shift base, FP32 corner offset
   struct St {
@@ -1294,30 +1026,68 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
     s.slp = 0;
     s.ox = s.oy = s.oz = 0.f;
     if (h < A.ncells_total && lane < 27) {
-      const int c0 = h % g.ns[0] + 1, c1 = (h / g.ns[0]) % g.ns[1] + 1, c2 = h / (g.ns[0] * g.ns[1]) + 1;
+      const int hl = BATCH ? h - A.sys_cell[sys] : h;
+      const int c0 = hl % g.ns[0] + 1, c1 = (hl / g.ns[0]) % g.ns[1] + 1, c2 = hl / (g.ns[0] * g.ns[1]) + 1;
       s.lin = stencil_cell(g, nullptr, 0, 3, 3, c0, c1, c2, lane, s.slp, s.ox, s.oy, s.oz);
       if (s.lin >= 0) {
-        s.start = clampi(A.cell_offsets[s.lin] - 1, nat);
-        s.cnt = max(clampi(A.cell_offsets[s.lin + 1] - 1, nat) - s.start, 0);
+        s.start = clampi(A.cell_offsets[coff + s.lin] - 1 + abase, nat);
+        s.cnt = max(clampi(A.cell_offsets[coff + s.lin + 1] - 1 + abase, nat) - s.start, 0);
       }
     }
   };
   int h = blockIdx.x * kSCWarps + warp;
   St cur;
-  stencil(h, cur);
+  if (!BATCH) stencil(h, cur);
   for (; h < A.ncells_total; h += nwarps) {
     St nxt;
-    stencil(h + nwarps, nxt);  // the next cell's ranges are loaded while this one is screened
+    if constexpr (BATCH) {
+      sys = clampi(A.cell_sys[h], A.nsys - 1);
+      if (!A.sys_sym[sys]) continue;
+      if (sys != cur_sys) {
+        __syncwarp();
+        const int* src = reinterpret_cast<const int*>(A.geo + sys);
+        int* dst = reinterpret_cast<int*>(&geo_w[warp]);
+        for (int k = lane; k < int(sizeof(Geometry) / 4); k += 32) dst[k] = src[k];
+        __syncwarp();
+        cur_sys = sys;
+      }
+      abase = A.sys_atom[sys];
+      coff = A.sys_cell[sys] + sys;
+      lo = g.lo;
+      hi = g.hi;
+      stencil(h, cur);
+    } else {
+      stencil(h + nwarps, nxt);  // the next cell's ranges are loaded while this one is screened
+    }
     const int hs = __shfl_sync(0xffffffffu, cur.start, 13), nb = __shfl_sync(0xffffffffu, cur.cnt, 13);
     if (nb > 32 || __any_sync(0xffffffffu, cur.cnt > 32)) {
-      if (lane == 0) atomicOr(A.sym_fail, 1);  // a crowded cell: the per-cell pass with lists counts instead
+      // a crowded cell: the per-cell pass with lists counts instead
+      if constexpr (BATCH) {
+        // the first warp to fail the system appends its cells and slot
+        // chunks to the lists the per-cell passes walk
+        int first = 0;
+        if (lane == 0) first = atomicExch(A.sys_fail + sys, 1) == 0;
+        if (__shfl_sync(0xffffffffu, first, 0)) {
+          const int c0 = A.sys_cell[sys], nc = A.sys_cell[sys + 1] - c0;
+          int base = 0;
+          if (lane == 0) base = atomicAdd(A.extra_cells, nc);
+          base = __shfl_sync(0xffffffffu, base, 0);
+          for (int c = lane; c < nc; c += 32) A.nonsym_cells[A.n_nonsym_cells + base + c] = c0 + c;
+          const int a0 = A.sys_atom[sys] & ~31, nch = (A.sys_atom[sys + 1] - a0 + 31) >> 5;
+          if (lane == 0) base = atomicAdd(A.extra_chunks, nch);
+          base = __shfl_sync(0xffffffffu, base, 0);
+          for (int k = lane; k < nch; k += 32) A.nonsym_chunks[A.n_nonsym_chunks + base + k] = a0 + 32 * k;
+        }
+      } else if (lane == 0) {
+        atomicOr(A.sym_fail, 1);
+      }
     } else if (nb > 0) {
       // words q < 13 of the home atoms that no other warp writes: their cell is empty or outside
       const unsigned zq = kMask ? __ballot_sync(0xffffffffu, lane < 13 && (cur.lin < 0 || cur.cnt == 0)) : 0u;
       if (zq)
         for (int t = lane; t < nb * 13; t += 32) {
           const int a = t / 13, q = t - 13 * a;
-          if ((zq >> q) & 1u) masks[kMaskStride * (hs + a) + q] = 0u;
+          if ((zq >> q) & 1u) mrow(hs + a)[q] = 0u;
         }
       unsigned hm = kPlainMeta;
       {
@@ -1328,7 +1098,7 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
           y = r.y;
           z = r.z;
           hm = __float_as_uint(r.w);
-          const int o = clampi(A.perm[hs + lane] - 1, nat - 1);
+          const int o = clampi(A.perm[hs + lane] - 1 + abase, nat - 1);
           W.horig[lane] = o;
           const double X0 = A.Xs[3LL * (hs + lane) + 0], X1 = A.Xs[3LL * (hs + lane) + 1],
                        X2 = A.Xs[3LL * (hs + lane) + 2];
@@ -1338,7 +1108,7 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
             xp.x = X0;
             xp.y = X1;
             xp.z = X2;
-            xp.perm = o + 1;
+            xp.perm = o + 1 - abase;  // j of the pair (system-local in a batch)
             xp.meta = hm;
             st_keep(A.xpk + hs + lane, xp, l2_keep_policy());
             const long long nz = (long long)0x8000000000000000ULL;
@@ -1400,7 +1170,7 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
         // (r2 = +inf against every home atom, +inf ones included: never accepted or rechecked)
         const float cx = !valid ? -inf : ex ? nan : r.x + qx, cy = !valid ? -inf : ex ? nan : r.y + qy,
                     cz = !valid ? -inf : ex ? nan : r.z + qz;
-        const int corig = clampi(A.perm[slot] - 1, nat - 1);
+        const int corig = clampi(A.perm[slot] - 1 + abase, nat - 1);
 #if NL_SC_PACKED
         const unsigned long long px = f2pack(cx, cx), py = f2pack(cy, cy), pz = f2pack(cz, cz);
 #endif
@@ -1482,7 +1252,7 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
         }
         if constexpr (kMask) {
           if (valid && fwd) {  // the candidate's word for its mirrored cell
-            masks[kMaskStride * slot + (26 - qq)] = col;
+            mrow(slot)[26 - qq] = col;
             if (col) atomicAdd(A.counts + corig, __popc(col));
           }
         } else {
@@ -1511,7 +1281,7 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
             w = __funnelshift_r(W.B[a][off >> 5], W.B[a][(off >> 5) + 1], off & 31);
             if (cnt < 32) w &= (1u << cnt) - 1u;
           }
-          masks[kMaskStride * (hs + a) + 13 + k] = w;
+          mrow(hs + a)[13 + k] = w;
           if (w) atomicAdd(&W.hcnt[a], __popc(w));
         }
       }
@@ -1520,7 +1290,7 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
       __syncwarp();
       }
     }
-    cur = nxt;
+    if constexpr (!BATCH) cur = nxt;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) rechecks += __shfl_xor_sync(0xffffffffu, rechecks, o);
@@ -1556,45 +1326,21 @@ struct __align__(16) EmitAtoms {
   unsigned mi[32];      // packed windings | exact bit
   int n[32];            // listed pairs (0 when written by the screening pass)
   int sys[32];          // batch: system of the slot
-  int cell[32];         // neighbour masks: 0-based home cell of the slot (batches: the cell's first slot)
-  unsigned char qmap[32];  // neighbour masks: stencil cell of the k-th non-empty mask word
 };
 
-// k-th (0-based) set bit of m (m has more than k set bits)
-__device__ __forceinline__ int kth_bit(unsigned m, int k) {
-  int pos = 0;
-#pragma unroll
-  for (int w = 16; w > 0; w >>= 1) {
-    const int c = __popc(m & ((1u << w) - 1u));
-    if (c <= k) {
-      k -= c;
-      m >>= w;
-      pos += w;
-    }
-  }
-  return pos;
-}
-
-// MASKS: the pairs come from the symmetric count pass's neighbour masks
-// instead of lists (both variants are launched; for a single system the
-// count's record in the workspace selects one, in a batch each takes the
-// atoms of its systems); lane r of a pass finds the atom's r-th pair from the
-// prefix counts of its 27 mask words (stencil order, then sorted order in the
-// cell), so the output order is the same.  Atoms of more than list_cap pairs
-// are left to the screening write pass (their cells are listed here).
-#ifndef NL_EMIT_MASK_MIN_BLOCKS
-#define NL_EMIT_MASK_MIN_BLOCKS 6  // resident blocks per SM the mask variant is compiled for
-#endif
+// The atoms whose pairs the per-cell count pass listed: a single system's
+// when the symmetric pass gave up (or did not apply), a batch's in the
+// systems the symmetric pass did not count.  Atoms of more than list_cap
+// pairs are left to the screening write pass.
 #ifndef NL_EMIT_BATCH_MIN_BLOCKS
-#define NL_EMIT_BATCH_MIN_BLOCKS 6  // likewise, the list variant for batches (4.94 -> 4.85 ms per 4,096 systems against 8)
+#define NL_EMIT_BATCH_MIN_BLOCKS 6  // the batch variant (4.94 -> 4.85 ms per 4,096 systems against 8)
 #endif
-template <typename TI, bool BATCH, bool MASKS>
-__global__ void __launch_bounds__(kEmitWarps * 32,
-                                  MASKS ? NL_EMIT_MASK_MIN_BLOCKS : (BATCH ? NL_EMIT_BATCH_MIN_BLOCKS : kEmitMinBlocks))
+template <typename TI, bool BATCH>
+__global__ void __launch_bounds__(kEmitWarps * 32, BATCH ? NL_EMIT_BATCH_MIN_BLOCKS : kEmitMinBlocks)
     k_emit(PairArgs<TI> A) {
   // the count recorded its choice in the workspace: sym_fail == 0 after a
-  // successful symmetric count (masks), non-zero otherwise (lists)
-  if (!BATCH && ((*A.sym_fail == 0) != MASKS)) return;
+  // successful symmetric count (the mask write pass), non-zero otherwise
+  if (!BATCH && *A.sym_fail == 0) return;
   __shared__ EmitAtoms ea[kEmitWarps];
   __shared__ double cs_blk[BATCH ? 1 : 3 * kCsN * kCsN * kCsN];
   if (!BATCH) {
@@ -1604,17 +1350,21 @@ __global__ void __launch_bounds__(kEmitWarps * 32,
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   EmitAtoms& E = ea[warp];
   const int K = A.list_cap;
-  // no atom has a winding (single systems record it): candidate words need no record
-  const bool plain = MASKS && !BATCH && *A.sym_wound == 0;
   const long long nwarps = (long long)gridDim.x * kEmitWarps;
   // batches: the next 32 atoms from a counter as warps free up (uneven pair
   // counts); single systems: a grid stride
-  unsigned* ework = BATCH ? reinterpret_cast<unsigned*>(A.work) + (MASKS ? 3 : 2) : nullptr;
+  unsigned* ework = BATCH ? reinterpret_cast<unsigned*>(A.work) + 2 : nullptr;
+  // with the symmetric pass, only the chunks of the systems it did not take
+  // or that failed it (a chunk met twice is written twice with the same values)
+  const bool nonsym = BATCH && A.sym && A.nonsym_chunks;
+  const unsigned nchunks = nonsym ? unsigned(A.n_nonsym_chunks + *A.extra_chunks) : 0u;
   auto next_c0 = [&](long long cur) -> long long {
     if (!BATCH) return cur + nwarps * 32;
     unsigned b = 0;
-    if (lane == 0) b = atomicAdd(ework, 32u);
-    return (long long)__shfl_sync(0xffffffffu, b, 0);
+    if (lane == 0) b = atomicAdd(ework, nonsym ? 1u : 32u);
+    b = __shfl_sync(0xffffffffu, b, 0);
+    if (!nonsym) return (long long)b;
+    return b < nchunks ? (long long)A.nonsym_chunks[b] : A.nat_total;
   };
   for (long long c0 = BATCH ? next_c0(0) : ((long long)blockIdx.x * kEmitWarps + warp) * 32; c0 < A.nat_total;
        c0 = next_c0(c0)) {
@@ -1624,37 +1374,10 @@ __global__ void __launch_bounds__(kEmitWarps * 32,
       const int slot = int(c0) + lane;
       const int sys = BATCH ? clampi(A.cell_sys[clampi(A.scell[slot], A.ncells_total - 1)], A.nsys - 1) : 0;
       E.sys[lane] = sys;
-      // batches: the mask variant writes the atoms of the systems the
-      // symmetric pass counted, the list variant the others
-      const bool own = !BATCH || ((A.sym && A.sys_sym[sys] && !A.sys_fail[sys]) == MASKS);
+      // batches: the atoms of the systems the symmetric pass did not count
+      const bool own = !BATCH || !(A.sym && A.sys_sym[sys] && !A.sys_fail[sys]);
       if (!own) {
-        E.n[lane] = 0;
-      } else if (MASKS) {
-        const unsigned* mw = sym_word<TI, BATCH>(A, slot);
-        int n = 0;
-#pragma unroll
-        for (int q = 0; q < 27; ++q) n += __popc(mw[q]);
-        const int hl = clampi(A.scell[slot], A.ncells_total - 1);
-        int abase = 0;
-        if (BATCH) {  // the home cell's first slot holds its stencil table
-          abase = A.sys_atom[sys];
-          const int coff = A.sys_cell[sys] + sys;
-          E.cell[lane] = clampi(A.cell_offsets[coff + hl - A.sys_cell[sys]] - 1 + abase, A.nat_total - 1);
-        } else {
-          E.cell[lane] = hl;
-        }
-        E.n[lane] = n > K ? 0 : n;
-        if (n > K && atomicExch(A.cell_flag + hl, 1) == 0) {  // the screening write pass takes the cell
-          const int u = atomicAdd(A.n_screen_cells, 1);
-          if (u < A.ncells_total) A.screen_cells[u] = hl;
-        }
-        const int orig = clampi(abase + A.perm[slot] - 1, A.nat_total - 1);
-        E.base[lane] = (long long)A.first[orig] - 1;
-        if ((long long)A.first[orig + 1] - 1 - E.base[lane] != n) {  // counts and masks disagree
-          atomicOr(A.err, kFlagInconsistent);
-          E.n[lane] = 0;
-        }
-      } else {
+        E.n[lane] = 0;      } else {
         int n = A.lcount[slot];
         E.n[lane] = n > K ? 0 : n;  // overflowed atoms belong to the screening pass
         E.base[lane] = (long long)A.first[clampi(A.sorig[slot], A.nat_total - 1)] - 1;
@@ -1735,8 +1458,6 @@ __global__ void __launch_bounds__(kEmitWarps * 32,
         uint2 e;
         int a, r;
         bool v;
-        unsigned m, slp;  // masks: this lane's mask word and stencil cell of the pass's atom
-        int st;
       };
       struct StG {
         double x0, x1, x2;
@@ -1751,59 +1472,19 @@ __global__ void __launch_bounds__(kEmitWarps * 32,
           const unsigned pd = E.pass[h];
           t.a = int(pd >> 8);
           t.r = 32 * int(pd & 255u) + lane;
-          if (MASKS) {
-            // the mask word and the stencil cell of lane `lane`; decoded in the gather stage
-            const unsigned* tab = sym_table<TI, BATCH>(A, E.cell[t.a], E.cell[t.a]);
-            t.st = lane < 27 ? int(tab[lane]) : 0;
-            t.slp = lane < 27 ? tab[27 + lane] : 0u;
-            t.m = lane < 27 ? __ldcs(sym_word<TI, BATCH>(A, c0 + t.a) + lane) : 0u;
-          } else {
-            t.e = __ldcs(A.lists + (c0 + t.a) * K + min(t.r, E.n[t.a] - 1));  // read once
-          }
+          t.e = __ldcs(A.lists + (c0 + t.a) * K + min(t.r, E.n[t.a] - 1));  // read once
         }
       };
       auto stage_g = [&](const StE& t, StG& u) {
         u.v = t.v;
         if (u.v) {
-          uint2 e = t.e;
-          if (MASKS) {
-            // lane r takes the atom's r-th pair.  Lane q holds mask word q
-            // (c_q pairs); its pairs are r in [ex_q, ex_q + c_q).  ex_q by
-            // bit-sliced ballots (c_q <= 32); the pass covers r in
-            // [base, base + 32): the non-empty runs starting before base are
-            // counted by a ballot, those starting in the window form a bit
-            // set, so the run of r is a popcount; its stencil cell comes from
-            // qmap, then the k-th atom of that cell's mask.
-            const unsigned lt = lt_mask();
-            const int c = __popc(t.m);
-            int ex = 0;
-#pragma unroll
-            for (int b = 0; b < 6; ++b) ex += __popc(__ballot_sync(0xffffffffu, (c >> b) & 1) & lt) << b;
-            const unsigned ne = __ballot_sync(0xffffffffu, c != 0);
-            const int base = t.r - lane;  // the pass's first pair (a multiple of 32)
-            const unsigned before = __ballot_sync(0xffffffffu, c != 0 && ex < base);
-            const unsigned win = __reduce_or_sync(0xffffffffu, c && ex >= base && ex < base + 32 ? 1u << (ex - base) : 0u);
-            if (c) E.qmap[__popc(ne & lt)] = (unsigned char)lane;
-            __syncwarp();
-            const int r = min(t.r, E.n[t.a] - 1);  // base <= r < base + 32
-            const int j = __popc(before) + __popc(win & (0xffffffffu >> (31 - (r - base)))) - 1;
-            const int q = E.qmap[j];
-            __syncwarp();
-            const unsigned mq = __shfl_sync(0xffffffffu, t.m, q);
-            const int exq = __shfl_sync(0xffffffffu, ex, q);
-            const int stq = __shfl_sync(0xffffffffu, t.st, q);
-            const unsigned slq = __shfl_sync(0xffffffffu, t.slp, q);
-            e = make_uint2(unsigned(stq + kth_bit(mq, max(r - exq, 0))), slq);  // (slot of j, loop-shift base)
-          }
+          const uint2 e = t.e;
           const int slot_j = clampi(int(e.x), A.nat_total - 1);
           u.x0 = __ldg(A.Xs + 3LL * slot_j + 0);
           u.x1 = __ldg(A.Xs + 3LL * slot_j + 1);
           u.x2 = __ldg(A.Xs + 3LL * slot_j + 2);
           u.oj = (long long)__ldg(A.perm + slot_j);
-          if (MASKS)
-            u.cw = cand_word(e.y, plain ? kPlainMeta : __float_as_uint(__ldg(&A.rec[slot_j].w)));
-          else
-            u.cw = e.y;
+          u.cw = e.y;
           u.a = t.a;
           u.r = t.r;
         }
@@ -1881,22 +1562,22 @@ __global__ void __launch_bounds__(kEmitWarps * 32,
 #ifndef NL_EO_PASSES
 #define NL_EO_PASSES 2  // passes whose gathers are in flight together
 #endif
-#ifndef NL_EO_PLANES
-#define NL_EO_PLANES 0  // 1: masks and cell starts loaded one stencil plane at a time (fewer registers)
-#endif
 constexpr int kEOWarps = 2;
-constexpr int kEOEnt = 1024;  // pair entries per warp
+constexpr int kEOEnt = 1024;  // pair entries per warp (896 with the C'S table read through L1: slower)
 constexpr int kEOPasses = NL_EO_PASSES;
-static_assert(kEOEnt >= 27 * 32, "an atom of the symmetric pass has fewer than 27 * 32 pairs");
+static_assert(kEOEnt >= 27 * 32 + 32, "a chunk holds an atom of 27 * 32 pairs from any offset");
 
 template <typename TI>
 struct __align__(16) EOSmem {
   uint2 ent[kEOEnt];           // entry: (sorted slot of j, atom | loop shift + 1 per axis << 5 + 2k);
                                // while the masks are expanded also the listed words (word, cell start)
   unsigned char code[kEOEnt];  // loop-shift code (bits 5.. of an entry's second word) of a listed word
-  double xi[32][4];            // the batch's atoms: FP64 position (and padding)
+  double xi[32][4];            // the batch's atoms: FP64 position; [3]: batches' system and i
   unsigned mi[32];             //   record meta (windings, exact bit)
 };
+// (shared memory per block: 8 resident blocks of 23.7 KB leave the L1 60 KB
+// of the SM's 256 KB; 512 bytes more per block took it to 28 KB and the
+// write pass from 0.49 to 0.74 ms at 1M atoms)
 
 // The three cells c - 1, c, c + 1 along one axis (c 1-based): 0-based wrapped
 // index, loop shift and whether the cell exists (wrap_and_shift,
@@ -1927,29 +1608,49 @@ __device__ __forceinline__ void axis3(int c, int n, int pbc, int* w, int* s, boo
   }
 }
 
-template <typename TI>
+// BATCH: the atoms of the systems the symmetric pass counted (sys_sym set,
+// sys_fail clear), in the launch's original order; each lane looks up its
+// atom's system, and each pair takes its atom's system geometry and C'S
+// table; i and j are system-local.  The atoms of the other systems are left
+// to the list write pass (a warp's chunks are runs of this kernel's atoms).
+template <typename TI, bool BATCH = false>
 __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(PairArgs<TI> A) {
-  if (*A.sym_fail != 0) return;  // the count pass used lists: k_emit writes them
+  if (!BATCH && *A.sym_fail != 0) return;  // the count pass used lists: k_emit writes them
   __shared__ EOSmem<TI> sm[kEOWarps];
-  __shared__ double cs_blk[3 * kCsN * kCsN * kCsN];
-  const Geometry& g = A.g;
-  for (int t = threadIdx.x; t < 3 * kCsN * kCsN * kCsN; t += blockDim.x) cs_blk[t] = A.cs_table[t];
-  __syncthreads();
+  constexpr bool kCsSmem = !BATCH;
+  __shared__ double cs_blk[kCsSmem ? 3 * kCsN * kCsN * kCsN : 1];
+  const Geometry& g = A.g;  // single systems
+  if (kCsSmem) {
+    for (int t = threadIdx.x; t < 3 * kCsN * kCsN * kCsN; t += blockDim.x) cs_blk[t] = A.cs_table[t];
+    __syncthreads();
+  }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   EOSmem<TI>& E = sm[warp];
-  const int nat = g.nat;
+  const int nat = BATCH ? A.nat_total : A.g.nat;  // bound of sorted slots and original indices
   const int sw = *A.sym_wound;
   const bool plain = (sw & 1) == 0;   // no atom has a winding or is exact: S = the loop shift
   const bool negzero = (sw & 2) != 0;  // a coordinate is -0: R needs the signed-zero rule for S = 0
   const unsigned* masks = reinterpret_cast<const unsigned*>(A.lists);
   const long long cap = A.capacity;
-  const double* zc = cs_blk + 3 * ((kCsN * kCsN + kCsN + 1) * kCsR);  // C'(0,0,0): signed zeros
+  constexpr int kZc = 3 * ((kCsN * kCsN + kCsN + 1) * kCsR);  // C'(0,0,0) in a C'S table: signed zeros
   const unsigned long long keep = l2_keep_policy();
   unsigned bad = 0;  // error flags of this lane
   const long long nwarps = (long long)gridDim.x * kEOWarps;
   for (long long o0 = ((long long)blockIdx.x * kEOWarps + warp) * 32; o0 < nat; o0 += nwarps * 32) {
     const int na = int(min(32LL, nat - o0));
-    const bool own = lane < na;
+    bool own = lane < na;
+    int sy = 0;  // batches: the atom's system (the last one whose first atom is at or before it)
+    if (BATCH && own) {
+      const int o = int(o0) + lane;
+      int lo_s = 0, hi_s = A.nsys - 1;
+      while (lo_s < hi_s) {
+        const int mid = (lo_s + hi_s + 1) >> 1;
+        if (A.sys_atom[mid] <= o) lo_s = mid;
+        else hi_s = mid - 1;
+      }
+      sy = lo_s;
+      own = A.sys_sym[sy] && !A.sys_fail[sy];
+    }
     // ---- lane a: atom o0 + a.  Header and output range first ...
     int2 hd = make_int2(0, 0);
     long long f = 0, n = 0;
@@ -1959,16 +1660,36 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
       f = (long long)A.first[o] - 1;
       n = (long long)A.first[o + 1] - 1 - f;
     }
-    const int slot = clampi(hd.x, nat - 1), hc = clampi(hd.y, g.ncells - 1);
+    const int slot = clampi(hd.x, nat - 1);
+    // the home cell within its system, the system's grid, its cell 0 in
+    // cell_offsets and its first slot / original atom
+    int ns0 = g.ns[0], ns1 = g.ns[1], ns2 = g.ns[2], pb0 = g.pbc[0], pb1 = g.pbc[1], pb2 = g.pbc[2];
+    int coff = 0, abase = 0;
+    if (BATCH) {
+      const Geometry& gs = A.geo[sy];
+      ns0 = max(gs.ns[0], 1);
+      ns1 = max(gs.ns[1], 1);
+      ns2 = max(gs.ns[2], 1);
+      pb0 = gs.pbc[0];
+      pb1 = gs.pbc[1];
+      pb2 = gs.pbc[2];
+      coff = A.sys_cell[sy] + sy;
+      abase = A.sys_atom[sy];
+    }
+    const int hc = clampi(hd.y - (BATCH ? A.sys_cell[sy] : 0), ns0 * ns1 * ns2 - 1);
+    const unsigned ownm = __ballot_sync(0xffffffffu, own);
     // ---- chunks of at most kEOEnt pairs, cut at atom boundaries; each chunk
     // loads, expands and writes its own atoms, so that the masks and cell
     // starts held for the expansion are dead while the chunk is written
-    int l0 = 0;
+    // (chunks are runs of consecutive lanes of this kernel's atoms: all of
+    // them for a single system)
+    int l0 = ownm ? __ffs(ownm) - 1 : 32;
     while (l0 < na) {
       const long long G = __shfl_sync(0xffffffffu, f, l0);
       // (entries are stored from index G mod 32: kEOEnt - 32 pairs per chunk)
       const unsigned inch = __ballot_sync(0xffffffffu, lane >= l0 && own && f + n - G <= kEOEnt - 32);
-      const int l1 = l0 + __popc(inch >> l0);
+      const unsigned gap = ~(inch >> l0);
+      const int l1 = gap ? l0 + __ffs(gap) - 1 : 32;
       if (l1 == l0) {  // an atom with more pairs than its masks can hold: counts and masks disagree
         bad |= kFlagInconsistent;
         break;
@@ -1976,82 +1697,34 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
       const int cnt = int(__shfl_sync(0xffffffffu, f + n, l1 - 1) - G);
       const bool mine = lane >= l0 && lane < l1;
       {
-        int wx[3], wy[3], wz[3], sx[3], sy[3], sz[3];
+        int wx[3], wy[3], wz[3], sx[3], sy3[3], sz[3];
         bool okx[3], oky[3], okz[3];
-        axis3(hc % g.ns[0] + 1, g.ns[0], g.pbc[0], wx, sx, okx);
-        axis3((hc / g.ns[0]) % g.ns[1] + 1, g.ns[1], g.pbc[1], wy, sy, oky);
-        axis3(hc / (g.ns[0] * g.ns[1]) + 1, g.ns[2], g.pbc[2], wz, sz, okz);
-#if NL_EO_PLANES
-        if (mine) {
-          E.xi[lane][0] = A.Xs[3LL * slot + 0];
-          E.xi[lane][1] = A.Xs[3LL * slot + 1];
-          E.xi[lane][2] = A.Xs[3LL * slot + 2];
-          E.mi[lane] = __float_as_uint(A.rec[slot].w);
-        }
-        // ---- the lane's non-empty words, listed at the end of its stretch
-        // [e0, e0 + nn) of the table (each holds a bit: nnz <= nn), written
-        // from the last word down.  The mask words and cell starts are
-        // loaded one stencil plane (dz) at a time, so that at most one
-        // plane's nine words and starts are held at once.
-        const uint4* mrow = reinterpret_cast<const uint4*>(masks + kMaskStride * slot);
-        const int e0 = mine ? int(f - G) + int(G & 31) : 0;  // the entry of output position p sits at p - (G - G mod 32)
-        const int nn = mine ? int(n) : 0;
-        int nnz = 0, tot = 0;
-#pragma unroll
-        for (int dz = 2; dz >= 0; --dz) {
-          const int u0 = (9 * dz) >> 2;  // the 16-byte words holding mask words 9 dz .. 9 dz + 8
-          uint4 mv[3];
-#pragma unroll
-          for (int k = 0; k < 3; ++k) mv[k] = mine ? __ldg(mrow + u0 + k) : make_uint4(0u, 0u, 0u, 0u);
-          unsigned st[9];
-#pragma unroll
-          for (int dy = 0; dy < 3; ++dy) {
-            const int rb = g.ns[0] * (wy[dy] + g.ns[1] * wz[dz]);
-            const bool rok = mine && oky[dy] && okz[dz];
-#pragma unroll
-            for (int dx = 0; dx < 3; ++dx)
-              st[3 * dy + dx] = unsigned(clampi((rok && okx[dx] ? A.cell_offsets[rb + wx[dx]] : TI(1)) - 1, nat));
-          }
-#pragma unroll
-          for (int r = 8; r >= 0; --r) {
-            const int q = 9 * dz + r, dx = r % 3, dy = r / 3;
-            unsigned mq = (&mv[(q >> 2) - u0].x)[q & 3];
-            if (mq && !(okx[dx] && oky[dy] && okz[dz])) {  // a neighbour in a cell outside an open axis
-              bad |= kFlagInconsistent;
-              mq = 0u;
-            }
-            if (mq) {
-              if (nnz < nn && e0 >= 0) {
-                const int k = e0 + nn - 1 - nnz;
-                E.ent[k] = make_uint2(mq, st[r]);
-                E.code[k] = (unsigned char)(unsigned(sx[dx] + 1) | unsigned(sy[dy] + 1) << 2 | unsigned(sz[dz] + 1) << 4);
-              }
-              ++nnz;
-              tot += __popc(mq);
-            }
-          }
-        }
-#else
+        axis3(hc % ns0 + 1, ns0, pb0, wx, sx, okx);
+        axis3((hc / ns0) % ns1 + 1, ns1, pb1, wy, sy3, oky);
+        axis3(hc / (ns0 * ns1) + 1, ns2, pb2, wz, sz, okz);
         // masks, position, meta and the 27 stencil cell starts, all in flight together
         uint4 mv[7];
-        const uint4* mrow = reinterpret_cast<const uint4*>(masks + kMaskStride * slot);
+        const uint4* mrow = reinterpret_cast<const uint4*>(
+            BATCH ? reinterpret_cast<const unsigned*>(A.lists + (long long)slot * A.list_cap) : masks + kMaskStride * slot);
 #pragma unroll
         for (int k = 0; k < 7; ++k) mv[k] = mine ? ld_stream(mrow + k) : make_uint4(0u, 0u, 0u, 0u);
         unsigned st[27];
 #pragma unroll
         for (int r = 0; r < 9; ++r) {
           const int dy = r % 3, dz = r / 3;
-          const int rb = g.ns[0] * (wy[dy] + g.ns[1] * wz[dz]);
+          const int rb = coff + ns0 * (wy[dy] + ns1 * wz[dz]);
           const bool rok = mine && oky[dy] && okz[dz];
 #pragma unroll
           for (int dx = 0; dx < 3; ++dx)
-            st[3 * r + dx] = unsigned(clampi((rok && okx[dx] ? A.cell_offsets[rb + wx[dx]] : TI(1)) - 1, nat));
+            st[3 * r + dx] =
+                unsigned(clampi((rok && okx[dx] ? A.cell_offsets[rb + wx[dx]] : TI(1 - abase)) - 1 + abase, nat));
         }
         if (mine) {
           E.xi[lane][0] = A.Xs[3LL * slot + 0];
           E.xi[lane][1] = A.Xs[3LL * slot + 1];
           E.xi[lane][2] = A.Xs[3LL * slot + 2];
           E.mi[lane] = __float_as_uint(A.rec[slot].w);
+          if (BATCH) E.xi[lane][3] = __hiloint2double(sy, int(o0) + lane + 1 - abase);  // system, i
         }
         // ---- the lane's non-empty words, listed at the end of its stretch
         // [e0, e0 + nn) of the table (each holds a bit: nnz <= nn), written
@@ -2071,14 +1744,13 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
             if (nnz < nn && e0 >= 0) {
               const int k = e0 + nn - 1 - nnz;
               E.ent[k] = make_uint2(mq, st[q]);
-              E.code[k] = (unsigned char)(unsigned(sx[q % 3] + 1) | unsigned(sy[(q / 3) % 3] + 1) << 2 |
+              E.code[k] = (unsigned char)(unsigned(sx[q % 3] + 1) | unsigned(sy3[(q / 3) % 3] + 1) << 2 |
                                           unsigned(sz[q / 9] + 1) << 4);
             }
             ++nnz;
             tot += __popc(mq);
           }
         }
-#endif
         const bool lok = mine && tot == nn && e0 >= 0;
         if (mine && !lok) bad |= kFlagInconsistent;  // counts and masks disagree
         const int li = e0 + nn - nnz;  // the first listed word
@@ -2141,20 +1813,22 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
         const unsigned info = u.en.y;
         const int a = int(info & 31u);
         const double* xi = E.xi[a];
+        const int ps = BATCH ? __double2hiint(xi[3]) : 0;  // batches: the pair's system
+        const double* cst = BATCH ? A.cs_sys + (long long)kCsTableDoubles * ps : cs_blk;
         const double x0 = u.w0.x, x1 = u.w0.y, x2 = __hiloint2double(u.w1.y, u.w1.x);
         int S0 = int((info >> 5) & 3u) - 1, S1 = int((info >> 7) & 3u) - 1, S2 = int((info >> 9) & 3u) - 1;
         bool snz = (info & (63u << 5)) != (21u << 5);  // (S0, S1, S2) != 0: the codes are not 1, 1, 1
         if (!plain) {  // windings or exact atoms: S = s_loop + wi - wj
           const double xj[3] = {x0, x1, x2};
           int S[3];
-          pair_S(g, xi, xj, E.mi[a], cand_word(cand_base(S0, S1, S2), unsigned(u.w1.w)), S);
+          pair_S(BATCH ? A.geo[ps] : g, xi, xj, E.mi[a], cand_word(cand_base(S0, S1, S2), unsigned(u.w1.w)), S);
           S0 = S[0];
           S1 = S[1];
           S2 = S[2];
           snz = (S0 | S1 | S2) != 0;
         }
         if (act) {
-          __stcs(oi + k, TI(ti0 + a));
+          __stcs(oi + k, BATCH ? TI(__double2loint(xi[3])) : TI(ti0 + a));
           __stcs(oj + k, TI(u.w1.z));
           __stcs(oS + 3 * k + 0, TI(S0));
           __stcs(oS + 3 * k + 1, TI(S1));
@@ -2167,14 +1841,15 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
             if (nz) {
               double c0, c1, c2;
               if (abs(S0) <= kCsR && abs(S1) <= kCsR && abs(S2) <= kCsR) {
-                const double* tb = cs_blk + 3 * ((S0 + kCsR) + kCsN * ((S1 + kCsR) + kCsN * (S2 + kCsR)));
+                const double* tb = cst + 3 * ((S0 + kCsR) + kCsN * ((S1 + kCsR) + kCsN * (S2 + kCsR)));
                 c0 = tb[0];
                 c1 = tb[1];
                 c2 = tb[2];
               } else {
-                c0 = cts_k(g.C, S0, S1, S2, 0);
-                c1 = cts_k(g.C, S0, S1, S2, 1);
-                c2 = cts_k(g.C, S0, S1, S2, 2);
+                const double* C = BATCH ? A.geo[ps].C : g.C;
+                c0 = cts_k(C, S0, S1, S2, 0);
+                c1 = cts_k(C, S0, S1, S2, 1);
+                c2 = cts_k(C, S0, S1, S2, 2);
               }
               R0 = dadd(R0, c0);
               R1 = dadd(R1, c1);
@@ -2182,9 +1857,9 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
             }
           }
           if (negzero && !nz) {  // a -0 coordinate: RN(d + C'(0,0,0)) differs from d when d is -0
-            R0 = add_signed_zero(R0, zc[0]);
-            R1 = add_signed_zero(R1, zc[1]);
-            R2 = add_signed_zero(R2, zc[2]);
+            R0 = add_signed_zero(R0, cst[kZc + 0]);
+            R1 = add_signed_zero(R1, cst[kZc + 1]);
+            R2 = add_signed_zero(R2, cst[kZc + 2]);
           }
           if (act) {
             __stcs(oR + 3 * k + 0, R0);
@@ -2202,7 +1877,8 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
           if (t == 0 || j + t < npass) write(32 * (j + t) + lane, u[t]);
       }
       __syncwarp();
-      l0 = l1;
+      const unsigned rest = l1 < 32 ? ownm & (~0u << l1) : 0u;  // the next run of this kernel's atoms
+      l0 = rest ? __ffs(rest) - 1 : 32;
     }
   }
   if (bad) atomicOr(A.err, bad);
@@ -2787,19 +2463,18 @@ static void launch_modes(int mode, const PairArgs<TI>& a, int num_sms, cudaStrea
   switch (mode) {
     case kModeCount:
       if (a.sym) {  // symmetric pass; the per-cell pass below counts what it gave up (or left)
-        if (BATCH) {
-          long long sb = ((long long)a.ncells_total + kSymWarps - 1) / kSymWarps;
-          if (sb > (long long)num_sms * pbps) sb = (long long)num_sms * pbps;
-          k_pairs_sym<TI, BATCH><<<int(sb), kSymWarps * 32, 0, st>>>(a);
-        } else {
-          const int sbps = a.pair_blocks_per_sm > 0 ? a.pair_blocks_per_sm : 2 * NL_SC_MIN_BLOCKS;
-          long long sb = ((long long)a.ncells_total + kSCWarps - 1) / kSCWarps;
-          if (sb > (long long)num_sms * sbps) sb = (long long)num_sms * sbps;
-          k_sym_count<TI, kSymMasks><<<int(sb), kSCWarps * 32, 0, st>>>(a);
-        }
+        const int sbps = a.pair_blocks_per_sm > 0 ? a.pair_blocks_per_sm : 2 * NL_SC_MIN_BLOCKS;
+        long long sb = ((long long)a.ncells_total + kSCWarps - 1) / kSCWarps;
+        if (sb > (long long)num_sms * sbps) sb = (long long)num_sms * sbps;
+        k_sym_count<TI, kSymMasks, BATCH><<<int(sb), kSCWarps * 32, 0, st>>>(a);
       }
       if (a.count_kernel != 2) {  // default: one warp per home cell
         k_pairs<TI, kModeCount, BATCH><<<int(blocks), kPairWarps * 32, 0, st>>>(a);
+        if (BATCH && a.sym && a.nonsym_cells && a.rounds) {  // the rounds the first launch listed
+          PairArgs<TI> r = a;
+          r.round_pass = 1;
+          k_pairs<TI, kModeCount, BATCH><<<int(blocks), kPairWarps * 32, 0, st>>>(r);
+        }
       } else {
         const int cbps = a.pair_blocks_per_sm > 0 ? a.pair_blocks_per_sm : NL_COUNT_MIN_BLOCKS;
         long long cb = ((long long)a.nat_total + kCountThreads - 1) / kCountThreads;
@@ -2812,14 +2487,12 @@ static void launch_modes(int mode, const PairArgs<TI>& a, int num_sms, cudaStrea
       if (a.list_cap > 0) {
         long long eb = ((long long)a.nat_total + 32 * kEmitWarps - 1) / (32 * kEmitWarps);
         if (eb > (long long)num_sms * ebps) eb = (long long)num_sms * ebps;
-        k_emit<TI, BATCH, false><<<int(eb), kEmitWarps * 32, 0, st>>>(a);
-        if (!BATCH) {  // masks: written in original atom order
+        k_emit<TI, BATCH><<<int(eb), kEmitWarps * 32, 0, st>>>(a);
+        if (!BATCH || a.sym) {  // masks: written in original atom order
           const int obps = a.emit_blocks_per_sm > 0 ? a.emit_blocks_per_sm : 2 * NL_EO_MIN_BLOCKS;
           long long ob = ((long long)a.nat_total + 32 * kEOWarps - 1) / (32 * kEOWarps);
           if (ob > (long long)num_sms * obps) ob = (long long)num_sms * obps;
-          k_emit_orig<TI><<<int(ob), kEOWarps * 32, 0, st>>>(a);
-        } else if (a.sym) {
-          k_emit<TI, BATCH, true><<<int(eb), kEmitWarps * 32, 0, st>>>(a);
+          k_emit_orig<TI, BATCH><<<int(ob), kEOWarps * 32, 0, st>>>(a);
         }
       }
       k_pairs<TI, kModeFill, BATCH><<<int(blocks), kPairWarps * 32, 0, st>>>(a);

@@ -84,6 +84,22 @@ struct PairArgs {
   int emit_blocks_per_sm;   // launch tuning (0 = default): list write grid
   int vec_ok;               // S and R start on 16-byte boundaries: the write pass stores 16-byte vectors
   int* work;                // batch: cell counters of the count and screening passes (zeroed per call)
+  // batches with the symmetric pass: the cells and 32-slot chunks of the
+  // systems it does not take (n_nonsym_* of them, uploaded), then those of
+  // the systems that fail it, appended by the pass (extra_* counts them)
+  int* nonsym_cells;
+  int n_nonsym_cells;
+  int* nonsym_chunks;
+  int n_nonsym_chunks;
+  int* extra_cells;
+  int* extra_chunks;
+  // the count pass over those cells takes 32 home atoms of a cell at a time:
+  // a first launch takes each cell's first 32 and lists the rest in rounds
+  // (cell, round; n_rounds of them), a second (round_pass) takes the rounds
+  int2* rounds;
+  int* n_rounds;
+  int* round_work;
+  int round_pass;
   unsigned long long* stats;  // [0] += FP64 rechecks
   unsigned* err;
 };
