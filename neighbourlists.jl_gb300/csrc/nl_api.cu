@@ -187,7 +187,7 @@ struct Layout {
   size_t err, stats, pcount, st_pairs, cell_flag, pend, bcount, st_cells, cell_count, bend;
   size_t totals, cell_start, cid, ticket, rec, tmp, rec_sorted, scell, counts, lcount, sorig, hdr, xpk, cs_table,
       screen_cells,
-      big_list, base_end, lists, end;
+      big_list, base_end, stab, lists, end;
   bool use_lists = true;  // the workspace holds the pair lists (it reaches `end`)
 };
 
@@ -247,6 +247,8 @@ Layout layout(int64_t nat, int64_t ncells) {
   // the pair lists come last: a workspace that ends before them still runs
   // every call, with the screening write pass for every cell
   L.base_end = o;
+  L.stab = o;  // the symmetric pass's stencil table: 28 words per cell
+  o += up(sizeof(unsigned) * 28 * size_t(ncells > 0 ? ncells : 1));
   L.lists = o;
   o += up(sizeof(uint2) * size_t(nl::kListCap) * n);
   L.end = o;
@@ -415,6 +417,7 @@ nl::PairArgs<TI> pair_args(const nl::Geometry& g, const TI* cell_offsets, const 
   a.scell = at<int>(ws, L.scell);
   a.list_cap = L.use_lists ? nl::kListCap : 0;
   a.lists = L.use_lists ? at<uint2>(ws, L.lists) : nullptr;
+  a.stab = L.use_lists ? at<unsigned>(ws, L.stab) : nullptr;
   a.lcount = at<int>(ws, L.lcount);
   a.sorig = at<int>(ws, L.sorig);
   a.hdr = at<int2>(ws, L.hdr);

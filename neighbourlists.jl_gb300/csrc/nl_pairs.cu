@@ -887,9 +887,11 @@ constexpr unsigned kPlainMeta = (128u) | (128u << 10) | (128u << 20);
 // candidates and atoms beyond the home cell get infinite coordinates, so the
 // screen needs no masks; the home atom itself (its own candidate in the
 // centre) is taken out of its row afterwards.  The next cell's stencil ranges
-// are loaded one cell ahead.  The
-// write pass finds stencil cells from cell_offsets, so no per-cell stencil
-// table is written; each home atom's (sorted slot, home cell) goes to hdr,
+// are loaded one cell ahead.  The write pass finds stencil cells from
+// cell_offsets (a per-cell table of them was slower there: 0.492 against
+// 0.484 ms at 1M atoms), the lazy sum's pass from a 28-word table row per
+// home cell (first sorted slot of its 27 cells, their loop shifts; 0.711
+// against 0.762 ms); each home atom's (sorted slot, home cell) goes to hdr,
 // indexed by its original index, for the original-order write pass.  Mask
 // words are kMaskStride per atom (27 used) so that they load as 16-byte
 // vectors.
@@ -1035,6 +1037,9 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
       }
     }
   };
+  // (batches: a grid stride as well; runs of 8 consecutive cells per warp,
+  // with the next cell's ranges loaded ahead within a system, were slower:
+  // 1.20 against 0.99 ms per 4,096-system batch)
   int h = blockIdx.x * kSCWarps + warp;
   St cur;
   if (!BATCH) stencil(h, cur);
@@ -1082,6 +1087,23 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
         atomicOr(A.sym_fail, 1);
       }
     } else if (nb > 0) {
+      if constexpr (SM == kSymMasksFix) {
+        // the stencil table row of the home cell, read by the lazy sum's
+        // pass (k_lazy_rows): words q < 27 the first sorted slot of stencil cell q
+        // (~0 outside an open axis), word 27 the loop shift + 1 of the
+        // three cells along each axis (2 bits each: x at bit 0, y at 6, z at
+        // 12), taken from the cells (dx, 1, 1), (1, dy, 1), (1, 1, dz)
+        const int s0 = field10(cur.slp, 0) - 640 + 1, s1 = field10(cur.slp, 1) - 640 + 1,
+                  s2 = field10(cur.slp, 2) - 640 + 1;
+        unsigned part = 0u;
+        if (cur.lin >= 0) {
+          if (lane >= 12 && lane <= 14) part |= unsigned(s0 & 3) << (2 * (lane - 12));
+          if (lane == 10 || lane == 13 || lane == 16) part |= unsigned(s1 & 3) << (6 + 2 * ((lane - 10) / 3));
+          if (lane == 4 || lane == 13 || lane == 22) part |= unsigned(s2 & 3) << (12 + 2 * ((lane - 4) / 9));
+        }
+        const unsigned shifts = __reduce_or_sync(0xffffffffu, part);
+        if (lane < 28) A.stab[28LL * h + lane] = lane < 27 ? (cur.lin >= 0 ? unsigned(cur.start) : ~0u) : shifts;
+      }
       // words q < 13 of the home atoms that no other warp writes: their cell is empty or outside
       const unsigned zq = kMask ? __ballot_sync(0xffffffffu, lane < 13 && (cur.lin < 0 || cur.cnt == 0)) : 0u;
       if (zq)
@@ -1359,12 +1381,15 @@ __global__ void __launch_bounds__(kEmitWarps * 32, BATCH ? NL_EMIT_BATCH_MIN_BLO
   const bool nonsym = BATCH && A.sym && A.nonsym_chunks;
   const unsigned nchunks = nonsym ? unsigned(A.n_nonsym_chunks + *A.extra_chunks) : 0u;
   auto next_c0 = [&](long long cur) -> long long {
-    if (!BATCH) return cur + nwarps * 32;
-    unsigned b = 0;
-    if (lane == 0) b = atomicAdd(ework, nonsym ? 1u : 32u);
-    b = __shfl_sync(0xffffffffu, b, 0);
-    if (!nonsym) return (long long)b;
-    return b < nchunks ? (long long)A.nonsym_chunks[b] : A.nat_total;
+    if constexpr (!BATCH) {
+      return cur + nwarps * 32;
+    } else {
+      unsigned b = 0;
+      if (lane == 0) b = atomicAdd(ework, nonsym ? 1u : 32u);
+      b = __shfl_sync(0xffffffffu, b, 0);
+      if (!nonsym) return (long long)b;
+      return b < nchunks ? (long long)A.nonsym_chunks[b] : A.nat_total;
+    }
   };
   for (long long c0 = BATCH ? next_c0(0) : ((long long)blockIdx.x * kEmitWarps + warp) * 32; c0 < A.nat_total;
        c0 = next_c0(c0)) {
@@ -1948,13 +1973,13 @@ template <typename TI>
 __global__ void __launch_bounds__(kLRWarps * 32, NL_LR_MIN_BLOCKS) k_lazy_rows(PairArgs<TI> A) {
   if (*A.sym_fail != 0) return;  // a crowded cell: the per-cell passes sum instead
   __shared__ LRSmem sm[kLRWarps];
-  __shared__ double cs_blk[3 * kCsN * kCsN * kCsN];
+  // the FP64 C'S table (only the FP64 pairs read it) through L1, the fixed-point
+  // one in shared memory (0.762 against 0.766 ms with both in shared memory)
+  const double* cs_blk = A.cs_table;
   __shared__ unsigned long long cs_fix[3 * kCsN * kCsN * kCsN];
   const Geometry& g = A.g;
   for (int t = threadIdx.x; t < 3 * kCsN * kCsN * kCsN; t += blockDim.x) {
-    const double c = A.cs_table[t];
-    cs_blk[t] = c;
-    cs_fix[t] = fix_mod(c);
+    cs_fix[t] = fix_mod(A.cs_table[t]);
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1979,32 +2004,28 @@ __global__ void __launch_bounds__(kLRWarps * 32, NL_LR_MIN_BLOCKS) k_lazy_rows(P
     int n = 0;        // the atom's pairs
     unsigned ne = 0;  // its non-empty words
     {
-      int wx[3], wy[3], wz[3], sx[3], sy[3], sz[3];
-      bool okx[3], oky[3], okz[3];
-      axis3(hc % g.ns[0] + 1, g.ns[0], g.pbc[0], wx, sx, okx);
-      axis3((hc / g.ns[0]) % g.ns[1] + 1, g.ns[1], g.pbc[1], wy, sy, oky);
-      axis3(hc / (g.ns[0] * g.ns[1]) + 1, g.ns[2], g.pbc[2], wz, sz, okz);
-      uint4 mv[7];
+      // the masks and the home cell's stencil table row (first slot of each
+      // stencil cell, ~0 outside an open axis; loop shifts per axis)
+      uint4 mv[7], sv[7];
       const uint4* mrow = reinterpret_cast<const uint4*>(masks + kMaskStride * slot);
+      const uint4* srow = reinterpret_cast<const uint4*>(A.stab + 28LL * hc);
 #pragma unroll
-      for (int k = 0; k < 7; ++k) mv[k] = own ? ld_stream(mrow + k) : make_uint4(0u, 0u, 0u, 0u);
+      for (int k = 0; k < 7; ++k) {
+        mv[k] = own ? ld_stream(mrow + k) : make_uint4(0u, 0u, 0u, 0u);
+        sv[k] = own ? __ldg(srow + k) : make_uint4(0u, 0u, 0u, 0u);
+      }
+      const unsigned shw = sv[6].w;
 #pragma unroll
-      for (int r = 0; r < 9; ++r) {
-        const int dy = r % 3, dz = r / 3;
-        const int rb = g.ns[0] * (wy[dy] + g.ns[1] * wz[dz]);
-        const bool rok = own && oky[dy] && okz[dz];
-#pragma unroll
-        for (int dx = 0; dx < 3; ++dx) {
-          const int q = 3 * r + dx;
-          wst[q] = unsigned(clampi((rok && okx[dx] ? A.cell_offsets[rb + wx[dx]] : TI(1)) - 1, nat));
-          wcd[q] = (unsigned char)(unsigned(sx[dx] + 1) | unsigned(sy[dy] + 1) << 2 | unsigned(sz[dz] + 1) << 4);
-        }
+      for (int q = 0; q < 27; ++q) {
+        wst[q] = min((&sv[q >> 2].x)[q & 3], unsigned(nat));
+        wcd[q] = (unsigned char)(((shw >> (2 * (q % 3))) & 3u) | ((shw >> (6 + 2 * ((q / 3) % 3))) & 3u) << 2 |
+                                 ((shw >> (12 + 2 * (q / 9))) & 3u) << 4);
       }
       const int me = slot - int(wst[13]);  // the atom's place in its own cell (bit of the centre word)
 #pragma unroll
       for (int q = 0; q < 27; ++q) {
         unsigned mq = (&mv[q >> 2].x)[q & 3];
-        if (mq && !(okx[q % 3] && oky[(q / 3) % 3] && okz[q / 9])) {  // a neighbour in a cell outside an open axis
+        if (mq && wst[q] == unsigned(nat)) {  // a neighbour in a cell outside an open axis
           bad |= kFlagInconsistent;
           mq = 0u;
         }

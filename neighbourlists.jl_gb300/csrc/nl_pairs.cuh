@@ -83,6 +83,7 @@ struct PairArgs {
   int pair_blocks_per_sm;   // launch tuning (0 = default): count / screening grids
   int emit_blocks_per_sm;   // launch tuning (0 = default): list write grid
   int vec_ok;               // S and R start on 16-byte boundaries: the write pass stores 16-byte vectors
+  unsigned* stab;           // stencil table: 28 words per cell (symmetric pass -> mask write passes)
   int* work;                // batch: cell counters of the count and screening passes (zeroed per call)
   // batches with the symmetric pass: the cells and 32-slot chunks of the
   // systems it does not take (n_nonsym_* of them, uploaded), then those of
