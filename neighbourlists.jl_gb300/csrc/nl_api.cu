@@ -238,8 +238,8 @@ Layout layout(int64_t nat, int64_t ncells) {
   o += up(sizeof(int2) * n);
   L.xpk = o;
   o += up(sizeof(nl::XPack) * n);
-  L.cs_table = o;
-  o += up(sizeof(double) * 3 * 125);
+  L.cs_table = o;  // C'S for |S_k| <= 2 in FP64, then (lazy sums) in the positions' fixed point
+  o += up(sizeof(double) * 2 * 3 * 125);
   L.screen_cells = o;
   o += up(sizeof(int) * size_t(ncells > 0 ? ncells : 1));
   L.big_list = o;

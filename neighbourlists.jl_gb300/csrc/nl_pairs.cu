@@ -1950,9 +1950,15 @@ struct LRSmem {
 // 2^11 A), so only C'S modulo 2^12 A matters (2^12 * 2^52 = 2^64); the
 // remainder is exact in FP64 and scaled into [-2^63, 2^63).
 __device__ __forceinline__ unsigned long long fix_mod(double c) {
+  if (fabs(c) < 2048.0) return (unsigned long long)__double2ll_rn(dmul(c, kFixScale));  // no reduction needed
   double r = remainder(c, 4096.0);  // exact, in [-2048, 2048]
   if (r >= 2048.0) r -= 4096.0;
   return (unsigned long long)__double2ll_rn(dmul(r, kFixScale));
+}
+
+// The C'S table in the fixed point (after the FP64 one in the workspace), once per call.
+__global__ void k_cs_fix(const double* __restrict__ cs, unsigned long long* __restrict__ out) {
+  for (int t = threadIdx.x; t < 3 * kCsN * kCsN * kCsN; t += blockDim.x) out[t] = fix_mod(cs[t]);
 }
 
 // v * 2^-52 (v a fixed-point value of magnitude below 2^63) as a double-float:
@@ -1978,9 +1984,8 @@ __global__ void __launch_bounds__(kLRWarps * 32, NL_LR_MIN_BLOCKS) k_lazy_rows(P
   const double* cs_blk = A.cs_table;
   __shared__ unsigned long long cs_fix[3 * kCsN * kCsN * kCsN];
   const Geometry& g = A.g;
-  for (int t = threadIdx.x; t < 3 * kCsN * kCsN * kCsN; t += blockDim.x) {
-    cs_fix[t] = fix_mod(A.cs_table[t]);
-  }
+  const unsigned long long* cs_fix_g = reinterpret_cast<const unsigned long long*>(A.cs_table + kCsTableDoubles);
+  for (int t = threadIdx.x; t < 3 * kCsN * kCsN * kCsN; t += blockDim.x) cs_fix[t] = cs_fix_g[t];
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   LRSmem& W = sm[warp];
@@ -2541,6 +2546,7 @@ void launch_sym_lazy(int what, const PairArgs<TI>& a, int num_sms, cudaStream_t 
     k_sym_count<TI, kSymCounts><<<int(sb), kSCWarps * 32, 0, st>>>(a);
   } else {
     k_cs_table<<<1, 128, 0, st>>>(a.g, a.cs_table, nullptr, 0, a.err);
+    k_cs_fix<<<1, 128, 0, st>>>(a.cs_table, reinterpret_cast<unsigned long long*>(a.cs_table + kCsTableDoubles));
     // the neighbour masks with fixed-point gather rows, then each atom's sum from its masks
     k_sym_count<TI, kSymMasksFix><<<int(sb), kSCWarps * 32, 0, st>>>(a);
     long long lb = ((long long)a.nat_total + 32 * kLRWarps - 1) / (32 * kLRWarps);
