@@ -1000,6 +1000,9 @@ int batch_impl32(const nl_batch& b, const float* X, TI* perm, float* Xs, TI* cel
   a.sys_cell = si.cell0;
   a.cell_sys = at<int>(ws, b.B.cell_sys);
   a.work = at<int>(ws, L.pcount) + 12;  // zeroed with the workspace's first region
+  a.rounds = at<int2>(ws, b.B.rounds);
+  a.n_rounds = at<int>(ws, L.pcount) + 3;    // likewise
+  a.round_work = at<int>(ws, L.pcount) + 9;  // likewise (two counters)
   a.nsys = b.nsys;
   a.nat_total = na;
   a.ncells_total = nc;

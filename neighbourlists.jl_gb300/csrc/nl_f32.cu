@@ -190,15 +190,22 @@ __global__ void __launch_bounds__(kW32Warps * 32, FILL ? NL_F32_MIN_FILL : NL_F3
   const int ncells = BATCH ? a.ncells_total : g.ncells;
   int cur_sys = -1, abase = 0, coff = 0;
 
-  // batches: the next cell from a counter as warps free up (uneven cells)
+  // batches: the next cell (second launch: the next listed round) from a
+  // counter as warps free up (uneven cells)
+  const bool split = BATCH && a.rounds;
+  const bool rpass = split && a.round_pass;
+  const int rcap = a.nat_total / 32 + 2;  // rounds the list holds
+  const int niter = rpass ? min(*a.n_rounds, rcap) : ncells;
+  int* ctr = rpass ? a.round_work + (FILL ? 1 : 0) : a.work + (FILL ? 1 : 0);
   auto next_cell = [&](int cur) -> int {
     if (!BATCH) return cur + nwarps;
     int b = 0;
-    if (lane == 0) b = atomicAdd(a.work + (FILL ? 1 : 0), 1);
+    if (lane == 0) b = atomicAdd(ctr, 1);
     return __shfl_sync(0xffffffffu, b, 0);
   };
-  for (int cell = BATCH ? next_cell(0) : blockIdx.x * kW32Warps + (threadIdx.x >> 5); cell < ncells;
-       cell = next_cell(cell)) {
+  for (int idx = BATCH ? next_cell(0) : blockIdx.x * kW32Warps + (threadIdx.x >> 5); idx < niter;
+       idx = next_cell(idx)) {
+    const int cell = rpass ? max(min(a.rounds[idx].x, ncells - 1), 0) : idx;
     int hl = cell;  // the cell within its system
     if constexpr (BATCH) {
       const int sys = max(min(a.cell_sys[cell], a.nsys - 1), 0);
@@ -220,7 +227,22 @@ __global__ void __launch_bounds__(kW32Warps * 32, FILL ? NL_F32_MIN_FILL : NL_F3
     const int hs = int(a.cell_offsets[coff + hl]) - 1 + abase, he = int(a.cell_offsets[coff + hl + 1]) - 1 + abase;
     if (hs >= he) continue;
     const int ci[3] = {hl % g.ns[0] + 1, (hl / g.ns[0]) % g.ns[1] + 1, hl / (g.ns[0] * g.ns[1]) + 1};
-    for (int h0 = hs; h0 < he; h0 += 32) {
+    int hb0 = hs, hb1 = he;  // the home atoms this warp takes
+    if (rpass) {
+      hb0 = min(hs + 32 * max(a.rounds[idx].y, 0), he);
+      hb1 = min(hb0 + 32, he);
+    } else if (split && he - hs > 32) {
+      hb1 = hs + 32;
+      if constexpr (!FILL) {  // the count pass lists the other rounds (the fill pass reads the same list)
+        const int nr = ((he - hs + 31) >> 5) - 1;
+        int base = 0;
+        if (lane == 0) base = atomicAdd(a.n_rounds, nr);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        for (int k = lane; k < nr; k += 32)
+          if (base + k < rcap) a.rounds[base + k] = make_int2(cell, k + 1);
+      }
+    }
+    for (int h0 = hb0; h0 < hb1; h0 += 32) {
       const int nh = min(32, he - h0);
       // this lane's home atom: running count (fill: write offset) and range
       int hcount = 0, hn = 0;
@@ -784,10 +806,15 @@ void launch_pairs32(bool fill, const Pairs32Args<TI>& a, int num_sms, cudaStream
   if (a.nsys > 0) {  // batches: the per-cell passes (count, then the screening fill)
     if (a.nat_total <= 0 || a.ncells_total <= 0) return;
     const int grid = grid_for(a.ncells_total, kW32Warps, num_sms * 12);
-    if (fill)
+    Pairs32Args<TI> r = a;
+    r.round_pass = 1;
+    if (fill) {
       k_pairs32<TI, true, true><<<grid, kW32Warps * 32, 0, st>>>(a);
-    else
+      if (a.rounds) k_pairs32<TI, true, true><<<grid, kW32Warps * 32, 0, st>>>(r);
+    } else {
       k_pairs32<TI, false, true><<<grid, kW32Warps * 32, 0, st>>>(a);
+      if (a.rounds) k_pairs32<TI, false, true><<<grid, kW32Warps * 32, 0, st>>>(r);
+    }
     return;
   }
   if (a.g.nat <= 0) return;

@@ -58,6 +58,13 @@ struct Pairs32Args {
   const int* sys_cell;       // nsys + 1
   const int* cell_sys;       // ncells_total
   int* work;                 // cell counters of the count and fill passes (zeroed per call)
+  // batches: a cell's home atoms are taken 32 at a time -- a first launch of
+  // each pass takes every cell's first 32 (the count pass lists the other
+  // rounds: cell, round), a second (round_pass) the listed rounds
+  int2* rounds;
+  int* n_rounds;
+  int* round_work;           // counters of the second launches (count, fill)
+  int round_pass;
   int nsys;
   int nat_total;
   int ncells_total;
