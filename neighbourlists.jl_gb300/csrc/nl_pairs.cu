@@ -990,7 +990,7 @@ __device__ __forceinline__ double f2d_exact(float x) {
 }
 
 // BATCH (masks only): the cells of the systems flagged in sys_sym, each warp
-// with its home cell's system geometry in shared memory, slots and original
+// reading its home cell's system geometry through L1, slots and original
 // indices offset to the launch's; a system with a crowded cell sets its
 // sys_fail, and the per-cell pass then counts all of it.  A batch keeps an
 // atom's mask words at the start of its own list region.
@@ -999,15 +999,16 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
   constexpr bool kMask = SM == kSymMasks || SM == kSymMasksFix;  // neighbour masks written
   static_assert(!BATCH || SM == kSymMasks, "batches take the mask variant only");
   __shared__ SCSmem sm[kSCWarps];
-  __shared__ Geometry geo_w[BATCH ? kSCWarps : 1];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   SCSmem& W = sm[warp];
-  const Geometry& g = BATCH ? geo_w[warp] : A.g;
+  // batches: the home cell's system geometry, read through L1 (copying it to
+  // shared memory for every cell was slower: 3.40 against 3.38 ms per batch)
+  const Geometry* gp = &A.g;
   const int nat = BATCH ? A.nat_total : A.g.nat;  // bound of sorted slots and original indices
   float lo = A.g.lo, hi = A.g.hi;
   // batches: the home cell's system, its first slot / original atom and the
   // index of its cell 0 in cell_offsets (zero for a single system)
-  int sys = 0, abase = 0, coff = 0, cur_sys = -1;
+  int sys = 0, abase = 0, coff = 0;
   const float inf = __int_as_float(0x7f800000), nan = __int_as_float(0x7fc00000);
   unsigned rechecks = 0;
   if (A.cap_rec && blockIdx.x == 0 && threadIdx.x == 0) *A.cap_rec = A.list_cap;
@@ -1029,6 +1030,7 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
     s.ox = s.oy = s.oz = 0.f;
     if (h < A.ncells_total && lane < 27) {
       const int hl = BATCH ? h - A.sys_cell[sys] : h;
+      const Geometry& g = *gp;
       const int c0 = hl % g.ns[0] + 1, c1 = (hl / g.ns[0]) % g.ns[1] + 1, c2 = hl / (g.ns[0] * g.ns[1]) + 1;
       s.lin = stencil_cell(g, nullptr, 0, 3, 3, c0, c1, c2, lane, s.slp, s.ox, s.oy, s.oz);
       if (s.lin >= 0) {
@@ -1039,7 +1041,9 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
   };
   // (batches: a grid stride as well; runs of 8 consecutive cells per warp,
   // with the next cell's ranges loaded ahead within a system, were slower:
-  // 1.20 against 0.99 ms per 4,096-system batch)
+  // 1.20 against 0.99 ms per 4,096-system batch, and so was the next cell's
+  // system and ranges loaded one grid-stride step ahead: 3.56 against 3.38 ms
+  // per batch with the default launch shapes)
   int h = blockIdx.x * kSCWarps + warp;
   St cur;
   if (!BATCH) stencil(h, cur);
@@ -1048,18 +1052,11 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
     if constexpr (BATCH) {
       sys = clampi(A.cell_sys[h], A.nsys - 1);
       if (!A.sys_sym[sys]) continue;
-      if (sys != cur_sys) {
-        __syncwarp();
-        const int* src = reinterpret_cast<const int*>(A.geo + sys);
-        int* dst = reinterpret_cast<int*>(&geo_w[warp]);
-        for (int k = lane; k < int(sizeof(Geometry) / 4); k += 32) dst[k] = src[k];
-        __syncwarp();
-        cur_sys = sys;
-      }
+      gp = A.geo + sys;
       abase = A.sys_atom[sys];
       coff = A.sys_cell[sys] + sys;
-      lo = g.lo;
-      hi = g.hi;
+      lo = gp->lo;
+      hi = gp->hi;
       stencil(h, cur);
     } else {
       stencil(h + nwarps, nxt);  // the next cell's ranges are loaded while this one is screened
@@ -1232,11 +1229,11 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
             const bool v1 = a + 1 < nb && (((vmask & ~(sb << 1)) >> lane) & 1u);
             if (u0 && v0) {
               ++rechecks;
-              l0 = exact_pair(g, A.Xs, hs + a, slot, W.hmeta[a], cw);
+              l0 = exact_pair(*gp, A.Xs, hs + a, slot, W.hmeta[a], cw);
             }
             if (u1 && v1) {
               ++rechecks;
-              l1 = exact_pair(g, A.Xs, hs + a + 1, slot, W.hmeta[a + 1], cw);
+              l1 = exact_pair(*gp, A.Xs, hs + a + 1, slot, W.hmeta[a + 1], cw);
             }
           }
           unsigned acc0 = __ballot_sync(0xffffffffu, l0), acc1 = __ballot_sync(0xffffffffu, l1);
