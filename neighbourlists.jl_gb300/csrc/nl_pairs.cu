@@ -994,10 +994,17 @@ __device__ __forceinline__ double f2d_exact(float x) {
 // indices offset to the launch's; a system with a crowded cell sets its
 // sys_fail, and the per-cell pass then counts all of it.  A batch keeps an
 // atom's mask words at the start of its own list region.
+#ifndef NL_SC_BATCH_MIN_BLOCKS
+#define NL_SC_BATCH_MIN_BLOCKS 5  // resident blocks per SM of the batch variant (no spills at 96 registers)
+#endif
 template <typename TI, int SM, bool BATCH = false>
-__global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(PairArgs<TI> A) {
+__global__ void __launch_bounds__(kSCWarps * 32, BATCH ? NL_SC_BATCH_MIN_BLOCKS : NL_SC_MIN_BLOCKS)
+    k_sym_count(PairArgs<TI> A) {
   constexpr bool kMask = SM == kSymMasks || SM == kSymMasksFix;  // neighbour masks written
   static_assert(!BATCH || SM == kSymMasks, "batches take the mask variant only");
+  // the screen's step: four home atoms (batches: 3.36 against 3.38 ms per
+  // batch) or two (single systems: 0.855 against 0.865 ms per 1M-atom step)
+  constexpr bool kQuad = BATCH && NL_SC_PACKED;
   __shared__ SCSmem sm[kSCWarps];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   SCSmem& W = sm[warp];
@@ -1196,6 +1203,74 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
         const bool fwd = qq > 13;  // a forward cell: this warp writes the candidate's column word
         const unsigned vmask = __ballot_sync(0xffffffffu, valid);  // the round's candidates
         unsigned col = 0u;
+        if constexpr (kQuad) {
+        // home atoms a .. a + 3 per step (+inf beyond the cell): two packed
+        // pairs from one 16-byte load per coordinate; one vote, one ballot
+        // per atom
+        for (int a = 0; a < nb; a += 4) {
+          const ulonglong2 hx4 = *reinterpret_cast<const ulonglong2*>(&W.hx[a]);  // a % 4 == 0: 16-byte aligned
+          const ulonglong2 hy4 = *reinterpret_cast<const ulonglong2*>(&W.hy[a]);
+          const ulonglong2 hz4 = *reinterpret_cast<const ulonglong2*>(&W.hz[a]);
+          float r2[4];
+          {
+            const unsigned long long rx = f2sub(px, hx4.x), ry = f2sub(py, hy4.x), rz = f2sub(pz, hz4.x);
+            f2unpack(f2fma(rz, rz, f2fma(ry, ry, f2mul(rx, rx))), r2[0], r2[1]);
+          }
+          {
+            const unsigned long long rx = f2sub(px, hx4.y), ry = f2sub(py, hy4.y), rz = f2sub(pz, hz4.y);
+            f2unpack(f2fma(rz, rz, f2fma(ry, ry, f2mul(rx, rx))), r2[2], r2[3]);
+          }
+          bool l[4], u[4];
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            l[k] = r2[k] < lo;
+            u[k] = !l[k] && !(r2[k] > hi);
+          }
+          if (__any_sync(0xffffffffu, u[0] || u[1] || u[2] || u[3])) {
+            const unsigned sb = rr == 0 ? 1u << a : 0u;  // the home atom itself
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              const bool v = a + k < nb && (((vmask & ~(sb << k)) >> lane) & 1u);
+              if (u[k] && v) {
+                ++rechecks;
+                l[k] = exact_pair(*gp, A.Xs, hs + a + k, slot, W.hmeta[a + k], cw);
+              }
+            }
+          }
+          unsigned row[4];
+          bool c[4];  // this lane's candidate joins the column of home atom a + k
+#pragma unroll
+          for (int k = 0; k < 4; ++k) row[k] = __ballot_sync(0xffffffffu, l[k]);
+          if constexpr (!kMask) {  // the home atom itself is no pair
+            const unsigned sb = rr == 0 ? 1u << a : 0u;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              row[k] &= ~(sb << k);
+              l[k] = l[k] && ((row[k] >> lane) & 1u);
+            }
+          }
+#pragma unroll
+          for (int k = 0; k < 4; ++k) c[k] = l[k];
+          if (A.half) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              const bool kk = l[k] && half_keep(W.horig[a + k], corig, cw, W.hmeta[a + k]);
+              row[k] = __ballot_sync(0xffffffffu, kk);
+              c[k] = l[k] && !kk;
+            }
+          }
+          if (lane == 0) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {  // a + k <= 31: nb <= 32 and a % 4 == 0
+              if constexpr (kMask)
+                W.B[a + k][rr] = row[k];
+              else
+                W.hcnt[a + k] += __popc(row[k]);
+            }
+          }
+          col |= ((c[0] ? 1u : 0u) | (c[1] ? 2u : 0u) | (c[2] ? 4u : 0u) | (c[3] ? 8u : 0u)) << a;
+        }
+        } else {
         for (int a = 0; a < nb; a += 2) {
           // home atoms a and a + 1 (+inf beyond the cell): packed (a, a + 1) pairs
           float r20, r21;
@@ -1268,6 +1343,7 @@ __global__ void __launch_bounds__(kSCWarps * 32, NL_SC_MIN_BLOCKS) k_sym_count(P
             }
           }
           col |= (c0 ? 1u << a : 0u) | (c1 ? 2u << a : 0u);
+        }
         }
         if constexpr (kMask) {
           if (valid && fwd) {  // the candidate's word for its mirrored cell
@@ -2486,7 +2562,9 @@ static void launch_modes(int mode, const PairArgs<TI>& a, int num_sms, cudaStrea
   switch (mode) {
     case kModeCount:
       if (a.sym) {  // symmetric pass; the per-cell pass below counts what it gave up (or left)
-        const int sbps = a.pair_blocks_per_sm > 0 ? a.pair_blocks_per_sm : 2 * NL_SC_MIN_BLOCKS;
+        // (default grid: twice the resident blocks; batches 14 per SM: 3.31
+        // against 3.47 ms per 4,096-system batch with 10)
+        const int sbps = a.pair_blocks_per_sm > 0 ? a.pair_blocks_per_sm : BATCH ? 14 : 2 * NL_SC_MIN_BLOCKS;
         long long sb = ((long long)a.ncells_total + kSCWarps - 1) / kSCWarps;
         if (sb > (long long)num_sms * sbps) sb = (long long)num_sms * sbps;
         k_sym_count<TI, kSymMasks, BATCH><<<int(sb), kSCWarps * 32, 0, st>>>(a);
