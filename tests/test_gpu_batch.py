@@ -176,3 +176,27 @@ def test_batch_symmetric_count_mixed(nlpkg, orc, count_kernel):
         (X6, Cc, 6.0, (True, True, False)),
     ]
     check_batch(nlpkg, orc, systems, count_kernel=count_kernel)
+
+
+@pytest.mark.parametrize("count_kernel", [0, 1])
+def test_batch_large_single_cells_in_rounds(nlpkg, orc, count_kernel):
+    """Systems whose cells the per-cell passes take in rounds of 32 home
+    atoms: one-cell periodic systems of 150 and 70 atoms (their stencils
+    images of the one cell), a symmetric-pass system with a crowded cell of
+    80 atoms (failed and handed to the per-cell passes with its cells and
+    slot chunks), and symmetric-pass systems around them."""
+    rng = np.random.default_rng(71)
+    X1 = rng.random((150, 3)) * 9.0
+    X2 = rng.random((70, 3)) * 7.0
+    Xr, Cr, Lr = cf.rand_config(2500, seed=72)
+    crowded = np.concatenate([Xr, Lr / 3 + rng.random((80, 3)) * 1.2])
+    Xa, Ca, La = cf.rand_config(1200, seed=73)
+    Xb, Cb, Lb = cf.rand_config(900, seed=74)
+    systems = [
+        (Xa, Ca, 5.0, (True, True, True)),
+        (X1, np.diag([9.0, 9.0, 9.0]), 6.0, (True, True, True)),
+        (crowded, Cr, 5.0, (True, True, True)),
+        (X2, np.diag([7.0, 7.0, 7.0]), 6.5, (True, True, False)),
+        (Xb, Cb, 5.0, (True, False, True)),
+    ]
+    check_batch(nlpkg, orc, systems, count_kernel=count_kernel)
