@@ -1817,11 +1817,13 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
             st[3 * r + dx] =
                 unsigned(clampi((rok && okx[dx] ? A.cell_offsets[rb + wx[dx]] : TI(1 - abase)) - 1 + abase, nat));
         }
-        if (mine) {
-          E.xi[lane][0] = A.Xs[3LL * slot + 0];
-          E.xi[lane][1] = A.Xs[3LL * slot + 1];
-          E.xi[lane][2] = A.Xs[3LL * slot + 2];
-          E.mi[lane] = __float_as_uint(A.rec[slot].w);
+        if (mine) {  // the atom's own gather row: its FP64 position and record meta
+          const double2 r0 = ld_keep(reinterpret_cast<const double2*>(A.xpk + slot), keep);
+          const int4 r1 = ld_keep(reinterpret_cast<const int4*>(A.xpk + slot) + 1, keep);
+          E.xi[lane][0] = r0.x;
+          E.xi[lane][1] = r0.y;
+          E.xi[lane][2] = __hiloint2double(r1.y, r1.x);
+          E.mi[lane] = unsigned(r1.w);
           if (BATCH) E.xi[lane][3] = __hiloint2double(sy, int(o0) + lane + 1 - abase);  // system, i
         }
         // ---- the lane's non-empty words, listed at the end of its stretch
