@@ -185,7 +185,7 @@ struct Layout {
   // [err 64 | stats 64] [pairs zero region: counters 64 | st_pairs | cell_flag]
   // [build zero region: counters 64 | st_cells | cell_count] [arrays...]
   size_t err, stats, pcount, st_pairs, cell_flag, pend, bcount, st_cells, cell_count, bend;
-  size_t totals, cell_start, cid, ticket, rec, tmp, rec_sorted, scell, counts, lcount, sorig, hdr, xpk, cs_table,
+  size_t totals, cell_start, cid, ticket, rec, tmp, rec_sorted, scell, counts, lcount, sorig, orow, xpk, cs_table,
       screen_cells,
       big_list, base_end, stab, lists, end;
   bool use_lists = true;  // the workspace holds the pair lists (it reaches `end`)
@@ -234,8 +234,8 @@ Layout layout(int64_t nat, int64_t ncells) {
   o += up(sizeof(int) * n);
   L.sorig = o;
   o += up(sizeof(int) * n);
-  L.hdr = o;
-  o += up(sizeof(int2) * n);
+  L.orow = o;
+  o += up(sizeof(nl::ORow) * n);
   L.xpk = o;
   o += up(sizeof(nl::XPack) * n);
   L.cs_table = o;  // C'S for |S_k| <= 2 in FP64, then (lazy sums) in the positions' fixed point
@@ -420,7 +420,7 @@ nl::PairArgs<TI> pair_args(const nl::Geometry& g, const TI* cell_offsets, const 
   a.stab = L.use_lists ? at<unsigned>(ws, L.stab) : nullptr;
   a.lcount = at<int>(ws, L.lcount);
   a.sorig = at<int>(ws, L.sorig);
-  a.hdr = at<int2>(ws, L.hdr);
+  a.orow = at<nl::ORow>(ws, L.orow);
   a.xpk = at<nl::XPack>(ws, L.xpk);
   a.cap_rec = at<int>(ws, L.pcount) + 2;  // the count pass's list_cap, checked by the write pass
   a.cs_table = at<double>(ws, L.cs_table);

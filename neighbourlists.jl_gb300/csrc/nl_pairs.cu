@@ -891,7 +891,7 @@ constexpr unsigned kPlainMeta = (128u) | (128u << 10) | (128u << 20);
 // cell_offsets (a per-cell table of them was slower there: 0.492 against
 // 0.484 ms at 1M atoms), the lazy sum's pass from a 28-word table row per
 // home cell (first sorted slot of its 27 cells, their loop shifts; 0.711
-// against 0.762 ms); each home atom's (sorted slot, home cell) goes to hdr,
+// against 0.762 ms); each home atom's (position, sorted slot, home cell) goes to orow,
 // indexed by its original index, for the original-order write pass.  Mask
 // words are kMaskStride per atom (27 used) so that they load as 16-byte
 // vectors.
@@ -1129,7 +1129,13 @@ __global__ void __launch_bounds__(kSCWarps * 32, BATCH ? NL_SC_BATCH_MIN_BLOCKS 
           const double X0 = A.Xs[3LL * (hs + lane) + 0], X1 = A.Xs[3LL * (hs + lane) + 1],
                        X2 = A.Xs[3LL * (hs + lane) + 2];
           if constexpr (SM == kSymMasks) {
-            A.hdr[o] = make_int2(hs + lane, h);  // the write pass walks atoms in original order
+            ORow orw;  // the write pass walks atoms in original order
+            orw.x = X0;
+            orw.y = X1;
+            orw.z = X2;
+            orw.slot = hs + lane;
+            orw.cell = h;
+            A.orow[o] = orw;
             XPack xp;
             xp.x = X0;
             xp.y = X1;
@@ -1749,12 +1755,17 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
       sy = lo_s;
       own = A.sys_sym[sy] && !A.sys_fail[sy];
     }
-    // ---- lane a: atom o0 + a.  Header and output range first ...
+    // ---- lane a: atom o0 + a.  Its row (position, slot, home cell) and output range first ...
     int2 hd = make_int2(0, 0);
     long long f = 0, n = 0;
     if (own) {
       const long long o = o0 + lane;
-      hd = ld_stream(A.hdr + o);
+      const double2 p01 = ld_stream(reinterpret_cast<const double2*>(A.orow + o));
+      const int4 p2 = ld_stream(reinterpret_cast<const int4*>(A.orow + o) + 1);
+      hd = make_int2(p2.z, p2.w);
+      E.xi[lane][0] = p01.x;
+      E.xi[lane][1] = p01.y;
+      E.xi[lane][2] = __hiloint2double(p2.y, p2.x);
       f = (long long)A.first[o] - 1;
       n = (long long)A.first[o + 1] - 1 - f;
     }
@@ -1817,13 +1828,8 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
             st[3 * r + dx] =
                 unsigned(clampi((rok && okx[dx] ? A.cell_offsets[rb + wx[dx]] : TI(1 - abase)) - 1 + abase, nat));
         }
-        if (mine) {  // the atom's own gather row: its FP64 position and record meta
-          const double2 r0 = ld_keep(reinterpret_cast<const double2*>(A.xpk + slot), keep);
-          const int4 r1 = ld_keep(reinterpret_cast<const int4*>(A.xpk + slot) + 1, keep);
-          E.xi[lane][0] = r0.x;
-          E.xi[lane][1] = r0.y;
-          E.xi[lane][2] = __hiloint2double(r1.y, r1.x);
-          E.mi[lane] = unsigned(r1.w);
+        if (mine) {  // record meta (windings, exact bit): only where some atom has one
+          E.mi[lane] = plain ? kPlainMeta : __float_as_uint(A.rec[slot].w);
           if (BATCH) E.xi[lane][3] = __hiloint2double(sy, int(o0) + lane + 1 - abase);  // system, i
         }
         // ---- the lane's non-empty words, listed at the end of its stretch

@@ -34,6 +34,13 @@ struct __align__(16) XPack {
   unsigned meta;
 };
 static_assert(sizeof(XPack) == 32, "one 32-byte row per slot");
+// An atom's row by its original index, for the original-order write pass
+struct __align__(16) ORow {
+  double x, y, z;
+  int slot;  // sorted slot (0-based, the launch's)
+  int cell;  // home cell (0-based, the launch's)
+};
+static_assert(sizeof(ORow) == 32, "one 32-byte row per original atom");
 
 template <typename TI>
 struct PairArgs {
@@ -62,7 +69,7 @@ struct PairArgs {
   uint2* lists;             // per sorted slot: list_cap accepted (slot_j, candidate word)
   int* lcount;              // per sorted slot: pairs of the atom (count pass)
   int* sorig;               // per sorted slot: original atom index within the launch (0-based)
-  int2* hdr;                // per original atom: (sorted slot, home cell), written by the symmetric count pass
+  ORow* orow;               // per original atom: position, sorted slot, home cell (symmetric count pass)
   XPack* xpk;               // per sorted slot: gather row of the original-order write pass (symmetric count pass)
   int list_cap;             // kListCap, or 0: no lists (every cell takes the screening write pass)
   int* cap_rec;             // list_cap of the count pass (the write pass checks it)
