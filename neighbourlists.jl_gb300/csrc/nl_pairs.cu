@@ -147,6 +147,24 @@ __device__ __forceinline__ void st_keep(XPack* dst, const XPack& v, unsigned lon
   *dst = v;
 #endif
 }
+// A whole 32-byte gather row (32-byte aligned) in one 256-bit load, with the
+// evict-last policy (NL_ROW_V4=0: two 16-byte loads)
+#ifndef NL_ROW_V4
+#define NL_ROW_V4 1
+#endif
+__device__ __forceinline__ void ld_row(const XPack* ptr, unsigned long long pol, double2& w0, int4& w1) {
+#if NL_ROW_V4 && NL_L2_HINTS
+  unsigned long long a, b, c, d;
+  asm("ld.global.nc.L2::cache_hint.v4.u64 {%0, %1, %2, %3}, [%4], %5;"
+      : "=l"(a), "=l"(b), "=l"(c), "=l"(d)
+      : "l"(ptr), "l"(pol));
+  w0 = make_double2(__longlong_as_double((long long)a), __longlong_as_double((long long)b));
+  w1 = make_int4(int(unsigned(c)), int(unsigned(c >> 32)), int(unsigned(d)), int(unsigned(d >> 32)));
+#else
+  w0 = ld_keep(reinterpret_cast<const double2*>(ptr), pol);
+  w1 = ld_keep(reinterpret_cast<const int4*>(ptr) + 1, pol);
+#endif
+}
 // read-once data: evict first from L1 and L2
 template <typename T>
 __device__ __forceinline__ T ld_stream(const T* ptr) {
@@ -1910,9 +1928,7 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
       // every lane loads (entries outside [off, hix) repeat an edge entry; their stores are off)
       auto load = [&](int k, Ld& u) {
         u.en = E.ent[min(max(k, off), hix - 1)];
-        const XPack* xp = A.xpk + min(u.en.x, unsigned(nat - 1));
-        u.w0 = ld_keep(reinterpret_cast<const double2*>(xp), keep);
-        u.w1 = ld_keep(reinterpret_cast<const int4*>(xp) + 1, keep);
+        ld_row(A.xpk + min(u.en.x, unsigned(nat - 1)), keep, u.w0, u.w1);
       };
       auto write = [&](int k, const Ld& u) {
         const bool act = k >= off && k < hix;
@@ -2271,10 +2287,10 @@ __global__ void __launch_bounds__(kLRWarps * 32, NL_LR_MIN_BLOCKS) k_lazy_rows(P
       take(on1, j1, c1);
       const XPack* p0 = A.xpk + min(unsigned(j0), unsigned(nat - 1));
       const XPack* p1 = A.xpk + min(unsigned(j1), unsigned(nat - 1));
-      const double2 a0 = ld_keep(reinterpret_cast<const double2*>(p0), keep);
-      const int4 b0 = ld_keep(reinterpret_cast<const int4*>(p0) + 1, keep);
-      const double2 a1 = ld_keep(reinterpret_cast<const double2*>(p1), keep);
-      const int4 b1 = ld_keep(reinterpret_cast<const int4*>(p1) + 1, keep);
+      double2 a0, a1;
+      int4 b0, b1;
+      ld_row(p0, keep, a0, b0);
+      ld_row(p1, keep, a1, b1);
       double r0, r1;
       const dfloat f0 = term(on0, j0, c0, a0, b0, r0), f1 = term(on1, j1, c1, a1, b1, r1);
       acc = df_add(df_add(acc, f0), f1);

@@ -28,7 +28,7 @@ constexpr int kCsTableDoubles = 3 * 125;
 // Per sorted slot, what the original-order write pass gathers for a
 // neighbour: its FP64 position, 1-based original index (perm) and record
 // meta (windings, exact bit), in one 32-byte row (two 16-byte loads).
-struct __align__(16) XPack {
+struct __align__(32) XPack {  // 32-byte aligned: read as one 256-bit load
   double x, y, z;
   int perm;
   unsigned meta;
