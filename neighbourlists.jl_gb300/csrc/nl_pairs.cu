@@ -2031,7 +2031,7 @@ __global__ void __launch_bounds__(kEOWarps * 32, NL_EO_MIN_BLOCKS) k_emit_orig(P
 constexpr int kLRWarps = 2;
 constexpr int kLRRow = 33;
 #ifndef NL_LR_MIN_BLOCKS
-#define NL_LR_MIN_BLOCKS 10  // 96 registers: 9 blocks fit the shared memory (0.659 against 0.684 ms with 8 at 128 registers)
+#define NL_LR_MIN_BLOCKS 10  // 96 registers, 10 resident blocks (0.659 against 0.684 ms with 8 at 128 registers)
 #endif
 #ifndef NL_LR_HALF
 #define NL_LR_HALF 1  // each unordered pair once (0: every atom walks all its pairs, no atomics)
