@@ -1644,7 +1644,7 @@ __global__ void __launch_bounds__(kEmitWarps * 32, BATCH ? NL_EMIT_BATCH_MIN_BLO
 
 // ------------------------------------------------------------------------
 // Write pass for the symmetric count pass's neighbour masks, in ORIGINAL atom
-// order (single systems).  Atom o's pairs occupy [first[o], first[o+1]) and
+// order (single systems; batches below).  Atom o's pairs occupy [first[o], first[o+1]) and
 // atoms follow one another in original order, so a warp that takes 32
 // consecutive original atoms writes one contiguous run of every output array:
 // its stores cover whole lines, and only the run's two ends share a sector
@@ -1652,13 +1652,16 @@ __global__ void __launch_bounds__(kEmitWarps * 32, BATCH ? NL_EMIT_BATCH_MIN_BLO
 // ~26-pair runs over the arrays; the partial sectors at both ends of every
 // run cost extra DRAM traffic.)  The neighbours' data are gathered from
 // anywhere in the sorted arrays, so they come from L2: one 32-byte row per
-// neighbour (XPack: position, perm, meta, written by the count pass).
+// neighbour (XPack: position, perm, meta, written by the count pass), read
+// as one 256-bit load.
 //
-// Per batch of 32 atoms, lane a holds atom o0 + a: its header (sorted slot,
-// home cell) and output range, then -- loads issued together -- its 27 mask
-// words (16-byte vector loads), position, record meta and the sorted start of
-// each of its 27 stencil cells (cell_offsets; the wrapped cell and loop shift
-// per axis follow from the home cell).  The masks are expanded into a
+// Per batch of 32 atoms, lane a holds atom o0 + a: its row by original index
+// (ORow: position, sorted slot, home cell, written by the count pass; read
+// coalesced) and output range, then -- loads issued together -- its 27 mask
+// words (16-byte vector loads) and the sorted start of each of its 27
+// stencil cells (cell_offsets; the wrapped cell and loop shift per axis
+// follow from the home cell); the record meta only where some atom has
+// windings or is exact.  The masks are expanded into a
 // shared-memory table of 8-byte entries (slot of j; atom and the three loop
 // shifts) at the pairs' output positions, in stencil order (dz, dy, dx) and
 // sorted order within each stencil cell -- the reference's traversal order.
