@@ -234,10 +234,6 @@ Layout layout(int64_t nat, int64_t ncells) {
   o += up(sizeof(int) * n);
   L.sorig = o;
   o += up(sizeof(int) * n);
-  L.orow = o;
-  o += up(sizeof(nl::ORow) * n);
-  L.xpk = o;
-  o += up(sizeof(nl::XPack) * n);
   L.cs_table = o;  // C'S for |S_k| <= 2 in FP64, then (lazy sums) in the positions' fixed point
   o += up(sizeof(double) * 2 * 3 * 125);
   L.screen_cells = o;
@@ -247,7 +243,14 @@ Layout layout(int64_t nat, int64_t ncells) {
   // the pair lists come last: a workspace that ends before them still runs
   // every call, with the screening write pass for every cell
   L.base_end = o;
-  L.stab = o;  // the symmetric pass's stencil table: 28 words per cell
+  // the symmetric passes' rows and tables (they run only with the lists):
+  // per original atom its row (ORow), per sorted slot its gather row
+  // (XPack), per cell the lazy sum's stencil table (28 words)
+  L.orow = o;
+  o += up(sizeof(nl::ORow) * n);
+  L.xpk = o;
+  o += up(sizeof(nl::XPack) * n);
+  L.stab = o;
   o += up(sizeof(unsigned) * 28 * size_t(ncells > 0 ? ncells : 1));
   L.lists = o;
   o += up(sizeof(uint2) * size_t(nl::kListCap) * n);
@@ -420,8 +423,8 @@ nl::PairArgs<TI> pair_args(const nl::Geometry& g, const TI* cell_offsets, const 
   a.stab = L.use_lists ? at<unsigned>(ws, L.stab) : nullptr;
   a.lcount = at<int>(ws, L.lcount);
   a.sorig = at<int>(ws, L.sorig);
-  a.orow = at<nl::ORow>(ws, L.orow);
-  a.xpk = at<nl::XPack>(ws, L.xpk);
+  a.orow = L.use_lists ? at<nl::ORow>(ws, L.orow) : nullptr;
+  a.xpk = L.use_lists ? at<nl::XPack>(ws, L.xpk) : nullptr;
   a.cap_rec = at<int>(ws, L.pcount) + 2;  // the count pass's list_cap, checked by the write pass
   a.cs_table = at<double>(ws, L.cs_table);
   a.screen_cells = at<int>(ws, L.screen_cells);
